@@ -1,0 +1,155 @@
+/* scisim_gpu.h -- C ABI of the GB300 (sm_103a) SCISim contact-path library.
+ *
+ * libscisim_gb300.so exposes SCISim's per-step contact path for Ball2D discs:
+ * unconstrained maps, spatial-grid broad phase, CCD narrow phase, contact bases
+ * and forcing terms, Delassus diagonal blocks, graph-coloured block Gauss-Seidel
+ * Coulomb solve, impulse cache, on one GPU.  All arguments are plain C types and
+ * host pointers in SCISim's own layouts (q, v interleaved [x0 y0 x1 y1 ...],
+ * FP64).  No call throws; every entry point returns an sg_status.
+ *
+ * Each entry point names the reference interface it replaces (file:line within
+ * breannansmith/scisim).  A context is single-threaded: one host thread per
+ * context, calls are stream-ordered on the context's own CUDA stream.
+ */
+#ifndef SCISIM_GPU_H
+#define SCISIM_GPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SG_API __attribute__((visibility("default")))
+#else
+#define SG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SG_OK = 0,
+  SG_NOT_CONVERGED = 1,  /* solve hit max_iters; the best iterate is returned
+                            (GeometricImpactFrictionMap.cpp:346-350 warns and goes on) */
+  SG_BAD_INPUT = 2,      /* invalid sizes, pointers or parameters */
+  SG_DEVICE_TIMEOUT = 3, /* a bounded device-side wait expired; the context stays usable */
+  SG_CUDA_ERROR = 4,     /* a CUDA runtime call failed (see sg_last_error_string) */
+  SG_CAPACITY = 5        /* a fixed internal limit was exceeded (e.g. > 64 colours) */
+} sg_status;
+
+enum { SG_SYMPLECTIC_EULER = 0, SG_VERLET = 1 };
+/* ImpulsesToCache (scisim/ConstrainedMaps/ImpulsesToCache.h) */
+enum { SG_CACHE_NONE = 0, SG_CACHE_NORMAL = 1, SG_CACHE_NORMAL_AND_FRICTION = 2 };
+/* Arithmetic of the Gauss-Seidel sweeps. */
+enum { SG_PRECISION_FP64 = 0, SG_PRECISION_FP32_REFINE = 1 };
+
+typedef struct {
+  int32_t integrator;  /* SG_SYMPLECTIC_EULER | SG_VERLET  (ball2d/SymplecticEulerMap.cpp, VerletMap.cpp) */
+  int32_t cache_mode;  /* SG_CACHE_*  (GeometricImpactFrictionMap ctor, GeometricImpactFrictionMap.cpp:20) */
+  int32_t precision;   /* SG_PRECISION_* */
+  int32_t device;      /* CUDA device ordinal */
+  double dt;
+  double gravity[2];   /* Ball2DGravityForce (ball2d/Forces/Ball2DGravityForce.cpp:36-46) */
+  double mu;           /* default friction coefficient (Ball2DSim::flow argument) */
+  double CoR;          /* default coefficient of restitution */
+  double tol;          /* absolute Coulomb residual tolerance (GeometricImpactFrictionMap m_abs_tol) */
+  uint32_t max_iters;  /* Gauss-Seidel iteration cap (m_max_iters) */
+  uint32_t eval_every; /* residual evaluation period (Sobogus m_eval_every) */
+} sg_config;
+
+typedef struct {
+  int64_t n_contacts;
+  int64_t n_ball_ball;
+  int64_t n_ball_plane;
+  uint32_t iterations; /* Gauss-Seidel sweeps executed */
+  int32_t succeeded;   /* error < tol */
+  double error;        /* best Coulomb residual (infinity norm of per-contact FB error) */
+  uint32_t n_colors;   /* colours of the contact graph */
+  uint32_t reserved;
+} sg_step_stats;
+
+typedef struct sg_ctx sg_ctx;
+
+/* Human-readable description of the last failure on this thread. */
+SG_API const char* sg_last_error_string(void);
+
+/* Creates a context on cfg->device; all device memory is owned by the context. */
+SG_API int sg_ctx_create(const sg_config* cfg, sg_ctx** out);
+SG_API void sg_ctx_destroy(sg_ctx* ctx);
+
+/* Uploads a Ball2D scene (replaces Ball2DState setup: ball2d/Ball2DState.cpp:40-77,
+ * StaticPlane ctor ball2d/StaticGeometry/StaticPlane.cpp:10-19).
+ * q, v: 2*nb interleaved; r, m: nb; plane_x, plane_n: 2*np (normals are normalised
+ * here, tangents t = (-n_y, n_x)).  Clears the impulse cache. */
+SG_API int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r,
+                     const double* m, int32_t np, const double* plane_x, const double* plane_n);
+
+/* Advances the device-resident scene by n_steps steps of
+ * GeometricImpactFrictionMap::flow (scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:267-442)
+ * as driven by Ball2DSim::flow (ball2d/Ball2DSim.cpp:305-326).  first_iteration is
+ * the step index of the first step (SCISim counts from 1).  stats (may be NULL)
+ * receives the last step's counters; total_contacts (may be NULL) the sum of
+ * active contacts over the n_steps steps.  Returns SG_NOT_CONVERGED if any step's
+ * solve hit max_iters. */
+SG_API int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_stats* stats,
+            int64_t* total_contacts);
+
+/* ImpactFrictionMap::flow with host buffers (scisim/ConstrainedMaps/ImpactFrictionMap.h:36):
+ * uploads (q0, v0), runs one step and downloads (q1, v1).  The impulse cache lives
+ * in the context, as SCISim's ConstraintCache lives in Ball2DSim. */
+SG_API int sg_flow(sg_ctx* ctx, uint32_t iteration, const double* q0, const double* v0, double* q1, double* v1,
+            sg_step_stats* stats);
+
+/* Downloads the device-resident state (Ball2DState q, v). */
+SG_API int sg_download_state(sg_ctx* ctx, double* q, double* v);
+
+/* Contacts of the last step in active-set order (Ball2DSim::computeActiveSet,
+ * ball2d/Ball2DSim.cpp:151-173): ia, ib (ib = -1 - plane for a static plane),
+ * n (2 per contact), alpha, beta (Sobogus.cpp:312-347).  Any output may be NULL.
+ * Returns the contact count, or -(count+1) if cap is too small. */
+SG_API int64_t sg_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* n, double* alpha,
+                         double* beta);
+
+/* The Gauss-Seidel processing order of the last step's solve (contacts of colour 0,
+ * then colour 1, ...) and the colour offsets (n_colors + 1 entries).  Returns the
+ * contact count, or -(count+1) if cap is too small. */
+SG_API int64_t sg_last_solve_order(sg_ctx* ctx, int64_t cap, int32_t* order, int32_t* color_offsets,
+                            int32_t* n_colors);
+
+/* FrictionSolver::solve for Ball2D (scisim/ConstrainedMaps/FrictionSolver.h:28,
+ * Sobogus::solve scisim/ConstrainedMaps/Sobogus.cpp:880-1088) on host buffers.
+ * m: nb masses; v0: 2nb; ia/ib: contact bodies (ib = -1 static); bases: 4 per contact,
+ * column-major [n t]; CoR, mu: per contact; alpha/beta: in = warm start, out = result;
+ * v2, f: 2nb outputs; error/iterations: outputs.  Returns SG_NOT_CONVERGED when the
+ * solve hit max_iters (solve_succeeded = false in SCISim). */
+SG_API int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc,
+                        const int32_t* ia, const int32_t* ib, const double* bases, const double* CoR,
+                        const double* mu, uint32_t max_iters, double tol, uint32_t eval_every,
+                        double* alpha, double* beta, double* v2, double* f, double* error,
+                        uint32_t* iterations);
+
+/* SpatialGridDetector::getPotentialOverlaps (ball2d/SpatialGridDetector.cpp:106-133):
+ * all overlapping pairs (i<j) of n AABBs [minx miny maxx maxy], in lexicographic
+ * order.  Returns SG_CAPACITY with *npairs = required count if cap is too small. */
+SG_API int sg_broadphase_2d(sg_ctx* ctx, int32_t n, const double* aabb, int64_t cap, int32_t* pairs,
+                     int64_t* npairs);
+
+/* CollisionDetectionUtilities::ballBallCCDCollisionHappens
+ * (scisim/CollisionDetection/CollisionDetectionUtilities.cpp:60-126) for n ball pairs;
+ * q0a, q1a, q0b, q1b: 2n; ra, rb: n.  Outputs coeffs (3n), hit (n), t (n). */
+SG_API int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1a, const double* ra,
+              const double* q0b, const double* q1b, const double* rb, double* coeffs, int32_t* hit,
+              double* t);
+
+/* Sets the iteration limit of every device-side wait (grid barriers); 0 restores the
+ * default (about a second).  Used to exercise the SG_DEVICE_TIMEOUT path. */
+SG_API int sg_set_spin_limit(sg_ctx* ctx, uint64_t spins);
+
+/* Runs a kernel that waits on a device flag nothing sets, with the context's spin
+ * limit; returns SG_DEVICE_TIMEOUT and leaves the context usable. */
+SG_API int sg_selftest_wait_timeout(sg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,126 @@
+// oracle.h -- CPU oracle for the SCISim per-step contact path.
+//
+// TEST INFRASTRUCTURE ONLY.  This is a plain C++ restatement of the reference
+// algorithm (breannansmith/scisim) used as the correctness checker for the GPU
+// library and as the timed CPU baseline.  Product code never links, imports or
+// executes anything under oracle/; only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / reference legs of bench.py do.
+//
+// Build: g++ -O2 -std=c++17 -ffp-contract=off -fopenmp (see oracle/Makefile).
+// FP contraction is off so every FP64 operation rounds the way the reference's
+// ISO C++ build does (CMakeLists.txt:250 disables GNU extensions).
+//
+// Parity status: the SCISim side (integrators, broad phase, CCD, constraints,
+// forcing terms, staggering, warm-start cache) follows the reference file:line
+// cited at each function and is pinned by the reference's own known-answer
+// tests (AABB fixtures, CCD cases, analytic slope scenes).  The Gauss-Seidel
+// solver, the local Coulomb solver and the residual live in the un-vendored
+// So-bogus library; they are restated from the published method (Daviet,
+// Bertails-Descoubes & Boissieux 2011) and are "parity unpinned" at the level of
+// individual iterates and residual scale.
+#ifndef SCISIM_ORACLE_H
+#define SCISIM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// ---------------------------------------------------------------- broad phase
+// aabb: n boxes as [minx, miny, maxx, maxy].  Writes pairs (i<j) in the
+// lexicographic order of std::set<std::pair<unsigned,unsigned>>.
+// Returns the number of pairs, or -1 if cap is too small (count still written to *total).
+int64_t or_grid_overlaps_2d(int n, const double* aabb, int64_t cap, int32_t* pairs, int64_t* total);
+int64_t or_allpairs_overlaps_2d(int n, const double* aabb, int64_t cap, int32_t* pairs, int64_t* total);
+// 3D boxes as [minx, miny, minz, maxx, maxy, maxz].
+int64_t or_grid_overlaps_3d(int n, const double* aabb, int64_t cap, int32_t* pairs, int64_t* total);
+int64_t or_allpairs_overlaps_3d(int n, const double* aabb, int64_t cap, int32_t* pairs, int64_t* total);
+
+// ---------------------------------------------------------------- narrow phase
+void or_ccd_coeffs_2d(const double* q0a, const double* q1a, double ra, const double* q0b,
+                      const double* q1b, double rb, double* c3);
+int or_ccd_happens(const double* c3, double* t_out);
+
+// ---------------------------------------------------------------- friction solve
+// Per-contact Fischer-Burmeister Coulomb error of (r, u) in local coordinates.
+double or_fb_error(int dim, const double* r, const double* u, double mu);
+// Local Coulomb solve: u = W r + b, W symmetric (2D: w00 w01 w11; 3D: w00 w01 w02 w11 w12 w22).
+void or_local_solve(int dim, const double* W, const double* b, double mu, double* r);
+
+typedef struct {
+  double tol;
+  uint32_t max_iters;
+  uint32_t eval_every;
+  const int32_t* order;   // optional sweep order (permutation of contacts) or NULL for 0..nc-1
+} or_gs_params;
+
+typedef struct {
+  double error;
+  uint32_t iterations;
+  int32_t succeeded;
+} or_gs_result;
+
+// Ball2D FrictionSolver::solve restatement (Sobogus::solve with Balls2D).
+// m: per-body mass; v0: 2nb; contacts: ia[nc] (>=0), ib[nc] (>=0 or -1 static);
+// bases: 4 per contact, column-major [n t]; CoR, mu per contact.
+// alpha/beta: in = warm start, out = solution.  v2, f: 2nb outputs.
+void or_sobogus_solve_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
+                         const int32_t* ib, const double* bases, const double* CoR, const double* mu,
+                         const or_gs_params* p, double* alpha, double* beta, double* v2, double* f,
+                         or_gs_result* res);
+
+// ---------------------------------------------------------------- Ball2D scene
+typedef struct or_ball2d or_ball2d;
+
+enum { OR_SYMPLECTIC_EULER = 0, OR_VERLET = 1 };
+enum { OR_CACHE_NONE = 0, OR_CACHE_NORMAL = 1, OR_CACHE_NORMAL_AND_FRICTION = 2 };
+
+typedef struct {
+  int32_t integrator;     // OR_SYMPLECTIC_EULER / OR_VERLET
+  int32_t cache_mode;     // OR_CACHE_*
+  double dt;
+  double gravity[2];
+  double mu;
+  double CoR;
+  double tol;
+  uint32_t max_iters;
+  uint32_t eval_every;
+} or_ball2d_params;
+
+typedef struct {
+  int64_t n_contacts;
+  int64_t n_ball_ball;
+  int64_t n_ball_plane;
+  uint32_t iterations;
+  int32_t succeeded;
+  double error;
+} or_step_stats;
+
+or_ball2d* or_ball2d_create(int nb, const double* q, const double* v, const double* r, const double* m,
+                            int np, const double* plane_x, const double* plane_n, const or_ball2d_params* p);
+void or_ball2d_destroy(or_ball2d* s);
+// One GeometricImpactFrictionMap::flow step.  order_cb: optional sweep order
+// supplier (NULL = sequential order, as the reference's uncoloured GS).
+int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* stats);
+// Runs n_steps steps starting at iteration first_iteration; returns the number of
+// steps whose solve did not converge.  stats (may be NULL) gets the last step's.
+int or_ball2d_run(or_ball2d* s, uint32_t first_iteration, uint32_t n_steps, or_step_stats* stats,
+                  int64_t* total_contacts);
+void or_ball2d_get_state(const or_ball2d* s, double* q, double* v);
+void or_ball2d_set_state(or_ball2d* s, const double* q, const double* v);
+// Contacts of the last step: ia, ib (ib=-1-plane_idx for planes), n (2 per contact), alpha, beta.
+int64_t or_ball2d_last_contacts(const or_ball2d* s, int64_t cap, int32_t* ia, int32_t* ib, double* n,
+                                double* alpha, double* beta);
+// Active set only (no solve) for the given (q0, q1): used for contact-set parity.
+int64_t or_ball2d_active_set(const or_ball2d* s, const double* q0, const double* q1, int64_t cap,
+                             int32_t* ia, int32_t* ib);
+// Unconstrained map only.
+void or_ball2d_umap(const or_ball2d* s, uint32_t iteration, const double* q0, const double* v0, double* q1,
+                    double* v1);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

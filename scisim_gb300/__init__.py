@@ -1,0 +1,12 @@
+"""GB300-native (sm_103a) SCISim contact path: Ball2D discs.
+
+The compute path is libscisim_gb300.so (CUDA kernels behind the C ABI in
+include/scisim_gpu.h); this package is its host-side mirror of SCISim's
+UnconstrainedMap / FrictionSolver / ImpactFrictionMap interfaces.
+"""
+from ._lib import Context, SgError  # noqa: F401
+from .ball2d import (Ball2DSim, Ball2DState, GeometricImpactFrictionMap, ImpulsesToCache, Sobogus,  # noqa: F401
+                     SobogusSolverType, StaticPlane, SymplecticEulerMap, VerletMap)
+
+__all__ = ["Context", "SgError", "Ball2DSim", "Ball2DState", "GeometricImpactFrictionMap", "ImpulsesToCache",
+           "Sobogus", "SobogusSolverType", "StaticPlane", "SymplecticEulerMap", "VerletMap"]

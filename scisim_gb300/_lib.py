@@ -1,0 +1,242 @@
+"""ctypes binding of libscisim_gb300.so (the C ABI declared in include/scisim_gpu.h).
+
+The library is the only compute path: if it is missing or cannot be loaded, every
+call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libscisim_gb300.so")
+
+SG_OK, SG_NOT_CONVERGED, SG_BAD_INPUT, SG_DEVICE_TIMEOUT, SG_CUDA_ERROR, SG_CAPACITY = range(6)
+STATUS_NAMES = {0: "SG_OK", 1: "SG_NOT_CONVERGED", 2: "SG_BAD_INPUT", 3: "SG_DEVICE_TIMEOUT",
+                4: "SG_CUDA_ERROR", 5: "SG_CAPACITY"}
+SYMPLECTIC_EULER, VERLET = 0, 1
+CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
+PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_i64 = C.c_int64
+
+
+class SgConfig(C.Structure):
+    _fields_ = [("integrator", C.c_int32), ("cache_mode", C.c_int32), ("precision", C.c_int32),
+                ("device", C.c_int32), ("dt", C.c_double), ("gravity", C.c_double * 2), ("mu", C.c_double),
+                ("CoR", C.c_double), ("tol", C.c_double), ("max_iters", C.c_uint32),
+                ("eval_every", C.c_uint32)]
+
+
+class SgStepStats(C.Structure):
+    _fields_ = [("n_contacts", C.c_int64), ("n_ball_ball", C.c_int64), ("n_ball_plane", C.c_int64),
+                ("iterations", C.c_uint32), ("succeeded", C.c_int32), ("error", C.c_double),
+                ("n_colors", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class SgError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = lib().sg_last_error_string().decode(errors="replace") if _lib is not None else ""
+        super().__init__("%s returned %s%s" % (where, STATUS_NAMES.get(status, status), (": " + msg) if msg else ""))
+
+
+# Every symbol the header declares, with its ctypes signature.
+SIGNATURES = {
+    "sg_last_error_string": (C.c_char_p, []),
+    "sg_ctx_create": (C.c_int, [C.POINTER(SgConfig), C.POINTER(C.c_void_p)]),
+    "sg_ctx_destroy": (None, [C.c_void_p]),
+    "sg_ball2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
+    "sg_step": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SgStepStats), C.POINTER(_i64)]),
+    "sg_flow": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp, C.POINTER(SgStepStats)]),
+    "sg_download_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "sg_last_contacts": (_i64, [C.c_void_p, _i64, _ip, _ip, _dp, _dp, _dp]),
+    "sg_last_solve_order": (_i64, [C.c_void_p, _i64, _ip, _ip, _ip]),
+    "sg_sobogus_solve_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, C.c_int32, _ip, _ip, _dp, _dp, _dp,
+                                      C.c_uint32, C.c_double, C.c_uint32, _dp, _dp, _dp, _dp, _dp,
+                                      C.POINTER(C.c_uint32)]),
+    "sg_broadphase_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _i64, _ip, C.POINTER(_i64)]),
+    "sg_ccd_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp]),
+    "sg_set_spin_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "sg_selftest_wait_timeout": (C.c_int, [C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib():
+    """Loads the library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libscisim_gb300.so is not built (run __graft_entry__.build()); "
+                               "there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, where):
+    if status not in (SG_OK, SG_NOT_CONVERGED):
+        raise SgError(status, where)
+    return status
+
+
+def dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """Owns one sg_ctx (device memory, stream, impulse cache)."""
+
+    def __init__(self, *, dt=0.01, gravity=(0.0, -9.81), mu=0.5, CoR=0.0, tol=1e-9, max_iters=5000,
+                 eval_every=1, integrator=SYMPLECTIC_EULER, cache_mode=CACHE_NONE,
+                 precision=PRECISION_FP64, device=0):
+        self.config = SgConfig(integrator, cache_mode, precision, device, dt, (C.c_double * 2)(*gravity), mu,
+                               CoR, tol, max_iters, eval_every)
+        h = C.c_void_p()
+        check(lib().sg_ctx_create(C.byref(self.config), C.byref(h)), "sg_ctx_create")
+        self._h = h
+        self.nb = 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sg_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- scene ---------------------------------------------------------------
+    def upload_ball2d(self, q, v, r, m, plane_x, plane_n):
+        q, v, r, m = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1)
+        px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        self.nb = r.shape[0]
+        self._keep = (q, v, r, m, px, pn)
+        check(lib().sg_ball2d_upload(self._h, self.nb, dptr(q), dptr(v), dptr(r), dptr(m), px.shape[0] // 2,
+                                     dptr(px), dptr(pn)), "sg_ball2d_upload")
+
+    def step(self, n_steps=1, first_iteration=1):
+        st = SgStepStats()
+        tot = _i64(0)
+        s = check(lib().sg_step(self._h, first_iteration, n_steps, C.byref(st), C.byref(tot)), "sg_step")
+        d = st.as_dict()
+        d["total_contacts"] = tot.value
+        d["status"] = s
+        return d
+
+    def flow(self, iteration, q0, v0, q1=None, v1=None):
+        q0, v0 = f64(q0), f64(v0)
+        q1 = np.empty_like(q0) if q1 is None else q1
+        v1 = np.empty_like(v0) if v1 is None else v1
+        st = SgStepStats()
+        s = check(lib().sg_flow(self._h, iteration, dptr(q0), dptr(v0), dptr(q1), dptr(v1), C.byref(st)),
+                  "sg_flow")
+        d = st.as_dict()
+        d["status"] = s
+        return q1, v1, d
+
+    def state(self):
+        q = np.empty(2 * self.nb)
+        v = np.empty(2 * self.nb)
+        check(lib().sg_download_state(self._h, dptr(q), dptr(v)), "sg_download_state")
+        return q, v
+
+    def last_contacts(self):
+        L = lib()
+        nc = L.sg_last_contacts(self._h, 0, None, None, None, None, None)
+        nc = -nc - 1 if nc < 0 else nc
+        ia, ib = np.empty(nc, np.int32), np.empty(nc, np.int32)
+        n, a, b = np.empty(2 * nc), np.empty(nc), np.empty(nc)
+        got = L.sg_last_contacts(self._h, nc, iptr(ia), iptr(ib), dptr(n), dptr(a), dptr(b))
+        if got != nc:
+            raise SgError(SG_CUDA_ERROR, "sg_last_contacts")
+        return dict(ia=ia, ib=ib, n=n.reshape(-1, 2), alpha=a, beta=b)
+
+    def last_solve_order(self):
+        L = lib()
+        nc = L.sg_last_solve_order(self._h, 0, None, None, None)
+        nc = -nc - 1 if nc < 0 else nc
+        order = np.empty(nc, np.int32)
+        offs = np.empty(65, np.int32)
+        ncol = C.c_int32(0)
+        L.sg_last_solve_order(self._h, nc, iptr(order), iptr(offs), C.byref(ncol))
+        return order, offs[: ncol.value + 1].copy()
+
+    def set_spin_limit(self, spins):
+        check(lib().sg_set_spin_limit(self._h, spins), "sg_set_spin_limit")
+
+    def selftest_wait_timeout(self):
+        return lib().sg_selftest_wait_timeout(self._h)
+
+    # -- standalone entry points ----------------------------------------------
+    def sobogus_solve_2d(self, m, v0, ia, ib, bases, CoR, mu, tol, max_iters, eval_every=1, alpha=None,
+                         beta=None):
+        m, v0, bases = f64(m), f64(v0), f64(bases)
+        ia, ib = i32(ia), i32(ib)
+        nc, nb = ia.shape[0], m.shape[0]
+        CoR = f64(np.broadcast_to(CoR, (nc,)))
+        mu = f64(np.broadcast_to(mu, (nc,)))
+        alpha = np.zeros(nc) if alpha is None else f64(alpha).copy()
+        beta = np.zeros(nc) if beta is None else f64(beta).copy()
+        v2, f = np.zeros(2 * nb), np.zeros(2 * nb)
+        err = C.c_double(0.0)
+        its = C.c_uint32(0)
+        s = check(lib().sg_sobogus_solve_2d(self._h, nb, dptr(m), dptr(v0), nc, iptr(ia), iptr(ib), dptr(bases),
+                                            dptr(CoR), dptr(mu), max_iters, tol, eval_every, dptr(alpha),
+                                            dptr(beta), dptr(v2), dptr(f), C.byref(err), C.byref(its)),
+                  "sg_sobogus_solve_2d")
+        return dict(alpha=alpha, beta=beta, v2=v2, f=f, error=err.value, iterations=its.value,
+                    succeeded=(s == SG_OK))
+
+    def broadphase_2d(self, aabb):
+        aabb = f64(aabb).reshape(-1, 4)
+        n = aabb.shape[0]
+        tot = _i64(0)
+        cap = 8 * n + 16
+        while True:
+            out = np.empty((cap, 2), np.int32)
+            s = lib().sg_broadphase_2d(self._h, n, dptr(aabb), cap, iptr(out), C.byref(tot))
+            if s == SG_CAPACITY and tot.value > cap:
+                cap = tot.value
+                continue
+            check(s, "sg_broadphase_2d")
+            return out[: tot.value].copy()
+
+    def ccd_2d(self, q0a, q1a, ra, q0b, q1b, rb):
+        arrs = [f64(x).reshape(-1) for x in (q0a, q1a, ra, q0b, q1b, rb)]
+        n = arrs[2].shape[0]
+        coeffs, hit, t = np.empty(3 * n), np.empty(n, np.int32), np.empty(n)
+        check(lib().sg_ccd_2d(self._h, n, *[dptr(a) for a in arrs], dptr(coeffs), iptr(hit), dptr(t)),
+              "sg_ccd_2d")
+        return coeffs.reshape(-1, 3), hit.astype(bool), t

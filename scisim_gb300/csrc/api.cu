@@ -1,0 +1,543 @@
+// api.cu -- the C ABI (include/scisim_gpu.h): contexts, scene upload, the
+// per-step pipeline of GeometricImpactFrictionMap::flow, and standalone entry
+// points for the FrictionSolver, the broad phase and the CCD narrow phase.
+#include "ctx.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <utility>
+
+namespace sg {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int grow(Buf& b, size_t bytes) {
+  if (bytes <= b.bytes && b.p) return SG_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  const size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+  SG_CUDA_TRY(cudaMalloc(&b.p, want));
+  b.bytes = want;
+  return SG_OK;
+}
+
+void release(Buf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+static constexpr unsigned long long kDefaultSpin = 1ull << 25;  // ~1-2 s of 32 ns sleeps
+
+static int ensure_contact_capacity(sg_ctx* ctx, int64_t nc) {
+  if (nc <= ctx->ccap && ctx->ia.p) return SG_OK;
+  const int64_t cap = std::max<int64_t>(nc + nc / 4 + 64, 1024);
+  const size_t c = (size_t)cap;
+  if (int r = grow(ctx->ia, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->ib, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->n, sizeof(double) * 2 * c)) return r;
+  if (int r = grow(ctx->c, sizeof(double) * 2 * c)) return r;
+  if (int r = grow(ctx->W, sizeof(double) * 3 * c)) return r;
+  if (int r = grow(ctx->mu, sizeof(double) * c)) return r;
+  if (int r = grow(ctx->r_loc, sizeof(double) * 2 * c)) return r;
+  if (int r = grow(ctx->key, sizeof(unsigned long long) * c)) return r;
+  if (int r = grow(ctx->ab, sizeof(double) * 2 * c)) return r;
+  ctx->ccap = cap;
+  return SG_OK;
+}
+
+static int upload(sg_ctx* ctx, Buf& b, const void* host, size_t bytes) {
+  if (int r = grow(b, bytes)) return r;
+  if (bytes) SG_CUDA_TRY(cudaMemcpyAsync(b.p, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return SG_OK;
+}
+
+static int validate_config(const sg_config* c) {
+  if (!c) return SG_BAD_INPUT;
+  if (c->integrator != SG_SYMPLECTIC_EULER && c->integrator != SG_VERLET) return SG_BAD_INPUT;
+  if (c->cache_mode < SG_CACHE_NONE || c->cache_mode > SG_CACHE_NORMAL_AND_FRICTION) return SG_BAD_INPUT;
+  if (c->precision != SG_PRECISION_FP64 && c->precision != SG_PRECISION_FP32_REFINE) return SG_BAD_INPUT;
+  if (!(c->dt > 0.0) || !(c->tol >= 0.0) || !(c->mu >= 0.0) || !(c->CoR >= 0.0 && c->CoR <= 1.0)) return SG_BAD_INPUT;
+  return SG_OK;
+}
+
+// One geometric impact-friction step on the device-resident scene.
+static int step_once(sg_ctx* ctx, sg_step_stats* out) {
+  const int nb = ctx->nb;
+  cudaStream_t s = ctx->stream;
+  sg_step_stats st{};
+  if (nb == 0) {
+    if (out) *out = st;
+    return SG_OK;
+  }
+  // Predictor + swept AABBs (GeometricImpactFrictionMap.cpp:279, Ball2DSim.cpp:566-572).
+  if (int r = ball2d_predict_and_bounds(ctx)) return r;
+  const double* aabb = ctx->aabb.as<double>();
+  if (int r = broadphase_build_grid(ctx, aabb, nb)) return r;
+  if (int r = broadphase_count_pairs(ctx, aabb, nb, true)) return r;
+  if (int r = plane_flags(ctx)) return r;
+  int totals[2] = {0, 0};
+  SG_CUDA_TRY(cudaMemcpyAsync(&totals[0], ctx->pair_off.as<int>() + nb, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(&totals[1], ctx->plane_off.as<int>() + (long)nb * ctx->np, sizeof(int),
+                              cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  const int npairs = totals[0], nplanes = totals[1];
+  const int nc = npairs + nplanes;
+  st.n_contacts = nc;
+  st.n_ball_ball = npairs;
+  st.n_ball_plane = nplanes;
+  ctx->last_nc = nc;
+  ctx->last_nbb = npairs;
+  if (nc == 0) {
+    // No active constraints: keep the predictor and clear the cache (:286-298).
+    std::swap(ctx->q, ctx->q1);
+    std::swap(ctx->v, ctx->v1);
+    ctx->prev_n = 0;
+    st.succeeded = 1;
+    if (out) *out = st;
+    return SG_OK;
+  }
+  if (int r = ensure_contact_capacity(ctx, nc)) return r;
+  if (int r = broadphase_write_pairs(ctx, aabb, nb, true, ctx->ia.as<int>(), ctx->ib.as<int>())) return r;
+  if (int r = plane_write(ctx, npairs)) return r;
+  if (int r = assemble_contacts(ctx, nc)) return r;
+  if (int r = grow(ctx->v2, sizeof(double) * 2 * (size_t)nb)) return r;
+  ContactProblem P;
+  P.nb = nb;
+  P.nc = nc;
+  P.minv = ctx->minv.as<double>();
+  P.m = ctx->m.as<double>();
+  P.v0 = ctx->v.as<double>();
+  P.ia = ctx->ia.as<int>();
+  P.ib = ctx->ib.as<int>();
+  P.n = ctx->n.as<double>();
+  P.c = ctx->c.as<double>();
+  P.W = ctx->W.as<double>();
+  P.mu = ctx->mu.as<double>();
+  P.r = ctx->r_loc.as<double>();
+  P.v2 = ctx->v2.as<double>();
+  SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, ctx->cfg.precision};
+  const int sr = solve_contacts(ctx, P, sp);
+  if (sr != SG_OK && sr != SG_NOT_CONVERGED) return sr;
+  st.iterations = ctx->h_stats.iterations;
+  st.succeeded = ctx->h_stats.converged;
+  st.error = ctx->h_stats.error;
+  st.n_colors = (uint32_t)ctx->h_stats.n_colors;
+  // Impulses and cache (Sobogus.cpp:312-347, GeometricImpactFrictionMap.cpp:428).
+  if (int r = extract_and_cache(ctx, nc)) return r;
+  if (ctx->cfg.cache_mode != SG_CACHE_NONE) {
+    std::swap(ctx->key, ctx->prev_key);
+    std::swap(ctx->ab, ctx->prev_ab);
+    ctx->prev_n = nc;
+    // keep ccap consistent with the smaller of the swapped buffers
+    const int64_t kcap = (int64_t)std::min(ctx->key.bytes / sizeof(unsigned long long), ctx->ab.bytes / (2 * sizeof(double)));
+    ctx->ccap = std::min<int64_t>(ctx->ccap, kcap);
+  } else {
+    ctx->prev_n = 0;
+  }
+  // Final map with the post-impact velocity (:441).
+  if (int r = ball2d_final_map(ctx, ctx->v2.as<double>())) return r;
+  std::swap(ctx->q, ctx->q1);
+  std::swap(ctx->v, ctx->v1);
+  if (out) *out = st;
+  return sr;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" {
+
+const char* sg_last_error_string(void) { return g_last_error.c_str(); }
+
+int sg_ctx_create(const sg_config* cfg, sg_ctx** out) {
+  if (!out) return SG_BAD_INPUT;
+  *out = nullptr;
+  if (validate_config(cfg) != SG_OK) {
+    set_error("invalid sg_config");
+    return SG_BAD_INPUT;
+  }
+  int ndev = 0;
+  SG_CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (cfg->device < 0 || cfg->device >= ndev) {
+    set_error("invalid CUDA device ordinal");
+    return SG_BAD_INPUT;
+  }
+  SG_CUDA_TRY(cudaSetDevice(cfg->device));
+  auto* ctx = new sg_ctx;
+  ctx->cfg = *cfg;
+  ctx->device = cfg->device;
+  ctx->spin_limit = kDefaultSpin;
+  cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    set_error(std::string("context setup failed: ") + cudaGetErrorString(e));
+    delete ctx;
+    return SG_CUDA_ERROR;
+  }
+  *out = ctx;
+  return SG_OK;
+}
+
+void sg_ctx_destroy(sg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  Buf* bufs[] = {&ctx->q, &ctx->v, &ctx->r, &ctx->m, &ctx->minv, &ctx->q1, &ctx->v1, &ctx->v2, &ctx->plane_x,
+                 &ctx->plane_n, &ctx->plane_t, &ctx->aabb, &ctx->cell_of, &ctx->cell_count, &ctx->cell_start,
+                 &ctx->cell_fill, &ctx->sorted, &ctx->pair_cnt, &ctx->pair_off, &ctx->grid, &ctx->plane_flag,
+                 &ctx->plane_off, &ctx->scan_tmp, &ctx->ia, &ctx->ib, &ctx->n, &ctx->c, &ctx->W, &ctx->mu,
+                 &ctx->r_loc, &ctx->r_cand, &ctx->r_best, &ctx->key, &ctx->ab, &ctx->prev_key, &ctx->prev_ab,
+                 &ctx->color, &ctx->perm, &ctx->body_cnt, &ctx->body_off, &ctx->body_fill, &ctx->body_adj,
+                 &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2};
+  for (Buf* b : bufs) release(*b);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
+                     int32_t np, const double* plane_x, const double* plane_n) {
+  if (!ctx || nb < 0 || np < 0 || (nb > 0 && (!q || !v || !r || !m)) || (np > 0 && (!plane_x || !plane_n))) {
+    set_error("sg_ball2d_upload: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  for (int i = 0; i < nb; ++i)
+    if (!(r[i] > 0.0) || !(m[i] > 0.0)) {
+      set_error("sg_ball2d_upload: radii and masses must be positive");
+      return SG_BAD_INPUT;
+    }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  ctx->nb = nb;
+  ctx->np = np;
+  const size_t b2 = sizeof(double) * 2 * (size_t)std::max(nb, 1), b1 = sizeof(double) * (size_t)std::max(nb, 1);
+  std::vector<double> minv(nb);
+  for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];  // Ball2DState createMinv (Ball2DState.cpp:55-67)
+  std::vector<double> pn(2 * (size_t)np), pt(2 * (size_t)np);
+  for (int p = 0; p < np; ++p) {
+    // StaticPlane: n = normalized(n), t = (-n_y, n_x) (StaticPlane.cpp:10-19)
+    double nx = plane_n[2 * p], ny = plane_n[2 * p + 1];
+    const double z = nx * nx + ny * ny;
+    if (!(z > 0.0)) {
+      set_error("sg_ball2d_upload: zero plane normal");
+      return SG_BAD_INPUT;
+    }
+    const double sq = std::sqrt(z);
+    nx = nx / sq;
+    ny = ny / sq;
+    pn[2 * p] = nx;
+    pn[2 * p + 1] = ny;
+    pt[2 * p] = -ny;
+    pt[2 * p + 1] = nx;
+  }
+  if (int e = upload(ctx, ctx->q, q, sizeof(double) * 2 * nb)) return e;
+  if (int e = upload(ctx, ctx->v, v, sizeof(double) * 2 * nb)) return e;
+  if (int e = upload(ctx, ctx->r, r, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->m, m, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->minv, minv.data(), sizeof(double) * nb)) return e;
+  if (int e = grow(ctx->q1, b2)) return e;
+  if (int e = grow(ctx->v1, b2)) return e;
+  if (int e = grow(ctx->v2, b2)) return e;
+  if (int e = grow(ctx->aabb, 2 * b2)) return e;
+  (void)b1;
+  if (int e = upload(ctx, ctx->plane_x, plane_x, sizeof(double) * 2 * np)) return e;
+  if (int e = upload(ctx, ctx->plane_n, pn.data(), sizeof(double) * 2 * np)) return e;
+  if (int e = upload(ctx, ctx->plane_t, pt.data(), sizeof(double) * 2 * np)) return e;
+  if (int e = grow(ctx->plane_x, 16)) return e;
+  if (int e = grow(ctx->plane_n, 16)) return e;
+  if (int e = grow(ctx->plane_t, 16)) return e;
+  ctx->prev_n = 0;
+  ctx->last_nc = 0;
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_stats* stats, int64_t* total_contacts) {
+  if (!ctx) return SG_BAD_INPUT;
+  (void)first_iteration;  // gravity is time independent
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  int64_t tot = 0;
+  int worst = SG_OK;
+  sg_step_stats st{};
+  for (uint32_t k = 0; k < n_steps; ++k) {
+    const int r = step_once(ctx, &st);
+    if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
+    if (r == SG_NOT_CONVERGED) worst = r;
+    tot += st.n_contacts;
+  }
+  if (stats) *stats = st;
+  if (total_contacts) *total_contacts = tot;
+  return worst;
+}
+
+int sg_flow(sg_ctx* ctx, uint32_t iteration, const double* q0, const double* v0, double* q1, double* v1,
+            sg_step_stats* stats) {
+  if (!ctx || (ctx->nb > 0 && (!q0 || !v0 || !q1 || !v1))) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  const size_t bytes = sizeof(double) * 2 * (size_t)ctx->nb;
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->q.p, q0, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->v.p, v0, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  const int r = sg_step(ctx, iteration, 1, stats, nullptr);
+  if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
+  SG_CUDA_TRY(cudaMemcpyAsync(q1, ctx->q.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaMemcpyAsync(v1, ctx->v.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+
+int sg_download_state(sg_ctx* ctx, double* q, double* v) {
+  if (!ctx) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  const size_t bytes = sizeof(double) * 2 * (size_t)ctx->nb;
+  if (q) SG_CUDA_TRY(cudaMemcpyAsync(q, ctx->q.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (v) SG_CUDA_TRY(cudaMemcpyAsync(v, ctx->v.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int64_t sg_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* n, double* alpha, double* beta) {
+  if (!ctx) return SG_BAD_INPUT;
+  const int64_t nc = ctx->last_nc;
+  if (nc > cap) return -(nc + 1);
+  if (nc == 0) return 0;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return -1;
+  cudaStream_t s = ctx->stream;
+  const size_t c = (size_t)nc;
+  if (ia) cudaMemcpyAsync(ia, ctx->ia.p, sizeof(int) * c, cudaMemcpyDeviceToHost, s);
+  if (ib) cudaMemcpyAsync(ib, ctx->ib.p, sizeof(int) * c, cudaMemcpyDeviceToHost, s);
+  if (n) cudaMemcpyAsync(n, ctx->n.p, sizeof(double) * 2 * c, cudaMemcpyDeviceToHost, s);
+  // (alpha, beta) were cached into prev_ab when caching is on, else into ab.
+  const double* abp = (ctx->cfg.cache_mode != SG_CACHE_NONE) ? ctx->prev_ab.as<double>() : ctx->ab.as<double>();
+  if (alpha || beta) {
+    std::vector<double> ab(2 * c);
+    cudaMemcpyAsync(ab.data(), abp, sizeof(double) * 2 * c, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (size_t k = 0; k < c; ++k) {
+      if (alpha) alpha[k] = ab[2 * k];
+      if (beta) beta[k] = ab[2 * k + 1];
+    }
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  return nc;
+}
+
+int64_t sg_last_solve_order(sg_ctx* ctx, int64_t cap, int32_t* order, int32_t* color_offsets, int32_t* n_colors) {
+  if (!ctx) return SG_BAD_INPUT;
+  const int64_t nc = ctx->last_nc;
+  if (nc > cap) return -(nc + 1);
+  if (n_colors) *n_colors = ctx->h_stats.n_colors;
+  if (color_offsets)
+    for (int c = 0; c <= ctx->h_stats.n_colors; ++c) color_offsets[c] = ctx->h_stats.color_off[c];
+  if (order && nc > 0) {
+    if (cudaMemcpy(order, ctx->perm.p, sizeof(int) * (size_t)nc, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  }
+  return nc;
+}
+
+int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc, const int32_t* ia,
+                        const int32_t* ib, const double* bases, const double* CoR, const double* mu, uint32_t max_iters,
+                        double tol, uint32_t eval_every, double* alpha, double* beta, double* v2, double* f,
+                        double* error, uint32_t* iterations) {
+  if (!ctx || nb < 0 || nc < 0 || (nb > 0 && (!m || !v0 || !v2 || !f)) ||
+      (nc > 0 && (!ia || !ib || !bases || !CoR || !mu || !alpha || !beta))) {
+    set_error("sg_sobogus_solve_2d: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  for (int k = 0; k < nc; ++k) {
+    if (ia[k] < 0 || ia[k] >= nb || ib[k] >= nb || ib[k] == ia[k] || ib[k] < -1) {
+      set_error("sg_sobogus_solve_2d: contact body index out of range");
+      return SG_BAD_INPUT;
+    }
+  }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  // Host-side assembly of the per-contact data (what the step pipeline does on the device).
+  std::vector<double> minv(nb), n(2 * (size_t)nc), c(2 * (size_t)nc), W(3 * (size_t)nc), rl(2 * (size_t)nc);
+  for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];
+  for (int k = 0; k < nc; ++k) {
+    const double* B = bases + 4 * k;
+    const double nx = B[0], ny = B[1], tx = B[2], ty = B[3];
+    n[2 * k] = nx;
+    n[2 * k + 1] = ny;
+    const int a = ia[k], b = ib[k];
+    double vrx = v0[2 * a], vry = v0[2 * a + 1];
+    if (b >= 0) {
+      vrx = vrx - v0[2 * b];
+      vry = vry - v0[2 * b + 1];
+    } else {
+      vrx = vrx - 0.0;
+      vry = vry - 0.0;
+    }
+    const double ndotv = nx * vrx + ny * vry;
+    const double nrel = -(0.0 * nx + 0.0 * ny);
+    const double drel = -(0.0 * tx + 0.0 * ty);
+    const double sc = CoR[k] * ndotv + nrel;
+    const double wx = (0.0 + nx * sc) + tx * drel;
+    const double wy = (0.0 + ny * sc) + ty * drel;
+    c[2 * k] = nx * wx + ny * wy;
+    c[2 * k + 1] = tx * wx + ty * wy;
+    const double nn = nx * nx + ny * ny, nt = nx * tx + ny * ty, tt = tx * tx + ty * ty;
+    double w00 = minv[a] * nn, w01 = minv[a] * nt, w11 = minv[a] * tt;
+    if (b >= 0) {
+      w00 = w00 + minv[b] * nn;
+      w01 = w01 + minv[b] * nt;
+      w11 = w11 + minv[b] * tt;
+    }
+    W[3 * k] = w00;
+    W[3 * k + 1] = w01;
+    W[3 * k + 2] = w11;
+    const double rwx = alpha[k] * nx + beta[k] * tx;
+    const double rwy = alpha[k] * ny + beta[k] * ty;
+    rl[2 * k] = nx * rwx + ny * rwy;
+    rl[2 * k + 1] = tx * rwx + ty * rwy;
+    if (std::fabs(tx + ny) > 0.0 || std::fabs(ty - nx) > 0.0) {
+      set_error("sg_sobogus_solve_2d: tangent must be (-n_y, n_x)");
+      return SG_BAD_INPUT;
+    }
+  }
+  // Device buffers: reuse the context's scene and contact buffers.
+  if (int e = upload(ctx, ctx->fs_m, m, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->fs_minv, minv.data(), sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->fs_v0, v0, sizeof(double) * 2 * nb)) return e;
+  if (int e = grow(ctx->fs_v2, sizeof(double) * 2 * (size_t)std::max(nb, 1))) return e;
+  if (int e = ensure_contact_capacity(ctx, nc)) return e;
+  std::vector<double> mus(mu, mu + nc);
+  if (nc > 0) {
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->ia.p, ia, sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->ib.p, ib, sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->n.p, n.data(), sizeof(double) * 2 * nc, cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->c.p, c.data(), sizeof(double) * 2 * nc, cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->W.p, W.data(), sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->mu.p, mus.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->r_loc.p, rl.data(), sizeof(double) * 2 * nc, cudaMemcpyHostToDevice, s));
+  }
+  ContactProblem P;
+  P.nb = nb;
+  P.nc = nc;
+  P.minv = ctx->fs_minv.as<double>();
+  P.m = ctx->fs_m.as<double>();
+  P.v0 = ctx->fs_v0.as<double>();
+  P.ia = ctx->ia.as<int>();
+  P.ib = ctx->ib.as<int>();
+  P.n = ctx->n.as<double>();
+  P.c = ctx->c.as<double>();
+  P.W = ctx->W.as<double>();
+  P.mu = ctx->mu.as<double>();
+  P.r = ctx->r_loc.as<double>();
+  P.v2 = ctx->fs_v2.as<double>();
+  SolveParams sp{tol, max_iters, eval_every, ctx->cfg.precision};
+  const int sr = solve_contacts(ctx, P, sp);
+  if (sr != SG_OK && sr != SG_NOT_CONVERGED) return sr;
+  ctx->last_nc = nc;
+  if (nb > 0) SG_CUDA_TRY(cudaMemcpyAsync(v2, ctx->fs_v2.p, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, s));
+  if (nc > 0) SG_CUDA_TRY(cudaMemcpyAsync(rl.data(), ctx->r_loc.p, sizeof(double) * 2 * nc, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  // r to world, alpha/beta and the friction force f (Sobogus.cpp:309-347).
+  for (int i = 0; i < 2 * nb; ++i) f[i] = 0.0;
+  for (int k = 0; k < nc; ++k) {
+    const double nx = n[2 * k], ny = n[2 * k + 1], tx = -ny, ty = nx;
+    const double rwx = nx * rl[2 * k] + tx * rl[2 * k + 1];
+    const double rwy = ny * rl[2 * k] + ty * rl[2 * k + 1];
+    alpha[k] = rwx * nx + rwy * ny;
+    beta[k] = (mu[k] == 0.0) ? 0.0 : (rwx * tx + rwy * ty);
+    const double f0x = beta[k] * tx, f0y = beta[k] * ty;
+    f[2 * ia[k]] += f0x;
+    f[2 * ia[k] + 1] += f0y;
+    if (ib[k] >= 0) {
+      f[2 * ib[k]] -= f0x;
+      f[2 * ib[k] + 1] -= f0y;
+    }
+  }
+  if (error) *error = (nc == 0) ? 0.0 : ctx->h_stats.error;
+  if (iterations) *iterations = ctx->h_stats.iterations;
+  return sr;
+}
+
+int sg_broadphase_2d(sg_ctx* ctx, int32_t n, const double* aabb, int64_t cap, int32_t* pairs, int64_t* npairs) {
+  if (!ctx || n < 0 || (n > 0 && !aabb) || !npairs || cap < 0 || (cap > 0 && !pairs)) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  *npairs = 0;
+  if (n == 0) return SG_OK;
+  cudaStream_t s = ctx->stream;
+  Buf d_aabb;
+  if (int e = upload(ctx, d_aabb, aabb, sizeof(double) * 4 * (size_t)n)) return e;
+  int rc = broadphase_build_grid(ctx, d_aabb.as<double>(), n);
+  if (!rc) rc = broadphase_count_pairs(ctx, d_aabb.as<double>(), n, false);
+  int total = 0;
+  if (!rc) {
+    if (cudaMemcpyAsync(&total, ctx->pair_off.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = SG_CUDA_ERROR;
+  }
+  *npairs = total;
+  if (!rc && total > cap) rc = SG_CAPACITY;
+  if (!rc && total > 0) {
+    Buf da, db;
+    rc = grow(da, sizeof(int) * (size_t)total);
+    if (!rc) rc = grow(db, sizeof(int) * (size_t)total);
+    if (!rc) rc = broadphase_write_pairs(ctx, d_aabb.as<double>(), n, false, da.as<int>(), db.as<int>());
+    if (!rc) {
+      std::vector<int> ha(total), hb(total);
+      cudaMemcpyAsync(ha.data(), da.p, sizeof(int) * total, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(hb.data(), db.p, sizeof(int) * total, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) rc = SG_CUDA_ERROR;
+      for (int k = 0; k < total && !rc; ++k) {
+        pairs[2 * k] = ha[k];
+        pairs[2 * k + 1] = hb[k];
+      }
+    }
+    release(da);
+    release(db);
+  }
+  release(d_aabb);
+  return rc;
+}
+
+int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1a, const double* ra, const double* q0b,
+              const double* q1b, const double* rb, double* coeffs, int32_t* hit, double* t) {
+  if (!ctx || n < 0) return SG_BAD_INPUT;
+  if (n == 0) return SG_OK;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  Buf b[9];
+  const size_t d2 = sizeof(double) * 2 * (size_t)n, d1 = sizeof(double) * (size_t)n;
+  int rc = upload(ctx, b[0], q0a, d2);
+  if (!rc) rc = upload(ctx, b[1], q1a, d2);
+  if (!rc) rc = upload(ctx, b[2], ra, d1);
+  if (!rc) rc = upload(ctx, b[3], q0b, d2);
+  if (!rc) rc = upload(ctx, b[4], q1b, d2);
+  if (!rc) rc = upload(ctx, b[5], rb, d1);
+  if (!rc) rc = grow(b[6], 3 * d1);
+  if (!rc) rc = grow(b[7], sizeof(int) * (size_t)n);
+  if (!rc) rc = grow(b[8], d1);
+  if (!rc)
+    rc = ccd_batch(ctx, n, b[0].as<double>(), b[1].as<double>(), b[2].as<double>(), b[3].as<double>(),
+                   b[4].as<double>(), b[5].as<double>(), b[6].as<double>(), b[7].as<int>(), b[8].as<double>());
+  if (!rc) {
+    cudaMemcpyAsync(coeffs, b[6].p, 3 * d1, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hit, b[7].p, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(t, b[8].p, d1, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) rc = SG_CUDA_ERROR;
+  }
+  for (auto& x : b) release(x);
+  return rc;
+}
+
+int sg_set_spin_limit(sg_ctx* ctx, uint64_t spins) {
+  if (!ctx) return SG_BAD_INPUT;
+  ctx->spin_limit = spins ? (unsigned long long)spins : kDefaultSpin;
+  return SG_OK;
+}
+
+int sg_selftest_wait_timeout(sg_ctx* ctx) {
+  if (!ctx) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  return wait_timeout_selftest(ctx);
+}
+
+}  // extern "C"

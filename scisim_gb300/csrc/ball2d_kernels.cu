@@ -1,0 +1,617 @@
+// ball2d_kernels.cu -- Ball2D unconstrained maps, broad phase, narrow phase and
+// contact assembly for sm_103a.
+//
+// Every kernel here computes in FP64 with the operation order of the SCISim
+// reference (the library is built with -fmad=false, so no multiply-add is
+// contracted); contact sets and forcing terms are therefore bit-identical to the
+// reference arithmetic.
+//
+// Layout in HBM: q, v interleaved [x0 y0 x1 y1 ...] (double2 per body, as SCISim's
+// VectorXs), r, m, minv one double per body; contacts as SoA arrays (ia, ib int32,
+// n double2, forcing c double2, W 3 doubles, mu, local impulse r double2, key u64).
+#include "ctx.hpp"
+
+#include <cmath>
+
+namespace sg {
+namespace {
+
+constexpr int kBlock = 256;
+
+inline int blocks_for(long n, int per = kBlock) { return (int)((n + per - 1) / per); }
+
+// std::min(a, b) / std::max(a, b) semantics (Eigen cwise min/max on arrays).
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+
+// ---------------------------------------------------------------------------
+// Unconstrained map with gravity F = m g (SymplecticEulerMap.cpp:21-32,
+// VerletMap.cpp:15-41, Ball2DGravityForce.cpp:36-46).
+__device__ __forceinline__ void umap_body(int integrator, double dt, double gx, double gy, double m, double minv,
+                                          double q0x, double q0y, double v0x, double v0y, double& q1x,
+                                          double& q1y, double& v1x, double& v1y) {
+  const double fx = m * gx;
+  const double fy = m * gy;
+  if (integrator == SG_SYMPLECTIC_EULER) {
+    const double sc = dt * minv;
+    v1x = v0x + sc * fx;
+    v1y = v0y + sc * fy;
+    q1x = q0x + dt * v1x;
+    q1y = q0y + dt * v1y;
+  } else {
+    const double sc = (0.5 * dt) * minv;
+    const double vhx = v0x + sc * fx;
+    const double vhy = v0y + sc * fy;
+    q1x = q0x + dt * vhx;
+    q1y = q0y + dt * vhy;
+    v1x = vhx + sc * fx;
+    v1y = vhy + sc * fy;
+  }
+}
+
+__global__ void k_predict_aabb(int nb, int integrator, double dt, double gx, double gy,
+                               const double2* __restrict__ q, const double2* __restrict__ v,
+                               const double* __restrict__ m, const double* __restrict__ minv,
+                               const double* __restrict__ rad, double2* __restrict__ q1, double2* __restrict__ v1,
+                               double4_32a* __restrict__ aabb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double2 q0 = q[i], v0 = v[i];
+  double2 qn, vn;
+  umap_body(integrator, dt, gx, gy, m[i], minv[i], q0.x, q0.y, v0.x, v0.y, qn.x, qn.y, vn.x, vn.y);
+  q1[i] = qn;
+  v1[i] = vn;
+  // Swept AABB [min(q0, q1) - r, max(q0, q1) + r] (Ball2DSim.cpp:566-572).
+  const double r = rad[i];
+  double4_32a b;
+  b.x = smin(qn.x, q0.x) - r;
+  b.y = smin(qn.y, q0.y) - r;
+  b.z = smax(qn.x, q0.x) + r;
+  b.w = smax(qn.y, q0.y) + r;
+  aabb[i] = b;
+}
+
+// Bounds of all boxes and the largest extent per axis (exact: min/max are order free).
+__global__ void k_bounds(int n, const double4_32a* __restrict__ aabb, GridParams* gp) {
+  double mn0 = INFINITY, mn1 = INFINITY, mx0 = -INFINITY, mx1 = -INFINITY, e0 = 0.0, e1 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double4_32a b = aabb[i];
+    mn0 = fmin(mn0, b.x);
+    mn1 = fmin(mn1, b.y);
+    mx0 = fmax(mx0, b.z);
+    mx1 = fmax(mx1, b.w);
+    e0 = fmax(e0, b.z - b.x);
+    e1 = fmax(e1, b.w - b.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn0 = fmin(mn0, __shfl_down_sync(0xffffffffu, mn0, o));
+    mn1 = fmin(mn1, __shfl_down_sync(0xffffffffu, mn1, o));
+    mx0 = fmax(mx0, __shfl_down_sync(0xffffffffu, mx0, o));
+    mx1 = fmax(mx1, __shfl_down_sync(0xffffffffu, mx1, o));
+    e0 = fmax(e0, __shfl_down_sync(0xffffffffu, e0, o));
+    e1 = fmax(e1, __shfl_down_sync(0xffffffffu, e1, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&gp->enc_min[0], f64_to_ordered(mn0));
+    atomicMin(&gp->enc_min[1], f64_to_ordered(mn1));
+    atomicMax(&gp->enc_max[0], f64_to_ordered(mx0));
+    atomicMax(&gp->enc_max[1], f64_to_ordered(mx1));
+    atomicMax(&gp->enc_ext[0], f64_to_ordered(e0));
+    atomicMax(&gp->enc_ext[1], f64_to_ordered(e1));
+  }
+}
+
+__global__ void k_bounds_init(GridParams* gp) {
+  gp->enc_min[0] = gp->enc_min[1] = ~0ull;
+  gp->enc_max[0] = gp->enc_max[1] = 0ull;
+  gp->enc_ext[0] = gp->enc_ext[1] = 0ull;
+}
+
+// Cell width h strictly above the largest box extent, so two overlapping boxes
+// have min corners in the same or adjacent cells (3x3 neighbourhood suffices).
+// The cell count is capped at `cap`; h grows if needed (larger cells stay correct).
+__global__ void k_grid_setup(GridParams* gp, long cap) {
+  const double mn0 = ordered_to_f64(gp->enc_min[0]), mn1 = ordered_to_f64(gp->enc_min[1]);
+  const double mx0 = ordered_to_f64(gp->enc_max[0]), mx1 = ordered_to_f64(gp->enc_max[1]);
+  const double e = fmax(ordered_to_f64(gp->enc_ext[0]), ordered_to_f64(gp->enc_ext[1]));
+  double h = e * (1.0 + 0x1p-20) + 1e-300;
+  if (!(h > 0.0) || !isfinite(h)) h = 1.0;
+  double span0 = mx0 - mn0, span1 = mx1 - mn1;
+  if (!isfinite(span0) || span0 < 0.0) span0 = 0.0;
+  if (!isfinite(span1) || span1 < 0.0) span1 = 0.0;
+  double d0 = floor(span0 / h) + 1.0, d1 = floor(span1 / h) + 1.0;
+  while (d0 * d1 > (double)cap) {
+    h = h * fmax(1.01, sqrt(d0 * d1 / (double)cap));
+    d0 = floor(span0 / h) + 1.0;
+    d1 = floor(span1 / h) + 1.0;
+  }
+  gp->origin[0] = isfinite(mn0) ? mn0 : 0.0;
+  gp->origin[1] = isfinite(mn1) ? mn1 : 0.0;
+  gp->h = h;
+  gp->dims[0] = (int)d0;
+  gp->dims[1] = (int)d1;
+  gp->ncells = (int)(d0 * d1);
+}
+
+__device__ __forceinline__ int cell_coord(double x, double o, double h, int dim) {
+  double f = (x - o) / h;
+  int c = (f > 0.0) ? (int)f : 0;  // NaN -> 0
+  return c < dim ? c : dim - 1;
+}
+
+__global__ void k_cell_count(int n, const double4_32a* __restrict__ aabb, const GridParams* __restrict__ gp,
+                             int* __restrict__ cell_of, int* __restrict__ cell_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a b = aabb[i];
+  const int cx = cell_coord(b.x, gp->origin[0], gp->h, gp->dims[0]);
+  const int cy = cell_coord(b.y, gp->origin[1], gp->h, gp->dims[1]);
+  const int cell = cx + gp->dims[0] * cy;
+  cell_of[i] = cell;
+  atomicAdd(&cell_count[cell], 1);
+}
+
+__global__ void k_cell_scatter(int n, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+                               int* __restrict__ cell_fill, int* __restrict__ sorted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cell = cell_of[i];
+  sorted[cell_start[cell] + atomicAdd(&cell_fill[cell], 1)] = i;
+}
+
+// AABB::overlaps (ball2d/SpatialGridDetector.cpp:15-26): touching boxes overlap.
+__device__ __forceinline__ bool aabb_overlap(const double4_32a& a, const double4_32a& b) {
+  if (a.z < b.x || a.w < b.y) return false;
+  if (b.z < a.x || b.w < a.y) return false;
+  return true;
+}
+
+// CollisionDetectionUtilities::computeCCDQuadraticCoeffs + ballBallCCDCollisionHappens
+// (CollisionDetectionUtilities.cpp:3-126).
+__device__ __forceinline__ void ccd_coeffs(double2 q0a, double2 q1a, double ra, double2 q0b, double2 q1b,
+                                           double rb, double& c0, double& c1, double& c2) {
+  const double d0x = q0a.x - q0b.x, d0y = q0a.y - q0b.y;
+  const double ex = (q1a.x - q1b.x) - d0x, ey = (q1a.y - q1b.y) - d0y;
+  const double rs = ra + rb;
+  c0 = (d0x * d0x + d0y * d0y) - rs * rs;
+  c1 = 2.0 * (d0x * ex + d0y * ey);
+  c2 = ex * ex + ey * ey;
+}
+
+__device__ __forceinline__ bool ccd_happens(double c0, double c1, double c2, double* t) {
+  if (c2 != 0.0) {
+    const double c1c1 = c1 * c1;
+    const double fc2c0 = 4.0 * c2 * c0;
+    if (c1c1 < fc2c0) return false;
+    const double ds = sqrt(c1c1 - fc2c0);
+    const double root1 = (c1 > 0.0) ? (2.0 * c0) / (-c1 - ds) : (-c1 + ds) / (2.0 * c2);
+    if (root1 < 0.0) return false;
+    const double root0 = (c1 >= 0.0) ? (-c1 - ds) / (2.0 * c2) : (2.0 * c0) / (-c1 + ds);
+    if (root0 > 1.0) return false;
+    if (t) *t = fmax(0.0, root0);
+    return true;
+  }
+  if (c0 <= 0.0) {
+    if (t) *t = 0.0;
+    return true;
+  }
+  return false;
+}
+
+struct PairScan {
+  const double4_32a* aabb;
+  const GridParams* gp;
+  const int* cell_start;
+  const int* sorted;
+  // narrow phase inputs (ccd mode)
+  const double2* q0;
+  const double2* q1;
+  const double* rad;
+};
+
+// Visits every j > i whose box overlaps box i (and, in ccd mode, whose CCD test
+// hits).  Scans the 3x3 cells around the cell of box i's min corner.
+template <bool kCcd, typename F>
+__device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
+  const double4_32a bi = s.aabb[i];
+  const GridParams& g = *s.gp;
+  const int cx = cell_coord(bi.x, g.origin[0], g.h, g.dims[0]);
+  const int cy = cell_coord(bi.y, g.origin[1], g.h, g.dims[1]);
+  double2 q0a, q1a;
+  double ra = 0.0;
+  if (kCcd) {
+    q0a = s.q0[i];
+    q1a = s.q1[i];
+    ra = s.rad[i];
+  }
+  for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y) {
+    for (int x = max(cx - 1, 0); x <= min(cx + 1, g.dims[0] - 1); ++x) {
+      const int cell = x + g.dims[0] * y;
+      const int e = s.cell_start[cell + 1];
+      for (int p = s.cell_start[cell]; p < e; ++p) {
+        const int j = s.sorted[p];
+        if (j <= i) continue;
+        if (!aabb_overlap(bi, s.aabb[j])) continue;
+        if (kCcd) {
+          double c0, c1, c2;
+          ccd_coeffs(q0a, q1a, ra, s.q0[j], s.q1[j], s.rad[j], c0, c1, c2);
+          if (!ccd_happens(c0, c1, c2, nullptr)) continue;
+        }
+        f(j);
+      }
+    }
+  }
+}
+
+template <bool kCcd>
+__global__ void k_pair_count(int n, PairScan s, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = 0;
+  visit_pairs<kCcd>(s, i, [&](int) { ++c; });
+  cnt[i] = c;
+}
+
+template <bool kCcd>
+__global__ void k_pair_write(int n, PairScan s, const int* __restrict__ off, int* __restrict__ out_a,
+                             int* __restrict__ out_b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int base = off[i];
+  int c = 0;
+  visit_pairs<kCcd>(s, i, [&](int j) {
+    // insertion into the sorted segment [base, base + c)
+    int p = base + c;
+    while (p > base && out_b[p - 1] > j) {
+      out_b[p] = out_b[p - 1];
+      --p;
+    }
+    out_b[p] = j;
+    ++c;
+  });
+  for (int k = 0; k < c; ++k) out_a[base + k] = i;
+}
+
+// StaticPlaneConstraint::isActive at the predictor position (BallStaticPlaneConstraint.cpp:10-14),
+// flattened plane-major like Ball2DSim::computeBallPlaneActiveSetAllPairs (Ball2DSim.cpp:747-762).
+__global__ void k_plane_flags(int nb, int np, const double2* __restrict__ q1, const double* __restrict__ rad,
+                              const double2* __restrict__ px, const double2* __restrict__ pn, int* __restrict__ flag) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nb * np) return;
+  const int p = (int)(t / nb), i = (int)(t - (long)p * nb);
+  const double2 x = px[p], nn = pn[p], qi = q1[i];
+  const double d = nn.x * (qi.x - x.x) + nn.y * (qi.y - x.y);
+  flag[t] = (d <= rad[i]) ? 1 : 0;
+}
+
+__global__ void k_plane_write(int nb, int np, int npairs, const int* __restrict__ flag, const int* __restrict__ off,
+                              int* __restrict__ ia, int* __restrict__ ib) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nb * np) return;
+  if (!flag[t]) return;
+  const int p = (int)(t / nb), i = (int)(t - (long)p * nb);
+  const int k = npairs + off[t];
+  ia[k] = i;
+  ib[k] = -1 - p;
+}
+
+// Contact keys: ball-ball (i, j) and plane-ball (p, i) in one sorted key space
+// (ConstraintCache keys, ball2d/ConstraintCache.cpp:20-50).
+__device__ __forceinline__ unsigned long long contact_key(int a, int b) {
+  if (b >= 0) return ((unsigned long long)(unsigned)a << 32) | (unsigned)b;
+  const unsigned p = (unsigned)(-1 - b);
+  return 0x8000000000000000ull | ((unsigned long long)p << 32) | (unsigned)a;
+}
+
+__device__ __forceinline__ long find_key(const unsigned long long* keys, long n, unsigned long long k) {
+  long lo = 0, hi = n;
+  while (lo < hi) {
+    const long mid = (lo + hi) >> 1;
+    if (keys[mid] < k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return (lo < n && keys[lo] == k) ? lo : -1;
+}
+
+struct AssembleArgs {
+  int nc;
+  const int* ia;
+  const int* ib;
+  const double2* q0;
+  const double2* v0;
+  const double* minv;
+  const double2* plane_n;
+  const double2* plane_t;
+  double mu, CoR;
+  int cache_mode;
+  const unsigned long long* prev_key;
+  const double2* prev_ab;
+  long prev_n;
+  double2* n;
+  double2* c;
+  double* W;
+  double* mu_out;
+  double2* r;
+  unsigned long long* key;
+};
+
+// Contact basis, forcing term, diagonal Delassus block and warm start per contact:
+// BallBallConstraint ctor (:26-37) and computeContactBasis (:244-252),
+// Constraint::computeForcingTerm (Constraint.cpp:18-34), evalKinematicRelVelGivenBases
+// (Constraint.cpp:92-126), Balls2DSobogusInterface::fromPrimal (:31-94),
+// initializeImpulses (GeometricImpactFrictionMap.cpp:174-220), solve2D warm start (Sobogus.cpp:299-301).
+__global__ void k_assemble(AssembleArgs A) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.nc) return;
+  const int a = A.ia[k], b = A.ib[k];
+  double nx, ny, tx, ty;
+  double vrx, vry;
+  const double2 va = A.v0[a];
+  if (b >= 0) {
+    const double2 qa = A.q0[a], qb = A.q0[b];
+    double dx = qa.x - qb.x, dy = qa.y - qb.y;
+    const double z = dx * dx + dy * dy;
+    if (z > 0.0) {
+      const double sq = sqrt(z);
+      dx = dx / sq;
+      dy = dy / sq;
+    }
+    nx = dx;
+    ny = dy;
+    tx = -dy;
+    ty = dx;
+    const double2 vb = A.v0[b];
+    vrx = va.x - vb.x;
+    vry = va.y - vb.y;
+  } else {
+    const int p = -1 - b;
+    const double2 pn = A.plane_n[p], pt = A.plane_t[p];
+    nx = pn.x;
+    ny = pn.y;
+    tx = pt.x;
+    ty = pt.y;
+    vrx = va.x - 0.0;
+    vry = va.y - 0.0;
+  }
+  const double ndotv = nx * vrx + ny * vry;
+  const double nrel = -(0.0 * nx + 0.0 * ny);
+  const double drel = -(0.0 * tx + 0.0 * ty);
+  const double s = A.CoR * ndotv + nrel;
+  const double wx = (0.0 + nx * s) + tx * drel;
+  const double wy = (0.0 + ny * s) + ty * drel;
+  A.n[k] = make_double2(nx, ny);
+  A.c[k] = make_double2(nx * wx + ny * wy, tx * wx + ty * wy);
+  const double nn = nx * nx + ny * ny;
+  const double nt = nx * tx + ny * ty;
+  const double tt = tx * tx + ty * ty;
+  const double ma = A.minv[a];
+  double w00 = ma * nn, w01 = ma * nt, w11 = ma * tt;
+  if (b >= 0) {
+    const double mb = A.minv[b];
+    w00 = w00 + mb * nn;
+    w01 = w01 + mb * nt;
+    w11 = w11 + mb * tt;
+  }
+  A.W[3 * k] = w00;
+  A.W[3 * k + 1] = w01;
+  A.W[3 * k + 2] = w11;
+  A.mu_out[k] = A.mu;
+  const unsigned long long key = contact_key(a, b);
+  A.key[k] = key;
+  double alpha = 0.0, beta = 0.0;
+  if (A.cache_mode != SG_CACHE_NONE && A.prev_n > 0) {
+    const long idx = find_key(A.prev_key, A.prev_n, key);
+    if (idx >= 0) {
+      const double2 ab = A.prev_ab[idx];
+      alpha = ab.x;
+      beta = (A.cache_mode == SG_CACHE_NORMAL_AND_FRICTION) ? ab.y : 0.0;
+    }
+  }
+  const double rwx = alpha * nx + beta * tx;
+  const double rwy = alpha * ny + beta * ty;
+  A.r[k] = make_double2(nx * rwx + ny * rwy, tx * rwx + ty * rwy);
+}
+
+// alpha = r_world . n, beta = r_world . t (Sobogus.cpp:312-330); caches (alpha, beta)
+// (cacheImpulses, GeometricImpactFrictionMap.cpp:222-264).
+__global__ void k_extract(int nc, const double2* __restrict__ n, const double2* __restrict__ r,
+                          const double* __restrict__ mu, int cache_mode, double2* __restrict__ ab) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const double2 nk = n[k], rk = r[k];
+  const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  const double rwx = nx * rk.x + tx * rk.y;
+  const double rwy = ny * rk.x + ty * rk.y;
+  const double alpha = rwx * nx + rwy * ny;
+  const double beta = (mu[k] == 0.0) ? 0.0 : (rwx * tx + rwy * ty);
+  (void)cache_mode;  // decaching applies the mode (k_assemble)
+  ab[k] = make_double2(alpha, beta);
+}
+
+__global__ void k_final_map(int nb, int integrator, double dt, double gx, double gy, const double2* __restrict__ q0,
+                            const double2* __restrict__ vin, const double* __restrict__ m,
+                            const double* __restrict__ minv, double2* __restrict__ q1, double2* __restrict__ v1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double2 q = q0[i], v = vin[i];
+  double2 qn, vn;
+  umap_body(integrator, dt, gx, gy, m[i], minv[i], q.x, q.y, v.x, v.y, qn.x, qn.y, vn.x, vn.y);
+  q1[i] = qn;
+  v1[i] = vn;
+}
+
+__global__ void k_ccd_batch(int n, const double2* q0a, const double2* q1a, const double* ra, const double2* q0b,
+                            const double2* q1b, const double* rb, double* coeffs, int* hit, double* t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double c0, c1, c2;
+  ccd_coeffs(q0a[i], q1a[i], ra[i], q0b[i], q1b[i], rb[i], c0, c1, c2);
+  coeffs[3 * i] = c0;
+  coeffs[3 * i + 1] = c1;
+  coeffs[3 * i + 2] = c2;
+  double tt = 0.0;
+  const bool h = ccd_happens(c0, c1, c2, &tt);
+  hit[i] = h ? 1 : 0;
+  t[i] = h ? tt : -1.0;
+}
+
+}  // namespace
+
+// ===========================================================================
+int ball2d_predict_and_bounds(sg_ctx* ctx) {
+  const int nb = ctx->nb;
+  if (nb <= 0) return SG_OK;
+  k_predict_aabb<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(
+      nb, ctx->cfg.integrator, ctx->cfg.dt, ctx->cfg.gravity[0], ctx->cfg.gravity[1], ctx->q.as<double2>(),
+      ctx->v.as<double2>(), ctx->m.as<double>(), ctx->minv.as<double>(), ctx->r.as<double>(), ctx->q1.as<double2>(),
+      ctx->v1.as<double2>(), ctx->aabb.as<double4_32a>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+static long grid_cap(int n) { return 4L * n + 64; }
+
+int broadphase_build_grid(sg_ctx* ctx, const double* aabb, int n) {
+  if (int r = grow(ctx->grid, sizeof(GridParams))) return r;
+  const long cap = grid_cap(n);
+  if (int r = grow(ctx->cell_count, sizeof(int) * (size_t)(cap + 1))) return r;
+  if (int r = grow(ctx->cell_start, sizeof(int) * (size_t)(cap + 1))) return r;
+  if (int r = grow(ctx->cell_fill, sizeof(int) * (size_t)(cap + 1))) return r;
+  if (int r = grow(ctx->cell_of, sizeof(int) * (size_t)n)) return r;
+  if (int r = grow(ctx->sorted, sizeof(int) * (size_t)n)) return r;
+  GridParams* gp = ctx->grid.as<GridParams>();
+  const double4_32a* bx = reinterpret_cast<const double4_32a*>(aabb);
+  k_bounds_init<<<1, 1, 0, ctx->stream>>>(gp);
+  const int nblk = std::min(blocks_for(n), ctx->num_sms * 8);
+  k_bounds<<<std::max(nblk, 1), kBlock, 0, ctx->stream>>>(n, bx, gp);
+  k_grid_setup<<<1, 1, 0, ctx->stream>>>(gp, cap);
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_count.p, 0, sizeof(int) * (size_t)(cap + 1), ctx->stream));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_fill.p, 0, sizeof(int) * (size_t)(cap + 1), ctx->stream));
+  k_cell_count<<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, bx, gp, ctx->cell_of.as<int>(), ctx->cell_count.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->cell_count.as<int>(), ctx->cell_start.as<int>(), (int)cap)) return r;
+  k_cell_scatter<<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, ctx->cell_of.as<int>(), ctx->cell_start.as<int>(),
+                                                            ctx->cell_fill.as<int>(), ctx->sorted.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+static PairScan make_scan(sg_ctx* ctx, const double* aabb, bool ccd) {
+  PairScan s;
+  s.aabb = reinterpret_cast<const double4_32a*>(aabb);
+  s.gp = ctx->grid.as<GridParams>();
+  s.cell_start = ctx->cell_start.as<int>();
+  s.sorted = ctx->sorted.as<int>();
+  s.q0 = ccd ? ctx->q.as<double2>() : nullptr;
+  s.q1 = ccd ? ctx->q1.as<double2>() : nullptr;
+  s.rad = ccd ? ctx->r.as<double>() : nullptr;
+  return s;
+}
+
+int broadphase_count_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd) {
+  if (int r = grow(ctx->pair_cnt, sizeof(int) * (size_t)(n + 1))) return r;
+  if (int r = grow(ctx->pair_off, sizeof(int) * (size_t)(n + 1))) return r;
+  const PairScan s = make_scan(ctx, aabb, ccd);
+  if (ccd)
+    k_pair_count<true><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_cnt.as<int>());
+  else
+    k_pair_count<false><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_cnt.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return scan_exclusive(ctx, ctx->pair_cnt.as<int>(), ctx->pair_off.as<int>(), n);
+}
+
+int broadphase_write_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd, int* out_a, int* out_b) {
+  const PairScan s = make_scan(ctx, aabb, ccd);
+  if (ccd)
+    k_pair_write<true><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_off.as<int>(), out_a, out_b);
+  else
+    k_pair_write<false><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_off.as<int>(), out_a, out_b);
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+int plane_flags(sg_ctx* ctx) {
+  const long t = (long)ctx->nb * ctx->np;
+  if (int r = grow(ctx->plane_flag, sizeof(int) * (size_t)(t + 1))) return r;
+  if (int r = grow(ctx->plane_off, sizeof(int) * (size_t)(t + 1))) return r;
+  if (t == 0) {
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->plane_off.p, 0, sizeof(int), ctx->stream));
+    return SG_OK;
+  }
+  k_plane_flags<<<blocks_for(t), kBlock, 0, ctx->stream>>>(ctx->nb, ctx->np, ctx->q1.as<double2>(), ctx->r.as<double>(),
+                                                           ctx->plane_x.as<double2>(), ctx->plane_n.as<double2>(),
+                                                           ctx->plane_flag.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return scan_exclusive(ctx, ctx->plane_flag.as<int>(), ctx->plane_off.as<int>(), (int)t);
+}
+
+int plane_write(sg_ctx* ctx, int npairs) {
+  const long t = (long)ctx->nb * ctx->np;
+  if (t == 0) return SG_OK;
+  k_plane_write<<<blocks_for(t), kBlock, 0, ctx->stream>>>(ctx->nb, ctx->np, npairs, ctx->plane_flag.as<int>(),
+                                                           ctx->plane_off.as<int>(), ctx->ia.as<int>(), ctx->ib.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+int assemble_contacts(sg_ctx* ctx, int nc) {
+  if (nc <= 0) return SG_OK;
+  AssembleArgs A;
+  A.nc = nc;
+  A.ia = ctx->ia.as<int>();
+  A.ib = ctx->ib.as<int>();
+  A.q0 = ctx->q.as<double2>();
+  A.v0 = ctx->v.as<double2>();
+  A.minv = ctx->minv.as<double>();
+  A.plane_n = ctx->plane_n.as<double2>();
+  A.plane_t = ctx->plane_t.as<double2>();
+  A.mu = ctx->cfg.mu;
+  A.CoR = ctx->cfg.CoR;
+  A.cache_mode = ctx->cfg.cache_mode;
+  A.prev_key = ctx->prev_key.as<unsigned long long>();
+  A.prev_ab = ctx->prev_ab.as<double2>();
+  A.prev_n = ctx->prev_n;
+  A.n = ctx->n.as<double2>();
+  A.c = ctx->c.as<double2>();
+  A.W = ctx->W.as<double>();
+  A.mu_out = ctx->mu.as<double>();
+  A.r = ctx->r_loc.as<double2>();
+  A.key = ctx->key.as<unsigned long long>();
+  k_assemble<<<blocks_for(nc), kBlock, 0, ctx->stream>>>(A);
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+int extract_and_cache(sg_ctx* ctx, int nc) {
+  if (nc <= 0) return SG_OK;
+  k_extract<<<blocks_for(nc), kBlock, 0, ctx->stream>>>(nc, ctx->n.as<double2>(), ctx->r_loc.as<double2>(),
+                                                        ctx->mu.as<double>(), ctx->cfg.cache_mode, ctx->ab.as<double2>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+int ball2d_final_map(sg_ctx* ctx, const double* vin) {
+  const int nb = ctx->nb;
+  if (nb <= 0) return SG_OK;
+  k_final_map<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(nb, ctx->cfg.integrator, ctx->cfg.dt, ctx->cfg.gravity[0],
+                                                          ctx->cfg.gravity[1], ctx->q.as<double2>(),
+                                                          reinterpret_cast<const double2*>(vin), ctx->m.as<double>(),
+                                                          ctx->minv.as<double>(), ctx->q1.as<double2>(),
+                                                          ctx->v1.as<double2>());
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+int ccd_batch(sg_ctx* ctx, int n, const double* q0a, const double* q1a, const double* ra, const double* q0b,
+              const double* q1b, const double* rb, double* coeffs, int* hit, double* t) {
+  if (n <= 0) return SG_OK;
+  k_ccd_batch<<<blocks_for(n), kBlock, 0, ctx->stream>>>(
+      n, reinterpret_cast<const double2*>(q0a), reinterpret_cast<const double2*>(q1a), ra,
+      reinterpret_cast<const double2*>(q0b), reinterpret_cast<const double2*>(q1b), rb, coeffs, hit, t);
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+}  // namespace sg

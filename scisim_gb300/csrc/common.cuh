@@ -1,0 +1,116 @@
+// common.cuh -- device utilities shared by the SCISim GB300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+namespace sg {
+
+constexpr int kMaxColors = 64;
+
+// ---------------------------------------------------------------------------
+// Order-preserving map of FP64 onto uint64, so that atomicMin/atomicMax on the
+// image give the exact (order-independent) FP64 min/max.  NaN maps above +inf.
+__device__ __forceinline__ unsigned long long f64_to_ordered(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ordered_to_f64(unsigned long long u) {
+  u = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+  return __longlong_as_double((long long)u);
+}
+__host__ __device__ constexpr unsigned long long ordered_neg_inf_floor() { return 0ull; }
+
+// Max over non-negative errors, NaN wins.
+__device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
+
+// ---------------------------------------------------------------------------
+// Bounded grid barrier for cooperative launches.  Every wait gives up after
+// spin_limit polls, raises `error` and returns false; callers return at once.
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+  int error;
+  int pad;
+};
+
+__device__ __forceinline__ bool grid_sync(GridBarrier* gb, unsigned long long spin_limit) {
+  __syncthreads();
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &gb->gen;
+    volatile int* verr = &gb->error;
+    const unsigned int g = *vgen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&gb->count, 1u);
+    int ok = 1;
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&gb->count, 0u);
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*vgen == g) {
+        if (*verr) break;
+        if (++spins > spin_limit) {
+          atomicExch(&gb->error, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (*verr) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_nanmax(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide nanmax; result valid in thread 0.  blockDim.x <= 1024.
+__device__ __forceinline__ double block_nanmax(double v) {
+  __shared__ double s[32];
+  v = warp_nanmax(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) s[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? s[lane] : 0.0;
+    v = warp_nanmax(v);
+  }
+  return v;
+}
+
+}  // namespace sg
+
+// ---------------------------------------------------------------------------
+// Host-side error plumbing.
+namespace sg {
+void set_error(const std::string& msg);
+}
+
+#define SG_CUDA_TRY(expr)                                                                        \
+  do {                                                                                           \
+    cudaError_t _e = (expr);                                                                     \
+    if (_e != cudaSuccess) {                                                                     \
+      ::sg::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e) + " (" __FILE__ ":" +   \
+                      std::to_string(__LINE__) + ")");                                          \
+      return SG_CUDA_ERROR;                                                                      \
+    }                                                                                            \
+  } while (0)

@@ -1,0 +1,138 @@
+// ctx.hpp -- internal state of an sg_ctx and the launchers of the kernel stages.
+#pragma once
+
+#include "../../include/scisim_gpu.h"
+#include "common.cuh"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace sg {
+
+// Uniform grid of the broad phase (device resident, written by k_grid_setup).
+struct GridParams {
+  unsigned long long enc_min[2];  // ordered encodings (atomics)
+  unsigned long long enc_max[2];
+  unsigned long long enc_ext[2];
+  double origin[2];
+  double h;
+  int dims[2];
+  int ncells;
+  int pad;
+};
+
+// Counters of one Gauss-Seidel solve (device resident).
+struct SolveStats {
+  unsigned long long err_slot[3];  // ordered encodings of the residual, rotating slots
+  int remaining[3];                // colouring: uncoloured contacts per round, rotating slots
+  int n_colors;
+  int status;                      // 0 ok, SG_CAPACITY / SG_DEVICE_TIMEOUT on failure
+  unsigned int iterations;
+  int converged;
+  double error;
+  int color_count[kMaxColors];
+  int color_off[kMaxColors + 1];
+  int color_fill[kMaxColors];
+};
+
+// A growable device buffer.
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+int grow(Buf& b, size_t bytes);  // contents are not preserved
+void release(Buf& b);
+
+// Sizes and pointers of one Ball2D contact problem, as the solver sees it.
+struct ContactProblem {
+  int nb = 0;
+  int nc = 0;
+  const double* minv = nullptr;  // nb
+  const double* m = nullptr;     // nb
+  const double* v0 = nullptr;    // 2nb
+  const int* ia = nullptr;       // nc
+  const int* ib = nullptr;       // nc, -1 static (any negative value)
+  const double* n = nullptr;     // 2nc (t = (-n_y, n_x))
+  const double* c = nullptr;     // 2nc local forcing E^T w
+  const double* W = nullptr;     // 3nc diagonal Delassus blocks
+  const double* mu = nullptr;    // nc
+  double* r = nullptr;           // 2nc in: warm start (local), out: solution
+  double* v2 = nullptr;          // 2nb out
+};
+
+struct SolveParams {
+  double tol;
+  unsigned int max_iters;
+  unsigned int eval_every;
+  int precision;
+};
+
+}  // namespace sg
+
+struct sg_ctx {
+  sg_config cfg{};
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int num_sms = 0;
+  unsigned long long spin_limit = 0;
+
+  // Ball2D scene
+  int nb = 0, np = 0;
+  sg::Buf q, v, r, m, minv, q1, v1, v2;
+  sg::Buf plane_x, plane_n, plane_t;
+
+  // broad phase
+  sg::Buf aabb, cell_of, cell_count, cell_start, cell_fill, sorted, pair_cnt, pair_off, grid;
+  sg::Buf plane_flag, plane_off, scan_tmp;
+
+  // contacts of the current step
+  int64_t ccap = 0;
+  sg::Buf ia, ib, n, c, W, mu, r_loc, r_cand, r_best, key, ab;
+  // impulse cache of the previous step (sorted keys and (alpha, beta))
+  sg::Buf prev_key, prev_ab;
+  int64_t prev_n = 0;
+
+  // solver
+  sg::Buf color, perm, body_cnt, body_off, body_fill, body_adj, v_run, stats, barrier;
+  // buffers of the standalone FrictionSolver entry (kept apart from the scene)
+  sg::Buf fs_m, fs_minv, fs_v0, fs_v2;
+
+  // host mirrors of the last step
+  int64_t last_nc = 0, last_nbb = 0;
+  sg::SolveStats h_stats{};
+
+  // pinned staging
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+};
+
+namespace sg {
+
+// Stage launchers (kernels in ball2d_kernels.cu / solver_kernels.cu / scan.cu).
+int scan_exclusive(sg_ctx* ctx, const int* in, int* out, int n);  // out[0..n], out[n] = total
+
+int ball2d_predict_and_bounds(sg_ctx* ctx);
+int broadphase_build_grid(sg_ctx* ctx, const double* aabb, int n);
+int broadphase_count_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd);
+int broadphase_write_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd, int* out_a, int* out_b);
+int plane_flags(sg_ctx* ctx);
+int plane_write(sg_ctx* ctx, int npairs);
+int assemble_contacts(sg_ctx* ctx, int nc);
+int extract_and_cache(sg_ctx* ctx, int nc);
+int ball2d_final_map(sg_ctx* ctx, const double* vin);
+int ccd_batch(sg_ctx* ctx, int n, const double* q0a, const double* q1a, const double* ra, const double* q0b,
+              const double* q1b, const double* rb, double* coeffs, int* hit, double* t);
+
+// Solver pipeline on a ContactProblem living in ctx buffers.
+int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp);
+int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc);
+
+int wait_timeout_selftest(sg_ctx* ctx);
+
+}  // namespace sg

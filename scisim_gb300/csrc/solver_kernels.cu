@@ -1,0 +1,610 @@
+// solver_kernels.cu -- graph-coloured block Gauss-Seidel Coulomb solve (FP64).
+//
+// The GPU form of Balls2DSobogusInterface::solve (scisim/ConstrainedMaps/bogus/
+// Ball2DSobogusInterface.cpp:102-148) and So-bogus's GaussSeidel + SOCLaw<2,double,true>.
+// The dual problem u = W r + b is evaluated matrix-free through body velocities
+// v = v0 + M^-1 H^T r: a contact's update reads the velocities of its two bodies,
+// solves the 2x2 local Coulomb problem with the diagonal block W_ii, and pushes
+// the impulse change back into the velocities.  Contacts of one colour share no
+// body, so a colour is one parallel phase; colours are separated by a bounded
+// grid barrier inside one persistent cooperative kernel per solve.
+//
+// Stages (all on the context stream):
+//   k_body_count/k_body_fill/k_body_sort  body -> contacts adjacency (ascending contact order)
+//   k_vel_init                             v = v0 + Minv H^T r_warm
+//   k_color_jp  (cooperative)              Jones-Plassmann colouring with hashed priorities,
+//                                          then the colour-ordered processing permutation
+//   k_gs        (cooperative)              sweeps, FB residual every eval_every sweeps,
+//                                          best-iterate tracking, early exit at tol
+//   k_final_velocity                       v2 = Minv (H^T r - f), f = -M v0
+#include "ctx.hpp"
+
+#include <algorithm>
+
+namespace sg {
+namespace {
+
+constexpr int kBlock = 256;
+inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
+
+// ---------------------------------------------------------------------------
+// Fischer-Burmeister Coulomb error (mu-scaled self-dual cone, De Saxce change of
+// variable); normal component first.
+__device__ __forceinline__ double fb_error_2d(double r0, double r1, double u0, double u1, double mu) {
+  const double nut = sqrt(u1 * u1);
+  if (mu == 0.0) {
+    const double fn = r0 + u0 - sqrt(r0 * r0 + u0 * u0);
+    double e2 = fn * fn;
+    e2 += r1 * r1;
+    return sqrt(e2);
+  }
+  const double x0 = mu * r0, x1 = r1;
+  const double y0 = u0 + mu * nut, y1 = mu * u1;
+  double z0 = 0.0;
+  z0 += x0 * x0;
+  z0 += x1 * x1;
+  z0 += y0 * y0;
+  z0 += y1 * y1;
+  const double zb = 2.0 * (x0 * x1 + y0 * y1);
+  double nzb2 = 0.0;
+  nzb2 += zb * zb;
+  const double nzb = sqrt(nzb2);
+  double l1 = z0 - nzb;
+  if (l1 < 0.0) l1 = 0.0;
+  const double l2 = z0 + nzb;
+  const double s1 = sqrt(l1), s2 = sqrt(l2);
+  const double sq0 = 0.5 * (s1 + s2);
+  const double half_diff = 0.5 * (s2 - s1);
+  const double sq1 = (nzb > 0.0) ? half_diff * (zb / nzb) : half_diff;
+  double e2 = 0.0;
+  const double p0 = x0 + y0 - sq0;
+  e2 += p0 * p0;
+  const double p1 = x1 + y1 - sq1;
+  e2 += p1 * p1;
+  return sqrt(e2);
+}
+
+// Local 2x2 Coulomb problem u = W r + b: take-off, stick, slide (+/-), else the
+// admissible candidate with the smallest FB error.
+__device__ __forceinline__ void local_solve_2d(double w00, double w01, double w11, double b0, double b1, double mu,
+                                               double& r0, double& r1) {
+  if (b0 >= 0.0) {
+    r0 = 0.0;
+    r1 = 0.0;
+    return;
+  }
+  const double det = w00 * w11 - w01 * w01;
+  const double rs0 = (w01 * b1 - w11 * b0) / det;
+  const double rs1 = (w01 * b0 - w00 * b1) / det;
+  if (rs0 >= 0.0 && fabs(rs1) <= mu * rs0) {
+    r0 = rs0;
+    r1 = rs1;
+    return;
+  }
+  double c0[2], c1[2];
+  bool have[2] = {false, false};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double s = (k == 0) ? 1.0 : -1.0;
+    const double den = w00 - s * mu * w01;
+    if (!(den > 0.0)) continue;
+    const double rn = -b0 / den;
+    const double rt = -s * mu * rn;
+    const double ut = w01 * rn + w11 * rt + b1;
+    c0[k] = rn;
+    c1[k] = rt;
+    have[k] = true;
+    if (s * ut >= 0.0) {
+      r0 = rn;
+      r1 = rt;
+      return;
+    }
+  }
+  double best = INFINITY, br0 = 0.0, br1 = 0.0;
+  {
+    const double e = fb_error_2d(0.0, 0.0, b0, b1, mu);
+    if (e < best) {
+      best = e;
+      br0 = 0.0;
+      br1 = 0.0;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    if (!have[k]) continue;
+    const double u0 = w00 * c0[k] + w01 * c1[k] + b0;
+    const double u1 = w01 * c0[k] + w11 * c1[k] + b1;
+    const double e = fb_error_2d(c0[k], c1[k], u0, u1, mu);
+    if (e < best) {
+      best = e;
+      br0 = c0[k];
+      br1 = c1[k];
+    }
+  }
+  r0 = br0;
+  r1 = br1;
+}
+
+// u = H v + c for contact k (body b < 0: static).
+__device__ __forceinline__ void local_velocity(const double2 nk, const double2 ck, const double2 va, bool has_b,
+                                               const double2 vb, double& u0, double& u1) {
+  const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  double hn = nx * va.x + ny * va.y;
+  double ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn = hn - (nx * vb.x + ny * vb.y);
+    ht = ht - (tx * vb.x + ty * vb.y);
+  }
+  u0 = hn + ck.x;
+  u1 = ht + ck.y;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_body_count(int nc, const int* __restrict__ ia, const int* __restrict__ ib, int* __restrict__ cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  atomicAdd(&cnt[ia[k]], 1);
+  const int b = ib[k];
+  if (b >= 0) atomicAdd(&cnt[b], 1);
+}
+
+__global__ void k_body_fill(int nc, const int* __restrict__ ia, const int* __restrict__ ib, const int* __restrict__ off,
+                            int* __restrict__ fill, int* __restrict__ adj) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int a = ia[k];
+  adj[off[a] + atomicAdd(&fill[a], 1)] = k;
+  const int b = ib[k];
+  if (b >= 0) adj[off[b] + atomicAdd(&fill[b], 1)] = k;
+}
+
+__global__ void k_body_sort(int nb, const int* __restrict__ off, int* __restrict__ adj) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int s = off[i], e = off[i + 1];
+  for (int p = s + 1; p < e; ++p) {
+    const int x = adj[p];
+    int q = p;
+    while (q > s && adj[q - 1] > x) {
+      adj[q] = adj[q - 1];
+      --q;
+    }
+    adj[q] = x;
+  }
+}
+
+// H^T r gathered per body in ascending contact order.
+__device__ __forceinline__ void gather_htr(int body, const int* __restrict__ off, const int* __restrict__ adj,
+                                           const int* __restrict__ ia, const double2* __restrict__ n,
+                                           const double2* __restrict__ r, double& hx, double& hy) {
+  hx = 0.0;
+  hy = 0.0;
+  const int e = off[body + 1];
+  for (int p = off[body]; p < e; ++p) {
+    const int k = adj[p];
+    const double sgn = (ia[k] == body) ? 1.0 : -1.0;
+    const double2 nk = n[k], rk = r[k];
+    const double tx = -nk.y, ty = nk.x;
+    const double px = nk.x * rk.x + tx * rk.y;
+    const double py = nk.y * rk.x + ty * rk.y;
+    hx = hx + sgn * px;
+    hy = hy + sgn * py;
+  }
+}
+
+__global__ void k_vel_init(int nb, const int* __restrict__ off, const int* __restrict__ adj, const int* __restrict__ ia,
+                           const double2* __restrict__ n, const double2* __restrict__ r, const double2* __restrict__ v0,
+                           const double* __restrict__ minv, double2* __restrict__ v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  double hx, hy;
+  gather_htr(i, off, adj, ia, n, r, hx, hy);
+  const double2 a = v0[i];
+  const double mi = minv[i];
+  v[i] = make_double2(a.x + mi * hx, a.y + mi * hy);
+}
+
+__global__ void k_final_velocity(int nb, const int* __restrict__ off, const int* __restrict__ adj,
+                                 const int* __restrict__ ia, const double2* __restrict__ n, const double2* __restrict__ r,
+                                 const double2* __restrict__ v0, const double* __restrict__ m,
+                                 const double* __restrict__ minv, double2* __restrict__ v2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double2 a = v0[i];
+  if (off[i + 1] == off[i]) {
+    v2[i] = a;
+    return;
+  }
+  double hx, hy;
+  gather_htr(i, off, adj, ia, n, r, hx, hy);
+  const double fx = -(m[i] * a.x);
+  const double fy = -(m[i] * a.y);
+  const double mi = minv[i];
+  v2[i] = make_double2(mi * (hx - fx), mi * (hy - fy));
+}
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned hash_prio(unsigned k) {
+  k ^= k >> 16;
+  k *= 0x7feb352du;
+  k ^= k >> 15;
+  k *= 0x846ca68bu;
+  k ^= k >> 16;
+  return k;
+}
+__device__ __forceinline__ bool prio_greater(unsigned pj, int j, unsigned pk, int k) {
+  return pj > pk || (pj == pk && j > k);
+}
+
+struct ColorArgs {
+  int nc;
+  const int* ia;
+  const int* ib;
+  const int* body_off;
+  const int* body_adj;
+  int* color;  // packed (round << 8) | colour, -1 uncoloured
+  int* perm;
+  SolveStats* st;
+  GridBarrier* gb;
+  unsigned long long spin;
+  int max_rounds;
+};
+
+__global__ void k_color_jp(ColorArgs A) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  volatile int* vcolor = A.color;
+  for (int round = 0;; ++round) {
+    if (round >= A.max_rounds) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_CAPACITY);
+      return;
+    }
+    int rem = 0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      if (vcolor[k] >= 0) continue;
+      const unsigned pk = hash_prio((unsigned)k);
+      unsigned long long used = 0ull;
+      bool is_max = true;
+      const int bodies[2] = {A.ia[k], A.ib[k]};
+      for (int bi = 0; bi < 2 && is_max; ++bi) {
+        const int body = bodies[bi];
+        if (body < 0) continue;
+        const int e = A.body_off[body + 1];
+        for (int p = A.body_off[body]; p < e; ++p) {
+          const int j = A.body_adj[p];
+          if (j == k) continue;
+          const int cj = vcolor[j];
+          if (cj >= 0 && (cj >> 8) < round) {
+            used |= 1ull << (cj & 63);
+          } else if (prio_greater(hash_prio((unsigned)j), j, pk, k)) {
+            is_max = false;
+            break;
+          }
+        }
+      }
+      if (is_max) {
+        const unsigned long long freec = ~used;
+        if (freec == 0ull) {
+          atomicExch(&A.st->status, (int)SG_CAPACITY);
+          vcolor[k] = (round << 8) | 63;
+        } else {
+          vcolor[k] = (round << 8) | (__ffsll((long long)freec) - 1);
+        }
+      } else {
+        ++rem;
+      }
+    }
+    rem = warp_sum(rem);
+    if ((threadIdx.x & 31) == 0 && rem) atomicAdd(&A.st->remaining[round % 3], rem);
+    if (tid == 0) A.st->remaining[(round + 1) % 3] = 0;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const int left = *((volatile int*)&A.st->remaining[round % 3]);
+    if (left == 0) break;
+  }
+  // Colour histogram.
+  __shared__ int hist[kMaxColors];
+  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) hist[c] = 0;
+  __syncthreads();
+  for (int k = tid; k < A.nc; k += nthr) atomicAdd(&hist[vcolor[k] & 63], 1);
+  __syncthreads();
+  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x)
+    if (hist[c]) atomicAdd(&A.st->color_count[c], hist[c]);
+  if (!grid_sync(A.gb, A.spin)) {
+    if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int off = 0, ncol = 0;
+    for (int c = 0; c < kMaxColors; ++c) {
+      A.st->color_off[c] = off;
+      const int cc = A.st->color_count[c];
+      off += cc;
+      if (cc) ncol = c + 1;
+    }
+    A.st->color_off[kMaxColors] = off;
+    A.st->n_colors = ncol;
+  }
+  if (!grid_sync(A.gb, A.spin)) {
+    if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+    return;
+  }
+  for (int k = tid; k < A.nc; k += nthr) {
+    const int c = vcolor[k] & 63;
+    A.perm[A.st->color_off[c] + atomicAdd(&A.st->color_fill[c], 1)] = k;
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct GsArgs {
+  int nc;
+  const int* ia;
+  const int* ib;
+  const double2* n;
+  const double2* c;
+  const double* W;
+  const double* mu;
+  const double* minv;
+  const int* perm;
+  double2* r;
+  double2* r_a;  // snapshot buffers for best-iterate tracking
+  double2* r_b;
+  double2* v;
+  SolveStats* st;
+  GridBarrier* gb;
+  unsigned long long spin;
+  double tol;
+  unsigned max_iters;
+  unsigned eval_every;
+};
+
+__device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
+  const int a = A.ia[k], b = A.ib[k];
+  const double2 nk = A.n[k], ck = A.c[k];
+  const double2 va = A.v[a];
+  const bool has_b = b >= 0;
+  const double2 vb = has_b ? A.v[b] : make_double2(0.0, 0.0);
+  double u0, u1;
+  local_velocity(nk, ck, va, has_b, vb, u0, u1);
+  const double2 rk = A.r[k];
+  const double r0 = rk.x, r1 = rk.y;
+  const double w00 = A.W[3 * k], w01 = A.W[3 * k + 1], w11 = A.W[3 * k + 2];
+  const double bt0 = u0 - (w00 * r0 + w01 * r1);
+  const double bt1 = u1 - (w01 * r0 + w11 * r1);
+  double rn0, rn1;
+  local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
+  const double d0 = rn0 - r0, d1 = rn1 - r1;
+  const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  const double px = nx * d0 + tx * d1;
+  const double py = ny * d0 + ty * d1;
+  const double ma = A.minv[a];
+  A.v[a] = make_double2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const double mb = A.minv[b];
+    A.v[b] = make_double2(vb.x - mb * px, vb.y - mb * py);
+  }
+  A.r[k] = make_double2(rn0, rn1);
+}
+
+__global__ void __launch_bounds__(kBlock) k_gs(GsArgs A) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  // A colouring that gave up (timeout or capacity) leaves no valid permutation.
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval_every = A.eval_every ? A.eval_every : 1u;
+  double2* best = A.r_a;
+  double2* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false;
+  unsigned it = 0;
+  unsigned n_eval = 0;
+  for (it = 1; it <= A.max_iters; ++it) {
+    for (int col = 0; col < ncol; ++col) {
+      const int e = s_off[col + 1];
+      for (int s = s_off[col] + tid; s < e; s += nthr) gs_update(A, A.perm[s]);
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+    }
+    if (it % eval_every == 0) {
+      double emax = 0.0;
+      for (int k = tid; k < A.nc; k += nthr) {
+        const int a = A.ia[k], b = A.ib[k];
+        const bool has_b = b >= 0;
+        const double2 va = A.v[a];
+        const double2 vb = has_b ? A.v[b] : make_double2(0.0, 0.0);
+        double u0, u1;
+        local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+        const double2 rk = A.r[k];
+        cand[k] = rk;
+        emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+      }
+      emax = block_nanmax(emax);
+      const int slot = n_eval % 3;
+      if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+      if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+      ++n_eval;
+      if (err < err_best) {
+        err_best = err;
+        double2* t = best;
+        best = cand;
+        cand = t;
+      }
+      if (err < A.tol) {
+        converged = true;
+        break;
+      }
+    }
+  }
+  if (!converged) {
+    // Return the best iterate (GaussSeidel: x = x_best when GSIter > maxIters).
+    if (err_best < INFINITY)
+      for (int k = tid; k < A.nc; k += nthr) A.r[k] = best[k];
+    it = A.max_iters;
+  }
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+  }
+}
+
+__global__ void k_wait_flag(const int* flag, int* status, unsigned long long spin) {
+  volatile const int* f = flag;
+  unsigned long long n = 0;
+  while (*f == 0) {
+    if (++n > spin) {
+      *status = SG_DEVICE_TIMEOUT;
+      return;
+    }
+    __nanosleep(32);
+  }
+  *status = SG_OK;
+}
+
+template <typename K>
+int coop_grid(sg_ctx* ctx, K kernel, long work) {
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kBlock, 0) != cudaSuccess || bps < 1) bps = 1;
+  long g = (long)bps * ctx->num_sms;
+  const long need = std::max(1L, (work + kBlock - 1) / kBlock);
+  return (int)std::min(g, need);
+}
+
+}  // namespace
+
+int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc) {
+  const size_t ncs = (size_t)std::max(nc, 1), nbs = (size_t)std::max(nb, 1);
+  if (int r = grow(ctx->color, sizeof(int) * ncs)) return r;
+  if (int r = grow(ctx->perm, sizeof(int) * ncs)) return r;
+  if (int r = grow(ctx->body_cnt, sizeof(int) * (nbs + 1))) return r;
+  if (int r = grow(ctx->body_off, sizeof(int) * (nbs + 1))) return r;
+  if (int r = grow(ctx->body_fill, sizeof(int) * (nbs + 1))) return r;
+  if (int r = grow(ctx->body_adj, sizeof(int) * 2 * ncs)) return r;
+  if (int r = grow(ctx->v_run, sizeof(double) * 2 * nbs)) return r;
+  if (int r = grow(ctx->r_cand, sizeof(double) * 2 * ncs)) return r;
+  if (int r = grow(ctx->r_best, sizeof(double) * 2 * ncs)) return r;
+  if (int r = grow(ctx->stats, sizeof(SolveStats))) return r;
+  if (int r = grow(ctx->barrier, sizeof(GridBarrier))) return r;
+  return SG_OK;
+}
+
+int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) {
+  const int nb = P.nb, nc = P.nc;
+  cudaStream_t s = ctx->stream;
+  if (int r = ensure_solver_capacity(ctx, nb, nc)) return r;
+  int* cnt = ctx->body_cnt.as<int>();
+  int* off = ctx->body_off.as<int>();
+  int* fill = ctx->body_fill.as<int>();
+  int* adj = ctx->body_adj.as<int>();
+  SolveStats* st = ctx->stats.as<SolveStats>();
+  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  const double2* n2 = reinterpret_cast<const double2*>(P.n);
+  double2* r2 = reinterpret_cast<double2*>(P.r);
+
+  SG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)(nb + 1), s));
+  SG_CUDA_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * (size_t)(nb + 1), s));
+  SG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(SolveStats), s));
+  if (nc > 0) {
+    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, cnt);
+    SG_CUDA_TRY(cudaGetLastError());
+  }
+  if (int r = scan_exclusive(ctx, cnt, off, nb)) return r;
+  if (nc > 0) {
+    k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, off, fill, adj);
+    k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
+    SG_CUDA_TRY(cudaGetLastError());
+  }
+  double2* vrun = ctx->v_run.as<double2>();
+  k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
+                                               P.minv, vrun);
+  SG_CUDA_TRY(cudaGetLastError());
+
+  if (nc > 0) {
+    // Colouring.
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->color.p, 0xff, sizeof(int) * (size_t)nc, s));
+    SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+    ColorArgs CA{nc, P.ia, P.ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit, 4096};
+    {
+      void* args[] = {&CA};
+      const int g = coop_grid(ctx, k_color_jp, nc);
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_color_jp, dim3(g), dim3(kBlock), args, 0, s));
+    }
+    // Gauss-Seidel.
+    SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+    GsArgs GA;
+    GA.nc = nc;
+    GA.ia = P.ia;
+    GA.ib = P.ib;
+    GA.n = n2;
+    GA.c = reinterpret_cast<const double2*>(P.c);
+    GA.W = P.W;
+    GA.mu = P.mu;
+    GA.minv = P.minv;
+    GA.perm = ctx->perm.as<int>();
+    GA.r = r2;
+    GA.r_a = ctx->r_cand.as<double2>();
+    GA.r_b = ctx->r_best.as<double2>();
+    GA.v = vrun;
+    GA.st = st;
+    GA.gb = gb;
+    GA.spin = ctx->spin_limit;
+    GA.tol = sp.tol;
+    GA.max_iters = sp.max_iters;
+    GA.eval_every = sp.eval_every;
+    {
+      void* args[] = {&GA};
+      const int g = coop_grid(ctx, k_gs, nc);
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kBlock), args, 0, s));
+    }
+  }
+  k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
+                                                     P.m, P.minv, reinterpret_cast<double2*>(P.v2));
+  SG_CUDA_TRY(cudaGetLastError());
+  SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (nc == 0) {
+    ctx->h_stats.iterations = 0;
+    ctx->h_stats.converged = 1;
+    ctx->h_stats.error = 0.0;
+  }
+  if (ctx->h_stats.status == SG_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its spin limit");
+    return SG_DEVICE_TIMEOUT;
+  }
+  if (ctx->h_stats.status == SG_CAPACITY) {
+    set_error("contact colouring exceeded 64 colours or its round limit");
+    return SG_CAPACITY;
+  }
+  return ctx->h_stats.converged ? SG_OK : SG_NOT_CONVERGED;
+}
+
+int wait_timeout_selftest(sg_ctx* ctx) {
+  Buf flag;
+  if (int r = grow(flag, 2 * sizeof(int))) return r;
+  SG_CUDA_TRY(cudaMemsetAsync(flag.p, 0, 2 * sizeof(int), ctx->stream));
+  int* f = flag.as<int>();
+  k_wait_flag<<<1, 1, 0, ctx->stream>>>(f, f + 1, ctx->spin_limit);
+  SG_CUDA_TRY(cudaGetLastError());
+  int status = -1;
+  SG_CUDA_TRY(cudaMemcpyAsync(&status, f + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  release(flag);
+  return status;
+}
+
+}  // namespace sg

@@ -1,0 +1,119 @@
+"""Seeded synthetic Ball2D scenes of the benchmark configurations.
+
+No public dataset is involved: every scene is generated from a fixed seed.
+
+  box_drop_1024   1,024 discs, r ~ U[0.04, 0.06], density 1, 32 x 32 lattice of
+                  spacing 0.13 with U[-0.01, 0.01] jitter, v ~ N(0, 0.1^2), static
+                  planes bounding [-2.5, 2.5] x [0, inf) (floor, two walls, and a lid
+                  far above), gravity (0, -9.81), symplectic Euler dt 0.01, CoR 0.3,
+                  mu 0.5, tol 1e-9, 5,000 iterations
+  dense_pile      262,144 discs, r log-uniform [0.02, 0.06], density 1, non-overlapping
+                  fill of a 40 x 60 box (area fraction ~0.5) built by size-sorted
+                  shelf packing with random slack, rows shuffled, bodies permuted;
+                  four walls; gravity -9.81, dt 0.005, CoR 0, mu 0.4
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def box_drop_1024(seed: int = 1, n_side: int = 32):
+    rng = np.random.default_rng(seed)
+    n = n_side * n_side
+    r = rng.uniform(0.04, 0.06, n)
+    m = math.pi * r * r  # density 1
+    ix, iy = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="xy")
+    x = (ix.reshape(-1) - (n_side - 1) / 2.0) * 0.13 + rng.uniform(-0.01, 0.01, n)
+    y = 0.1 + iy.reshape(-1) * 0.13 + rng.uniform(-0.01, 0.01, n)
+    q = np.stack([x, y], axis=1).reshape(-1)
+    v = rng.normal(0.0, 0.1, 2 * n)
+    plane_x = np.array([[0.0, 0.0], [-2.5, 0.0], [2.5, 0.0], [0.0, 1000.0]])
+    plane_n = np.array([[0.0, 1.0], [1.0, 0.0], [-1.0, 0.0], [0.0, -1.0]])
+    return dict(q=q, v=v, r=r, m=m, plane_x=plane_x, plane_n=plane_n, dt=0.01, gravity=(0.0, -9.81), CoR=0.3,
+                mu=0.5, tol=1e-9, max_iters=5000, name="box_drop_1024")
+
+
+def dense_pile(n: int = 262144, seed: int = 2, width: float = 40.0, height: float = 60.0, rmin: float = 0.02,
+               rmax: float = 0.06):
+    """Non-overlapping polydisperse fill of a width x height box (walls at x = +-width/2, floor y = 0)."""
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(math.log(rmin), math.log(rmax), n))
+    order = np.argsort(-r, kind="stable")
+    rs = r[order]
+    # Shelf packing of the size-sorted discs: rows of similar radii.
+    rows = []
+    i = 0
+    gap = 0.002
+    while i < n:
+        w = 0.0
+        j = i
+        while j < n and w + 2.0 * rs[j] + gap <= width:
+            w += 2.0 * rs[j] + gap
+            j += 1
+        if j == i:
+            raise ValueError("disc wider than the box")
+        rows.append((i, j, w))
+        i = j
+    heights = np.array([2.0 * rs[a] + gap for a, _, _ in rows])
+    slack_y = height - heights.sum()
+    if slack_y < 0:
+        raise ValueError("discs do not fit in the box")
+    row_order = rng.permutation(len(rows))
+    vgaps = rng.dirichlet(np.ones(len(rows) + 1)) * slack_y
+    pos = np.empty((n, 2))
+    y = vgaps[0]
+    for k, ri in enumerate(row_order):
+        a, b, w = rows[ri]
+        hrow = heights[ri]
+        cnt = b - a
+        hgaps = rng.dirichlet(np.ones(cnt + 1)) * (width - w)
+        x = -0.5 * width
+        for t in range(cnt):
+            rad = rs[a + t]
+            x += hgaps[t] + 0.5 * gap + rad
+            jit = rng.uniform(-1.0, 1.0) * (0.5 * hrow - 0.5 * gap - rad)
+            pos[a + t] = (x, y + 0.5 * hrow + jit)
+            x += rad + 0.5 * gap
+        y += hrow + vgaps[k + 1]
+    # Undo the size sort, then permute body indices.
+    q = np.empty((n, 2))
+    q[order] = pos
+    perm = rng.permutation(n)
+    q = q[perm]
+    r = r[perm]
+    m = math.pi * r * r
+    v = np.zeros(2 * n)
+    plane_x = np.array([[0.0, 0.0], [-0.5 * width, 0.0], [0.5 * width, 0.0], [0.0, height]])
+    plane_n = np.array([[0.0, 1.0], [1.0, 0.0], [-1.0, 0.0], [0.0, -1.0]])
+    return dict(q=q.reshape(-1), v=v, r=r, m=m, plane_x=plane_x, plane_n=plane_n, dt=0.005, gravity=(0.0, -9.81),
+                CoR=0.0, mu=0.4, tol=1e-6, max_iters=5000, name="dense_pile_%d" % n)
+
+
+def min_gap(q, r, plane_x=None, plane_n=None):
+    """Smallest pairwise gap (brute force on a grid; for tests of the generators)."""
+    q = np.asarray(q).reshape(-1, 2)
+    n = q.shape[0]
+    h = 2.0 * r.max()
+    keys = np.floor(q / h).astype(np.int64)
+    cells = {}
+    for i, (a, b) in enumerate(keys):
+        cells.setdefault((a, b), []).append(i)
+    best = np.inf
+    for (a, b), idx in cells.items():
+        cand = []
+        for da in (-1, 0, 1):
+            for db in (-1, 0, 1):
+                cand += cells.get((a + da, b + db), [])
+        cand = np.array(cand)
+        for i in idx:
+            js = cand[cand > i]
+            if js.size:
+                d = np.sqrt(((q[js] - q[i]) ** 2).sum(1)) - r[js] - r[i]
+                best = min(best, d.min())
+    if plane_x is not None:
+        for x, nn in zip(np.asarray(plane_x).reshape(-1, 2), np.asarray(plane_n).reshape(-1, 2)):
+            d = (q - x) @ (nn / np.linalg.norm(nn)) - r
+            best = min(best, d.min())
+    return best
