@@ -1,0 +1,357 @@
+#!/usr/bin/env python
+"""Contact-steps/s of SCISim's Ball2D contact path on one GB300.
+
+Workload (the headline configuration): the Ball2D dense pile, 262,144 discs with
+radii log-uniform in [0.02, 0.06] (density 1), seeded non-overlapping fill of a
+40 x 60 box with four walls, gravity -9.81, symplectic Euler dt 0.005, CoR 0,
+mu 0.4, Coulomb residual tolerance 1e-6 (FP64-evaluated), at most 5,000
+Gauss-Seidel iterations per step.  The job starts from the fill; the first
+--preroll steps (the pile forming) are run but not timed, then --warmup steps,
+then --steps timed steps.
+
+A step is one GeometricImpactFrictionMap::flow of the whole scene: predictor,
+broad + narrow phase, contact assembly, coloured block Gauss-Seidel to tolerance,
+impulse cache, final map.  value = sum of active contacts over the timed steps /
+their device time (inputs resident in HBM, L2 flushed between steps).  e2e = the
+same through the reference-facing C-ABI call sg_flow with pinned host buffers
+(q0, v0 up; q1, v1 down) inside the timed region.
+
+Solver forms: "warm" (impulse cache NORMAL_AND_FRICTION, the previous step's
+impulses as the start) is the headline; "plain" (cold start, FP64) is timed on the
+same state and reported beside it.
+
+--impl reference times the reference algorithm's CPU implementation (the oracle,
+a restatement of SCISim + So-bogus; the reference itself needs Eigen/So-bogus,
+absent here) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "contact-steps/s to Coulomb residual<=1e-6: warm-start+batched vs plain GPU"
+UNIT = "contact-steps/s"
+WORKLOAD = "ball2d_dense_pile_262144"
+# Algorithmic bytes of the Gauss-Seidel kernel (FP64), per contact:
+#   update: perm 4, ia 4, ib 4, n 16, c 16, W 24, mu 8, r 16+16, minv 2x8, v_a 16+16, v_b 16+16
+#   residual: ia 4, ib 4, v_a 16, v_b 16, n 16, c 16, r 16, snapshot 16, mu 8
+BYTES_PER_CONTACT_SWEEP = 188
+BYTES_PER_CONTACT_EVAL = 112
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = os.path.join(HERE, "gpurun_out", "clocks.csv") if os.path.isdir(
+            os.path.join(HERE, "gpurun_out")) else "/tmp/sg_clocks.csv"
+
+    def start(self):
+        try:
+            self.fh = open(self.out, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.out):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_scene(n):
+    """The dense-pile fill with n discs: the 40 x 60 box for 262,144 discs; other sizes
+    keep the depth (60) and the area fraction by scaling the width."""
+    from scisim_gb300 import scenes
+    return scenes.dense_pile(n=n, seed=2, width=40.0 * n / 262144.0, height=60.0)
+
+
+def solver_kw(s, **over):
+    kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, max_iters=5000, eval_every=1)
+    kw.update(over)
+    return kw
+
+
+# --------------------------------------------------------------------------- CPU leg
+def cpu_sample(args, steps):
+    """The oracle on a strip of the same workload: same disc distribution, depth and
+    solver settings, width 40/128 (2,048 discs).  Pre-rolled to the same step on the
+    CPU, then `steps` timed steps.  Returns (contact-steps/s, description)."""
+    from oracle import oracle as O  # checker / CPU baseline only
+    O.build()
+    n = max(2048, args.n // 128)
+    s = make_scene(n)
+    frac = 262144.0 / n
+    kw = solver_kw(s)
+    sim = O.Ball2D(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"],
+                   cache_mode=O.CACHE_NORMAL_AND_FRICTION, **kw)
+    t0 = time.perf_counter()
+    sim.set_solver(kw["tol"], args.preroll_iters)
+    sim.run(args.preroll)
+    sim.set_solver(kw["tol"], kw["max_iters"])
+    sim.run(args.warmup)
+    pre = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    st, tot, bad = sim.run(steps)
+    dt = time.perf_counter() - t0
+    desc = ("oracle (C++ restatement of SCISim + So-bogus, sequential block GS, 1 thread) on a %d-disc strip "
+            "(width 40/%d, same depth, radii, density and solver settings), pre-rolled %d steps on the CPU in "
+            "%.1f s, then %d timed steps: %d contact-steps in %.2f s" % (n, frac, args.preroll + args.warmup, pre,
+                                                                         steps, tot, dt))
+    return tot / dt, desc, 1
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    value, desc, cores = cpu_sample(args, args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dense-pile fill)",
+            "config": {"workload": WORKLOAD, "sample": "2,048-disc strip of the same fill",
+                       "tol": 1e-6, "max_iters": 5000, "warm_start": "normal_and_friction"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- GPU leg
+def timed_steps(ctx, torch, stream, k, flush):
+    """k steps, each bracketed by CUDA events on the library's stream; L2 flushed between."""
+    ms, contacts = [], []
+    for _ in range(k):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = ctx.step(1)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        contacts.append(st["n_contacts"])
+    return ms, contacts
+
+
+def run_ours(args):
+    import torch
+
+    from scisim_gb300 import _lib
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    s = make_scene(args.n)
+    nb = s["r"].shape[0]
+    fast = _lib.Context(device=local, cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision,
+                        **solver_kw(s))
+    fast.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    stream = torch.cuda.ExternalStream(fast.stream_ptr(), device=local)
+    t0 = time.perf_counter()
+    # The pile forms during the pre-roll; its solves are capped at --preroll-iters sweeps
+    # (warm started) so that forming the pile costs seconds, not the full-tolerance price.
+    fast.reconfigure(max_iters=args.preroll_iters)
+    pre = fast.step(args.preroll) if args.preroll else {"total_contacts": 0}
+    fast.reconfigure(max_iters=5000)
+    log("preroll %d steps in %.1f s, last step %s" % (args.preroll, time.perf_counter() - t0, pre))
+    pw = fast.step(args.warmup) if args.warmup else None
+    log("warmup", pw)
+    q_snap, v_snap = fast.state()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    fast.profile_enable(True)
+    fast.profile_read(reset=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms, contacts = timed_steps(fast, torch, stream, args.steps, flush)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    prof = fast.profile_read(reset=True)
+    total_ms = float(sum(ms))
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    csteps = int(sum(contacts))
+    value = csteps * ws / (total_ms / 1e3)
+    log("fast: %d contact-steps in %.1f ms; per step ms %s; profile %s" % (csteps, total_ms, [round(x, 2) for x in ms],
+                                                                         prof))
+    # Roofline of the dominant kernel (the Gauss-Seidel solve): algorithmic bytes per
+    # launch over its CUDA-event duration.
+    hbm, peak_kind = peaks()
+    gl = max(prof["gs_launches"], 1)
+    bytes_per_launch = (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP +
+                        prof["contact_evals"] * BYTES_PER_CONTACT_EVAL) / gl
+    gs_ms_per_launch = prof["gs_ms"] / gl
+    achieved = bytes_per_launch / (gs_ms_per_launch / 1e3) / 1e9 if gs_ms_per_launch > 0 else 0.0
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "gs_dram_bytes_per_contact_sweep.json")
+    if os.path.exists(tp):
+        d = json.load(open(tp))
+        traffic = d["bytes_per_contact_sweep"] * (prof["contact_sweeps"] + prof["contact_evals"]) / gl
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                "kernel": "k_gs (cooperative coloured block Gauss-Seidel)",
+                "bytes_per_launch": bytes_per_launch, "ms_per_launch": gs_ms_per_launch,
+                "gs_share_of_step": prof["gs_ms"] / total_ms if total_ms else None}
+
+    # Plain FP64 GPU solver (cold start) on the same state.
+    plain = None
+    if args.plain_steps > 0:
+        pctx = _lib.Context(device=local, cache_mode=_lib.CACHE_NONE, precision=_lib.PRECISION_FP64, **solver_kw(s))
+        pctx.upload_ball2d(q_snap, v_snap, s["r"], s["m"], s["plane_x"], s["plane_n"])
+        pstream = torch.cuda.ExternalStream(pctx.stream_ptr(), device=local)
+        pms, pc = timed_steps(pctx, torch, pstream, args.plain_steps, flush)
+        pst = pctx.profile_read()
+        plain = {"value": sum(pc) / (sum(pms) / 1e3), "unit": UNIT, "steps": args.plain_steps,
+                 "ms_per_step": sum(pms) / len(pms), "gs_iterations_per_step": pst["contact_sweeps"] / max(sum(pc), 1)}
+        log("plain:", plain)
+        pctx.close()
+
+    # e2e through sg_flow with pinned host buffers.
+    e2e = None
+    if args.e2e_steps > 0:
+        ectx = _lib.Context(device=local, cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision,
+                            **solver_kw(s))
+        ectx.upload_ball2d(q_snap, v_snap, s["r"], s["m"], s["plane_x"], s["plane_n"])
+        bufs = [torch.empty(2 * nb, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+        bufs[0][:] = q_snap
+        bufs[1][:] = v_snap
+        it = 1
+        for _ in range(args.warmup):
+            ectx.flow(it, bufs[0], bufs[1], bufs[2], bufs[3])
+            bufs = [bufs[2], bufs[3], bufs[0], bufs[1]]
+            it += 1
+        torch.cuda.synchronize()
+        ec = 0
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            _, _, st = ectx.flow(it, bufs[0], bufs[1], bufs[2], bufs[3])
+            bufs = [bufs[2], bufs[3], bufs[0], bufs[1]]
+            ec += st["n_contacts"]
+            it += 1
+        el = time.perf_counter() - t0
+        e2e = {"value": ec / el, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * nb, "d2h_bytes_per_step": 2 * 16 * nb,
+               "steps": args.e2e_steps, "api": "sg_flow (ImpactFrictionMap::flow), pinned host q/v"}
+        log("e2e:", e2e)
+        ectx.close()
+
+    cpu = None
+    if rank == 0 and args.cpu_steps > 0:
+        v, desc, cores = cpu_sample(args, args.cpu_steps)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+        log("cpu:", cpu)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == 0 else "f32+f64",
+                "data": "synthetic (seeded dense-pile fill, no dataset)",
+                "config": {"workload": WORKLOAD, "discs": nb, "box": [40, 60], "dt": s["dt"], "mu": s["mu"],
+                           "CoR": s["CoR"], "tol": 1e-6, "max_iters": 5000, "form": "warm start (cache)",
+                           "preroll_steps": args.preroll, "timed_steps": [args.preroll + args.warmup + 1,
+                                                                           args.preroll + args.warmup + args.steps],
+                           "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1
+                           else "single GPU"},
+                "contacts_per_step": csteps / args.steps, "gs_iterations_per_step": prof["contact_sweeps"] / max(csteps, 1),
+                "plain_fp64_gpu": plain,
+                "warm_over_plain": (value / ws) / plain["value"] if plain else None,
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": prof["kernel_launches"]}
+        print(json.dumps(line), flush=True)
+    fast.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=262144)
+    ap.add_argument("--preroll", type=int, default=600)
+    ap.add_argument("--preroll-iters", type=int, default=50)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--precision", type=int, default=0, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -76,6 +76,12 @@ SG_API const char* sg_last_error_string(void);
 SG_API int sg_ctx_create(const sg_config* cfg, sg_ctx** out);
 SG_API void sg_ctx_destroy(sg_ctx* ctx);
 
+/* Replaces the solver settings (tol, max_iters, eval_every, cache mode, precision,
+ * mu, CoR, dt, gravity, integrator) of a context, keeping its scene and impulse cache
+ * (as rebuilding a GeometricImpactFrictionMap with new settings on the same
+ * Ball2DSim would).  cfg->device must equal the context's device. */
+SG_API int sg_ctx_reconfigure(sg_ctx* ctx, const sg_config* cfg);
+
 /* Uploads a Ball2D scene (replaces Ball2DState setup: ball2d/Ball2DState.cpp:40-77,
  * StaticPlane ctor ball2d/StaticGeometry/StaticPlane.cpp:10-19).
  * q, v: 2*nb interleaved; r, m: nb; plane_x, plane_n: 2*np (normals are normalised
@@ -139,6 +145,27 @@ SG_API int sg_broadphase_2d(sg_ctx* ctx, int32_t n, const double* aabb, int64_t 
 SG_API int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1a, const double* ra,
               const double* q0b, const double* q1b, const double* rb, double* coeffs, int32_t* hit,
               double* t);
+
+/* Counters of the work done since the last reset (no counterpart in SCISim, which has
+ * no timing instrumentation: scisim/Timer/TimeUtils.cpp only prints wall-clock strings).
+ * gs_ms sums the CUDA-event durations of the Gauss-Seidel kernel (recorded only while
+ * profiling is enabled); contact_sweeps / contact_evals count contact updates and
+ * residual evaluations; kernel_launches counts this library's kernel launches. */
+typedef struct {
+  double gs_ms;
+  uint64_t gs_launches;
+  uint64_t contact_sweeps;
+  uint64_t contact_evals;
+  uint64_t kernel_launches;
+  uint64_t steps;
+  uint64_t contacts;
+} sg_profile;
+
+SG_API int sg_profile_enable(sg_ctx* ctx, int32_t on);
+SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
+
+/* The context's CUDA stream (cudaStream_t) for stream-ordered timing by the caller. */
+SG_API int sg_ctx_stream(sg_ctx* ctx, void** stream);
 
 /* Sets the iteration limit of every device-side wait (grid barriers); 0 restores the
  * default (about a second).  Used to exercise the SG_DEVICE_TIMEOUT path. */

@@ -204,6 +204,8 @@ struct or_ball2d {
   // last step's contacts
   std::vector<int32_t> last_ia, last_ib;
   std::vector<double> last_n, last_alpha, last_beta;
+  // sweep order for the next step only (empty: sequential active-set order)
+  std::vector<int32_t> next_order;
 };
 
 namespace {
@@ -423,10 +425,12 @@ extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* s
   s->cache_bb.clear();
   s->cache_pb.clear();
   std::vector<double> v2(2 * nb), f(2 * nb);
-  or_gs_params gp{s->p.tol, s->p.max_iters, s->p.eval_every, nullptr};
+  or_gs_params gp{s->p.tol, s->p.max_iters, s->p.eval_every,
+                  int64_t(s->next_order.size()) == int64_t(nc) ? s->next_order.data() : nullptr};
   or_gs_result gr{};
   or_sobogus_solve_2d(nb, s->m.data(), s->v.data(), nc, ia.data(), ib.data(), bases.data(), CoR.data(), mu.data(),
                       &gp, alpha.data(), beta.data(), v2.data(), f.data(), &gr);
+  s->next_order.clear();
   // cacheImpulses (:222-264)
   if (s->p.cache_mode != OR_CACHE_NONE) {
     for (int k = 0; k < nc; ++k) {
@@ -466,4 +470,13 @@ extern "C" int or_ball2d_run(or_ball2d* s, uint32_t first_iteration, uint32_t n_
   if (stats) *stats = st;
   if (total_contacts) *total_contacts = tot;
   return bad;
+}
+
+extern "C" void or_ball2d_set_solver(or_ball2d* s, double tol, uint32_t max_iters) {
+  s->p.tol = tol;
+  s->p.max_iters = max_iters;
+}
+
+extern "C" void or_ball2d_set_next_order(or_ball2d* s, int64_t nc, const int32_t* order) {
+  s->next_order.assign(order, order + nc);
 }

@@ -335,11 +335,30 @@ extern "C" void or_local_solve(int dim, const double* W, const double* b, double
 }
 
 // ---------------------------------------------------------------------------
-// Ball2D Sobogus::solve.
+// Ball2D Sobogus::solve.  eval_only: set up from (alpha, beta) and return the
+// residual of that impulse without iterating.
+static double solve2d_impl(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
+                           const double* bases, const double* CoR, const double* mu, const or_gs_params* p,
+                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only);
+
 extern "C" void or_sobogus_solve_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
                                     const int32_t* ib, const double* bases, const double* CoR,
                                     const double* mu, const or_gs_params* p, double* alpha, double* beta,
                                     double* v2, double* f, or_gs_result* res) {
+  solve2d_impl(nb, m, v0, nc, ia, ib, bases, CoR, mu, p, alpha, beta, v2, f, res, false);
+}
+
+extern "C" double or_residual_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
+                                 const int32_t* ib, const double* bases, const double* CoR, const double* mu,
+                                 const double* alpha, const double* beta) {
+  std::vector<double> a(alpha, alpha + nc), b(beta, beta + nc);
+  return solve2d_impl(nb, m, v0, nc, ia, ib, bases, CoR, mu, nullptr, a.data(), b.data(), nullptr, nullptr, nullptr,
+                      true);
+}
+
+static double solve2d_impl(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
+                           const double* bases, const double* CoR, const double* mu, const or_gs_params* p,
+                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only) {
   // Minv as the reference builds it: 1.0 / m (ball2d/Ball2DState.cpp:55-67).
   std::vector<double> minv(nb);
   for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];
@@ -466,6 +485,7 @@ extern "C" void or_sobogus_solve_2d(int nb, const double* m, const double* v0, i
     return err;
   };
 
+  if (eval_only) return nc == 0 ? 0.0 : residual();
   const uint32_t eval_every = p->eval_every == 0 ? 1 : p->eval_every;
   std::vector<double> Rbest(R);
   double err_best = std::numeric_limits<double>::infinity();
@@ -548,4 +568,5 @@ extern "C" void or_sobogus_solve_2d(int nb, const double* m, const double* v0, i
   res->error = err_best;
   res->iterations = it;
   res->succeeded = err_best < p->tol ? 1 : 0;
+  return err_best;
 }

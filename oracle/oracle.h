@@ -70,6 +70,11 @@ void or_sobogus_solve_2d(int nb, const double* m, const double* v0, int nc, cons
                          const or_gs_params* p, double* alpha, double* beta, double* v2, double* f,
                          or_gs_result* res);
 
+// Coulomb residual (the solver's error function) of given impulses (alpha, beta).
+double or_residual_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
+                      const double* bases, const double* CoR, const double* mu, const double* alpha,
+                      const double* beta);
+
 // ---------------------------------------------------------------- Ball2D scene
 typedef struct or_ball2d or_ball2d;
 
@@ -109,6 +114,11 @@ int or_ball2d_run(or_ball2d* s, uint32_t first_iteration, uint32_t n_steps, or_s
                   int64_t* total_contacts);
 void or_ball2d_get_state(const or_ball2d* s, double* q, double* v);
 void or_ball2d_set_state(or_ball2d* s, const double* q, const double* v);
+// Sweep order for the next step's solve only (a permutation of its nc contacts, e.g.
+// the GPU's colour order); ignored if the contact count differs.
+void or_ball2d_set_next_order(or_ball2d* s, int64_t nc, const int32_t* order);
+// New solver tolerance and iteration cap (scene and impulse cache kept).
+void or_ball2d_set_solver(or_ball2d* s, double tol, uint32_t max_iters);
 // Contacts of the last step: ia, ib (ib=-1-plane_idx for planes), n (2 per contact), alpha, beta.
 int64_t or_ball2d_last_contacts(const or_ball2d* s, int64_t cap, int32_t* ia, int32_t* ib, double* n,
                                 double* alpha, double* beta);

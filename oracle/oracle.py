@@ -87,6 +87,10 @@ def lib():
         L.or_ball2d_active_set.restype = i64
         L.or_ball2d_active_set.argtypes = [C.c_void_p, _dp, _dp, i64, _ip, _ip]
         L.or_ball2d_umap.argtypes = [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp]
+        L.or_ball2d_set_next_order.argtypes = [C.c_void_p, C.c_int64, _ip]
+        L.or_ball2d_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_uint32]
+        L.or_residual_2d.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.or_residual_2d.restype = C.c_double
         _lib = L
     return _lib
 
@@ -183,6 +187,18 @@ def sobogus_solve_2d(m, v0, ia, ib, bases, CoR, mu, tol, max_iters, eval_every=1
                 succeeded=bool(gr.succeeded))
 
 
+def residual_2d(m, v0, ia, ib, bases, CoR, mu, alpha, beta):
+    """The solver's Coulomb residual of given impulses (alpha, beta)."""
+    m, v0, bases = f64(m), f64(v0), f64(bases)
+    ia, ib = i32(ia), i32(ib)
+    nc = ia.shape[0]
+    CoR = f64(np.broadcast_to(CoR, (nc,)))
+    mu = f64(np.broadcast_to(mu, (nc,)))
+    a, b = f64(alpha), f64(beta)
+    return lib().or_residual_2d(m.shape[0], _d(m), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(CoR), _d(mu),
+                                _d(a), _d(b))
+
+
 class Ball2D:
     """Ball2D system stepped by GeometricImpactFrictionMap + Sobogus (CPU oracle)."""
 
@@ -231,6 +247,14 @@ class Ball2D:
     def set_state(self, q, v):
         q, v = f64(q), f64(v)
         lib().or_ball2d_set_state(self._h, _d(q), _d(v))
+
+    def set_solver(self, tol, max_iters):
+        lib().or_ball2d_set_solver(self._h, tol, max_iters)
+
+    def set_next_order(self, order):
+        """Sweep order for the next step's solve (e.g. the GPU's colour order)."""
+        order = i32(order)
+        lib().or_ball2d_set_next_order(self._h, order.shape[0], _i(order))
 
     def last_contacts(self):
         L = lib()

@@ -41,6 +41,12 @@ class SgStepStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class SgProfile(C.Structure):
+    _fields_ = [("gs_ms", C.c_double), ("gs_launches", C.c_uint64), ("contact_sweeps", C.c_uint64),
+                ("contact_evals", C.c_uint64), ("kernel_launches", C.c_uint64), ("steps", C.c_uint64),
+                ("contacts", C.c_uint64)]
+
+
 class SgError(RuntimeError):
     def __init__(self, status, where):
         self.status = status
@@ -53,6 +59,7 @@ SIGNATURES = {
     "sg_last_error_string": (C.c_char_p, []),
     "sg_ctx_create": (C.c_int, [C.POINTER(SgConfig), C.POINTER(C.c_void_p)]),
     "sg_ctx_destroy": (None, [C.c_void_p]),
+    "sg_ctx_reconfigure": (C.c_int, [C.c_void_p, C.POINTER(SgConfig)]),
     "sg_ball2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
     "sg_step": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SgStepStats), C.POINTER(_i64)]),
     "sg_flow": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp, C.POINTER(SgStepStats)]),
@@ -64,6 +71,9 @@ SIGNATURES = {
                                       C.POINTER(C.c_uint32)]),
     "sg_broadphase_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _i64, _ip, C.POINTER(_i64)]),
     "sg_ccd_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp]),
+    "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "sg_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sg_set_spin_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sg_selftest_wait_timeout": (C.c_int, [C.c_void_p]),
 }
@@ -125,6 +135,18 @@ class Context:
     @property
     def handle(self):
         return self._h
+
+    def reconfigure(self, **changes):
+        """New solver settings on the same scene and impulse cache."""
+        c = self.config
+        fields = {k: getattr(c, k) for k, _ in SgConfig._fields_}
+        fields["gravity"] = tuple(c.gravity)
+        fields.update(changes)
+        cfg = SgConfig(fields["integrator"], fields["cache_mode"], fields["precision"], fields["device"],
+                       fields["dt"], (C.c_double * 2)(*fields["gravity"]), fields["mu"], fields["CoR"],
+                       fields["tol"], fields["max_iters"], fields["eval_every"])
+        check(lib().sg_ctx_reconfigure(self._h, C.byref(cfg)), "sg_ctx_reconfigure")
+        self.config = cfg
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -192,6 +214,19 @@ class Context:
         ncol = C.c_int32(0)
         L.sg_last_solve_order(self._h, nc, iptr(order), iptr(offs), C.byref(ncol))
         return order, offs[: ncol.value + 1].copy()
+
+    def profile_enable(self, on=True):
+        check(lib().sg_profile_enable(self._h, 1 if on else 0), "sg_profile_enable")
+
+    def profile_read(self, reset=False):
+        p = SgProfile()
+        check(lib().sg_profile_read(self._h, C.byref(p), 1 if reset else 0), "sg_profile_read")
+        return {k: getattr(p, k) for k, _ in p._fields_}
+
+    def stream_ptr(self):
+        s = C.c_void_p()
+        check(lib().sg_ctx_stream(self._h, C.byref(s)), "sg_ctx_stream")
+        return s.value or 0
 
     def set_spin_limit(self, spins):
         check(lib().sg_set_spin_limit(self._h, spins), "sg_set_spin_limit")

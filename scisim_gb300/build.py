@@ -2,9 +2,10 @@
 
 Each translation unit under csrc/ is compiled by nvcc in parallel, then linked
 into scisim_gb300/libscisim_gb300.so with the static CUDA runtime, so the library
-has no run-time dependency beyond the driver.  FP contraction is off
-(-fmad=false): the FP64 contact path reproduces the reference's separately
-rounded operations bit for bit.
+has no run-time dependency beyond the driver.  FP contraction is off in device
+code (-fmad=false) and in host code (-ffp-contract=off; GCC on aarch64 contracts
+by default): the FP64 contact path reproduces the reference's separately rounded
+operations bit for bit.
 """
 from __future__ import annotations
 
@@ -19,7 +20,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libscisim_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler",
+              "-fPIC,-fvisibility=hidden,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

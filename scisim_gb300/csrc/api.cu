@@ -87,6 +87,11 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   SG_CUDA_TRY(cudaStreamSynchronize(s));
   const int npairs = totals[0], nplanes = totals[1];
   const int nc = npairs + nplanes;
+  // predictor 1, grid 8 (bounds init/reduce/setup, count, 3-kernel scan, scatter),
+  // pair count + scan 4, plane flags + scan 4
+  ctx->kernel_launches += 1 + 8 + 4 + (ctx->np > 0 ? 4 : 0);
+  ctx->steps += 1;
+  ctx->contacts_total += (uint64_t)nc;
   st.n_contacts = nc;
   st.n_ball_ball = npairs;
   st.n_ball_plane = nplanes;
@@ -141,6 +146,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   }
   // Final map with the post-impact velocity (:441).
   if (int r = ball2d_final_map(ctx, ctx->v2.as<double>())) return r;
+  ctx->kernel_launches += 2 + (ctx->np > 0 ? 1 : 0) + 1 + 1;  // write pairs, assemble, plane write, extract, final map
   std::swap(ctx->q, ctx->q1);
   std::swap(ctx->v, ctx->v1);
   if (out) *out = st;
@@ -197,8 +203,19 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                  &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2};
   for (Buf* b : bufs) release(*b);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx->ev_gs0) cudaEventDestroy(ctx->ev_gs0);
+  if (ctx->ev_gs1) cudaEventDestroy(ctx->ev_gs1);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+
+int sg_ctx_reconfigure(sg_ctx* ctx, const sg_config* cfg) {
+  if (!ctx || validate_config(cfg) != SG_OK || cfg->device != ctx->device) {
+    set_error("sg_ctx_reconfigure: invalid sg_config");
+    return SG_BAD_INPUT;
+  }
+  ctx->cfg = *cfg;
+  return SG_OK;
 }
 
 int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
@@ -526,6 +543,40 @@ int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1a, cons
   }
   for (auto& x : b) release(x);
   return rc;
+}
+
+int sg_ctx_stream(sg_ctx* ctx, void** stream) {
+  if (!ctx || !stream) return SG_BAD_INPUT;
+  *stream = (void*)ctx->stream;
+  return SG_OK;
+}
+
+int sg_profile_enable(sg_ctx* ctx, int32_t on) {
+  if (!ctx) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  if (on && !ctx->ev_gs0) {
+    SG_CUDA_TRY(cudaEventCreate(&ctx->ev_gs0));
+    SG_CUDA_TRY(cudaEventCreate(&ctx->ev_gs1));
+  }
+  ctx->profile = on != 0;
+  return SG_OK;
+}
+
+int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset) {
+  if (!ctx || !out) return SG_BAD_INPUT;
+  out->gs_ms = ctx->gs_ms;
+  out->gs_launches = ctx->gs_launches;
+  out->contact_sweeps = ctx->contact_sweeps;
+  out->contact_evals = ctx->contact_evals;
+  out->kernel_launches = ctx->kernel_launches;
+  out->steps = ctx->steps;
+  out->contacts = ctx->contacts_total;
+  if (reset) {
+    ctx->gs_ms = 0.0;
+    ctx->gs_launches = ctx->contact_sweeps = ctx->contact_evals = ctx->kernel_launches = 0;
+    ctx->steps = ctx->contacts_total = 0;
+  }
+  return SG_OK;
 }
 
 int sg_set_spin_limit(sg_ctx* ctx, uint64_t spins) {

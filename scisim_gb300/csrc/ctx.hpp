@@ -107,6 +107,13 @@ struct sg_ctx {
   int64_t last_nc = 0, last_nbb = 0;
   sg::SolveStats h_stats{};
 
+  // profiling counters (sg_profile_read)
+  bool profile = false;
+  cudaEvent_t ev_gs0 = nullptr, ev_gs1 = nullptr;
+  double gs_ms = 0.0;
+  uint64_t gs_launches = 0, contact_sweeps = 0, contact_evals = 0, kernel_launches = 0, steps = 0;
+  uint64_t contacts_total = 0;
+
   // pinned staging
   void* pinned = nullptr;
   size_t pinned_bytes = 0;

@@ -333,7 +333,7 @@ __global__ void k_color_jp(ColorArgs A) {
   }
   for (int k = tid; k < A.nc; k += nthr) {
     const int c = vcolor[k] & 63;
-    A.perm[A.st->color_off[c] + atomicAdd(&A.st->color_fill[c], 1)] = k;
+    A.perm[*((volatile int*)&A.st->color_off[c]) + atomicAdd(&A.st->color_fill[c], 1)] = k;
   }
 }
 
@@ -363,12 +363,14 @@ struct GsArgs {
 __device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
   const int a = A.ia[k], b = A.ib[k];
   const double2 nk = A.n[k], ck = A.c[k];
-  const double2 va = A.v[a];
+  // Velocities and impulses are written by other SMs between grid barriers: read
+  // them at L2 (ld.global.cg) so a stale L1 line is never used.
+  const double2 va = __ldcg(&A.v[a]);
   const bool has_b = b >= 0;
-  const double2 vb = has_b ? A.v[b] : make_double2(0.0, 0.0);
+  const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
   double u0, u1;
   local_velocity(nk, ck, va, has_b, vb, u0, u1);
-  const double2 rk = A.r[k];
+  const double2 rk = __ldcg(&A.r[k]);
   const double r0 = rk.x, r1 = rk.y;
   const double w00 = A.W[3 * k], w01 = A.W[3 * k + 1], w11 = A.W[3 * k + 2];
   const double bt0 = u0 - (w00 * r0 + w01 * r1);
@@ -420,11 +422,11 @@ __global__ void __launch_bounds__(kBlock) k_gs(GsArgs A) {
       for (int k = tid; k < A.nc; k += nthr) {
         const int a = A.ia[k], b = A.ib[k];
         const bool has_b = b >= 0;
-        const double2 va = A.v[a];
-        const double2 vb = has_b ? A.v[b] : make_double2(0.0, 0.0);
+        const double2 va = __ldcg(&A.v[a]);
+        const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
         double u0, u1;
         local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
-        const double2 rk = A.r[k];
+        const double2 rk = __ldcg(&A.r[k]);
         cand[k] = rk;
         emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
       }
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(kBlock) k_gs(GsArgs A) {
   if (!converged) {
     // Return the best iterate (GaussSeidel: x = x_best when GSIter > maxIters).
     if (err_best < INFINITY)
-      for (int k = tid; k < A.nc; k += nthr) A.r[k] = best[k];
+      for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
     it = A.max_iters;
   }
   if (tid == 0) {
@@ -569,9 +571,13 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     {
       void* args[] = {&GA};
       const int g = coop_grid(ctx, k_gs, nc);
+      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
       SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kBlock), args, 0, s));
+      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
     }
+    ctx->kernel_launches += 6;  // body_count, body_fill, body_sort, color, gs (+ scan below)
   }
+  ctx->kernel_launches += 2 + (nb > 0 ? 3 : 0);  // vel_init, final_velocity, scan
   k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                      P.m, P.minv, reinterpret_cast<double2*>(P.v2));
   SG_CUDA_TRY(cudaGetLastError());
@@ -581,6 +587,17 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     ctx->h_stats.iterations = 0;
     ctx->h_stats.converged = 1;
     ctx->h_stats.error = 0.0;
+  } else if (ctx->h_stats.status == 0) {
+    const uint64_t its = ctx->h_stats.iterations;
+    const uint64_t ee = sp.eval_every ? sp.eval_every : 1;
+    ctx->gs_launches += 1;
+    ctx->contact_sweeps += its * (uint64_t)nc;
+    ctx->contact_evals += (its / ee + (ctx->h_stats.converged && its % ee ? 1 : 0)) * (uint64_t)nc;
+    if (ctx->profile) {
+      float ms = 0.f;
+      SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
+      ctx->gs_ms += ms;
+    }
   }
   if (ctx->h_stats.status == SG_DEVICE_TIMEOUT) {
     set_error("a device-side wait exceeded its spin limit");
