@@ -133,6 +133,26 @@ SG_API int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const d
                         double* alpha, double* beta, double* v2, double* f, double* error,
                         uint32_t* iterations);
 
+/* The FrictionSolver solve above for callers that cannot allocate GPU memory: code
+ * that runs inside another runtime's memory pool, in a real-time loop, or under a
+ * policy that forbids device allocation after start-up.  It has no counterpart in the
+ * reference.  Every array argument is a DEVICE pointer the caller owns (same meanings
+ * and layouts as sg_sobogus_solve_2d); error and iterations are host pointers; stream
+ * is a cudaStream_t (NULL = default stream).  No context is needed and nothing is
+ * allocated: all scratch lives in one fixed static device array of about 8.1 MB that
+ * every GPU loading the library keeps until the process exits.  Limits: at most
+ * 16,384 bodies and 65,536 contacts; larger problems return SG_CAPACITY.  The first
+ * call on a device looks up that array's device address (cudaGetSymbolAddress), so
+ * make the first call on each device before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller.  Returns as sg_sobogus_solve_2d; invalid contact
+ * indices or tangents give SG_BAD_INPUT before any solve work. */
+SG_API int sg_sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int32_t nc,
+                                       const int32_t* ia, const int32_t* ib, const double* bases,
+                                       const double* CoR, const double* mu, uint32_t max_iters, double tol,
+                                       uint32_t eval_every, double* alpha, double* beta, double* v2, double* f,
+                                       void* stream, double* error, uint32_t* iterations);
+
 /* SpatialGridDetector::getPotentialOverlaps (ball2d/SpatialGridDetector.cpp:106-133):
  * all overlapping pairs (i<j) of n AABBs [minx miny maxx maxy], in lexicographic
  * order.  Returns SG_CAPACITY with *npairs = required count if cap is too small. */

@@ -69,6 +69,10 @@ SIGNATURES = {
     "sg_sobogus_solve_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, C.c_int32, _ip, _ip, _dp, _dp, _dp,
                                       C.c_uint32, C.c_double, C.c_uint32, _dp, _dp, _dp, _dp, _dp,
                                       C.POINTER(C.c_uint32)]),
+    "sg_sobogus_solve_2d_noalloc": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_double,
+                                              C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint32)]),
     "sg_broadphase_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _i64, _ip, C.POINTER(_i64)]),
     "sg_ccd_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp]),
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),

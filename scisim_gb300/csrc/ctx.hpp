@@ -123,6 +123,8 @@ namespace sg {
 
 // Stage launchers (kernels in ball2d_kernels.cu / solver_kernels.cu / scan.cu).
 int scan_exclusive(sg_ctx* ctx, const int* in, int* out, int n);  // out[0..n], out[n] = total
+int scan_tile_count(int n);
+int scan_exclusive_raw(const int* in, int* out, int n, int* tiles, cudaStream_t stream);
 
 int ball2d_predict_and_bounds(sg_ctx* ctx);
 int broadphase_build_grid(sg_ctx* ctx, const double* aabb, int n);

@@ -115,4 +115,21 @@ int scan_exclusive(sg_ctx* ctx, const int* in, int* out, int n) {
   return SG_OK;
 }
 
+// The same scan with a caller-provided tile buffer of scan_tile_count(n) + 1 ints
+// (no allocation).
+int scan_tile_count(int n) { return n <= 0 ? 0 : (n + kTile - 1) / kTile; }
+
+int scan_exclusive_raw(const int* in, int* out, int n, int* tiles, cudaStream_t stream) {
+  const int ntiles = scan_tile_count(n);
+  if (n <= 0) {
+    SG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(int), stream));
+    return SG_OK;
+  }
+  k_tile_reduce<<<ntiles, kThreads, 0, stream>>>(in, n, tiles);
+  k_scan_tile_sums<<<1, kThreads, 0, stream>>>(tiles, ntiles, out + n);
+  k_tile_scan<<<ntiles, kThreads, 0, stream>>>(in, n, tiles, out);
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
 }  // namespace sg

@@ -624,4 +624,296 @@ int wait_timeout_selftest(sg_ctx* ctx) {
   return status;
 }
 
+// ===========================================================================
+// Allocation-free FrictionSolver entry (sg_sobogus_solve_2d_noalloc).
+//
+// For callers that cannot call cudaMalloc -- code running where the device
+// allocator must not be touched (inside another runtime's memory pool or a
+// real-time loop, or under a policy that forbids allocation after start-up) -- the
+// whole solve runs on the caller's device buffers plus one fixed scratch array
+// declared at file scope below.  Every GPU that loads the library holds the array
+// (kNoAllocScratchBytes, about 8.1 MB) until the process exits.  It bounds the
+// problem size to kNoAllocMaxBodies bodies and kNoAllocMaxContacts contacts.
+namespace {
+
+constexpr int kNoAllocMaxBodies = 16384;
+constexpr int kNoAllocMaxContacts = 65536;
+constexpr size_t na_align(size_t x) { return (x + 255) & ~size_t(255); }
+// Scratch layout (byte offsets, each region 256-byte aligned).
+constexpr size_t kNaStats = 0;
+constexpr size_t kNaBarrier = na_align(kNaStats + sizeof(SolveStats));
+constexpr size_t kNaFlag = na_align(kNaBarrier + sizeof(GridBarrier));
+constexpr size_t kNaCnt = na_align(kNaFlag + sizeof(int));
+constexpr size_t kNaOff = na_align(kNaCnt + sizeof(int) * (kNoAllocMaxBodies + 1));
+constexpr size_t kNaFill = na_align(kNaOff + sizeof(int) * (kNoAllocMaxBodies + 1));
+constexpr size_t kNaTiles = na_align(kNaFill + sizeof(int) * (kNoAllocMaxBodies + 1));
+constexpr size_t kNaMinv = na_align(kNaTiles + sizeof(int) * 64);
+constexpr size_t kNaVrun = na_align(kNaMinv + sizeof(double) * kNoAllocMaxBodies);
+constexpr size_t kNaAdj = na_align(kNaVrun + sizeof(double2) * kNoAllocMaxBodies);
+constexpr size_t kNaColor = na_align(kNaAdj + sizeof(int) * 2 * kNoAllocMaxContacts);
+constexpr size_t kNaPerm = na_align(kNaColor + sizeof(int) * kNoAllocMaxContacts);
+constexpr size_t kNaN = na_align(kNaPerm + sizeof(int) * kNoAllocMaxContacts);
+constexpr size_t kNaC = na_align(kNaN + sizeof(double2) * kNoAllocMaxContacts);
+constexpr size_t kNaW = na_align(kNaC + sizeof(double2) * kNoAllocMaxContacts);
+constexpr size_t kNaR = na_align(kNaW + sizeof(double) * 3 * kNoAllocMaxContacts);
+constexpr size_t kNaRa = na_align(kNaR + sizeof(double2) * kNoAllocMaxContacts);
+constexpr size_t kNaRb = na_align(kNaRa + sizeof(double2) * kNoAllocMaxContacts);
+constexpr size_t kNoAllocScratchBytes = na_align(kNaRb + sizeof(double2) * kNoAllocMaxContacts);
+static_assert(kNoAllocScratchBytes < 9u * 1024u * 1024u, "scratch must stay modest");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device ordinal, looked up once per device.
+constexpr int kNaMaxDevices = 64;
+unsigned char* g_na_addr[kNaMaxDevices] = {};
+
+int na_scratch_address(unsigned char** out) {
+  int dev = -1;
+  SG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNaMaxDevices) {
+    set_error("sg_sobogus_solve_2d_noalloc: device ordinal beyond 63");
+    return SG_BAD_INPUT;
+  }
+  if (!g_na_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") + cudaGetErrorString(e));
+      return SG_CUDA_ERROR;
+    }
+    g_na_addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_na_addr[dev];
+  return SG_OK;
+}
+
+__global__ void k_na_minv(int nb, const double* __restrict__ m, double* __restrict__ minv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nb) minv[i] = 1.0 / m[i];
+}
+
+// Per-contact assembly of sg_sobogus_solve_2d, on the device, with the same
+// operation order; invalid contacts raise *flag and touch nothing else.
+__global__ void k_na_assemble(int nb, int nc, const double* __restrict__ minv, const double2* __restrict__ v0,
+                              const int* __restrict__ ia, const int* __restrict__ ib, const double* __restrict__ bases,
+                              const double* __restrict__ CoR, const double* __restrict__ alpha,
+                              const double* __restrict__ beta, double2* __restrict__ n, double2* __restrict__ c,
+                              double* __restrict__ W, double2* __restrict__ r, int* flag) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int a = ia[k], b = ib[k];
+  const double nx = bases[4 * k], ny = bases[4 * k + 1], tx = bases[4 * k + 2], ty = bases[4 * k + 3];
+  if (a < 0 || a >= nb || b < -1 || b >= nb || b == a || tx != -ny || ty != nx) {
+    atomicExch(flag, 1);
+    return;
+  }
+  const double2 va = v0[a];
+  double vrx = va.x, vry = va.y;
+  if (b >= 0) {
+    const double2 vb = v0[b];
+    vrx = vrx - vb.x;
+    vry = vry - vb.y;
+  } else {
+    vrx = vrx - 0.0;
+    vry = vry - 0.0;
+  }
+  const double ndotv = nx * vrx + ny * vry;
+  const double nrel = -(0.0 * nx + 0.0 * ny);
+  const double drel = -(0.0 * tx + 0.0 * ty);
+  const double sc = CoR[k] * ndotv + nrel;
+  const double wx = (0.0 + nx * sc) + tx * drel;
+  const double wy = (0.0 + ny * sc) + ty * drel;
+  n[k] = make_double2(nx, ny);
+  c[k] = make_double2(nx * wx + ny * wy, tx * wx + ty * wy);
+  const double nn = nx * nx + ny * ny, nt = nx * tx + ny * ty, tt = tx * tx + ty * ty;
+  double w00 = minv[a] * nn, w01 = minv[a] * nt, w11 = minv[a] * tt;
+  if (b >= 0) {
+    w00 = w00 + minv[b] * nn;
+    w01 = w01 + minv[b] * nt;
+    w11 = w11 + minv[b] * tt;
+  }
+  W[3 * k] = w00;
+  W[3 * k + 1] = w01;
+  W[3 * k + 2] = w11;
+  const double rwx = alpha[k] * nx + beta[k] * tx;
+  const double rwy = alpha[k] * ny + beta[k] * ty;
+  r[k] = make_double2(nx * rwx + ny * rwy, tx * rwx + ty * rwy);
+}
+
+__global__ void k_na_extract(int nc, const double2* __restrict__ n, const double2* __restrict__ r,
+                             const double* __restrict__ mu, double* __restrict__ alpha, double* __restrict__ beta) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const double2 nk = n[k], rk = r[k];
+  const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  const double rwx = nx * rk.x + tx * rk.y;
+  const double rwy = ny * rk.x + ty * rk.y;
+  alpha[k] = rwx * nx + rwy * ny;
+  beta[k] = (mu[k] == 0.0) ? 0.0 : (rwx * tx + rwy * ty);
+}
+
+// Friction force per body, summed over its contacts in ascending contact order.
+__global__ void k_na_force(int nb, const int* __restrict__ off, const int* __restrict__ adj, const int* __restrict__ ia,
+                           const double2* __restrict__ n, const double* __restrict__ beta, double2* __restrict__ f) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  double fx = 0.0, fy = 0.0;
+  const int e = off[i + 1];
+  for (int p = off[i]; p < e; ++p) {
+    const int k = adj[p];
+    const double2 nk = n[k];
+    const double f0x = beta[k] * -nk.y, f0y = beta[k] * nk.x;
+    if (ia[k] == i) {
+      fx += f0x;
+      fy += f0y;
+    } else {
+      fx -= f0x;
+      fy -= f0y;
+    }
+  }
+  f[i] = make_double2(fx, fy);
+}
+
+}  // namespace
+
+int sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int32_t nc, const int32_t* ia,
+                             const int32_t* ib, const double* bases, const double* CoR, const double* mu,
+                             uint32_t max_iters, double tol, uint32_t eval_every, double* alpha, double* beta,
+                             double* v2, double* f, void* stream, double* error, uint32_t* iterations) {
+  if (nb < 0 || nc < 0 || (nb > 0 && (!m || !v0 || !v2 || !f)) ||
+      (nc > 0 && (!ia || !ib || !bases || !CoR || !mu || !alpha || !beta)) || !(tol >= 0.0)) {
+    set_error("sg_sobogus_solve_2d_noalloc: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  if (nb > kNoAllocMaxBodies || nc > kNoAllocMaxContacts) {
+    set_error("sg_sobogus_solve_2d_noalloc: " + std::to_string(nb) + " bodies / " + std::to_string(nc) +
+              " contacts exceed the fixed scratch limits of " + std::to_string(kNoAllocMaxBodies) + " bodies and " +
+              std::to_string(kNoAllocMaxContacts) + " contacts");
+    return SG_CAPACITY;
+  }
+  unsigned char* base = nullptr;
+  if (int r = na_scratch_address(&base)) return r;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  SolveStats* st = reinterpret_cast<SolveStats*>(base + kNaStats);
+  GridBarrier* gb = reinterpret_cast<GridBarrier*>(base + kNaBarrier);
+  int* flag = reinterpret_cast<int*>(base + kNaFlag);
+  int* cnt = reinterpret_cast<int*>(base + kNaCnt);
+  int* off = reinterpret_cast<int*>(base + kNaOff);
+  int* fill = reinterpret_cast<int*>(base + kNaFill);
+  int* tiles = reinterpret_cast<int*>(base + kNaTiles);
+  double* minv = reinterpret_cast<double*>(base + kNaMinv);
+  double2* vrun = reinterpret_cast<double2*>(base + kNaVrun);
+  int* adj = reinterpret_cast<int*>(base + kNaAdj);
+  int* color = reinterpret_cast<int*>(base + kNaColor);
+  int* perm = reinterpret_cast<int*>(base + kNaPerm);
+  double2* n2 = reinterpret_cast<double2*>(base + kNaN);
+  double2* c2 = reinterpret_cast<double2*>(base + kNaC);
+  double* W = reinterpret_cast<double*>(base + kNaW);
+  double2* r2 = reinterpret_cast<double2*>(base + kNaR);
+  double2* ra = reinterpret_cast<double2*>(base + kNaRa);
+  double2* rb = reinterpret_cast<double2*>(base + kNaRb);
+
+  // The array keeps the previous call's contents: clear what must start at zero.
+  SG_CUDA_TRY(cudaMemsetAsync(base, 0, kNaCnt, s));  // stats, barrier, flag
+  SG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)(nb + 1), s));
+  SG_CUDA_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * (size_t)(nb + 1), s));
+  if (nb > 0) k_na_minv<<<blocks_for(nb), kBlock, 0, s>>>(nb, m, minv);
+  if (nc > 0) {
+    k_na_assemble<<<blocks_for(nc), kBlock, 0, s>>>(nb, nc, minv, reinterpret_cast<const double2*>(v0), ia, ib, bases,
+                                                    CoR, alpha, beta, n2, c2, W, r2, flag);
+    SG_CUDA_TRY(cudaGetLastError());
+    int h_flag = 0;
+    SG_CUDA_TRY(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_flag) {
+      set_error("sg_sobogus_solve_2d_noalloc: contact body index out of range or tangent not (-n_y, n_x)");
+      return SG_BAD_INPUT;
+    }
+    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, cnt);
+  }
+  if (int r = scan_exclusive_raw(cnt, off, nb, tiles, s)) return r;
+  if (nc > 0) {
+    k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, off, fill, adj);
+    k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
+  }
+  if (nb > 0)
+    k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, ia, n2, r2, reinterpret_cast<const double2*>(v0), minv,
+                                                 vrun);
+  SG_CUDA_TRY(cudaGetLastError());
+  int dev = 0, sms = 0;
+  SG_CUDA_TRY(cudaGetDevice(&dev));
+  SG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  auto grid_for = [&](auto kernel) {
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kBlock, 0) != cudaSuccess || bps < 1) bps = 1;
+    const long need = std::max(1L, ((long)nc + kBlock - 1) / kBlock);
+    return (int)std::min((long)bps * sms, need);
+  };
+  const unsigned long long spin = 1ull << 25;
+  if (nc > 0) {
+    SG_CUDA_TRY(cudaMemsetAsync(color, 0xff, sizeof(int) * (size_t)nc, s));
+    ColorArgs CA{nc, ia, ib, off, adj, color, perm, st, gb, spin, 4096};
+    void* cargs[] = {&CA};
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_color_jp, dim3(grid_for(k_color_jp)), dim3(kBlock), cargs, 0, s));
+    SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+    GsArgs GA;
+    GA.nc = nc;
+    GA.ia = ia;
+    GA.ib = ib;
+    GA.n = n2;
+    GA.c = c2;
+    GA.W = W;
+    GA.mu = mu;
+    GA.minv = minv;
+    GA.perm = perm;
+    GA.r = r2;
+    GA.r_a = ra;
+    GA.r_b = rb;
+    GA.v = vrun;
+    GA.st = st;
+    GA.gb = gb;
+    GA.spin = spin;
+    GA.tol = tol;
+    GA.max_iters = max_iters;
+    GA.eval_every = eval_every;
+    void* gargs[] = {&GA};
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(grid_for(k_gs)), dim3(kBlock), gargs, 0, s));
+  }
+  if (nb > 0)
+    k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, ia, n2, r2, reinterpret_cast<const double2*>(v0),
+                                                       m, minv, reinterpret_cast<double2*>(v2));
+  if (nc > 0) k_na_extract<<<blocks_for(nc), kBlock, 0, s>>>(nc, n2, r2, mu, alpha, beta);
+  if (nb > 0)
+    k_na_force<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, ia, n2, beta, reinterpret_cast<double2*>(f));
+  SG_CUDA_TRY(cudaGetLastError());
+  SolveStats h{};
+  SG_CUDA_TRY(cudaMemcpyAsync(&h, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (nc == 0) {
+    h.iterations = 0;
+    h.converged = 1;
+    h.error = 0.0;
+  }
+  if (error) *error = h.error;
+  if (iterations) *iterations = h.iterations;
+  if (h.status == SG_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its spin limit");
+    return SG_DEVICE_TIMEOUT;
+  }
+  if (h.status == SG_CAPACITY) {
+    set_error("contact colouring exceeded 64 colours or its round limit");
+    return SG_CAPACITY;
+  }
+  return h.converged ? SG_OK : SG_NOT_CONVERGED;
+}
+
 }  // namespace sg
+
+extern "C" int sg_sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int32_t nc,
+                                           const int32_t* ia, const int32_t* ib, const double* bases,
+                                           const double* CoR, const double* mu, uint32_t max_iters, double tol,
+                                           uint32_t eval_every, double* alpha, double* beta, double* v2, double* f,
+                                           void* stream, double* error, uint32_t* iterations) {
+  return sg::sobogus_solve_2d_noalloc(nb, m, v0, nc, ia, ib, bases, CoR, mu, max_iters, tol, eval_every, alpha, beta,
+                                      v2, f, stream, error, iterations);
+}
