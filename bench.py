@@ -44,8 +44,21 @@ WORKLOAD = "ball2d_dense_pile_262144"
 # Algorithmic bytes of the Gauss-Seidel kernel (FP64), per contact:
 #   update: perm 4, ia 4, ib 4, n 16, c 16, W 24, mu 8, r 16+16, minv 2x8, v_a 16+16, v_b 16+16
 #   residual: ia 4, ib 4, v_a 16, v_b 16, n 16, c 16, r 16, snapshot 16, mu 8
+#   FP32 sweep: (ia, ib) 8, n 8, c 8, (w00, w01, w11, mu) 16, r 8+8, minv 2x4, v_a 8+8, v_b 8+8
+#   FP32 -> FP64 lift: per contact perm 4, r32 8, r64 16 w, two adjacency visits x (adj 4, ia 4,
+#   n 16, r 16); per body v0 16, minv 8, v 16 w
 BYTES_PER_CONTACT_SWEEP = 188
+BYTES_PER_CONTACT_SWEEP32 = 96
 BYTES_PER_CONTACT_EVAL = 112
+BYTES_PER_CONTACT_LIFT = 108
+BYTES_PER_BODY_LIFT = 40
+
+
+def gs_bytes(prof):
+    """Algorithmic bytes moved by the Gauss-Seidel kernel(s) counted in a profile."""
+    return (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP + prof["contact_sweeps32"] * BYTES_PER_CONTACT_SWEEP32 +
+            prof["contact_evals"] * BYTES_PER_CONTACT_EVAL + prof["contact_lifts"] * BYTES_PER_CONTACT_LIFT +
+            prof["body_lifts"] * BYTES_PER_BODY_LIFT)
 
 
 def log(*a):
@@ -247,15 +260,14 @@ def run_ours(args):
     # launch over its CUDA-event duration.
     hbm, peak_kind = peaks()
     gl = max(prof["gs_launches"], 1)
-    bytes_per_launch = (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP +
-                        prof["contact_evals"] * BYTES_PER_CONTACT_EVAL) / gl
+    bytes_per_launch = gs_bytes(prof) / gl
     gs_ms_per_launch = prof["gs_ms"] / gl
     achieved = bytes_per_launch / (gs_ms_per_launch / 1e3) / 1e9 if gs_ms_per_launch > 0 else 0.0
     traffic = None
     tp = os.path.join(HERE, "profiles", "gs_dram_bytes_per_contact_sweep.json")
     if os.path.exists(tp):
         d = json.load(open(tp))
-        traffic = d["bytes_per_contact_sweep"] * (prof["contact_sweeps"] + prof["contact_evals"]) / gl
+        traffic = d["dram_bytes_per_algorithmic_byte"] * bytes_per_launch
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                 "kernel": "k_gs (cooperative coloured block Gauss-Seidel)",
@@ -271,7 +283,8 @@ def run_ours(args):
         pms, pc = timed_steps(pctx, torch, pstream, args.plain_steps, flush)
         pst = pctx.profile_read()
         plain = {"value": sum(pc) / (sum(pms) / 1e3), "unit": UNIT, "steps": args.plain_steps,
-                 "ms_per_step": sum(pms) / len(pms), "gs_iterations_per_step": pst["contact_sweeps"] / max(sum(pc), 1)}
+                 "ms_per_step": sum(pms) / len(pms),
+                 "gs_iterations_per_step": (pst["contact_sweeps"] + pst["contact_sweeps32"]) / max(sum(pc), 1)}
         log("plain:", plain)
         pctx.close()
 
@@ -320,7 +333,9 @@ def run_ours(args):
                                                                            args.preroll + args.warmup + args.steps],
                            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1
                            else "single GPU"},
-                "contacts_per_step": csteps / args.steps, "gs_iterations_per_step": prof["contact_sweeps"] / max(csteps, 1),
+                "contacts_per_step": csteps / args.steps,
+                "gs_iterations_per_step": (prof["contact_sweeps"] + prof["contact_sweeps32"]) / max(csteps, 1),
+                "fp32_sweep_share": prof["contact_sweeps32"] / max(prof["contact_sweeps"] + prof["contact_sweeps32"], 1),
                 "plain_fp64_gpu": plain,
                 "warm_over_plain": (value / ws) / plain["value"] if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
@@ -344,7 +359,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=10)
-    ap.add_argument("--precision", type=int, default=0, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
+    ap.add_argument("--precision", type=int, default=1, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

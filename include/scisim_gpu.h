@@ -179,6 +179,9 @@ typedef struct {
   uint64_t kernel_launches;
   uint64_t steps;
   uint64_t contacts;
+  uint64_t contact_sweeps32; /* contact updates in FP32 sweeps (SG_PRECISION_FP32_REFINE) */
+  uint64_t contact_lifts;    /* contacts lifted FP32 -> FP64 before a residual evaluation */
+  uint64_t body_lifts;       /* body velocities re-gathered in FP64 for those evaluations */
 } sg_profile;
 
 SG_API int sg_profile_enable(sg_ctx* ctx, int32_t on);

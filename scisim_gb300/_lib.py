@@ -44,7 +44,8 @@ class SgStepStats(C.Structure):
 class SgProfile(C.Structure):
     _fields_ = [("gs_ms", C.c_double), ("gs_launches", C.c_uint64), ("contact_sweeps", C.c_uint64),
                 ("contact_evals", C.c_uint64), ("kernel_launches", C.c_uint64), ("steps", C.c_uint64),
-                ("contacts", C.c_uint64)]
+                ("contacts", C.c_uint64), ("contact_sweeps32", C.c_uint64), ("contact_lifts", C.c_uint64),
+                ("body_lifts", C.c_uint64)]
 
 
 class SgError(RuntimeError):

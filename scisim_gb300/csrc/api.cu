@@ -571,10 +571,14 @@ int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset) {
   out->kernel_launches = ctx->kernel_launches;
   out->steps = ctx->steps;
   out->contacts = ctx->contacts_total;
+  out->contact_sweeps32 = ctx->contact_sweeps32;
+  out->contact_lifts = ctx->contact_lifts;
+  out->body_lifts = ctx->body_lifts;
   if (reset) {
     ctx->gs_ms = 0.0;
     ctx->gs_launches = ctx->contact_sweeps = ctx->contact_evals = ctx->kernel_launches = 0;
     ctx->steps = ctx->contacts_total = 0;
+    ctx->contact_sweeps32 = ctx->contact_lifts = ctx->body_lifts = 0;
   }
   return SG_OK;
 }

@@ -35,6 +35,10 @@ struct SolveStats {
   int color_count[kMaxColors];
   int color_off[kMaxColors + 1];
   int color_fill[kMaxColors];
+  unsigned int sweeps32;  // FP32 sweeps (mixed-precision solve)
+  unsigned int sweeps64;  // FP64 sweeps
+  unsigned int evals;     // FP64 residual evaluations
+  unsigned int lifts;     // FP32 -> FP64 lifts (impulses + body velocity gather)
 };
 
 // A growable device buffer.
@@ -100,6 +104,8 @@ struct sg_ctx {
 
   // solver
   sg::Buf color, perm, body_cnt, body_off, body_fill, body_adj, v_run, stats, barrier;
+  // FP32 sweep data, packed in colour order (mixed-precision solve)
+  sg::Buf pk_ab, pk_n, pk_c, pk_w, pk_r, v32, minv32;
   // buffers of the standalone FrictionSolver entry (kept apart from the scene)
   sg::Buf fs_m, fs_minv, fs_v0, fs_v2;
 
@@ -112,6 +118,7 @@ struct sg_ctx {
   cudaEvent_t ev_gs0 = nullptr, ev_gs1 = nullptr;
   double gs_ms = 0.0;
   uint64_t gs_launches = 0, contact_sweeps = 0, contact_evals = 0, kernel_launches = 0, steps = 0;
+  uint64_t contact_sweeps32 = 0, contact_lifts = 0, body_lifts = 0;
   uint64_t contacts_total = 0;
 
   // pinned staging

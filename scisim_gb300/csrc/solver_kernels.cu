@@ -462,6 +462,252 @@ __global__ void __launch_bounds__(kBlock) k_gs(GsArgs A) {
     A.st->iterations = it;
     A.st->converged = converged ? 1 : 0;
     A.st->error = err_best;
+    A.st->sweeps64 = it;
+    A.st->evals = n_eval;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP32 sweeps over colour-packed FP32 copies of the contact data,
+// FP64 residual on the FP64 image of the iterate every eval32 sweeps, and FP64
+// sweeps to finish (a closing refinement sweep once FP32 reaches tol, or FP64
+// sweeps from the point where FP32 stops making progress near tol).
+__device__ __forceinline__ void local_solve_2d_f(float w00, float w01, float w11, float b0, float b1, float mu,
+                                                 float& r0, float& r1) {
+  if (b0 >= 0.0f) {
+    r0 = 0.0f;
+    r1 = 0.0f;
+    return;
+  }
+  const float det = w00 * w11 - w01 * w01;
+  const float rs0 = (w01 * b1 - w11 * b0) / det;
+  const float rs1 = (w01 * b0 - w00 * b1) / det;
+  if (rs0 >= 0.0f && fabsf(rs1) <= mu * rs0) {
+    r0 = rs0;
+    r1 = rs1;
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const float s = (k == 0) ? 1.0f : -1.0f;
+    const float den = w00 - s * mu * w01;
+    if (!(den > 0.0f)) continue;
+    const float rn = -b0 / den;
+    const float rt = -s * mu * rn;
+    const float ut = w01 * rn + w11 * rt + b1;
+    if (s * ut >= 0.0f) {
+      r0 = rn;
+      r1 = rt;
+      return;
+    }
+  }
+  // Degenerate local problem in FP32: project the stick solution onto the cone.
+  const float rn = fmaxf(rs0, 0.0f);
+  r0 = rn;
+  r1 = fminf(fmaxf(rs1, -mu * rn), mu * rn);
+}
+
+struct Gs32Args {
+  const int2* ab;    // (ia, ib) in colour order
+  const float2* n;   // normal
+  const float2* c;   // local forcing
+  const float4* w;   // w00, w01, w11, mu
+  float2* r;         // local impulse
+  float2* v;         // running body velocity
+  const float* minv;
+  const double* minv64;
+  const double2* v0;
+  const int* body_off;
+  const int* body_adj;
+  int nb;
+  unsigned eval32;
+};
+
+__device__ __forceinline__ void gs_update32(const Gs32Args& B, int s) {
+  const int2 ab = B.ab[s];
+  const float2 nk = B.n[s], ck = B.c[s];
+  const float4 w = B.w[s];
+  const float2 va = __ldcg(&B.v[ab.x]);
+  const bool has_b = ab.y >= 0;
+  const float2 vb = has_b ? __ldcg(&B.v[ab.y]) : make_float2(0.0f, 0.0f);
+  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  float hn = nx * va.x + ny * va.y;
+  float ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn -= nx * vb.x + ny * vb.y;
+    ht -= tx * vb.x + ty * vb.y;
+  }
+  const float u0 = hn + ck.x, u1 = ht + ck.y;
+  const float2 rk = __ldcg(&B.r[s]);
+  const float bt0 = u0 - (w.x * rk.x + w.y * rk.y);
+  const float bt1 = u1 - (w.y * rk.x + w.z * rk.y);
+  float rn0, rn1;
+  local_solve_2d_f(w.x, w.y, w.z, bt0, bt1, w.w, rn0, rn1);
+  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
+  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
+  const float ma = B.minv[ab.x];
+  B.v[ab.x] = make_float2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const float mb = B.minv[ab.y];
+    B.v[ab.y] = make_float2(vb.x - mb * px, vb.y - mb * py);
+  }
+  B.r[s] = make_float2(rn0, rn1);
+}
+
+__global__ void k_pack32(int nc, const int* __restrict__ perm, const int* __restrict__ ia, const int* __restrict__ ib,
+                         const double2* __restrict__ n, const double2* __restrict__ c, const double* __restrict__ W,
+                         const double* __restrict__ mu, const double2* __restrict__ r, int2* __restrict__ ab,
+                         float2* __restrict__ n32, float2* __restrict__ c32, float4* __restrict__ w32,
+                         float2* __restrict__ r32) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nc) return;
+  const int k = perm[s];
+  const int b = ib[k];
+  ab[s] = make_int2(ia[k], b >= 0 ? b : -1);
+  const double2 nk = n[k], ck = c[k], rk = r[k];
+  n32[s] = make_float2((float)nk.x, (float)nk.y);
+  c32[s] = make_float2((float)ck.x, (float)ck.y);
+  w32[s] = make_float4((float)W[3 * k], (float)W[3 * k + 1], (float)W[3 * k + 2], (float)mu[k]);
+  r32[s] = make_float2((float)rk.x, (float)rk.y);
+}
+
+__global__ void k_vel32(int nb, const double2* __restrict__ v, const double* __restrict__ minv, float2* __restrict__ v32,
+                        float* __restrict__ minv32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double2 a = v[i];
+  v32[i] = make_float2((float)a.x, (float)a.y);
+  minv32[i] = (float)minv[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_gs_mixed(GsArgs A, Gs32Args B) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
+  double2* best = A.r_a;
+  double2* cand = A.r_b;
+  double err_best = INFINITY, err_prev = INFINITY;
+  bool converged = false, fp64 = false;
+  unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0;
+  for (it = 1; it <= A.max_iters; ++it) {
+    bool do_eval;
+    if (!fp64) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + tid; s < e; s += nthr) gs_update32(B, s);
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      ++s32;
+      do_eval = (it % eval32 == 0) || it == A.max_iters;
+      if (do_eval) {
+        // Lift the FP32 iterate to FP64: impulses, then body velocities v = v0 + Minv H^T r.
+        for (int s = tid; s < A.nc; s += nthr) {
+          const float2 r32 = __ldcg(&B.r[s]);
+          A.r[A.perm[s]] = make_double2((double)r32.x, (double)r32.y);
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+        for (int i = tid; i < B.nb; i += nthr) {
+          double hx = 0.0, hy = 0.0;
+          const int e = B.body_off[i + 1];
+          for (int p = B.body_off[i]; p < e; ++p) {
+            const int k = B.body_adj[p];
+            const double sgn = (A.ia[k] == i) ? 1.0 : -1.0;
+            const double2 nk = A.n[k], rk = __ldcg(&A.r[k]);
+            const double px = nk.x * rk.x + (-nk.y) * rk.y;
+            const double py = nk.y * rk.x + nk.x * rk.y;
+            hx = hx + sgn * px;
+            hy = hy + sgn * py;
+          }
+          const double2 a = B.v0[i];
+          const double mi = B.minv64[i];
+          A.v[i] = make_double2(a.x + mi * hx, a.y + mi * hy);
+        }
+        ++lifts;
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+    } else {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + tid; s < e; s += nthr) gs_update(A, A.perm[s]);
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      ++s64;
+      do_eval = (it % eval64 == 0) || it == A.max_iters;
+    }
+    if (!do_eval) continue;
+    double emax = 0.0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int a = A.ia[k], b = A.ib[k];
+      const bool has_b = b >= 0;
+      const double2 va = __ldcg(&A.v[a]);
+      const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+      double u0, u1;
+      local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+      const double2 rk = __ldcg(&A.r[k]);
+      cand[k] = rk;
+      emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+    }
+    emax = block_nanmax(emax);
+    const int slot = n_eval % 3;
+    if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+    if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    ++n_eval;
+    if (err < err_best) {
+      err_best = err;
+      double2* t = best;
+      best = cand;
+      cand = t;
+    }
+    if (fp64) {
+      if (err < A.tol) {
+        converged = true;
+        break;
+      }
+    } else if (err < A.tol || (err <= 64.0 * A.tol && !(err < 0.9 * err_prev))) {
+      // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
+      // FP64 sweeps when FP32 stalls within a factor 64 of tol (its rounding floor).
+      fp64 = true;
+    }
+    err_prev = err;
+  }
+  if (it > A.max_iters) it = A.max_iters;
+  if (!converged) {
+    if (err_best < INFINITY)
+      for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+  }
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps32 = s32;
+    A.st->sweeps64 = s64;
+    A.st->evals = n_eval;
+    A.st->lifts = lifts;
   }
 }
 
@@ -568,7 +814,42 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     GA.tol = sp.tol;
     GA.max_iters = sp.max_iters;
     GA.eval_every = sp.eval_every;
-    {
+    if (sp.precision == SG_PRECISION_FP32_REFINE) {
+      const size_t c = (size_t)nc, b = (size_t)std::max(nb, 1);
+      if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
+      if (int r = grow(ctx->pk_n, sizeof(float2) * c)) return r;
+      if (int r = grow(ctx->pk_c, sizeof(float2) * c)) return r;
+      if (int r = grow(ctx->pk_w, sizeof(float4) * c)) return r;
+      if (int r = grow(ctx->pk_r, sizeof(float2) * c)) return r;
+      if (int r = grow(ctx->v32, sizeof(float2) * b)) return r;
+      if (int r = grow(ctx->minv32, sizeof(float) * b)) return r;
+      k_pack32<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), P.ia, P.ib, n2,
+                                                 reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2,
+                                                 ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
+                                                 ctx->pk_w.as<float4>(), ctx->pk_r.as<float2>());
+      k_vel32<<<blocks_for(nb), kBlock, 0, s>>>(nb, vrun, P.minv, ctx->v32.as<float2>(), ctx->minv32.as<float>());
+      SG_CUDA_TRY(cudaGetLastError());
+      Gs32Args GB;
+      GB.ab = ctx->pk_ab.as<int2>();
+      GB.n = ctx->pk_n.as<float2>();
+      GB.c = ctx->pk_c.as<float2>();
+      GB.w = ctx->pk_w.as<float4>();
+      GB.r = ctx->pk_r.as<float2>();
+      GB.v = ctx->v32.as<float2>();
+      GB.minv = ctx->minv32.as<float>();
+      GB.minv64 = P.minv;
+      GB.v0 = reinterpret_cast<const double2*>(P.v0);
+      GB.body_off = off;
+      GB.body_adj = adj;
+      GB.nb = nb;
+      GB.eval32 = 8;
+      void* args[] = {&GA, &GB};
+      const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb));
+      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kBlock), args, 0, s));
+      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+      ctx->kernel_launches += 2;
+    } else {
       void* args[] = {&GA};
       const int g = coop_grid(ctx, k_gs, nc);
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
@@ -588,11 +869,12 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     ctx->h_stats.converged = 1;
     ctx->h_stats.error = 0.0;
   } else if (ctx->h_stats.status == 0) {
-    const uint64_t its = ctx->h_stats.iterations;
-    const uint64_t ee = sp.eval_every ? sp.eval_every : 1;
     ctx->gs_launches += 1;
-    ctx->contact_sweeps += its * (uint64_t)nc;
-    ctx->contact_evals += (its / ee + (ctx->h_stats.converged && its % ee ? 1 : 0)) * (uint64_t)nc;
+    ctx->contact_sweeps += (uint64_t)ctx->h_stats.sweeps64 * (uint64_t)nc;
+    ctx->contact_sweeps32 += (uint64_t)ctx->h_stats.sweeps32 * (uint64_t)nc;
+    ctx->contact_evals += (uint64_t)ctx->h_stats.evals * (uint64_t)nc;
+    ctx->contact_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nc;
+    ctx->body_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nb;
     if (ctx->profile) {
       float ms = 0.f;
       SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));

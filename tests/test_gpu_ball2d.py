@@ -359,6 +359,52 @@ def test_slope_scene_gpu_matches_oracle(gpulib, oracle):
     ctx.close()
 
 
+# ---------------------------------------------------------------- FP32 sweeps + FP64 refinement
+@pytest.mark.parametrize("mu,CoR", [(0.5, 0.0), (0.0, 0.3)])
+def test_fp32_refine_solve_meets_fp64_residual(gpulib, oracle, mu, CoR):
+    """Mixed precision: the returned impulses meet tol under the oracle's FP64 residual;
+    frictionless post-impact velocities agree with the FP64 solve to 1e-6 relative."""
+    m, v0, ia, ib, bases = cluster_problem(21, n=260, spread=4.0)
+    c32 = gpulib.Context(precision=gpulib.PRECISION_FP32_REFINE)
+    c64 = gpulib.Context(precision=gpulib.PRECISION_FP64)
+    g = c32.sobogus_solve_2d(m, v0, ia, ib, bases, CoR, mu, 1e-9, 20000)
+    ref = c64.sobogus_solve_2d(m, v0, ia, ib, bases, CoR, mu, 1e-9, 20000)
+    assert g["succeeded"] and g["error"] <= 1e-9
+    res = oracle.residual_2d(m, v0, ia, ib, bases, CoR, mu, g["alpha"], g["beta"])
+    assert res <= 2e-9
+    if mu == 0.0:
+        assert np.abs(g["v2"] - ref["v2"]).max() <= 1e-6 * np.abs(ref["v2"]).max()
+    c32.close()
+    c64.close()
+
+
+def test_fp32_refine_steps(gpulib, oracle):
+    """Box drop with FP32 sweeps: exact contact sets, residual <= tol (FP64-evaluated) or the
+    iteration cap, and positions within 1e-6 of the FP64 GPU path after 40 steps."""
+    s = box_scene(12, seed=2)
+    kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-9, max_iters=5000)
+    a = gpulib.Context(precision=gpulib.PRECISION_FP32_REFINE, **kw)
+    b = gpulib.Context(precision=gpulib.PRECISION_FP64, **kw)
+    for c in (a, b):
+        c.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    ora = oracle.Ball2D(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"], **kw)
+    for step in range(40):
+        q0, v0 = a.state()
+        st = a.step(1)
+        b.step(1)
+        if st["n_contacts"]:
+            q1p, _ = ora.umap(q0, v0)
+            ia, ib = ora.active_set(q0, q1p)
+            gc = a.last_contacts()
+            assert np.array_equal(gc["ia"], ia) and np.array_equal(gc["ib"], ib)
+            assert st["error"] <= kw["tol"] or st["iterations"] == kw["max_iters"]
+    qa, _ = a.state()
+    qb, _ = b.state()
+    assert np.abs(qa - qb).max() <= 1e-6
+    a.close()
+    b.close()
+
+
 # ---------------------------------------------------------------- failure paths
 def test_wait_timeout_is_reported_and_context_survives(gpulib):
     ctx = gpulib.Context()
