@@ -39,6 +39,7 @@ struct SolveStats {
   unsigned int sweeps64;  // FP64 sweeps
   unsigned int evals;     // FP64 residual evaluations
   unsigned int lifts;     // FP32 -> FP64 lifts (impulses + body velocity gather)
+  unsigned long long mag_slot[3];  // ordered max of |u| + |r| per evaluation (FP32 rounding floor)
 };
 
 // A growable device buffer.

@@ -25,6 +25,7 @@ namespace sg {
 namespace {
 
 constexpr int kBlock = 256;
+constexpr int kGsBlock = 512;  // sweep kernels: one fat block per SM (fewer barrier arrivals)
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------------------
@@ -304,6 +305,46 @@ __global__ void k_color_jp(ColorArgs A) {
     const int left = *((volatile int*)&A.st->remaining[round % 3]);
     if (left == 0) break;
   }
+  // Iterated greedy recolouring: visit the colour classes from the highest down; a
+  // class is an independent set, so all of its contacts can move at once to the
+  // smallest colour that none of their neighbours uses.  Never adds a colour.
+  {
+    int cmax_local = 0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int c = vcolor[k] & 63;
+      vcolor[k] = c;
+      cmax_local = max(cmax_local, c);
+    }
+    for (int o = 16; o > 0; o >>= 1) cmax_local = max(cmax_local, __shfl_down_sync(0xffffffffu, cmax_local, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&A.st->n_colors, cmax_local);
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const int cmax = *((volatile int*)&A.st->n_colors);
+    for (int c = cmax; c >= 1; --c) {
+      for (int k = tid; k < A.nc; k += nthr) {
+        if (vcolor[k] != c) continue;
+        unsigned long long used = 0ull;
+        const int bodies[2] = {A.ia[k], A.ib[k]};
+        for (int bi = 0; bi < 2; ++bi) {
+          const int body = bodies[bi];
+          if (body < 0) continue;
+          const int e = A.body_off[body + 1];
+          for (int p = A.body_off[body]; p < e; ++p) {
+            const int j = A.body_adj[p];
+            if (j != k) used |= 1ull << (vcolor[j] & 63);
+          }
+        }
+        const int lowest = __ffsll((long long)~used) - 1;
+        if (lowest >= 0 && lowest < c) vcolor[k] = lowest;
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+    }
+  }
   // Colour histogram.
   __shared__ int hist[kMaxColors];
   for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) hist[c] = 0;
@@ -390,7 +431,7 @@ __device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
   A.r[k] = make_double2(rn0, rn1);
 }
 
-__global__ void __launch_bounds__(kBlock) k_gs(GsArgs A) {
+__global__ void __launch_bounds__(kGsBlock, 1) k_gs(GsArgs A) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   // A colouring that gave up (timeout or capacity) leaves no valid permutation.
@@ -580,7 +621,7 @@ __global__ void k_vel32(int nb, const double2* __restrict__ v, const double* __r
   minv32[i] = (float)minv[i];
 }
 
-__global__ void __launch_bounds__(kBlock) k_gs_mixed(GsArgs A, Gs32Args B) {
+__global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   if (*((volatile int*)&A.st->status) != 0) return;
@@ -655,7 +696,7 @@ __global__ void __launch_bounds__(kBlock) k_gs_mixed(GsArgs A, Gs32Args B) {
       do_eval = (it % eval64 == 0) || it == A.max_iters;
     }
     if (!do_eval) continue;
-    double emax = 0.0;
+    double emax = 0.0, mag = 0.0;
     for (int k = tid; k < A.nc; k += nthr) {
       const int a = A.ia[k], b = A.ib[k];
       const bool has_b = b >= 0;
@@ -666,16 +707,25 @@ __global__ void __launch_bounds__(kBlock) k_gs_mixed(GsArgs A, Gs32Args B) {
       const double2 rk = __ldcg(&A.r[k]);
       cand[k] = rk;
       emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+      mag = fmax(mag, fabs(u0) + fabs(u1) + fabs(rk.x) + fabs(rk.y));
     }
     emax = block_nanmax(emax);
+    mag = block_nanmax(mag);
     const int slot = n_eval % 3;
-    if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
-    if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+    if (threadIdx.x == 0) {
+      atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+      atomicMax(&A.st->mag_slot[slot], f64_to_ordered(mag));
+    }
+    if (tid == 0) {
+      A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+      A.st->mag_slot[(n_eval + 1) % 3] = 0ull;
+    }
     if (!grid_sync(A.gb, A.spin)) {
       if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
       return;
     }
     const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    const double floor32 = 16.0 * 1.1920929e-7 * ordered_to_f64(*((volatile unsigned long long*)&A.st->mag_slot[slot]));
     ++n_eval;
     if (err < err_best) {
       err_best = err;
@@ -688,9 +738,10 @@ __global__ void __launch_bounds__(kBlock) k_gs_mixed(GsArgs A, Gs32Args B) {
         converged = true;
         break;
       }
-    } else if (err < A.tol || (err <= 64.0 * A.tol && !(err < 0.9 * err_prev))) {
+    } else if (err < A.tol || (err <= fmax(64.0 * A.tol, floor32) && !(err < 0.9 * err_prev))) {
       // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
-      // FP64 sweeps when FP32 stalls within a factor 64 of tol (its rounding floor).
+      // FP64 sweeps when FP32 stalls near tol or near its own rounding floor
+      // (16 eps_fp32 times the largest |u| + |r| of the iterate).
       fp64 = true;
     }
     err_prev = err;
@@ -725,11 +776,11 @@ __global__ void k_wait_flag(const int* flag, int* status, unsigned long long spi
 }
 
 template <typename K>
-int coop_grid(sg_ctx* ctx, K kernel, long work) {
+int coop_grid(sg_ctx* ctx, K kernel, long work, int block = kBlock, int max_per_sm = 64) {
   int bps = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kBlock, 0) != cudaSuccess || bps < 1) bps = 1;
-  long g = (long)bps * ctx->num_sms;
-  const long need = std::max(1L, (work + kBlock - 1) / kBlock);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, block, 0) != cudaSuccess || bps < 1) bps = 1;
+  long g = (long)std::min(bps, max_per_sm) * ctx->num_sms;
+  const long need = std::max(1L, (work + block - 1) / block);
   return (int)std::min(g, need);
 }
 
@@ -842,18 +893,18 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.body_off = off;
       GB.body_adj = adj;
       GB.nb = nb;
-      GB.eval32 = 8;
+      GB.eval32 = 16;
       void* args[] = {&GA, &GB};
-      const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb));
+      const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGsBlock, 1);
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kBlock), args, 0, s));
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGsBlock), args, 0, s));
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
       ctx->kernel_launches += 2;
     } else {
       void* args[] = {&GA};
-      const int g = coop_grid(ctx, k_gs, nc);
+      const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kBlock), args, 0, s));
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kGsBlock), args, 0, s));
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
     }
     ctx->kernel_launches += 6;  // body_count, body_fill, body_sort, color, gs (+ scan below)
