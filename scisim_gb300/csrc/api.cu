@@ -31,7 +31,7 @@ void release(Buf& b) {
   b.bytes = 0;
 }
 
-static constexpr unsigned long long kDefaultSpin = 1ull << 25;  // ~1-2 s of 32 ns sleeps
+static constexpr unsigned long long kDefaultSpin = 1ull << 22;  // ~1 s of L2 polls
 
 static int ensure_contact_capacity(sg_ctx* ctx, int64_t nc) {
   if (nc <= ctx->ccap && ctx->ia.p) return SG_OK;

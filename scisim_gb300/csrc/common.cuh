@@ -37,34 +37,31 @@ struct GridBarrier {
   int pad;
 };
 
+// Monotonic counter: barrier number b is complete when count reaches (b + 1) * gridDim.x,
+// so each arrival is one atomic and the release needs no reset.  The counter starts
+// at zero for every launch (the host clears the struct) and 2^32 arrivals are far
+// beyond any launch here.
 __device__ __forceinline__ bool grid_sync(GridBarrier* gb, unsigned long long spin_limit) {
   __syncthreads();
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
-    volatile unsigned int* vgen = &gb->gen;
+    volatile unsigned int* vcount = &gb->count;
     volatile int* verr = &gb->error;
-    const unsigned int g = *vgen;
     __threadfence();
-    const unsigned int arrived = atomicAdd(&gb->count, 1u);
-    int ok = 1;
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&gb->count, 0u);
-      __threadfence();
-      atomicAdd(&gb->gen, 1u);
-    } else {
-      unsigned long long spins = 0;
-      while (*vgen == g) {
+    const unsigned int old = atomicAdd(&gb->count, 1u);
+    const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
+    unsigned long long spins = 0;
+    while ((int)(*vcount - target) < 0) {
+      if ((++spins & 255ull) == 0ull) {
         if (*verr) break;
-        if (++spins > spin_limit) {
+        if (spins > spin_limit) {
           atomicExch(&gb->error, 1);
           break;
         }
-        __nanosleep(32);
       }
     }
     __threadfence();
-    if (*verr) ok = 0;
-    s_ok = ok;
+    s_ok = (*verr) ? 0 : 1;
   }
   __syncthreads();
   return s_ok != 0;

@@ -564,6 +564,56 @@ struct Gs32Args {
   unsigned eval32;
 };
 
+// The velocity-independent data of one packed contact (prefetched before the
+// barrier that precedes its colour).
+struct C32 {
+  int2 ab;
+  float2 n, c;
+  float4 w;
+  float2 r;
+};
+
+__device__ __forceinline__ C32 load32(const Gs32Args& B, int s) {
+  C32 x;
+  x.ab = B.ab[s];
+  x.n = B.n[s];
+  x.c = B.c[s];
+  x.w = B.w[s];
+  x.r = __ldcg(&B.r[s]);  // written only by this thread, in the previous sweep
+  return x;
+}
+
+__device__ __forceinline__ void apply32(const Gs32Args& B, int s, const C32& x) {
+  const int2 ab = x.ab;
+  const float2 nk = x.n, ck = x.c;
+  const float4 w = x.w;
+  const float2 va = __ldcg(&B.v[ab.x]);
+  const bool has_b = ab.y >= 0;
+  const float2 vb = has_b ? __ldcg(&B.v[ab.y]) : make_float2(0.0f, 0.0f);
+  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  float hn = nx * va.x + ny * va.y;
+  float ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn -= nx * vb.x + ny * vb.y;
+    ht -= tx * vb.x + ty * vb.y;
+  }
+  const float u0 = hn + ck.x, u1 = ht + ck.y;
+  const float2 rk = x.r;
+  const float bt0 = u0 - (w.x * rk.x + w.y * rk.y);
+  const float bt1 = u1 - (w.y * rk.x + w.z * rk.y);
+  float rn0, rn1;
+  local_solve_2d_f(w.x, w.y, w.z, bt0, bt1, w.w, rn0, rn1);
+  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
+  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
+  const float ma = B.minv[ab.x];
+  B.v[ab.x] = make_float2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const float mb = B.minv[ab.y];
+    B.v[ab.y] = make_float2(vb.x - mb * px, vb.y - mb * py);
+  }
+  B.r[s] = make_float2(rn0, rn1);
+}
+
 __device__ __forceinline__ void gs_update32(const Gs32Args& B, int s) {
   const int2 ab = B.ab[s];
   const float2 nk = B.n[s], ck = B.c[s];
@@ -637,20 +687,39 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
   double2* cand = A.r_b;
   double err_best = INFINITY, err_prev = INFINITY;
   bool converged = false, fp64 = false;
-  unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0;
+  unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
+  C32 pf;
+  bool have_pf = false, have_pf_valid = false;
   for (it = 1; it <= A.max_iters; ++it) {
     bool do_eval;
     if (!fp64) {
+      // Each thread's first contact of the next colour is loaded before the barrier
+      // that precedes it; after the barrier only the two body velocities remain.
+      if (!have_pf_valid) {
+        const int s0 = s_off[0] + tid;
+        have_pf = s0 < s_off[1];
+        if (have_pf) pf = load32(B, s0);
+        have_pf_valid = true;
+      }
       for (int col = 0; col < ncol; ++col) {
-        const int e = s_off[col + 1];
-        for (int s = s_off[col] + tid; s < e; s += nthr) gs_update32(B, s);
+        const int s0 = s_off[col] + tid, e = s_off[col + 1];
+        const C32 cur = pf;
+        const bool have = have_pf;
+        const int nxt = (col + 1 < ncol) ? col + 1 : 0;
+        const int sn = s_off[nxt] + tid;
+        have_pf = sn < s_off[nxt + 1];
+        if (have_pf && nxt != 0) pf = load32(B, sn);
+        if (have) apply32(B, s0, cur);
+        for (int s = s0 + nthr; s < e; s += nthr) gs_update32(B, s);
+        if (nxt == 0 && have_pf) pf = load32(B, sn);  // colour 0 of the next sweep, after our own writes
         if (!grid_sync(A.gb, A.spin)) {
           if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
           return;
         }
       }
       ++s32;
-      do_eval = (it % eval32 == 0) || it == A.max_iters;
+      // Check after sweeps 1, 2, 4, ... up to eval32, then every eval32 sweeps.
+      do_eval = (it <= eval32 ? (it & (it - 1)) == 0 : it % eval32 == 0) || it == A.max_iters;
       if (do_eval) {
         // Lift the FP32 iterate to FP64: impulses, then body velocities v = v0 + Minv H^T r.
         for (int s = tid; s < A.nc; s += nthr) {
@@ -675,7 +744,11 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
           }
           const double2 a = B.v0[i];
           const double mi = B.minv64[i];
-          A.v[i] = make_double2(a.x + mi * hx, a.y + mi * hy);
+          const double2 vi = make_double2(a.x + mi * hx, a.y + mi * hy);
+          A.v[i] = vi;
+          // Resynchronise the FP32 running velocity with the impulses: removes the
+          // rounding drift that incremental FP32 updates accumulate.
+          B.v[i] = make_float2((float)vi.x, (float)vi.y);
         }
         ++lifts;
         if (!grid_sync(A.gb, A.spin)) {
@@ -732,7 +805,12 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
       double2* t = best;
       best = cand;
       cand = t;
+      since_best = 0;
+    } else {
+      ++since_best;
     }
+    // FP32 no longer improves the best iterate and is close to its rounding floor.
+    if (!fp64 && since_best >= 16 && err <= 100.0 * floor32) fp64 = true;
     if (fp64) {
       if (err < A.tol) {
         converged = true;
@@ -1182,7 +1260,7 @@ int sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int3
     const long need = std::max(1L, ((long)nc + kBlock - 1) / kBlock);
     return (int)std::min((long)bps * sms, need);
   };
-  const unsigned long long spin = 1ull << 25;
+  const unsigned long long spin = 1ull << 22;  // about a second of barrier polls
   if (nc > 0) {
     SG_CUDA_TRY(cudaMemsetAsync(color, 0xff, sizeof(int) * (size_t)nc, s));
     ColorArgs CA{nc, ia, ib, off, adj, color, perm, st, gb, spin, 4096};
