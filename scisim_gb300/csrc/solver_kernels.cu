@@ -685,7 +685,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
   const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
   double2* best = A.r_a;
   double2* cand = A.r_b;
-  double err_best = INFINITY, err_prev = INFINITY;
+  double err_best = INFINITY;
   bool converged = false, fp64 = false;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   C32 pf;
@@ -769,21 +769,29 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
       do_eval = (it % eval64 == 0) || it == A.max_iters;
     }
     if (!do_eval) continue;
-    double emax = 0.0, mag = 0.0;
+    // emax: the residual.  excess: the largest amount by which a contact's error exceeds
+    // the FP32 rounding floor of that contact, 64 eps_fp32 times the magnitudes entering
+    // u = H v + c (|v_a| + |v_b| + |c|) and r; when it is below tol, FP32 sweeps can no
+    // longer make progress and FP64 sweeps take over.
+    double emax = 0.0, excess = -INFINITY;
     for (int k = tid; k < A.nc; k += nthr) {
       const int a = A.ia[k], b = A.ib[k];
       const bool has_b = b >= 0;
       const double2 va = __ldcg(&A.v[a]);
       const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+      const double2 ck = A.c[k];
       double u0, u1;
-      local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+      local_velocity(A.n[k], ck, va, has_b, vb, u0, u1);
       const double2 rk = __ldcg(&A.r[k]);
       cand[k] = rk;
-      emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
-      mag = fmax(mag, fabs(u0) + fabs(u1) + fabs(rk.x) + fabs(rk.y));
+      const double ek = fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]);
+      emax = nanmax(emax, ek);
+      const double scale = fabs(va.x) + fabs(va.y) + fabs(vb.x) + fabs(vb.y) + fabs(ck.x) + fabs(ck.y) +
+                           fabs(rk.x) + fabs(rk.y);
+      excess = nanmax(excess, ek - 64.0 * 1.1920929e-7 * scale);
     }
     emax = block_nanmax(emax);
-    mag = block_nanmax(mag);
+    const double mag = block_nanmax(excess);
     const int slot = n_eval % 3;
     if (threadIdx.x == 0) {
       atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
@@ -798,7 +806,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
       return;
     }
     const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
-    const double floor32 = 16.0 * 1.1920929e-7 * ordered_to_f64(*((volatile unsigned long long*)&A.st->mag_slot[slot]));
+    const double excess32 = ordered_to_f64(*((volatile unsigned long long*)&A.st->mag_slot[slot]));
     ++n_eval;
     if (err < err_best) {
       err_best = err;
@@ -809,20 +817,17 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
     } else {
       ++since_best;
     }
-    // FP32 no longer improves the best iterate and is close to its rounding floor.
-    if (!fp64 && since_best >= 16 && err <= 100.0 * floor32) fp64 = true;
     if (fp64) {
       if (err < A.tol) {
         converged = true;
         break;
       }
-    } else if (err < A.tol || (err <= fmax(64.0 * A.tol, floor32) && !(err < 0.9 * err_prev))) {
+    } else if (err < A.tol || excess32 <= A.tol || (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
       // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
-      // FP64 sweeps when FP32 stalls near tol or near its own rounding floor
-      // (16 eps_fp32 times the largest |u| + |r| of the iterate).
+      // FP64 sweeps once every contact's remaining error is within FP32 rounding of
+      // its floor (or FP32 stopped improving the best iterate close to it).
       fp64 = true;
     }
-    err_prev = err;
   }
   if (it > A.max_iters) it = A.max_iters;
   if (!converged) {
