@@ -39,7 +39,8 @@ struct SolveStats {
   unsigned int sweeps64;  // FP64 sweeps
   unsigned int evals;     // FP64 residual evaluations
   unsigned int lifts;     // FP32 -> FP64 lifts (impulses + body velocity gather)
-  unsigned long long mag_slot[3];  // ordered max of |u| + |r| per evaluation (FP32 rounding floor)
+  unsigned long long mag_slot[3];  // ordered max of the FP32 rounding-floor excess per evaluation
+  int ig_max[4];                   // highest colour after each iterated-greedy pass
 };
 
 // A growable device buffer.

@@ -305,9 +305,11 @@ __global__ void k_color_jp(ColorArgs A) {
     const int left = *((volatile int*)&A.st->remaining[round % 3]);
     if (left == 0) break;
   }
-  // Iterated greedy recolouring: visit the colour classes from the highest down; a
-  // class is an independent set, so all of its contacts can move at once to the
-  // smallest colour that none of their neighbours uses.  Never adds a colour.
+  // Iterated greedy recolouring (Culberson): re-colour the classes one at a time in
+  // reverse order, each vertex taking the smallest colour unused by the neighbours
+  // already re-coloured in this pass.  A class is an independent set, so a class is
+  // re-coloured in parallel; a pass never adds colours and usually removes some.
+  // A.perm serves as the new-colour array until the permutation is built.
   {
     int cmax_local = 0;
     for (int k = tid; k < A.nc; k += nthr) {
@@ -321,28 +323,51 @@ __global__ void k_color_jp(ColorArgs A) {
       if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
       return;
     }
-    const int cmax = *((volatile int*)&A.st->n_colors);
-    for (int c = cmax; c >= 1; --c) {
-      for (int k = tid; k < A.nc; k += nthr) {
-        if (vcolor[k] != c) continue;
-        unsigned long long used = 0ull;
-        const int bodies[2] = {A.ia[k], A.ib[k]};
-        for (int bi = 0; bi < 2; ++bi) {
-          const int body = bodies[bi];
-          if (body < 0) continue;
-          const int e = A.body_off[body + 1];
-          for (int p = A.body_off[body]; p < e; ++p) {
-            const int j = A.body_adj[p];
-            if (j != k) used |= 1ull << (vcolor[j] & 63);
-          }
-        }
-        const int lowest = __ffsll((long long)~used) - 1;
-        if (lowest >= 0 && lowest < c) vcolor[k] = lowest;
-      }
+    int cmax = *((volatile int*)&A.st->n_colors);
+    volatile int* vnew = A.perm;
+    for (int pass = 0; pass < 3; ++pass) {
+      for (int k = tid; k < A.nc; k += nthr) vnew[k] = -1;
       if (!grid_sync(A.gb, A.spin)) {
         if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
         return;
       }
+      int newmax = 0;
+      for (int c = cmax; c >= 0; --c) {
+        for (int k = tid; k < A.nc; k += nthr) {
+          if (vcolor[k] != c) continue;
+          unsigned long long used = 0ull;
+          const int bodies[2] = {A.ia[k], A.ib[k]};
+          for (int bi = 0; bi < 2; ++bi) {
+            const int body = bodies[bi];
+            if (body < 0) continue;
+            const int e = A.body_off[body + 1];
+            for (int p = A.body_off[body]; p < e; ++p) {
+              const int j = A.body_adj[p];
+              const int cj = vnew[j];
+              if (j != k && cj >= 0) used |= 1ull << cj;
+            }
+          }
+          int nc_k = __ffsll((long long)~used) - 1;
+          if (nc_k < 0) {
+            atomicExch(&A.st->status, (int)SG_CAPACITY);
+            nc_k = 63;
+          }
+          vnew[k] = nc_k;
+          newmax = max(newmax, nc_k);
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      for (int k = tid; k < A.nc; k += nthr) vcolor[k] = vnew[k];
+      for (int o = 16; o > 0; o >>= 1) newmax = max(newmax, __shfl_down_sync(0xffffffffu, newmax, o));
+      if ((threadIdx.x & 31) == 0) atomicMax(&A.st->ig_max[pass], newmax);
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      cmax = *((volatile int*)&A.st->ig_max[pass]);
     }
   }
   // Colour histogram.
