@@ -25,7 +25,8 @@ namespace sg {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kGsBlock = 512;  // sweep kernels: one fat block per SM (fewer barrier arrivals)
+constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (fewer barrier arrivals)
+constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------------------
@@ -696,7 +697,7 @@ __global__ void k_vel32(int nb, const double2* __restrict__ v, const double* __r
   minv32[i] = (float)minv[i];
 }
 
-__global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) {
+__global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   if (*((volatile int*)&A.st->status) != 0) return;
@@ -706,6 +707,9 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
   for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
   __syncthreads();
   const int ncol = s_ncol;
+  // Trailing colours with at most two contacts per thread of one block form the tail.
+  int tail = ncol;
+  while (tail > 0 && s_off[tail] - s_off[tail - 1] <= 2 * (int)blockDim.x) --tail;
   const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
   const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
   double2* best = A.r_a;
@@ -713,6 +717,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
   double err_best = INFINITY;
   bool converged = false, fp64 = false;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
+  unsigned next_eval = 1, interval = eval32;
   C32 pf;
   bool have_pf = false, have_pf_valid = false;
   for (it = 1; it <= A.max_iters; ++it) {
@@ -722,15 +727,15 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
       // that precedes it; after the barrier only the two body velocities remain.
       if (!have_pf_valid) {
         const int s0 = s_off[0] + tid;
-        have_pf = s0 < s_off[1];
+        have_pf = tail > 0 && s0 < s_off[1];
         if (have_pf) pf = load32(B, s0);
         have_pf_valid = true;
       }
-      for (int col = 0; col < ncol; ++col) {
+      for (int col = 0; col < tail; ++col) {
         const int s0 = s_off[col] + tid, e = s_off[col + 1];
         const C32 cur = pf;
         const bool have = have_pf;
-        const int nxt = (col + 1 < ncol) ? col + 1 : 0;
+        const int nxt = (col + 1 < tail) ? col + 1 : 0;
         const int sn = s_off[nxt] + tid;
         have_pf = sn < s_off[nxt + 1];
         if (have_pf && nxt != 0) pf = load32(B, sn);
@@ -742,9 +747,25 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
           return;
         }
       }
+      if (tail < ncol) {
+        // The small trailing colours run in block 0 alone, separated by block
+        // barriers, then one grid barrier (instead of one grid barrier each).
+        if (blockIdx.x == 0) {
+          for (int col = tail; col < ncol; ++col) {
+            for (int s = s_off[col] + threadIdx.x; s < s_off[col + 1]; s += blockDim.x) gs_update32(B, s);
+            __syncthreads();
+          }
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
       ++s32;
-      // Check after sweeps 1, 2, 4, ... up to eval32, then every eval32 sweeps.
-      do_eval = (it <= eval32 ? (it & (it - 1)) == 0 : it % eval32 == 0) || it == A.max_iters;
+      // FP64 checks after sweeps 1, 2, 4, ... eval32, then at an interval that grows
+      // (up to 16 eval32) while the residual is far above tol: a check costs several
+      // sweeps, and the final check at max_iters always happens.
+      do_eval = it == next_eval || it == A.max_iters;
       if (do_eval) {
         // Lift the FP32 iterate to FP64: impulses, then body velocities v = v0 + Minv H^T r.
         for (int s = tid; s < A.nc; s += nthr) {
@@ -841,6 +862,14 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_mixed(GsArgs A, Gs32Args B) 
       since_best = 0;
     } else {
       ++since_best;
+    }
+    if (!fp64) {
+      if (it < eval32) {
+        next_eval = 2 * it;
+      } else {
+        interval = (err > 1e3 * A.tol) ? min(2u * interval, 16u * eval32) : (err > 10.0 * A.tol ? interval : eval32);
+        next_eval = it + interval;
+      }
     }
     if (fp64) {
       if (err < A.tol) {
@@ -1003,9 +1032,9 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.nb = nb;
       GB.eval32 = 16;
       void* args[] = {&GA, &GB};
-      const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGsBlock, 1);
+      const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGsBlock), args, 0, s));
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
       ctx->kernel_launches += 2;
     } else {
