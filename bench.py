@@ -263,11 +263,14 @@ def run_ours(args):
     bytes_per_launch = gs_bytes(prof) / gl
     gs_ms_per_launch = prof["gs_ms"] / gl
     achieved = bytes_per_launch / (gs_ms_per_launch / 1e3) / 1e9 if gs_ms_per_launch > 0 else 0.0
+    # DRAM traffic per launch: the ratio of DRAM bytes to algorithmic bytes from one ncu
+    # capture of the same kernel on a smaller case, scaled to this launch's algorithmic bytes.
     traffic = None
-    tp = os.path.join(HERE, "profiles", "gs_dram_bytes_per_contact_sweep.json")
-    if os.path.exists(tp):
-        d = json.load(open(tp))
-        traffic = d["dram_bytes_per_algorithmic_byte"] * bytes_per_launch
+    tp = os.path.join(HERE, "profiles", "k_gs_mixed_traffic.txt")
+    if os.path.exists(tp) and args.precision == 1:
+        for line in open(tp):
+            if line.startswith("dram_bytes_per_algorithmic_byte"):
+                traffic = float(line.split()[1]) * bytes_per_launch
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                 "kernel": "k_gs (cooperative coloured block Gauss-Seidel)",
