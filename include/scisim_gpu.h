@@ -1,11 +1,13 @@
 /* scisim_gpu.h -- C ABI of the GB300 (sm_103a) SCISim contact-path library.
  *
- * libscisim_gb300.so exposes SCISim's per-step contact path for Ball2D discs:
- * unconstrained maps, spatial-grid broad phase, CCD narrow phase, contact bases
- * and forcing terms, Delassus diagonal blocks, graph-coloured block Gauss-Seidel
- * Coulomb solve, impulse cache, on one GPU.  All arguments are plain C types and
- * host pointers in SCISim's own layouts (q, v interleaved [x0 y0 x1 y1 ...],
- * FP64).  No call throws; every entry point returns an sg_status.
+ * libscisim_gb300.so exposes SCISim's per-step contact path for Ball2D discs and
+ * RigidBody3D spheres: unconstrained maps, spatial-grid broad phase, CCD / sphere
+ * narrow phase, contact bases and forcing terms, Delassus diagonal blocks,
+ * graph-coloured block Gauss-Seidel Coulomb solve, impulse cache, on one GPU.  All
+ * arguments are plain C types and host pointers in SCISim's own layouts (Ball2D q, v
+ * interleaved [x0 y0 x1 y1 ...]; RigidBody3D q = [x (3nb) | R row-major (9nb)],
+ * v = [v (3nb) | omega (3nb)]; FP64).  No call throws; every entry point returns an
+ * sg_status.
  *
  * Each entry point names the reference interface it replaces (file:line within
  * breannansmith/scisim).  A context is single-threaded: one host thread per
@@ -36,19 +38,22 @@ typedef enum {
   SG_CAPACITY = 5        /* a fixed internal limit was exceeded (e.g. > 64 colours) */
 } sg_status;
 
-enum { SG_SYMPLECTIC_EULER = 0, SG_VERLET = 1 };
+/* Unconstrained maps: ball2d/SymplecticEulerMap.cpp, ball2d/VerletMap.cpp (Ball2D) and
+ * rigidbody3d/UnconstrainedMaps/SplitHamMap.cpp (RigidBody3D). */
+enum { SG_SYMPLECTIC_EULER = 0, SG_VERLET = 1, SG_SPLIT_HAM = 2 };
 /* ImpulsesToCache (scisim/ConstrainedMaps/ImpulsesToCache.h) */
 enum { SG_CACHE_NONE = 0, SG_CACHE_NORMAL = 1, SG_CACHE_NORMAL_AND_FRICTION = 2 };
 /* Arithmetic of the Gauss-Seidel sweeps. */
 enum { SG_PRECISION_FP64 = 0, SG_PRECISION_FP32_REFINE = 1 };
 
 typedef struct {
-  int32_t integrator;  /* SG_SYMPLECTIC_EULER | SG_VERLET  (ball2d/SymplecticEulerMap.cpp, VerletMap.cpp) */
+  int32_t integrator;  /* SG_SYMPLECTIC_EULER | SG_VERLET (Ball2D scenes), SG_SPLIT_HAM (sphere scenes) */
   int32_t cache_mode;  /* SG_CACHE_*  (GeometricImpactFrictionMap ctor, GeometricImpactFrictionMap.cpp:20) */
   int32_t precision;   /* SG_PRECISION_* */
   int32_t device;      /* CUDA device ordinal */
   double dt;
-  double gravity[2];   /* Ball2DGravityForce (ball2d/Forces/Ball2DGravityForce.cpp:36-46) */
+  double gravity[3];   /* Ball2DGravityForce (ball2d/Forces/Ball2DGravityForce.cpp:36-46) uses [0..1];
+                          NearEarthGravityForce (rigidbody3d/Forces/NearEarthGravityForce.cpp:39-54) [0..2] */
   double mu;           /* default friction coefficient (Ball2DSim::flow argument) */
   double CoR;          /* default coefficient of restitution */
   double tol;          /* absolute Coulomb residual tolerance (GeometricImpactFrictionMap m_abs_tol) */
@@ -89,9 +94,22 @@ SG_API int sg_ctx_reconfigure(sg_ctx* ctx, const sg_config* cfg);
 SG_API int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r,
                      const double* m, int32_t np, const double* plane_x, const double* plane_n);
 
+/* Uploads a RigidBody3D scene of spheres (replaces RigidBody3DState setup:
+ * rigidbody3d/RigidBody3DState.cpp:140-300, StaticPlane rigidbody3d/StaticGeometry/StaticPlane.cpp:10-15).
+ * q: 12nb [x | R row-major], v: 6nb [v | omega]; r, m: nb; I0: 3nb principal moments
+ * (RigidBodySphere::computeMassAndInertia, rigidbody3d/Geometry/RigidBodySphere.cpp:10-18, gives
+ * m and I0 from r and the density); plane_x, plane_n: 3np (normals are normalised here).
+ * The world inertia is formed from R as the reference's constructor does.  The context's
+ * integrator must be SG_SPLIT_HAM; the 3D geometric map keeps no impulse cache
+ * (rigidbody3dutils/RigidBody3DSceneParser.cpp:1877-1880). */
+SG_API int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r,
+                              const double* m, const double* I0, int32_t np, const double* plane_x,
+                              const double* plane_n);
+
 /* Advances the device-resident scene by n_steps steps of
  * GeometricImpactFrictionMap::flow (scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:267-442)
- * as driven by Ball2DSim::flow (ball2d/Ball2DSim.cpp:305-326).  first_iteration is
+ * as driven by Ball2DSim::flow (ball2d/Ball2DSim.cpp:305-326) or RigidBody3DSim::flow
+ * (rigidbody3d/RigidBody3DSim.cpp:557-630, world inertia updated after each step).  first_iteration is
  * the step index of the first step (SCISim counts from 1).  stats (may be NULL)
  * receives the last step's counters; total_contacts (may be NULL) the sum of
  * active contacts over the n_steps steps.  Returns SG_NOT_CONVERGED if any step's
@@ -105,15 +123,28 @@ SG_API int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_s
 SG_API int sg_flow(sg_ctx* ctx, uint32_t iteration, const double* q0, const double* v0, double* q1, double* v1,
             sg_step_stats* stats);
 
-/* Downloads the device-resident state (Ball2DState q, v). */
+/* Downloads the device-resident state (Ball2DState / RigidBody3DState q, v). */
 SG_API int sg_download_state(sg_ctx* ctx, double* q, double* v);
 
 /* Contacts of the last step in active-set order (Ball2DSim::computeActiveSet,
  * ball2d/Ball2DSim.cpp:151-173): ia, ib (ib = -1 - plane for a static plane),
  * n (2 per contact), alpha, beta (Sobogus.cpp:312-347).  Any output may be NULL.
- * Returns the contact count, or -(count+1) if cap is too small. */
+ * Returns the contact count, or -(count+1) if cap is too small; INT64_MIN on a
+ * sphere-scene context. */
 SG_API int64_t sg_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* n, double* alpha,
                          double* beta);
+
+/* Contacts of the last sphere-scene step in active-set order (RigidBody3DSim::computeActiveSet,
+ * rigidbody3d/RigidBody3DSim.cpp:250-262): ia, ib (ib = -1 - plane), bases (9 per contact,
+ * column-major [n s t], RigidBody3DSim::computeContactBases :277-290), alpha (1) and beta (2
+ * per contact, Sobogus.cpp:526-542).  Any output may be NULL.  Returns the contact count,
+ * -(count+1) if cap is too small, INT64_MIN on a Ball2D context. */
+SG_API int64_t sg_sphere3d_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* bases,
+                                         double* alpha, double* beta);
+
+/* World inertia and its inverse of every sphere (the angular blocks of RigidBody3DState's
+ * M and Minv, rigidbody3d/RigidBody3DState.cpp:428-462), 9 per body, row-major. */
+SG_API int sg_sphere3d_world_inertia(sg_ctx* ctx, double* Iw, double* Iinv);
 
 /* The Gauss-Seidel processing order of the last step's solve (contacts of colour 0,
  * then colour 1, ...) and the colour offsets (n_colors + 1 entries).  Returns the

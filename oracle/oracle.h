@@ -129,6 +129,57 @@ int64_t or_ball2d_active_set(const or_ball2d* s, const double* q0, const double*
 void or_ball2d_umap(const or_ball2d* s, uint32_t iteration, const double* q0, const double* v0, double* q1,
                     double* v1);
 
+// ---------------------------------------------------------------- RigidBody3D spheres
+// 3D So-bogus restatement (Sobogus.cpp:184-251,486-594).  Body b: mass m[b], world inertia Iw and
+// its inverse Iinv (row-major 3x3, 9 per body); v0, v2, f: [v (3nb) | omega (3nb)].  Contact k:
+// bases 9 per contact, column-major [n s t]; arm_a/arm_b: contact point minus body centre
+// (arm_a = -r n for plane contacts, whose ib is -1).  alpha (nc) / beta (2nc): warm start in, solution out.
+void or_sobogus_solve_3d(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0, int nc,
+                         const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
+                         const double* arm_b, const double* CoR, const double* mu, const or_gs_params* p,
+                         double* alpha, double* beta, double* v2, double* f, or_gs_result* res);
+double or_residual_3d(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0, int nc,
+                      const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
+                      const double* arm_b, const double* CoR, const double* mu, const double* alpha,
+                      const double* beta);
+
+// RigidBodySphere::computeMassAndInertia (RigidBodySphere.cpp:10-18): mass and principal inertia.
+void or_sphere_mass_inertia(double r, double density, double* M, double* I);
+
+typedef struct or_sphere3d or_sphere3d;
+
+typedef struct {
+  double dt;
+  double gravity[3];
+  double mu;
+  double CoR;
+  double tol;
+  uint32_t max_iters;
+  uint32_t eval_every;
+} or_sphere3d_params;
+
+// q: [x (3nb) | R row-major (9nb)], v: [v (3nb) | omega (3nb)], r, m per body, I0: 3 per body.
+// Planes: x and unit n, 3 each.  SplitHam integrator, geometric staggering, no impulse cache.
+or_sphere3d* or_sphere3d_create(int nb, const double* q, const double* v, const double* r, const double* m,
+                                const double* I0, int np, const double* plane_x, const double* plane_n,
+                                const or_sphere3d_params* p);
+void or_sphere3d_destroy(or_sphere3d* s);
+int or_sphere3d_step(or_sphere3d* s, uint32_t iteration, or_step_stats* stats);
+int or_sphere3d_run(or_sphere3d* s, uint32_t first_iteration, uint32_t n_steps, or_step_stats* stats,
+                    int64_t* total_contacts);
+void or_sphere3d_get_state(const or_sphere3d* s, double* q, double* v);
+// Sets (q, v) and recomputes the world inertia from R (updateMandMinv).
+void or_sphere3d_set_state(or_sphere3d* s, const double* q, const double* v);
+void or_sphere3d_world_inertia(const or_sphere3d* s, double* Iw, double* Iinv);
+void or_sphere3d_umap(const or_sphere3d* s, const double* q0, const double* v0, double* q1, double* v1);
+void or_sphere3d_set_solver(or_sphere3d* s, double tol, uint32_t max_iters);
+void or_sphere3d_set_next_order(or_sphere3d* s, int64_t nc, const int32_t* order);
+int64_t or_sphere3d_active_set(const or_sphere3d* s, const double* q0, const double* q1, int64_t cap,
+                               int32_t* ia, int32_t* ib);
+// Contacts of the last step (ib = -1 - plane for planes); any output pointer may be NULL.
+int64_t or_sphere3d_last_contacts(const or_sphere3d* s, int64_t cap, int32_t* ia, int32_t* ib, double* bases,
+                                  double* arm_a, double* arm_b, double* alpha, double* beta);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,11 @@ class Ball2DParams(C.Structure):
                 ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
 
 
+class Sphere3DParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("gravity", C.c_double * 3), ("mu", C.c_double), ("CoR", C.c_double),
+                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("n_contacts", C.c_int64), ("n_ball_ball", C.c_int64), ("n_ball_plane", C.c_int64),
                 ("iterations", C.c_uint32), ("succeeded", C.c_int32), ("error", C.c_double)]
@@ -91,6 +96,32 @@ def lib():
         L.or_ball2d_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_uint32]
         L.or_residual_2d.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
         L.or_residual_2d.restype = C.c_double
+        L.or_sobogus_solve_3d.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp,
+                                          _dp, _dp, C.POINTER(GsParams), _dp, _dp, _dp, _dp,
+                                          C.POINTER(GsResult)]
+        L.or_residual_3d.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp,
+                                     _dp, _dp, _dp]
+        L.or_residual_3d.restype = C.c_double
+        L.or_sphere_mass_inertia.argtypes = [C.c_double, C.c_double, _dp, _dp]
+        L.or_sphere3d_create.restype = C.c_void_p
+        L.or_sphere3d_create.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp,
+                                         C.POINTER(Sphere3DParams)]
+        L.or_sphere3d_destroy.argtypes = [C.c_void_p]
+        L.or_sphere3d_step.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(StepStats)]
+        L.or_sphere3d_step.restype = C.c_int
+        L.or_sphere3d_run.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(StepStats),
+                                      C.POINTER(C.c_int64)]
+        L.or_sphere3d_run.restype = C.c_int
+        L.or_sphere3d_get_state.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_sphere3d_set_state.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_sphere3d_world_inertia.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_sphere3d_umap.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.or_sphere3d_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_uint32]
+        L.or_sphere3d_set_next_order.argtypes = [C.c_void_p, C.c_int64, _ip]
+        L.or_sphere3d_active_set.restype = i64
+        L.or_sphere3d_active_set.argtypes = [C.c_void_p, _dp, _dp, i64, _ip, _ip]
+        L.or_sphere3d_last_contacts.restype = i64
+        L.or_sphere3d_last_contacts.argtypes = [C.c_void_p, i64, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -285,4 +316,129 @@ class Ball2D:
         q1 = np.zeros_like(q0)
         v1 = np.zeros_like(v0)
         lib().or_ball2d_umap(self._h, self.iteration + 1, _d(q0), _d(v0), _d(q1), _d(v1))
+        return q1, v1
+
+
+# ------------------------------------------------------------------ RigidBody3D spheres
+def sphere_mass_inertia(r, density):
+    """RigidBodySphere::computeMassAndInertia: (mass, principal moment)."""
+    M, I = C.c_double(0.0), C.c_double(0.0)
+    lib().or_sphere_mass_inertia(r, density, C.byref(M), C.byref(I))
+    return M.value, I.value
+
+
+def sobogus_solve_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, tol, max_iters, eval_every=1,
+                     alpha=None, beta=None, order=None):
+    """RigidBodies3D FrictionSolver::solve.  Returns dict(alpha, beta, v2, f, error, iterations, succeeded)."""
+    m, Iinv, Iw, v0 = f64(m), f64(Iinv), f64(Iw), f64(v0)
+    bases, arm_a, arm_b = f64(bases), f64(arm_a), f64(arm_b)
+    ia, ib = i32(ia), i32(ib)
+    nc, nb = ia.shape[0], m.shape[0]
+    CoR = f64(np.broadcast_to(CoR, (nc,)))
+    mu = f64(np.broadcast_to(mu, (nc,)))
+    alpha = np.zeros(nc) if alpha is None else f64(alpha).copy()
+    beta = np.zeros(2 * nc) if beta is None else f64(beta).copy()
+    v2, f = np.zeros(6 * nb), np.zeros(6 * nb)
+    order_arr = None if order is None else i32(order)
+    gp = GsParams(tol, max_iters, eval_every, _i(order_arr) if order_arr is not None else None)
+    gr = GsResult()
+    lib().or_sobogus_solve_3d(nb, _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(arm_a),
+                              _d(arm_b), _d(CoR), _d(mu), C.byref(gp), _d(alpha), _d(beta), _d(v2), _d(f),
+                              C.byref(gr))
+    return dict(alpha=alpha, beta=beta, v2=v2, f=f, error=gr.error, iterations=gr.iterations,
+                succeeded=bool(gr.succeeded))
+
+
+def residual_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, alpha, beta):
+    """The 3D solver's Coulomb residual of given impulses (alpha, beta)."""
+    m, Iinv, Iw, v0 = f64(m), f64(Iinv), f64(Iw), f64(v0)
+    bases, arm_a, arm_b = f64(bases), f64(arm_a), f64(arm_b)
+    ia, ib = i32(ia), i32(ib)
+    nc = ia.shape[0]
+    CoR = f64(np.broadcast_to(CoR, (nc,)))
+    mu = f64(np.broadcast_to(mu, (nc,)))
+    a, b = f64(alpha), f64(beta)
+    return lib().or_residual_3d(m.shape[0], _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases),
+                                _d(arm_a), _d(arm_b), _d(CoR), _d(mu), _d(a), _d(b))
+
+
+class Sphere3D:
+    """RigidBody3D spheres stepped by SplitHam + GeometricImpactFrictionMap + Sobogus (CPU oracle)."""
+
+    def __init__(self, q, v, r, m, I0, plane_x, plane_n, *, dt, gravity=(0.0, 0.0, -9.81), mu=0.5,
+                 CoR=0.0, tol=1e-9, max_iters=5000, eval_every=1):
+        self.q, self.v = f64(q), f64(v)
+        self.r, self.m, self.I0 = f64(r), f64(m), f64(I0)
+        self.nb = self.r.shape[0]
+        px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        self.np = px.shape[0] // 3
+        p = Sphere3DParams(dt, (C.c_double * 3)(*gravity), mu, CoR, tol, max_iters, eval_every)
+        self._h = lib().or_sphere3d_create(self.nb, _d(self.q), _d(self.v), _d(self.r), _d(self.m),
+                                           _d(self.I0), self.np, _d(px), _d(pn), C.byref(p))
+        self.iteration = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().or_sphere3d_destroy(h)
+            self._h = None
+
+    def step(self):
+        self.iteration += 1
+        st = StepStats()
+        lib().or_sphere3d_step(self._h, self.iteration, C.byref(st))
+        return dict(n_contacts=st.n_contacts, n_sphere_sphere=st.n_ball_ball, n_sphere_plane=st.n_ball_plane,
+                    iterations=st.iterations, succeeded=bool(st.succeeded), error=st.error)
+
+    def run(self, n_steps):
+        st = StepStats()
+        tot = C.c_int64(0)
+        bad = lib().or_sphere3d_run(self._h, self.iteration + 1, n_steps, C.byref(st), C.byref(tot))
+        self.iteration += n_steps
+        return (dict(n_contacts=st.n_contacts, iterations=st.iterations, succeeded=bool(st.succeeded),
+                     error=st.error), tot.value, bad)
+
+    def state(self):
+        q, v = np.zeros(12 * self.nb), np.zeros(6 * self.nb)
+        lib().or_sphere3d_get_state(self._h, _d(q), _d(v))
+        return q, v
+
+    def set_state(self, q, v):
+        q, v = f64(q), f64(v)
+        lib().or_sphere3d_set_state(self._h, _d(q), _d(v))
+
+    def world_inertia(self):
+        Iw, Iinv = np.zeros(9 * self.nb), np.zeros(9 * self.nb)
+        lib().or_sphere3d_world_inertia(self._h, _d(Iw), _d(Iinv))
+        return Iw, Iinv
+
+    def set_solver(self, tol, max_iters):
+        lib().or_sphere3d_set_solver(self._h, tol, max_iters)
+
+    def set_next_order(self, order):
+        order = i32(order)
+        lib().or_sphere3d_set_next_order(self._h, order.shape[0], _i(order))
+
+    def last_contacts(self):
+        L = lib()
+        nc = L.or_sphere3d_last_contacts(self._h, 0, None, None, None, None, None, None, None)
+        ia, ib = np.zeros(nc, np.int32), np.zeros(nc, np.int32)
+        E, ra, rb = np.zeros(9 * nc), np.zeros(3 * nc), np.zeros(3 * nc)
+        a, b = np.zeros(nc), np.zeros(2 * nc)
+        L.or_sphere3d_last_contacts(self._h, nc, _i(ia), _i(ib), _d(E), _d(ra), _d(rb), _d(a), _d(b))
+        return dict(ia=ia, ib=ib, bases=E.reshape(-1, 3, 3), arm_a=ra.reshape(-1, 3), arm_b=rb.reshape(-1, 3),
+                    alpha=a, beta=b.reshape(-1, 2))
+
+    def active_set(self, q0, q1):
+        q0, q1 = f64(q0), f64(q1)
+        L = lib()
+        k = L.or_sphere3d_active_set(self._h, _d(q0), _d(q1), 0, None, None)
+        ia, ib = np.zeros(k, np.int32), np.zeros(k, np.int32)
+        L.or_sphere3d_active_set(self._h, _d(q0), _d(q1), k, _i(ia), _i(ib))
+        return ia, ib
+
+    def umap(self, q0, v0):
+        q0, v0 = f64(q0), f64(v0)
+        q1, v1 = np.zeros_like(q0), np.zeros_like(v0)
+        lib().or_sphere3d_umap(self._h, _d(q0), _d(v0), _d(q1), _d(v1))
         return q1, v1

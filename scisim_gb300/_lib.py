@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "libscisim_gb300.so")
 SG_OK, SG_NOT_CONVERGED, SG_BAD_INPUT, SG_DEVICE_TIMEOUT, SG_CUDA_ERROR, SG_CAPACITY = range(6)
 STATUS_NAMES = {0: "SG_OK", 1: "SG_NOT_CONVERGED", 2: "SG_BAD_INPUT", 3: "SG_DEVICE_TIMEOUT",
                 4: "SG_CUDA_ERROR", 5: "SG_CAPACITY"}
-SYMPLECTIC_EULER, VERLET = 0, 1
+SYMPLECTIC_EULER, VERLET, SPLIT_HAM = 0, 1, 2
 CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
 PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
 
@@ -27,7 +27,7 @@ _i64 = C.c_int64
 
 class SgConfig(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("cache_mode", C.c_int32), ("precision", C.c_int32),
-                ("device", C.c_int32), ("dt", C.c_double), ("gravity", C.c_double * 2), ("mu", C.c_double),
+                ("device", C.c_int32), ("dt", C.c_double), ("gravity", C.c_double * 3), ("mu", C.c_double),
                 ("CoR", C.c_double), ("tol", C.c_double), ("max_iters", C.c_uint32),
                 ("eval_every", C.c_uint32)]
 
@@ -62,10 +62,13 @@ SIGNATURES = {
     "sg_ctx_destroy": (None, [C.c_void_p]),
     "sg_ctx_reconfigure": (C.c_int, [C.c_void_p, C.POINTER(SgConfig)]),
     "sg_ball2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
+    "sg_sphere3d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
     "sg_step": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SgStepStats), C.POINTER(_i64)]),
     "sg_flow": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp, C.POINTER(SgStepStats)]),
     "sg_download_state": (C.c_int, [C.c_void_p, _dp, _dp]),
     "sg_last_contacts": (_i64, [C.c_void_p, _i64, _ip, _ip, _dp, _dp, _dp]),
+    "sg_sphere3d_last_contacts": (_i64, [C.c_void_p, _i64, _ip, _ip, _dp, _dp, _dp]),
+    "sg_sphere3d_world_inertia": (C.c_int, [C.c_void_p, _dp, _dp]),
     "sg_last_solve_order": (_i64, [C.c_void_p, _i64, _ip, _ip, _ip]),
     "sg_sobogus_solve_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, C.c_int32, _ip, _ip, _dp, _dp, _dp,
                                       C.c_uint32, C.c_double, C.c_uint32, _dp, _dp, _dp, _dp, _dp,
@@ -124,18 +127,26 @@ def i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+def _g3(gravity):
+    g = tuple(float(x) for x in gravity)
+    if not 2 <= len(g) <= 3:
+        raise ValueError("gravity has 2 (Ball2D) or 3 (RigidBody3D) components")
+    return (C.c_double * 3)(*(g + (0.0,) * (3 - len(g))))
+
+
 class Context:
     """Owns one sg_ctx (device memory, stream, impulse cache)."""
 
     def __init__(self, *, dt=0.01, gravity=(0.0, -9.81), mu=0.5, CoR=0.0, tol=1e-9, max_iters=5000,
                  eval_every=1, integrator=SYMPLECTIC_EULER, cache_mode=CACHE_NONE,
                  precision=PRECISION_FP64, device=0):
-        self.config = SgConfig(integrator, cache_mode, precision, device, dt, (C.c_double * 2)(*gravity), mu,
+        self.config = SgConfig(integrator, cache_mode, precision, device, dt, _g3(gravity), mu,
                                CoR, tol, max_iters, eval_every)
         h = C.c_void_p()
         check(lib().sg_ctx_create(C.byref(self.config), C.byref(h)), "sg_ctx_create")
         self._h = h
         self.nb = 0
+        self.dim = 2
 
     @property
     def handle(self):
@@ -148,7 +159,7 @@ class Context:
         fields["gravity"] = tuple(c.gravity)
         fields.update(changes)
         cfg = SgConfig(fields["integrator"], fields["cache_mode"], fields["precision"], fields["device"],
-                       fields["dt"], (C.c_double * 2)(*fields["gravity"]), fields["mu"], fields["CoR"],
+                       fields["dt"], _g3(fields["gravity"]), fields["mu"], fields["CoR"],
                        fields["tol"], fields["max_iters"], fields["eval_every"])
         check(lib().sg_ctx_reconfigure(self._h, C.byref(cfg)), "sg_ctx_reconfigure")
         self.config = cfg
@@ -169,9 +180,24 @@ class Context:
         q, v, r, m = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1)
         px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
         self.nb = r.shape[0]
+        self.dim = 2
         self._keep = (q, v, r, m, px, pn)
         check(lib().sg_ball2d_upload(self._h, self.nb, dptr(q), dptr(v), dptr(r), dptr(m), px.shape[0] // 2,
                                      dptr(px), dptr(pn)), "sg_ball2d_upload")
+
+    def upload_sphere3d(self, q, v, r, m, I0, plane_x, plane_n):
+        """RigidBody3D spheres: q 12nb [x | R row-major], v 6nb [v | omega], r, m, I0 (3 per body)."""
+        q, v, r, m = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1)
+        I0 = f64(I0).reshape(-1)
+        px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        nb = r.shape[0]
+        if q.shape[0] != 12 * nb or v.shape[0] != 6 * nb or m.shape[0] != nb or I0.shape[0] != 3 * nb:
+            raise ValueError("inconsistent RigidBody3D state sizes")
+        self.nb = nb
+        self.dim = 3
+        self._keep = (q, v, r, m, I0, px, pn)
+        check(lib().sg_sphere3d_upload(self._h, nb, dptr(q), dptr(v), dptr(r), dptr(m), dptr(I0), px.shape[0] // 3,
+                                       dptr(px), dptr(pn)), "sg_sphere3d_upload")
 
     def step(self, n_steps=1, first_iteration=1):
         st = SgStepStats()
@@ -194,8 +220,8 @@ class Context:
         return q1, v1, d
 
     def state(self):
-        q = np.empty(2 * self.nb)
-        v = np.empty(2 * self.nb)
+        q = np.empty((12 if self.dim == 3 else 2) * self.nb)
+        v = np.empty((6 if self.dim == 3 else 2) * self.nb)
         check(lib().sg_download_state(self._h, dptr(q), dptr(v)), "sg_download_state")
         return q, v
 
@@ -209,6 +235,22 @@ class Context:
         if got != nc:
             raise SgError(SG_CUDA_ERROR, "sg_last_contacts")
         return dict(ia=ia, ib=ib, n=n.reshape(-1, 2), alpha=a, beta=b)
+
+    def sphere3d_last_contacts(self):
+        L = lib()
+        nc = L.sg_sphere3d_last_contacts(self._h, 0, None, None, None, None, None)
+        nc = -nc - 1 if nc < 0 else nc
+        ia, ib = np.empty(nc, np.int32), np.empty(nc, np.int32)
+        E, a, b = np.empty(9 * nc), np.empty(nc), np.empty(2 * nc)
+        got = L.sg_sphere3d_last_contacts(self._h, nc, iptr(ia), iptr(ib), dptr(E), dptr(a), dptr(b))
+        if got != nc:
+            raise SgError(SG_CUDA_ERROR, "sg_sphere3d_last_contacts")
+        return dict(ia=ia, ib=ib, bases=E.reshape(-1, 3, 3), alpha=a, beta=b.reshape(-1, 2))
+
+    def sphere3d_world_inertia(self):
+        Iw, Iinv = np.empty(9 * self.nb), np.empty(9 * self.nb)
+        check(lib().sg_sphere3d_world_inertia(self._h, dptr(Iw), dptr(Iinv)), "sg_sphere3d_world_inertia")
+        return Iw, Iinv
 
     def last_solve_order(self):
         L = lib()

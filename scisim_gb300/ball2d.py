@@ -32,8 +32,9 @@ class ImpulsesToCache(enum.IntEnum):
 
 
 class SobogusSolverType(enum.Enum):
-    """scisim/ConstrainedMaps/Sobogus.h (RigidBodies3D and RigidBody2D are not built here)."""
+    """scisim/ConstrainedMaps/Sobogus.h (RigidBody2D is not built here)."""
     Balls2D = "balls_2d"
+    RigidBodies3D = "rigid_bodies_3d"
 
 
 class UnconstrainedMap:
@@ -76,8 +77,8 @@ class Sobogus(FrictionSolver):
 
     def __init__(self, solver_type=SobogusSolverType.Balls2D, eval_every: int = 1, precision: str = "fp64",
                  device: int = 0):
-        if solver_type != SobogusSolverType.Balls2D:
-            raise ValueError("only SobogusSolverType.Balls2D is available")
+        if solver_type not in (SobogusSolverType.Balls2D, SobogusSolverType.RigidBodies3D):
+            raise ValueError("SobogusSolverType.RigidBody2D is not available")
         if eval_every < 1:
             raise ValueError("eval_every must be positive")
         self.solver_type = solver_type
@@ -90,9 +91,10 @@ class Sobogus(FrictionSolver):
         return "sobogus"
 
     def numFrictionImpulsesPerNormal(self, ambient_space_dimensions):
-        if ambient_space_dimensions != 2:
-            raise ValueError("Balls2D solver is two dimensional")
-        return 1
+        dim = 2 if self.solver_type == SobogusSolverType.Balls2D else 3
+        if ambient_space_dimensions != dim:
+            raise ValueError("solver type %s is %dD" % (self.solver_type.value, dim))
+        return dim - 1
 
     def solve(self, M_diag, v0, body_a, body_b, contact_bases, CoR, mu, max_iters, tol, alpha, beta):
         """FrictionSolver::solve (Sobogus.cpp:880-1088) for Ball2D contacts.
@@ -101,6 +103,8 @@ class Sobogus(FrictionSolver):
         contact_bases: 2 x 2nc matrix [n0 t0 n1 t1 ...] as SCISim builds it; alpha/beta
         are the warm start, updated in place.  Returns (f, v2, solve_succeeded, error).
         """
+        if self.solver_type != SobogusSolverType.Balls2D:
+            raise ValueError("the standalone solve takes Balls2D contacts; sphere scenes solve inside each step")
         if self._ctx is None:
             self._ctx = _lib.Context(precision=self.precision, device=self.device)
         B = np.asarray(contact_bases, dtype=np.float64)
@@ -134,15 +138,14 @@ class GeometricImpactFrictionMap:
         self._key = None
 
     def _context(self, sim, umap, solver, dt, CoR, mu):
-        key = (sim.nballs, id(sim), umap.integrator, solver.eval_every, solver.precision, float(dt), float(CoR),
+        key = (sim.nbodies, id(sim), umap.integrator, solver.eval_every, solver.precision, float(dt), float(CoR),
                float(mu), tuple(sim.gravity))
         if self._ctx is None or key != self._key:
             self._ctx = _lib.Context(dt=dt, gravity=sim.gravity, mu=mu, CoR=CoR, tol=self.abs_tol,
                                      max_iters=self.max_iters, eval_every=solver.eval_every,
                                      integrator=umap.integrator, cache_mode=int(self.impulses_to_cache),
                                      precision=solver.precision, device=solver.device)
-            st = sim.state
-            self._ctx.upload_ball2d(st.q, st.v, st.r, st.m, st.plane_x(), st.plane_n())
+            sim.upload(self._ctx)
             self._key = key
         return self._ctx
 
@@ -157,7 +160,9 @@ class GeometricImpactFrictionMap:
         return q1, v1
 
     def last_contacts(self):
-        return self._ctx.last_contacts() if self._ctx is not None else None
+        if self._ctx is None:
+            return None
+        return self._ctx.sphere3d_last_contacts() if self._ctx.dim == 3 else self._ctx.last_contacts()
 
 
 class StaticPlane:
@@ -200,6 +205,14 @@ class Ball2DSim:
     @property
     def nballs(self):
         return self.state.nballs()
+
+    @property
+    def nbodies(self):
+        return self.state.nballs()
+
+    def upload(self, ctx):
+        st = self.state
+        ctx.upload_ball2d(st.q, st.v, st.r, st.m, st.plane_x(), st.plane_n())
 
     def flow(self, iteration, dt, umap, CoR, mu, solver, ifmap):
         q1, v1 = ifmap.flow(self, umap, solver, iteration, dt, CoR, mu, self.state.q, self.state.v)

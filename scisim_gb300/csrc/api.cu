@@ -58,7 +58,8 @@ static int upload(sg_ctx* ctx, Buf& b, const void* host, size_t bytes) {
 
 static int validate_config(const sg_config* c) {
   if (!c) return SG_BAD_INPUT;
-  if (c->integrator != SG_SYMPLECTIC_EULER && c->integrator != SG_VERLET) return SG_BAD_INPUT;
+  if (c->integrator != SG_SYMPLECTIC_EULER && c->integrator != SG_VERLET && c->integrator != SG_SPLIT_HAM)
+    return SG_BAD_INPUT;
   if (c->cache_mode < SG_CACHE_NONE || c->cache_mode > SG_CACHE_NORMAL_AND_FRICTION) return SG_BAD_INPUT;
   if (c->precision != SG_PRECISION_FP64 && c->precision != SG_PRECISION_FP32_REFINE) return SG_BAD_INPUT;
   if (!(c->dt > 0.0) || !(c->tol >= 0.0) || !(c->mu >= 0.0) || !(c->CoR >= 0.0 && c->CoR <= 1.0)) return SG_BAD_INPUT;
@@ -194,6 +195,10 @@ void sg_ctx_destroy(sg_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  Buf* bufs3[] = {&ctx->I0, &ctx->Iw, &ctx->Iinv, &ctx->E3, &ctx->Aa3, &ctx->Ab3, &ctx->c3, &ctx->W3,
+                  &ctx->r3, &ctx->r3a, &ctx->r3b, &ctx->ab3, &ctx->vrun3, &ctx->pk_ab, &ctx->pk_n, &ctx->pk_c,
+                  &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32};
+  for (Buf* b : bufs3) release(*b);
   Buf* bufs[] = {&ctx->q, &ctx->v, &ctx->r, &ctx->m, &ctx->minv, &ctx->q1, &ctx->v1, &ctx->v2, &ctx->plane_x,
                  &ctx->plane_n, &ctx->plane_t, &ctx->aabb, &ctx->cell_of, &ctx->cell_count, &ctx->cell_start,
                  &ctx->cell_fill, &ctx->sorted, &ctx->pair_cnt, &ctx->pair_off, &ctx->grid, &ctx->plane_flag,
@@ -230,6 +235,7 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
       return SG_BAD_INPUT;
     }
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  ctx->dim = 2;
   ctx->nb = nb;
   ctx->np = np;
   const size_t b2 = sizeof(double) * 2 * (size_t)std::max(nb, 1), b1 = sizeof(double) * (size_t)std::max(nb, 1);
@@ -274,15 +280,83 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
   return SG_OK;
 }
 
+static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
+                         const double* I0, int32_t np, const double* plane_x, const double* plane_n) {
+  if (!ctx || nb < 0 || np < 0 || (nb > 0 && (!q || !v || !r || !m || !I0)) || (np > 0 && (!plane_x || !plane_n))) {
+    set_error("sg_sphere3d_upload: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  for (int i = 0; i < nb; ++i)
+    if (!(r[i] > 0.0) || !(m[i] > 0.0) || !(I0[3 * i] > 0.0) || !(I0[3 * i + 1] > 0.0) || !(I0[3 * i + 2] > 0.0)) {
+      set_error("sg_sphere3d_upload: radii, masses and inertias must be positive");
+      return SG_BAD_INPUT;
+    }
+  std::vector<double> pn(3 * (size_t)np);
+  for (int p = 0; p < np; ++p) {
+    // StaticPlane: n = n.normalized() (rigidbody3d/StaticGeometry/StaticPlane.cpp:10-15)
+    const double* n = plane_n + 3 * p;
+    const double z = (n[0] * n[0] + n[1] * n[1]) + n[2] * n[2];
+    if (!(z > 0.0)) {
+      set_error("sg_sphere3d_upload: zero plane normal");
+      return SG_BAD_INPUT;
+    }
+    const double sq = std::sqrt(z);
+    for (int j = 0; j < 3; ++j) pn[3 * p + j] = n[j] / sq;
+  }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  ctx->dim = 3;
+  ctx->nb = nb;
+  ctx->np = np;
+  const size_t nbs = (size_t)std::max(nb, 1);
+  std::vector<double> minv(nb);
+  for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];  // formWorldSpaceInverseMassMatrix (RigidBody3DState.cpp:208-214)
+  if (int e = upload(ctx, ctx->q, q, sizeof(double) * 12 * nb)) return e;
+  if (int e = upload(ctx, ctx->v, v, sizeof(double) * 6 * nb)) return e;
+  if (int e = upload(ctx, ctx->r, r, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->m, m, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->minv, minv.data(), sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->I0, I0, sizeof(double) * 3 * nb)) return e;
+  if (int e = grow(ctx->Iw, sizeof(double) * 9 * nbs)) return e;
+  if (int e = grow(ctx->Iinv, sizeof(double) * 9 * nbs)) return e;
+  if (int e = grow(ctx->q1, sizeof(double) * 12 * nbs)) return e;
+  if (int e = grow(ctx->v1, sizeof(double) * 6 * nbs)) return e;
+  if (int e = grow(ctx->v2, sizeof(double) * 6 * nbs)) return e;
+  if (int e = grow(ctx->aabb, sizeof(double) * 6 * nbs)) return e;
+  if (int e = upload(ctx, ctx->plane_x, plane_x, sizeof(double) * 3 * np)) return e;
+  if (int e = upload(ctx, ctx->plane_n, pn.data(), sizeof(double) * 3 * np)) return e;
+  if (int e = grow(ctx->plane_x, 16)) return e;
+  if (int e = grow(ctx->plane_n, 16)) return e;
+  // World inertia at construction (RigidBody3DState.cpp:140-230).
+  if (int e = sphere3d_update_inertia(ctx, true)) return e;
+  ctx->prev_n = 0;
+  ctx->last_nc = 0;
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+static int check_integrator(const sg_ctx* ctx) {
+  const bool split = ctx->cfg.integrator == SG_SPLIT_HAM;
+  if ((ctx->dim == 3) != split) {
+    set_error(ctx->dim == 3 ? "sphere scenes step with SG_SPLIT_HAM"
+                            : "Ball2D scenes step with SG_SYMPLECTIC_EULER or SG_VERLET");
+    return SG_BAD_INPUT;
+  }
+  return SG_OK;
+}
+
+static size_t q_doubles(const sg_ctx* ctx) { return (size_t)ctx->nb * (ctx->dim == 3 ? 12 : 2); }
+static size_t v_doubles(const sg_ctx* ctx) { return (size_t)ctx->nb * (ctx->dim == 3 ? 6 : 2); }
+
 int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_stats* stats, int64_t* total_contacts) {
   if (!ctx) return SG_BAD_INPUT;
   (void)first_iteration;  // gravity is time independent
+  if (int e = check_integrator(ctx)) return e;
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
   int64_t tot = 0;
   int worst = SG_OK;
   sg_step_stats st{};
   for (uint32_t k = 0; k < n_steps; ++k) {
-    const int r = step_once(ctx, &st);
+    const int r = ctx->dim == 3 ? sphere3d_step(ctx, &st) : step_once(ctx, &st);
     if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
     if (r == SG_NOT_CONVERGED) worst = r;
     tot += st.n_contacts;
@@ -295,14 +369,18 @@ int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_sta
 int sg_flow(sg_ctx* ctx, uint32_t iteration, const double* q0, const double* v0, double* q1, double* v1,
             sg_step_stats* stats) {
   if (!ctx || (ctx->nb > 0 && (!q0 || !v0 || !q1 || !v1))) return SG_BAD_INPUT;
+  if (int e = check_integrator(ctx)) return e;
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
-  const size_t bytes = sizeof(double) * 2 * (size_t)ctx->nb;
-  SG_CUDA_TRY(cudaMemcpyAsync(ctx->q.p, q0, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  SG_CUDA_TRY(cudaMemcpyAsync(ctx->v.p, v0, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  const size_t qb = sizeof(double) * q_doubles(ctx), vb = sizeof(double) * v_doubles(ctx);
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->q.p, q0, qb, cudaMemcpyHostToDevice, ctx->stream));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->v.p, v0, vb, cudaMemcpyHostToDevice, ctx->stream));
+  // A 3D state carries its own orientations: the world inertia follows them (updateMandMinv).
+  if (ctx->dim == 3)
+    if (int e = sphere3d_update_inertia(ctx, false)) return e;
   const int r = sg_step(ctx, iteration, 1, stats, nullptr);
   if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
-  SG_CUDA_TRY(cudaMemcpyAsync(q1, ctx->q.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA_TRY(cudaMemcpyAsync(v1, ctx->v.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaMemcpyAsync(q1, ctx->q.p, qb, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaMemcpyAsync(v1, ctx->v.p, vb, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return r;
 }
@@ -310,15 +388,18 @@ int sg_flow(sg_ctx* ctx, uint32_t iteration, const double* q0, const double* v0,
 int sg_download_state(sg_ctx* ctx, double* q, double* v) {
   if (!ctx) return SG_BAD_INPUT;
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
-  const size_t bytes = sizeof(double) * 2 * (size_t)ctx->nb;
-  if (q) SG_CUDA_TRY(cudaMemcpyAsync(q, ctx->q.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  if (v) SG_CUDA_TRY(cudaMemcpyAsync(v, ctx->v.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (q) SG_CUDA_TRY(cudaMemcpyAsync(q, ctx->q.p, sizeof(double) * q_doubles(ctx), cudaMemcpyDeviceToHost, ctx->stream));
+  if (v) SG_CUDA_TRY(cudaMemcpyAsync(v, ctx->v.p, sizeof(double) * v_doubles(ctx), cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }
 
 int64_t sg_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* n, double* alpha, double* beta) {
   if (!ctx) return SG_BAD_INPUT;
+  if (ctx->dim != 2) {
+    set_error("sg_last_contacts: sphere scenes use sg_sphere3d_last_contacts");
+    return INT64_MIN;
+  }
   const int64_t nc = ctx->last_nc;
   if (nc > cap) return -(nc + 1);
   if (nc == 0) return 0;
@@ -341,6 +422,56 @@ int64_t sg_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, dou
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
   return nc;
+}
+
+int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
+                       const double* I0, int32_t np, const double* plane_x, const double* plane_n) {
+  return sphere3d_upload_impl(ctx, nb, q, v, r, m, I0, np, plane_x, plane_n);
+}
+
+int64_t sg_sphere3d_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* bases, double* alpha,
+                                  double* beta) {
+  if (!ctx) return INT64_MIN;
+  if (ctx->dim != 3) {
+    set_error("sg_sphere3d_last_contacts: not a sphere scene");
+    return INT64_MIN;
+  }
+  const int64_t nc = ctx->last_nc;
+  if (nc > cap) return -(nc + 1);
+  if (nc == 0) return 0;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return INT64_MIN;
+  cudaStream_t s = ctx->stream;
+  const size_t c = (size_t)nc;
+  if (ia) cudaMemcpyAsync(ia, ctx->ia.p, sizeof(int) * c, cudaMemcpyDeviceToHost, s);
+  if (ib) cudaMemcpyAsync(ib, ctx->ib.p, sizeof(int) * c, cudaMemcpyDeviceToHost, s);
+  if (bases) {
+    // Device rows n, s, t of each contact = columns of the 3x3 basis: column-major [n s t].
+    cudaMemcpyAsync(bases, ctx->E3.p, sizeof(double) * 9 * c, cudaMemcpyDeviceToHost, s);
+  }
+  if (alpha || beta) {
+    std::vector<double> ab(3 * c);
+    cudaMemcpyAsync(ab.data(), ctx->ab3.p, sizeof(double) * 3 * c, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return INT64_MIN;
+    for (size_t k = 0; k < c; ++k) {
+      if (alpha) alpha[k] = ab[3 * k];
+      if (beta) {
+        beta[2 * k] = ab[3 * k + 1];
+        beta[2 * k + 1] = ab[3 * k + 2];
+      }
+    }
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return INT64_MIN;
+  return nc;
+}
+
+int sg_sphere3d_world_inertia(sg_ctx* ctx, double* Iw, double* Iinv) {
+  if (!ctx || ctx->dim != 3) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  const size_t bytes = sizeof(double) * 9 * (size_t)ctx->nb;
+  if (Iw && bytes) SG_CUDA_TRY(cudaMemcpyAsync(Iw, ctx->Iw.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (Iinv && bytes) SG_CUDA_TRY(cudaMemcpyAsync(Iinv, ctx->Iinv.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
 }
 
 int64_t sg_last_solve_order(sg_ctx* ctx, int64_t cap, int32_t* order, int32_t* color_offsets, int32_t* n_colors) {

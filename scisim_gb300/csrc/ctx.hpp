@@ -88,10 +88,13 @@ struct sg_ctx {
   int num_sms = 0;
   unsigned long long spin_limit = 0;
 
-  // Ball2D scene
+  // Scene: dim 2 = Ball2D (q, v: 2 per body), dim 3 = RigidBody3D spheres
+  // (q: [x (3nb) | R row-major (9nb)], v: [v (3nb) | omega (3nb)], SCISim's layouts).
+  int dim = 2;
   int nb = 0, np = 0;
   sg::Buf q, v, r, m, minv, q1, v1, v2;
   sg::Buf plane_x, plane_n, plane_t;
+  sg::Buf I0, Iw, Iinv;  // 3D: principal inertia (3nb), world inertia and inverse (9nb, row-major)
 
   // broad phase
   sg::Buf aabb, cell_of, cell_count, cell_start, cell_fill, sorted, pair_cnt, pair_off, grid;
@@ -108,6 +111,11 @@ struct sg_ctx {
   sg::Buf color, perm, body_cnt, body_off, body_fill, body_adj, v_run, stats, barrier;
   // FP32 sweep data, packed in colour order (mixed-precision solve)
   sg::Buf pk_ab, pk_n, pk_c, pk_w, pk_r, v32, minv32;
+  // 3D contacts: basis rows n s t (9), angular rows (r_a x s, r_a x t) and (r_b x s, r_b x t)
+  // (6 each), forcing (3), Delassus block (6), impulse (3: current, candidate, best),
+  // (alpha, beta0, beta1) out (3); running velocities (2 double4 per body: v, omega).
+  int64_t ccap3 = 0;
+  sg::Buf E3, Aa3, Ab3, c3, W3, r3, r3a, r3b, ab3, vrun3;
   // buffers of the standalone FrictionSolver entry (kept apart from the scene)
   sg::Buf fs_m, fs_minv, fs_v0, fs_v2;
 
@@ -150,6 +158,25 @@ int ccd_batch(sg_ctx* ctx, int n, const double* q0a, const double* q1a, const do
 // Solver pipeline on a ContactProblem living in ctx buffers.
 int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp);
 int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc);
+// Body -> contact adjacency (ctx->body_off / body_adj, ascending contact order), the
+// solve counters cleared, and the contact colouring with its processing permutation
+// (ctx->perm, colour offsets in ctx->stats).  Shared by the 2D and 3D solvers.
+int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib);
+
+// Grid size of a cooperative launch: all blocks resident (at most max_per_sm per SM),
+// no more than the work needs.
+template <typename K>
+int coop_grid(sg_ctx* ctx, K kernel, long work, int block, int max_per_sm = 64) {
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, block, 0) != cudaSuccess || bps < 1) bps = 1;
+  long g = (long)(bps < max_per_sm ? bps : max_per_sm) * ctx->num_sms;
+  const long need = (work + block - 1) / block > 1 ? (work + block - 1) / block : 1;
+  return (int)(g < need ? g : need);
+}
+
+// RigidBody3D sphere scenes (sphere3d_kernels.cu).
+int sphere3d_update_inertia(sg_ctx* ctx, bool construction);
+int sphere3d_step(sg_ctx* ctx, sg_step_stats* out);
 
 int wait_timeout_selftest(sg_ctx* ctx);
 

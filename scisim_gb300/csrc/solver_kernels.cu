@@ -912,15 +912,6 @@ __global__ void k_wait_flag(const int* flag, int* status, unsigned long long spi
   *status = SG_OK;
 }
 
-template <typename K>
-int coop_grid(sg_ctx* ctx, K kernel, long work, int block = kBlock, int max_per_sm = 64) {
-  int bps = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, block, 0) != cudaSuccess || bps < 1) bps = 1;
-  long g = (long)std::min(bps, max_per_sm) * ctx->num_sms;
-  const long need = std::max(1L, (work + block - 1) / block);
-  return (int)std::min(g, need);
-}
-
 }  // namespace
 
 int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc) {
@@ -939,47 +930,56 @@ int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc) {
   return SG_OK;
 }
 
-int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) {
-  const int nb = P.nb, nc = P.nc;
+int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib) {
   cudaStream_t s = ctx->stream;
-  if (int r = ensure_solver_capacity(ctx, nb, nc)) return r;
   int* cnt = ctx->body_cnt.as<int>();
   int* off = ctx->body_off.as<int>();
   int* fill = ctx->body_fill.as<int>();
   int* adj = ctx->body_adj.as<int>();
   SolveStats* st = ctx->stats.as<SolveStats>();
   GridBarrier* gb = ctx->barrier.as<GridBarrier>();
-  const double2* n2 = reinterpret_cast<const double2*>(P.n);
-  double2* r2 = reinterpret_cast<double2*>(P.r);
-
   SG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)(nb + 1), s));
   SG_CUDA_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * (size_t)(nb + 1), s));
   SG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(SolveStats), s));
   if (nc > 0) {
-    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, cnt);
+    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, cnt);
     SG_CUDA_TRY(cudaGetLastError());
   }
   if (int r = scan_exclusive(ctx, cnt, off, nb)) return r;
-  if (nc > 0) {
-    k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, off, fill, adj);
-    k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
-    SG_CUDA_TRY(cudaGetLastError());
-  }
+  ctx->kernel_launches += nb > 0 ? 3 : 0;
+  if (nc == 0) return SG_OK;
+  k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, off, fill, adj);
+  k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
+  SG_CUDA_TRY(cudaGetLastError());
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->color.p, 0xff, sizeof(int) * (size_t)nc, s));
+  SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+  ColorArgs CA{nc, ia, ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit, 4096};
+  void* args[] = {&CA};
+  const int g = coop_grid(ctx, k_color_jp, nc, kBlock);
+  SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_color_jp, dim3(g), dim3(kBlock), args, 0, s));
+  ctx->kernel_launches += 4;  // body_count, body_fill, body_sort, colouring
+  return SG_OK;
+}
+
+int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) {
+  const int nb = P.nb, nc = P.nc;
+  cudaStream_t s = ctx->stream;
+  if (int r = ensure_solver_capacity(ctx, nb, nc)) return r;
+  int* off = ctx->body_off.as<int>();
+  int* adj = ctx->body_adj.as<int>();
+  SolveStats* st = ctx->stats.as<SolveStats>();
+  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  const double2* n2 = reinterpret_cast<const double2*>(P.n);
+  double2* r2 = reinterpret_cast<double2*>(P.r);
+
+  // Adjacency and colouring first: the velocity initialisation reads the adjacency.
+  if (int r = prepare_contact_graph(ctx, nb, nc, P.ia, P.ib)) return r;
   double2* vrun = ctx->v_run.as<double2>();
   k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                P.minv, vrun);
   SG_CUDA_TRY(cudaGetLastError());
 
   if (nc > 0) {
-    // Colouring.
-    SG_CUDA_TRY(cudaMemsetAsync(ctx->color.p, 0xff, sizeof(int) * (size_t)nc, s));
-    SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-    ColorArgs CA{nc, P.ia, P.ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit, 4096};
-    {
-      void* args[] = {&CA};
-      const int g = coop_grid(ctx, k_color_jp, nc);
-      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_color_jp, dim3(g), dim3(kBlock), args, 0, s));
-    }
     // Gauss-Seidel.
     SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
     GsArgs GA;
@@ -1044,9 +1044,9 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kGsBlock), args, 0, s));
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
     }
-    ctx->kernel_launches += 6;  // body_count, body_fill, body_sort, color, gs (+ scan below)
+    ctx->kernel_launches += 1;  // gs
   }
-  ctx->kernel_launches += 2 + (nb > 0 ? 3 : 0);  // vel_init, final_velocity, scan
+  ctx->kernel_launches += 2;  // vel_init, final_velocity
   k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                      P.m, P.minv, reinterpret_cast<double2*>(P.v2));
   SG_CUDA_TRY(cudaGetLastError());

@@ -1,0 +1,1340 @@
+// sphere3d_kernels.cu -- RigidBody3D spheres on sm_103a: split-Hamiltonian map, q1 grid
+// broad phase, sphere/plane narrow phase, velocity-dependent contact bases, 3x3 Delassus
+// blocks and the coloured block Gauss-Seidel Coulomb solve over 6-dof bodies.
+//
+// Reference path (breannansmith/scisim), one step of GeometricImpactFrictionMap::flow
+// (scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:267-442) driven by
+// RigidBody3DSim::flow (rigidbody3d/RigidBody3DSim.cpp:557-630):
+//   k_splitham        SplitHamMap::flow (rigidbody3d/UnconstrainedMaps/SplitHamMap.cpp:17-182),
+//                     gravity NearEarthGravityForce (rigidbody3d/Forces/NearEarthGravityForce.cpp:39-54),
+//                     q1 AABBs cm +- r (rigidbody3d/Geometry/RigidBodySphere.cpp:45-49)
+//   k_inertia         RigidBody3DState::updateMandMinv (rigidbody3d/RigidBody3DState.cpp:428-462)
+//   k_*3 grid         SpatialGridDetector::getPotentialOverlaps (rigidbody3d/SpatialGridDetector.cpp:110-137):
+//                     the all-pairs AABB-overlap set, lexicographic (i < j), from a uniform
+//                     grid whose cell exceeds every box, scanning 27 cells
+//   k_pair_*3         sphereSphereNarrowPhaseCollision (RigidBody3DSim.cpp:793-819): active at q1
+//   k_plane_*3        computeBodyPlaneActiveSetAllPairs (RigidBody3DSim.cpp:1414-1452), plane-major
+//   k_assemble3       computeContactBasis (SphereSphereConstraint.cpp:273-300,
+//                     StaticPlaneSphereConstraint.cpp:255-283, FrictionUtilities.cpp:19-29),
+//                     forcing terms (scisim/Constraints/Constraint.cpp:18-34, 92-126),
+//                     H rows (SphereSphereConstraint.cpp:229-271, StaticPlaneSphereConstraint.cpp:197-221),
+//                     Sobogus initialize3D / solve3D warm start (scisim/ConstrainedMaps/Sobogus.cpp:184-251,
+//                     486-518)
+//   k_gs3             RigidBodies3DSobogusInterface::solve (scisim/ConstrainedMaps/bogus/
+//                     RigidBody3DSobogusInterface.cpp:99-145) with So-bogus's GaussSeidel and
+//                     SOCLaw<3>: matrix-free through body velocities (v, omega) = v0 + M^-1 H^T r
+//   k_final_vel3      v2 = M^-1 (H^T r - f), f = -M v0
+//   k_extract3        alpha, beta (Sobogus.cpp:526-542)
+// Every FP64 expression keeps the operation order of the CPU restatement (products of
+// fixed-size matrices as sequential sums, no contraction: the library is built with
+// -fmad=false), so contact sets and solver iterates are bit-identical to it.  sin and cos
+// come from CUDA's math library, so orientations and angular velocities agree with the
+// host's to a few ulps rather than bit for bit.
+//
+// Layout in HBM: q = [x (3nb) | R row-major (9nb)], v = [v (3nb) | omega (3nb)] (SCISim's
+// VectorXs layouts), per-body r, m, 1/m, I0 (3), world inertia and inverse (9 each, row
+// major); contacts SoA: basis rows (9), angular rows (6 + 6), forcing (3), Delassus
+// block (6), mu, impulse (3); running velocities as two double4_32a per body.
+#include "ctx.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <utility>
+
+namespace sg {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kGs3Block = 256;
+inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
+
+struct Grid3 {
+  unsigned long long enc_min[3];
+  unsigned long long enc_max[3];
+  unsigned long long enc_ext[3];
+  double origin[3];
+  double h;
+  int dims[3];
+  int ncells;
+};
+
+// ---------------------------------------------------------------------------
+// Small fixed-size algebra (sequential sums, as the host restatement).
+__device__ __forceinline__ double dot3(const double* a, const double* b) {
+  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+__device__ __forceinline__ void cross3(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ void normalize3(double* v) {
+  const double z = dot3(v, v);
+  if (z > 0.0) {
+    const double s = sqrt(z);
+    v[0] = v[0] / s;
+    v[1] = v[1] / s;
+    v[2] = v[2] / s;
+  }
+}
+// y = A x (A row-major); y may alias x.
+__device__ __forceinline__ void matvec3(const double* A, const double* x, double* y) {
+  const double t0 = (A[0] * x[0] + A[1] * x[1]) + A[2] * x[2];
+  const double t1 = (A[3] * x[0] + A[4] * x[1]) + A[5] * x[2];
+  const double t2 = (A[6] * x[0] + A[7] * x[1]) + A[8] * x[2];
+  y[0] = t0;
+  y[1] = t1;
+  y[2] = t2;
+}
+__device__ __forceinline__ void matmul3(const double* A, const double* B, double* C) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[3 * i + j] = (A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j]) + A[3 * i + 2] * B[6 + j];
+}
+// R diag(d) R^T, element (i,j) = sum_k (R_ik d_k) R_jk.
+__device__ __forceinline__ void rdrt(const double* R, const double* d, double* out) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      out[3 * i + j] = ((R[3 * i] * d[0]) * R[3 * j] + (R[3 * i + 1] * d[1]) * R[3 * j + 1]) +
+                       (R[3 * i + 2] * d[2]) * R[3 * j + 2];
+}
+// Rotation by `angle` about the unit axis -e_axis (Rodrigues' formula); the axis
+// components are 0 or -1, so every product below is exact except 1 - cos.
+__device__ __forceinline__ void rot_neg_axis(int axis, double angle, double* R) {
+  const double c = cos(angle), s = sin(angle);
+  const double a0 = axis == 0 ? -1.0 : 0.0, a1 = axis == 1 ? -1.0 : 0.0, a2 = axis == 2 ? -1.0 : 0.0;
+  const double omc = 1.0 - c;
+  R[0] = (omc * a0) * a0 + c;
+  R[4] = (omc * a1) * a1 + c;
+  R[8] = (omc * a2) * a2 + c;
+  R[1] = (omc * a0) * a1 - s * a2;
+  R[3] = (omc * a0) * a1 + s * a2;
+  R[2] = (omc * a0) * a2 + s * a1;
+  R[6] = (omc * a0) * a2 - s * a1;
+  R[5] = (omc * a1) * a2 - s * a0;
+  R[7] = (omc * a1) * a2 + s * a0;
+}
+
+// ---------------------------------------------------------------------------
+// SplitHamMap::flow for one sphere with the state's world inertia Iw (the reference's
+// sparse M); gravity F = m g, no torque.  Optionally writes the q1 AABB.
+__global__ void k_splitham(int nb, double dt, double gx, double gy, double gz, const double* __restrict__ q0,
+                           const double* __restrict__ v0, const double* __restrict__ m,
+                           const double* __restrict__ I0, const double* __restrict__ Iw,
+                           const double* __restrict__ rad, double* __restrict__ q1, double* __restrict__ v1,
+                           double* __restrict__ aabb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double h = 0.5 * dt;
+  const double hdt = (0.5 * dt) * dt;
+  const double mi = m[i];
+  const double minv = 1.0 / mi;
+  const double g[3] = {gx, gy, gz};
+  double p[3], x1[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double F = mi * g[j];
+    p[j] = mi * v0[3 * i + j];
+    p[j] = p[j] + h * F;
+    x1[j] = q0[3 * i + j] + (dt * v0[3 * i + j] + (hdt * minv) * F);
+  }
+  double Iwi[9], w0[3], L[3];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Iwi[j] = Iw[9 * (size_t)i + j];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) w0[j] = v0[3 * (size_t)nb + 3 * i + j];
+  matvec3(Iwi, w0, L);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) L[j] = L[j] + h * 0.0;
+  const double I[3] = {I0[3 * i], I0[3 * i + 1], I0[3 * i + 2]};
+  double Rc[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Rc[j] = q0[3 * (size_t)nb + 9 * (size_t)i + j];
+  double pB[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) pB[k] = (Rc[k] * L[0] + Rc[3 + k] * L[1]) + Rc[6 + k] * L[2];
+  const int axes[5] = {2, 1, 0, 1, 2};
+#pragma unroll
+  for (int st = 0; st < 5; ++st) {
+    const int ax = axes[st];
+    const double ang = st == 2 ? (dt * pB[ax]) / I[ax] : (h * pB[ax]) / I[ax];
+    double Ri[9], Rf[9], tmp[9];
+    rot_neg_axis(ax, -ang, Ri);
+    matmul3(Rc, Ri, tmp);
+#pragma unroll
+    for (int j = 0; j < 9; ++j) Rc[j] = tmp[j];
+    rot_neg_axis(ax, ang, Rf);
+    matvec3(Rf, pB, pB);
+  }
+#pragma unroll
+  for (int j = 0; j < 9; ++j) q1[3 * (size_t)nb + 9 * (size_t)i + j] = Rc[j];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double F = mi * g[j];
+    p[j] = p[j] + h * F;
+    L[j] = L[j] + h * 0.0;
+    q1[3 * i + j] = x1[j];
+    v1[3 * i + j] = p[j] / mi;
+  }
+  const double di[3] = {1.0 / I[0], 1.0 / I[1], 1.0 / I[2]};
+  double Wm[9], w1[3];
+  rdrt(Rc, di, Wm);
+  matvec3(Wm, L, w1);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) v1[3 * (size_t)nb + 3 * i + j] = w1[j];
+  if (aabb) {
+    const double r = rad[i];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      aabb[6 * (size_t)i + j] = x1[j] - r;
+      aabb[6 * (size_t)i + 3 + j] = x1[j] + r;
+    }
+  }
+}
+
+// World inertia and its inverse from R (updateMandMinv).  At construction the
+// reference inserts I(row, col) at sparse entry (col, row) (RigidBody3DState.cpp:175-182).
+__global__ void k_inertia(int nb, const double* __restrict__ q, const double* __restrict__ I0,
+                          double* __restrict__ Iw, double* __restrict__ Iinv, int construction) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  double R[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) R[j] = q[3 * (size_t)nb + 9 * (size_t)i + j];
+  const double d[3] = {I0[3 * i], I0[3 * i + 1], I0[3 * i + 2]};
+  const double di[3] = {1.0 / d[0], 1.0 / d[1], 1.0 / d[2]};
+  double A[9], B[9];
+  rdrt(R, d, A);
+  rdrt(R, di, B);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int src = construction ? 3 * c + r : 3 * r + c;
+      Iw[9 * (size_t)i + 3 * r + c] = A[src];
+      Iinv[9 * (size_t)i + 3 * r + c] = B[src];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Broad phase on a uniform 3D grid.
+__global__ void k_bounds3_init(Grid3* g) {
+  for (int a = 0; a < 3; ++a) {
+    g->enc_min[a] = ~0ull;
+    g->enc_max[a] = 0ull;
+    g->enc_ext[a] = 0ull;
+  }
+}
+
+__global__ void k_bounds3(int n, const double* __restrict__ aabb, Grid3* g) {
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY}, ex[3] = {0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double lo = aabb[6 * (size_t)i + a], hi = aabb[6 * (size_t)i + 3 + a];
+      mn[a] = fmin(mn[a], lo);
+      mx[a] = fmax(mx[a], hi);
+      ex[a] = fmax(ex[a], hi - lo);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[a] = fmin(mn[a], __shfl_down_sync(0xffffffffu, mn[a], o));
+      mx[a] = fmax(mx[a], __shfl_down_sync(0xffffffffu, mx[a], o));
+      ex[a] = fmax(ex[a], __shfl_down_sync(0xffffffffu, ex[a], o));
+    }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&g->enc_min[a], f64_to_ordered(mn[a]));
+      atomicMax(&g->enc_max[a], f64_to_ordered(mx[a]));
+      atomicMax(&g->enc_ext[a], f64_to_ordered(ex[a]));
+    }
+  }
+}
+
+// Cell width strictly above the largest box extent: two overlapping boxes have min
+// corners in the same or adjacent cells, so 27 cells suffice.  The cell count is capped
+// at `cap` (h grows; larger cells stay correct).
+__global__ void k_grid3_setup(Grid3* g, long cap) {
+  double mn[3], span[3];
+  double e = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = ordered_to_f64(g->enc_min[a]);
+    span[a] = ordered_to_f64(g->enc_max[a]) - mn[a];
+    if (!isfinite(span[a]) || span[a] < 0.0) span[a] = 0.0;
+    e = fmax(e, ordered_to_f64(g->enc_ext[a]));
+  }
+  double h = e * (1.0 + 0x1p-20) + 1e-300;
+  if (!(h > 0.0) || !isfinite(h)) h = 1.0;
+  double d[3];
+  for (int a = 0; a < 3; ++a) d[a] = floor(span[a] / h) + 1.0;
+  while (d[0] * d[1] * d[2] > (double)cap) {
+    h = h * fmax(1.01, cbrt(d[0] * d[1] * d[2] / (double)cap));
+    for (int a = 0; a < 3; ++a) d[a] = floor(span[a] / h) + 1.0;
+  }
+  for (int a = 0; a < 3; ++a) {
+    g->origin[a] = isfinite(mn[a]) ? mn[a] : 0.0;
+    g->dims[a] = (int)d[a];
+  }
+  g->h = h;
+  g->ncells = (int)(d[0] * d[1] * d[2]);
+}
+
+__device__ __forceinline__ int cell_coord3(double x, double o, double h, int dim) {
+  const double f = (x - o) / h;
+  const int c = (f > 0.0) ? (int)f : 0;  // NaN -> 0
+  return c < dim ? c : dim - 1;
+}
+
+__global__ void k_cell_count3(int n, const double* __restrict__ aabb, const Grid3* __restrict__ g,
+                              int* __restrict__ cell_of, int* __restrict__ cell_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cx = cell_coord3(aabb[6 * (size_t)i], g->origin[0], g->h, g->dims[0]);
+  const int cy = cell_coord3(aabb[6 * (size_t)i + 1], g->origin[1], g->h, g->dims[1]);
+  const int cz = cell_coord3(aabb[6 * (size_t)i + 2], g->origin[2], g->h, g->dims[2]);
+  const int cell = cx + g->dims[0] * (cy + g->dims[1] * cz);
+  cell_of[i] = cell;
+  atomicAdd(&cell_count[cell], 1);
+}
+
+__global__ void k_cell_scatter3(int n, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+                                int* __restrict__ cell_fill, int* __restrict__ sorted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cell = cell_of[i];
+  sorted[cell_start[cell] + atomicAdd(&cell_fill[cell], 1)] = i;
+}
+
+struct Scan3 {
+  const double* aabb;
+  const Grid3* g;
+  const int* cell_start;
+  const int* sorted;
+  const double* x1;   // q1 positions (3 per body)
+  const double* rad;
+};
+
+// AABB::overlaps (rigidbody3d/SpatialGridDetector.cpp:8-25) then SphereSphereConstraint::isActive
+// at q1 (SphereSphereConstraint.cpp:9-12), for every j > i found in the 27 cells around the
+// cell of box i's min corner.
+template <typename F>
+__device__ __forceinline__ void visit_pairs3(const Scan3& s, int i, F&& f) {
+  double bi[6];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) bi[a] = s.aabb[6 * (size_t)i + a];
+  const Grid3& g = *s.g;
+  const int cx = cell_coord3(bi[0], g.origin[0], g.h, g.dims[0]);
+  const int cy = cell_coord3(bi[1], g.origin[1], g.h, g.dims[1]);
+  const int cz = cell_coord3(bi[2], g.origin[2], g.h, g.dims[2]);
+  const double xi[3] = {s.x1[3 * (size_t)i], s.x1[3 * (size_t)i + 1], s.x1[3 * (size_t)i + 2]};
+  const double ri = s.rad[i];
+  for (int z = max(cz - 1, 0); z <= min(cz + 1, g.dims[2] - 1); ++z)
+    for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y)
+      for (int x = max(cx - 1, 0); x <= min(cx + 1, g.dims[0] - 1); ++x) {
+        const int cell = x + g.dims[0] * (y + g.dims[1] * z);
+        const int e = s.cell_start[cell + 1];
+        for (int p = s.cell_start[cell]; p < e; ++p) {
+          const int j = s.sorted[p];
+          if (j <= i) continue;
+          const double* bj = s.aabb + 6 * (size_t)j;
+          if (bi[3] < bj[0] || bi[4] < bj[1] || bi[5] < bj[2]) continue;
+          if (bj[3] < bi[0] || bj[4] < bi[1] || bj[5] < bi[2]) continue;
+          const double d[3] = {xi[0] - s.x1[3 * (size_t)j], xi[1] - s.x1[3 * (size_t)j + 1],
+                               xi[2] - s.x1[3 * (size_t)j + 2]};
+          const double rs = ri + s.rad[j];
+          if (!(dot3(d, d) <= rs * rs)) continue;
+          f(j);
+        }
+      }
+}
+
+__global__ void k_pair_count3(int n, Scan3 s, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = 0;
+  visit_pairs3(s, i, [&](int) { ++c; });
+  cnt[i] = c;
+}
+
+__global__ void k_pair_write3(int n, Scan3 s, const int* __restrict__ off, int* __restrict__ out_a,
+                              int* __restrict__ out_b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int base = off[i];
+  int c = 0;
+  visit_pairs3(s, i, [&](int j) {
+    int p = base + c;
+    while (p > base && out_b[p - 1] > j) {
+      out_b[p] = out_b[p - 1];
+      --p;
+    }
+    out_b[p] = j;
+    ++c;
+  });
+  for (int k = 0; k < c; ++k) out_a[base + k] = i;
+}
+
+// StaticPlaneSphereConstraint::isActive at q1 (StaticPlaneSphereConstraint.cpp:13-17), plane-major.
+__global__ void k_plane_flags3(int nb, int np, const double* __restrict__ x1, const double* __restrict__ rad,
+                               const double* __restrict__ px, const double* __restrict__ pn, int* __restrict__ flag) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nb * np) return;
+  const int p = (int)(t / nb), i = (int)(t - (long)p * nb);
+  const double d[3] = {x1[3 * (size_t)i] - px[3 * p], x1[3 * (size_t)i + 1] - px[3 * p + 1],
+                       x1[3 * (size_t)i + 2] - px[3 * p + 2]};
+  const double n[3] = {pn[3 * p], pn[3 * p + 1], pn[3 * p + 2]};
+  flag[t] = (dot3(n, d) <= rad[i]) ? 1 : 0;
+}
+
+__global__ void k_plane_write3(int nb, int np, int npairs, const int* __restrict__ flag, const int* __restrict__ off,
+                               int* __restrict__ ia, int* __restrict__ ib) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nb * np) return;
+  if (!flag[t]) return;
+  const int p = (int)(t / nb), i = (int)(t - (long)p * nb);
+  const int k = npairs + off[t];
+  ia[k] = i;
+  ib[k] = -1 - p;
+}
+
+// ---------------------------------------------------------------------------
+// Contact assembly.
+struct Assemble3 {
+  int nb, nc;
+  const int* ia;
+  const int* ib;
+  const double* q0;
+  const double* v0;
+  const double* rad;
+  const double* minv;
+  const double* Iinv;
+  const double* plane_n;
+  double mu, CoR;
+  double* E;    // 9 per contact: n, s, t
+  double* Aa;   // 6: r_a x s, r_a x t
+  double* Ab;   // 6: r_b x s, r_b x t
+  double* c;    // 3
+  double* W;    // 6: w00 w01 w02 w11 w12 w22
+  double* mu_out;
+  double* r;    // 3
+};
+
+__device__ void orthogonal_vector(const double* n, double* o) {
+  const double ax = fabs(n[0]), ay = fabs(n[1]), az = fabs(n[2]);
+  o[0] = o[1] = o[2] = 0.0;
+  if (ax <= ay && ax <= az)
+    o[0] = 1.0;
+  else if (ay <= az)
+    o[1] = 1.0;
+  else
+    o[2] = 1.0;
+  const double d = dot3(n, o);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) o[j] = o[j] - d * n[j];
+  normalize3(o);
+}
+
+__global__ void k_assemble3(Assemble3 A) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.nc) return;
+  const int nb = A.nb;
+  const int a = A.ia[k], b = A.ib[k];
+  const bool has_b = b >= 0;
+  double n[3], ra[3], rb[3] = {0.0, 0.0, 0.0}, sv[3], vr[3];
+  const double* xa = A.q0 + 3 * (size_t)a;
+  const double* va = A.v0 + 3 * (size_t)a;
+  const double* wa = A.v0 + 3 * (size_t)nb + 3 * (size_t)a;
+  if (has_b) {
+    const double* xb = A.q0 + 3 * (size_t)b;
+    const double* vb = A.v0 + 3 * (size_t)b;
+    const double* wb = A.v0 + 3 * (size_t)nb + 3 * (size_t)b;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) n[j] = xa[j] - xb[j];
+    normalize3(n);
+    const double frac = A.rad[a] / (A.rad[a] + A.rad[b]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double p = xa[j] + frac * (xb[j] - xa[j]);
+      ra[j] = p - xa[j];
+      rb[j] = p - xb[j];
+    }
+    double ca[3], cb[3];
+    const double wa_[3] = {wa[0], wa[1], wa[2]}, wb_[3] = {wb[0], wb[1], wb[2]};
+    cross3(wa_, ra, ca);
+    cross3(wb_, rb, cb);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      sv[j] = ((va[j] + ca[j]) - vb[j]) - cb[j];
+      vr[j] = va[j] - vb[j];
+    }
+  } else {
+    const int pl = -1 - b;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) n[j] = A.plane_n[3 * pl + j];
+    const double nr = -A.rad[a];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ra[j] = nr * n[j];
+    double ca[3];
+    const double wa_[3] = {wa[0], wa[1], wa[2]};
+    cross3(wa_, ra, ca);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      sv[j] = (va[j] + ca[j]) - 0.0;
+      vr[j] = va[j] - 0.0;
+    }
+  }
+  // Basis [n s t]: s opposes the tangential relative velocity, t = n x s.
+  double s[3] = {sv[0], sv[1], sv[2]}, t[3], tmp[3];
+  cross3(n, s, tmp);
+  if (dot3(tmp, tmp) < 1.0e-9) {
+    orthogonal_vector(n, s);
+  } else {
+    const double d = dot3(s, n);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) s[j] = s[j] - d * n[j];
+    normalize3(s);
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) s[j] = s[j] * -1.0;
+  cross3(n, s, t);
+  normalize3(t);
+  double* E = A.E + 9 * (size_t)k;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    E[j] = n[j];
+    E[3 + j] = s[j];
+    E[6 + j] = t[j];
+  }
+  double as[3], at[3], bs[3] = {0.0, 0.0, 0.0}, bt[3] = {0.0, 0.0, 0.0};
+  cross3(ra, s, as);
+  cross3(ra, t, at);
+  if (has_b) {
+    cross3(rb, s, bs);
+    cross3(rb, t, bt);
+  }
+  double* Aa = A.Aa + 6 * (size_t)k;
+  double* Ab = A.Ab + 6 * (size_t)k;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Aa[j] = as[j];
+    Aa[3 + j] = at[j];
+    Ab[j] = bs[j];
+    Ab[3 + j] = bt[j];
+  }
+  // Forcing term w = n (CoR n.v + nrel) + s drel0 + t drel1 (kinematic velocities are zero).
+  const double ndotv = dot3(n, vr);
+  const double zero[3] = {0.0, 0.0, 0.0};
+  const double nrel = -dot3(zero, n);
+  const double drel0 = -dot3(zero, s), drel1 = -dot3(zero, t);
+  const double sc = A.CoR * ndotv + nrel;
+  double w[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) w[j] = ((0.0 + n[j] * sc) + s[j] * drel0) + t[j] * drel1;
+  A.c[3 * (size_t)k] = dot3(n, w);
+  A.c[3 * (size_t)k + 1] = dot3(s, w);
+  A.c[3 * (size_t)k + 2] = dot3(t, w);
+  // Delassus block W = H_a M_a^-1 H_a^T + H_b M_b^-1 H_b^T; the normal row has no angular part.
+  const double* B[3] = {n, s, t};
+  const double* AaR[3] = {nullptr, as, at};
+  const double* AbR[3] = {nullptr, bs, bt};
+  double Ia[9], Ib[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Ia[j] = A.Iinv[9 * (size_t)a + j];
+  if (has_b) {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) Ib[j] = A.Iinv[9 * (size_t)b + j];
+  }
+  const double ma = A.minv[a], mb = has_b ? A.minv[b] : 0.0;
+  double* Wk = A.W + 6 * (size_t)k;
+  int q = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      double wij = ma * dot3(B[i], B[j]);
+      if (i > 0) {
+        double x[3];
+        matvec3(Ia, AaR[j], x);
+        wij = wij + dot3(AaR[i], x);
+      }
+      if (has_b) {
+        double wb = mb * dot3(B[i], B[j]);
+        if (i > 0) {
+          double x[3];
+          matvec3(Ib, AbR[j], x);
+          wb = wb + dot3(AbR[i], x);
+        }
+        wij = wij + wb;
+      }
+      Wk[q++] = wij;
+    }
+  A.mu_out[k] = A.mu;
+  // Warm start from alpha = beta = 0 (the 3D geometric map has no impulse cache):
+  // r = alpha n + beta0 s + beta1 t, then local r = E^T r.
+  double rw[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) rw[j] = (0.0 * n[j] + 0.0 * s[j]) + 0.0 * t[j];
+  A.r[3 * (size_t)k] = dot3(n, rw);
+  A.r[3 * (size_t)k + 1] = dot3(s, rw);
+  A.r[3 * (size_t)k + 2] = dot3(t, rw);
+}
+
+// ---------------------------------------------------------------------------
+// Coulomb law, 3D: Fischer-Burmeister error in the mu-scaled self-dual cone (De Saxce
+// change of variable) and the local solve (take-off, stick, slide).
+__device__ double fb_error_3d(const double* r, const double* u, double mu) {
+  double ut2 = 0.0;
+  ut2 += u[1] * u[1];
+  ut2 += u[2] * u[2];
+  const double nut = sqrt(ut2);
+  if (mu == 0.0) {
+    const double fn = r[0] + u[0] - sqrt(r[0] * r[0] + u[0] * u[0]);
+    double e2 = fn * fn;
+    e2 += r[1] * r[1];
+    e2 += r[2] * r[2];
+    return sqrt(e2);
+  }
+  const double x[3] = {mu * r[0], r[1], r[2]};
+  const double y[3] = {u[0] + mu * nut, mu * u[1], mu * u[2]};
+  double z0 = 0.0;
+  z0 += x[0] * x[0];
+  z0 += x[1] * x[1];
+  z0 += x[2] * x[2];
+  z0 += y[0] * y[0];
+  z0 += y[1] * y[1];
+  z0 += y[2] * y[2];
+  const double zb0 = 2.0 * (x[0] * x[1] + y[0] * y[1]);
+  const double zb1 = 2.0 * (x[0] * x[2] + y[0] * y[2]);
+  double nzb2 = 0.0;
+  nzb2 += zb0 * zb0;
+  nzb2 += zb1 * zb1;
+  const double nzb = sqrt(nzb2);
+  double l1 = z0 - nzb;
+  if (l1 < 0.0) l1 = 0.0;
+  const double l2 = z0 + nzb;
+  const double s1 = sqrt(l1), s2 = sqrt(l2);
+  const double sq0 = 0.5 * (s1 + s2);
+  const double half_diff = 0.5 * (s2 - s1);
+  const double sq1 = (nzb > 0.0) ? half_diff * (zb0 / nzb) : half_diff;
+  const double sq2 = (nzb > 0.0) ? half_diff * (zb1 / nzb) : 0.0;
+  double e2 = 0.0;
+  const double p0 = x[0] + y[0] - sq0;
+  e2 += p0 * p0;
+  const double p1 = x[1] + y[1] - sq1;
+  e2 += p1 * p1;
+  const double p2 = x[2] + y[2] - sq2;
+  e2 += p2 * p2;
+  return sqrt(e2);
+}
+
+__device__ __forceinline__ void apply_w(const double* a, const double* rc, const double* b, double* u) {
+  u[0] = a[0] * rc[0] + a[1] * rc[1] + a[2] * rc[2] + b[0];
+  u[1] = a[1] * rc[0] + a[3] * rc[1] + a[4] * rc[2] + b[1];
+  u[2] = a[2] * rc[0] + a[4] * rc[1] + a[5] * rc[2] + b[2];
+}
+
+// Anisotropic sliding: root search on the sliding direction over the unit circle through
+// the rational chart d = +-((1-s^2), 2s)/(1+s^2), s in [-1, 1] per half circle; sign
+// changes of g = u_T x d on a 256-point grid per half are refined by bisection and the
+// admissible root with the smallest Coulomb error is kept.  Rarely reached (the fixed
+// point on the direction handles near-isotropic tangential blocks), so kept out of line.
+__device__ __noinline__ bool slide_root_search(const double* a, const double* b, double mu, double* r) {
+  const double a00 = a[0], a01 = a[1], a02 = a[2], a11 = a[3], a12 = a[4], a22 = a[5];
+  auto eval = [&](double s, double sign, double* out) -> bool {
+    const double den_s = 1.0 + s * s;
+    const double e0 = sign * (1.0 - s * s) / den_s, e1 = sign * (2.0 * s) / den_s;
+    const double den = a00 - mu * (a01 * e0 + a02 * e1);
+    if (!(den > 0.0)) return false;
+    const double n_ = -b[0] / den;
+    const double t0 = -mu * n_ * e0, t1 = -mu * n_ * e1;
+    const double v0 = a01 * n_ + a11 * t0 + a12 * t1 + b[1];
+    const double v1 = a02 * n_ + a12 * t0 + a22 * t1 + b[2];
+    out[0] = v0 * e1 - v1 * e0;
+    out[1] = v0 * e0 + v1 * e1;
+    out[2] = n_;
+    out[3] = t0;
+    out[4] = t1;
+    return true;
+  };
+  double best_e = INFINITY;
+  double best_r[3] = {0.0, 0.0, 0.0};
+  constexpr int kGrid = 256;
+  for (int half = 0; half < 2; ++half) {
+    const double sign = half == 0 ? 1.0 : -1.0;
+    double s_prev = -1.0, f_prev[5];
+    bool ok_prev = eval(s_prev, sign, f_prev);
+    for (int k = 1; k <= kGrid; ++k) {
+      const double s_cur = -1.0 + 2.0 * double(k) / double(kGrid);
+      double f_cur[5];
+      const bool ok_cur = eval(s_cur, sign, f_cur);
+      if (ok_prev && ok_cur && ((f_prev[0] <= 0.0) != (f_cur[0] <= 0.0))) {
+        double lo = s_prev, hi = s_cur, flo = f_prev[0];
+        double fm[5] = {f_cur[0], f_cur[1], f_cur[2], f_cur[3], f_cur[4]};
+        for (int it = 0; it < 80; ++it) {
+          const double mid = 0.5 * (lo + hi);
+          if (!eval(mid, sign, fm)) break;
+          if ((fm[0] <= 0.0) == (flo <= 0.0)) {
+            lo = mid;
+            flo = fm[0];
+          } else {
+            hi = mid;
+          }
+        }
+        if (fm[1] >= 0.0 && fm[2] >= 0.0) {
+          const double rc[3] = {fm[2], fm[3], fm[4]};
+          double u[3];
+          apply_w(a, rc, b, u);
+          const double e = fb_error_3d(rc, u, mu);
+          if (e < best_e) {
+            best_e = e;
+            best_r[0] = rc[0];
+            best_r[1] = rc[1];
+            best_r[2] = rc[2];
+          }
+        }
+      }
+      s_prev = s_cur;
+      ok_prev = ok_cur;
+      for (int i = 0; i < 5; ++i) f_prev[i] = f_cur[i];
+    }
+  }
+  if (best_e < INFINITY) {
+    r[0] = best_r[0];
+    r[1] = best_r[1];
+    r[2] = best_r[2];
+    return true;
+  }
+  return false;
+}
+
+__device__ __noinline__ void local_fallback_3d(const double* a, const double* b, double mu, double rs0, double rs1,
+                                               double rs2, bool slide_ok, double rn, double rt0, double rt1,
+                                               double* r) {
+  if (slide_root_search(a, b, mu, r)) return;
+  double best = INFINITY;
+  double br[3] = {0.0, 0.0, 0.0};
+  auto consider = [&](double x0, double x1, double x2) {
+    const double rc[3] = {x0, x1, x2};
+    double u[3];
+    apply_w(a, rc, b, u);
+    const double e = fb_error_3d(rc, u, mu);
+    if (e < best) {
+      best = e;
+      br[0] = x0;
+      br[1] = x1;
+      br[2] = x2;
+    }
+  };
+  consider(0.0, 0.0, 0.0);
+  if (rs0 >= 0.0) {
+    const double nt = sqrt(rs1 * rs1 + rs2 * rs2);
+    const double sc = (nt > mu * rs0 && nt > 0.0) ? (mu * rs0) / nt : 1.0;
+    consider(rs0, rs1 * sc, rs2 * sc);
+  }
+  if (slide_ok && rn >= 0.0) consider(rn, rt0, rt1);
+  r[0] = br[0];
+  r[1] = br[1];
+  r[2] = br[2];
+}
+
+// Local Coulomb problem u = W r + b, W = (w00 w01 w02 w11 w12 w22) SPD.
+__device__ __forceinline__ void local_solve_3d(const double* a, const double* b, double mu, double* r) {
+  if (b[0] >= 0.0) {
+    r[0] = r[1] = r[2] = 0.0;
+    return;
+  }
+  const double a00 = a[0], a01 = a[1], a02 = a[2], a11 = a[3], a12 = a[4], a22 = a[5];
+  const double c00 = a11 * a22 - a12 * a12;
+  const double c01 = a02 * a12 - a01 * a22;
+  const double c02 = a01 * a12 - a02 * a11;
+  const double c11 = a00 * a22 - a02 * a02;
+  const double c12 = a01 * a02 - a00 * a12;
+  const double c22 = a00 * a11 - a01 * a01;
+  const double det = a00 * c00 + a01 * c01 + a02 * c02;
+  const double rs0 = -(c00 * b[0] + c01 * b[1] + c02 * b[2]) / det;
+  const double rs1 = -(c01 * b[0] + c11 * b[1] + c12 * b[2]) / det;
+  const double rs2 = -(c02 * b[0] + c12 * b[1] + c22 * b[2]) / det;
+  if (rs0 >= 0.0 && sqrt(rs1 * rs1 + rs2 * rs2) <= mu * rs0) {
+    r[0] = rs0;
+    r[1] = rs1;
+    r[2] = rs2;
+    return;
+  }
+  double d0 = b[1], d1 = b[2];
+  {
+    const double nd = sqrt(d0 * d0 + d1 * d1);
+    if (nd > 0.0) {
+      d0 = d0 / nd;
+      d1 = d1 / nd;
+    } else {
+      d0 = 1.0;
+      d1 = 0.0;
+    }
+  }
+  double rn = 0.0, rt0 = 0.0, rt1 = 0.0, ut0 = 0.0, ut1 = 0.0;
+  bool slide_ok = false;
+  for (int it = 0; it < 64; ++it) {
+    const double den = a00 - mu * (a01 * d0 + a02 * d1);
+    if (!(den > 0.0)) break;
+    rn = -b[0] / den;
+    rt0 = -mu * rn * d0;
+    rt1 = -mu * rn * d1;
+    ut0 = a01 * rn + a11 * rt0 + a12 * rt1 + b[1];
+    ut1 = a02 * rn + a12 * rt0 + a22 * rt1 + b[2];
+    const double nu = sqrt(ut0 * ut0 + ut1 * ut1);
+    if (!(nu > 0.0)) {
+      slide_ok = true;
+      break;
+    }
+    const double e0 = ut0 / nu, e1 = ut1 / nu;
+    const double ch = fmax(fabs(e0 - d0), fabs(e1 - d1));
+    d0 = e0;
+    d1 = e1;
+    if (ch <= 1.0e-15) {
+      const double den2 = a00 - mu * (a01 * d0 + a02 * d1);
+      if (!(den2 > 0.0)) break;
+      rn = -b[0] / den2;
+      rt0 = -mu * rn * d0;
+      rt1 = -mu * rn * d1;
+      ut0 = a01 * rn + a11 * rt0 + a12 * rt1 + b[1];
+      ut1 = a02 * rn + a12 * rt0 + a22 * rt1 + b[2];
+      slide_ok = true;
+      break;
+    }
+  }
+  if (slide_ok && rn >= 0.0 && (ut0 * d0 + ut1 * d1) >= 0.0) {
+    r[0] = rn;
+    r[1] = rt0;
+    r[2] = rt1;
+    return;
+  }
+  local_fallback_3d(a, b, mu, rs0, rs1, rs2, slide_ok, rn, rt0, rt1, r);
+}
+
+// ---------------------------------------------------------------------------
+// Solver.  Running velocities: V[2i] = (v, 0), V[2i+1] = (omega, 0).
+struct Contacts3 {
+  const int* ia;
+  const int* ib;
+  const double* E;
+  const double* Aa;
+  const double* Ab;
+  const double* c;
+  const double* W;
+  const double* mu;
+};
+
+// Running velocities are written by other SMs between grid barriers: read at L2.
+__device__ __forceinline__ double4_32a ld4cg(const double4_32a* p) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  const double2 a = __ldcg(q), b = __ldcg(q + 1);
+  return make_double4_32a(a.x, a.y, b.x, b.y);
+}
+
+// u = H v + c at the current running velocities.
+__device__ __forceinline__ void local_u3(const Contacts3& C, int k, const double4_32a* V, double* u, int a, int b,
+                                        const double* E, const double* Aa, const double* Ab) {
+  const double4_32a la = ld4cg(&V[2 * a]), wa = ld4cg(&V[2 * a + 1]);
+  const double va[3] = {la.x, la.y, la.z}, oa[3] = {wa.x, wa.y, wa.z};
+  double vb[3] = {0.0, 0.0, 0.0}, ob[3] = {0.0, 0.0, 0.0};
+  const bool has_b = b >= 0;
+  if (has_b) {
+    const double4_32a lb = ld4cg(&V[2 * b]), wb = ld4cg(&V[2 * b + 1]);
+    vb[0] = lb.x;
+    vb[1] = lb.y;
+    vb[2] = lb.z;
+    ob[0] = wb.x;
+    ob[1] = wb.y;
+    ob[2] = wb.z;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double h = dot3(E + 3 * i, va);
+    if (i > 0) h = h + dot3(Aa + 3 * (i - 1), oa);
+    if (has_b) {
+      double hb = dot3(E + 3 * i, vb);
+      if (i > 0) hb = hb + dot3(Ab + 3 * (i - 1), ob);
+      h = h - hb;
+    }
+    u[i] = h + C.c[3 * (size_t)k + i];
+  }
+}
+
+__device__ __forceinline__ void load_contact(const Contacts3& C, int k, double* E, double* Aa, double* Ab) {
+#pragma unroll
+  for (int j = 0; j < 9; ++j) E[j] = C.E[9 * (size_t)k + j];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    Aa[j] = C.Aa[6 * (size_t)k + j];
+    Ab[j] = C.Ab[6 * (size_t)k + j];
+  }
+}
+
+__device__ __forceinline__ void gather_htr3(int body, const int* __restrict__ off, const int* __restrict__ adj,
+                                            const Contacts3& C, const double* r, double* hl, double* ha) {
+  hl[0] = hl[1] = hl[2] = 0.0;
+  ha[0] = ha[1] = ha[2] = 0.0;
+  const int e = off[body + 1];
+  for (int p = off[body]; p < e; ++p) {
+    const int k = adj[p];
+    const bool is_a = C.ia[k] == body;
+    const double sgn = is_a ? 1.0 : -1.0;
+    const double* E = C.E + 9 * (size_t)k;
+    const double* A = (is_a ? C.Aa : C.Ab) + 6 * (size_t)k;
+    const double r0 = r[3 * (size_t)k], r1 = r[3 * (size_t)k + 1], r2 = r[3 * (size_t)k + 2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double pl = (E[j] * r0 + E[3 + j] * r1) + E[6 + j] * r2;
+      const double pa = A[j] * r1 + A[3 + j] * r2;
+      hl[j] = hl[j] + sgn * pl;
+      ha[j] = ha[j] + sgn * pa;
+    }
+  }
+}
+
+__global__ void k_vel_init3(int nb, const int* __restrict__ off, const int* __restrict__ adj, Contacts3 C,
+                            const double* __restrict__ r, const double* __restrict__ v0,
+                            const double* __restrict__ minv, const double* __restrict__ Iinv, double4_32a* __restrict__ V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  double hl[3], ha[3], Ii[9], wa[3];
+  gather_htr3(i, off, adj, C, r, hl, ha);
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Ii[j] = Iinv[9 * (size_t)i + j];
+  matvec3(Ii, ha, wa);
+  const double mi = minv[i];
+  const double* vl = v0 + 3 * (size_t)i;
+  const double* va = v0 + 3 * (size_t)nb + 3 * (size_t)i;
+  V[2 * i] = make_double4_32a(vl[0] + mi * hl[0], vl[1] + mi * hl[1], vl[2] + mi * hl[2], 0.0);
+  V[2 * i + 1] = make_double4_32a(va[0] + wa[0], va[1] + wa[1], va[2] + wa[2], 0.0);
+}
+
+__global__ void k_final_vel3(int nb, const int* __restrict__ off, const int* __restrict__ adj, Contacts3 C,
+                             const double* __restrict__ r, const double* __restrict__ v0, const double* __restrict__ m,
+                             const double* __restrict__ minv, const double* __restrict__ Iw,
+                             const double* __restrict__ Iinv, double* __restrict__ v2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double* vl = v0 + 3 * (size_t)i;
+  const double* va = v0 + 3 * (size_t)nb + 3 * (size_t)i;
+  double* ol = v2 + 3 * (size_t)i;
+  double* oa = v2 + 3 * (size_t)nb + 3 * (size_t)i;
+  if (off[i + 1] == off[i]) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      ol[j] = vl[j];
+      oa[j] = va[j];
+    }
+    return;
+  }
+  double hl[3], ha[3], Lw[3], rhs[3], wa[3], M[9];
+  gather_htr3(i, off, adj, C, r, hl, ha);
+#pragma unroll
+  for (int j = 0; j < 9; ++j) M[j] = Iw[9 * (size_t)i + j];
+  const double w0[3] = {va[0], va[1], va[2]};
+  matvec3(M, w0, Lw);
+  const double mi = m[i], ivm = minv[i];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double fl = -(mi * vl[j]);
+    ol[j] = ivm * (hl[j] - fl);
+    rhs[j] = ha[j] - (-Lw[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 9; ++j) M[j] = Iinv[9 * (size_t)i + j];
+  matvec3(M, rhs, wa);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) oa[j] = wa[j];
+}
+
+__global__ void k_extract3(int nc, const double* __restrict__ E3, const double* __restrict__ r, double* __restrict__ ab) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const double* E = E3 + 9 * (size_t)k;
+  const double r0 = r[3 * (size_t)k], r1 = r[3 * (size_t)k + 1], r2 = r[3 * (size_t)k + 2];
+  double rw[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) rw[j] = (E[j] * r0 + E[3 + j] * r1) + E[6 + j] * r2;
+  ab[3 * (size_t)k] = dot3(rw, E);
+  ab[3 * (size_t)k + 1] = dot3(rw, E + 3);
+  ab[3 * (size_t)k + 2] = dot3(rw, E + 6);
+}
+
+struct Gs3Args {
+  int nc;
+  Contacts3 C;
+  const double* minv;
+  const double* Iinv;
+  const int* perm;
+  double* r;
+  double* r_a;
+  double* r_b;
+  double4_32a* V;
+  SolveStats* st;
+  GridBarrier* gb;
+  unsigned long long spin;
+  double tol;
+  unsigned max_iters;
+  unsigned eval_every;
+};
+
+__device__ __forceinline__ void gs_update3(const Gs3Args& A, int k) {
+  const Contacts3& C = A.C;
+  const int a = C.ia[k], b = C.ib[k];
+  const bool has_b = b >= 0;
+  double E[9], Aa[6], Ab[6];
+  load_contact(C, k, E, Aa, Ab);
+  double u[3];
+  local_u3(C, k, A.V, u, a, b, E, Aa, Ab);
+  const double r0 = __ldcg(&A.r[3 * (size_t)k]), r1 = __ldcg(&A.r[3 * (size_t)k + 1]),
+               r2 = __ldcg(&A.r[3 * (size_t)k + 2]);
+  double W[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) W[j] = C.W[6 * (size_t)k + j];
+  const double bt[3] = {u[0] - ((W[0] * r0 + W[1] * r1) + W[2] * r2), u[1] - ((W[1] * r0 + W[3] * r1) + W[4] * r2),
+                        u[2] - ((W[2] * r0 + W[4] * r1) + W[5] * r2)};
+  double rn[3];
+  local_solve_3d(W, bt, C.mu[k], rn);
+  const double d0 = rn[0] - r0, d1 = rn[1] - r1, d2 = rn[2] - r2;
+  double pl[3], pa[3], pb[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    pl[j] = (E[j] * d0 + E[3 + j] * d1) + E[6 + j] * d2;
+    pa[j] = Aa[j] * d1 + Aa[3 + j] * d2;
+    pb[j] = Ab[j] * d1 + Ab[3 + j] * d2;
+  }
+  double Ii[9], wa[3];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)a + j];
+  matvec3(Ii, pa, wa);
+  const double ma = A.minv[a];
+  {
+    const double4_32a la = ld4cg(&A.V[2 * a]), oa = ld4cg(&A.V[2 * a + 1]);
+    A.V[2 * a] = make_double4_32a(la.x + ma * pl[0], la.y + ma * pl[1], la.z + ma * pl[2], 0.0);
+    A.V[2 * a + 1] = make_double4_32a(oa.x + wa[0], oa.y + wa[1], oa.z + wa[2], 0.0);
+  }
+  if (has_b) {
+    double wb[3];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)b + j];
+    matvec3(Ii, pb, wb);
+    const double mb = A.minv[b];
+    const double4_32a lb = ld4cg(&A.V[2 * b]), ob = ld4cg(&A.V[2 * b + 1]);
+    A.V[2 * b] = make_double4_32a(lb.x - mb * pl[0], lb.y - mb * pl[1], lb.z - mb * pl[2], 0.0);
+    A.V[2 * b + 1] = make_double4_32a(ob.x - wb[0], ob.y - wb[1], ob.z - wb[2], 0.0);
+  }
+  A.r[3 * (size_t)k] = rn[0];
+  A.r[3 * (size_t)k + 1] = rn[1];
+  A.r[3 * (size_t)k + 2] = rn[2];
+}
+
+__global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval_every = A.eval_every ? A.eval_every : 1u;
+  double* best = A.r_a;
+  double* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false;
+  unsigned it = 0;
+  unsigned n_eval = 0;
+  for (it = 1; it <= A.max_iters; ++it) {
+    for (int col = 0; col < ncol; ++col) {
+      const int e = s_off[col + 1];
+      for (int s = s_off[col] + tid; s < e; s += nthr) gs_update3(A, A.perm[s]);
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+    }
+    if (it % eval_every == 0) {
+      double emax = 0.0;
+      for (int k = tid; k < A.nc; k += nthr) {
+        const int a = A.C.ia[k], b = A.C.ib[k];
+        double E[9], Aa[6], Ab[6], u[3];
+        load_contact(A.C, k, E, Aa, Ab);
+        local_u3(A.C, k, A.V, u, a, b, E, Aa, Ab);
+        const double rk[3] = {__ldcg(&A.r[3 * (size_t)k]), __ldcg(&A.r[3 * (size_t)k + 1]),
+                              __ldcg(&A.r[3 * (size_t)k + 2])};
+        cand[3 * (size_t)k] = rk[0];
+        cand[3 * (size_t)k + 1] = rk[1];
+        cand[3 * (size_t)k + 2] = rk[2];
+        emax = nanmax(emax, fb_error_3d(rk, u, A.C.mu[k]));
+      }
+      emax = block_nanmax(emax);
+      const int slot = n_eval % 3;
+      if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+      if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+      ++n_eval;
+      if (err < err_best) {
+        err_best = err;
+        double* t = best;
+        best = cand;
+        cand = t;
+      }
+      if (err < A.tol) {
+        converged = true;
+        break;
+      }
+    }
+  }
+  if (!converged) {
+    if (err_best < INFINITY)
+      for (int k = tid; k < 3 * A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+    it = A.max_iters;
+  }
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps64 = it;
+    A.st->evals = n_eval;
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+int sphere3d_update_inertia(sg_ctx* ctx, bool construction) {
+  const int nb = ctx->nb;
+  if (nb <= 0) return SG_OK;
+  k_inertia<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(nb, ctx->q.as<double>(), ctx->I0.as<double>(),
+                                                        ctx->Iw.as<double>(), ctx->Iinv.as<double>(),
+                                                        construction ? 1 : 0);
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+static int ensure_contacts3(sg_ctx* ctx, int64_t nc) {
+  if (nc <= ctx->ccap3 && ctx->E3.p) return SG_OK;
+  const int64_t cap = std::max<int64_t>(nc + nc / 4 + 64, 1024);
+  const size_t c = (size_t)cap;
+  if (int r = grow(ctx->ia, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->ib, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->mu, sizeof(double) * c)) return r;
+  if (int r = grow(ctx->E3, sizeof(double) * 9 * c)) return r;
+  if (int r = grow(ctx->Aa3, sizeof(double) * 6 * c)) return r;
+  if (int r = grow(ctx->Ab3, sizeof(double) * 6 * c)) return r;
+  if (int r = grow(ctx->c3, sizeof(double) * 3 * c)) return r;
+  if (int r = grow(ctx->W3, sizeof(double) * 6 * c)) return r;
+  if (int r = grow(ctx->r3, sizeof(double) * 3 * c)) return r;
+  if (int r = grow(ctx->r3a, sizeof(double) * 3 * c)) return r;
+  if (int r = grow(ctx->r3b, sizeof(double) * 3 * c)) return r;
+  if (int r = grow(ctx->ab3, sizeof(double) * 3 * c)) return r;
+  ctx->ccap3 = cap;
+  return SG_OK;
+}
+
+static int splitham(sg_ctx* ctx, const double* v0, bool with_aabb) {
+  const int nb = ctx->nb;
+  const double* g = ctx->cfg.gravity;
+  k_splitham<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(
+      nb, ctx->cfg.dt, g[0], g[1], g[2], ctx->q.as<double>(), v0, ctx->m.as<double>(), ctx->I0.as<double>(),
+      ctx->Iw.as<double>(), ctx->r.as<double>(), ctx->q1.as<double>(), ctx->v1.as<double>(),
+      with_aabb ? ctx->aabb.as<double>() : nullptr);
+  SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+// One GeometricImpactFrictionMap::flow step of a sphere scene (cache forced NONE in 3D:
+// rigidbody3dutils/RigidBody3DSceneParser.cpp:1877-1880), then updateMandMinv.
+int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
+  const int nb = ctx->nb, np = ctx->np;
+  cudaStream_t s = ctx->stream;
+  sg_step_stats st{};
+  if (nb == 0) {
+    if (out) *out = st;
+    return SG_OK;
+  }
+  // Predictor and q1 AABBs.
+  if (int r = splitham(ctx, ctx->v.as<double>(), true)) return r;
+  // Grid.
+  const long cap = 4L * nb + 64;
+  if (int r = grow(ctx->grid, sizeof(Grid3))) return r;
+  if (int r = grow(ctx->cell_count, sizeof(int) * (size_t)(cap + 1))) return r;
+  if (int r = grow(ctx->cell_start, sizeof(int) * (size_t)(cap + 1))) return r;
+  if (int r = grow(ctx->cell_fill, sizeof(int) * (size_t)(cap + 1))) return r;
+  if (int r = grow(ctx->cell_of, sizeof(int) * (size_t)nb)) return r;
+  if (int r = grow(ctx->sorted, sizeof(int) * (size_t)nb)) return r;
+  if (int r = grow(ctx->pair_cnt, sizeof(int) * (size_t)(nb + 1))) return r;
+  if (int r = grow(ctx->pair_off, sizeof(int) * (size_t)(nb + 1))) return r;
+  Grid3* g = ctx->grid.as<Grid3>();
+  const double* aabb = ctx->aabb.as<double>();
+  k_bounds3_init<<<1, 1, 0, s>>>(g);
+  k_bounds3<<<std::max(1, std::min(blocks_for(nb), ctx->num_sms * 8)), kBlock, 0, s>>>(nb, aabb, g);
+  k_grid3_setup<<<1, 1, 0, s>>>(g, cap);
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_count.p, 0, sizeof(int) * (size_t)(cap + 1), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_fill.p, 0, sizeof(int) * (size_t)(cap + 1), s));
+  k_cell_count3<<<blocks_for(nb), kBlock, 0, s>>>(nb, aabb, g, ctx->cell_of.as<int>(), ctx->cell_count.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->cell_count.as<int>(), ctx->cell_start.as<int>(), (int)cap)) return r;
+  k_cell_scatter3<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ctx->cell_start.as<int>(),
+                                                   ctx->cell_fill.as<int>(), ctx->sorted.as<int>());
+  Scan3 sc{aabb, g, ctx->cell_start.as<int>(), ctx->sorted.as<int>(), ctx->q1.as<double>(), ctx->r.as<double>()};
+  k_pair_count3<<<blocks_for(nb), kBlock, 0, s>>>(nb, sc, ctx->pair_cnt.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->pair_cnt.as<int>(), ctx->pair_off.as<int>(), nb)) return r;
+  // Planes.
+  const long t = (long)nb * np;
+  if (int r = grow(ctx->plane_flag, sizeof(int) * (size_t)(t + 1))) return r;
+  if (int r = grow(ctx->plane_off, sizeof(int) * (size_t)(t + 1))) return r;
+  if (t > 0) {
+    k_plane_flags3<<<blocks_for(t), kBlock, 0, s>>>(nb, np, ctx->q1.as<double>(), ctx->r.as<double>(),
+                                                    ctx->plane_x.as<double>(), ctx->plane_n.as<double>(),
+                                                    ctx->plane_flag.as<int>());
+    SG_CUDA_TRY(cudaGetLastError());
+    if (int r = scan_exclusive(ctx, ctx->plane_flag.as<int>(), ctx->plane_off.as<int>(), (int)t)) return r;
+  } else {
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->plane_off.p, 0, sizeof(int), s));
+  }
+  int totals[2] = {0, 0};
+  SG_CUDA_TRY(cudaMemcpyAsync(&totals[0], ctx->pair_off.as<int>() + nb, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(&totals[1], ctx->plane_off.as<int>() + t, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  const int npairs = totals[0], nplanes = totals[1];
+  const int nc = npairs + nplanes;
+  // splitham 1, bounds 3, cell count 1, scan 3, scatter 1, pair count 1, scan 3, planes 1 + 3
+  ctx->kernel_launches += 14 + (t > 0 ? 4 : 0);
+  ctx->steps += 1;
+  ctx->contacts_total += (uint64_t)nc;
+  st.n_contacts = nc;
+  st.n_ball_ball = npairs;
+  st.n_ball_plane = nplanes;
+  ctx->last_nc = nc;
+  ctx->last_nbb = npairs;
+  if (nc == 0) {
+    std::swap(ctx->q, ctx->q1);
+    std::swap(ctx->v, ctx->v1);
+    if (int r = sphere3d_update_inertia(ctx, false)) return r;
+    ctx->kernel_launches += 1;
+    st.succeeded = 1;
+    if (out) *out = st;
+    return SG_OK;
+  }
+  if (int r = ensure_contacts3(ctx, nc)) return r;
+  int* ia = ctx->ia.as<int>();
+  int* ib = ctx->ib.as<int>();
+  k_pair_write3<<<blocks_for(nb), kBlock, 0, s>>>(nb, sc, ctx->pair_off.as<int>(), ia, ib);
+  if (t > 0)
+    k_plane_write3<<<blocks_for(t), kBlock, 0, s>>>(nb, np, npairs, ctx->plane_flag.as<int>(),
+                                                    ctx->plane_off.as<int>(), ia, ib);
+  SG_CUDA_TRY(cudaGetLastError());
+  Assemble3 A;
+  A.nb = nb;
+  A.nc = nc;
+  A.ia = ia;
+  A.ib = ib;
+  A.q0 = ctx->q.as<double>();
+  A.v0 = ctx->v.as<double>();
+  A.rad = ctx->r.as<double>();
+  A.minv = ctx->minv.as<double>();
+  A.Iinv = ctx->Iinv.as<double>();
+  A.plane_n = ctx->plane_n.as<double>();
+  A.mu = ctx->cfg.mu;
+  A.CoR = ctx->cfg.CoR;
+  A.E = ctx->E3.as<double>();
+  A.Aa = ctx->Aa3.as<double>();
+  A.Ab = ctx->Ab3.as<double>();
+  A.c = ctx->c3.as<double>();
+  A.W = ctx->W3.as<double>();
+  A.mu_out = ctx->mu.as<double>();
+  A.r = ctx->r3.as<double>();
+  k_assemble3<<<blocks_for(nc), kBlock, 0, s>>>(A);
+  SG_CUDA_TRY(cudaGetLastError());
+
+  // Solve.
+  if (int r = ensure_solver_capacity(ctx, nb, nc)) return r;
+  if (int r = grow(ctx->vrun3, sizeof(double4_32a) * 2 * (size_t)nb)) return r;
+  if (int r = grow(ctx->v2, sizeof(double) * 6 * (size_t)nb)) return r;
+  if (int r = prepare_contact_graph(ctx, nb, nc, ia, ib)) return r;
+  const int* off = ctx->body_off.as<int>();
+  const int* adj = ctx->body_adj.as<int>();
+  Contacts3 C{ia, ib, A.E, A.Aa, A.Ab, A.c, A.W, A.mu_out};
+  double4_32a* V = ctx->vrun3.as<double4_32a>();
+  k_vel_init3<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, C, A.r, ctx->v.as<double>(), ctx->minv.as<double>(),
+                                                ctx->Iinv.as<double>(), V);
+  SG_CUDA_TRY(cudaGetLastError());
+  SolveStats* sst = ctx->stats.as<SolveStats>();
+  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+  Gs3Args G;
+  G.nc = nc;
+  G.C = C;
+  G.minv = ctx->minv.as<double>();
+  G.Iinv = ctx->Iinv.as<double>();
+  G.perm = ctx->perm.as<int>();
+  G.r = A.r;
+  G.r_a = ctx->r3a.as<double>();
+  G.r_b = ctx->r3b.as<double>();
+  G.V = V;
+  G.st = sst;
+  G.gb = gb;
+  G.spin = ctx->spin_limit;
+  G.tol = ctx->cfg.tol;
+  G.max_iters = ctx->cfg.max_iters;
+  G.eval_every = ctx->cfg.eval_every;
+  {
+    void* args[] = {&G};
+    const int grid = coop_grid(ctx, k_gs3, nc, kGs3Block, 1);
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs3, dim3(grid), dim3(kGs3Block), args, 0, s));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+  }
+  k_final_vel3<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, C, A.r, ctx->v.as<double>(), ctx->m.as<double>(),
+                                                 ctx->minv.as<double>(), ctx->Iw.as<double>(), ctx->Iinv.as<double>(),
+                                                 ctx->v2.as<double>());
+  k_extract3<<<blocks_for(nc), kBlock, 0, s>>>(nc, A.E, A.r, ctx->ab3.as<double>());
+  SG_CUDA_TRY(cudaGetLastError());
+  SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, sst, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  // pair write, plane write, assemble, vel init, gs, final velocity, extract
+  ctx->kernel_launches += 6 + (t > 0 ? 1 : 0);
+  if (ctx->h_stats.status == SG_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its spin limit");
+    return SG_DEVICE_TIMEOUT;
+  }
+  if (ctx->h_stats.status == SG_CAPACITY) {
+    set_error("contact colouring exceeded 64 colours or its round limit");
+    return SG_CAPACITY;
+  }
+  ctx->gs_launches += 1;
+  ctx->contact_sweeps += (uint64_t)ctx->h_stats.sweeps64 * (uint64_t)nc;
+  ctx->contact_evals += (uint64_t)ctx->h_stats.evals * (uint64_t)nc;
+  if (ctx->profile) {
+    float ms = 0.f;
+    SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
+    ctx->gs_ms += ms;
+  }
+  st.iterations = ctx->h_stats.iterations;
+  st.succeeded = ctx->h_stats.converged;
+  st.error = ctx->h_stats.error;
+  st.n_colors = (uint32_t)ctx->h_stats.n_colors;
+  // Final map with the post-impact velocity, then the world inertia of the new state.
+  if (int r = splitham(ctx, ctx->v2.as<double>(), false)) return r;
+  std::swap(ctx->q, ctx->q1);
+  std::swap(ctx->v, ctx->v1);
+  if (int r = sphere3d_update_inertia(ctx, false)) return r;
+  ctx->kernel_launches += 2;
+  if (out) *out = st;
+  return st.succeeded ? SG_OK : SG_NOT_CONVERGED;
+}
+
+}  // namespace sg

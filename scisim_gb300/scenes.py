@@ -11,6 +11,11 @@ No public dataset is involved: every scene is generated from a fixed seed.
                   fill of a 40 x 60 box (area fraction ~0.5) built by size-sorted
                   shelf packing with random slack, rows shuffled, bodies permuted;
                   four walls; gravity -9.81, dt 0.005, CoR 0, mu 0.4
+  sphere_pile     65,536 spheres, r ~ U[0.05, 0.1], density 1, jittered lattice of spacing
+                  0.2 filling a 6 x 6 footprint (volume fraction ~0.18 of a 6 x 6 x 20
+                  box), v ~ N(0, 0.1^2), omega ~ N(0, 1), identity orientations; floor
+                  and four walls; gravity (0, -9.81, 0), split-Hamiltonian dt 0.004,
+                  CoR 0.2, mu 0.6
 """
 from __future__ import annotations
 
@@ -89,6 +94,46 @@ def dense_pile(n: int = 262144, seed: int = 2, width: float = 40.0, height: floa
     plane_n = np.array([[0.0, 1.0], [1.0, 0.0], [-1.0, 0.0], [0.0, -1.0]])
     return dict(q=q.reshape(-1), v=v, r=r, m=m, plane_x=plane_x, plane_n=plane_n, dt=0.005, gravity=(0.0, -9.81),
                 CoR=0.0, mu=0.4, tol=1e-6, max_iters=5000, name="dense_pile_%d" % n)
+
+
+def sphere_mass_inertia(r, density=1.0):
+    """Mass and principal moment of solid spheres, in the operation order of
+    RigidBodySphere::computeMassAndInertia (rigidbody3d/Geometry/RigidBodySphere.cpp:10-18)."""
+    r = np.asarray(r, dtype=np.float64)
+    m = 4.0 * math.pi * r * r * r / 3.0
+    i = 2.0 * m * r * r / 5.0
+    return m * density, i * density
+
+
+def sphere_pile(n: int = 65536, seed: int = 5, width: float = 6.0, depth: float = 6.0, rmin: float = 0.05,
+                rmax: float = 0.1, spacing: float = 0.2):
+    """Spheres on a jittered lattice above the floor y = 0 inside walls x in [0, width],
+    z in [0, depth].  Lattice sites are `spacing` apart and every sphere stays inside its
+    site's cube, so the initial configuration has no overlaps."""
+    if 2.0 * rmax > spacing:
+        raise ValueError("sphere wider than a lattice site")
+    rng = np.random.default_rng(seed)
+    nx, nz = int(width / spacing), int(depth / spacing)
+    per_layer = nx * nz
+    layers = -(-n // per_layer)
+    idx = np.arange(n)
+    iy, rem = np.divmod(idx, per_layer)
+    iz, ix = np.divmod(rem, nx)
+    r = rng.uniform(rmin, rmax, n)
+    slack = 0.5 * spacing - r - 1e-4
+    centre = np.stack([(ix + 0.5) * spacing, (iy + 0.5) * spacing, (iz + 0.5) * spacing], axis=1)
+    x = centre + rng.uniform(-1.0, 1.0, (n, 3)) * slack[:, None]
+    perm = rng.permutation(n)
+    x, r = x[perm], r[perm]
+    m, i0 = sphere_mass_inertia(r)
+    R = np.tile(np.eye(3).reshape(-1), n)
+    q = np.concatenate([x.reshape(-1), R])
+    v = np.concatenate([rng.normal(0.0, 0.1, 3 * n), rng.normal(0.0, 1.0, 3 * n)])
+    plane_x = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [width, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, depth]])
+    plane_n = np.array([[0.0, 1.0, 0.0], [1.0, 0.0, 0.0], [-1.0, 0.0, 0.0], [0.0, 0.0, 1.0], [0.0, 0.0, -1.0]])
+    del layers
+    return dict(q=q, v=v, r=r, m=m, I0=np.repeat(i0, 3), plane_x=plane_x, plane_n=plane_n, dt=0.004,
+                gravity=(0.0, -9.81, 0.0), CoR=0.2, mu=0.6, tol=1e-6, max_iters=5000, name="sphere_pile_%d" % n)
 
 
 def min_gap(q, r, plane_x=None, plane_n=None):

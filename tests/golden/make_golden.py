@@ -16,6 +16,8 @@ Run in a checkout that has the reference sources (default location given by
                                     (assets/ball2d/tests_friction/ball_plane/mu_0p5/*)
                                     with the tolerances registered in
                                     ball2dcli/CMakeLists.txt:78-98
+  sphere_inertia.json               the sphere mass/inertia known answer of
+                                    rigidbody3dtests/rigidbody3d_inertia_tests.cpp:17-47
 """
 from __future__ import annotations
 
@@ -121,6 +123,17 @@ def extract_slope_scenes(ref):
     return scenes
 
 
+def extract_sphere_inertia(ref):
+    src = open(os.path.join(ref, "rigidbody3dtests", "rigidbody3d_inertia_tests.cpp")).read()
+    body = src.split("static int testSpherePoolBreak()")[1].split("static int")[0]
+    r = re.search(r"RigidBodySphere sphere\{ %s \};" % _num, body).group(1)
+    rho = re.search(r"computeMassAndInertia\( %s," % _num, body).group(1)
+    M, tolM = re.search(r"fabs\( M - %s \) > %s" % (_num, _num), body).groups()
+    I, tolI = re.search(r"Vector3s::Constant\( %s \) \)\.lpNorm<Eigen::Infinity>\(\) > %s" % (_num, _num),
+                        body).groups()
+    return [dict(r=float(r), density=float(rho), M=float(M), I=float(I), tol_M=float(tolM), tol_I=float(tolI))]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -145,6 +158,8 @@ def main():
         json.dump(extract_ccd_cases(args.ref), fh, indent=1)
     with open(os.path.join(HERE, "slope_scenes.json"), "w") as fh:
         json.dump(extract_slope_scenes(args.ref), fh, indent=1)
+    with open(os.path.join(HERE, "sphere_inertia.json"), "w") as fh:
+        json.dump(extract_sphere_inertia(args.ref), fh, indent=1)
 
 
 if __name__ == "__main__":
