@@ -93,10 +93,11 @@ def test_sphere3d_frictionless_and_restitution(gpulib, oracle):
 
 
 def test_sphere3d_free_flight(gpulib, oracle):
-    s = make_scene(n=64, seed=2, width=4.0, depth=4.0)
+    # one layer of 8 x 8 spheres on a 0.5 lattice (gaps >= 0.3), far above the floor: no contacts
+    s = scenes.sphere_pile(n=64, seed=2, width=4.0, depth=4.0, spacing=0.5)
     q = s["q"].copy()
     nb = s["r"].shape[0]
-    q[1: 3 * nb: 3] += 5.0  # far above the floor, still on the lattice (no contacts)
+    q[1: 3 * nb: 3] += 5.0
     s2 = dict(s, q=q)
     ctx = gpu_ctx(gpulib, s2)
     sim = oracle_sim(oracle, s2)
