@@ -98,7 +98,7 @@ def test_sphere3d_free_flight(gpulib, oracle):
     q = s["q"].copy()
     nb = s["r"].shape[0]
     q[1: 3 * nb: 3] += 5.0
-    s2 = dict(s, q=q)
+    s2 = dict(s, q=q, plane_x=s["plane_x"][:1], plane_n=s["plane_n"][:1])  # floor only
     ctx = gpu_ctx(gpulib, s2)
     sim = oracle_sim(oracle, s2)
     for _ in range(5):
