@@ -106,6 +106,29 @@ SG_API int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const do
                               const double* m, const double* I0, int32_t np, const double* plane_x,
                               const double* plane_n);
 
+/* Uploads n_scenes independent Ball2D scenes stepped together (no counterpart in the
+ * reference, whose driver steps one Ball2DSim; each scene evolves exactly as
+ * Ball2DSim::flow would step it alone, ball2d/Ball2DSim.cpp:305-326).  Scene s owns bodies
+ * [body_off[s], body_off[s+1]) of q, v (interleaved, 2 per body), r, m and planes
+ * [plane_off[s], plane_off[s+1]) of plane_x, plane_n (2 per plane); mu[s] and CoR[s] are
+ * its coefficients.  Contacts never join bodies of different scenes; each scene's
+ * Gauss-Seidel solve stops at its own tolerance (or max_iters) and keeps its own best
+ * iterate.  sg_step then runs the whole batch from a CUDA graph of 8 steps with device-side
+ * contact counts; a chunk whose contacts overflow the capacity is re-run from its start
+ * with more capacity.  Global indices are kept (ib = -1 - global plane index). */
+SG_API int sg_batch2d_upload(sg_ctx* ctx, int32_t n_scenes, const int32_t* body_off, const double* q,
+                             const double* v, const double* r, const double* m, const int32_t* plane_off,
+                             const double* plane_x, const double* plane_n, const double* mu, const double* CoR);
+
+/* Contact capacity of a batched context (default 3 per body + 1024).  It grows by itself
+ * when a step overflows it; a smaller value bounds device memory up front. */
+SG_API int sg_batch2d_set_capacity(sg_ctx* ctx, int32_t contacts);
+
+/* Per-scene results of the last batched step: contact count, Gauss-Seidel sweeps, best
+ * residual and whether the scene's solve reached the tolerance (any output may be NULL). */
+SG_API int sg_batch2d_scene_stats(sg_ctx* ctx, int32_t* n_contacts, uint32_t* iterations, double* error,
+                                  int32_t* succeeded);
+
 /* Advances the device-resident scene by n_steps steps of
  * GeometricImpactFrictionMap::flow (scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:267-442)
  * as driven by Ball2DSim::flow (ball2d/Ball2DSim.cpp:305-326) or RigidBody3DSim::flow

@@ -63,6 +63,9 @@ SIGNATURES = {
     "sg_ctx_reconfigure": (C.c_int, [C.c_void_p, C.POINTER(SgConfig)]),
     "sg_ball2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
     "sg_sphere3d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
+    "sg_batch2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _ip, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
+    "sg_batch2d_scene_stats": (C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_uint32), _dp, _ip]),
+    "sg_batch2d_set_capacity": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_step": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SgStepStats), C.POINTER(_i64)]),
     "sg_flow": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp, C.POINTER(SgStepStats)]),
     "sg_download_state": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -184,6 +187,33 @@ class Context:
         self._keep = (q, v, r, m, px, pn)
         check(lib().sg_ball2d_upload(self._h, self.nb, dptr(q), dptr(v), dptr(r), dptr(m), px.shape[0] // 2,
                                      dptr(px), dptr(pn)), "sg_ball2d_upload")
+
+    def upload_batch2d(self, body_off, q, v, r, m, plane_off, plane_x, plane_n, mu, CoR):
+        """Independent Ball2D scenes stepped together (global body and plane indices)."""
+        bo, po = i32(body_off).reshape(-1), i32(plane_off).reshape(-1)
+        q, v, r, m = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1)
+        px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        mu, CoR = f64(mu).reshape(-1), f64(CoR).reshape(-1)
+        S = bo.shape[0] - 1
+        if po.shape[0] != S + 1 or mu.shape[0] != S or CoR.shape[0] != S or r.shape[0] != bo[-1]:
+            raise ValueError("inconsistent batch sizes")
+        self.nb = r.shape[0]
+        self.dim = 2
+        self.n_scenes = S
+        self._keep = (bo, po, q, v, r, m, px, pn, mu, CoR)
+        check(lib().sg_batch2d_upload(self._h, S, iptr(bo), dptr(q), dptr(v), dptr(r), dptr(m), iptr(po), dptr(px),
+                                      dptr(pn), dptr(mu), dptr(CoR)), "sg_batch2d_upload")
+
+    def batch_set_capacity(self, contacts):
+        check(lib().sg_batch2d_set_capacity(self._h, int(contacts)), "sg_batch2d_set_capacity")
+
+    def batch_scene_stats(self):
+        S = self.n_scenes
+        nc, it = np.empty(S, np.int32), np.empty(S, np.uint32)
+        err, ok = np.empty(S), np.empty(S, np.int32)
+        check(lib().sg_batch2d_scene_stats(self._h, iptr(nc), it.ctypes.data_as(C.POINTER(C.c_uint32)), dptr(err),
+                                           iptr(ok)), "sg_batch2d_scene_stats")
+        return dict(n_contacts=nc, iterations=it, error=err, succeeded=ok.astype(bool))
 
     def upload_sphere3d(self, q, v, r, m, I0, plane_x, plane_n):
         """RigidBody3D spheres: q 12nb [x | R row-major], v 6nb [v | omega], r, m, I0 (3 per body)."""

@@ -199,6 +199,13 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->r3, &ctx->r3a, &ctx->r3b, &ctx->ab3, &ctx->vrun3, &ctx->pk_ab, &ctx->pk_n, &ctx->pk_c,
                   &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32};
   for (Buf* b : bufs3) release(*b);
+  Buf* bufsb[] = {&ctx->sb_off,  &ctx->sp_off,   &ctx->sf_off,      &ctx->scene_of, &ctx->s_mu,    &ctx->s_CoR,
+                  &ctx->s_grid,  &ctx->s_cells,  &ctx->s_cell_off,  &ctx->s_nc,     &ctx->s_npairs, &ctx->sc_off,
+                  &ctx->prev_sc_off, &ctx->cscene, &ctx->b_ctl,     &ctx->b_sums,   &ctx->s_err,   &ctx->s_best,
+                  &ctx->s_bestbuf, &ctx->s_done, &ctx->s_iters,     &ctx->snap_q,   &ctx->snap_v,  &ctx->snap_key,
+                  &ctx->snap_ab, &ctx->snap_off};
+  for (Buf* b : bufsb) release(*b);
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
   Buf* bufs[] = {&ctx->q, &ctx->v, &ctx->r, &ctx->m, &ctx->minv, &ctx->q1, &ctx->v1, &ctx->v2, &ctx->plane_x,
                  &ctx->plane_n, &ctx->plane_t, &ctx->aabb, &ctx->cell_of, &ctx->cell_count, &ctx->cell_start,
                  &ctx->cell_fill, &ctx->sorted, &ctx->pair_cnt, &ctx->pair_off, &ctx->grid, &ctx->plane_flag,
@@ -220,6 +227,10 @@ int sg_ctx_reconfigure(sg_ctx* ctx, const sg_config* cfg) {
     return SG_BAD_INPUT;
   }
   ctx->cfg = *cfg;
+  if (ctx->graph) {
+    cudaGraphExecDestroy(ctx->graph);  // kernel arguments carry the old settings
+    ctx->graph = nullptr;
+  }
   return SG_OK;
 }
 
@@ -236,6 +247,11 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
     }
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
   ctx->dim = 2;
+  ctx->n_scenes = 0;
+  if (ctx->graph) {
+    cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
   ctx->nb = nb;
   ctx->np = np;
   const size_t b2 = sizeof(double) * 2 * (size_t)std::max(nb, 1), b1 = sizeof(double) * (size_t)std::max(nb, 1);
@@ -305,6 +321,7 @@ static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const 
   }
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
   ctx->dim = 3;
+  ctx->n_scenes = 0;
   ctx->nb = nb;
   ctx->np = np;
   const size_t nbs = (size_t)std::max(nb, 1);
@@ -334,6 +351,196 @@ static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const 
   return SG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Batched Ball2D scenes.
+static constexpr int kGraphSteps = 8;  // steps per captured graph (even: pointer swaps cancel)
+
+static int batch_upload(sg_ctx* ctx, int32_t S, const int32_t* body_off, const double* q, const double* v,
+                        const double* r, const double* m, const int32_t* plane_off, const double* plane_x,
+                        const double* plane_n, const double* mu, const double* CoR) {
+  if (!ctx || S < 1 || !body_off || !plane_off || !mu || !CoR || body_off[0] != 0 || plane_off[0] != 0) {
+    set_error("sg_batch2d_upload: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  std::vector<int> sf(S + 1, 0), scene_of;
+  long cells = 0;
+  for (int s = 0; s < S; ++s) {
+    const int ns = body_off[s + 1] - body_off[s], np = plane_off[s + 1] - plane_off[s];
+    if (ns < 0 || np < 0 || !(mu[s] >= 0.0) || !(CoR[s] >= 0.0 && CoR[s] <= 1.0)) {
+      set_error("sg_batch2d_upload: offsets must not decrease; mu >= 0, 0 <= CoR <= 1 per scene");
+      return SG_BAD_INPUT;
+    }
+    const long f = (long)sf[s] + (long)ns * np;
+    cells += 4L * ns + 64;
+    if (f > (1L << 30) || cells > (1L << 30)) {
+      set_error("sg_batch2d_upload: batch too large");
+      return SG_CAPACITY;
+    }
+    sf[s + 1] = (int)f;
+    scene_of.insert(scene_of.end(), (size_t)ns, s);
+  }
+  const int N = body_off[S], NP = plane_off[S];
+  if (int e = sg_ball2d_upload(ctx, N, q, v, r, m, NP, plane_x, plane_n)) return e;
+  ctx->n_scenes = S;
+  ctx->bcells = cells;
+  ctx->bflags = sf[S];
+  const size_t s1 = sizeof(int) * (size_t)(S + 1);
+  if (int e = upload(ctx, ctx->sb_off, body_off, s1)) return e;
+  if (int e = upload(ctx, ctx->sp_off, plane_off, s1)) return e;
+  if (int e = upload(ctx, ctx->sf_off, sf.data(), s1)) return e;
+  if (int e = upload(ctx, ctx->scene_of, scene_of.data(), sizeof(int) * (size_t)N)) return e;
+  if (int e = upload(ctx, ctx->s_mu, mu, sizeof(double) * (size_t)S)) return e;
+  if (int e = upload(ctx, ctx->s_CoR, CoR, sizeof(double) * (size_t)S)) return e;
+  const size_t nbs = (size_t)std::max(N, 1);
+  Buf* ints_s1[] = {&ctx->s_cells, &ctx->s_cell_off, &ctx->s_nc, &ctx->s_npairs, &ctx->sc_off, &ctx->prev_sc_off,
+                    &ctx->snap_off, &ctx->s_bestbuf, &ctx->s_done, &ctx->s_iters};
+  for (Buf* b : ints_s1)
+    if (int e = grow(*b, s1)) return e;
+  if (int e = grow(ctx->s_grid, 48 * (size_t)S)) return e;
+  if (int e = grow(ctx->s_best, sizeof(double) * (size_t)S)) return e;
+  if (int e = grow(ctx->s_err, sizeof(unsigned long long) * 3 * (size_t)S)) return e;
+  if (int e = grow(ctx->b_ctl, 4 * sizeof(int))) return e;
+  if (int e = grow(ctx->b_sums, 4 * sizeof(unsigned long long))) return e;
+  if (int e = grow(ctx->cell_count, sizeof(int) * (size_t)(cells + 1))) return e;
+  if (int e = grow(ctx->cell_start, sizeof(int) * (size_t)(cells + 1))) return e;
+  if (int e = grow(ctx->cell_fill, sizeof(int) * (size_t)(cells + 1))) return e;
+  if (int e = grow(ctx->cell_of, sizeof(int) * nbs)) return e;
+  if (int e = grow(ctx->sorted, sizeof(int) * nbs)) return e;
+  if (int e = grow(ctx->pair_cnt, sizeof(int) * (nbs + 1))) return e;
+  if (int e = grow(ctx->pair_off, sizeof(int) * (nbs + 1))) return e;
+  if (int e = grow(ctx->plane_flag, sizeof(int) * (size_t)(sf[S] + 1))) return e;
+  if (int e = grow(ctx->plane_off, sizeof(int) * (size_t)(sf[S] + 1))) return e;
+  if (int e = grow(ctx->snap_q, sizeof(double) * 2 * nbs)) return e;
+  if (int e = grow(ctx->snap_v, sizeof(double) * 2 * nbs)) return e;
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->prev_sc_off.p, 0, s1, ctx->stream));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->sc_off.p, 0, s1, ctx->stream));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_ctl.p, 0, 4 * sizeof(int), ctx->stream));
+  if (int e = batch2d_reserve(ctx, std::max(3 * N + 1024, ctx->bcap))) return e;
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+// State a chunk of steps starts from (positions, velocities, impulse cache, counters).
+static int batch_snapshot(sg_ctx* ctx, bool restore) {
+  cudaStream_t s = ctx->stream;
+  const size_t b2 = sizeof(double) * 2 * (size_t)ctx->nb;
+  const size_t s1 = sizeof(int) * (size_t)(ctx->n_scenes + 1);
+  const size_t kb = sizeof(unsigned long long) * (size_t)ctx->bcap, ab = sizeof(double) * 2 * (size_t)ctx->bcap;
+  auto cp = [&](Buf& live, Buf& snap, size_t bytes) -> cudaError_t {
+    if (!bytes) return cudaSuccess;
+    return restore ? cudaMemcpyAsync(live.p, snap.p, bytes, cudaMemcpyDeviceToDevice, s)
+                   : cudaMemcpyAsync(snap.p, live.p, bytes, cudaMemcpyDeviceToDevice, s);
+  };
+  SG_CUDA_TRY(cp(ctx->q, ctx->snap_q, b2));
+  SG_CUDA_TRY(cp(ctx->v, ctx->snap_v, b2));
+  if (ctx->cfg.cache_mode != SG_CACHE_NONE) {
+    SG_CUDA_TRY(cp(ctx->prev_key, ctx->snap_key, kb));
+    SG_CUDA_TRY(cp(ctx->prev_ab, ctx->snap_ab, ab));
+    SG_CUDA_TRY(cp(ctx->prev_sc_off, ctx->snap_off, s1));
+  }
+  return SG_OK;
+}
+
+static int batch_build_graph(sg_ctx* ctx) {
+  cudaStream_t s = ctx->stream;
+  const uint64_t l0 = ctx->kernel_launches, st0 = ctx->steps;
+  Buf saved[8] = {ctx->q, ctx->q1, ctx->v, ctx->v1, ctx->key, ctx->prev_key, ctx->ab, ctx->prev_ab};
+  Buf saved_off[2] = {ctx->sc_off, ctx->prev_sc_off};
+  SG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  int rc = SG_OK;
+  for (int k = 0; k < kGraphSteps && rc == SG_OK; ++k) rc = batch2d_step_enqueue(ctx);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(s, &g);
+  ctx->q = saved[0], ctx->q1 = saved[1], ctx->v = saved[2], ctx->v1 = saved[3];
+  ctx->key = saved[4], ctx->prev_key = saved[5], ctx->ab = saved[6], ctx->prev_ab = saved[7];
+  ctx->sc_off = saved_off[0], ctx->prev_sc_off = saved_off[1];
+  ctx->graph_launches = ctx->kernel_launches - l0;
+  ctx->kernel_launches = l0;
+  ctx->steps = st0;
+  if (rc != SG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  SG_CUDA_TRY(ce);
+  const cudaError_t ie = cudaGraphInstantiate(&ctx->graph, g, 0);
+  cudaGraphDestroy(g);
+  SG_CUDA_TRY(ie);
+  return SG_OK;
+}
+
+static int batch_step(sg_ctx* ctx, uint32_t n_steps, sg_step_stats* out, int64_t* total) {
+  cudaStream_t s = ctx->stream;
+  const int S = ctx->n_scenes;
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_sums.p, 0, 4 * sizeof(unsigned long long), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_ctl.as<int>() + 1, 0, sizeof(int), s));
+  uint32_t done = 0;
+  unsigned long long sums_before[2] = {0, 0};
+  int retries = 0;
+  while (done < n_steps) {
+    const uint32_t chunk = std::min<uint32_t>(kGraphSteps, n_steps - done);
+    if (int e = batch_snapshot(ctx, false)) return e;
+    SG_CUDA_TRY(cudaMemcpyAsync(sums_before, ctx->b_sums.p, sizeof sums_before, cudaMemcpyDeviceToHost, s));
+    if (chunk == (uint32_t)kGraphSteps) {
+      if (!ctx->graph)
+        if (int e = batch_build_graph(ctx)) return e;
+      SG_CUDA_TRY(cudaGraphLaunch(ctx->graph, s));
+      ctx->kernel_launches += ctx->graph_launches;
+      ctx->steps += chunk;
+    } else {
+      for (uint32_t k = 0; k < chunk; ++k)
+        if (int e = batch2d_step_enqueue(ctx)) return e;
+    }
+    int overflow = 0;
+    SG_CUDA_TRY(cudaMemcpyAsync(&overflow, ctx->b_ctl.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (overflow > 0) {
+      // Restore the chunk's starting state, grow the contact capacity and step again.
+      if (++retries > 8) {
+        set_error("batched step: contact capacity kept overflowing");
+        return SG_CAPACITY;
+      }
+      if (int e = batch_snapshot(ctx, true)) return e;
+      SG_CUDA_TRY(cudaMemcpyAsync(ctx->b_sums.p, sums_before, sizeof sums_before, cudaMemcpyHostToDevice, s));
+      SG_CUDA_TRY(cudaMemsetAsync(ctx->b_ctl.as<int>() + 1, 0, sizeof(int), s));
+      if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+      }
+      ctx->steps -= chunk;
+      if (int e = batch2d_reserve(ctx, overflow + overflow / 4 + 1024)) return e;
+      continue;
+    }
+    done += chunk;
+  }
+  // Counters and the last step's per-scene results.
+  unsigned long long sums[2] = {0, 0};
+  int ctl[1] = {0};
+  std::vector<unsigned> iters(S);
+  std::vector<double> best(S);
+  std::vector<int> sdone(S);
+  SG_CUDA_TRY(cudaMemcpyAsync(sums, ctx->b_sums.p, sizeof sums, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctl, ctx->b_ctl.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(iters.data(), ctx->s_iters.p, sizeof(unsigned) * S, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(best.data(), ctx->s_best.p, sizeof(double) * S, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(sdone.data(), ctx->s_done.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, ctx->stats.p, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  sg_step_stats st{};
+  st.n_contacts = ctl[0];
+  st.succeeded = 1;
+  for (int k = 0; k < S; ++k) {
+    st.iterations = std::max(st.iterations, iters[k]);
+    if (!sdone[k]) st.succeeded = 0;
+    if (best[k] < INFINITY && best[k] > st.error) st.error = best[k];
+  }
+  st.n_colors = (uint32_t)ctx->h_stats.n_colors;
+  ctx->last_nc = ctl[0];
+  ctx->contacts_total += sums[0];
+  if (out) *out = st;
+  if (total) *total = (int64_t)sums[0];
+  return sums[1] ? SG_NOT_CONVERGED : SG_OK;
+}
+
 static int check_integrator(const sg_ctx* ctx) {
   const bool split = ctx->cfg.integrator == SG_SPLIT_HAM;
   if ((ctx->dim == 3) != split) {
@@ -352,6 +559,7 @@ int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_sta
   (void)first_iteration;  // gravity is time independent
   if (int e = check_integrator(ctx)) return e;
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  if (ctx->n_scenes > 0) return batch_step(ctx, n_steps, stats, total_contacts);
   int64_t tot = 0;
   int worst = SG_OK;
   sg_step_stats st{};
@@ -422,6 +630,50 @@ int64_t sg_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, dou
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
   return nc;
+}
+
+int sg_batch2d_upload(sg_ctx* ctx, int32_t n_scenes, const int32_t* body_off, const double* q, const double* v,
+                      const double* r, const double* m, const int32_t* plane_off, const double* plane_x,
+                      const double* plane_n, const double* mu, const double* CoR) {
+  if (!ctx) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  return batch_upload(ctx, n_scenes, body_off, q, v, r, m, plane_off, plane_x, plane_n, mu, CoR);
+}
+
+int sg_batch2d_set_capacity(sg_ctx* ctx, int32_t contacts) {
+  if (!ctx || ctx->n_scenes == 0 || contacts < 1) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  if (ctx->graph) {
+    cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  // Shrinking keeps the allocations but caps the pipeline at `contacts`.
+  if (contacts > ctx->bcap) return batch2d_reserve(ctx, contacts);
+  ctx->bcap = contacts;
+  return SG_OK;
+}
+
+int sg_batch2d_scene_stats(sg_ctx* ctx, int32_t* n_contacts, uint32_t* iterations, double* error,
+                           int32_t* succeeded) {
+  if (!ctx || ctx->n_scenes == 0) return SG_BAD_INPUT;
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  const int S = ctx->n_scenes;
+  cudaStream_t s = ctx->stream;
+  // After a cached step the step's offsets were swapped into prev_sc_off.
+  const Buf& off = ctx->cfg.cache_mode != SG_CACHE_NONE ? ctx->prev_sc_off : ctx->sc_off;
+  std::vector<int> o(S + 1), d(S);
+  SG_CUDA_TRY(cudaMemcpyAsync(o.data(), off.p, sizeof(int) * (S + 1), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d.data(), ctx->s_done.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
+  if (iterations)
+    SG_CUDA_TRY(cudaMemcpyAsync(iterations, ctx->s_iters.p, sizeof(unsigned) * S, cudaMemcpyDeviceToHost, s));
+  if (error) SG_CUDA_TRY(cudaMemcpyAsync(error, ctx->s_best.p, sizeof(double) * S, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int k = 0; k < S; ++k) {
+    if (n_contacts) n_contacts[k] = o[k + 1] - o[k];
+    if (succeeded) succeeded[k] = d[k];
+    if (error && o[k + 1] == o[k]) error[k] = 0.0;
+  }
+  return SG_OK;
 }
 
 int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,

@@ -11,7 +11,9 @@
 // n double2, forcing c double2, W 3 doubles, mu, local impulse r double2, key u64).
 #include "ctx.hpp"
 
+#include <algorithm>
 #include <cmath>
+#include <utility>
 
 namespace sg {
 namespace {
@@ -342,9 +344,9 @@ struct AssembleArgs {
 // Constraint::computeForcingTerm (Constraint.cpp:18-34), evalKinematicRelVelGivenBases
 // (Constraint.cpp:92-126), Balls2DSobogusInterface::fromPrimal (:31-94),
 // initializeImpulses (GeometricImpactFrictionMap.cpp:174-220), solve2D warm start (Sobogus.cpp:299-301).
-__global__ void k_assemble(AssembleArgs A) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= A.nc) return;
+__device__ __forceinline__ void assemble_one(const AssembleArgs& A, int k, double mu, double CoR,
+                                             const unsigned long long* prev_key, const double2* prev_ab,
+                                             long prev_n) {
   const int a = A.ia[k], b = A.ib[k];
   double nx, ny, tx, ty;
   double vrx, vry;
@@ -378,7 +380,7 @@ __global__ void k_assemble(AssembleArgs A) {
   const double ndotv = nx * vrx + ny * vry;
   const double nrel = -(0.0 * nx + 0.0 * ny);
   const double drel = -(0.0 * tx + 0.0 * ty);
-  const double s = A.CoR * ndotv + nrel;
+  const double s = CoR * ndotv + nrel;
   const double wx = (0.0 + nx * s) + tx * drel;
   const double wy = (0.0 + ny * s) + ty * drel;
   A.n[k] = make_double2(nx, ny);
@@ -397,14 +399,14 @@ __global__ void k_assemble(AssembleArgs A) {
   A.W[3 * k] = w00;
   A.W[3 * k + 1] = w01;
   A.W[3 * k + 2] = w11;
-  A.mu_out[k] = A.mu;
+  A.mu_out[k] = mu;
   const unsigned long long key = contact_key(a, b);
   A.key[k] = key;
   double alpha = 0.0, beta = 0.0;
-  if (A.cache_mode != SG_CACHE_NONE && A.prev_n > 0) {
-    const long idx = find_key(A.prev_key, A.prev_n, key);
+  if (A.cache_mode != SG_CACHE_NONE && prev_n > 0) {
+    const long idx = find_key(prev_key, prev_n, key);
     if (idx >= 0) {
-      const double2 ab = A.prev_ab[idx];
+      const double2 ab = prev_ab[idx];
       alpha = ab.x;
       beta = (A.cache_mode == SG_CACHE_NORMAL_AND_FRICTION) ? ab.y : 0.0;
     }
@@ -414,11 +416,19 @@ __global__ void k_assemble(AssembleArgs A) {
   A.r[k] = make_double2(nx * rwx + ny * rwy, tx * rwx + ty * rwy);
 }
 
+__global__ void k_assemble(AssembleArgs A) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.nc) return;
+  assemble_one(A, k, A.mu, A.CoR, A.prev_key, A.prev_ab, A.prev_n);
+}
+
 // alpha = r_world . n, beta = r_world . t (Sobogus.cpp:312-330); caches (alpha, beta)
 // (cacheImpulses, GeometricImpactFrictionMap.cpp:222-264).
-__global__ void k_extract(int nc, const double2* __restrict__ n, const double2* __restrict__ r,
-                          const double* __restrict__ mu, int cache_mode, double2* __restrict__ ab) {
+__global__ void k_extract(int nc, const int* __restrict__ nc_dev, const double2* __restrict__ n,
+                          const double2* __restrict__ r, const double* __restrict__ mu, int cache_mode,
+                          double2* __restrict__ ab) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nc_dev) nc = *nc_dev;
   if (k >= nc) return;
   const double2 nk = n[k], rk = r[k];
   const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
@@ -440,6 +450,256 @@ __global__ void k_final_map(int nb, int integrator, double dt, double gx, double
   umap_body(integrator, dt, gx, gy, m[i], minv[i], q.x, q.y, v.x, v.y, qn.x, qn.y, vn.x, vn.y);
   q1[i] = qn;
   v1[i] = vn;
+}
+
+// ---------------------------------------------------------------------------
+// Batched scenes.  Scene s owns bodies [sb_off[s], sb_off[s+1]) and planes
+// [sp_off[s], sp_off[s+1]); each scene has its own uniform grid (cells
+// [s_cell_off[s], s_cell_off[s+1]) of one global cell array) and its contacts are
+// [sc_off[s], sc_off[s+1]) of the step: its ball-ball pairs in (i, j) order, then its
+// plane contacts plane-major (Ball2DSim::computeActiveSet per scene, Ball2DSim.cpp:151-173).
+// Every launch is sized by static counts (bodies, scenes, cell and flag capacities,
+// contact capacity); the contact count lives on the device, so a step enqueues with no
+// host synchronisation and can be captured in a CUDA graph.
+struct SceneGrid {
+  double origin[2];
+  double h;
+  int dims[2];
+  int ncells;
+  int pad;
+};
+
+// One block per scene: bounds and largest extent of the scene's boxes, then the grid
+// (cell strictly wider than any box, at most 4 n + 64 cells), as k_grid_setup.
+__global__ void k_scene_grid(const int* __restrict__ sb_off, const double4_32a* __restrict__ aabb,
+                             SceneGrid* __restrict__ grids, int* __restrict__ s_cells) {
+  const int sc = blockIdx.x;
+  const int b0 = sb_off[sc], b1 = sb_off[sc + 1];
+  double mn0 = INFINITY, mn1 = INFINITY, mx0 = -INFINITY, mx1 = -INFINITY, e = 0.0;
+  for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+    const double4_32a b = aabb[i];
+    mn0 = fmin(mn0, b.x);
+    mn1 = fmin(mn1, b.y);
+    mx0 = fmax(mx0, b.z);
+    mx1 = fmax(mx1, b.w);
+    e = fmax(e, fmax(b.z - b.x, b.w - b.y));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn0 = fmin(mn0, __shfl_down_sync(0xffffffffu, mn0, o));
+    mn1 = fmin(mn1, __shfl_down_sync(0xffffffffu, mn1, o));
+    mx0 = fmax(mx0, __shfl_down_sync(0xffffffffu, mx0, o));
+    mx1 = fmax(mx1, __shfl_down_sync(0xffffffffu, mx1, o));
+    e = fmax(e, __shfl_down_sync(0xffffffffu, e, o));
+  }
+  __shared__ double red[5][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = mn0;
+    red[1][wid] = mn1;
+    red[2][wid] = mx0;
+    red[3][wid] = mx1;
+    red[4][wid] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int nw = (blockDim.x + 31) >> 5;
+  for (int w = 1; w < nw; ++w) {
+    mn0 = fmin(mn0, red[0][w]);
+    mn1 = fmin(mn1, red[1][w]);
+    mx0 = fmax(mx0, red[2][w]);
+    mx1 = fmax(mx1, red[3][w]);
+    e = fmax(e, red[4][w]);
+  }
+  const long cap = 4L * (b1 - b0) + 64;
+  double h = e * (1.0 + 0x1p-20) + 1e-300;
+  if (!(h > 0.0) || !isfinite(h)) h = 1.0;
+  double span0 = mx0 - mn0, span1 = mx1 - mn1;
+  if (!isfinite(span0) || span0 < 0.0) span0 = 0.0;
+  if (!isfinite(span1) || span1 < 0.0) span1 = 0.0;
+  double d0 = floor(span0 / h) + 1.0, d1 = floor(span1 / h) + 1.0;
+  while (d0 * d1 > (double)cap) {
+    h = h * fmax(1.01, sqrt(d0 * d1 / (double)cap));
+    d0 = floor(span0 / h) + 1.0;
+    d1 = floor(span1 / h) + 1.0;
+  }
+  SceneGrid g;
+  g.origin[0] = isfinite(mn0) ? mn0 : 0.0;
+  g.origin[1] = isfinite(mn1) ? mn1 : 0.0;
+  g.h = h;
+  g.dims[0] = (int)d0;
+  g.dims[1] = (int)d1;
+  g.ncells = (int)(d0 * d1);
+  g.pad = 0;
+  grids[sc] = g;
+  s_cells[sc] = g.ncells;
+}
+
+__global__ void k_cell_count_b(int n, const int* __restrict__ scene_of, const double4_32a* __restrict__ aabb,
+                               const SceneGrid* __restrict__ grids, const int* __restrict__ s_cell_off,
+                               int* __restrict__ cell_of, int* __restrict__ cell_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = scene_of[i];
+  const SceneGrid g = grids[sc];
+  const double4_32a b = aabb[i];
+  const int cx = cell_coord(b.x, g.origin[0], g.h, g.dims[0]);
+  const int cy = cell_coord(b.y, g.origin[1], g.h, g.dims[1]);
+  const int cell = s_cell_off[sc] + cx + g.dims[0] * cy;
+  cell_of[i] = cell;
+  atomicAdd(&cell_count[cell], 1);
+}
+
+struct BatchScan {
+  const int* scene_of;
+  const SceneGrid* grids;
+  const int* s_cell_off;
+  const double4_32a* aabb;
+  const int* cell_start;
+  const int* sorted;
+  const double2* q0;
+  const double2* q1;
+  const double* rad;
+};
+
+// visit_pairs<true> within the scene grid of body i.
+template <typename F>
+__device__ __forceinline__ void visit_pairs_b(const BatchScan& s, int i, F&& f) {
+  const int sc = s.scene_of[i];
+  const SceneGrid g = s.grids[sc];
+  const int base = s.s_cell_off[sc];
+  const double4_32a bi = s.aabb[i];
+  const int cx = cell_coord(bi.x, g.origin[0], g.h, g.dims[0]);
+  const int cy = cell_coord(bi.y, g.origin[1], g.h, g.dims[1]);
+  const double2 q0a = s.q0[i], q1a = s.q1[i];
+  const double ra = s.rad[i];
+  for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y) {
+    for (int x = max(cx - 1, 0); x <= min(cx + 1, g.dims[0] - 1); ++x) {
+      const int cell = base + x + g.dims[0] * y;
+      const int e = s.cell_start[cell + 1];
+      for (int p = s.cell_start[cell]; p < e; ++p) {
+        const int j = s.sorted[p];
+        if (j <= i) continue;
+        if (!aabb_overlap(bi, s.aabb[j])) continue;
+        double c0, c1, c2;
+        ccd_coeffs(q0a, q1a, ra, s.q0[j], s.q1[j], s.rad[j], c0, c1, c2);
+        if (!ccd_happens(c0, c1, c2, nullptr)) continue;
+        f(j);
+      }
+    }
+  }
+}
+
+__global__ void k_pair_count_b(int n, BatchScan s, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = 0;
+  visit_pairs_b(s, i, [&](int) { ++c; });
+  cnt[i] = c;
+}
+
+// StaticPlaneConstraint::isActive per (plane, body) of each scene, plane-major within
+// the scene's flag range [sf_off[s], sf_off[s+1]).
+__global__ void k_plane_flags_b(int n, const int* __restrict__ scene_of, const int* __restrict__ sb_off,
+                                const int* __restrict__ sp_off, const int* __restrict__ sf_off,
+                                const double2* __restrict__ q1, const double* __restrict__ rad,
+                                const double2* __restrict__ px, const double2* __restrict__ pn,
+                                int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = scene_of[i];
+  const int b0 = sb_off[sc], ns = sb_off[sc + 1] - b0;
+  const int p0 = sp_off[sc], p1 = sp_off[sc + 1];
+  const double2 qi = q1[i];
+  const double ri = rad[i];
+  for (int p = p0; p < p1; ++p) {
+    const double2 x = px[p], nn = pn[p];
+    const double d = nn.x * (qi.x - x.x) + nn.y * (qi.y - x.y);
+    flag[sf_off[sc] + (long)(p - p0) * ns + (i - b0)] = (d <= ri) ? 1 : 0;
+  }
+}
+
+// Per scene: ball-ball and plane contact counts.
+__global__ void k_scene_counts(int S, const int* __restrict__ sb_off, const int* __restrict__ sf_off,
+                               const int* __restrict__ pair_off, const int* __restrict__ plane_off,
+                               int* __restrict__ s_nc, int* __restrict__ s_npairs) {
+  const int sc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sc >= S) return;
+  const int np = pair_off[sb_off[sc + 1]] - pair_off[sb_off[sc]];
+  const int nq = plane_off[sf_off[sc + 1]] - plane_off[sf_off[sc]];
+  s_npairs[sc] = np;
+  s_nc[sc] = np + nq;
+}
+
+// Total contacts against the capacity: on overflow the step keeps no contacts and the
+// needed count is recorded for the host, which restores the chunk's starting state,
+// grows the buffers and steps again.
+__global__ void k_capacity(const int* __restrict__ total, int cap, int* __restrict__ nc_dev,
+                           int* __restrict__ overflow, unsigned long long* __restrict__ contacts_sum) {
+  const int nc = *total;
+  if (nc > cap) {
+    *nc_dev = 0;
+    if (nc > *overflow) *overflow = nc;
+  } else {
+    *nc_dev = nc;
+    *contacts_sum += (unsigned long long)nc;
+  }
+}
+
+__global__ void k_pair_write_b(int n, BatchScan s, const int* __restrict__ sb_off, const int* __restrict__ pair_off,
+                               const int* __restrict__ sc_off, const int* __restrict__ pair_cnt, int cap,
+                               int* __restrict__ out_a, int* __restrict__ out_b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = s.scene_of[i];
+  const int base = sc_off[sc] + (pair_off[i] - pair_off[sb_off[sc]]);
+  if (base + pair_cnt[i] > cap) return;
+  int c = 0;
+  visit_pairs_b(s, i, [&](int j) {
+    int p = base + c;
+    while (p > base && out_b[p - 1] > j) {
+      out_b[p] = out_b[p - 1];
+      --p;
+    }
+    out_b[p] = j;
+    ++c;
+  });
+  for (int k = 0; k < c; ++k) out_a[base + k] = i;
+}
+
+__global__ void k_plane_write_b(int n, const int* __restrict__ scene_of, const int* __restrict__ sb_off,
+                                const int* __restrict__ sp_off, const int* __restrict__ sf_off,
+                                const int* __restrict__ flag, const int* __restrict__ plane_off,
+                                const int* __restrict__ sc_off, const int* __restrict__ s_npairs, int cap,
+                                int* __restrict__ ia, int* __restrict__ ib) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = scene_of[i];
+  const int b0 = sb_off[sc], ns = sb_off[sc + 1] - b0;
+  const int p0 = sp_off[sc], p1 = sp_off[sc + 1];
+  const int fbase = sf_off[sc];
+  const int cbase = sc_off[sc] + s_npairs[sc] - plane_off[fbase];
+  for (int p = p0; p < p1; ++p) {
+    const long t = fbase + (long)(p - p0) * ns + (i - b0);
+    if (!flag[t]) continue;
+    const int k = cbase + plane_off[t];
+    if (k < cap) {
+      ia[k] = i;
+      ib[k] = -1 - p;
+    }
+  }
+}
+
+// Per-scene mu and CoR, warm start searched in the scene's own slice of the previous
+// step's (sorted) keys.
+__global__ void k_assemble_b(AssembleArgs A, const int* __restrict__ nc_dev, const int* __restrict__ scene_of,
+                             const double* __restrict__ s_mu, const double* __restrict__ s_CoR,
+                             const int* __restrict__ prev_sc_off, int* __restrict__ cscene) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *nc_dev) return;
+  const int sc = scene_of[A.ia[k]];
+  cscene[k] = sc;
+  const int p0 = prev_sc_off[sc], p1 = prev_sc_off[sc + 1];
+  assemble_one(A, k, s_mu[sc], s_CoR[sc], A.prev_key + p0, A.prev_ab + p0, (long)(p1 - p0));
 }
 
 __global__ void k_ccd_batch(int n, const double2* q0a, const double2* q1a, const double* ra, const double2* q0b,
@@ -586,7 +846,7 @@ int assemble_contacts(sg_ctx* ctx, int nc) {
 
 int extract_and_cache(sg_ctx* ctx, int nc) {
   if (nc <= 0) return SG_OK;
-  k_extract<<<blocks_for(nc), kBlock, 0, ctx->stream>>>(nc, ctx->n.as<double2>(), ctx->r_loc.as<double2>(),
+  k_extract<<<blocks_for(nc), kBlock, 0, ctx->stream>>>(nc, nullptr, ctx->n.as<double2>(), ctx->r_loc.as<double2>(),
                                                         ctx->mu.as<double>(), ctx->cfg.cache_mode, ctx->ab.as<double2>());
   SG_CUDA_TRY(cudaGetLastError());
   return SG_OK;
@@ -601,6 +861,172 @@ int ball2d_final_map(sg_ctx* ctx, const double* vin) {
                                                           ctx->minv.as<double>(), ctx->q1.as<double2>(),
                                                           ctx->v1.as<double2>());
   SG_CUDA_TRY(cudaGetLastError());
+  return SG_OK;
+}
+
+// ===========================================================================
+// Batched scenes: capacity and one step.
+int batch2d_reserve(sg_ctx* ctx, int cap) {
+  const size_t c = (size_t)std::max(cap, 1), nb = (size_t)std::max(ctx->nb, 1);
+  if (int r = grow(ctx->ia, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->ib, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->n, sizeof(double) * 2 * c)) return r;
+  if (int r = grow(ctx->c, sizeof(double) * 2 * c)) return r;
+  if (int r = grow(ctx->W, sizeof(double) * 3 * c)) return r;
+  if (int r = grow(ctx->mu, sizeof(double) * c)) return r;
+  if (int r = grow(ctx->r_loc, sizeof(double) * 2 * c)) return r;
+  if (int r = grow(ctx->cscene, sizeof(int) * c)) return r;
+  // The impulse cache keeps its contents across a capacity change.
+  for (Buf* b : {&ctx->key, &ctx->prev_key, &ctx->snap_key}) {
+    if (b->bytes >= sizeof(unsigned long long) * c && b->p) continue;
+    Buf nbuf;
+    if (int r = grow(nbuf, sizeof(unsigned long long) * c)) return r;
+    SG_CUDA_TRY(cudaMemsetAsync(nbuf.p, 0, nbuf.bytes, ctx->stream));
+    if (b->p) SG_CUDA_TRY(cudaMemcpyAsync(nbuf.p, b->p, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    release(*b);
+    *b = nbuf;
+  }
+  for (Buf* b : {&ctx->ab, &ctx->prev_ab, &ctx->snap_ab}) {
+    if (b->bytes >= sizeof(double) * 2 * c && b->p) continue;
+    Buf nbuf;
+    if (int r = grow(nbuf, sizeof(double) * 2 * c)) return r;
+    SG_CUDA_TRY(cudaMemsetAsync(nbuf.p, 0, nbuf.bytes, ctx->stream));
+    if (b->p) SG_CUDA_TRY(cudaMemcpyAsync(nbuf.p, b->p, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    release(*b);
+    *b = nbuf;
+  }
+  if (int r = ensure_solver_capacity(ctx, ctx->nb, (int)c)) return r;
+  if (int r = grow(ctx->v2, sizeof(double) * 2 * nb)) return r;
+  // Scan scratch for the largest scan of a step, so that nothing allocates while capturing.
+  const long big = std::max<long>({(long)ctx->nb + 1, ctx->bcells + 1, ctx->bflags + 1, (long)ctx->n_scenes + 1,
+                                   (long)c});
+  if (int r = grow(ctx->scan_tmp, sizeof(int) * (size_t)(scan_tile_count((int)big) + 2))) return r;
+  ctx->bcap = (int)c;
+  ctx->ccap = std::min<int64_t>(ctx->ccap, (int64_t)c);
+  return SG_OK;
+}
+
+int batch2d_step_enqueue(sg_ctx* ctx) {
+  const int N = ctx->nb, S = ctx->n_scenes, cap = ctx->bcap;
+  cudaStream_t s = ctx->stream;
+  if (int r = ball2d_predict_and_bounds(ctx)) return r;
+  const double4_32a* aabb = ctx->aabb.as<double4_32a>();
+  SceneGrid* grids = ctx->s_grid.as<SceneGrid>();
+  k_scene_grid<<<S, kBlock, 0, s>>>(ctx->sb_off.as<int>(), aabb, grids, ctx->s_cells.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->s_cells.as<int>(), ctx->s_cell_off.as<int>(), S)) return r;
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_count.p, 0, sizeof(int) * (size_t)(ctx->bcells + 1), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_fill.p, 0, sizeof(int) * (size_t)(ctx->bcells + 1), s));
+  k_cell_count_b<<<blocks_for(N), kBlock, 0, s>>>(N, ctx->scene_of.as<int>(), aabb, grids, ctx->s_cell_off.as<int>(),
+                                                 ctx->cell_of.as<int>(), ctx->cell_count.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->cell_count.as<int>(), ctx->cell_start.as<int>(), (int)ctx->bcells)) return r;
+  k_cell_scatter<<<blocks_for(N), kBlock, 0, s>>>(N, ctx->cell_of.as<int>(), ctx->cell_start.as<int>(),
+                                                 ctx->cell_fill.as<int>(), ctx->sorted.as<int>());
+  BatchScan bs{ctx->scene_of.as<int>(), grids,          ctx->s_cell_off.as<int>(), aabb,
+               ctx->cell_start.as<int>(), ctx->sorted.as<int>(), ctx->q.as<double2>(), ctx->q1.as<double2>(),
+               ctx->r.as<double>()};
+  k_pair_count_b<<<blocks_for(N), kBlock, 0, s>>>(N, bs, ctx->pair_cnt.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->pair_cnt.as<int>(), ctx->pair_off.as<int>(), N)) return r;
+  if (ctx->bflags > 0) {
+    k_plane_flags_b<<<blocks_for(N), kBlock, 0, s>>>(N, ctx->scene_of.as<int>(), ctx->sb_off.as<int>(),
+                                                     ctx->sp_off.as<int>(), ctx->sf_off.as<int>(), ctx->q1.as<double2>(),
+                                                     ctx->r.as<double>(), ctx->plane_x.as<double2>(),
+                                                     ctx->plane_n.as<double2>(), ctx->plane_flag.as<int>());
+    SG_CUDA_TRY(cudaGetLastError());
+    if (int r = scan_exclusive(ctx, ctx->plane_flag.as<int>(), ctx->plane_off.as<int>(), (int)ctx->bflags)) return r;
+  } else {
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->plane_off.p, 0, sizeof(int), s));
+  }
+  k_scene_counts<<<blocks_for(S), kBlock, 0, s>>>(S, ctx->sb_off.as<int>(), ctx->sf_off.as<int>(),
+                                                 ctx->pair_off.as<int>(), ctx->plane_off.as<int>(), ctx->s_nc.as<int>(),
+                                                 ctx->s_npairs.as<int>());
+  if (int r = scan_exclusive(ctx, ctx->s_nc.as<int>(), ctx->sc_off.as<int>(), S)) return r;
+  int* ctl = ctx->b_ctl.as<int>();  // [0] contact count, [1] overflow (largest count seen)
+  unsigned long long* sums = ctx->b_sums.as<unsigned long long>();  // [0] contacts, [1] unconverged scene solves
+  k_capacity<<<1, 1, 0, s>>>(ctx->sc_off.as<int>() + S, cap, ctl, ctl + 1, sums);
+  k_pair_write_b<<<blocks_for(N), kBlock, 0, s>>>(N, bs, ctx->sb_off.as<int>(), ctx->pair_off.as<int>(),
+                                                 ctx->sc_off.as<int>(), ctx->pair_cnt.as<int>(), cap,
+                                                 ctx->ia.as<int>(), ctx->ib.as<int>());
+  if (ctx->bflags > 0)
+    k_plane_write_b<<<blocks_for(N), kBlock, 0, s>>>(N, ctx->scene_of.as<int>(), ctx->sb_off.as<int>(),
+                                                     ctx->sp_off.as<int>(), ctx->sf_off.as<int>(),
+                                                     ctx->plane_flag.as<int>(), ctx->plane_off.as<int>(),
+                                                     ctx->sc_off.as<int>(), ctx->s_npairs.as<int>(), cap,
+                                                     ctx->ia.as<int>(), ctx->ib.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  AssembleArgs A;
+  A.nc = cap;
+  A.ia = ctx->ia.as<int>();
+  A.ib = ctx->ib.as<int>();
+  A.q0 = ctx->q.as<double2>();
+  A.v0 = ctx->v.as<double2>();
+  A.minv = ctx->minv.as<double>();
+  A.plane_n = ctx->plane_n.as<double2>();
+  A.plane_t = ctx->plane_t.as<double2>();
+  A.mu = 0.0;
+  A.CoR = 0.0;
+  A.cache_mode = ctx->cfg.cache_mode;
+  A.prev_key = ctx->prev_key.as<unsigned long long>();
+  A.prev_ab = ctx->prev_ab.as<double2>();
+  A.prev_n = 0;
+  A.n = ctx->n.as<double2>();
+  A.c = ctx->c.as<double2>();
+  A.W = ctx->W.as<double>();
+  A.mu_out = ctx->mu.as<double>();
+  A.r = ctx->r_loc.as<double2>();
+  A.key = ctx->key.as<unsigned long long>();
+  k_assemble_b<<<blocks_for(cap), kBlock, 0, s>>>(A, ctl, ctx->scene_of.as<int>(), ctx->s_mu.as<double>(),
+                                                 ctx->s_CoR.as<double>(), ctx->prev_sc_off.as<int>(),
+                                                 ctx->cscene.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  ContactProblem P;
+  P.nb = N;
+  P.nc = cap;
+  P.minv = ctx->minv.as<double>();
+  P.m = ctx->m.as<double>();
+  P.v0 = ctx->v.as<double>();
+  P.ia = ctx->ia.as<int>();
+  P.ib = ctx->ib.as<int>();
+  P.n = ctx->n.as<double>();
+  P.c = ctx->c.as<double>();
+  P.W = ctx->W.as<double>();
+  P.mu = ctx->mu.as<double>();
+  P.r = ctx->r_loc.as<double>();
+  P.v2 = ctx->v2.as<double>();
+  BatchSolve X;
+  X.S = S;
+  X.nc_dev = ctl;
+  X.cscene = ctx->cscene.as<int>();
+  X.sc_off = ctx->sc_off.as<int>();
+  X.err_slot = ctx->s_err.as<unsigned long long>();
+  X.best = ctx->s_best.as<double>();
+  X.bestbuf = ctx->s_bestbuf.as<int>();
+  X.done = ctx->s_done.as<int>();
+  X.iters = ctx->s_iters.as<unsigned>();
+  X.done_count = ctl + 2;
+  X.unconverged = sums + 1;
+  SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, SG_PRECISION_FP64};
+  if (int r = solve_contacts_batch(ctx, P, sp, X)) return r;
+  k_extract<<<blocks_for(cap), kBlock, 0, s>>>(cap, ctl, ctx->n.as<double2>(), ctx->r_loc.as<double2>(),
+                                              ctx->mu.as<double>(), ctx->cfg.cache_mode, ctx->ab.as<double2>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = ball2d_final_map(ctx, ctx->v2.as<double>())) return r;
+  // predictor 1, scene grid 1 + scan 3, cell count 1 + scan 3, scatter 1, pair count 1 + scan 3,
+  // plane flags 1 + scan 3, scene counts 1 + scan 3, capacity 1, pair write 1, plane write 1,
+  // assemble 1, extract 1, final map 1 (+ the solver's own count)
+  ctx->kernel_launches += 25 + (ctx->bflags > 0 ? 5 : 0);
+  ctx->steps += 1;
+  std::swap(ctx->q, ctx->q1);
+  std::swap(ctx->v, ctx->v1);
+  if (ctx->cfg.cache_mode != SG_CACHE_NONE) {
+    std::swap(ctx->key, ctx->prev_key);
+    std::swap(ctx->ab, ctx->prev_ab);
+    std::swap(ctx->sc_off, ctx->prev_sc_off);
+  }
   return SG_OK;
 }
 

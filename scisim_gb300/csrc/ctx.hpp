@@ -72,6 +72,21 @@ struct ContactProblem {
   double* v2 = nullptr;          // 2nb out
 };
 
+// Per-scene solver state of a batched solve (device arrays of S entries).
+struct BatchSolve {
+  int S = 0;
+  const int* nc_dev = nullptr;
+  const int* cscene = nullptr;
+  const int* sc_off = nullptr;
+  unsigned long long* err_slot = nullptr;  // 3 S
+  double* best = nullptr;
+  int* bestbuf = nullptr;
+  int* done = nullptr;
+  unsigned* iters = nullptr;
+  int* done_count = nullptr;
+  unsigned long long* unconverged = nullptr;
+};
+
 struct SolveParams {
   double tol;
   unsigned int max_iters;
@@ -116,6 +131,19 @@ struct sg_ctx {
   // (alpha, beta0, beta1) out (3); running velocities (2 double4 per body: v, omega).
   int64_t ccap3 = 0;
   sg::Buf E3, Aa3, Ab3, c3, W3, r3, r3a, r3b, ab3, vrun3;
+  // Batched Ball2D scenes (sg_batch2d_upload).  Scene s owns bodies [sb_off[s], sb_off[s+1]),
+  // planes [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]); its contacts of a
+  // step are [sc_off[s], sc_off[s+1]).  Counts live on the device (b_ctl: contact count,
+  // overflow); the step loop is replayed from a CUDA graph of kGraphSteps steps.
+  int n_scenes = 0;  // 0: not a batched context
+  long bcells = 0, bflags = 0;
+  int bcap = 0;
+  sg::Buf sb_off, sp_off, sf_off, scene_of, s_mu, s_CoR, s_grid, s_cells, s_cell_off, s_nc, s_npairs;
+  sg::Buf sc_off, prev_sc_off, cscene, b_ctl, b_sums;
+  sg::Buf s_err, s_best, s_bestbuf, s_done, s_iters;
+  sg::Buf snap_q, snap_v, snap_key, snap_ab, snap_off;
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_launches = 0;  // kernel launches per graph replay
   // buffers of the standalone FrictionSolver entry (kept apart from the scene)
   sg::Buf fs_m, fs_minv, fs_v0, fs_v2;
 
@@ -157,11 +185,30 @@ int ccd_batch(sg_ctx* ctx, int n, const double* q0a, const double* q1a, const do
 
 // Solver pipeline on a ContactProblem living in ctx buffers.
 int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp);
+// Batched scenes, launches sized to the capacity P.nc, count and scene data on the
+// device, no host synchronisation (capturable).
+int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp, const BatchSolve& X);
 int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc);
 // Body -> contact adjacency (ctx->body_off / body_adj, ascending contact order), the
 // solve counters cleared, and the contact colouring with its processing permutation
 // (ctx->perm, colour offsets in ctx->stats).  Shared by the 2D and 3D solvers.
-int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib);
+// nc is the host-side count (or, with nc_dev, the capacity the launches are sized to).
+int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const int* nc_dev = nullptr);
+
+// Cooperative launch through cudaLaunchKernelEx (capturable in a CUDA graph).
+inline cudaError_t launch_cooperative(const void* kernel, int grid, int block, void** args, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, kernel, args);
+}
 
 // Grid size of a cooperative launch: all blocks resident (at most max_per_sm per SM),
 // no more than the work needs.
@@ -173,6 +220,11 @@ int coop_grid(sg_ctx* ctx, K kernel, long work, int block, int max_per_sm = 64) 
   const long need = (work + block - 1) / block > 1 ? (work + block - 1) / block : 1;
   return (int)(g < need ? g : need);
 }
+
+// Batched Ball2D scenes (ball2d_kernels.cu): capacity for `cap` contacts (outside any
+// capture) and one step enqueued without host synchronisation.
+int batch2d_reserve(sg_ctx* ctx, int cap);
+int batch2d_step_enqueue(sg_ctx* ctx);
 
 // RigidBody3D sphere scenes (sphere3d_kernels.cu).
 int sphere3d_update_inertia(sg_ctx* ctx, bool construction);

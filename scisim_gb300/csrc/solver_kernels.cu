@@ -142,17 +142,22 @@ __device__ __forceinline__ void local_velocity(const double2 nk, const double2 c
 }
 
 // ---------------------------------------------------------------------------
-__global__ void k_body_count(int nc, const int* __restrict__ ia, const int* __restrict__ ib, int* __restrict__ cnt) {
+// nc_dev (optional): the contact count on the device, for launches sized to a capacity.
+__global__ void k_body_count(int nc, const int* __restrict__ nc_dev, const int* __restrict__ ia,
+                             const int* __restrict__ ib, int* __restrict__ cnt) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nc_dev) nc = *nc_dev;
   if (k >= nc) return;
   atomicAdd(&cnt[ia[k]], 1);
   const int b = ib[k];
   if (b >= 0) atomicAdd(&cnt[b], 1);
 }
 
-__global__ void k_body_fill(int nc, const int* __restrict__ ia, const int* __restrict__ ib, const int* __restrict__ off,
-                            int* __restrict__ fill, int* __restrict__ adj) {
+__global__ void k_body_fill(int nc, const int* __restrict__ nc_dev, const int* __restrict__ ia,
+                            const int* __restrict__ ib, const int* __restrict__ off, int* __restrict__ fill,
+                            int* __restrict__ adj) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nc_dev) nc = *nc_dev;
   if (k >= nc) return;
   const int a = ia[k];
   adj[off[a] + atomicAdd(&fill[a], 1)] = k;
@@ -240,6 +245,7 @@ __device__ __forceinline__ bool prio_greater(unsigned pj, int j, unsigned pk, in
 
 struct ColorArgs {
   int nc;
+  const int* nc_dev;  // optional device-side count (overrides nc)
   const int* ia;
   const int* ib;
   const int* body_off;
@@ -255,6 +261,7 @@ struct ColorArgs {
 __global__ void k_color_jp(ColorArgs A) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
+  if (A.nc_dev) A.nc = *A.nc_dev;
   volatile int* vcolor = A.color;
   for (int round = 0;; ++round) {
     if (round >= A.max_rounds) {
@@ -530,6 +537,152 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs(GsArgs A) {
     A.st->converged = converged ? 1 : 0;
     A.st->error = err_best;
     A.st->sweeps64 = it;
+    A.st->evals = n_eval;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched scenes: one coloured sweep over the contacts of all scenes (scenes share no
+// body, so the global colouring is a colouring of every scene), with each scene's own
+// residual, best iterate, convergence test and iteration count, as if every scene were
+// solved alone (Sobogus::solve per Ball2DSim).  A converged scene's contacts stop
+// updating; the kernel ends when every scene has converged or at max_iters.
+struct GsBatchArgs {
+  GsArgs g;              // g.nc unused; g.r_a / g.r_b are the two snapshot buffers
+  const int* nc_dev;     // contact count on the device
+  const int* cscene;     // contact -> scene
+  const int* sc_off;     // scene contact offsets (S + 1)
+  int S;
+  unsigned long long* err_slot;  // 3 S ordered residual maxima (rotating)
+  double* best;                  // S
+  int* bestbuf;                  // S: which snapshot buffer holds the scene's best iterate
+  int* done;                     // S: converged (or no contacts)
+  unsigned* iters;               // S
+  int* done_count;
+  unsigned long long* unconverged;  // running count of scene solves that hit max_iters
+};
+
+// Max of v over the lanes of each run of equal keys (runs are contiguous lanes); the
+// first lane of each run with key >= 0 adds it to slots[key].
+__device__ __forceinline__ void run_max_atomic(unsigned long long v, int key, unsigned long long* slots) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+    const int kw = __shfl_down_sync(0xffffffffu, key, o);
+    if (lane + o < 32 && kw == key && w > v) v = w;
+  }
+  const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+  if (key >= 0 && (lane == 0 || kprev != key)) atomicMax(&slots[key], v);
+}
+
+__global__ void __launch_bounds__(kGsBlock, 1) k_gs_batch(GsBatchArgs B) {
+  const GsArgs& A = B.g;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  const int nc = *B.nc_dev;
+  const int S = B.S;
+  for (int sc = tid; sc < S; sc += nthr) {
+    B.best[sc] = INFINITY;
+    B.bestbuf[sc] = 0;
+    B.iters[sc] = 0;
+    const bool empty = B.sc_off[sc + 1] == B.sc_off[sc];
+    B.done[sc] = empty ? 1 : 0;
+    if (empty) atomicAdd(B.done_count, 1);
+  }
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval_every = A.eval_every ? A.eval_every : 1u;
+  double2* bufs[2] = {A.r_a, A.r_b};
+  if (!grid_sync(A.gb, A.spin)) {
+    if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+    return;
+  }
+  unsigned n_eval = 0;
+  unsigned it = 0;
+  if (*((volatile int*)B.done_count) < S) {
+    for (it = 1; it <= A.max_iters; ++it) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + tid; s < e; s += nthr) {
+          const int k = A.perm[s];
+          if (__ldcg(&B.done[B.cscene[k]])) continue;
+          gs_update(A, k);
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      if (it % eval_every != 0) continue;
+      const int slot = n_eval % 3;
+      unsigned long long* slots = B.err_slot + (size_t)slot * S;
+      const int lane = threadIdx.x & 31;
+      for (int k0 = tid - lane; k0 < nc; k0 += nthr) {
+        const int k = k0 + lane;
+        int key = -1;
+        unsigned long long v = 0ull;
+        if (k < nc) {
+          const int sc = B.cscene[k];
+          if (!__ldcg(&B.done[sc])) {
+            const int a = A.ia[k], b = A.ib[k];
+            const bool has_b = b >= 0;
+            const double2 va = __ldcg(&A.v[a]);
+            const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+            double u0, u1;
+            local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+            const double2 rk = __ldcg(&A.r[k]);
+            bufs[1 - __ldcg(&B.bestbuf[sc])][k] = rk;
+            v = f64_to_ordered(fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+            key = sc;
+          }
+        }
+        run_max_atomic(v, key, slots);
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      unsigned long long* next = B.err_slot + (size_t)((n_eval + 1) % 3) * S;
+      for (int sc = tid; sc < S; sc += nthr) {
+        next[sc] = 0ull;
+        if (B.done[sc]) continue;
+        const double err = ordered_to_f64(__ldcg(&slots[sc]));
+        if (err < B.best[sc]) {
+          B.best[sc] = err;
+          B.bestbuf[sc] ^= 1;
+        }
+        if (err < A.tol) {
+          B.done[sc] = 1;
+          B.iters[sc] = it;
+          atomicAdd(B.done_count, 1);
+        }
+      }
+      ++n_eval;
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      if (*((volatile int*)B.done_count) == S) break;
+    }
+  }
+  // Scenes that did not converge return their best iterate (GaussSeidel: x = x_best).
+  for (int k = tid; k < nc; k += nthr) {
+    const int sc = B.cscene[k];
+    if (__ldcg(&B.done[sc])) continue;
+    if (__ldcg(&B.best[sc]) < INFINITY) A.r[k] = __ldcg(&bufs[__ldcg(&B.bestbuf[sc])][k]);
+  }
+  for (int sc = tid; sc < S; sc += nthr)
+    if (!__ldcg(&B.done[sc])) B.iters[sc] = A.max_iters;
+  if (tid == 0) *B.unconverged += (unsigned long long)(S - *((volatile int*)B.done_count));
+  if (tid == 0) {
+    A.st->iterations = it > A.max_iters ? A.max_iters : it;
+    A.st->sweeps64 = it > A.max_iters ? A.max_iters : it;
     A.st->evals = n_eval;
   }
 }
@@ -930,7 +1083,7 @@ int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc) {
   return SG_OK;
 }
 
-int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib) {
+int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const int* nc_dev) {
   cudaStream_t s = ctx->stream;
   int* cnt = ctx->body_cnt.as<int>();
   int* off = ctx->body_off.as<int>();
@@ -942,21 +1095,22 @@ int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int*
   SG_CUDA_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * (size_t)(nb + 1), s));
   SG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(SolveStats), s));
   if (nc > 0) {
-    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, cnt);
+    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, nc_dev, ia, ib, cnt);
     SG_CUDA_TRY(cudaGetLastError());
   }
   if (int r = scan_exclusive(ctx, cnt, off, nb)) return r;
   ctx->kernel_launches += nb > 0 ? 3 : 0;
   if (nc == 0) return SG_OK;
-  k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, off, fill, adj);
+  k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, nc_dev, ia, ib, off, fill, adj);
   k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
   SG_CUDA_TRY(cudaGetLastError());
   SG_CUDA_TRY(cudaMemsetAsync(ctx->color.p, 0xff, sizeof(int) * (size_t)nc, s));
   SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-  ColorArgs CA{nc, ia, ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit, 4096};
+  ColorArgs CA{nc, nc_dev, ia, ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit,
+               4096};
   void* args[] = {&CA};
   const int g = coop_grid(ctx, k_color_jp, nc, kBlock);
-  SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_color_jp, dim3(g), dim3(kBlock), args, 0, s));
+  SG_CUDA_TRY(launch_cooperative((const void*)k_color_jp, g, kBlock, args, s));
   ctx->kernel_launches += 4;  // body_count, body_fill, body_sort, colouring
   return SG_OK;
 }
@@ -1078,6 +1232,65 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     return SG_CAPACITY;
   }
   return ctx->h_stats.converged ? SG_OK : SG_NOT_CONVERGED;
+}
+
+int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp, const BatchSolve& X) {
+  const int nb = P.nb, cap = P.nc;
+  cudaStream_t s = ctx->stream;
+  int* off = ctx->body_off.as<int>();
+  int* adj = ctx->body_adj.as<int>();
+  SolveStats* st = ctx->stats.as<SolveStats>();
+  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  const double2* n2 = reinterpret_cast<const double2*>(P.n);
+  double2* r2 = reinterpret_cast<double2*>(P.r);
+  if (int r = prepare_contact_graph(ctx, nb, cap, P.ia, P.ib, X.nc_dev)) return r;
+  double2* vrun = ctx->v_run.as<double2>();
+  k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
+                                               P.minv, vrun);
+  SG_CUDA_TRY(cudaGetLastError());
+  SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+  SG_CUDA_TRY(cudaMemsetAsync(X.err_slot, 0, sizeof(unsigned long long) * 3 * (size_t)X.S, s));
+  SG_CUDA_TRY(cudaMemsetAsync(X.done_count, 0, sizeof(int), s));
+  GsBatchArgs B;
+  GsArgs& GA = B.g;
+  GA.nc = cap;
+  GA.ia = P.ia;
+  GA.ib = P.ib;
+  GA.n = n2;
+  GA.c = reinterpret_cast<const double2*>(P.c);
+  GA.W = P.W;
+  GA.mu = P.mu;
+  GA.minv = P.minv;
+  GA.perm = ctx->perm.as<int>();
+  GA.r = r2;
+  GA.r_a = ctx->r_cand.as<double2>();
+  GA.r_b = ctx->r_best.as<double2>();
+  GA.v = vrun;
+  GA.st = st;
+  GA.gb = gb;
+  GA.spin = ctx->spin_limit;
+  GA.tol = sp.tol;
+  GA.max_iters = sp.max_iters;
+  GA.eval_every = sp.eval_every;
+  B.nc_dev = X.nc_dev;
+  B.cscene = X.cscene;
+  B.sc_off = X.sc_off;
+  B.S = X.S;
+  B.err_slot = X.err_slot;
+  B.best = X.best;
+  B.bestbuf = X.bestbuf;
+  B.done = X.done;
+  B.iters = X.iters;
+  B.done_count = X.done_count;
+  B.unconverged = X.unconverged;
+  void* args[] = {&B};
+  const int g = coop_grid(ctx, k_gs_batch, std::max(cap, X.S), kGsBlock, 1);
+  SG_CUDA_TRY(launch_cooperative((const void*)k_gs_batch, g, kGsBlock, args, s));
+  k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
+                                                     P.m, P.minv, reinterpret_cast<double2*>(P.v2));
+  SG_CUDA_TRY(cudaGetLastError());
+  ctx->kernel_launches += 3;  // vel_init, gs, final velocity
+  return SG_OK;
 }
 
 int wait_timeout_selftest(sg_ctx* ctx) {
@@ -1299,11 +1512,11 @@ int sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int3
       set_error("sg_sobogus_solve_2d_noalloc: contact body index out of range or tangent not (-n_y, n_x)");
       return SG_BAD_INPUT;
     }
-    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, cnt);
+    k_body_count<<<blocks_for(nc), kBlock, 0, s>>>(nc, nullptr, ia, ib, cnt);
   }
   if (int r = scan_exclusive_raw(cnt, off, nb, tiles, s)) return r;
   if (nc > 0) {
-    k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, ib, off, fill, adj);
+    k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, nullptr, ia, ib, off, fill, adj);
     k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
   }
   if (nb > 0)
@@ -1322,7 +1535,7 @@ int sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int3
   const unsigned long long spin = 1ull << 22;  // about a second of barrier polls
   if (nc > 0) {
     SG_CUDA_TRY(cudaMemsetAsync(color, 0xff, sizeof(int) * (size_t)nc, s));
-    ColorArgs CA{nc, ia, ib, off, adj, color, perm, st, gb, spin, 4096};
+    ColorArgs CA{nc, nullptr, ia, ib, off, adj, color, perm, st, gb, spin, 4096};
     void* cargs[] = {&CA};
     SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_color_jp, dim3(grid_for(k_color_jp)), dim3(kBlock), cargs, 0, s));
     SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));

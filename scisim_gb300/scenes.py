@@ -11,6 +11,8 @@ No public dataset is involved: every scene is generated from a fixed seed.
                   fill of a 40 x 60 box (area fraction ~0.5) built by size-sorted
                   shelf packing with random slack, rows shuffled, bodies permuted;
                   four walls; gravity -9.81, dt 0.005, CoR 0, mu 0.4
+  ball2d_batch    4,096 independent Ball2D scenes of 16-4,096 discs (log-uniform), radii
+                  U[0.03, 0.05], per-scene mu U[0.1, 0.8] and CoR U[0, 0.5], dt 0.01
   sphere_pile     65,536 spheres, r ~ U[0.05, 0.1], density 1, jittered lattice of spacing
                   0.2 filling a 6 x 6 footprint (volume fraction ~0.18 of a 6 x 6 x 20
                   box), v ~ N(0, 0.1^2), omega ~ N(0, 1), identity orientations; floor
@@ -94,6 +96,50 @@ def dense_pile(n: int = 262144, seed: int = 2, width: float = 40.0, height: floa
     plane_n = np.array([[0.0, 1.0], [1.0, 0.0], [-1.0, 0.0], [0.0, -1.0]])
     return dict(q=q.reshape(-1), v=v, r=r, m=m, plane_x=plane_x, plane_n=plane_n, dt=0.005, gravity=(0.0, -9.81),
                 CoR=0.0, mu=0.4, tol=1e-6, max_iters=5000, name="dense_pile_%d" % n)
+
+
+def ball2d_batch(n_scenes: int = 4096, seed: int = 3, nmin: int = 16, nmax: int = 4096, rmin: float = 0.03,
+                 rmax: float = 0.05, spacing: float = 0.11):
+    """Independent Ball2D scenes: disc counts log-uniform in [nmin, nmax], radii U[rmin, rmax],
+    density 1, a jittered square lattice per scene above its floor between two walls,
+    v ~ N(0, 0.1^2), per-scene mu ~ U[0.1, 0.8] and CoR ~ U[0, 0.5]; symplectic Euler
+    dt 0.01, gravity (0, -9.81).  Every scene lives in its own coordinates."""
+    rng = np.random.default_rng(seed)
+    counts = np.rint(np.exp(rng.uniform(math.log(nmin), math.log(nmax), n_scenes))).astype(np.int64)
+    body_off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    plane_off = (3 * np.arange(n_scenes + 1)).astype(np.int32)
+    N = int(body_off[-1])
+    q = np.empty((N, 2))
+    r = rng.uniform(rmin, rmax, N)
+    px = np.empty((3 * n_scenes, 2))
+    pn = np.empty((3 * n_scenes, 2))
+    jit = 0.5 * spacing - rmax - 1e-3
+    for s in range(n_scenes):
+        n = int(counts[s])
+        side = int(math.ceil(math.sqrt(n)))
+        k = np.arange(n)
+        ix, iy = k % side, k // side
+        x = (ix - 0.5 * (side - 1)) * spacing + rng.uniform(-jit, jit, n)
+        y = 0.5 * spacing + iy * spacing + rng.uniform(-jit, jit, n)
+        q[body_off[s]:body_off[s + 1]] = np.stack([x, y], 1)
+        half = 0.5 * side * spacing + 0.05
+        px[3 * s:3 * s + 3] = [[0.0, 0.0], [-half, 0.0], [half, 0.0]]
+        pn[3 * s:3 * s + 3] = [[0.0, 1.0], [1.0, 0.0], [-1.0, 0.0]]
+    v = rng.normal(0.0, 0.1, 2 * N)
+    mu = rng.uniform(0.1, 0.8, n_scenes)
+    CoR = rng.uniform(0.0, 0.5, n_scenes)
+    return dict(body_off=body_off, plane_off=plane_off, q=q.reshape(-1), v=v, r=r, m=math.pi * r * r,
+                plane_x=px, plane_n=pn, mu=mu, CoR=CoR, dt=0.01, gravity=(0.0, -9.81), tol=1e-6, max_iters=5000,
+                name="ball2d_batch_%d" % n_scenes)
+
+
+def batch_scene(b, s):
+    """Scene s of a batch as a standalone Ball2D scene (local indices)."""
+    b0, b1 = int(b["body_off"][s]), int(b["body_off"][s + 1])
+    p0, p1 = int(b["plane_off"][s]), int(b["plane_off"][s + 1])
+    return dict(q=b["q"][2 * b0:2 * b1], v=b["v"][2 * b0:2 * b1], r=b["r"][b0:b1], m=b["m"][b0:b1],
+                plane_x=b["plane_x"][p0:p1], plane_n=b["plane_n"][p0:p1], mu=float(b["mu"][s]),
+                CoR=float(b["CoR"][s]), dt=b["dt"], gravity=b["gravity"])
 
 
 def sphere_mass_inertia(r, density=1.0):
