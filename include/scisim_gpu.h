@@ -220,6 +220,37 @@ SG_API int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1
               const double* q0b, const double* q1b, const double* rb, double* coeffs, int32_t* hit,
               double* t);
 
+/* Learned warm start for single Ball2D scenes (no counterpart in the reference, whose solve
+ * starts from the impulse cache, GeometricImpactFrictionMap.cpp:174-220).  A 12 -> 64 -> 64 -> 3
+ * network (GELU) maps 12 per-contact features (relative velocity, gap, mass ratio, gravity
+ * direction, mu, CoR, cached impulse, coordination; scaled by |g| dt and the contact's
+ * effective mass) to a start impulse for the contacts the impulse cache missed (cached
+ * contacts keep their cached impulse); each step evaluates the FP64
+ * Coulomb residual of the cache start and of the network start and solves from the smaller,
+ * to the same tolerance as ever.  Parameters: W1 (64x12 row-major), b1 (64), W2 (64x64), b2,
+ * W3 (3x64), b3 (3): sg_mlp_param_count() floats.  Inference runs on the tensor cores (BF16
+ * inputs and weights, FP32 accumulation); training (FP32 forward, backward, Adam) on CUDA cores. */
+SG_API int sg_mlp_param_count(void);
+SG_API int sg_mlp_load(sg_ctx* ctx, const float* params, int32_t n_params);
+/* warm_start: use the loaded network in every step; record: keep each step's features and
+ * targets (the converged impulses, scaled) for sg_mlp_last_samples. */
+SG_API int sg_mlp_enable(sg_ctx* ctx, int32_t warm_start, int32_t record);
+/* Features (12 per contact) and targets (3 per contact) of the last recorded step.  Returns
+ * the sample count, -(count+1) if cap is too small, INT64_MIN when recording is off. */
+SG_API int64_t sg_mlp_last_samples(sg_ctx* ctx, int64_t cap, float* x, float* t);
+/* Trains params (in: initial, out: trained) with Adam on n samples for `epochs` passes in
+ * minibatches of `batch`; epoch_loss (may be NULL) receives the mean loss of each epoch. */
+SG_API int sg_mlp_train(sg_ctx* ctx, int64_t n, const float* x, const float* t, int32_t epochs, int32_t batch,
+                        float lr, uint64_t seed, float* params, double* epoch_loss);
+/* Mean loss and its gradient over n samples (the training kernel's forward and backward). */
+SG_API int sg_mlp_grad(sg_ctx* ctx, const float* params, int32_t n, const float* x, const float* t, float* grad,
+                       double* loss);
+/* Network outputs (3 per sample): tensor_cores = 1 runs the BF16 inference kernel, 0 the FP32 one. */
+SG_API int sg_mlp_infer(sg_ctx* ctx, const float* params, int32_t n, const float* x, float* y,
+                        int32_t tensor_cores);
+/* Steps that evaluated the network start and steps that solved from it. */
+SG_API int sg_mlp_stats(sg_ctx* ctx, uint64_t* steps_evaluated, uint64_t* steps_network_start);
+
 /* Counters of the work done since the last reset (no counterpart in SCISim, which has
  * no timing instrumentation: scisim/Timer/TimeUtils.cpp only prints wall-clock strings).
  * gs_ms sums the CUDA-event durations of the Gauss-Seidel kernel (recorded only while

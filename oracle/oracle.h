@@ -180,6 +180,13 @@ int64_t or_sphere3d_active_set(const or_sphere3d* s, const double* q0, const dou
 int64_t or_sphere3d_last_contacts(const or_sphere3d* s, int64_t cap, int32_t* ia, int32_t* ib, double* bases,
                                   double* arm_a, double* arm_b, double* alpha, double* beta);
 
+// ---------------------------------------------------------------- warm-start network
+// 12 -> 64 -> 64 -> 3 MLP with GELU; parameters W1 (64x12), b1, W2 (64x64), b2, W3 (3x64), b3.
+int or_mlp_param_count(void);
+void or_mlp_forward(const float* params, int n, const float* x, double* y);
+// Mean loss over n samples and its gradient (FP64) with respect to the packed parameters.
+double or_mlp_loss_grad(const float* params, int n, const float* x, const float* t, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

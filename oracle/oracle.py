@@ -96,6 +96,10 @@ def lib():
         L.or_ball2d_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_uint32]
         L.or_residual_2d.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
         L.or_residual_2d.restype = C.c_double
+        L.or_mlp_param_count.restype = C.c_int
+        L.or_mlp_forward.argtypes = [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), _dp]
+        L.or_mlp_loss_grad.argtypes = [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), _dp]
+        L.or_mlp_loss_grad.restype = C.c_double
         L.or_sobogus_solve_3d.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp,
                                           _dp, _dp, C.POINTER(GsParams), _dp, _dp, _dp, _dp,
                                           C.POINTER(GsResult)]
@@ -442,3 +446,29 @@ class Sphere3D:
         q1, v1 = np.zeros_like(q0), np.zeros_like(v0)
         lib().or_sphere3d_umap(self._h, _d(q0), _d(v0), _d(q1), _d(v1))
         return q1, v1
+
+
+# ------------------------------------------------------------------ warm-start network
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def mlp_param_count():
+    return lib().or_mlp_param_count()
+
+
+def mlp_forward(params, x):
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 12)
+    y = np.zeros((x.shape[0], 3))
+    lib().or_mlp_forward(_fp(params), x.shape[0], _fp(x), _d(y))
+    return y
+
+
+def mlp_loss_grad(params, x, t):
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 12)
+    t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 3)
+    g = np.zeros(params.shape[0])
+    loss = lib().or_mlp_loss_grad(_fp(params), x.shape[0], _fp(x), _fp(t), _d(g))
+    return loss, g

@@ -82,6 +82,17 @@ SIGNATURES = {
                                               C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint32)]),
     "sg_broadphase_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _i64, _ip, C.POINTER(_i64)]),
     "sg_ccd_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp]),
+    "sg_mlp_param_count": (C.c_int, []),
+    "sg_mlp_load": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
+    "sg_mlp_enable": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "sg_mlp_last_samples": (_i64, [C.c_void_p, _i64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "sg_mlp_train": (C.c_int, [C.c_void_p, _i64, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, C.c_int32,
+                               C.c_float, C.c_uint64, C.POINTER(C.c_float), _dp]),
+    "sg_mlp_grad": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
+                              C.POINTER(C.c_float), C.POINTER(C.c_float), _dp]),
+    "sg_mlp_infer": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
+                               C.POINTER(C.c_float), C.c_int32]),
+    "sg_mlp_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "sg_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -128,6 +139,31 @@ def f64(a):
 
 def i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def mlp_param_count():
+    return lib().sg_mlp_param_count()
+
+
+def mlp_init(seed=0):
+    """Initial network parameters (scaled normal weights, zero biases), packed as the C ABI
+    expects: W1 (64x12), b1, W2 (64x64), b2, W3 (3x64), b3."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_in, fan_out in ((12, 64), (64, 64), (64, 3)):
+        parts.append(rng.normal(0.0, (2.0 / (fan_in + fan_out)) ** 0.5, (fan_out, fan_in)).reshape(-1))
+        parts.append(np.zeros(fan_out))
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.shape[0] == mlp_param_count()
+    return p
 
 
 def _g3(gravity):
@@ -291,6 +327,54 @@ class Context:
         ncol = C.c_int32(0)
         L.sg_last_solve_order(self._h, nc, iptr(order), iptr(offs), C.byref(ncol))
         return order, offs[: ncol.value + 1].copy()
+
+    # -- learned warm start ------------------------------------------------------
+    def mlp_load(self, params):
+        params = f32(params)
+        check(lib().sg_mlp_load(self._h, fptr(params), params.shape[0]), "sg_mlp_load")
+
+    def mlp_enable(self, warm_start=True, record=False):
+        check(lib().sg_mlp_enable(self._h, 1 if warm_start else 0, 1 if record else 0), "sg_mlp_enable")
+
+    def mlp_last_samples(self):
+        L = lib()
+        n = L.sg_mlp_last_samples(self._h, 0, None, None)
+        if n == -(2 ** 63):
+            raise SgError(SG_BAD_INPUT, "sg_mlp_last_samples")
+        n = -n - 1 if n < 0 else n
+        x, t = np.empty((n, 12), np.float32), np.empty((n, 3), np.float32)
+        got = L.sg_mlp_last_samples(self._h, n, fptr(x), fptr(t))
+        if got != n:
+            raise SgError(SG_CUDA_ERROR, "sg_mlp_last_samples")
+        return x, t
+
+    def mlp_train(self, x, t, params, epochs=5, batch=4096, lr=1e-3, seed=0):
+        x, t = f32(x).reshape(-1, 12), f32(t).reshape(-1, 3)
+        p = f32(params).copy()
+        losses = np.zeros(epochs)
+        check(lib().sg_mlp_train(self._h, x.shape[0], fptr(x), fptr(t), epochs, batch, lr, seed, fptr(p),
+                                 dptr(losses)), "sg_mlp_train")
+        return p, losses
+
+    def mlp_grad(self, params, x, t):
+        params, x, t = f32(params), f32(x).reshape(-1, 12), f32(t).reshape(-1, 3)
+        g = np.zeros(params.shape[0], np.float32)
+        loss = C.c_double(0.0)
+        check(lib().sg_mlp_grad(self._h, fptr(params), x.shape[0], fptr(x), fptr(t), fptr(g), C.byref(loss)),
+              "sg_mlp_grad")
+        return loss.value, g
+
+    def mlp_infer(self, params, x, tensor_cores=True):
+        params, x = f32(params), f32(x).reshape(-1, 12)
+        y = np.zeros((x.shape[0], 3), np.float32)
+        check(lib().sg_mlp_infer(self._h, fptr(params), x.shape[0], fptr(x), fptr(y), 1 if tensor_cores else 0),
+              "sg_mlp_infer")
+        return y
+
+    def mlp_stats(self):
+        a, b = C.c_uint64(0), C.c_uint64(0)
+        check(lib().sg_mlp_stats(self._h, C.byref(a), C.byref(b)), "sg_mlp_stats")
+        return dict(evaluated=a.value, network_start=b.value)
 
     def profile_enable(self, on=True):
         check(lib().sg_profile_enable(self._h, 1 if on else 0), "sg_profile_enable")

@@ -99,6 +99,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   ctx->last_nc = nc;
   ctx->last_nbb = npairs;
   if (nc == 0) {
+    ctx->mlp_last_n = 0;
     // No active constraints: keep the predictor and clear the cache (:286-298).
     std::swap(ctx->q, ctx->q1);
     std::swap(ctx->v, ctx->v1);
@@ -126,7 +127,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   P.mu = ctx->mu.as<double>();
   P.r = ctx->r_loc.as<double>();
   P.v2 = ctx->v2.as<double>();
-  SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, ctx->cfg.precision};
+  SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, ctx->cfg.precision, true};
   const int sr = solve_contacts(ctx, P, sp);
   if (sr != SG_OK && sr != SG_NOT_CONVERGED) return sr;
   st.iterations = ctx->h_stats.iterations;
@@ -199,6 +200,9 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->r3, &ctx->r3a, &ctx->r3b, &ctx->ab3, &ctx->vrun3, &ctx->pk_ab, &ctx->pk_n, &ctx->pk_c,
                   &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32};
   for (Buf* b : bufs3) release(*b);
+  Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
+                  &ctx->mlp_choice};
+  for (Buf* b : bufsm) release(*b);
   Buf* bufsb[] = {&ctx->sb_off,  &ctx->sp_off,   &ctx->sf_off,      &ctx->scene_of, &ctx->s_mu,    &ctx->s_CoR,
                   &ctx->s_grid,  &ctx->s_cells,  &ctx->s_cell_off,  &ctx->s_nc,     &ctx->s_npairs, &ctx->sc_off,
                   &ctx->prev_sc_off, &ctx->cscene, &ctx->b_ctl,     &ctx->b_sums,   &ctx->s_err,   &ctx->s_best,

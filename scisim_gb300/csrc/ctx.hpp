@@ -92,6 +92,7 @@ struct SolveParams {
   unsigned int max_iters;
   unsigned int eval_every;
   int precision;
+  bool learned = false;  // a scene step: the learned warm start and sample recording apply
 };
 
 }  // namespace sg
@@ -144,6 +145,12 @@ struct sg_ctx {
   sg::Buf snap_q, snap_v, snap_key, snap_ab, snap_off;
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_launches = 0;  // kernel launches per graph replay
+  // Learned warm start (mlp_kernels.cu): network parameters, per-contact features and
+  // targets of the last step, training samples, start-selection slots and counter.
+  bool mlp_loaded = false, mlp_on = false, mlp_record = false;
+  int64_t mlp_last_n = 0;
+  uint64_t mlp_evals = 0;
+  sg::Buf mlp_p, mlp_feat, mlp_tgt, mlp_x, mlp_t, mlp_slots, mlp_choice;
   // buffers of the standalone FrictionSolver entry (kept apart from the scene)
   sg::Buf fs_m, fs_minv, fs_v0, fs_v2;
 
@@ -225,6 +232,12 @@ int coop_grid(sg_ctx* ctx, K kernel, long work, int block, int max_per_sm = 64) 
 // capture) and one step enqueued without host synchronisation.
 int batch2d_reserve(sg_ctx* ctx, int cap);
 int batch2d_step_enqueue(sg_ctx* ctx);
+
+// Learned warm start (mlp_kernels.cu).
+int mlp_param_count();
+int mlp_features(sg_ctx* ctx, const ContactProblem& P);
+int mlp_predict(sg_ctx* ctx, const ContactProblem& P, double* r_alt);
+int mlp_targets(sg_ctx* ctx, const ContactProblem& P);
 
 // RigidBody3D sphere scenes (sphere3d_kernels.cu).
 int sphere3d_update_inertia(sg_ctx* ctx, bool construction);

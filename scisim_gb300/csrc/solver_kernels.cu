@@ -1052,6 +1052,37 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
   }
 }
 
+// FP64 Coulomb residual of a start impulse r at running velocities v (one residual
+// evaluation of k_gs), maximum into *slot (ordered encoding).
+__global__ void k_start_err(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
+                            const double2* __restrict__ n, const double2* __restrict__ c,
+                            const double* __restrict__ mu, const double2* __restrict__ r,
+                            const double2* __restrict__ v, unsigned long long* slot) {
+  double emax = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
+    const int a = ia[k], b = ib[k];
+    const bool has_b = b >= 0;
+    const double2 va = v[a];
+    const double2 vb = has_b ? v[b] : make_double2(0.0, 0.0);
+    double u0, u1;
+    local_velocity(n[k], c[k], va, has_b, vb, u0, u1);
+    const double2 rk = r[k];
+    emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, mu[k]));
+  }
+  emax = block_nanmax(emax);
+  if (threadIdx.x == 0) atomicMax(slot, f64_to_ordered(emax));
+}
+
+// Keeps the start with the smaller residual (slot[0]: current, slot[1]: network).
+__global__ void k_select_start(int nc, double2* __restrict__ r, const double2* __restrict__ r_alt,
+                               const unsigned long long* __restrict__ slot, unsigned long long* chosen) {
+  const double e_cur = ordered_to_f64(slot[0]), e_alt = ordered_to_f64(slot[1]);
+  const bool take = e_alt < e_cur;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0 && take) *chosen += 1ull;
+  if (k < nc && take) r[k] = r_alt[k];
+}
+
 __global__ void k_wait_flag(const int* flag, int* status, unsigned long long spin) {
   volatile const int* f = flag;
   unsigned long long n = 0;
@@ -1129,6 +1160,34 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
   // Adjacency and colouring first: the velocity initialisation reads the adjacency.
   if (int r = prepare_contact_graph(ctx, nb, nc, P.ia, P.ib)) return r;
   double2* vrun = ctx->v_run.as<double2>();
+  if (sp.learned && nc > 0 && (ctx->mlp_on || ctx->mlp_record)) {
+    if (int r = mlp_features(ctx, P)) return r;
+    if (ctx->mlp_on) {
+      // Network start into the (not yet used) candidate buffer; the start with the smaller
+      // FP64 residual goes to the solve.
+      double2* r_alt = ctx->r_cand.as<double2>();
+      if (int r = mlp_predict(ctx, P, reinterpret_cast<double*>(r_alt))) return r;
+      if (int r = grow(ctx->mlp_slots, 2 * sizeof(unsigned long long))) return r;
+      if (!ctx->mlp_choice.p) {
+        if (int r = grow(ctx->mlp_choice, sizeof(unsigned long long))) return r;
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->mlp_choice.p, 0, sizeof(unsigned long long), s));
+      }
+      unsigned long long* slots = ctx->mlp_slots.as<unsigned long long>();
+      SG_CUDA_TRY(cudaMemsetAsync(slots, 0, 2 * sizeof(unsigned long long), s));
+      const int eb = std::max(1, std::min(blocks_for(nc), ctx->num_sms * 8));
+      const double2* starts[2] = {r2, r_alt};
+      for (int w = 0; w < 2; ++w) {
+        k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, starts[w],
+                                                     reinterpret_cast<const double2*>(P.v0), P.minv, vrun);
+        k_start_err<<<eb, kBlock, 0, s>>>(nc, P.ia, P.ib, n2, reinterpret_cast<const double2*>(P.c), P.mu, starts[w],
+                                          vrun, slots + w);
+      }
+      k_select_start<<<blocks_for(nc), kBlock, 0, s>>>(nc, r2, r_alt, slots, ctx->mlp_choice.as<unsigned long long>());
+      SG_CUDA_TRY(cudaGetLastError());
+      ctx->mlp_evals += 1;
+      ctx->kernel_launches += 5;
+    }
+  }
   k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                P.minv, vrun);
   SG_CUDA_TRY(cudaGetLastError());
@@ -1204,6 +1263,10 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
   k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                      P.m, P.minv, reinterpret_cast<double2*>(P.v2));
   SG_CUDA_TRY(cudaGetLastError());
+  if (sp.learned && ctx->mlp_record) {
+    if (int r = mlp_targets(ctx, P)) return r;
+    ctx->mlp_last_n = nc;
+  }
   SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
   SG_CUDA_TRY(cudaStreamSynchronize(s));
   if (nc == 0) {

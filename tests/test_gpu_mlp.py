@@ -1,0 +1,159 @@
+"""Learned warm start: the network's GPU kernels against the CPU oracle, and what the trained
+network gains over the solve without it.
+
+Bars: FP32 training gradients within 2e-3 relative (norm) of the FP64 oracle; FP32 inference
+within 1e-4 and BF16 tensor-core inference within 3e-2 (relative to the output scale) of the
+oracle; recorded features equal to a host restatement within 1e-5; a trained network starts a
+cold solve closer to the solution than zero does, and the cache-or-network start never costs
+more than 10 % extra sweeps over the cache start alone.
+"""
+import numpy as np
+import pytest
+
+from scisim_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_data(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0.0, 1.0, (n, 12)).astype(np.float32)
+    t = np.stack([np.tanh(x[:, 0] - 0.5 * x[:, 2]) + 0.3 * x[:, 8], 0.2 * x[:, 1] * x[:, 6],
+                  (x[:, 0] + x[:, 4] > 0).astype(np.float64)], 1).astype(np.float32)
+    return x, t
+
+
+def test_mlp_gradients_match_oracle(gpulib, oracle):
+    ctx = gpulib.Context()
+    p = gpulib.mlp_init(3)
+    p += np.random.default_rng(4).normal(0, 0.05, p.shape).astype(np.float32)  # nonzero biases
+    for n in (1, 127, 1000):
+        x, t = rand_data(n, n)
+        lg, gg = ctx.mlp_grad(p, x, t)
+        lo, go = oracle.mlp_loss_grad(p, x, t)
+        assert abs(lg - lo) <= 1e-4 * max(1.0, abs(lo))
+        assert np.linalg.norm(gg - go) <= 2e-3 * np.linalg.norm(go)
+
+
+def test_mlp_inference_fp32_and_bf16(gpulib, oracle):
+    ctx = gpulib.Context()
+    p = gpulib.mlp_init(5)
+    x, _ = rand_data(4099, 9)   # not a multiple of 16: ragged last tile
+    yo = oracle.mlp_forward(p, x)
+    scale = np.abs(yo).max(0) + 1e-3
+    y32 = ctx.mlp_infer(p, x, tensor_cores=False)
+    ytc = ctx.mlp_infer(p, x, tensor_cores=True)
+    assert np.abs(y32 - yo).max(0).max() <= 1e-4 * scale.max()
+    assert np.all(np.abs(ytc - yo).max(0) <= 3e-2 * scale)
+
+
+def test_mlp_training_reduces_loss(gpulib):
+    ctx = gpulib.Context()
+    x, t = rand_data(20000, 1)
+    p0 = gpulib.mlp_init(0)
+    p, losses = ctx.mlp_train(x, t, p0, epochs=8, batch=512, lr=3e-3, seed=7)
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.5 * losses[0]
+    l_end, _ = ctx.mlp_grad(p, x, t)
+    assert abs(l_end - losses[-1]) < 0.25 * losses[0]
+
+
+def pile_ctx(gpulib, s, **kw):
+    cfg = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, max_iters=3000,
+               cache_mode=gpulib.CACHE_NORMAL_AND_FRICTION)
+    cfg.update(kw)
+    ctx = gpulib.Context(**cfg)
+    ctx.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    return ctx
+
+
+def test_mlp_features_match_host_restatement(gpulib):
+    s = scenes.box_drop_1024()
+    ctx = pile_ctx(gpulib, s, mu=0.5, CoR=0.3)
+    ctx.mlp_load(gpulib.mlp_init(0))
+    ctx.mlp_enable(warm_start=False, record=True)
+    ctx.step(40)
+    prev = ctx.last_contacts()
+    q0, v0 = ctx.state()
+    ctx.step(1)
+    x, _ = ctx.mlp_last_samples()
+    c = ctx.last_contacts()
+    nc = c["ia"].shape[0]
+    assert x.shape == (nc, 12) and nc > 100
+    q, v, r, m = q0.reshape(-1, 2), v0.reshape(-1, 2), s["r"], s["m"]
+    minv = 1.0 / m
+    g = np.array(s["gravity"])
+    vs = np.linalg.norm(g) * s["dt"]
+    deg = np.bincount(np.concatenate([c["ia"], c["ib"][c["ib"] >= 0]]), minlength=r.shape[0])
+    key_prev = {(int(a), int(b)): (al, be) for a, b, al, be in zip(prev["ia"], prev["ib"], prev["alpha"], prev["beta"])}
+    px, pn = np.asarray(s["plane_x"]), np.asarray(s["plane_n"], float)
+    pn = pn / np.linalg.norm(pn, axis=1, keepdims=True)
+    for k in range(nc):
+        a, b = int(c["ia"][k]), int(c["ib"][k])
+        n = c["n"][k]
+        t = np.array([-n[1], n[0]])
+        if b >= 0:
+            vr = v[a] - v[b]
+            gap = np.linalg.norm(q[a] - q[b]) - r[a] - r[b]
+            mr = minv[b] / (minv[a] + minv[b])
+            dg = deg[a] + deg[b]
+            W00 = minv[a] + minv[b]
+        else:
+            vr = v[a]
+            gap = pn[-1 - b] @ (q[a] - px[-1 - b]) - r[a]
+            mr = 0.0
+            dg = deg[a]
+            W00 = minv[a]
+        al, be = key_prev.get((a, b), (0.0, 0.0))
+        meff = 1.0 / W00
+        want = [np.arcsinh(n @ vr / vs), np.arcsinh(t @ vr / vs), np.arcsinh(gap / (vs * s["dt"])), mr,
+                g @ n / np.linalg.norm(g), g @ t / np.linalg.norm(g), 0.5, 0.3, np.arcsinh(al / (meff * vs)),
+                np.arcsinh(be / (meff * vs)), 1.0 if (al != 0 or be != 0) else 0.0, dg / 8.0]
+        np.testing.assert_allclose(x[k], np.array(want, np.float32), rtol=1e-5, atol=1e-5)
+
+
+def test_mlp_trained_start_gains(gpulib):
+    """Record the plain solver's samples over the box drop's 200 steps, train, then from the
+    step-200 state: (a) with no cache and 100 sweeps per step, the network start ends closer
+    to the solution than the zero start; (b) with the cache, the cache-or-network start needs
+    at most 10 % more sweeps than the cache start to reach 1e-6."""
+    s = scenes.box_drop_1024()
+    rec = pile_ctx(gpulib, s, mu=0.5, CoR=0.3)
+    rec.mlp_load(gpulib.mlp_init(0))
+    rec.mlp_enable(warm_start=False, record=True)
+    xs, ts = [], []
+    for _ in range(200):
+        rec.step(1)
+        x, t = rec.mlp_last_samples()
+        xs.append(x)
+        ts.append(t)
+    q_held, v_held = rec.state()
+    X, T = np.concatenate(xs), np.concatenate(ts)
+    assert X.shape[0] > 100000
+    p, losses = rec.mlp_train(X, T, gpulib.mlp_init(1), epochs=8, batch=2048, lr=2e-3, seed=3)
+    assert losses[-1] < 0.8 * losses[0]
+
+    def run(cache, mlp, max_iters, steps=20, prime=10):
+        ctx = pile_ctx(gpulib, dict(s, q=q_held, v=v_held), mu=0.5, CoR=0.3, cache_mode=cache, max_iters=max_iters)
+        ctx.step(prime)  # identical priming steps (deterministic): same state and cache in every run
+        if mlp:
+            ctx.mlp_load(p)
+            ctx.mlp_enable(warm_start=True)
+        its, logerr = 0, 0.0
+        for _ in range(steps):
+            st = ctx.step(1)
+            its += st["iterations"]
+            logerr += np.log10(max(st["error"], 1e-300))
+        return its, logerr / steps, (ctx.mlp_stats() if mlp else None)
+
+    _, cold_err, _ = run(gpulib.CACHE_NONE, False, 100)
+    _, net_err, stats = run(gpulib.CACHE_NONE, True, 100)
+    warm, _, _ = run(gpulib.CACHE_NORMAL_AND_FRICTION, False, 3000)
+    warm_net, _, stats2 = run(gpulib.CACHE_NORMAL_AND_FRICTION, True, 3000)
+    print("held-out steps: mean log10 residual after 100 sweeps: zero start %.3f, network start %.3f "
+          "(network taken %d/%d); sweeps to 1e-6: cache %d, cache-or-network %d (network taken %d/%d)"
+          % (cold_err, net_err, stats["network_start"], stats["evaluated"], warm, warm_net, stats2["network_start"],
+             stats2["evaluated"]))
+    assert stats["network_start"] > 0
+    assert net_err < cold_err
+    assert warm_net <= 1.1 * warm
