@@ -52,6 +52,12 @@ BYTES_PER_CONTACT_SWEEP32 = 96
 BYTES_PER_CONTACT_EVAL = 112
 BYTES_PER_CONTACT_LIFT = 108
 BYTES_PER_BODY_LIFT = 40
+# 3D spheres (FP64), per contact:
+#   update: perm 4, ia 4, ib 4, basis 72, angular rows 96, c 24, W 48, mu 8, r 24+24,
+#           minv 2x8, Iinv 2x72, (v, omega) 2x(32+32) r + 2x(32+32) w
+#   residual: ia 4, ib 4, basis 72, angular rows 96, c 24, (v, omega) 2x64, r 24, snapshot 24, mu 8
+BYTES_PER_CONTACT_SWEEP_3D = 724
+BYTES_PER_CONTACT_EVAL_3D = 384
 
 
 def gs_bytes(prof):
@@ -207,6 +213,112 @@ def timed_steps(ctx, torch, stream, k, flush):
     return ms, contacts
 
 
+def batch_leg(args, torch, local, flush):
+    """Batched Ball2D scenes (independent scenes of 16-4,096 discs stepped together from a
+    CUDA graph, warm start from each scene's impulse cache) against the plain solver on a
+    sample of the same scenes (one context per scene, FP64, cold start), over the same steps
+    from the same state."""
+    from scisim_gb300 import _lib, scenes
+    b = scenes.ball2d_batch(n_scenes=args.batch_scenes)
+    S, N = len(b["mu"]), int(b["body_off"][-1])
+    kw = dict(dt=b["dt"], gravity=b["gravity"], tol=1e-6, max_iters=args.preroll_iters, device=local,
+              integrator=_lib.SYMPLECTIC_EULER)
+    ctx = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, **kw)
+    ctx.upload_batch2d(b["body_off"], b["q"], b["v"], b["r"], b["m"], b["plane_off"], b["plane_x"], b["plane_n"],
+                       b["mu"], b["CoR"])
+    t0 = time.perf_counter()
+    ctx.step(args.batch_preroll)
+    ctx.reconfigure(max_iters=5000)
+    ctx.step(8)  # warm-up: one graph replay at the full settings (graph built here)
+    log("batch preroll %d + 8 steps in %.1f s" % (args.batch_preroll, time.perf_counter() - t0))
+    q0, v0 = ctx.state()
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=local)
+    ctx.profile_read(reset=True)
+    flush.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st = ctx.step(args.batch_steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    prof = ctx.profile_read(reset=True)
+    stats = ctx.batch_scene_stats()
+    value = st["total_contacts"] / (ms / 1e3)
+    log("batch: %d scenes, %d discs, %d contact-steps in %.1f ms" % (S, N, st["total_contacts"], ms))
+    # Plain: the first scenes of a fixed random sample, each alone, cold FP64, same steps.
+    rng = np.random.default_rng(0)
+    pick = rng.choice(S, min(args.batch_plain_scenes, S), replace=False)
+    pc, pms = 0, 0.0
+    for sc in pick:
+        b0, b1 = int(b["body_off"][sc]), int(b["body_off"][sc + 1])
+        p0, p1 = int(b["plane_off"][sc]), int(b["plane_off"][sc + 1])
+        c = _lib.Context(cache_mode=_lib.CACHE_NONE, mu=float(b["mu"][sc]), CoR=float(b["CoR"][sc]),
+                         **dict(kw, max_iters=5000))
+        c.upload_ball2d(q0[2 * b0:2 * b1], v0[2 * b0:2 * b1], b["r"][b0:b1], b["m"][b0:b1], b["plane_x"][p0:p1],
+                        b["plane_n"][p0:p1])
+        cs = torch.cuda.ExternalStream(c.stream_ptr(), device=local)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(cs)
+        r = c.step(args.batch_steps)
+        a1.record(cs)
+        a1.synchronize()
+        pc += r["total_contacts"]
+        pms += a0.elapsed_time(a1)
+        c.close()
+    plain = pc / (pms / 1e3) if pms > 0 else None
+    out = {"workload": "ball2d_batch_%d" % S, "scenes": S, "discs": N, "value": value, "unit": UNIT,
+           "steps": args.batch_steps, "timed_steps": [args.batch_preroll + 9, args.batch_preroll + 8 + args.batch_steps],
+           "ms_per_step": ms / args.batch_steps, "contacts_per_step": st["total_contacts"] / args.batch_steps,
+           "form": "batched (one CUDA graph per 8 steps), warm start (cache), FP64 sweeps",
+           "scenes_converged_last_step": int(stats["succeeded"].sum()),
+           "gs_iterations_mean_last_step": float(stats["iterations"].mean()),
+           "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
+                              "form": "one context per scene, cold start, FP64, same steps from the same state"},
+           "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"]}
+    ctx.close()
+    return out
+
+
+def sphere_leg(args, torch, local, flush):
+    """RigidBody3D spheres (65,536 by default): FP64 3x3-block solve, no impulse cache (the
+    reference's 3D geometric map keeps none), after a pre-roll with capped solves."""
+    from scisim_gb300 import _lib, scenes
+    s = scenes.sphere_pile(n=args.spheres)
+    kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, max_iters=args.preroll_iters,
+              integrator=_lib.SPLIT_HAM, device=local)
+    ctx = _lib.Context(**kw)
+    ctx.upload_sphere3d(s["q"], s["v"], s["r"], s["m"], s["I0"], s["plane_x"], s["plane_n"])
+    t0 = time.perf_counter()
+    ctx.step(args.sphere_preroll)
+    ctx.reconfigure(max_iters=5000)
+    log("spheres preroll %d steps in %.1f s" % (args.sphere_preroll, time.perf_counter() - t0))
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=local)
+    ctx.profile_enable(True)
+    ctx.profile_read(reset=True)
+    ms, contacts = timed_steps(ctx, torch, stream, args.sphere_steps, flush)
+    prof = ctx.profile_read(reset=True)
+    tot = float(sum(ms))
+    value = sum(contacts) / (tot / 1e3)
+    hbm, peak_kind = peaks()
+    gl = max(prof["gs_launches"], 1)
+    b_launch = (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP_3D + prof["contact_evals"] * BYTES_PER_CONTACT_EVAL_3D) / gl
+    ms_launch = prof["gs_ms"] / gl
+    ach = b_launch / (ms_launch / 1e3) / 1e9 if ms_launch > 0 else 0.0
+    out = {"workload": "sphere_pile_%d" % args.spheres, "value": value, "unit": UNIT, "steps": args.sphere_steps,
+           "timed_steps": [args.sphere_preroll + 1, args.sphere_preroll + args.sphere_steps],
+           "ms_per_step": tot / args.sphere_steps, "contacts_per_step": sum(contacts) / args.sphere_steps,
+           "gs_iterations_per_step": prof["contact_sweeps"] / max(sum(contacts), 1),
+           "form": "FP64 sweeps, cold start (no 3D impulse cache in the reference's geometric map)",
+           "roofline": {"kernel": "k_gs3", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                        "frac": ach / hbm, "peak_kind": peak_kind, "bytes_per_launch": b_launch,
+                        "ms_per_launch": ms_launch, "gs_share_of_step": prof["gs_ms"] / tot if tot else None},
+           "gpu_launches": prof["kernel_launches"]}
+    ctx.close()
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -319,6 +431,15 @@ def run_ours(args):
         log("e2e:", e2e)
         ectx.close()
 
+    batched = None
+    if rank == 0 and args.batch_scenes > 0:
+        batched = batch_leg(args, torch, local, flush)
+        log("batched:", batched)
+    spheres = None
+    if rank == 0 and args.spheres > 0:
+        spheres = sphere_leg(args, torch, local, flush)
+        log("spheres:", spheres)
+
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
         v, desc, cores = cpu_sample(args, args.cpu_steps)
@@ -342,7 +463,7 @@ def run_ours(args):
                 "plain_fp64_gpu": plain,
                 "warm_over_plain": (value / ws) / plain["value"] if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "gpu_launches": prof["kernel_launches"]}
+                "gpu_launches": prof["kernel_launches"], "batched": batched, "spheres": spheres}
         print(json.dumps(line), flush=True)
     fast.close()
     if ws > 1:
@@ -363,6 +484,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--precision", type=int, default=1, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
+    ap.add_argument("--batch-scenes", type=int, default=512, help="batched-scene leg (0 = skip)")
+    ap.add_argument("--batch-preroll", type=int, default=40)
+    ap.add_argument("--batch-steps", type=int, default=8)
+    ap.add_argument("--batch-plain-scenes", type=int, default=16)
+    ap.add_argument("--spheres", type=int, default=65536, help="sphere leg (0 = skip)")
+    ap.add_argument("--sphere-preroll", type=int, default=100)
+    ap.add_argument("--sphere-steps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -766,49 +766,68 @@ __device__ __forceinline__ void local_solve_3d(const double* a, const double* b,
     r[2] = rs2;
     return;
   }
-  double d0 = b[1], d1 = b[2];
-  {
-    const double nd = sqrt(d0 * d0 + d1 * d1);
-    if (nd > 0.0) {
-      d0 = d0 / nd;
-      d1 = d1 / nd;
-    } else {
-      d0 = 1.0;
-      d1 = 0.0;
-    }
-  }
-  double rn = 0.0, rt0 = 0.0, rt1 = 0.0, ut0 = 0.0, ut1 = 0.0;
+  // Slide: u_n = 0, r_T = -mu r_n d with |d| = 1, u_T = alpha d with alpha >= 0.  For a given
+  // r_n, (alpha I + mu r_n W_TT) d = W_Tn r_n + b_T =: g, and |d(alpha)|^2 - 1 is convex and
+  // decreasing in alpha, so Newton from alpha = 0 climbs monotonically to the root.  r_n
+  // follows from the normal row, r_n (W_nn - mu W_nT . d) = -b_n; the two are iterated.
+  double d0 = 1.0, d1 = 0.0;
+  double rn = -b[0] / a00, rt0 = 0.0, rt1 = 0.0, ut0 = 0.0, ut1 = 0.0;
   bool slide_ok = false;
-  for (int it = 0; it < 64; ++it) {
-    const double den = a00 - mu * (a01 * d0 + a02 * d1);
-    if (!(den > 0.0)) break;
-    rn = -b[0] / den;
+  if (mu == 0.0) {
+    rt0 = 0.0;
+    rt1 = 0.0;
+    slide_ok = true;
+  } else {
+    for (int outer = 0; outer < 8; ++outer) {
+      const double c = mu * rn;
+      const double g0 = a01 * rn + b[1], g1 = a02 * rn + b[2];
+      const double m00 = c * a11, m01 = c * a12, m11 = c * a22;
+      // Start at alpha = |g| - lambda_max(c W_TT) (the root when W_TT is isotropic), which
+      // is never right of the root.
+      const double hs = 0.5 * (m00 + m11), hd = 0.5 * (m00 - m11);
+      const double lmax = hs + sqrt(hd * hd + m01 * m01);
+      double al = sqrt(g0 * g0 + g1 * g1) - lmax;
+      if (!(al > 0.0)) al = 0.0;
+      double e0 = 0.0, e1 = 0.0;
+      for (int it = 0; it < 64; ++it) {
+        const double p00 = al + m00, p11 = al + m11;
+        const double inv = 1.0 / (p00 * p11 - m01 * m01);
+        e0 = (p11 * g0 - m01 * g1) * inv;
+        e1 = (p00 * g1 - m01 * g0) * inv;
+        const double f = e0 * e0 + e1 * e1 - 1.0;
+        const double q0 = (p11 * e0 - m01 * e1) * inv, q1 = (p00 * e1 - m01 * e0) * inv;
+        const double fp = -2.0 * (e0 * q0 + e1 * q1);
+        if (!(f > 0.0) || !(fp < 0.0)) break;
+        const double step = -f / fp;
+        al = al + step;
+        if (!(step > 1.0e-15 * (1.0 + al))) {
+          const double p00n = al + m00, p11n = al + m11;
+          const double invn = 1.0 / (p00n * p11n - m01 * m01);
+          e0 = (p11n * g0 - m01 * g1) * invn;
+          e1 = (p00n * g1 - m01 * g0) * invn;
+          break;
+        }
+      }
+      const double ne = sqrt(e0 * e0 + e1 * e1);
+      if (!(ne > 0.0)) break;
+      d0 = e0 / ne;
+      d1 = e1 / ne;
+      const double den = a00 - mu * (a01 * d0 + a02 * d1);
+      if (!(den > 0.0)) break;
+      const double rn_new = -b[0] / den;
+      const bool same = fabs(rn_new - rn) <= 1.0e-15 * fabs(rn_new);
+      rn = rn_new;
+      if (same) {
+        slide_ok = true;
+        break;
+      }
+    }
     rt0 = -mu * rn * d0;
     rt1 = -mu * rn * d1;
-    ut0 = a01 * rn + a11 * rt0 + a12 * rt1 + b[1];
-    ut1 = a02 * rn + a12 * rt0 + a22 * rt1 + b[2];
-    const double nu = sqrt(ut0 * ut0 + ut1 * ut1);
-    if (!(nu > 0.0)) {
-      slide_ok = true;
-      break;
-    }
-    const double e0 = ut0 / nu, e1 = ut1 / nu;
-    const double ch = fmax(fabs(e0 - d0), fabs(e1 - d1));
-    d0 = e0;
-    d1 = e1;
-    if (ch <= 1.0e-15) {
-      const double den2 = a00 - mu * (a01 * d0 + a02 * d1);
-      if (!(den2 > 0.0)) break;
-      rn = -b[0] / den2;
-      rt0 = -mu * rn * d0;
-      rt1 = -mu * rn * d1;
-      ut0 = a01 * rn + a11 * rt0 + a12 * rt1 + b[1];
-      ut1 = a02 * rn + a12 * rt0 + a22 * rt1 + b[2];
-      slide_ok = true;
-      break;
-    }
   }
-  if (slide_ok && rn >= 0.0 && (ut0 * d0 + ut1 * d1) >= 0.0) {
+  ut0 = a01 * rn + a11 * rt0 + a12 * rt1 + b[1];
+  ut1 = a02 * rn + a12 * rt0 + a22 * rt1 + b[2];
+  if (slide_ok && rn >= 0.0 && (mu == 0.0 || (ut0 * d0 + ut1 * d1) >= 0.0)) {
     r[0] = rn;
     r[1] = rt0;
     r[2] = rt1;

@@ -51,6 +51,19 @@ def test_local_solve_isotropic_3d_exact(oracle):
         assert oracle.fb_error(3, r, u, mu) <= 1e-12 * (1 + np.abs(b).max())
 
 
+def test_local_solve_weak_slide_3d(oracle):
+    """A sphere contact with isotropic W_TT where the slide barely exceeds the cone (the case
+    whose sliding direction a plain fixed point cannot find): solved to the Coulomb law."""
+    Wp = np.array([2104.1729537535039, -2.3361012610506652e-13, 5.840253152626663e-14, 7232.3270716106308,
+                   -1.3642420526593924e-12, 7232.3270716106308])
+    b = np.array([-0.61783481435953869, -1.4683859110528765, 0.017832300158811997])
+    W = np.array([[Wp[0], Wp[1], Wp[2]], [Wp[1], Wp[3], Wp[4]], [Wp[2], Wp[4], Wp[5]]])
+    r = oracle.local_solve(3, Wp, b, 0.6)
+    u = W @ r + b
+    assert oracle.fb_error(3, r, u, 0.6) <= 1e-12 * np.abs(b).max()
+    assert abs(np.hypot(r[1], r[2]) - 0.6 * r[0]) <= 1e-15 * r[0] * 10  # on the cone boundary
+
+
 def two_ball_problem(ma, mb, va, vb, n):
     n = np.asarray(n, float) / np.linalg.norm(n)
     t = np.array([-n[1], n[0]])
