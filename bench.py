@@ -223,7 +223,7 @@ def batch_leg(args, torch, local, flush):
     S, N = len(b["mu"]), int(b["body_off"][-1])
     kw = dict(dt=b["dt"], gravity=b["gravity"], tol=1e-6, max_iters=args.preroll_iters, device=local,
               integrator=_lib.SYMPLECTIC_EULER)
-    ctx = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, **kw)
+    ctx = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision, **kw)
     ctx.upload_batch2d(b["body_off"], b["q"], b["v"], b["r"], b["m"], b["plane_off"], b["plane_x"], b["plane_n"],
                        b["mu"], b["CoR"])
     t0 = time.perf_counter()
@@ -254,7 +254,7 @@ def batch_leg(args, torch, local, flush):
         b0, b1 = int(b["body_off"][sc]), int(b["body_off"][sc + 1])
         p0, p1 = int(b["plane_off"][sc]), int(b["plane_off"][sc + 1])
         c = _lib.Context(cache_mode=_lib.CACHE_NONE, mu=float(b["mu"][sc]), CoR=float(b["CoR"][sc]),
-                         **dict(kw, max_iters=5000))
+                         precision=_lib.PRECISION_FP64, **dict(kw, max_iters=5000))
         c.upload_ball2d(q0[2 * b0:2 * b1], v0[2 * b0:2 * b1], b["r"][b0:b1], b["m"][b0:b1], b["plane_x"][p0:p1],
                         b["plane_n"][p0:p1])
         cs = torch.cuda.ExternalStream(c.stream_ptr(), device=local)
@@ -271,7 +271,9 @@ def batch_leg(args, torch, local, flush):
     out = {"workload": "ball2d_batch_%d" % S, "scenes": S, "discs": N, "value": value, "unit": UNIT,
            "steps": args.batch_steps, "timed_steps": [args.batch_preroll + 9, args.batch_preroll + 8 + args.batch_steps],
            "ms_per_step": ms / args.batch_steps, "contacts_per_step": st["total_contacts"] / args.batch_steps,
-           "form": "batched (one CUDA graph per 8 steps), warm start (cache), FP64 sweeps",
+           "form": "batched (one CUDA graph per 8 steps), warm start (cache), %s" % (
+               "FP32 sweeps + FP64 residual and refinement per scene" if args.precision == 1 else "FP64 sweeps"),
+           "fp32_sweep_share": prof["contact_sweeps32"] / max(prof["contact_sweeps"] + prof["contact_sweeps32"], 1),
            "scenes_converged_last_step": int(stats["succeeded"].sum()),
            "gs_iterations_mean_last_step": float(stats["iterations"].mean()),
            "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),

@@ -207,7 +207,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->s_grid,  &ctx->s_cells,  &ctx->s_cell_off,  &ctx->s_nc,     &ctx->s_npairs, &ctx->sc_off,
                   &ctx->prev_sc_off, &ctx->cscene, &ctx->b_ctl,     &ctx->b_sums,   &ctx->s_err,   &ctx->s_best,
                   &ctx->s_bestbuf, &ctx->s_done, &ctx->s_iters,     &ctx->snap_q,   &ctx->snap_v,  &ctx->snap_key,
-                  &ctx->snap_ab, &ctx->snap_off};
+                  &ctx->snap_ab, &ctx->snap_off, &ctx->s_mode, &ctx->s_since, &ctx->s_exc, &ctx->s_gmax,
+                  &ctx->b_work, &ctx->pk_scene};
   for (Buf* b : bufsb) release(*b);
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
   Buf* bufs[] = {&ctx->q, &ctx->v, &ctx->r, &ctx->m, &ctx->minv, &ctx->q1, &ctx->v1, &ctx->v2, &ctx->plane_x,
@@ -477,6 +478,7 @@ static int batch_step(sg_ctx* ctx, uint32_t n_steps, sg_step_stats* out, int64_t
   const int S = ctx->n_scenes;
   SG_CUDA_TRY(cudaMemsetAsync(ctx->b_sums.p, 0, 4 * sizeof(unsigned long long), s));
   SG_CUDA_TRY(cudaMemsetAsync(ctx->b_ctl.as<int>() + 1, 0, sizeof(int), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_work.p, 0, 5 * sizeof(unsigned long long), s));
   uint32_t done = 0;
   unsigned long long sums_before[2] = {0, 0};
   int retries = 0;
@@ -540,6 +542,13 @@ static int batch_step(sg_ctx* ctx, uint32_t n_steps, sg_step_stats* out, int64_t
   st.n_colors = (uint32_t)ctx->h_stats.n_colors;
   ctx->last_nc = ctl[0];
   ctx->contacts_total += sums[0];
+  unsigned long long work[5] = {0, 0, 0, 0, 0};
+  SG_CUDA_TRY(cudaMemcpy(work, ctx->b_work.p, sizeof work, cudaMemcpyDeviceToHost));
+  ctx->contact_sweeps32 += work[0];
+  ctx->contact_sweeps += work[1];
+  ctx->contact_evals += work[2];
+  ctx->contact_lifts += work[3];
+  ctx->body_lifts += work[4];
   if (out) *out = st;
   if (total) *total = (int64_t)sums[0];
   return sums[1] ? SG_NOT_CONVERGED : SG_OK;

@@ -899,6 +899,21 @@ int batch2d_reserve(sg_ctx* ctx, int cap) {
   }
   if (int r = ensure_solver_capacity(ctx, ctx->nb, (int)c)) return r;
   if (int r = grow(ctx->v2, sizeof(double) * 2 * nb)) return r;
+  // FP32 sweep data (packed in colour order) and per-scene mode state.
+  if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
+  if (int r = grow(ctx->pk_n, sizeof(float2) * c)) return r;
+  if (int r = grow(ctx->pk_c, sizeof(float2) * c)) return r;
+  if (int r = grow(ctx->pk_w, sizeof(float4) * c)) return r;
+  if (int r = grow(ctx->pk_r, sizeof(float2) * c)) return r;
+  if (int r = grow(ctx->pk_scene, sizeof(int) * c)) return r;
+  if (int r = grow(ctx->v32, sizeof(float2) * nb)) return r;
+  if (int r = grow(ctx->minv32, sizeof(float) * nb)) return r;
+  const size_t S = (size_t)std::max(ctx->n_scenes, 1);
+  if (int r = grow(ctx->s_mode, sizeof(int) * S)) return r;
+  if (int r = grow(ctx->s_since, sizeof(unsigned) * S)) return r;
+  if (int r = grow(ctx->s_exc, sizeof(unsigned long long) * 3 * S)) return r;
+  if (int r = grow(ctx->s_gmax, sizeof(unsigned long long) * 3)) return r;
+  if (int r = grow(ctx->b_work, sizeof(unsigned long long) * 5)) return r;
   // Scan scratch for the largest scan of a step, so that nothing allocates while capturing.
   const long big = std::max<long>({(long)ctx->nb + 1, ctx->bcells + 1, ctx->bflags + 1, (long)ctx->n_scenes + 1,
                                    (long)c});
@@ -1009,7 +1024,15 @@ int batch2d_step_enqueue(sg_ctx* ctx) {
   X.iters = ctx->s_iters.as<unsigned>();
   X.done_count = ctl + 2;
   X.unconverged = sums + 1;
-  SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, SG_PRECISION_FP64};
+  X.pscene = ctx->pk_scene.as<int>();
+  X.scene_of = ctx->scene_of.as<int>();
+  X.mode = ctx->s_mode.as<int>();
+  X.since = ctx->s_since.as<unsigned>();
+  X.exc_slot = ctx->s_exc.as<unsigned long long>();
+  X.gmax = ctx->s_gmax.as<unsigned long long>();
+  X.work = ctx->b_work.as<unsigned long long>();
+  X.n64 = ctl + 3;
+  SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, ctx->cfg.precision};
   if (int r = solve_contacts_batch(ctx, P, sp, X)) return r;
   k_extract<<<blocks_for(cap), kBlock, 0, s>>>(cap, ctl, ctx->n.as<double2>(), ctx->r_loc.as<double2>(),
                                               ctx->mu.as<double>(), ctx->cfg.cache_mode, ctx->ab.as<double2>());

@@ -85,6 +85,15 @@ struct BatchSolve {
   unsigned* iters = nullptr;
   int* done_count = nullptr;
   unsigned long long* unconverged = nullptr;
+  // FP32 sweeps (SG_PRECISION_FP32_REFINE)
+  int* pscene = nullptr;            // scene of each packed contact (capacity)
+  const int* scene_of = nullptr;    // scene of each body
+  int* mode = nullptr;              // S
+  unsigned* since = nullptr;        // S
+  unsigned long long* exc_slot = nullptr;  // 3 S
+  unsigned long long* gmax = nullptr;      // 3
+  unsigned long long* work = nullptr;      // 5 counters (FP32 / FP64 updates, evaluations, lifts)
+  int* n64 = nullptr;                      // scenes in FP64 mode
 };
 
 struct SolveParams {
@@ -141,7 +150,7 @@ struct sg_ctx {
   int bcap = 0;
   sg::Buf sb_off, sp_off, sf_off, scene_of, s_mu, s_CoR, s_grid, s_cells, s_cell_off, s_nc, s_npairs;
   sg::Buf sc_off, prev_sc_off, cscene, b_ctl, b_sums;
-  sg::Buf s_err, s_best, s_bestbuf, s_done, s_iters;
+  sg::Buf s_err, s_best, s_bestbuf, s_done, s_iters, s_mode, s_since, s_exc, s_gmax, b_work, pk_scene;
   sg::Buf snap_q, snap_v, snap_key, snap_ab, snap_off;
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_launches = 0;  // kernel launches per graph replay

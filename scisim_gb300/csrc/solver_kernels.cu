@@ -560,6 +560,7 @@ struct GsBatchArgs {
   unsigned* iters;               // S
   int* done_count;
   unsigned long long* unconverged;  // running count of scene solves that hit max_iters
+  unsigned long long* work;         // [1] FP64 contact updates, [2] contact evaluations
 };
 
 // Max of v over the lanes of each run of equal keys (runs are contiguous lanes); the
@@ -605,6 +606,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_batch(GsBatchArgs B) {
   }
   unsigned n_eval = 0;
   unsigned it = 0;
+  unsigned long long n64w = 0, nevw = 0;
   if (*((volatile int*)B.done_count) < S) {
     for (it = 1; it <= A.max_iters; ++it) {
       for (int col = 0; col < ncol; ++col) {
@@ -613,6 +615,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_batch(GsBatchArgs B) {
           const int k = A.perm[s];
           if (__ldcg(&B.done[B.cscene[k]])) continue;
           gs_update(A, k);
+          ++n64w;
         }
         if (!grid_sync(A.gb, A.spin)) {
           if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
@@ -640,6 +643,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_batch(GsBatchArgs B) {
             bufs[1 - __ldcg(&B.bestbuf[sc])][k] = rk;
             v = f64_to_ordered(fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
             key = sc;
+            ++nevw;
           }
         }
         run_max_atomic(v, key, slots);
@@ -680,6 +684,8 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs_batch(GsBatchArgs B) {
   for (int sc = tid; sc < S; sc += nthr)
     if (!__ldcg(&B.done[sc])) B.iters[sc] = A.max_iters;
   if (tid == 0) *B.unconverged += (unsigned long long)(S - *((volatile int*)B.done_count));
+  atomicAdd(&B.work[1], n64w);
+  atomicAdd(&B.work[2], nevw);
   if (tid == 0) {
     A.st->iterations = it > A.max_iters ? A.max_iters : it;
     A.st->sweeps64 = it > A.max_iters ? A.max_iters : it;
@@ -839,6 +845,26 @@ __global__ void k_pack32(int nc, const int* __restrict__ perm, const int* __rest
   c32[s] = make_float2((float)ck.x, (float)ck.y);
   w32[s] = make_float4((float)W[3 * k], (float)W[3 * k + 1], (float)W[3 * k + 2], (float)mu[k]);
   r32[s] = make_float2((float)rk.x, (float)rk.y);
+}
+
+// Batched packing: device-side count; also the scene of every packed contact.
+__global__ void k_pack32_b(const int* __restrict__ nc_dev, const int* __restrict__ perm, const int* __restrict__ ia,
+                           const int* __restrict__ ib, const double2* __restrict__ n, const double2* __restrict__ c,
+                           const double* __restrict__ W, const double* __restrict__ mu, const double2* __restrict__ r,
+                           const int* __restrict__ cscene, int2* __restrict__ ab, float2* __restrict__ n32,
+                           float2* __restrict__ c32, float4* __restrict__ w32, float2* __restrict__ r32,
+                           int* __restrict__ pscene) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= *nc_dev) return;
+  const int k = perm[s];
+  const int b = ib[k];
+  ab[s] = make_int2(ia[k], b >= 0 ? b : -1);
+  const double2 nk = n[k], ck = c[k], rk = r[k];
+  n32[s] = make_float2((float)nk.x, (float)nk.y);
+  c32[s] = make_float2((float)ck.x, (float)ck.y);
+  w32[s] = make_float4((float)W[3 * k], (float)W[3 * k + 1], (float)W[3 * k + 2], (float)mu[k]);
+  r32[s] = make_float2((float)rk.x, (float)rk.y);
+  pscene[s] = cscene[k];
 }
 
 __global__ void k_vel32(int nb, const double2* __restrict__ v, const double* __restrict__ minv, float2* __restrict__ v32,
@@ -1081,6 +1107,233 @@ __global__ void k_select_start(int nc, double2* __restrict__ r, const double2* _
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k == 0 && take) *chosen += 1ull;
   if (k < nc && take) r[k] = r_alt[k];
+}
+
+// ---------------------------------------------------------------------------
+// Batched scenes with FP32 sweeps: every scene is in one of three modes, FP32 sweeping,
+// FP64 sweeping (refinement) or done, and moves between them on its own FP64 residual
+// exactly as a single scene does in k_gs_mixed (FP64 hand-over when FP32 reached tol or
+// hit its rounding floor; done when an FP64 residual is below tol).  FP32 scenes are
+// checked on a common schedule (sweeps 1, 2, 4, ... eval32, then an interval that grows
+// while the largest FP32-scene residual is far above tol); FP64 scenes every eval_every
+// sweeps.  A contact's colour slot runs the update of its scene's mode.
+struct GsMixedBatchArgs {
+  GsBatchArgs X;          // per-scene state (err_slot, best, bestbuf, done, iters, done_count)
+  const int* pscene;      // scene of each packed contact
+  const int* scene_of;    // scene of each body
+  int* mode;              // S: 0 FP32, 1 FP64
+  unsigned* since;        // S: checks since the scene's best
+  unsigned long long* exc_slot;  // 3 S: FP32 rounding-floor excess per scene
+  unsigned long long* gmax;      // 3: largest residual of the FP32 scenes per check
+  int* n64;                      // scenes in FP64 mode
+  unsigned long long* work;      // [0] FP32 contact updates, [1] FP64 contact updates, [2] contact
+                                 // evaluations, [3] contact lifts, [4] body lifts
+};
+
+__global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed_batch(GsMixedBatchArgs M, Gs32Args B) {
+  GsBatchArgs& X = M.X;
+  const GsArgs& A = X.g;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  const int nc = *X.nc_dev;
+  const int S = X.S;
+  for (int sc = tid; sc < S; sc += nthr) {
+    X.best[sc] = INFINITY;
+    X.bestbuf[sc] = 0;
+    X.iters[sc] = 0;
+    M.mode[sc] = 0;
+    M.since[sc] = 0;
+    const bool empty = X.sc_off[sc + 1] == X.sc_off[sc];
+    X.done[sc] = empty ? 1 : 0;
+    if (empty) atomicAdd(X.done_count, 1);
+  }
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
+  double2* bufs[2] = {A.r_a, A.r_b};
+  if (!grid_sync(A.gb, A.spin)) {
+    if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+    return;
+  }
+  unsigned long long n32 = 0, n64 = 0, nev = 0, nlc = 0, nlb = 0;
+  unsigned it = 0, n_eval = 0, next_eval = 1, interval = eval32;
+  if (*((volatile int*)X.done_count) < S) {
+    for (it = 1; it <= A.max_iters; ++it) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + tid; s < e; s += nthr) {
+          const int sc = M.pscene[s];
+          if (__ldcg(&X.done[sc])) continue;
+          if (__ldcg(&M.mode[sc]) == 0) {
+            gs_update32(B, s);
+            ++n32;
+          } else {
+            gs_update(A, A.perm[s]);
+            ++n64;
+          }
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      const bool due32 = it == next_eval || it == A.max_iters;
+      const bool due64 = *((volatile int*)M.n64) > 0 && ((it % eval64 == 0) || it == A.max_iters);
+      if (!due32 && !due64) continue;
+      if (due32) {
+        // Lift the FP32 scenes' iterates to FP64 and resynchronise their FP32 velocities.
+        for (int s = tid; s < nc; s += nthr) {
+          const int sc = M.pscene[s];
+          if (__ldcg(&X.done[sc]) || __ldcg(&M.mode[sc]) != 0) continue;
+          const float2 r32 = __ldcg(&B.r[s]);
+          A.r[A.perm[s]] = make_double2((double)r32.x, (double)r32.y);
+          ++nlc;
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+        for (int i = tid; i < B.nb; i += nthr) {
+          const int sc = M.scene_of[i];
+          if (__ldcg(&X.done[sc]) || __ldcg(&M.mode[sc]) != 0) continue;
+          double hx = 0.0, hy = 0.0;
+          const int e = B.body_off[i + 1];
+          for (int p = B.body_off[i]; p < e; ++p) {
+            const int k = B.body_adj[p];
+            const double sgn = (A.ia[k] == i) ? 1.0 : -1.0;
+            const double2 nk = A.n[k], rk = __ldcg(&A.r[k]);
+            const double px = nk.x * rk.x + (-nk.y) * rk.y;
+            const double py = nk.y * rk.x + nk.x * rk.y;
+            hx = hx + sgn * px;
+            hy = hy + sgn * py;
+          }
+          const double2 a = B.v0[i];
+          const double mi = B.minv64[i];
+          const double2 vi = make_double2(a.x + mi * hx, a.y + mi * hy);
+          A.v[i] = vi;
+          B.v[i] = make_float2((float)vi.x, (float)vi.y);
+          ++nlb;
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      // FP64 residual and FP32 floor excess of every due scene.
+      const int slot = n_eval % 3;
+      unsigned long long* eslots = X.err_slot + (size_t)slot * S;
+      unsigned long long* xslots = M.exc_slot + (size_t)slot * S;
+      const int lane = threadIdx.x & 31;
+      for (int k0 = tid - lane; k0 < nc; k0 += nthr) {
+        const int k = k0 + lane;
+        int key = -1;
+        unsigned long long ve = 0ull, vx = 0ull;
+        if (k < nc) {
+          const int sc = X.cscene[k];
+          const int md = __ldcg(&M.mode[sc]);
+          if (!__ldcg(&X.done[sc]) && ((md == 0 && due32) || (md == 1 && due64))) {
+            const int a = A.ia[k], b = A.ib[k];
+            const bool has_b = b >= 0;
+            const double2 va = __ldcg(&A.v[a]);
+            const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+            const double2 ck = A.c[k];
+            double u0, u1;
+            local_velocity(A.n[k], ck, va, has_b, vb, u0, u1);
+            const double2 rk = __ldcg(&A.r[k]);
+            bufs[1 - __ldcg(&X.bestbuf[sc])][k] = rk;
+            const double ek = fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]);
+            const double scale = fabs(va.x) + fabs(va.y) + fabs(vb.x) + fabs(vb.y) + fabs(ck.x) + fabs(ck.y) +
+                                 fabs(rk.x) + fabs(rk.y);
+            ve = f64_to_ordered(ek);
+            vx = f64_to_ordered(ek - 64.0 * 1.1920929e-7 * scale);
+            key = sc;
+            ++nev;
+          }
+        }
+        run_max_atomic(ve, key, eslots);
+        run_max_atomic(vx, key, xslots);
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      // Per-scene decisions (one thread per scene).
+      unsigned long long* enext = X.err_slot + (size_t)((n_eval + 1) % 3) * S;
+      unsigned long long* xnext = M.exc_slot + (size_t)((n_eval + 1) % 3) * S;
+      double gm = 0.0;
+      for (int sc = tid; sc < S; sc += nthr) {
+        enext[sc] = 0ull;
+        xnext[sc] = 0ull;
+        if (X.done[sc]) continue;
+        const int md = M.mode[sc];
+        if (!((md == 0 && due32) || (md == 1 && due64))) continue;
+        const double err = ordered_to_f64(__ldcg(&eslots[sc]));
+        const double exc = ordered_to_f64(__ldcg(&xslots[sc]));
+        if (err < X.best[sc]) {
+          X.best[sc] = err;
+          X.bestbuf[sc] ^= 1;
+          M.since[sc] = 0;
+        } else {
+          M.since[sc] += 1;
+        }
+        if (md == 1) {
+          if (err < A.tol) {
+            X.done[sc] = 1;
+            X.iters[sc] = it;
+            atomicAdd(X.done_count, 1);
+            atomicSub(M.n64, 1);
+          }
+        } else {
+          gm = nanmax(gm, err);
+          if (err < A.tol || exc <= A.tol || (M.since[sc] >= 16 && exc <= 16.0 * A.tol)) {
+            M.mode[sc] = 1;
+            atomicAdd(M.n64, 1);
+          }
+        }
+      }
+      gm = block_nanmax(gm);
+      if (threadIdx.x == 0 && due32) atomicMax(&M.gmax[slot], f64_to_ordered(gm));
+      if (tid == 0) M.gmax[(n_eval + 1) % 3] = 0ull;
+      ++n_eval;
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      if (due32) {
+        const double g = ordered_to_f64(*((volatile unsigned long long*)&M.gmax[slot]));
+        if (it < eval32) {
+          next_eval = 2 * it;
+        } else {
+          interval = (g > 1e3 * A.tol) ? min(2u * interval, 16u * eval32) : (g > 10.0 * A.tol ? interval : eval32);
+          next_eval = it + interval;
+        }
+      }
+      if (*((volatile int*)X.done_count) == S) break;
+    }
+  }
+  for (int k = tid; k < nc; k += nthr) {
+    const int sc = X.cscene[k];
+    if (__ldcg(&X.done[sc])) continue;
+    if (__ldcg(&X.best[sc]) < INFINITY) A.r[k] = __ldcg(&bufs[__ldcg(&X.bestbuf[sc])][k]);
+  }
+  for (int sc = tid; sc < S; sc += nthr)
+    if (!__ldcg(&X.done[sc])) X.iters[sc] = A.max_iters;
+  if (tid == 0) *X.unconverged += (unsigned long long)(S - *((volatile int*)X.done_count));
+  atomicAdd(&M.work[0], n32);
+  atomicAdd(&M.work[1], n64);
+  atomicAdd(&M.work[2], nev);
+  atomicAdd(&M.work[3], nlc);
+  atomicAdd(&M.work[4], nlb);
+  if (tid == 0) {
+    A.st->iterations = it > A.max_iters ? A.max_iters : it;
+    A.st->evals = n_eval;
+  }
 }
 
 __global__ void k_wait_flag(const int* flag, int* status, unsigned long long spin) {
@@ -1346,9 +1599,50 @@ int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams
   B.iters = X.iters;
   B.done_count = X.done_count;
   B.unconverged = X.unconverged;
-  void* args[] = {&B};
-  const int g = coop_grid(ctx, k_gs_batch, std::max(cap, X.S), kGsBlock, 1);
-  SG_CUDA_TRY(launch_cooperative((const void*)k_gs_batch, g, kGsBlock, args, s));
+  B.work = X.work;
+  if (sp.precision == SG_PRECISION_FP32_REFINE) {
+    k_pack32_b<<<blocks_for(cap), kBlock, 0, s>>>(X.nc_dev, ctx->perm.as<int>(), P.ia, P.ib, n2,
+                                                 reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2, X.cscene,
+                                                 ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
+                                                 ctx->pk_w.as<float4>(), ctx->pk_r.as<float2>(), X.pscene);
+    k_vel32<<<blocks_for(nb), kBlock, 0, s>>>(nb, vrun, P.minv, ctx->v32.as<float2>(), ctx->minv32.as<float>());
+    SG_CUDA_TRY(cudaGetLastError());
+    SG_CUDA_TRY(cudaMemsetAsync(X.exc_slot, 0, sizeof(unsigned long long) * 3 * (size_t)X.S, s));
+    SG_CUDA_TRY(cudaMemsetAsync(X.gmax, 0, sizeof(unsigned long long) * 3, s));
+    Gs32Args GB;
+    GB.ab = ctx->pk_ab.as<int2>();
+    GB.n = ctx->pk_n.as<float2>();
+    GB.c = ctx->pk_c.as<float2>();
+    GB.w = ctx->pk_w.as<float4>();
+    GB.r = ctx->pk_r.as<float2>();
+    GB.v = ctx->v32.as<float2>();
+    GB.minv = ctx->minv32.as<float>();
+    GB.minv64 = P.minv;
+    GB.v0 = reinterpret_cast<const double2*>(P.v0);
+    GB.body_off = off;
+    GB.body_adj = adj;
+    GB.nb = nb;
+    GB.eval32 = 16;
+    GsMixedBatchArgs M;
+    M.X = B;
+    M.pscene = X.pscene;
+    M.scene_of = X.scene_of;
+    M.mode = X.mode;
+    M.since = X.since;
+    M.exc_slot = X.exc_slot;
+    M.gmax = X.gmax;
+    M.work = X.work;
+    M.n64 = X.n64;
+    SG_CUDA_TRY(cudaMemsetAsync(X.n64, 0, sizeof(int), s));
+    void* args[] = {&M, &GB};
+    const int g = coop_grid(ctx, k_gs_mixed_batch, std::max(std::max(cap, X.S), nb), kGs32Block, 1);
+    SG_CUDA_TRY(launch_cooperative((const void*)k_gs_mixed_batch, g, kGs32Block, args, s));
+    ctx->kernel_launches += 2;  // pack, vel32
+  } else {
+    void* args[] = {&B};
+    const int g = coop_grid(ctx, k_gs_batch, std::max(cap, X.S), kGsBlock, 1);
+    SG_CUDA_TRY(launch_cooperative((const void*)k_gs_batch, g, kGsBlock, args, s));
+  }
   k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                      P.m, P.minv, reinterpret_cast<double2*>(P.v2));
   SG_CUDA_TRY(cudaGetLastError());

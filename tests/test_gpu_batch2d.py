@@ -122,3 +122,36 @@ def test_batch_flow_and_stats(gpulib):
     assert stats["n_contacts"].sum() == st["n_contacts"]
     assert np.all(stats["error"][stats["succeeded"]] < 1e-6)
     assert tot > 0
+
+
+def test_batch_fp32_refine(gpulib, oracle):
+    """FP32 sweeps + FP64 refinement per scene: every scene that reports convergence meets the
+    tolerance under the oracle's FP64 residual of its own contacts, and the trajectories stay
+    within 1e-3 of the FP64 batch."""
+    b = small_batch(seed=5, n_scenes=12, nmax=400)
+    f64 = gpu_batch(gpulib, b, tol=1e-6, max_iters=3000)
+    f32 = gpu_batch(gpulib, b, tol=1e-6, max_iters=3000, precision=gpulib.PRECISION_FP32_REFINE)
+    f64.step(24)
+    f32.step(23)
+    q0, v0 = f32.state()
+    f32.step(1)
+    stats = f32.batch_scene_stats()
+    g = f32.last_contacts()
+    coff = np.concatenate([[0], np.cumsum(stats["n_contacts"])])
+    checked = 0
+    for s in range(len(b["mu"])):
+        c0, c1 = int(coff[s]), int(coff[s + 1])
+        if c1 == c0 or not stats["succeeded"][s]:
+            continue
+        b0, b1 = int(b["body_off"][s]), int(b["body_off"][s + 1])
+        ia, ib = local_contacts(g, c0, c1, b0, int(b["plane_off"][s]))
+        n = g["n"][c0:c1]
+        bases = np.concatenate([n, np.stack([-n[:, 1], n[:, 0]], 1)], 1).reshape(-1)
+        res = oracle.residual_2d(b["m"][b0:b1], v0[2 * b0:2 * b1], ia, np.where(ib >= 0, ib, -1), bases,
+                                 float(b["CoR"][s]), float(b["mu"][s]), g["alpha"][c0:c1], g["beta"][c0:c1])
+        assert res <= 1e-6 * 1.001
+        checked += 1
+    assert checked >= 3
+    qa, _ = f64.state()
+    qb, _ = f32.state()
+    assert np.abs(qa - qb).max() <= 1e-3
