@@ -321,6 +321,68 @@ def sphere_leg(args, torch, local, flush):
     return out
 
 
+def mlp_leg(args, torch, local):
+    """Learned warm start on the hopper (V-wedge): record the plain solver's per-contact
+    samples, train the network on the GPU, then step the same state twice, from the impulse
+    cache and from the cache-or-network start (chosen per step by the smaller FP64 residual),
+    to the same tolerance, and compare sweeps and contact-steps/s."""
+    from scisim_gb300 import _lib, scenes
+    s = scenes.hopper(args.mlp_hopper)
+    kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, device=local)
+    rec = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=_lib.PRECISION_FP64,
+                       max_iters=args.preroll_iters, **kw)
+    rec.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    t0 = time.perf_counter()
+    rec.step(args.mlp_preroll)
+    rec.reconfigure(max_iters=args.mlp_record_iters)
+    rec.mlp_load(_lib.mlp_init(0))
+    rec.mlp_enable(warm_start=False, record=True)
+    xs, ts = [], []
+    for _ in range(args.mlp_record_steps):
+        rec.step(1)
+        x, t = rec.mlp_last_samples()
+        xs.append(x)
+        ts.append(t)
+    q0, v0 = rec.state()
+    X, T = np.concatenate(xs), np.concatenate(ts)
+    t1 = time.perf_counter()
+    p, losses = rec.mlp_train(X, T, _lib.mlp_init(1), epochs=args.mlp_epochs, batch=4096, lr=2e-3, seed=3)
+    t_train = time.perf_counter() - t1
+    rec.close()
+    log("mlp: %d samples recorded in %.1f s, trained in %.2f s, epoch losses %s" % (X.shape[0], t1 - t0, t_train,
+                                                                                   [round(x, 4) for x in losses]))
+    out = {"workload": "hopper_%d" % args.mlp_hopper, "samples": int(X.shape[0]), "epochs": args.mlp_epochs,
+           "train_s": t_train, "epoch_loss": [float(x) for x in losses]}
+    for name, use in (("cache", False), ("cache_or_network", True)):
+        ctx = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision, max_iters=5000, **kw)
+        ctx.upload_ball2d(q0, v0, s["r"], s["m"], s["plane_x"], s["plane_n"])
+        ctx.step(1)  # prime the impulse cache identically in both runs
+        if use:
+            ctx.mlp_load(p)
+            ctx.mlp_enable(warm_start=True)
+        stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=local)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its, cs, conv, lerr = 0, 0, 0, 0.0
+        for _ in range(args.mlp_eval_steps):
+            st = ctx.step(1)
+            its += st["iterations"]
+            cs += st["n_contacts"]
+            conv += int(st["succeeded"])
+            lerr += float(np.log10(max(st["error"], 1e-300)))
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"sweeps": its, "contact_steps": cs, "converged_steps": conv, "ms": ms,
+                     "value": cs / (ms / 1e3), "unit": UNIT, "mean_log10_residual": lerr / args.mlp_eval_steps}
+        if use:
+            out[name]["network_start_steps"] = ctx.mlp_stats()["network_start"]
+        ctx.close()
+    out["sweeps_saved_frac"] = 1.0 - out["cache_or_network"]["sweeps"] / max(out["cache"]["sweeps"], 1)
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -437,6 +499,10 @@ def run_ours(args):
     if rank == 0 and args.batch_scenes > 0:
         batched = batch_leg(args, torch, local, flush)
         log("batched:", batched)
+    learned = None
+    if rank == 0 and args.mlp_hopper > 0:
+        learned = mlp_leg(args, torch, local)
+        log("learned:", learned)
     spheres = None
     if rank == 0 and args.spheres > 0:
         spheres = sphere_leg(args, torch, local, flush)
@@ -465,7 +531,8 @@ def run_ours(args):
                 "plain_fp64_gpu": plain,
                 "warm_over_plain": (value / ws) / plain["value"] if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "gpu_launches": prof["kernel_launches"], "batched": batched, "spheres": spheres}
+                "gpu_launches": prof["kernel_launches"], "batched": batched, "spheres": spheres,
+                "learned": learned}
         print(json.dumps(line), flush=True)
     fast.close()
     if ws > 1:
@@ -493,6 +560,12 @@ def main():
     ap.add_argument("--spheres", type=int, default=65536, help="sphere leg (0 = skip)")
     ap.add_argument("--sphere-preroll", type=int, default=100)
     ap.add_argument("--sphere-steps", type=int, default=3)
+    ap.add_argument("--mlp-hopper", type=int, default=0, help="learned-warm-start study on a hopper (0 = skip)")
+    ap.add_argument("--mlp-preroll", type=int, default=1500)
+    ap.add_argument("--mlp-record-steps", type=int, default=100)
+    ap.add_argument("--mlp-record-iters", type=int, default=1000)
+    ap.add_argument("--mlp-epochs", type=int, default=6)
+    ap.add_argument("--mlp-eval-steps", type=int, default=30)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -11,6 +11,9 @@ No public dataset is involved: every scene is generated from a fixed seed.
                   fill of a 40 x 60 box (area fraction ~0.5) built by size-sorted
                   shelf packing with random slack, rows shuffled, bodies permuted;
                   four walls; gravity -9.81, dt 0.005, CoR 0, mu 0.4
+  hopper          262,144 discs, radii U[0.02, 0.05], filled above a V-wedge of two planes
+                  at +-30 deg from the vertical (infinite planes: no outlet), mu 0.5, CoR 0.1,
+                  dt 0.005
   ball2d_batch    4,096 independent Ball2D scenes of 16-4,096 discs (log-uniform), radii
                   U[0.03, 0.05], per-scene mu U[0.1, 0.8] and CoR U[0, 0.5], dt 0.01
   sphere_pile     65,536 spheres, r ~ U[0.05, 0.1], density 1, jittered lattice of spacing
@@ -43,10 +46,13 @@ def box_drop_1024(seed: int = 1, n_side: int = 32):
 
 
 def dense_pile(n: int = 262144, seed: int = 2, width: float = 40.0, height: float = 60.0, rmin: float = 0.02,
-               rmax: float = 0.06):
+               rmax: float = 0.06, radii: str = "loguniform"):
     """Non-overlapping polydisperse fill of a width x height box (walls at x = +-width/2, floor y = 0)."""
     rng = np.random.default_rng(seed)
-    r = np.exp(rng.uniform(math.log(rmin), math.log(rmax), n))
+    if radii == "uniform":
+        r = rng.uniform(rmin, rmax, n)
+    else:
+        r = np.exp(rng.uniform(math.log(rmin), math.log(rmax), n))
     order = np.argsort(-r, kind="stable")
     rs = r[order]
     # Shelf packing of the size-sorted discs: rows of similar radii.
@@ -96,6 +102,26 @@ def dense_pile(n: int = 262144, seed: int = 2, width: float = 40.0, height: floa
     plane_n = np.array([[0.0, 1.0], [1.0, 0.0], [-1.0, 0.0], [0.0, -1.0]])
     return dict(q=q.reshape(-1), v=v, r=r, m=m, plane_x=plane_x, plane_n=plane_n, dt=0.005, gravity=(0.0, -9.81),
                 CoR=0.0, mu=0.4, tol=1e-6, max_iters=5000, name="dense_pile_%d" % n)
+
+
+def hopper(n: int = 262144, seed: int = 4, angle_deg: float = 30.0, outlet: float = 0.5):
+    """Discs (radii U[0.02, 0.05], density 1) filled above a funnel of two static planes
+    inclined angle_deg from the vertical whose lines pass through (+-outlet/2, 0).  SCISim's
+    StaticPlane is an infinite line (ball2d/StaticGeometry/StaticPlane.cpp:10-23), so the two
+    planes meet below the outlet and form a V-wedge with no opening.  mu 0.5, CoR 0.1,
+    dt 0.005, gravity (0, -9.81)."""
+    t = math.tan(math.radians(angle_deg))
+    width = 30.0 * math.sqrt(n / 262144.0)
+    height = 71.4 * math.sqrt(n / 262144.0)
+    s = dense_pile(n=n, seed=seed, width=width, height=height, rmin=0.02, rmax=0.05, radii="uniform")
+    y0 = max(0.0, (0.5 * width - 0.5 * outlet) / t) + 0.1
+    q = s["q"].reshape(-1, 2).copy()
+    q[:, 1] += y0
+    c, sn = math.cos(math.radians(angle_deg)), math.sin(math.radians(angle_deg))
+    plane_x = np.array([[-0.5 * outlet, 0.0], [0.5 * outlet, 0.0]])
+    plane_n = np.array([[c, sn], [-c, sn]])
+    return dict(q=q.reshape(-1), v=s["v"], r=s["r"], m=s["m"], plane_x=plane_x, plane_n=plane_n, dt=0.005,
+                gravity=(0.0, -9.81), CoR=0.1, mu=0.5, tol=1e-6, max_iters=5000, name="hopper_%d" % n)
 
 
 def ball2d_batch(n_scenes: int = 4096, seed: int = 3, nmin: int = 16, nmax: int = 4096, rmin: float = 0.03,
