@@ -1072,8 +1072,10 @@ __global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
   unsigned n_eval = 0;
   for (it = 1; it <= A.max_iters; ++it) {
     for (int col = 0; col < ncol; ++col) {
+      // Consecutive contacts of a colour go to consecutive blocks (one per SM), so that a
+      // small colour spreads its FP64 work over every SM instead of filling a few.
       const int e = s_off[col + 1];
-      for (int s = s_off[col] + tid; s < e; s += nthr) gs_update3(A, A.perm[s]);
+      for (int s = s_off[col] + blockIdx.x + gridDim.x * threadIdx.x; s < e; s += nthr) gs_update3(A, A.perm[s]);
       if (!grid_sync(A.gb, A.spin)) {
         if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
         return;
@@ -1312,7 +1314,7 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   G.eval_every = ctx->cfg.eval_every;
   {
     void* args[] = {&G};
-    const int grid = coop_grid(ctx, k_gs3, nc, kGs3Block, 1);
+    const int grid = coop_grid(ctx, k_gs3, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
     if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
     SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs3, dim3(grid), dim3(kGs3Block), args, 0, s));
     if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
