@@ -58,6 +58,13 @@ BYTES_PER_BODY_LIFT = 40
 #   residual: ia 4, ib 4, basis 72, angular rows 96, c 24, (v, omega) 2x64, r 24, snapshot 24, mu 8
 BYTES_PER_CONTACT_SWEEP_3D = 724
 BYTES_PER_CONTACT_EVAL_3D = 384
+#   FP32 sweep: (a, b) 8, basis 36, angular rows 48, c 12, W 24, mu 4, r 12+12, minv 2x4, Iinv 2x36,
+#               (v, omega) 2x(16+16) r + 2x(16+16) w
+#   FP32 -> FP64 lift: per contact perm 4, r32 12, r64 24 w, two adjacency visits x (adj 4, ia 4, basis 72,
+#               angular rows 48, r 24); per body v0 48, minv 8, Iinv 72, (v, omega) 64 w + 32 w
+BYTES_PER_CONTACT_SWEEP32_3D = 364
+BYTES_PER_CONTACT_LIFT_3D = 344
+BYTES_PER_BODY_LIFT_3D = 224
 
 
 def gs_bytes(prof):
@@ -290,7 +297,7 @@ def sphere_leg(args, torch, local, flush):
     s = scenes.sphere_pile(n=args.spheres)
     kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, max_iters=args.preroll_iters,
               integrator=_lib.SPLIT_HAM, device=local)
-    ctx = _lib.Context(**kw)
+    ctx = _lib.Context(precision=args.precision, **kw)
     ctx.upload_sphere3d(s["q"], s["v"], s["r"], s["m"], s["I0"], s["plane_x"], s["plane_n"])
     t0 = time.perf_counter()
     ctx.step(args.sphere_preroll)
@@ -305,15 +312,19 @@ def sphere_leg(args, torch, local, flush):
     value = sum(contacts) / (tot / 1e3)
     hbm, peak_kind = peaks()
     gl = max(prof["gs_launches"], 1)
-    b_launch = (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP_3D + prof["contact_evals"] * BYTES_PER_CONTACT_EVAL_3D) / gl
+    b_launch = (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP_3D + prof["contact_sweeps32"] * BYTES_PER_CONTACT_SWEEP32_3D +
+                prof["contact_evals"] * BYTES_PER_CONTACT_EVAL_3D + prof["contact_lifts"] * BYTES_PER_CONTACT_LIFT_3D +
+                prof["body_lifts"] * BYTES_PER_BODY_LIFT_3D) / gl
     ms_launch = prof["gs_ms"] / gl
     ach = b_launch / (ms_launch / 1e3) / 1e9 if ms_launch > 0 else 0.0
     out = {"workload": "sphere_pile_%d" % args.spheres, "value": value, "unit": UNIT, "steps": args.sphere_steps,
            "timed_steps": [args.sphere_preroll + 1, args.sphere_preroll + args.sphere_steps],
            "ms_per_step": tot / args.sphere_steps, "contacts_per_step": sum(contacts) / args.sphere_steps,
-           "gs_iterations_per_step": prof["contact_sweeps"] / max(sum(contacts), 1),
-           "form": "FP64 sweeps, cold start (no 3D impulse cache in the reference's geometric map)",
-           "roofline": {"kernel": "k_gs3", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+           "gs_iterations_per_step": (prof["contact_sweeps"] + prof["contact_sweeps32"]) / max(sum(contacts), 1),
+           "fp32_sweep_share": prof["contact_sweeps32"] / max(prof["contact_sweeps"] + prof["contact_sweeps32"], 1),
+           "form": ("FP32 sweeps + FP64 residual and refinement" if args.precision == 1 else "FP64 sweeps") +
+                   ", cold start (no 3D impulse cache in the reference's geometric map)",
+           "roofline": {"kernel": "k_gs3_mixed" if args.precision == 1 else "k_gs3", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                         "frac": ach / hbm, "peak_kind": peak_kind, "bytes_per_launch": b_launch,
                         "ms_per_launch": ms_launch, "gs_share_of_step": prof["gs_ms"] / tot if tot else None},
            "gpu_launches": prof["kernel_launches"]}

@@ -198,7 +198,7 @@ void sg_ctx_destroy(sg_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   Buf* bufs3[] = {&ctx->I0, &ctx->Iw, &ctx->Iinv, &ctx->E3, &ctx->Aa3, &ctx->Ab3, &ctx->c3, &ctx->W3,
                   &ctx->r3, &ctx->r3a, &ctx->r3b, &ctx->ab3, &ctx->vrun3, &ctx->pk_ab, &ctx->pk_n, &ctx->pk_c,
-                  &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32};
+                  &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32, &ctx->pk3, &ctx->Iinv32};
   for (Buf* b : bufs3) release(*b);
   Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
                   &ctx->mlp_choice};

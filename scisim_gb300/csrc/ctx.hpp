@@ -141,6 +141,7 @@ struct sg_ctx {
   // (alpha, beta0, beta1) out (3); running velocities (2 double4 per body: v, omega).
   int64_t ccap3 = 0;
   sg::Buf E3, Aa3, Ab3, c3, W3, r3, r3a, r3b, ab3, vrun3;
+  sg::Buf pk3, Iinv32;  // 3D FP32 sweep data (colour-packed contacts, body inverse inertia)
   // Batched Ball2D scenes (sg_batch2d_upload).  Scene s owns bodies [sb_off[s], sb_off[s+1]),
   // planes [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]); its contacts of a
   // step are [sc_off[s], sc_off[s+1]).  Counts live on the device (b_ctl: contact count,

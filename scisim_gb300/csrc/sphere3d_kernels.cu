@@ -1131,6 +1131,389 @@ __global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision for spheres, as k_gs_mixed for discs: FP32 sweeps over colour-packed
+// FP32 copies (contact s of the packed arrays is contact perm[s]), the FP64 image lifted and
+// checked on a growing schedule, FP64 sweeps to finish once FP32 reached tol or its rounding
+// floor.
+constexpr int kGs3mBlock = 256;
+
+struct Gs3m {
+  const int2* ab;       // (a, b) per packed contact
+  const float* E;       // 9 per packed contact
+  const float* Aa;      // 6
+  const float* Ab;      // 6
+  const float* c;       // 3
+  const float* W;       // 6
+  const float* mu;
+  float* r;             // 3
+  float4* V;            // 2 per body: (v, 0), (omega, 0)
+  const float* minv;
+  const float* Iinv;    // 9 per body
+  const double* v0;     // [v (3nb) | omega (3nb)]
+  const int* body_off;
+  const int* body_adj;
+  int nb;
+  unsigned eval32;
+  unsigned long long* work;  // [0] FP32 updates, [1] FP64 updates, [2] evaluations, [3] lifts (contacts), [4] lifts (bodies)
+};
+
+__device__ __forceinline__ float dot3f(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+__device__ __forceinline__ void matvec3f(const float* A, const float* x, float* y) {
+  const float t0 = (A[0] * x[0] + A[1] * x[1]) + A[2] * x[2];
+  const float t1 = (A[3] * x[0] + A[4] * x[1]) + A[5] * x[2];
+  const float t2 = (A[6] * x[0] + A[7] * x[1]) + A[8] * x[2];
+  y[0] = t0;
+  y[1] = t1;
+  y[2] = t2;
+}
+
+// The 3D local Coulomb solve in FP32: take-off, stick, and the slide by Newton on the slip
+// speed; a degenerate problem takes the stick solution projected onto the cone.
+__device__ void local_solve_3d_f(const float* a, const float* b, float mu, float* r) {
+  if (b[0] >= 0.0f) {
+    r[0] = r[1] = r[2] = 0.0f;
+    return;
+  }
+  const float a00 = a[0], a01 = a[1], a02 = a[2], a11 = a[3], a12 = a[4], a22 = a[5];
+  const float c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+  const float c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
+  const float det = a00 * c00 + a01 * c01 + a02 * c02;
+  const float rs0 = -(c00 * b[0] + c01 * b[1] + c02 * b[2]) / det;
+  const float rs1 = -(c01 * b[0] + c11 * b[1] + c12 * b[2]) / det;
+  const float rs2 = -(c02 * b[0] + c12 * b[1] + c22 * b[2]) / det;
+  if (rs0 >= 0.0f && sqrtf(rs1 * rs1 + rs2 * rs2) <= mu * rs0) {
+    r[0] = rs0;
+    r[1] = rs1;
+    r[2] = rs2;
+    return;
+  }
+  float rn = -b[0] / a00, d0 = 1.0f, d1 = 0.0f;
+  bool ok = false;
+  if (mu == 0.0f) {
+    r[0] = rn;
+    r[1] = r[2] = 0.0f;
+    return;
+  }
+  for (int outer = 0; outer < 4; ++outer) {
+    const float cc = mu * rn;
+    const float g0 = a01 * rn + b[1], g1 = a02 * rn + b[2];
+    const float m00 = cc * a11, m01 = cc * a12, m11 = cc * a22;
+    const float hs = 0.5f * (m00 + m11), hd = 0.5f * (m00 - m11);
+    float al = sqrtf(g0 * g0 + g1 * g1) - (hs + sqrtf(hd * hd + m01 * m01));
+    if (!(al > 0.0f)) al = 0.0f;
+    float e0 = 0.0f, e1 = 0.0f;
+    for (int it = 0; it < 24; ++it) {
+      const float p00 = al + m00, p11 = al + m11;
+      const float inv = 1.0f / (p00 * p11 - m01 * m01);
+      e0 = (p11 * g0 - m01 * g1) * inv;
+      e1 = (p00 * g1 - m01 * g0) * inv;
+      const float f = e0 * e0 + e1 * e1 - 1.0f;
+      const float q0 = (p11 * e0 - m01 * e1) * inv, q1 = (p00 * e1 - m01 * e0) * inv;
+      const float fp = -2.0f * (e0 * q0 + e1 * q1);
+      if (!(f > 0.0f) || !(fp < 0.0f)) break;
+      const float step = -f / fp;
+      al += step;
+      if (!(step > 1e-7f * (1.0f + al))) break;
+    }
+    const float ne = sqrtf(e0 * e0 + e1 * e1);
+    if (!(ne > 0.0f)) break;
+    d0 = e0 / ne;
+    d1 = e1 / ne;
+    const float den = a00 - mu * (a01 * d0 + a02 * d1);
+    if (!(den > 0.0f)) break;
+    const float rn_new = -b[0] / den;
+    const bool same = fabsf(rn_new - rn) <= 1e-7f * fabsf(rn_new);
+    rn = rn_new;
+    if (same) {
+      ok = true;
+      break;
+    }
+  }
+  if (ok && rn >= 0.0f) {
+    r[0] = rn;
+    r[1] = -mu * rn * d0;
+    r[2] = -mu * rn * d1;
+    return;
+  }
+  const float rn2 = fmaxf(rs0, 0.0f);
+  const float nt = sqrtf(rs1 * rs1 + rs2 * rs2);
+  const float sc = (nt > mu * rn2 && nt > 0.0f) ? (mu * rn2) / nt : 1.0f;
+  r[0] = rn2;
+  r[1] = rs1 * sc;
+  r[2] = rs2 * sc;
+}
+
+__device__ __forceinline__ void gs_update3_f(const Gs3m& B, int s) {
+  const int2 ab = B.ab[s];
+  const int a = ab.x, b = ab.y;
+  const bool has_b = b >= 0;
+  float E[9], Aa[6], Ab[6], W[6], c[3];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) E[j] = B.E[9 * (size_t)s + j];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    Aa[j] = B.Aa[6 * (size_t)s + j];
+    Ab[j] = B.Ab[6 * (size_t)s + j];
+    W[j] = B.W[6 * (size_t)s + j];
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) c[j] = B.c[3 * (size_t)s + j];
+  const float4 la = __ldcg(&B.V[2 * a]), wa = __ldcg(&B.V[2 * a + 1]);
+  const float va[3] = {la.x, la.y, la.z}, oa[3] = {wa.x, wa.y, wa.z};
+  float vb[3] = {0.0f, 0.0f, 0.0f}, ob[3] = {0.0f, 0.0f, 0.0f};
+  float4 lb = make_float4(0.f, 0.f, 0.f, 0.f), wb = lb;
+  if (has_b) {
+    lb = __ldcg(&B.V[2 * b]);
+    wb = __ldcg(&B.V[2 * b + 1]);
+    vb[0] = lb.x;
+    vb[1] = lb.y;
+    vb[2] = lb.z;
+    ob[0] = wb.x;
+    ob[1] = wb.y;
+    ob[2] = wb.z;
+  }
+  float u[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float h = dot3f(E + 3 * i, va);
+    if (i > 0) h += dot3f(Aa + 3 * (i - 1), oa);
+    if (has_b) {
+      float hb = dot3f(E + 3 * i, vb);
+      if (i > 0) hb += dot3f(Ab + 3 * (i - 1), ob);
+      h -= hb;
+    }
+    u[i] = h + c[i];
+  }
+  const float r0 = __ldcg(&B.r[3 * (size_t)s]), r1 = __ldcg(&B.r[3 * (size_t)s + 1]), r2 = __ldcg(&B.r[3 * (size_t)s + 2]);
+  const float bt[3] = {u[0] - ((W[0] * r0 + W[1] * r1) + W[2] * r2), u[1] - ((W[1] * r0 + W[3] * r1) + W[4] * r2),
+                       u[2] - ((W[2] * r0 + W[4] * r1) + W[5] * r2)};
+  float rn[3];
+  local_solve_3d_f(W, bt, B.mu[s], rn);
+  const float d0 = rn[0] - r0, d1 = rn[1] - r1, d2 = rn[2] - r2;
+  float pl[3], pa[3], pb[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    pl[j] = (E[j] * d0 + E[3 + j] * d1) + E[6 + j] * d2;
+    pa[j] = Aa[j] * d1 + Aa[3 + j] * d2;
+    pb[j] = Ab[j] * d1 + Ab[3 + j] * d2;
+  }
+  float Ii[9], w[3];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Ii[j] = B.Iinv[9 * (size_t)a + j];
+  matvec3f(Ii, pa, w);
+  const float ma = B.minv[a];
+  B.V[2 * a] = make_float4(la.x + ma * pl[0], la.y + ma * pl[1], la.z + ma * pl[2], 0.0f);
+  B.V[2 * a + 1] = make_float4(wa.x + w[0], wa.y + w[1], wa.z + w[2], 0.0f);
+  if (has_b) {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) Ii[j] = B.Iinv[9 * (size_t)b + j];
+    matvec3f(Ii, pb, w);
+    const float mb = B.minv[b];
+    B.V[2 * b] = make_float4(lb.x - mb * pl[0], lb.y - mb * pl[1], lb.z - mb * pl[2], 0.0f);
+    B.V[2 * b + 1] = make_float4(wb.x - w[0], wb.y - w[1], wb.z - w[2], 0.0f);
+  }
+  B.r[3 * (size_t)s] = rn[0];
+  B.r[3 * (size_t)s + 1] = rn[1];
+  B.r[3 * (size_t)s + 2] = rn[2];
+}
+
+__global__ void k_pack3(int nc, const int* __restrict__ perm, Contacts3 C, const double* __restrict__ r, Gs3m B,
+                        float* __restrict__ r32) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nc) return;
+  const int k = perm[s];
+  const int b = C.ib[k];
+  const_cast<int2*>(B.ab)[s] = make_int2(C.ia[k], b >= 0 ? b : -1);
+  float* E = const_cast<float*>(B.E) + 9 * (size_t)s;
+  float* Aa = const_cast<float*>(B.Aa) + 6 * (size_t)s;
+  float* Ab = const_cast<float*>(B.Ab) + 6 * (size_t)s;
+  float* W = const_cast<float*>(B.W) + 6 * (size_t)s;
+  float* cc = const_cast<float*>(B.c) + 3 * (size_t)s;
+  for (int j = 0; j < 9; ++j) E[j] = (float)C.E[9 * (size_t)k + j];
+  for (int j = 0; j < 6; ++j) {
+    Aa[j] = (float)C.Aa[6 * (size_t)k + j];
+    Ab[j] = (float)C.Ab[6 * (size_t)k + j];
+    W[j] = (float)C.W[6 * (size_t)k + j];
+  }
+  for (int j = 0; j < 3; ++j) {
+    cc[j] = (float)C.c[3 * (size_t)k + j];
+    r32[3 * (size_t)s + j] = (float)r[3 * (size_t)k + j];
+  }
+  const_cast<float*>(B.mu)[s] = (float)C.mu[k];
+}
+
+__global__ void k_body32(int nb, const double4_32a* __restrict__ V, const double* __restrict__ minv,
+                         const double* __restrict__ Iinv, float4* __restrict__ V32, float* __restrict__ minv32,
+                         float* __restrict__ Iinv32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double4_32a a = V[2 * i], w = V[2 * i + 1];
+  V32[2 * i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.0f);
+  V32[2 * i + 1] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.0f);
+  minv32[i] = (float)minv[i];
+  for (int j = 0; j < 9; ++j) Iinv32[9 * (size_t)i + j] = (float)Iinv[9 * (size_t)i + j];
+}
+
+__global__ void __launch_bounds__(kGs3mBlock, 1) k_gs3_mixed(Gs3Args A, Gs3m B) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
+  double* best = A.r_a;
+  double* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false, fp64 = false;
+  unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
+  unsigned next_eval = 1, interval = eval32;
+  for (it = 1; it <= A.max_iters; ++it) {
+    bool do_eval;
+    if (!fp64) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + blockIdx.x + gridDim.x * threadIdx.x; s < e; s += nthr) gs_update3_f(B, s);
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      ++s32;
+      do_eval = it == next_eval || it == A.max_iters;
+      if (do_eval) {
+        for (int s = tid; s < A.nc; s += nthr) {
+          const int k = A.perm[s];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) A.r[3 * (size_t)k + j] = (double)__ldcg(&B.r[3 * (size_t)s + j]);
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+        for (int i = tid; i < B.nb; i += nthr) {
+          double hl[3], ha[3], Ii[9], wa[3];
+          gather_htr3(i, B.body_off, B.body_adj, A.C, A.r, hl, ha);
+#pragma unroll
+          for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)i + j];
+          matvec3(Ii, ha, wa);
+          const double mi = A.minv[i];
+          const double* vl = B.v0 + 3 * (size_t)i;
+          const double* va = B.v0 + 3 * (size_t)B.nb + 3 * (size_t)i;
+          const double4_32a lv = make_double4_32a(vl[0] + mi * hl[0], vl[1] + mi * hl[1], vl[2] + mi * hl[2], 0.0);
+          const double4_32a wv = make_double4_32a(va[0] + wa[0], va[1] + wa[1], va[2] + wa[2], 0.0);
+          A.V[2 * i] = lv;
+          A.V[2 * i + 1] = wv;
+          B.V[2 * i] = make_float4((float)lv.x, (float)lv.y, (float)lv.z, 0.0f);
+          B.V[2 * i + 1] = make_float4((float)wv.x, (float)wv.y, (float)wv.z, 0.0f);
+        }
+        ++lifts;
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+    } else {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + blockIdx.x + gridDim.x * threadIdx.x; s < e; s += nthr) gs_update3(A, A.perm[s]);
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      ++s64;
+      do_eval = (it % eval64 == 0) || it == A.max_iters;
+    }
+    if (!do_eval) continue;
+    double emax = 0.0, excess = -INFINITY;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int a = A.C.ia[k], b = A.C.ib[k];
+      double E[9], Aa[6], Ab[6], u[3];
+      load_contact(A.C, k, E, Aa, Ab);
+      local_u3(A.C, k, A.V, u, a, b, E, Aa, Ab);
+      const double rk[3] = {__ldcg(&A.r[3 * (size_t)k]), __ldcg(&A.r[3 * (size_t)k + 1]),
+                            __ldcg(&A.r[3 * (size_t)k + 2])};
+      cand[3 * (size_t)k] = rk[0];
+      cand[3 * (size_t)k + 1] = rk[1];
+      cand[3 * (size_t)k + 2] = rk[2];
+      const double ek = fb_error_3d(rk, u, A.C.mu[k]);
+      emax = nanmax(emax, ek);
+      const double4_32a la = ld4cg(&A.V[2 * a]), wa = ld4cg(&A.V[2 * a + 1]);
+      double scale = fabs(la.x) + fabs(la.y) + fabs(la.z) + fabs(wa.x) + fabs(wa.y) + fabs(wa.z);
+      if (b >= 0) {
+        const double4_32a lb = ld4cg(&A.V[2 * b]), wb = ld4cg(&A.V[2 * b + 1]);
+        scale += fabs(lb.x) + fabs(lb.y) + fabs(lb.z) + fabs(wb.x) + fabs(wb.y) + fabs(wb.z);
+      }
+      scale += fabs(A.C.c[3 * (size_t)k]) + fabs(A.C.c[3 * (size_t)k + 1]) + fabs(A.C.c[3 * (size_t)k + 2]) +
+               fabs(rk[0]) + fabs(rk[1]) + fabs(rk[2]);
+      excess = nanmax(excess, ek - 64.0 * 1.1920929e-7 * scale);
+    }
+    emax = block_nanmax(emax);
+    const double mag = block_nanmax(excess);
+    const int slot = n_eval % 3;
+    if (threadIdx.x == 0) {
+      atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+      atomicMax(&A.st->mag_slot[slot], f64_to_ordered(mag));
+    }
+    if (tid == 0) {
+      A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+      A.st->mag_slot[(n_eval + 1) % 3] = 0ull;
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    const double excess32 = ordered_to_f64(*((volatile unsigned long long*)&A.st->mag_slot[slot]));
+    ++n_eval;
+    if (err < err_best) {
+      err_best = err;
+      double* t = best;
+      best = cand;
+      cand = t;
+      since_best = 0;
+    } else {
+      ++since_best;
+    }
+    if (!fp64) {
+      if (it < eval32) {
+        next_eval = 2 * it;
+      } else {
+        interval = (err > 1e3 * A.tol) ? min(2u * interval, 16u * eval32) : (err > 10.0 * A.tol ? interval : eval32);
+        next_eval = it + interval;
+      }
+    }
+    if (fp64) {
+      if (err < A.tol) {
+        converged = true;
+        break;
+      }
+    } else if (err < A.tol || excess32 <= A.tol || (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
+      fp64 = true;
+    }
+  }
+  if (it > A.max_iters) it = A.max_iters;
+  if (!converged) {
+    if (err_best < INFINITY)
+      for (int k = tid; k < 3 * A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+  }
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps32 = s32;
+    A.st->sweeps64 = s64;
+    A.st->evals = n_eval;
+    A.st->lifts = lifts;
+  }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1312,7 +1695,44 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   G.tol = ctx->cfg.tol;
   G.max_iters = ctx->cfg.max_iters;
   G.eval_every = ctx->cfg.eval_every;
-  {
+  if (ctx->cfg.precision == SG_PRECISION_FP32_REFINE) {
+    const size_t c = (size_t)std::max(nc, 1), b1 = (size_t)std::max(nb, 1);
+    if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
+    if (int r = grow(ctx->pk3, sizeof(float) * 31 * c)) return r;   // E 9, Aa 6, Ab 6, c 3, W 6, mu 1
+    if (int r = grow(ctx->pk_r, sizeof(float) * 3 * c)) return r;
+    if (int r = grow(ctx->v32, sizeof(float4) * 2 * b1)) return r;
+    if (int r = grow(ctx->minv32, sizeof(float) * b1)) return r;
+    if (int r = grow(ctx->Iinv32, sizeof(float) * 9 * b1)) return r;
+    float* f = ctx->pk3.as<float>();
+    Gs3m B;
+    B.ab = ctx->pk_ab.as<int2>();
+    B.E = f;
+    B.Aa = f + 9 * c;
+    B.Ab = f + 15 * c;
+    B.c = f + 21 * c;
+    B.W = f + 24 * c;
+    B.mu = f + 30 * c;
+    B.r = ctx->pk_r.as<float>();
+    B.V = ctx->v32.as<float4>();
+    B.minv = ctx->minv32.as<float>();
+    B.Iinv = ctx->Iinv32.as<float>();
+    B.v0 = ctx->v.as<double>();
+    B.body_off = off;
+    B.body_adj = adj;
+    B.nb = nb;
+    B.eval32 = 16;
+    B.work = nullptr;
+    k_pack3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), C, A.r, B, B.r);
+    k_body32<<<blocks_for(nb), kBlock, 0, s>>>(nb, V, ctx->minv.as<double>(), ctx->Iinv.as<double>(), B.V,
+                                              const_cast<float*>(B.minv), const_cast<float*>(B.Iinv));
+    SG_CUDA_TRY(cudaGetLastError());
+    void* args[] = {&G, &B};
+    const int grid = coop_grid(ctx, k_gs3_mixed, (long)ctx->num_sms * kGs3mBlock, kGs3mBlock, 1);
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_mixed, grid, kGs3mBlock, args, s));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+    ctx->kernel_launches += 2;
+  } else {
     void* args[] = {&G};
     const int grid = coop_grid(ctx, k_gs3, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
     if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
@@ -1338,7 +1758,10 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   }
   ctx->gs_launches += 1;
   ctx->contact_sweeps += (uint64_t)ctx->h_stats.sweeps64 * (uint64_t)nc;
+  ctx->contact_sweeps32 += (uint64_t)ctx->h_stats.sweeps32 * (uint64_t)nc;
   ctx->contact_evals += (uint64_t)ctx->h_stats.evals * (uint64_t)nc;
+  ctx->contact_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nc;
+  ctx->body_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nb;
   if (ctx->profile) {
     float ms = 0.f;
     SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));

@@ -197,3 +197,35 @@ def test_sphere3d_bad_inputs(gpulib):
     with pytest.raises(gpulib.SgError):
         ctx2.upload_sphere3d(s["q"], s["v"], s["r"], s["m"], s["I0"], s["plane_x"], np.zeros((5, 3)))
     assert gpulib.lib().sg_last_contacts(ctx.handle, 0, None, None, None, None, None) == -(2 ** 63)
+
+
+def test_sphere3d_fp32_refine(gpulib, oracle):
+    """FP32 sweeps + FP64 checks and refinement for spheres: a converged step meets the
+    tolerance under the oracle's FP64 residual of the GPU's impulses, and positions stay within
+    1e-3 of the FP64 solve after 60 steps."""
+    s = make_scene(n=900, seed=12)
+    f64 = gpu_ctx(gpulib, s, tol=1e-7, max_iters=3000)
+    f32 = gpu_ctx(gpulib, s, tol=1e-7, max_iters=3000, precision=gpulib.PRECISION_FP32_REFINE)
+    f64.step(60)
+    f32.step(59)
+    q0, v0 = f32.state()
+    st = f32.step(1)
+    g = f32.sphere3d_last_contacts()
+    sim = oracle_sim(oracle, s, q=q0, v=v0, tol=1e-7, max_iters=3000)
+    sim.set_state(q0, v0)
+    Iw, Iinv = sim.world_inertia()
+    sim.set_next_order(f32.last_solve_order()[0])
+    sim.step()
+    c = sim.last_contacts()
+    assert np.array_equal(g["ia"], c["ia"]) and np.array_equal(g["ib"], c["ib"])
+    ib = np.where(g["ib"] >= 0, g["ib"], -1)
+    res = oracle.residual_3d(s["m"], Iinv, Iw, v0, g["ia"], ib, g["bases"].reshape(-1), c["arm_a"].reshape(-1),
+                             c["arm_b"].reshape(-1), s["CoR"], s["mu"], g["alpha"], g["beta"].reshape(-1))
+    assert st["n_contacts"] > 100
+    if st["succeeded"]:
+        assert res <= 1e-7 * 1.001
+    assert abs(res - st["error"]) <= 1e-12 + 1e-6 * st["error"]
+    nb = s["r"].shape[0]
+    qa, _ = f64.state()
+    qb, _ = f32.state()
+    assert np.abs(qa[:3 * nb] - qb[:3 * nb]).max() <= 1e-3
