@@ -267,10 +267,17 @@ typedef struct {
   uint64_t contact_sweeps32; /* contact updates in FP32 sweeps (SG_PRECISION_FP32_REFINE) */
   uint64_t contact_lifts;    /* contacts lifted FP32 -> FP64 before a residual evaluation */
   uint64_t body_lifts;       /* body velocities re-gathered in FP64 for those evaluations */
+  uint64_t two_level_solves; /* FP32 solves that ran the two-level (patch) sweeps */
 } sg_profile;
 
 SG_API int sg_profile_enable(sg_ctx* ctx, int32_t on);
 SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
+
+/* Two-level FP32 sweeps for large single-scene steps (default on): contacts inside a spatial
+ * patch (one per SM) are swept on shared-memory velocities with block barriers, the contacts
+ * between patches over the grid -- a Gauss-Seidel order of the same kind as the colour order,
+ * with fewer grid barriers.  0 keeps the one-level colour sweeps. */
+SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
 
 /* The context's CUDA stream (cudaStream_t) for stream-ordered timing by the caller. */
 SG_API int sg_ctx_stream(sg_ctx* ctx, void** stream);

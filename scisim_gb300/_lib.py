@@ -45,7 +45,7 @@ class SgProfile(C.Structure):
     _fields_ = [("gs_ms", C.c_double), ("gs_launches", C.c_uint64), ("contact_sweeps", C.c_uint64),
                 ("contact_evals", C.c_uint64), ("kernel_launches", C.c_uint64), ("steps", C.c_uint64),
                 ("contacts", C.c_uint64), ("contact_sweeps32", C.c_uint64), ("contact_lifts", C.c_uint64),
-                ("body_lifts", C.c_uint64)]
+                ("body_lifts", C.c_uint64), ("two_level_solves", C.c_uint64)]
 
 
 class SgError(RuntimeError):
@@ -95,6 +95,7 @@ SIGNATURES = {
     "sg_mlp_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "sg_set_two_level": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sg_set_spin_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sg_selftest_wait_timeout": (C.c_int, [C.c_void_p]),
@@ -383,6 +384,9 @@ class Context:
         p = SgProfile()
         check(lib().sg_profile_read(self._h, C.byref(p), 1 if reset else 0), "sg_profile_read")
         return {k: getattr(p, k) for k, _ in p._fields_}
+
+    def set_two_level(self, on=True):
+        check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
 
     def stream_ptr(self):
         s = C.c_void_p()

@@ -198,7 +198,10 @@ void sg_ctx_destroy(sg_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   Buf* bufs3[] = {&ctx->I0, &ctx->Iw, &ctx->Iinv, &ctx->E3, &ctx->Aa3, &ctx->Ab3, &ctx->c3, &ctx->W3,
                   &ctx->r3, &ctx->r3a, &ctx->r3b, &ctx->ab3, &ctx->vrun3, &ctx->pk_ab, &ctx->pk_n, &ctx->pk_c,
-                  &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32, &ctx->pk3, &ctx->Iinv32};
+                  &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32, &ctx->pk3, &ctx->Iinv32, &ctx->pt_setup,
+                  &ctx->pt_patch, &ctx->pt_lidx, &ctx->pt_body, &ctx->pt_cnt, &ctx->pt_start, &ctx->pt_fill,
+                  &ctx->pt_key, &ctx->pt_kcnt, &ctx->pt_kstart, &ctx->pt_kfill, &ctx->pt_order, &ctx->pt_max,
+                  &ctx->pt_bcolor, &ctx->pt_rem};
   for (Buf* b : bufs3) release(*b);
   Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
                   &ctx->mlp_choice};
@@ -941,6 +944,12 @@ int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1a, cons
   return rc;
 }
 
+int sg_set_two_level(sg_ctx* ctx, int32_t on) {
+  if (!ctx) return SG_BAD_INPUT;
+  ctx->patches = on != 0;
+  return SG_OK;
+}
+
 int sg_ctx_stream(sg_ctx* ctx, void** stream) {
   if (!ctx || !stream) return SG_BAD_INPUT;
   *stream = (void*)ctx->stream;
@@ -970,7 +979,9 @@ int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset) {
   out->contact_sweeps32 = ctx->contact_sweeps32;
   out->contact_lifts = ctx->contact_lifts;
   out->body_lifts = ctx->body_lifts;
+  out->two_level_solves = ctx->patched_solves;
   if (reset) {
+    ctx->patched_solves = 0;
     ctx->gs_ms = 0.0;
     ctx->gs_launches = ctx->contact_sweeps = ctx->contact_evals = ctx->kernel_launches = 0;
     ctx->steps = ctx->contacts_total = 0;

@@ -142,6 +142,12 @@ struct sg_ctx {
   int64_t ccap3 = 0;
   sg::Buf E3, Aa3, Ab3, c3, W3, r3, r3a, r3b, ab3, vrun3;
   sg::Buf pk3, Iinv32;  // 3D FP32 sweep data (colour-packed contacts, body inverse inertia)
+  // Two-level FP32 sweeps (spatial patches, one per SM): patch of each body, patch-local
+  // index, bodies by patch, contact keys (patch, colour) and the packed order.
+  bool patches = true;
+  uint64_t patched_solves = 0;
+  sg::Buf pt_setup, pt_patch, pt_lidx, pt_body, pt_cnt, pt_start, pt_fill, pt_key, pt_kcnt, pt_kstart, pt_kfill,
+      pt_order, pt_max, pt_bcolor, pt_rem;
   // Batched Ball2D scenes (sg_batch2d_upload).  Scene s owns bodies [sb_off[s], sb_off[s+1]),
   // planes [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]); its contacts of a
   // step are [sc_off[s], sc_off[s+1]).  Counts live on the device (b_ctl: contact count,

@@ -1078,6 +1078,452 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
   }
 }
 
+// ---------------------------------------------------------------------------
+// Two-level sweeps: bodies are split into spatial patches (one per block, one block per SM).
+// A contact whose two bodies lie in one patch (or whose second body is a static plane) is
+// interior to that patch; the others are boundary contacts.  One FP32 sweep processes every
+// patch's interior contacts colour by colour inside its block, on shared-memory copies of the
+// patch's velocities with block barriers only, then the boundary contacts colour by colour
+// over the grid.  Patches share no body through interior contacts, so the sweep equals the
+// sequential Gauss-Seidel order "interior contacts patch by patch, each patch by colour, then
+// boundary contacts by colour" -- a valid Gauss-Seidel order of the same kind as the colour
+// order of k_gs_mixed, with about one grid barrier per boundary colour instead of one per colour.
+constexpr int kPatchBodyCap = 16384;  // bodies of one patch in shared memory (12 B each)
+
+struct PatchSetup {
+  int T0, T1, P, d0, d1;
+};
+
+struct PatchArgs {
+  const PatchSetup* ps;
+  const int* pstart;  // P + 1 body offsets
+  const int* pbody;   // bodies in patch order
+  const int* goff;    // (P + 1) * kMaxColors + 1 contact offsets: patch-major, then boundary
+  const int* order;   // packed index -> contact
+  int cap;            // shared-memory body capacity of the launch
+};
+
+// Tiles of grid cells, roughly square, at most max_patches of them.
+__global__ void k_patch_setup(const GridParams* __restrict__ gp, int max_patches, PatchSetup* ps) {
+  const int d0 = gp->dims[0], d1 = gp->dims[1];
+  int T0 = (int)sqrt((double)max_patches * (double)d0 / (double)d1);
+  T0 = max(1, min(min(d0, max_patches), T0));
+  const int T1 = max(1, min(d1, max_patches / T0));
+  ps->T0 = T0;
+  ps->T1 = T1;
+  ps->P = T0 * T1;
+  ps->d0 = d0;
+  ps->d1 = d1;
+}
+
+__global__ void k_patch_of_body(int nb, const int* __restrict__ cell_of, const PatchSetup* __restrict__ ps,
+                                int* __restrict__ patch, int* __restrict__ pcount) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int d0 = ps->d0, d1 = ps->d1;
+  const int cell = cell_of[i];
+  const int cx = cell % d0, cy = cell / d0;
+  const int tx = (int)((long)cx * ps->T0 / d0), ty = (int)((long)cy * ps->T1 / d1);
+  const int p = tx + ps->T0 * ty;
+  patch[i] = p;
+  atomicAdd(&pcount[p], 1);
+}
+
+__global__ void k_patch_scatter(int nb, const int* __restrict__ patch, const int* __restrict__ pstart,
+                                int* __restrict__ pfill, int* __restrict__ pbody, int* __restrict__ lidx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int p = patch[i];
+  const int j = atomicAdd(&pfill[p], 1);
+  pbody[pstart[p] + j] = i;
+  lidx[i] = j;
+}
+
+__global__ void k_patch_max(int n, const int* __restrict__ pcount, int* __restrict__ out) {
+  int m = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, pcount[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// Patch of each contact (its patch if interior, P if boundary); boundary contacts get their
+// own colouring below.
+__global__ void k_contact_side(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
+                               const int* __restrict__ patch, const PatchSetup* __restrict__ ps,
+                               int* __restrict__ cpatch, int* __restrict__ bcolor) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int a = ia[k], b = ib[k];
+  const int pa = patch[a];
+  const bool interior = b < 0 || patch[b] == pa;
+  cpatch[k] = interior ? pa : ps->P;
+  bcolor[k] = -1;
+}
+
+// Jones-Plassmann colouring of the boundary contacts alone (interior contacts neither take
+// nor block colours): the boundary subgraph is a set of thin bands, so it needs far fewer
+// colours than the whole contact graph.
+struct BColorArgs {
+  int nc;
+  const int* ia;
+  const int* ib;
+  const int* body_off;
+  const int* body_adj;
+  const int* cpatch;
+  const PatchSetup* ps;
+  int* bcolor;     // packed (round << 8) | colour, -1 uncoloured
+  int* remaining;  // 3 rotating counters
+  int* status;
+  GridBarrier* gb;
+  unsigned long long spin;
+  int max_rounds;
+};
+
+__global__ void k_color_boundary(BColorArgs A) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  const int P = A.ps->P;
+  volatile int* vcolor = A.bcolor;
+  for (int round = 0;; ++round) {
+    if (round >= A.max_rounds) {
+      if (tid == 0) atomicExch(A.status, (int)SG_CAPACITY);
+      return;
+    }
+    int rem = 0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      if (A.cpatch[k] != P || vcolor[k] >= 0) continue;
+      const unsigned pk = hash_prio((unsigned)k);
+      unsigned long long used = 0ull;
+      bool is_max = true;
+      const int bodies[2] = {A.ia[k], A.ib[k]};
+      for (int bi = 0; bi < 2 && is_max; ++bi) {
+        const int body = bodies[bi];
+        if (body < 0) continue;
+        const int e = A.body_off[body + 1];
+        for (int p = A.body_off[body]; p < e; ++p) {
+          const int j = A.body_adj[p];
+          if (j == k || A.cpatch[j] != P) continue;
+          const int cj = vcolor[j];
+          if (cj >= 0 && (cj >> 8) < round) {
+            used |= 1ull << (cj & 63);
+          } else if (prio_greater(hash_prio((unsigned)j), j, pk, k)) {
+            is_max = false;
+            break;
+          }
+        }
+      }
+      if (is_max) {
+        const unsigned long long freec = ~used;
+        if (freec == 0ull) {
+          atomicExch(A.status, (int)SG_CAPACITY);
+          vcolor[k] = (round << 8) | 63;
+        } else {
+          vcolor[k] = (round << 8) | (__ffsll((long long)freec) - 1);
+        }
+      } else {
+        ++rem;
+      }
+    }
+    rem = warp_sum(rem);
+    if ((threadIdx.x & 31) == 0 && rem) atomicAdd(&A.remaining[round % 3], rem);
+    if (tid == 0) A.remaining[(round + 1) % 3] = 0;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(A.status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    if (*((volatile int*)&A.remaining[round % 3]) == 0) break;
+  }
+}
+
+__global__ void k_contact_key(int nc, const int* __restrict__ color, const int* __restrict__ bcolor,
+                              const int* __restrict__ cpatch, const PatchSetup* __restrict__ ps, int* __restrict__ key,
+                              int* __restrict__ kcount) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int cp = cpatch[k];
+  const int c = (cp == ps->P ? bcolor[k] : color[k]) & (kMaxColors - 1);
+  const int kk = cp * kMaxColors + c;
+  key[k] = kk;
+  atomicAdd(&kcount[kk], 1);
+}
+
+__global__ void k_contact_scatter(int nc, const int* __restrict__ key, const int* __restrict__ kstart,
+                                  int* __restrict__ kfill, int* __restrict__ order) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int kk = key[k];
+  order[kstart[kk] + atomicAdd(&kfill[kk], 1)] = k;
+}
+
+// Packs in patch order; interior contacts carry patch-local body indices.
+__global__ void k_pack32_patch(int nc, const int* __restrict__ order, const int* __restrict__ key,
+                               const PatchSetup* __restrict__ ps, const int* __restrict__ ia,
+                               const int* __restrict__ ib, const int* __restrict__ lidx,
+                               const double2* __restrict__ n, const double2* __restrict__ c,
+                               const double* __restrict__ W, const double* __restrict__ mu,
+                               const double2* __restrict__ r, int2* __restrict__ ab, float2* __restrict__ n32,
+                               float2* __restrict__ c32, float4* __restrict__ w32, float2* __restrict__ r32) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nc) return;
+  const int k = order[s];
+  const int a = ia[k], b = ib[k];
+  const bool interior = key[k] < ps->P * kMaxColors;
+  if (interior)
+    ab[s] = make_int2(lidx[a], b >= 0 ? lidx[b] : -1);
+  else
+    ab[s] = make_int2(a, b >= 0 ? b : -1);
+  const double2 nk = n[k], ck = c[k], rk = r[k];
+  n32[s] = make_float2((float)nk.x, (float)nk.y);
+  c32[s] = make_float2((float)ck.x, (float)ck.y);
+  w32[s] = make_float4((float)W[3 * k], (float)W[3 * k + 1], (float)W[3 * k + 2], (float)mu[k]);
+  r32[s] = make_float2((float)rk.x, (float)rk.y);
+}
+
+// gs_update32 on the patch's shared-memory velocities (ab holds patch-local indices).
+__device__ __forceinline__ void gs_update32_local(const Gs32Args& B, int s, float2* sv, const float* sm) {
+  const int2 ab = B.ab[s];
+  const float2 nk = B.n[s], ck = B.c[s];
+  const float4 w = B.w[s];
+  const float2 va = sv[ab.x];
+  const bool has_b = ab.y >= 0;
+  const float2 vb = has_b ? sv[ab.y] : make_float2(0.0f, 0.0f);
+  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  float hn = nx * va.x + ny * va.y;
+  float ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn -= nx * vb.x + ny * vb.y;
+    ht -= tx * vb.x + ty * vb.y;
+  }
+  const float u0 = hn + ck.x, u1 = ht + ck.y;
+  const float2 rk = __ldcg(&B.r[s]);
+  const float bt0 = u0 - (w.x * rk.x + w.y * rk.y);
+  const float bt1 = u1 - (w.y * rk.x + w.z * rk.y);
+  float rn0, rn1;
+  local_solve_2d_f(w.x, w.y, w.z, bt0, bt1, w.w, rn0, rn1);
+  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
+  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
+  const float ma = sm[ab.x];
+  sv[ab.x] = make_float2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const float mb = sm[ab.y];
+    sv[ab.y] = make_float2(vb.x - mb * px, vb.y - mb * py);
+  }
+  B.r[s] = make_float2(rn0, rn1);
+}
+
+__global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B, PatchArgs Q) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  __syncthreads();
+  const int ncol = s_ncol;
+  // This block's patch: its bodies and its interior contacts by colour; the boundary
+  // contacts by colour, with a tail of small colours as in k_gs_mixed.
+  extern __shared__ float2 sv[];
+  float* sm = reinterpret_cast<float*>(sv + Q.cap);
+  __shared__ int s_goff[kMaxColors + 1];
+  __shared__ int s_boff[kMaxColors + 1];
+  const int P = Q.ps->P;
+  const int pb0 = blockIdx.x < P ? Q.pstart[blockIdx.x] : 0;
+  const int pb1 = blockIdx.x < P ? Q.pstart[blockIdx.x + 1] : 0;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) {
+    s_goff[c] = blockIdx.x < P ? Q.goff[blockIdx.x * kMaxColors + c] : 0;
+    s_boff[c] = Q.goff[P * kMaxColors + c];
+  }
+  for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) sm[j - pb0] = B.minv[Q.pbody[j]];
+  __syncthreads();
+  int btail = ncol;
+  while (btail > 0 && s_boff[btail] - s_boff[btail - 1] <= 2 * (int)blockDim.x) --btail;
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
+  double2* best = A.r_a;
+  double2* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false, fp64 = false;
+  unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
+  unsigned next_eval = 1, interval = eval32;
+  for (it = 1; it <= A.max_iters; ++it) {
+    bool do_eval;
+    if (!fp64) {
+      // Interior contacts of this block's patch, colour by colour, on shared-memory copies
+      // of the patch's body velocities (block barriers only).
+      for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) sv[j - pb0] = __ldcg(&B.v[Q.pbody[j]]);
+      __syncthreads();
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_goff[col + 1];
+        for (int s = s_goff[col] + threadIdx.x; s < e; s += blockDim.x) gs_update32_local(B, s, sv, sm);
+        __syncthreads();
+      }
+      for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) B.v[Q.pbody[j]] = sv[j - pb0];
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      // Contacts between patches, colour by colour over the grid; the small trailing colours
+      // run in block 0 alone.
+      for (int col = 0; col < btail; ++col) {
+        const int b0 = s_boff[col], e = s_boff[col + 1];
+        if (b0 == e) continue;
+        for (int s = b0 + tid; s < e; s += nthr) gs_update32(B, s);
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      if (btail < ncol && s_boff[btail] < s_boff[ncol]) {
+        if (blockIdx.x == 0) {
+          for (int col = btail; col < ncol; ++col) {
+            for (int s = s_boff[col] + threadIdx.x; s < s_boff[col + 1]; s += blockDim.x) gs_update32(B, s);
+            __syncthreads();
+          }
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      ++s32;
+      // FP64 checks after sweeps 1, 2, 4, ... eval32, then at an interval that grows
+      // (up to 16 eval32) while the residual is far above tol: a check costs several
+      // sweeps, and the final check at max_iters always happens.
+      do_eval = it == next_eval || it == A.max_iters;
+      if (do_eval) {
+        // Lift the FP32 iterate to FP64: impulses, then body velocities v = v0 + Minv H^T r.
+        for (int s = tid; s < A.nc; s += nthr) {
+          const float2 r32 = __ldcg(&B.r[s]);
+          A.r[Q.order[s]] = make_double2((double)r32.x, (double)r32.y);
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+        for (int i = tid; i < B.nb; i += nthr) {
+          double hx = 0.0, hy = 0.0;
+          const int e = B.body_off[i + 1];
+          for (int p = B.body_off[i]; p < e; ++p) {
+            const int k = B.body_adj[p];
+            const double sgn = (A.ia[k] == i) ? 1.0 : -1.0;
+            const double2 nk = A.n[k], rk = __ldcg(&A.r[k]);
+            const double px = nk.x * rk.x + (-nk.y) * rk.y;
+            const double py = nk.y * rk.x + nk.x * rk.y;
+            hx = hx + sgn * px;
+            hy = hy + sgn * py;
+          }
+          const double2 a = B.v0[i];
+          const double mi = B.minv64[i];
+          const double2 vi = make_double2(a.x + mi * hx, a.y + mi * hy);
+          A.v[i] = vi;
+          // Resynchronise the FP32 running velocity with the impulses: removes the
+          // rounding drift that incremental FP32 updates accumulate.
+          B.v[i] = make_float2((float)vi.x, (float)vi.y);
+        }
+        ++lifts;
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+    } else {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + tid; s < e; s += nthr) gs_update(A, A.perm[s]);
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      ++s64;
+      do_eval = (it % eval64 == 0) || it == A.max_iters;
+    }
+    if (!do_eval) continue;
+    // emax: the residual.  excess: the largest amount by which a contact's error exceeds
+    // the FP32 rounding floor of that contact, 64 eps_fp32 times the magnitudes entering
+    // u = H v + c (|v_a| + |v_b| + |c|) and r; when it is below tol, FP32 sweeps can no
+    // longer make progress and FP64 sweeps take over.
+    double emax = 0.0, excess = -INFINITY;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int a = A.ia[k], b = A.ib[k];
+      const bool has_b = b >= 0;
+      const double2 va = __ldcg(&A.v[a]);
+      const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+      const double2 ck = A.c[k];
+      double u0, u1;
+      local_velocity(A.n[k], ck, va, has_b, vb, u0, u1);
+      const double2 rk = __ldcg(&A.r[k]);
+      cand[k] = rk;
+      const double ek = fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]);
+      emax = nanmax(emax, ek);
+      const double scale = fabs(va.x) + fabs(va.y) + fabs(vb.x) + fabs(vb.y) + fabs(ck.x) + fabs(ck.y) +
+                           fabs(rk.x) + fabs(rk.y);
+      excess = nanmax(excess, ek - 64.0 * 1.1920929e-7 * scale);
+    }
+    emax = block_nanmax(emax);
+    const double mag = block_nanmax(excess);
+    const int slot = n_eval % 3;
+    if (threadIdx.x == 0) {
+      atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+      atomicMax(&A.st->mag_slot[slot], f64_to_ordered(mag));
+    }
+    if (tid == 0) {
+      A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+      A.st->mag_slot[(n_eval + 1) % 3] = 0ull;
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    const double excess32 = ordered_to_f64(*((volatile unsigned long long*)&A.st->mag_slot[slot]));
+    ++n_eval;
+    if (err < err_best) {
+      err_best = err;
+      double2* t = best;
+      best = cand;
+      cand = t;
+      since_best = 0;
+    } else {
+      ++since_best;
+    }
+    if (!fp64) {
+      if (it < eval32) {
+        next_eval = 2 * it;
+      } else {
+        interval = (err > 1e3 * A.tol) ? min(2u * interval, 16u * eval32) : (err > 10.0 * A.tol ? interval : eval32);
+        next_eval = it + interval;
+      }
+    }
+    if (fp64) {
+      if (err < A.tol) {
+        converged = true;
+        break;
+      }
+    } else if (err < A.tol || excess32 <= A.tol || (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
+      // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
+      // FP64 sweeps once every contact's remaining error is within FP32 rounding of
+      // its floor (or FP32 stopped improving the best iterate close to it).
+      fp64 = true;
+    }
+  }
+  if (it > A.max_iters) it = A.max_iters;
+  if (!converged) {
+    if (err_best < INFINITY)
+      for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+  }
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps32 = s32;
+    A.st->sweeps64 = s64;
+    A.st->evals = n_eval;
+    A.st->lifts = lifts;
+  }
+}
+
 // FP64 Coulomb residual of a start impulse r at running velocities v (one residual
 // evaluation of k_gs), maximum into *slot (ordered encoding).
 __global__ void k_start_err(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
@@ -1477,10 +1923,78 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       if (int r = grow(ctx->pk_r, sizeof(float2) * c)) return r;
       if (int r = grow(ctx->v32, sizeof(float2) * b)) return r;
       if (int r = grow(ctx->minv32, sizeof(float) * b)) return r;
-      k_pack32<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), P.ia, P.ib, n2,
-                                                 reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2,
-                                                 ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
-                                                 ctx->pk_w.as<float4>(), ctx->pk_r.as<float2>());
+      // Two-level sweeps for large scene steps (the broad phase's grid gives the patches).
+      int pmax = 0;
+      const int maxP = ctx->num_sms;
+      const bool try_patches = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 && nc >= 20000;
+      if (try_patches) {
+        const size_t keys = (size_t)(maxP + 1) * kMaxColors + 1;
+        if (int r = grow(ctx->pt_setup, sizeof(PatchSetup))) return r;
+        if (int r = grow(ctx->pt_patch, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_lidx, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_body, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_cnt, sizeof(int) * (size_t)(maxP + 2))) return r;
+        if (int r = grow(ctx->pt_start, sizeof(int) * (size_t)(maxP + 2))) return r;
+        if (int r = grow(ctx->pt_fill, sizeof(int) * (size_t)(maxP + 2))) return r;
+        if (int r = grow(ctx->pt_key, sizeof(int) * c)) return r;
+        if (int r = grow(ctx->pt_kcnt, sizeof(int) * keys)) return r;
+        if (int r = grow(ctx->pt_kstart, sizeof(int) * keys)) return r;
+        if (int r = grow(ctx->pt_kfill, sizeof(int) * keys)) return r;
+        if (int r = grow(ctx->pt_order, sizeof(int) * c)) return r;
+        if (int r = grow(ctx->pt_max, sizeof(int))) return r;
+        if (int r = grow(ctx->pt_bcolor, sizeof(int) * c)) return r;
+        if (int r = grow(ctx->pt_rem, 4 * sizeof(int))) return r;
+        PatchSetup* ps = ctx->pt_setup.as<PatchSetup>();
+        k_patch_setup<<<1, 1, 0, s>>>(ctx->grid.as<GridParams>(), maxP, ps);
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_cnt.p, 0, sizeof(int) * (size_t)(maxP + 2), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_fill.p, 0, sizeof(int) * (size_t)(maxP + 2), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kcnt.p, 0, sizeof(int) * keys, s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kfill.p, 0, sizeof(int) * keys, s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, sizeof(int), s));
+        k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, ctx->pt_patch.as<int>(),
+                                                         ctx->pt_cnt.as<int>());
+        SG_CUDA_TRY(cudaGetLastError());
+        if (int r = scan_exclusive(ctx, ctx->pt_cnt.as<int>(), ctx->pt_start.as<int>(), maxP)) return r;
+        k_patch_scatter<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_patch.as<int>(), ctx->pt_start.as<int>(),
+                                                         ctx->pt_fill.as<int>(), ctx->pt_body.as<int>(),
+                                                         ctx->pt_lidx.as<int>());
+        k_patch_max<<<1, kBlock, 0, s>>>(maxP, ctx->pt_cnt.as<int>(), ctx->pt_max.as<int>());
+        int* cpatch = ctx->pt_order.as<int>();  // scratch until the order is built
+        int* bcolor = ctx->pt_bcolor.as<int>();
+        k_contact_side<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, ctx->pt_patch.as<int>(), ps, cpatch, bcolor);
+        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_rem.p, 0, 4 * sizeof(int), s));
+        {
+          BColorArgs BA{nc, P.ia, P.ib, off, adj, cpatch, ps, bcolor, ctx->pt_rem.as<int>(), &st->status, gb,
+                        ctx->spin_limit, 4096};
+          void* bargs[] = {&BA};
+          const int g = coop_grid(ctx, k_color_boundary, nc, kBlock);
+          SG_CUDA_TRY(launch_cooperative((const void*)k_color_boundary, g, kBlock, bargs, s));
+        }
+        k_contact_key<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->color.as<int>(), bcolor, cpatch, ps,
+                                                       ctx->pt_key.as<int>(), ctx->pt_kcnt.as<int>());
+        SG_CUDA_TRY(cudaGetLastError());
+        if (int r = scan_exclusive(ctx, ctx->pt_kcnt.as<int>(), ctx->pt_kstart.as<int>(), (int)(keys - 1))) return r;
+        k_contact_scatter<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_key.as<int>(), ctx->pt_kstart.as<int>(),
+                                                           ctx->pt_kfill.as<int>(), ctx->pt_order.as<int>());
+        SG_CUDA_TRY(cudaGetLastError());
+        SG_CUDA_TRY(cudaMemcpyAsync(&pmax, ctx->pt_max.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SG_CUDA_TRY(cudaStreamSynchronize(s));
+        ctx->kernel_launches += 15;  // setup, of_body, 3 scan, scatter, max, side, colour, key, 3 scan, scatter
+      }
+      const bool patched = try_patches && pmax > 0 && pmax <= kPatchBodyCap;
+      if (patched)
+        k_pack32_patch<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_order.as<int>(), ctx->pt_key.as<int>(),
+                                                         ctx->pt_setup.as<PatchSetup>(), P.ia, P.ib,
+                                                         ctx->pt_lidx.as<int>(), n2, reinterpret_cast<const double2*>(P.c),
+                                                         P.W, P.mu, r2, ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(),
+                                                         ctx->pk_c.as<float2>(), ctx->pk_w.as<float4>(),
+                                                         ctx->pk_r.as<float2>());
+      else
+        k_pack32<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), P.ia, P.ib, n2,
+                                                   reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2,
+                                                   ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
+                                                   ctx->pk_w.as<float4>(), ctx->pk_r.as<float2>());
       k_vel32<<<blocks_for(nb), kBlock, 0, s>>>(nb, vrun, P.minv, ctx->v32.as<float2>(), ctx->minv32.as<float>());
       SG_CUDA_TRY(cudaGetLastError());
       Gs32Args GB;
@@ -1497,11 +2011,40 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.body_adj = adj;
       GB.nb = nb;
       GB.eval32 = 16;
-      void* args[] = {&GA, &GB};
-      const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
-      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
-      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+      if (patched) {
+        PatchArgs Q{ctx->pt_setup.as<PatchSetup>(), ctx->pt_start.as<int>(), ctx->pt_body.as<int>(),
+                    ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), pmax};
+        const size_t smem = (size_t)12 * (size_t)pmax;
+        static bool attr_set = false;
+        if (!attr_set) {
+          SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           12 * kPatchBodyCap));
+          attr_set = true;
+        }
+        void* args[] = {&GA, &GB, &Q};
+        // The boundary colouring used the barrier: start it afresh for this grid.
+        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(maxP);
+        lc.blockDim = dim3(kGs32Block);
+        lc.dynamicSmemBytes = smem;
+        lc.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        SG_CUDA_TRY(cudaLaunchKernelExC(&lc, (const void*)k_gs_patch, args));
+        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+        ctx->patched_solves += 1;
+      } else {
+        void* args[] = {&GA, &GB};
+        const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
+        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+        SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
+        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+      }
       ctx->kernel_launches += 2;
     } else {
       void* args[] = {&GA};

@@ -1,0 +1,62 @@
+"""Two-level FP32 sweeps (spatial patches on shared-memory velocities, boundary contacts over
+the grid) on a dense pile large enough to use them.
+
+Bars: the two-level path runs; every step that reports convergence meets the tolerance under
+the oracle's FP64 residual of the GPU's impulses; the reported residual equals the oracle's
+evaluation; positions stay within 5e-3 of the one-level FP32 solve and of FP64 after four
+steps from a common state (both are Gauss-Seidel orders of a solve that hits its iteration cap
+in this still-settling pile, so their iterates differ within the residual they reach).
+"""
+import numpy as np
+import pytest
+
+from scisim_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def pile(gpulib, s, **kw):
+    cfg = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, max_iters=2000,
+               cache_mode=gpulib.CACHE_NORMAL_AND_FRICTION)
+    cfg.update(kw)
+    ctx = gpulib.Context(**cfg)
+    ctx.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    return ctx
+
+
+def test_two_level_sweeps(gpulib, oracle):
+    n = 32768
+    s = scenes.dense_pile(n=n, seed=2, width=20.0, height=15.0)
+    # Form the pile once (capped solves), then start all three solvers from that state.
+    pre = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE, max_iters=50)
+    pre.step(420)
+    q, v = pre.state()
+    s = dict(s, q=q, v=v)
+    two = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE)
+    one = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE)
+    one.set_two_level(False)
+    f64 = pile(gpulib, s)
+    two.profile_enable(True)
+    two.profile_read(reset=True)
+    checked = 0
+    for _ in range(4):
+        q0, v0 = two.state()
+        st = two.step(1)
+        g = two.last_contacts()
+        assert st["n_contacts"] >= 20000
+        nb = s["r"].shape[0]
+        bases = np.concatenate([g["n"], np.stack([-g["n"][:, 1], g["n"][:, 0]], 1)], 1).reshape(-1)
+        ib = np.where(g["ib"] >= 0, g["ib"], -1)
+        res = oracle.residual_2d(s["m"], v0, g["ia"], ib, bases, s["CoR"], s["mu"], g["alpha"], g["beta"])
+        assert abs(res - st["error"]) <= 1e-12 + 1e-6 * st["error"]
+        if st["succeeded"]:
+            assert res <= 1e-6 * 1.001
+            checked += 1
+        one.step(1)
+        f64.step(1)
+    prof = two.profile_read()
+    assert prof["two_level_solves"] == 4
+    qa, _ = two.state()
+    qb, _ = one.state()
+    qc, _ = f64.state()
+    assert np.abs(qa - qb).max() <= 5e-3 and np.abs(qa - qc).max() <= 5e-3
