@@ -268,16 +268,40 @@ typedef struct {
   uint64_t contact_lifts;    /* contacts lifted FP32 -> FP64 before a residual evaluation */
   uint64_t body_lifts;       /* body velocities re-gathered in FP64 for those evaluations */
   uint64_t two_level_solves; /* FP32 solves that ran the two-level (patch) sweeps */
+  /* Two-level sweeps as the first block sees them (summed over those solves): time in the
+   * patch-interior colours, waiting at the grid barrier after them, and in the contacts
+   * between patches; the contacts between patches and the colours of those swept over the
+   * grid, summed per solve. */
+  double patch_interior_ms;
+  double patch_wait_ms;
+  double patch_boundary_ms;
+  uint64_t boundary_contacts;
+  uint64_t boundary_colors;
+  double patch_interior_max_ms; /* the slowest block's patch-interior time, summed over solves */
+  int64_t patch_slowest_block;  /* that block (= its patch) in the last two-level solve */
+  uint64_t patch_contacts_staged; /* per-patch contact capacity staged in shared memory, summed */
 } sg_profile;
 
 SG_API int sg_profile_enable(sg_ctx* ctx, int32_t on);
 SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
 
 /* Two-level FP32 sweeps for large single-scene steps (default on): contacts inside a spatial
- * patch (one per SM) are swept on shared-memory velocities with block barriers, the contacts
- * between patches over the grid -- a Gauss-Seidel order of the same kind as the colour order,
- * with fewer grid barriers.  0 keeps the one-level colour sweeps. */
+ * patch (one per SM) are swept on shared-memory velocities with block barriers, then the
+ * contacts between patches that lie inside one tile of the patch tiling shifted by half a
+ * tile, the same way; the few left over are swept over the grid.  A Gauss-Seidel order of
+ * the same kind as the colour order, with three grid barriers a sweep instead of one per
+ * colour.  0 keeps the one-level colour sweeps. */
 SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
+
+/* Layout of the last solve's two-level sweeps (diagnostics and tests).  counts[0] = patches P,
+ * counts[1] = shifted tiles Pb (the patch tiling shifted by half a tile).  Per contact, in the
+ * order of sg_last_contacts: its group (g < P: inside patch g; P <= g < P + Pb: between patches,
+ * both bodies in shifted tile g - P; g = P + Pb: the rest, swept over the grid) and the colour
+ * it is swept in.  Per body: its patch, its shifted tile and its band flag (1 for an endpoint of
+ * a contact between patches).  SG_BAD_INPUT unless the last solve ran the two-level sweeps on
+ * nc contacts of the scene's nb bodies. */
+SG_API int sg_last_patch_layout(sg_ctx* ctx, int64_t nc, int64_t nb, int32_t* counts, int32_t* group,
+                                int32_t* color, int32_t* body_patch, int32_t* body_tile, int32_t* body_band);
 
 /* The context's CUDA stream (cudaStream_t) for stream-ordered timing by the caller. */
 SG_API int sg_ctx_stream(sg_ctx* ctx, void** stream);

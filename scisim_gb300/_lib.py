@@ -45,7 +45,10 @@ class SgProfile(C.Structure):
     _fields_ = [("gs_ms", C.c_double), ("gs_launches", C.c_uint64), ("contact_sweeps", C.c_uint64),
                 ("contact_evals", C.c_uint64), ("kernel_launches", C.c_uint64), ("steps", C.c_uint64),
                 ("contacts", C.c_uint64), ("contact_sweeps32", C.c_uint64), ("contact_lifts", C.c_uint64),
-                ("body_lifts", C.c_uint64), ("two_level_solves", C.c_uint64)]
+                ("body_lifts", C.c_uint64), ("two_level_solves", C.c_uint64), ("patch_interior_ms", C.c_double),
+                ("patch_wait_ms", C.c_double), ("patch_boundary_ms", C.c_double), ("boundary_contacts", C.c_uint64),
+                ("boundary_colors", C.c_uint64), ("patch_interior_max_ms", C.c_double),
+                ("patch_slowest_block", C.c_int64), ("patch_contacts_staged", C.c_uint64)]
 
 
 class SgError(RuntimeError):
@@ -96,6 +99,7 @@ SIGNATURES = {
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "sg_set_two_level": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_last_patch_layout": (C.c_int, [C.c_void_p, _i64, _i64, _ip, _ip, _ip, _ip, _ip, _ip]),
     "sg_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sg_set_spin_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sg_selftest_wait_timeout": (C.c_int, [C.c_void_p]),
@@ -387,6 +391,20 @@ class Context:
 
     def set_two_level(self, on=True):
         check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
+
+    def patch_layout(self, nc, nb):
+        """Layout of the last two-level solve: patches P, shifted tiles Pb, each contact's group
+        and colour, each body's patch, shifted tile and band flag."""
+        counts = np.zeros(2, np.int32)
+        group = np.zeros(nc, np.int32)
+        color = np.zeros(nc, np.int32)
+        bp = np.zeros(nb, np.int32)
+        bt = np.zeros(nb, np.int32)
+        band = np.zeros(nb, np.int32)
+        check(lib().sg_last_patch_layout(self._h, nc, nb, iptr(counts), iptr(group), iptr(color), iptr(bp),
+                                         iptr(bt), iptr(band)), "sg_last_patch_layout")
+        return {"P": int(counts[0]), "Pb": int(counts[1]), "group": group, "color": color, "body_patch": bp,
+                "body_tile": bt, "body_band": band}
 
     def stream_ptr(self):
         s = C.c_void_p()

@@ -201,7 +201,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32, &ctx->pk3, &ctx->Iinv32, &ctx->pt_setup,
                   &ctx->pt_patch, &ctx->pt_lidx, &ctx->pt_body, &ctx->pt_cnt, &ctx->pt_start, &ctx->pt_fill,
                   &ctx->pt_key, &ctx->pt_kcnt, &ctx->pt_kstart, &ctx->pt_kfill, &ctx->pt_order, &ctx->pt_max,
-                  &ctx->pt_bcolor, &ctx->pt_rem};
+                  &ctx->pt_bcolor, &ctx->pt_rem, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
+                  &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill};
   for (Buf* b : bufs3) release(*b);
   Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
                   &ctx->mlp_choice};
@@ -944,6 +945,33 @@ int sg_ccd_2d(sg_ctx* ctx, int32_t n, const double* q0a, const double* q1a, cons
   return rc;
 }
 
+int sg_last_patch_layout(sg_ctx* ctx, int64_t nc, int64_t nb, int32_t* counts, int32_t* group, int32_t* color,
+                         int32_t* body_patch, int32_t* body_tile, int32_t* body_band) {
+  if (!ctx || !counts || !group || !color || !body_patch || !body_tile || !body_band) return SG_BAD_INPUT;
+  if (!ctx->last_patched || nc != ctx->last_nc || nb != (int64_t)ctx->nb) {
+    set_error("sg_last_patch_layout: the last solve did not run the two-level sweeps on this many contacts/bodies");
+    return SG_BAD_INPUT;
+  }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const size_t c = (size_t)nc, b = (size_t)nb;
+  std::vector<int32_t> key(c);
+  if (c) SG_CUDA_TRY(cudaMemcpyAsync(key.data(), ctx->pt_key.p, sizeof(int32_t) * c, cudaMemcpyDeviceToHost, s));
+  if (b) {
+    SG_CUDA_TRY(cudaMemcpyAsync(body_patch, ctx->pt_patch.p, sizeof(int32_t) * b, cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(body_tile, ctx->pt_qpatch.p, sizeof(int32_t) * b, cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaMemcpyAsync(body_band, ctx->pt_band.p, sizeof(int32_t) * b, cudaMemcpyDeviceToHost, s));
+  }
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  for (size_t k = 0; k < c; ++k) {
+    group[k] = key[k] / kMaxColors;
+    color[k] = key[k] % kMaxColors;
+  }
+  counts[0] = ctx->last_patch_P;
+  counts[1] = ctx->last_patch_Pb;
+  return SG_OK;
+}
+
 int sg_set_two_level(sg_ctx* ctx, int32_t on) {
   if (!ctx) return SG_BAD_INPUT;
   ctx->patches = on != 0;
@@ -980,8 +1008,20 @@ int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset) {
   out->contact_lifts = ctx->contact_lifts;
   out->body_lifts = ctx->body_lifts;
   out->two_level_solves = ctx->patched_solves;
+  out->patch_interior_ms = 1e-6 * (double)ctx->patch_phase_ns[0];
+  out->patch_wait_ms = 1e-6 * (double)ctx->patch_phase_ns[1];
+  out->patch_boundary_ms = 1e-6 * (double)ctx->patch_phase_ns[2];
+  out->boundary_contacts = ctx->patch_boundary_contacts;
+  out->boundary_colors = ctx->patch_boundary_colors;
+  out->patch_interior_max_ms = 1e-6 * (double)ctx->patch_interior_max_ns;
+  out->patch_slowest_block = ctx->patch_slowest_block;
+  out->patch_contacts_staged = ctx->patch_staged;
   if (reset) {
     ctx->patched_solves = 0;
+    ctx->patch_phase_ns[0] = ctx->patch_phase_ns[1] = ctx->patch_phase_ns[2] = 0;
+    ctx->patch_boundary_contacts = ctx->patch_boundary_colors = 0;
+    ctx->patch_interior_max_ns = 0;
+    ctx->patch_staged = 0;
     ctx->gs_ms = 0.0;
     ctx->gs_launches = ctx->contact_sweeps = ctx->contact_evals = ctx->kernel_launches = 0;
     ctx->steps = ctx->contacts_total = 0;

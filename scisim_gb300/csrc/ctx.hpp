@@ -41,6 +41,13 @@ struct SolveStats {
   unsigned int lifts;     // FP32 -> FP64 lifts (impulses + body velocity gather)
   unsigned long long mag_slot[3];  // ordered max of the FP32 rounding-floor excess per evaluation
   int ig_max[4];                   // highest colour after each iterated-greedy pass
+  // Two-level sweeps, as block 0 sees them: time in the patch-interior colours, waiting at
+  // the barrier after them, and in the contacts between patches (ns); the contacts between
+  // patches and the colours of those swept over the grid.
+  unsigned long long phase_ns[3];
+  unsigned long long interior_max;  // slowest block's patch-interior time: (ns << 8) | block
+  int boundary_contacts;
+  int boundary_colors;
 };
 
 // A growable device buffer.
@@ -146,8 +153,19 @@ struct sg_ctx {
   // index, bodies by patch, contact keys (patch, colour) and the packed order.
   bool patches = true;
   uint64_t patched_solves = 0;
+  bool last_patched = false;  // the last FP32 solve ran the two-level sweeps
+  int last_patch_P = 0, last_patch_Pb = 0;
+  uint64_t patch_phase_ns[3] = {0, 0, 0};
+  uint64_t patch_interior_max_ns = 0;
+  uint64_t patch_staged = 0;  // patch contacts staged in shared memory per launch, summed
+  int patch_slowest_block = -1;
+  uint64_t patch_boundary_contacts = 0;
+  uint64_t patch_boundary_colors = 0;
   sg::Buf pt_setup, pt_patch, pt_lidx, pt_body, pt_cnt, pt_start, pt_fill, pt_key, pt_kcnt, pt_kstart, pt_kfill,
       pt_order, pt_max, pt_bcolor, pt_rem;
+  // Shifted tiles and band bodies: tile of each body, band flag, tile-local slot, band bodies by
+  // tile; band bodies per patch and the scatter's fill counters.
+  sg::Buf pt_qpatch, pt_band, pt_lidxq, pt_qbody, pt_bcnt, pt_nfill, pt_qcnt, pt_qstart, pt_qfill;
   // Batched Ball2D scenes (sg_batch2d_upload).  Scene s owns bodies [sb_off[s], sb_off[s+1]),
   // planes [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]); its contacts of a
   // step are [sc_off[s], sc_off[s+1]).  Counts live on the device (b_ctl: contact count,

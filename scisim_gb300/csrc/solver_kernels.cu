@@ -27,6 +27,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (fewer barrier arrivals)
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
+constexpr int kPatchBlock = 1024;  // two-level kernel
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------------------
@@ -1090,53 +1091,96 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
 // order of k_gs_mixed, with about one grid barrier per boundary colour instead of one per colour.
 constexpr int kPatchBodyCap = 16384;  // bodies of one patch in shared memory (12 B each)
 
+// Patches: T0 x T1 tiles of broad-phase grid cells (one block each), and the same tiling shifted
+// by half a tile, (T0 + 1) x (T1 + 1) tiles whose centres are the patch corners.
 struct PatchSetup {
-  int T0, T1, P, d0, d1;
+  int T0, T1, P, d0, d1, Pb;
 };
 
+// Contact groups (the "patch" of a contact's key): g < P, the interior of patch g; P <= g < P + Pb,
+// a contact between patches whose bodies share shifted tile g - P; g = P + Pb, the rest.
 struct PatchArgs {
   const PatchSetup* ps;
   const int* pstart;  // P + 1 body offsets
-  const int* pbody;   // bodies in patch order
-  const int* goff;    // (P + 1) * kMaxColors + 1 contact offsets: patch-major, then boundary
+  const int* pbody;   // bodies in patch order, each patch's band bodies first
+  const int* pband;   // band bodies (endpoints of contacts between patches) per patch
+  const int* qstart;  // Pb + 1 offsets of the shifted tiles' band bodies
+  const int* qbody;
+  const int* goff;    // (P + Pb + 1) * kMaxColors + 1 contact offsets by (group, colour)
   const int* order;   // packed index -> contact
-  int cap;            // shared-memory body capacity of the launch
+  int cap;            // shared-memory body slots for a patch
+  int capq;           // and for a shifted tile
+  int stage_p;        // contacts of a patch staged in shared memory (its first ones, by colour)
+  int stage_q;        // and of a shifted tile
 };
 
-// Tiles of grid cells, roughly square, at most max_patches of them.
+// T0 x T1 with (T0 + 1)(T1 + 1) <= max_patches, the largest T0 T1 weighted towards square
+// tiles (cells are square).
 __global__ void k_patch_setup(const GridParams* __restrict__ gp, int max_patches, PatchSetup* ps) {
   const int d0 = gp->dims[0], d1 = gp->dims[1];
-  int T0 = (int)sqrt((double)max_patches * (double)d0 / (double)d1);
-  T0 = max(1, min(min(d0, max_patches), T0));
-  const int T1 = max(1, min(d1, max_patches / T0));
-  ps->T0 = T0;
-  ps->T1 = T1;
-  ps->P = T0 * T1;
+  int bT0 = 1, bT1 = 1;
+  double best = -1.0;
+  for (int T0 = 1; T0 <= d0 && 2 * (T0 + 1) <= max_patches; ++T0) {
+    const int T1 = min(d1, max_patches / (T0 + 1) - 1);
+    if (T1 < 1) break;
+    const double a = ((double)d0 * T1) / ((double)d1 * T0);
+    const double score = (double)T0 * T1 * sqrt(a < 1.0 ? a : 1.0 / a);
+    if (score > best) {
+      best = score;
+      bT0 = T0;
+      bT1 = T1;
+    }
+  }
+  ps->T0 = bT0;
+  ps->T1 = bT1;
+  ps->P = bT0 * bT1;
+  ps->Pb = (bT0 + 1) * (bT1 + 1);
   ps->d0 = d0;
   ps->d1 = d1;
 }
 
 __global__ void k_patch_of_body(int nb, const int* __restrict__ cell_of, const PatchSetup* __restrict__ ps,
-                                int* __restrict__ patch, int* __restrict__ pcount) {
+                                int* __restrict__ patch, int* __restrict__ qpatch, int* __restrict__ pcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
-  const int d0 = ps->d0, d1 = ps->d1;
+  const long d0 = ps->d0, d1 = ps->d1, T0 = ps->T0, T1 = ps->T1;
   const int cell = cell_of[i];
-  const int cx = cell % d0, cy = cell / d0;
-  const int tx = (int)((long)cx * ps->T0 / d0), ty = (int)((long)cy * ps->T1 / d1);
-  const int p = tx + ps->T0 * ty;
+  const long cx = cell % d0, cy = cell / d0;
+  const int p = (int)(cx * T0 / d0 + T0 * (cy * T1 / d1));
+  // Shifted tile: floor(cx T0 / d0 + 1/2), in [0, T0].
+  const int q = (int)((2 * cx * T0 + d0) / (2 * d0) + (T0 + 1) * ((2 * cy * T1 + d1) / (2 * d1)));
   patch[i] = p;
+  qpatch[i] = q;
   atomicAdd(&pcount[p], 1);
 }
 
-__global__ void k_patch_scatter(int nb, const int* __restrict__ patch, const int* __restrict__ pstart,
-                                int* __restrict__ pfill, int* __restrict__ pbody, int* __restrict__ lidx) {
+__global__ void k_band_count(int nb, const int* __restrict__ band, const int* __restrict__ patch,
+                             const int* __restrict__ qpatch, int* __restrict__ bcount, int* __restrict__ qcount) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb || !band[i]) return;
+  atomicAdd(&bcount[patch[i]], 1);
+  atomicAdd(&qcount[qpatch[i]], 1);
+}
+
+// Bodies by patch, band bodies first; band bodies also by shifted tile.  Patch-local slots.
+__global__ void k_patch_scatter(int nb, const int* __restrict__ patch, const int* __restrict__ qpatch,
+                                const int* __restrict__ band, const int* __restrict__ pstart,
+                                const int* __restrict__ bcount, int* __restrict__ bfill, int* __restrict__ nfill,
+                                int* __restrict__ pbody, int* __restrict__ lidx, const int* __restrict__ qstart,
+                                int* __restrict__ qfill, int* __restrict__ qbody, int* __restrict__ lidxq) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
   const int p = patch[i];
-  const int j = atomicAdd(&pfill[p], 1);
+  const bool bd = band[i] != 0;
+  const int j = bd ? atomicAdd(&bfill[p], 1) : bcount[p] + atomicAdd(&nfill[p], 1);
   pbody[pstart[p] + j] = i;
   lidx[i] = j;
+  if (bd) {
+    const int q = qpatch[i];
+    const int jq = atomicAdd(&qfill[q], 1);
+    qbody[qstart[q] + jq] = i;
+    lidxq[i] = jq;
+  }
 }
 
 __global__ void k_patch_max(int n, const int* __restrict__ pcount, int* __restrict__ out) {
@@ -1146,23 +1190,30 @@ __global__ void k_patch_max(int n, const int* __restrict__ pcount, int* __restri
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-// Patch of each contact (its patch if interior, P if boundary); boundary contacts get their
-// own colouring below.
+// Group of each contact (PatchArgs); the endpoints of contacts between patches are band bodies.
+// Contacts of groups >= P get their own colouring below.
 __global__ void k_contact_side(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
-                               const int* __restrict__ patch, const PatchSetup* __restrict__ ps,
-                               int* __restrict__ cpatch, int* __restrict__ bcolor) {
+                               const int* __restrict__ patch, const int* __restrict__ qpatch,
+                               const PatchSetup* __restrict__ ps, int* __restrict__ cpatch, int* __restrict__ bcolor,
+                               int* __restrict__ band) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nc) return;
   const int a = ia[k], b = ib[k];
   const int pa = patch[a];
-  const bool interior = b < 0 || patch[b] == pa;
-  cpatch[k] = interior ? pa : ps->P;
   bcolor[k] = -1;
+  if (b < 0 || patch[b] == pa) {
+    cpatch[k] = pa;
+    return;
+  }
+  band[a] = 1;
+  band[b] = 1;
+  const int qa = qpatch[a];
+  cpatch[k] = qpatch[b] == qa ? ps->P + qa : ps->P + ps->Pb;
 }
 
-// Jones-Plassmann colouring of the boundary contacts alone (interior contacts neither take
-// nor block colours): the boundary subgraph is a set of thin bands, so it needs far fewer
-// colours than the whole contact graph.
+// Jones-Plassmann colouring of the contacts between patches, each group (shifted tile, or the
+// remainder) on its own: contacts of other groups neither take nor block colours.  These
+// subgraphs are short bands, so they need far fewer colours than the whole contact graph.
 struct BColorArgs {
   int nc;
   const int* ia;
@@ -1191,7 +1242,8 @@ __global__ void k_color_boundary(BColorArgs A) {
     }
     int rem = 0;
     for (int k = tid; k < A.nc; k += nthr) {
-      if (A.cpatch[k] != P || vcolor[k] >= 0) continue;
+      const int gk = A.cpatch[k];
+      if (gk < P || vcolor[k] >= 0) continue;
       const unsigned pk = hash_prio((unsigned)k);
       unsigned long long used = 0ull;
       bool is_max = true;
@@ -1202,7 +1254,7 @@ __global__ void k_color_boundary(BColorArgs A) {
         const int e = A.body_off[body + 1];
         for (int p = A.body_off[body]; p < e; ++p) {
           const int j = A.body_adj[p];
-          if (j == k || A.cpatch[j] != P) continue;
+          if (j == k || A.cpatch[j] != gk) continue;
           const int cj = vcolor[j];
           if (cj >= 0 && (cj >> 8) < round) {
             used |= 1ull << (cj & 63);
@@ -1235,16 +1287,98 @@ __global__ void k_color_boundary(BColorArgs A) {
   }
 }
 
-__global__ void k_contact_key(int nc, const int* __restrict__ color, const int* __restrict__ bcolor,
-                              const int* __restrict__ cpatch, const PatchSetup* __restrict__ ps, int* __restrict__ key,
-                              int* __restrict__ kcount) {
+// Colour of each contact within its group: the global colour inside a patch, the group's own
+// colouring between patches (in place over the latter); the highest colour into *maxc.
+__global__ void k_group_color_init(int nc, const int* __restrict__ color, const int* __restrict__ cpatch,
+                                   const PatchSetup* __restrict__ ps, int* __restrict__ gcolor, int* __restrict__ maxc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int c = 0;
+  if (k < nc) {
+    c = (cpatch[k] >= ps->P ? gcolor[k] : color[k]) & (kMaxColors - 1);
+    gcolor[k] = c;
+  }
+  for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_down_sync(0xffffffffu, c, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxc, c);
+}
+
+struct RecolorArgs {
+  int nc;
+  const int* ia;
+  const int* ib;
+  const int* body_off;
+  const int* body_adj;
+  const int* cpatch;
+  int* gcolor;
+  const int* maxc;
+  int* status;
+  GridBarrier* gb;
+  unsigned long long spin;
+};
+
+// Each group's colouring compacted on its own (the group's contacts are swept by one block or
+// one grid, so its colour count, not the global one, sets its barriers): colour classes from
+// the highest down, every contact of the class moves to the lowest colour that its neighbours
+// in the group leave free.  Two contacts of one class share no body, so a class moves at once
+// and the colouring stays proper.
+__global__ void k_recolor_groups(RecolorArgs A) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  const int top = *((volatile const int*)A.maxc);
+  for (int col = top; col >= 1; --col) {
+    for (int k = tid; k < A.nc; k += nthr) {
+      if (__ldcg(&A.gcolor[k]) != col) continue;
+      const int g = A.cpatch[k];
+      unsigned long long used = 0ull;
+      const int bodies[2] = {A.ia[k], A.ib[k]};
+      for (int bi = 0; bi < 2; ++bi) {
+        const int body = bodies[bi];
+        if (body < 0) continue;
+        const int e = A.body_off[body + 1];
+        for (int p = A.body_off[body]; p < e; ++p) {
+          const int j = A.body_adj[p];
+          if (j != k && A.cpatch[j] == g) used |= 1ull << (__ldcg(&A.gcolor[j]) & (kMaxColors - 1));
+        }
+      }
+      const int lowest = __ffsll((long long)~used) - 1;
+      if (lowest >= 0 && lowest < col) A.gcolor[k] = lowest;
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(A.status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+  }
+}
+
+__global__ void k_contact_key(int nc, const int* __restrict__ gcolor, const int* __restrict__ cpatch,
+                              int* __restrict__ key, int* __restrict__ kcount) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nc) return;
   const int cp = cpatch[k];
-  const int c = (cp == ps->P ? bcolor[k] : color[k]) & (kMaxColors - 1);
+  const int c = gcolor[k] & (kMaxColors - 1);
   const int kk = cp * kMaxColors + c;
   key[k] = kk;
   atomicAdd(&kcount[kk], 1);
+}
+
+// Largest contact count of a patch (out[0]) and of a shifted tile (out[1]).
+__global__ void k_group_max(const PatchSetup* __restrict__ ps, const int* __restrict__ kstart, int* __restrict__ out) {
+  const int P = ps->P, Pb = ps->Pb;
+  int mp = 0, mq = 0;
+  for (int g = threadIdx.x; g < P + Pb; g += blockDim.x) {
+    const int n = kstart[(g + 1) * kMaxColors] - kstart[g * kMaxColors];
+    if (g < P)
+      mp = max(mp, n);
+    else
+      mq = max(mq, n);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mp = max(mp, __shfl_down_sync(0xffffffffu, mp, o));
+    mq = max(mq, __shfl_down_sync(0xffffffffu, mq, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], mp);
+    atomicMax(&out[1], mq);
+  }
 }
 
 __global__ void k_contact_scatter(int nc, const int* __restrict__ key, const int* __restrict__ kstart,
@@ -1255,10 +1389,11 @@ __global__ void k_contact_scatter(int nc, const int* __restrict__ key, const int
   order[kstart[kk] + atomicAdd(&kfill[kk], 1)] = k;
 }
 
-// Packs in patch order; interior contacts carry patch-local body indices.
+// Packs in (group, colour) order; contacts of a patch carry patch-local body slots, those of a
+// shifted tile tile-local slots, the rest global body indices.
 __global__ void k_pack32_patch(int nc, const int* __restrict__ order, const int* __restrict__ key,
                                const PatchSetup* __restrict__ ps, const int* __restrict__ ia,
-                               const int* __restrict__ ib, const int* __restrict__ lidx,
+                               const int* __restrict__ ib, const int* __restrict__ lidx, const int* __restrict__ lidxq,
                                const double2* __restrict__ n, const double2* __restrict__ c,
                                const double* __restrict__ W, const double* __restrict__ mu,
                                const double2* __restrict__ r, int2* __restrict__ ab, float2* __restrict__ n32,
@@ -1267,9 +1402,11 @@ __global__ void k_pack32_patch(int nc, const int* __restrict__ order, const int*
   if (s >= nc) return;
   const int k = order[s];
   const int a = ia[k], b = ib[k];
-  const bool interior = key[k] < ps->P * kMaxColors;
-  if (interior)
+  const int g = key[k] / kMaxColors;
+  if (g < ps->P)
     ab[s] = make_int2(lidx[a], b >= 0 ? lidx[b] : -1);
+  else if (g < ps->P + ps->Pb)
+    ab[s] = make_int2(lidxq[a], lidxq[b]);
   else
     ab[s] = make_int2(a, b >= 0 ? b : -1);
   const double2 nk = n[k], ck = c[k], rk = r[k];
@@ -1277,6 +1414,12 @@ __global__ void k_pack32_patch(int nc, const int* __restrict__ order, const int*
   c32[s] = make_float2((float)ck.x, (float)ck.y);
   w32[s] = make_float4((float)W[3 * k], (float)W[3 * k + 1], (float)W[3 * k + 2], (float)mu[k]);
   r32[s] = make_float2((float)rk.x, (float)rk.y);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
 // gs_update32 on the patch's shared-memory velocities (ab holds patch-local indices).
@@ -1295,7 +1438,8 @@ __device__ __forceinline__ void gs_update32_local(const Gs32Args& B, int s, floa
     ht -= tx * vb.x + ty * vb.y;
   }
   const float u0 = hn + ck.x, u1 = ht + ck.y;
-  const float2 rk = __ldcg(&B.r[s]);
+  // Read through L1: only this thread writes this impulse while the sweeps run.
+  const float2 rk = B.r[s];
   const float bt0 = u0 - (w.x * rk.x + w.y * rk.y);
   const float bt1 = u1 - (w.y * rk.x + w.z * rk.y);
   float rn0, rn1;
@@ -1311,7 +1455,68 @@ __device__ __forceinline__ void gs_update32_local(const Gs32Args& B, int s, floa
   B.r[s] = make_float2(rn0, rn1);
 }
 
-__global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B, PatchArgs Q) {
+// A contact staged in shared memory: both body slots in one word (16 bits each, 0xffff for a
+// static plane), normal, forcing and friction coefficient; the impulse kept there too (and
+// stored to global memory for the FP64 checks).  The Delassus block of a disc contact is
+// (1/m_a + 1/m_b) I (n and t = (-n_y, n_x) are orthonormal, so n.t is exactly 0 and
+// n.n = t.t = 1 to rounding), so it is formed from the slots' inverse masses.
+struct Staged {
+  unsigned* ab;
+  float2* n;
+  float2* c;
+  float* mu;
+  float2* r;
+};
+
+__device__ __forceinline__ void stage_contact(const Gs32Args& B, const Staged& S, int i, int s) {
+  const int2 ab = B.ab[s];
+  S.ab[i] = (unsigned)ab.x | ((ab.y >= 0 ? (unsigned)ab.y : 0xffffu) << 16);
+  S.n[i] = B.n[s];
+  S.c[i] = B.c[s];
+  S.mu[i] = B.w[s].w;
+  S.r[i] = B.r[s];
+}
+
+__device__ __forceinline__ void gs_update32_staged(const Gs32Args& B, const Staged& S, int i, int s, float2* sv,
+                                                   const float* sm) {
+  const unsigned ab = S.ab[i];
+  const int a = (int)(ab & 0xffffu), b = (int)(ab >> 16);
+  const bool has_b = b != 0xffff;
+  const float2 nk = S.n[i], ck = S.c[i];
+  const float2 va = sv[a];
+  const float2 vb = has_b ? sv[b] : make_float2(0.0f, 0.0f);
+  const float ma = sm[a], mb = has_b ? sm[b] : 0.0f;
+  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  float hn = nx * va.x + ny * va.y;
+  float ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn -= nx * vb.x + ny * vb.y;
+    ht -= tx * vb.x + ty * vb.y;
+  }
+  const float u0 = hn + ck.x, u1 = ht + ck.y;
+  const float2 rk = S.r[i];
+  const float wd = ma + mb;
+  const float bt0 = u0 - wd * rk.x;
+  const float bt1 = u1 - wd * rk.y;
+  float rn0, rn1;
+  local_solve_2d_f(wd, 0.0f, wd, bt0, bt1, S.mu[i], rn0, rn1);
+  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
+  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
+  sv[a] = make_float2(va.x + ma * px, va.y + ma * py);
+  if (has_b) sv[b] = make_float2(vb.x - mb * px, vb.y - mb * py);
+  const float2 rn = make_float2(rn0, rn1);
+  S.r[i] = rn;
+  B.r[s] = rn;
+}
+
+// Highest non-empty colour + 1 of a group's offsets.
+__device__ __forceinline__ int group_colors(const int* off) {
+  int n = kMaxColors;
+  while (n > 0 && off[n] == off[n - 1]) --n;
+  return n;
+}
+
+__global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args B, PatchArgs Q) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   if (*((volatile int*)&A.st->status) != 0) return;
@@ -1321,22 +1526,51 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
   for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
   __syncthreads();
   const int ncol = s_ncol;
-  // This block's patch: its bodies and its interior contacts by colour; the boundary
-  // contacts by colour, with a tail of small colours as in k_gs_mixed.
+  // This block's patch (its bodies, band bodies first, and its interior contacts by colour)
+  // and its shifted tile (band bodies, contacts by colour), both swept on shared-memory
+  // velocities; the remaining contacts by colour over the grid, with a tail of small colours
+  // as in k_gs_mixed.  Slots: patch velocities, patch 1/m, tile velocities, tile 1/m (cap and
+  // capq even, so every float2 stays 8-byte aligned), then the staged contacts (Staged), the
+  // patch's first stage_p in slots [0, stage_p), the tile's first stage_q after them.
   extern __shared__ float2 sv[];
   float* sm = reinterpret_cast<float*>(sv + Q.cap);
+  float2* svq = reinterpret_cast<float2*>(sm + Q.cap);
+  float* smq = reinterpret_cast<float*>(svq + Q.capq);
+  const int cs = Q.stage_p + Q.stage_q;
+  Staged S;
+  S.n = reinterpret_cast<float2*>(smq + Q.capq);
+  S.c = S.n + cs;
+  S.r = S.c + cs;
+  S.ab = reinterpret_cast<unsigned*>(S.r + cs);
+  S.mu = reinterpret_cast<float*>(S.ab + cs);
   __shared__ int s_goff[kMaxColors + 1];
+  __shared__ int s_hoff[kMaxColors + 1];
   __shared__ int s_boff[kMaxColors + 1];
-  const int P = Q.ps->P;
-  const int pb0 = blockIdx.x < P ? Q.pstart[blockIdx.x] : 0;
-  const int pb1 = blockIdx.x < P ? Q.pstart[blockIdx.x + 1] : 0;
+  const int P = Q.ps->P, Pb = Q.ps->Pb;
+  const bool has_p = blockIdx.x < P, has_q = blockIdx.x < Pb;
+  const int pb0 = has_p ? Q.pstart[blockIdx.x] : 0;
+  const int pb1 = has_p ? Q.pstart[blockIdx.x + 1] : 0;
+  const int pbe = pb0 + (has_p ? Q.pband[blockIdx.x] : 0);  // band bodies: [pb0, pbe)
+  const int qb0 = has_q ? Q.qstart[blockIdx.x] : 0;
+  const int qb1 = has_q ? Q.qstart[blockIdx.x + 1] : 0;
   for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) {
-    s_goff[c] = blockIdx.x < P ? Q.goff[blockIdx.x * kMaxColors + c] : 0;
-    s_boff[c] = Q.goff[P * kMaxColors + c];
+    s_goff[c] = has_p ? Q.goff[blockIdx.x * kMaxColors + c] : 0;
+    s_hoff[c] = has_q ? Q.goff[(P + blockIdx.x) * kMaxColors + c] : 0;
+    s_boff[c] = Q.goff[(P + Pb) * kMaxColors + c];
   }
   for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) sm[j - pb0] = B.minv[Q.pbody[j]];
+  for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) smq[j - qb0] = B.minv[Q.qbody[j]];
   __syncthreads();
-  int btail = ncol;
+  // Colours of each group (a group's own colouring may use more colours than the whole graph's).
+  const int ncol_p = group_colors(s_goff), ncol_q = group_colors(s_hoff);
+  const int ncol_r = group_colors(s_boff);
+  const int sp0 = s_goff[0], sq0 = s_hoff[0];
+  const int sp_end = sp0 + min(s_goff[ncol_p] - sp0, Q.stage_p);  // staged: [sp0, sp_end)
+  const int sq_end = sq0 + min(s_hoff[ncol_q] - sq0, Q.stage_q);
+  for (int s = sp0 + threadIdx.x; s < sp_end; s += blockDim.x) stage_contact(B, S, s - sp0, s);
+  for (int s = sq0 + threadIdx.x; s < sq_end; s += blockDim.x) stage_contact(B, S, Q.stage_p + s - sq0, s);
+  __syncthreads();
+  int btail = ncol_r;
   while (btail > 0 && s_boff[btail] - s_boff[btail - 1] <= 2 * (int)blockDim.x) --btail;
   const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
   const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
@@ -1346,25 +1580,68 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
   bool converged = false, fp64 = false;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   unsigned next_eval = 1, interval = eval32;
+  // Phase timers of block 0 (shared memory, so that they take no registers from the sweeps):
+  // interior, wait, boundary totals, then the current sweep's marks.
+  __shared__ unsigned long long s_t[6];
+  const bool timer = tid == 0;
+  const bool btimer = threadIdx.x == 0;  // every block: its own patch-interior total in s_t[0]
+  if (btimer) s_t[0] = s_t[1] = s_t[2] = 0ull;
+  // The patch's shared-memory velocities persist between sweeps: only band bodies are
+  // touched outside the patch, so only they are reloaded and written back, except after an
+  // FP64 check, which resets every velocity from the impulses.
+  bool reload_all = true;
   for (it = 1; it <= A.max_iters; ++it) {
     bool do_eval;
     if (!fp64) {
-      // Interior contacts of this block's patch, colour by colour, on shared-memory copies
-      // of the patch's body velocities (block barriers only).
-      for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) sv[j - pb0] = __ldcg(&B.v[Q.pbody[j]]);
+      if (btimer) s_t[3] = globaltimer_ns();
+      // Interior contacts of this block's patch, colour by colour (block barriers only).
+      const int lend = reload_all ? pb1 : pbe;
+      reload_all = false;
+      for (int j = pb0 + threadIdx.x; j < lend; j += blockDim.x) sv[j - pb0] = __ldcg(&B.v[Q.pbody[j]]);
       __syncthreads();
-      for (int col = 0; col < ncol; ++col) {
+      for (int col = 0; col < ncol_p; ++col) {
         const int e = s_goff[col + 1];
-        for (int s = s_goff[col] + threadIdx.x; s < e; s += blockDim.x) gs_update32_local(B, s, sv, sm);
+        for (int s = s_goff[col] + threadIdx.x; s < e; s += blockDim.x) {
+          if (s < sp_end)
+            gs_update32_staged(B, S, s - sp0, s, sv, sm);
+          else
+            gs_update32_local(B, s, sv, sm);
+        }
         __syncthreads();
       }
-      for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) B.v[Q.pbody[j]] = sv[j - pb0];
+      for (int j = pb0 + threadIdx.x; j < pbe; j += blockDim.x) B.v[Q.pbody[j]] = sv[j - pb0];
+      if (btimer) {
+        s_t[4] = globaltimer_ns();
+        s_t[0] += s_t[4] - s_t[3];
+      }
       if (!grid_sync(A.gb, A.spin)) {
         if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
         return;
       }
-      // Contacts between patches, colour by colour over the grid; the small trailing colours
-      // run in block 0 alone.
+      if (timer) s_t[5] = globaltimer_ns();
+      // Contacts between patches within this block's shifted tile, colour by colour on the
+      // tile's shared-memory velocities (block barriers only).
+      if (qb1 > qb0) {
+        for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) svq[j - qb0] = __ldcg(&B.v[Q.qbody[j]]);
+        __syncthreads();
+        for (int col = 0; col < ncol_q; ++col) {
+          const int e = s_hoff[col + 1];
+          for (int s = s_hoff[col] + threadIdx.x; s < e; s += blockDim.x) {
+            if (s < sq_end)
+              gs_update32_staged(B, S, Q.stage_p + s - sq0, s, svq, smq);
+            else
+              gs_update32_local(B, s, svq, smq);
+          }
+          __syncthreads();
+        }
+        for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) B.v[Q.qbody[j]] = svq[j - qb0];
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      // The remaining contacts (across patches and shifted tiles), colour by colour over the
+      // grid; the small trailing colours run in block 0 alone.
       for (int col = 0; col < btail; ++col) {
         const int b0 = s_boff[col], e = s_boff[col + 1];
         if (b0 == e) continue;
@@ -1374,9 +1651,9 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
           return;
         }
       }
-      if (btail < ncol && s_boff[btail] < s_boff[ncol]) {
+      if (btail < ncol_r && s_boff[btail] < s_boff[ncol_r]) {
         if (blockIdx.x == 0) {
-          for (int col = btail; col < ncol; ++col) {
+          for (int col = btail; col < ncol_r; ++col) {
             for (int s = s_boff[col] + threadIdx.x; s < s_boff[col + 1]; s += blockDim.x) gs_update32(B, s);
             __syncthreads();
           }
@@ -1385,6 +1662,11 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
           if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
           return;
         }
+      }
+      if (timer) {
+        const unsigned long long t3 = globaltimer_ns();
+        s_t[1] += s_t[5] - s_t[4];
+        s_t[2] += t3 - s_t[5];
       }
       ++s32;
       // FP64 checks after sweeps 1, 2, 4, ... eval32, then at an interval that grows
@@ -1422,6 +1704,7 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
           B.v[i] = make_float2((float)vi.x, (float)vi.y);
         }
         ++lifts;
+        reload_all = true;
         if (!grid_sync(A.gb, A.spin)) {
           if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
           return;
@@ -1513,6 +1796,7 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
     if (err_best < INFINITY)
       for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
   }
+  if (btimer) atomicMax(&A.st->interior_max, (s_t[0] << 8) | (unsigned long long)blockIdx.x);
   if (tid == 0) {
     A.st->iterations = it;
     A.st->converged = converged ? 1 : 0;
@@ -1521,6 +1805,13 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_patch(GsArgs A, Gs32Args B
     A.st->sweeps64 = s64;
     A.st->evals = n_eval;
     A.st->lifts = lifts;
+    A.st->phase_ns[0] = s_t[0];
+    A.st->phase_ns[1] = s_t[1];
+    A.st->phase_ns[2] = s_t[2];
+    A.st->boundary_contacts = Q.goff[(P + Pb + 1) * kMaxColors] - Q.goff[P * kMaxColors];
+    int nbc = 0;
+    for (int c = 0; c < ncol_r; ++c) nbc += s_boff[c + 1] > s_boff[c];
+    A.st->boundary_colors = nbc;
   }
 }
 
@@ -1853,6 +2144,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
   int* adj = ctx->body_adj.as<int>();
   SolveStats* st = ctx->stats.as<SolveStats>();
   GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  bool patched_run = false;
   const double2* n2 = reinterpret_cast<const double2*>(P.n);
   double2* r2 = reinterpret_cast<double2*>(P.r);
 
@@ -1927,41 +2219,68 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       int pmax = 0;
       const int maxP = ctx->num_sms;
       const bool try_patches = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 && nc >= 20000;
+      int pmaxq = 0, cmax_p = 0, cmax_q = 0;
+      PatchSetup hps{};
       if (try_patches) {
-        const size_t keys = (size_t)(maxP + 1) * kMaxColors + 1;
+        // Groups: at most maxP patches, maxP shifted tiles and the remainder (a degenerate
+        // setup is rejected below before any launch uses it).
+        const int groups = 2 * maxP + 8;
+        const size_t keys = (size_t)groups * kMaxColors + 1;
+        const size_t gsz = sizeof(int) * (size_t)(groups + 1);
         if (int r = grow(ctx->pt_setup, sizeof(PatchSetup))) return r;
         if (int r = grow(ctx->pt_patch, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_qpatch, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_band, sizeof(int) * b)) return r;
         if (int r = grow(ctx->pt_lidx, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_lidxq, sizeof(int) * b)) return r;
         if (int r = grow(ctx->pt_body, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_cnt, sizeof(int) * (size_t)(maxP + 2))) return r;
-        if (int r = grow(ctx->pt_start, sizeof(int) * (size_t)(maxP + 2))) return r;
-        if (int r = grow(ctx->pt_fill, sizeof(int) * (size_t)(maxP + 2))) return r;
+        if (int r = grow(ctx->pt_qbody, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_cnt, gsz)) return r;
+        if (int r = grow(ctx->pt_start, gsz)) return r;
+        if (int r = grow(ctx->pt_fill, gsz)) return r;
+        if (int r = grow(ctx->pt_bcnt, gsz)) return r;
+        if (int r = grow(ctx->pt_nfill, gsz)) return r;
+        if (int r = grow(ctx->pt_qcnt, gsz)) return r;
+        if (int r = grow(ctx->pt_qstart, gsz)) return r;
+        if (int r = grow(ctx->pt_qfill, gsz)) return r;
         if (int r = grow(ctx->pt_key, sizeof(int) * c)) return r;
         if (int r = grow(ctx->pt_kcnt, sizeof(int) * keys)) return r;
         if (int r = grow(ctx->pt_kstart, sizeof(int) * keys)) return r;
         if (int r = grow(ctx->pt_kfill, sizeof(int) * keys)) return r;
         if (int r = grow(ctx->pt_order, sizeof(int) * c)) return r;
-        if (int r = grow(ctx->pt_max, sizeof(int))) return r;
+        if (int r = grow(ctx->pt_max, 5 * sizeof(int))) return r;
         if (int r = grow(ctx->pt_bcolor, sizeof(int) * c)) return r;
         if (int r = grow(ctx->pt_rem, 4 * sizeof(int))) return r;
         PatchSetup* ps = ctx->pt_setup.as<PatchSetup>();
         k_patch_setup<<<1, 1, 0, s>>>(ctx->grid.as<GridParams>(), maxP, ps);
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_cnt.p, 0, sizeof(int) * (size_t)(maxP + 2), s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_fill.p, 0, sizeof(int) * (size_t)(maxP + 2), s));
+        for (Buf* z : {&ctx->pt_cnt, &ctx->pt_fill, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qfill})
+          SG_CUDA_TRY(cudaMemsetAsync(z->p, 0, gsz, s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kcnt.p, 0, sizeof(int) * keys, s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kfill.p, 0, sizeof(int) * keys, s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, sizeof(int), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, 5 * sizeof(int), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_band.p, 0, sizeof(int) * b, s));
         k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, ctx->pt_patch.as<int>(),
-                                                         ctx->pt_cnt.as<int>());
+                                                         ctx->pt_qpatch.as<int>(), ctx->pt_cnt.as<int>());
         SG_CUDA_TRY(cudaGetLastError());
-        if (int r = scan_exclusive(ctx, ctx->pt_cnt.as<int>(), ctx->pt_start.as<int>(), maxP)) return r;
-        k_patch_scatter<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_patch.as<int>(), ctx->pt_start.as<int>(),
-                                                         ctx->pt_fill.as<int>(), ctx->pt_body.as<int>(),
-                                                         ctx->pt_lidx.as<int>());
-        k_patch_max<<<1, kBlock, 0, s>>>(maxP, ctx->pt_cnt.as<int>(), ctx->pt_max.as<int>());
         int* cpatch = ctx->pt_order.as<int>();  // scratch until the order is built
         int* bcolor = ctx->pt_bcolor.as<int>();
-        k_contact_side<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, ctx->pt_patch.as<int>(), ps, cpatch, bcolor);
+        k_contact_side<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, ctx->pt_patch.as<int>(),
+                                                         ctx->pt_qpatch.as<int>(), ps, cpatch, bcolor,
+                                                         ctx->pt_band.as<int>());
+        k_band_count<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_band.as<int>(), ctx->pt_patch.as<int>(),
+                                                       ctx->pt_qpatch.as<int>(), ctx->pt_bcnt.as<int>(),
+                                                       ctx->pt_qcnt.as<int>());
+        SG_CUDA_TRY(cudaGetLastError());
+        if (int r = scan_exclusive(ctx, ctx->pt_cnt.as<int>(), ctx->pt_start.as<int>(), groups)) return r;
+        if (int r = scan_exclusive(ctx, ctx->pt_qcnt.as<int>(), ctx->pt_qstart.as<int>(), groups)) return r;
+        k_patch_scatter<<<blocks_for(nb), kBlock, 0, s>>>(
+            nb, ctx->pt_patch.as<int>(), ctx->pt_qpatch.as<int>(), ctx->pt_band.as<int>(), ctx->pt_start.as<int>(),
+            ctx->pt_bcnt.as<int>(), ctx->pt_fill.as<int>(), ctx->pt_nfill.as<int>(), ctx->pt_body.as<int>(),
+            ctx->pt_lidx.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qfill.as<int>(), ctx->pt_qbody.as<int>(),
+            ctx->pt_lidxq.as<int>());
+        k_patch_max<<<1, kBlock, 0, s>>>(groups, ctx->pt_cnt.as<int>(), ctx->pt_max.as<int>());
+        k_patch_max<<<1, kBlock, 0, s>>>(groups, ctx->pt_qcnt.as<int>(), ctx->pt_max.as<int>() + 1);
+        SG_CUDA_TRY(cudaGetLastError());
         SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_rem.p, 0, 4 * sizeof(int), s));
         {
@@ -1971,22 +2290,52 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
           const int g = coop_grid(ctx, k_color_boundary, nc, kBlock);
           SG_CUDA_TRY(launch_cooperative((const void*)k_color_boundary, g, kBlock, bargs, s));
         }
-        k_contact_key<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->color.as<int>(), bcolor, cpatch, ps,
-                                                       ctx->pt_key.as<int>(), ctx->pt_kcnt.as<int>());
+        k_group_color_init<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->color.as<int>(), cpatch, ps, bcolor,
+                                                            ctx->pt_max.as<int>() + 2);
+        SG_CUDA_TRY(cudaGetLastError());
+        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+        {
+          RecolorArgs RA{nc, P.ia, P.ib, off, adj, cpatch, bcolor, ctx->pt_max.as<int>() + 2, &st->status, gb,
+                         ctx->spin_limit};
+          void* rargs[] = {&RA};
+          const int g = coop_grid(ctx, k_recolor_groups, nc, kBlock);
+          SG_CUDA_TRY(launch_cooperative((const void*)k_recolor_groups, g, kBlock, rargs, s));
+        }
+        k_contact_key<<<blocks_for(nc), kBlock, 0, s>>>(nc, bcolor, cpatch, ctx->pt_key.as<int>(),
+                                                       ctx->pt_kcnt.as<int>());
         SG_CUDA_TRY(cudaGetLastError());
         if (int r = scan_exclusive(ctx, ctx->pt_kcnt.as<int>(), ctx->pt_kstart.as<int>(), (int)(keys - 1))) return r;
         k_contact_scatter<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_key.as<int>(), ctx->pt_kstart.as<int>(),
                                                            ctx->pt_kfill.as<int>(), ctx->pt_order.as<int>());
+        k_group_max<<<1, kBlock, 0, s>>>(ps, ctx->pt_kstart.as<int>(), ctx->pt_max.as<int>() + 3);
         SG_CUDA_TRY(cudaGetLastError());
-        SG_CUDA_TRY(cudaMemcpyAsync(&pmax, ctx->pt_max.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        int hmax[5] = {0, 0, 0, 0, 0};
+        SG_CUDA_TRY(cudaMemcpyAsync(hmax, ctx->pt_max.p, 5 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        SG_CUDA_TRY(cudaMemcpyAsync(&hps, ps, sizeof(PatchSetup), cudaMemcpyDeviceToHost, s));
         SG_CUDA_TRY(cudaStreamSynchronize(s));
-        ctx->kernel_launches += 15;  // setup, of_body, 3 scan, scatter, max, side, colour, key, 3 scan, scatter
+        pmax = hmax[0];
+        pmaxq = hmax[1];
+        cmax_p = hmax[3];
+        cmax_q = hmax[4];
+        // setup, of_body, side, band_count, 2 x 3 scan, scatter, 2 max, colour, colour init,
+        // recolour, key, 3 scan, scatter, group max
+        ctx->kernel_launches += 22;
       }
-      const bool patched = try_patches && pmax > 0 && pmax <= kPatchBodyCap;
+      // Shared-memory slots rounded up to even counts (8-byte alignment of the second block).
+      const int capp = (pmax + 1) & ~1, capq = (pmaxq + 1) & ~1;
+      // Body slots must fit in shared memory beside the kernel's static arrays (12 B each).
+      const bool patched = try_patches && hps.P >= 2 && hps.Pb <= maxP && pmax > 0 &&
+                           capp + capq <= kPatchBodyCap;
+      patched_run = patched;
+      ctx->last_patched = patched;
+      if (patched) {
+        ctx->last_patch_P = hps.P;
+        ctx->last_patch_Pb = hps.Pb;
+      }
       if (patched)
         k_pack32_patch<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_order.as<int>(), ctx->pt_key.as<int>(),
                                                          ctx->pt_setup.as<PatchSetup>(), P.ia, P.ib,
-                                                         ctx->pt_lidx.as<int>(), n2, reinterpret_cast<const double2*>(P.c),
+                                                         ctx->pt_lidx.as<int>(), ctx->pt_lidxq.as<int>(), n2, reinterpret_cast<const double2*>(P.c),
                                                          P.W, P.mu, r2, ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(),
                                                          ctx->pk_c.as<float2>(), ctx->pk_w.as<float4>(),
                                                          ctx->pk_r.as<float2>());
@@ -2012,22 +2361,34 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.nb = nb;
       GB.eval32 = 16;
       if (patched) {
-        PatchArgs Q{ctx->pt_setup.as<PatchSetup>(), ctx->pt_start.as<int>(), ctx->pt_body.as<int>(),
-                    ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), pmax};
-        const size_t smem = (size_t)12 * (size_t)pmax;
-        static bool attr_set = false;
-        if (!attr_set) {
-          SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           12 * kPatchBodyCap));
-          attr_set = true;
+        // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
+        // contacts as fit (the patch's first), 32 B each.
+        static int dyn_budget = -1;
+        if (dyn_budget < 0) {
+          int optin = 0;
+          SG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+          cudaFuncAttributes fa{};
+          SG_CUDA_TRY(cudaFuncGetAttributes(&fa, k_gs_patch));
+          const int budget = optin - (int)fa.sharedSizeBytes;
+          SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch, cudaFuncAttributeMaxDynamicSharedMemorySize, budget));
+          dyn_budget = budget;
         }
+        const int body_bytes = 12 * (capp + capq);
+        const int avail = std::max(0, dyn_budget - body_bytes) / 32;
+        const int stage_p = std::min(cmax_p, avail);
+        const int stage_q = std::min(cmax_q, avail - stage_p);
+        PatchArgs Q{ctx->pt_setup.as<PatchSetup>(), ctx->pt_start.as<int>(), ctx->pt_body.as<int>(),
+                    ctx->pt_bcnt.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qbody.as<int>(),
+                    ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), capp, capq, stage_p, stage_q};
+        const size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q);
+        ctx->patch_staged += (uint64_t)stage_p;
         void* args[] = {&GA, &GB, &Q};
         // The boundary colouring used the barrier: start it afresh for this grid.
         SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(maxP);
-        lc.blockDim = dim3(kGs32Block);
+        lc.blockDim = dim3(kPatchBlock);
         lc.dynamicSmemBytes = smem;
         lc.stream = s;
         cudaLaunchAttribute at[1];
@@ -2076,6 +2437,13 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     ctx->contact_evals += (uint64_t)ctx->h_stats.evals * (uint64_t)nc;
     ctx->contact_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nc;
     ctx->body_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nb;
+    if (patched_run) {
+      for (int q = 0; q < 3; ++q) ctx->patch_phase_ns[q] += ctx->h_stats.phase_ns[q];
+      ctx->patch_interior_max_ns += ctx->h_stats.interior_max >> 8;
+      ctx->patch_slowest_block = (int)(ctx->h_stats.interior_max & 255ull);
+      ctx->patch_boundary_contacts += (uint64_t)ctx->h_stats.boundary_contacts;
+      ctx->patch_boundary_colors += (uint64_t)ctx->h_stats.boundary_colors;
+    }
     if (ctx->profile) {
       float ms = 0.f;
       SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));

@@ -1,5 +1,5 @@
-"""Two-level FP32 sweeps (spatial patches on shared-memory velocities, boundary contacts over
-the grid) on a dense pile large enough to use them.
+"""Two-level FP32 sweeps (spatial patches on shared-memory velocities, contacts between patches
+by shifted tile, the rest over the grid) on a dense pile large enough to use them.
 
 Bars: the two-level path runs; every step that reports convergence meets the tolerance under
 the oracle's FP64 residual of the GPU's impulses; the reported residual equals the oracle's
@@ -60,3 +60,46 @@ def test_two_level_sweeps(gpulib, oracle):
     qb, _ = one.state()
     qc, _ = f64.state()
     assert np.abs(qa - qb).max() <= 5e-3 and np.abs(qa - qc).max() <= 5e-3
+
+
+def test_patch_layout_is_race_free(gpulib):
+    """The partition the two-level sweeps run on, read back after a step and checked on the
+    host: every contact's group holds both its bodies (patch interiors by patch, contacts between
+    patches by shifted tile), band flags mark exactly the bodies that blocks other than their
+    patch's touch, and no body occurs twice among the contacts of one (group, colour), so the
+    contacts a block or the grid updates together never share a body."""
+    n = 32768
+    s = scenes.dense_pile(n=n, seed=2, width=20.0, height=15.0)
+    ctx = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE, max_iters=50)
+    ctx.step(420)
+    st = ctx.step(1)
+    nb, nc = s["r"].shape[0], st["n_contacts"]
+    g = ctx.last_contacts()
+    L = ctx.patch_layout(nc, nb)
+    P, Pb = L["P"], L["Pb"]
+    assert 2 <= P < Pb
+    grp, col = L["group"], L["color"]
+    bp, bt, band = L["body_patch"], L["body_tile"], L["body_band"]
+    ia, ib = g["ia"], g["ib"]
+    has_b = ib >= 0
+    inside = grp < P
+    tile = (grp >= P) & (grp < P + Pb)
+    rest = grp == P + Pb
+    assert np.all(inside | tile | rest)
+    assert np.all(bp[ia[inside]] == grp[inside])
+    m = inside & has_b
+    assert np.all(bp[ib[m]] == grp[m])
+    between = ~inside
+    assert np.all(has_b[between])
+    assert np.all(bp[ia[between]] != bp[ib[between]])
+    assert np.all(bt[ia[tile]] == grp[tile] - P) and np.all(bt[ib[tile]] == grp[tile] - P)
+    assert np.all(bt[ia[rest]] != bt[ib[rest]])
+    expect = np.zeros(nb, np.int32)
+    expect[ia[between]] = 1
+    expect[ib[between]] = 1
+    assert np.array_equal(band, expect)
+    key = grp.astype(np.int64) * 64 + col
+    pairs = np.concatenate([np.stack([key, ia], 1), np.stack([key[has_b], ib[has_b]], 1)])
+    assert np.unique(pairs, axis=0).shape[0] == pairs.shape[0]
+    # Most contacts between patches are swept inside a shifted tile.
+    assert tile.sum() > 0 and rest.sum() < 0.25 * between.sum()
