@@ -202,7 +202,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->pt_patch, &ctx->pt_lidx, &ctx->pt_body, &ctx->pt_cnt, &ctx->pt_start, &ctx->pt_fill,
                   &ctx->pt_key, &ctx->pt_kcnt, &ctx->pt_kstart, &ctx->pt_kfill, &ctx->pt_order, &ctx->pt_max,
                   &ctx->pt_bcolor, &ctx->pt_rem, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
-                  &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill};
+                  &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill,
+                  &ctx->pt_cflag, &ctx->pt_cpos, &ctx->pt_cbody};
   for (Buf* b : bufs3) release(*b);
   Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
                   &ctx->mlp_choice};

@@ -166,6 +166,8 @@ struct sg_ctx {
   // Shifted tiles and band bodies: tile of each body, band flag, tile-local slot, band bodies by
   // tile; band bodies per patch and the scatter's fill counters.
   sg::Buf pt_qpatch, pt_band, pt_lidxq, pt_qbody, pt_bcnt, pt_nfill, pt_qcnt, pt_qstart, pt_qfill;
+  // Bodies of the remaining contacts: flag, slot (exclusive scan of the flags), compacted list.
+  sg::Buf pt_cflag, pt_cpos, pt_cbody;
   // Batched Ball2D scenes (sg_batch2d_upload).  Scene s owns bodies [sb_off[s], sb_off[s+1]),
   // planes [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]); its contacts of a
   // step are [sc_off[s], sc_off[s+1]).  Counts live on the device (b_ctl: contact count,

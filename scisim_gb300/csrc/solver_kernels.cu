@@ -27,7 +27,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (fewer barrier arrivals)
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
-constexpr int kPatchBlock = 1024;  // two-level kernel
+constexpr int kPatchBlock = 768;  // two-level kernel
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------------------
@@ -1112,7 +1112,27 @@ struct PatchArgs {
   int capq;           // and for a shifted tile
   int stage_p;        // contacts of a patch staged in shared memory (its first ones, by colour)
   int stage_q;        // and of a shifted tile
+  const int* cbody;   // bodies of the remaining contacts (group P + Pb), and each body's slot
+  const int* cslot;   //   among them (valid for those bodies only)
+  int capc;           // their shared-memory slots (even), 0 if the remainder is not staged
+  int ncbody;         // their number
+  int stage_c;        // remaining contacts staged in block 0 (all of them, or 0)
 };
+
+// Bodies of the remaining contacts (group P + Pb): flagged here, compacted by a scan.
+__global__ void k_rest_mark(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
+                            const int* __restrict__ cpatch, const PatchSetup* __restrict__ ps, int* __restrict__ flag) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc || cpatch[k] != ps->P + ps->Pb) return;
+  flag[ia[k]] = 1;
+  flag[ib[k]] = 1;
+}
+
+__global__ void k_rest_scatter(int nb, const int* __restrict__ flag, const int* __restrict__ pos,
+                               int* __restrict__ cbody) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nb && flag[i]) cbody[pos[i]] = i;
+}
 
 // T0 x T1 with (T0 + 1)(T1 + 1) <= max_patches, the largest T0 T1 weighted towards square
 // tiles (cells are square).
@@ -1360,9 +1380,11 @@ __global__ void k_contact_key(int nc, const int* __restrict__ gcolor, const int*
   atomicAdd(&kcount[kk], 1);
 }
 
-// Largest contact count of a patch (out[0]) and of a shifted tile (out[1]).
+// Largest contact count of a patch (out[0]) and of a shifted tile (out[1]); the remaining
+// contacts (out[2]).
 __global__ void k_group_max(const PatchSetup* __restrict__ ps, const int* __restrict__ kstart, int* __restrict__ out) {
   const int P = ps->P, Pb = ps->Pb;
+  if (threadIdx.x == 0) out[2] = kstart[(P + Pb + 1) * kMaxColors] - kstart[(P + Pb) * kMaxColors];
   int mp = 0, mq = 0;
   for (int g = threadIdx.x; g < P + Pb; g += blockDim.x) {
     const int n = kstart[(g + 1) * kMaxColors] - kstart[g * kMaxColors];
@@ -1456,8 +1478,8 @@ __device__ __forceinline__ void gs_update32_local(const Gs32Args& B, int s, floa
 }
 
 // A contact staged in shared memory: both body slots in one word (16 bits each, 0xffff for a
-// static plane), normal, forcing and friction coefficient; the impulse kept there too (and
-// stored to global memory for the FP64 checks).  The Delassus block of a disc contact is
+// static plane), normal, forcing and friction coefficient; the impulse kept there too (written
+// back to global memory before each FP64 check).  The Delassus block of a disc contact is
 // (1/m_a + 1/m_b) I (n and t = (-n_y, n_x) are orthonormal, so n.t is exactly 0 and
 // n.n = t.t = 1 to rounding), so it is formed from the slots' inverse masses.
 struct Staged {
@@ -1477,8 +1499,7 @@ __device__ __forceinline__ void stage_contact(const Gs32Args& B, const Staged& S
   S.r[i] = B.r[s];
 }
 
-__device__ __forceinline__ void gs_update32_staged(const Gs32Args& B, const Staged& S, int i, int s, float2* sv,
-                                                   const float* sm) {
+__device__ __forceinline__ void gs_update32_staged(const Staged& S, int i, float2* sv, const float* sm) {
   const unsigned ab = S.ab[i];
   const int a = (int)(ab & 0xffffu), b = (int)(ab >> 16);
   const bool has_b = b != 0xffff;
@@ -1498,15 +1519,21 @@ __device__ __forceinline__ void gs_update32_staged(const Gs32Args& B, const Stag
   const float wd = ma + mb;
   const float bt0 = u0 - wd * rk.x;
   const float bt1 = u1 - wd * rk.y;
-  float rn0, rn1;
-  local_solve_2d_f(wd, 0.0f, wd, bt0, bt1, S.mu[i], rn0, rn1);
+  // Coulomb local problem with W = wd I: open if bt0 >= 0; otherwise r = -bt / wd with its
+  // tangential part clamped to the cone (for an isotropic W the sliding solution keeps the
+  // stick solution's normal part, so stick and slide are this one expression).
+  float rn0 = 0.0f, rn1 = 0.0f;
+  if (bt0 < 0.0f) {
+    const float inv = __frcp_rn(wd);
+    const float mu = S.mu[i];
+    rn0 = -bt0 * inv;
+    rn1 = fminf(fmaxf(-bt1 * inv, -mu * rn0), mu * rn0);
+  }
   const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
   const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
   sv[a] = make_float2(va.x + ma * px, va.y + ma * py);
   if (has_b) sv[b] = make_float2(vb.x - mb * px, vb.y - mb * py);
-  const float2 rn = make_float2(rn0, rn1);
-  S.r[i] = rn;
-  B.r[s] = rn;
+  S.r[i] = make_float2(rn0, rn1);
 }
 
 // Highest non-empty colour + 1 of a group's offsets.
@@ -1543,6 +1570,15 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   S.r = S.c + cs;
   S.ab = reinterpret_cast<unsigned*>(S.r + cs);
   S.mu = reinterpret_cast<float*>(S.ab + cs);
+  // Then the remainder's bodies (velocities, 1/m) and contacts, used by block 0 alone.
+  float2* svc = reinterpret_cast<float2*>(S.mu + cs);
+  float* smc = reinterpret_cast<float*>(svc + Q.capc);
+  Staged SC;
+  SC.n = reinterpret_cast<float2*>(smc + Q.capc);
+  SC.c = SC.n + Q.stage_c;
+  SC.r = SC.c + Q.stage_c;
+  SC.ab = reinterpret_cast<unsigned*>(SC.r + Q.stage_c);
+  SC.mu = reinterpret_cast<float*>(SC.ab + Q.stage_c);
   __shared__ int s_goff[kMaxColors + 1];
   __shared__ int s_hoff[kMaxColors + 1];
   __shared__ int s_boff[kMaxColors + 1];
@@ -1569,9 +1605,26 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   const int sq_end = sq0 + min(s_hoff[ncol_q] - sq0, Q.stage_q);
   for (int s = sp0 + threadIdx.x; s < sp_end; s += blockDim.x) stage_contact(B, S, s - sp0, s);
   for (int s = sq0 + threadIdx.x; s < sq_end; s += blockDim.x) stage_contact(B, S, Q.stage_p + s - sq0, s);
-  __syncthreads();
   int btail = ncol_r;
   while (btail > 0 && s_boff[btail] - s_boff[btail - 1] <= 2 * (int)blockDim.x) --btail;
+  // The remainder swept by block 0 in shared memory when all its colours are small and it
+  // was staged whole (bodies compacted on the host side: cslot maps a body to its slot).
+  const int sc0 = s_boff[0], nrest = s_boff[ncol_r] - sc0;
+  const bool rest_staged = btail == 0 && nrest > 0 && Q.stage_c == nrest;
+  const int ncb = rest_staged ? Q.ncbody : 0;
+  if (rest_staged && blockIdx.x == 0) {
+    for (int s = sc0 + threadIdx.x; s < sc0 + nrest; s += blockDim.x) {
+      const int2 ab = B.ab[s];
+      const int i = s - sc0;
+      SC.ab[i] = (unsigned)Q.cslot[ab.x] | ((unsigned)Q.cslot[ab.y] << 16);
+      SC.n[i] = B.n[s];
+      SC.c[i] = B.c[s];
+      SC.mu[i] = B.w[s].w;
+      SC.r[i] = B.r[s];
+    }
+    for (int j = threadIdx.x; j < ncb; j += blockDim.x) smc[j] = B.minv[Q.cbody[j]];
+  }
+  __syncthreads();
   const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
   const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
   double2* best = A.r_a;
@@ -1603,7 +1656,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
         const int e = s_goff[col + 1];
         for (int s = s_goff[col] + threadIdx.x; s < e; s += blockDim.x) {
           if (s < sp_end)
-            gs_update32_staged(B, S, s - sp0, s, sv, sm);
+            gs_update32_staged(S, s - sp0, sv, sm);
           else
             gs_update32_local(B, s, sv, sm);
         }
@@ -1628,7 +1681,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
           const int e = s_hoff[col + 1];
           for (int s = s_hoff[col] + threadIdx.x; s < e; s += blockDim.x) {
             if (s < sq_end)
-              gs_update32_staged(B, S, Q.stage_p + s - sq0, s, svq, smq);
+              gs_update32_staged(S, Q.stage_p + s - sq0, svq, smq);
             else
               gs_update32_local(B, s, svq, smq);
           }
@@ -1640,27 +1693,45 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
         if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
         return;
       }
-      // The remaining contacts (across patches and shifted tiles), colour by colour over the
-      // grid; the small trailing colours run in block 0 alone.
-      for (int col = 0; col < btail; ++col) {
-        const int b0 = s_boff[col], e = s_boff[col + 1];
-        if (b0 == e) continue;
-        for (int s = b0 + tid; s < e; s += nthr) gs_update32(B, s);
-        if (!grid_sync(A.gb, A.spin)) {
-          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
-          return;
-        }
-      }
-      if (btail < ncol_r && s_boff[btail] < s_boff[ncol_r]) {
+      // The remaining contacts (across patches and shifted tiles): staged, by block 0 on
+      // shared-memory velocities; otherwise colour by colour over the grid, the small trailing
+      // colours in block 0 alone.
+      if (rest_staged) {
         if (blockIdx.x == 0) {
-          for (int col = btail; col < ncol_r; ++col) {
-            for (int s = s_boff[col] + threadIdx.x; s < s_boff[col + 1]; s += blockDim.x) gs_update32(B, s);
+          for (int j = threadIdx.x; j < ncb; j += blockDim.x) svc[j] = __ldcg(&B.v[Q.cbody[j]]);
+          __syncthreads();
+          for (int col = 0; col < ncol_r; ++col) {
+            for (int s = s_boff[col] + threadIdx.x; s < s_boff[col + 1]; s += blockDim.x)
+              gs_update32_staged(SC, s - sc0, svc, smc);
             __syncthreads();
           }
+          for (int j = threadIdx.x; j < ncb; j += blockDim.x) B.v[Q.cbody[j]] = svc[j];
         }
         if (!grid_sync(A.gb, A.spin)) {
           if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
           return;
+        }
+      } else {
+        for (int col = 0; col < btail; ++col) {
+          const int b0 = s_boff[col], e = s_boff[col + 1];
+          if (b0 == e) continue;
+          for (int s = b0 + tid; s < e; s += nthr) gs_update32(B, s);
+          if (!grid_sync(A.gb, A.spin)) {
+            if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+            return;
+          }
+        }
+        if (btail < ncol_r && s_boff[btail] < s_boff[ncol_r]) {
+          if (blockIdx.x == 0) {
+            for (int col = btail; col < ncol_r; ++col) {
+              for (int s = s_boff[col] + threadIdx.x; s < s_boff[col + 1]; s += blockDim.x) gs_update32(B, s);
+              __syncthreads();
+            }
+          }
+          if (!grid_sync(A.gb, A.spin)) {
+            if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+            return;
+          }
         }
       }
       if (timer) {
@@ -1674,6 +1745,15 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
       // sweeps, and the final check at max_iters always happens.
       do_eval = it == next_eval || it == A.max_iters;
       if (do_eval) {
+        // Staged impulses back to global memory first.
+        for (int s = sp0 + threadIdx.x; s < sp_end; s += blockDim.x) B.r[s] = S.r[s - sp0];
+        for (int s = sq0 + threadIdx.x; s < sq_end; s += blockDim.x) B.r[s] = S.r[Q.stage_p + s - sq0];
+        if (rest_staged && blockIdx.x == 0)
+          for (int s = sc0 + threadIdx.x; s < sc0 + nrest; s += blockDim.x) B.r[s] = SC.r[s - sc0];
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
         // Lift the FP32 iterate to FP64: impulses, then body velocities v = v0 + Minv H^T r.
         for (int s = tid; s < A.nc; s += nthr) {
           const float2 r32 = __ldcg(&B.r[s]);
@@ -2219,7 +2299,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       int pmax = 0;
       const int maxP = ctx->num_sms;
       const bool try_patches = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 && nc >= 20000;
-      int pmaxq = 0, cmax_p = 0, cmax_q = 0;
+      int pmaxq = 0, cmax_p = 0, cmax_q = 0, nrest = 0, nrest_bodies = 0;
       PatchSetup hps{};
       if (try_patches) {
         // Groups: at most maxP patches, maxP shifted tiles and the remainder (a degenerate
@@ -2248,7 +2328,10 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         if (int r = grow(ctx->pt_kstart, sizeof(int) * keys)) return r;
         if (int r = grow(ctx->pt_kfill, sizeof(int) * keys)) return r;
         if (int r = grow(ctx->pt_order, sizeof(int) * c)) return r;
-        if (int r = grow(ctx->pt_max, 5 * sizeof(int))) return r;
+        if (int r = grow(ctx->pt_max, 7 * sizeof(int))) return r;
+        if (int r = grow(ctx->pt_cflag, sizeof(int) * b)) return r;
+        if (int r = grow(ctx->pt_cpos, sizeof(int) * (b + 1))) return r;
+        if (int r = grow(ctx->pt_cbody, sizeof(int) * b)) return r;
         if (int r = grow(ctx->pt_bcolor, sizeof(int) * c)) return r;
         if (int r = grow(ctx->pt_rem, 4 * sizeof(int))) return r;
         PatchSetup* ps = ctx->pt_setup.as<PatchSetup>();
@@ -2257,7 +2340,8 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
           SG_CUDA_TRY(cudaMemsetAsync(z->p, 0, gsz, s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kcnt.p, 0, sizeof(int) * keys, s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kfill.p, 0, sizeof(int) * keys, s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, 5 * sizeof(int), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, 7 * sizeof(int), s));
+        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_cflag.p, 0, sizeof(int) * b, s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_band.p, 0, sizeof(int) * b, s));
         k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, ctx->pt_patch.as<int>(),
                                                          ctx->pt_qpatch.as<int>(), ctx->pt_cnt.as<int>());
@@ -2267,6 +2351,13 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         k_contact_side<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, ctx->pt_patch.as<int>(),
                                                          ctx->pt_qpatch.as<int>(), ps, cpatch, bcolor,
                                                          ctx->pt_band.as<int>());
+        k_rest_mark<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, cpatch, ps, ctx->pt_cflag.as<int>());
+        SG_CUDA_TRY(cudaGetLastError());
+        if (int r = scan_exclusive(ctx, ctx->pt_cflag.as<int>(), ctx->pt_cpos.as<int>(), nb)) return r;
+        k_rest_scatter<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_cflag.as<int>(), ctx->pt_cpos.as<int>(),
+                                                        ctx->pt_cbody.as<int>());
+        SG_CUDA_TRY(cudaMemcpyAsync(ctx->pt_max.as<int>() + 6, ctx->pt_cpos.as<int>() + nb, sizeof(int),
+                                    cudaMemcpyDeviceToDevice, s));
         k_band_count<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_band.as<int>(), ctx->pt_patch.as<int>(),
                                                        ctx->pt_qpatch.as<int>(), ctx->pt_bcnt.as<int>(),
                                                        ctx->pt_qcnt.as<int>());
@@ -2309,17 +2400,19 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
                                                            ctx->pt_kfill.as<int>(), ctx->pt_order.as<int>());
         k_group_max<<<1, kBlock, 0, s>>>(ps, ctx->pt_kstart.as<int>(), ctx->pt_max.as<int>() + 3);
         SG_CUDA_TRY(cudaGetLastError());
-        int hmax[5] = {0, 0, 0, 0, 0};
-        SG_CUDA_TRY(cudaMemcpyAsync(hmax, ctx->pt_max.p, 5 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        int hmax[7] = {0, 0, 0, 0, 0, 0, 0};
+        SG_CUDA_TRY(cudaMemcpyAsync(hmax, ctx->pt_max.p, 7 * sizeof(int), cudaMemcpyDeviceToHost, s));
         SG_CUDA_TRY(cudaMemcpyAsync(&hps, ps, sizeof(PatchSetup), cudaMemcpyDeviceToHost, s));
         SG_CUDA_TRY(cudaStreamSynchronize(s));
         pmax = hmax[0];
         pmaxq = hmax[1];
         cmax_p = hmax[3];
         cmax_q = hmax[4];
-        // setup, of_body, side, band_count, 2 x 3 scan, scatter, 2 max, colour, colour init,
-        // recolour, key, 3 scan, scatter, group max
-        ctx->kernel_launches += 22;
+        nrest = hmax[5];
+        nrest_bodies = hmax[6];
+        // setup, of_body, side, rest mark, 3 scan, rest scatter, band_count, 2 x 3 scan, scatter,
+        // 2 max, colour, colour init, recolour, key, 3 scan, scatter, group max
+        ctx->kernel_launches += 27;
       }
       // Shared-memory slots rounded up to even counts (8-byte alignment of the second block).
       const int capp = (pmax + 1) & ~1, capq = (pmaxq + 1) & ~1;
@@ -2374,13 +2467,20 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
           dyn_budget = budget;
         }
         const int body_bytes = 12 * (capp + capq);
-        const int avail = std::max(0, dyn_budget - body_bytes) / 32;
+        // The remainder first (block 0 sweeps it whole or not at all), then the patch, the tile.
+        int capc = (nrest_bodies + 1) & ~1, stage_c = nrest;
+        int rest_bytes = 12 * capc + 32 * stage_c;
+        if (nrest == 0 || nrest_bodies > kPatchBodyCap || rest_bytes > dyn_budget - body_bytes) {
+          capc = stage_c = rest_bytes = 0;
+        }
+        const int avail = std::max(0, dyn_budget - body_bytes - rest_bytes) / 32;
         const int stage_p = std::min(cmax_p, avail);
         const int stage_q = std::min(cmax_q, avail - stage_p);
         PatchArgs Q{ctx->pt_setup.as<PatchSetup>(), ctx->pt_start.as<int>(), ctx->pt_body.as<int>(),
                     ctx->pt_bcnt.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qbody.as<int>(),
-                    ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), capp, capq, stage_p, stage_q};
-        const size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q);
+                    ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), capp, capq, stage_p, stage_q,
+                    ctx->pt_cbody.as<int>(), ctx->pt_cpos.as<int>(), capc, capc ? nrest_bodies : 0, stage_c};
+        const size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q) + (size_t)rest_bytes;
         ctx->patch_staged += (uint64_t)stage_p;
         void* args[] = {&GA, &GB, &Q};
         // The boundary colouring used the barrier: start it afresh for this grid.
