@@ -39,29 +39,36 @@ struct GridBarrier {
 
 // Monotonic counter: barrier number b is complete when count reaches (b + 1) * gridDim.x,
 // so each arrival is one atomic and the release needs no reset.  The counter starts
-// at zero for every launch (the host clears the struct) and 2^32 arrivals are far
-// beyond any launch here.
+// at zero for every launch (the host clears the struct) and 2^31 arrivals are far
+// beyond any launch here.  An error (a wait that ran out) sets the counter's top bit,
+// so waiters see it in the word they poll and the release costs no further read;
+// `error` mirrors it for the host side.
+constexpr unsigned int kBarrierError = 0x80000000u;
+
 __device__ __forceinline__ bool grid_sync(GridBarrier* gb, unsigned long long spin_limit) {
   __syncthreads();
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
     volatile unsigned int* vcount = &gb->count;
-    volatile int* verr = &gb->error;
     __threadfence();
     const unsigned int old = atomicAdd(&gb->count, 1u);
-    const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
+    int ok = (old & kBarrierError) ? 0 : 1;
+    const unsigned int target = ((old & ~kBarrierError) / gridDim.x + 1u) * gridDim.x;
     unsigned long long spins = 0;
-    while ((int)(*vcount - target) < 0) {
-      if ((++spins & 255ull) == 0ull) {
-        if (*verr) break;
-        if (spins > spin_limit) {
-          atomicExch(&gb->error, 1);
-          break;
-        }
+    while (ok) {
+      const unsigned int v = *vcount;
+      if (v & kBarrierError) {
+        ok = 0;
+      } else if ((int)(v - target) >= 0) {
+        break;
+      } else if ((++spins & 255ull) == 0ull && spins > spin_limit) {
+        atomicOr(&gb->count, kBarrierError);
+        atomicExch(&gb->error, 1);
+        ok = 0;
       }
     }
     __threadfence();
-    s_ok = (*verr) ? 0 : 1;
+    s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;

@@ -27,7 +27,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (fewer barrier arrivals)
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
-constexpr int kPatchBlock = 768;  // two-level kernel
+constexpr int kPatchBlock = 384;  // two-level kernel
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------------------
