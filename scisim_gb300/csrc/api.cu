@@ -203,7 +203,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->pt_key, &ctx->pt_kcnt, &ctx->pt_kstart, &ctx->pt_kfill, &ctx->pt_order, &ctx->pt_max,
                   &ctx->pt_bcolor, &ctx->pt_rem, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
                   &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill,
-                  &ctx->pt_cflag, &ctx->pt_cpos, &ctx->pt_cbody};
+                  &ctx->pt_cflag, &ctx->pt_cpos, &ctx->pt_cbody, &ctx->pt_hist, &ctx->pt_pref,
+                  &ctx->pt_cuts, &ctx->pt_maps};
   for (Buf* b : bufs3) release(*b);
   Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
                   &ctx->mlp_choice};

@@ -168,6 +168,9 @@ struct sg_ctx {
   sg::Buf pt_qpatch, pt_band, pt_lidxq, pt_qbody, pt_bcnt, pt_nfill, pt_qcnt, pt_qstart, pt_qfill;
   // Bodies of the remaining contacts: flag, slot (exclusive scan of the flags), compacted list.
   sg::Buf pt_cflag, pt_cpos, pt_cbody;
+  // Contact-balanced cuts: per-column/row contact histograms, their prefix sums, the cuts, and
+  // the cell column/row -> patch and shifted-tile maps.
+  sg::Buf pt_hist, pt_pref, pt_cuts, pt_maps;
   // Batched Ball2D scenes (sg_batch2d_upload).  Scene s owns bodies [sb_off[s], sb_off[s+1]),
   // planes [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]); its contacts of a
   // step are [sc_off[s], sc_off[s+1]).  Counts live on the device (b_ctl: contact count,

@@ -1159,16 +1159,81 @@ __global__ void k_patch_setup(const GridParams* __restrict__ gp, int max_patches
   ps->d1 = d1;
 }
 
+// Contacts (by the cell of their first body) plus bodies per cell column and per cell row: the
+// cuts between patches sit at quantiles of these, so that patches carry about equal work and
+// no patch collects every body that is still in free flight.
+__global__ void k_patch_hist(int nc, int nb, const int* __restrict__ ia, const int* __restrict__ cell_of,
+                             const PatchSetup* __restrict__ ps, int* __restrict__ hx, int* __restrict__ hy) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc + nb) return;
+  const int d0 = ps->d0;
+  const int cell = cell_of[k < nc ? ia[k] : k - nc];
+  atomicAdd(&hx[cell % d0], 1);
+  atomicAdd(&hy[cell / d0], 1);
+}
+
+// Cuts X[0..T0] (cell columns) and Y[0..T1] (rows), strictly increasing from 0 to d: cut t at
+// the first cell where the exclusive prefix count reaches t/T of the total.  One block.
+__device__ void cuts_1d(const int* __restrict__ pref, int d, int T, int* __restrict__ cut) {
+  const long total = pref[d];
+  for (int t = 1 + threadIdx.x; t < T; t += blockDim.x) {
+    const long target = total * t / T;
+    int lo = 0, hi = d;  // first c in [0, d] with pref[c] >= target
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (pref[mid] >= target)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    cut[t] = lo;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cut[0] = 0;
+    cut[T] = d;
+    for (int t = 1; t < T; ++t) cut[t] = max(cut[t], cut[t - 1] + 1);
+    for (int t = T - 1; t >= 1; --t) cut[t] = min(cut[t], cut[t + 1] - 1);
+  }
+  __syncthreads();
+}
+
+__global__ void k_patch_cuts(const PatchSetup* __restrict__ ps, const int* __restrict__ px,
+                             const int* __restrict__ py, int* __restrict__ cx, int* __restrict__ cy) {
+  cuts_1d(px, ps->d0, ps->T0, cx);
+  cuts_1d(py, ps->d1, ps->T1, cy);
+}
+
+// Cell column/row -> patch column/row and shifted-tile column/row.  The shifted tiles' cuts sit
+// halfway between neighbouring patch cuts, so every patch corner is a shifted tile's centre.
+__device__ __forceinline__ void tile_maps_1d(int c, const int* __restrict__ cut, int T, int* __restrict__ a,
+                                             int* __restrict__ b) {
+  int ta = 0, tb = 0;
+  for (int t = 1; t < T; ++t) ta += cut[t] <= c;
+  for (int t = 0; t < T; ++t) tb += (cut[t] + cut[t + 1] + 1) / 2 <= c;
+  a[c] = ta;
+  b[c] = tb;
+}
+
+__global__ void k_patch_maps(const PatchSetup* __restrict__ ps, const int* __restrict__ cx, const int* __restrict__ cy,
+                             int* __restrict__ colA, int* __restrict__ colB, int* __restrict__ rowA,
+                             int* __restrict__ rowB) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ps->d0) tile_maps_1d(i, cx, ps->T0, colA, colB);
+  if (i < ps->d1) tile_maps_1d(i, cy, ps->T1, rowA, rowB);
+}
+
 __global__ void k_patch_of_body(int nb, const int* __restrict__ cell_of, const PatchSetup* __restrict__ ps,
-                                int* __restrict__ patch, int* __restrict__ qpatch, int* __restrict__ pcount) {
+                                const int* __restrict__ colA, const int* __restrict__ colB,
+                                const int* __restrict__ rowA, const int* __restrict__ rowB, int* __restrict__ patch,
+                                int* __restrict__ qpatch, int* __restrict__ pcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
-  const long d0 = ps->d0, d1 = ps->d1, T0 = ps->T0, T1 = ps->T1;
+  const int d0 = ps->d0, T0 = ps->T0;
   const int cell = cell_of[i];
-  const long cx = cell % d0, cy = cell / d0;
-  const int p = (int)(cx * T0 / d0 + T0 * (cy * T1 / d1));
-  // Shifted tile: floor(cx T0 / d0 + 1/2), in [0, T0].
-  const int q = (int)((2 * cx * T0 + d0) / (2 * d0) + (T0 + 1) * ((2 * cy * T1 + d1) / (2 * d1)));
+  const int cx = cell % d0, cy = cell / d0;
+  const int p = colA[cx] + T0 * rowA[cy];
+  const int q = colB[cx] + (T0 + 1) * rowB[cy];
   patch[i] = p;
   qpatch[i] = q;
   atomicAdd(&pcount[p], 1);
@@ -2329,6 +2394,12 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         if (int r = grow(ctx->pt_kfill, sizeof(int) * keys)) return r;
         if (int r = grow(ctx->pt_order, sizeof(int) * c)) return r;
         if (int r = grow(ctx->pt_max, 7 * sizeof(int))) return r;
+        // Cell columns and rows number at most the broad phase's cell capacity (4 nb + 64).
+        const size_t gcap = 4 * (size_t)nb + 64;
+        if (int r = grow(ctx->pt_hist, 2 * sizeof(int) * gcap)) return r;
+        if (int r = grow(ctx->pt_pref, 2 * sizeof(int) * (gcap + 1))) return r;
+        if (int r = grow(ctx->pt_cuts, 2 * sizeof(int) * (size_t)(maxP + 2))) return r;
+        if (int r = grow(ctx->pt_maps, 4 * sizeof(int) * gcap)) return r;
         if (int r = grow(ctx->pt_cflag, sizeof(int) * b)) return r;
         if (int r = grow(ctx->pt_cpos, sizeof(int) * (b + 1))) return r;
         if (int r = grow(ctx->pt_cbody, sizeof(int) * b)) return r;
@@ -2343,8 +2414,26 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, 7 * sizeof(int), s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_cflag.p, 0, sizeof(int) * b, s));
         SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_band.p, 0, sizeof(int) * b, s));
-        k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, ctx->pt_patch.as<int>(),
-                                                         ctx->pt_qpatch.as<int>(), ctx->pt_cnt.as<int>());
+        {
+          int* hx = ctx->pt_hist.as<int>();
+          int* hy = hx + gcap;
+          int* px = ctx->pt_pref.as<int>();
+          int* py = px + gcap + 1;
+          int* cx = ctx->pt_cuts.as<int>();
+          int* cy = cx + maxP + 2;
+          int* maps = ctx->pt_maps.as<int>();
+          SG_CUDA_TRY(cudaMemsetAsync(hx, 0, 2 * sizeof(int) * gcap, s));
+          k_patch_hist<<<blocks_for((long)nc + nb), kBlock, 0, s>>>(nc, nb, P.ia, ctx->cell_of.as<int>(), ps, hx, hy);
+          SG_CUDA_TRY(cudaGetLastError());
+          if (int r = scan_exclusive(ctx, hx, px, (int)gcap)) return r;
+          if (int r = scan_exclusive(ctx, hy, py, (int)gcap)) return r;
+          k_patch_cuts<<<1, kBlock, 0, s>>>(ps, px, py, cx, cy);
+          k_patch_maps<<<blocks_for((long)gcap), kBlock, 0, s>>>(ps, cx, cy, maps, maps + gcap, maps + 2 * gcap,
+                                                               maps + 3 * gcap);
+          k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, maps, maps + gcap,
+                                                           maps + 2 * gcap, maps + 3 * gcap, ctx->pt_patch.as<int>(),
+                                                           ctx->pt_qpatch.as<int>(), ctx->pt_cnt.as<int>());
+        }
         SG_CUDA_TRY(cudaGetLastError());
         int* cpatch = ctx->pt_order.as<int>();  // scratch until the order is built
         int* bcolor = ctx->pt_bcolor.as<int>();
@@ -2410,9 +2499,10 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         cmax_q = hmax[4];
         nrest = hmax[5];
         nrest_bodies = hmax[6];
-        // setup, of_body, side, rest mark, 3 scan, rest scatter, band_count, 2 x 3 scan, scatter,
-        // 2 max, colour, colour init, recolour, key, 3 scan, scatter, group max
-        ctx->kernel_launches += 27;
+        // setup, hist, 2 x 3 scan, cuts, maps, of_body, side, rest mark, 3 scan, rest scatter,
+        // band_count, 2 x 3 scan, scatter, 2 max, colour, colour init, recolour, key, 3 scan,
+        // scatter, group max
+        ctx->kernel_launches += 36;
       }
       // Shared-memory slots rounded up to even counts (8-byte alignment of the second block).
       const int capp = (pmax + 1) & ~1, capq = (pmaxq + 1) & ~1;
@@ -2502,6 +2592,8 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       } else {
         void* args[] = {&GA, &GB};
         const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
+        // The patch setup's colouring kernels used the barrier with their own grid: reset it.
+        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
         SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
