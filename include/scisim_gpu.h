@@ -293,6 +293,42 @@ SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
  * colour.  0 keeps the one-level colour sweeps. */
 SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
 
+/* Checkpoint / resume of a context holding one Ball2D or sphere scene (replaces SCISim's binary
+ * serialisation of the simulation, ball2dcli/ball2d_cli.cpp:199-316, Ball2DSim.cpp:810-822).
+ * The checkpoint holds the context's settings, the scene (positions, velocities, radii, masses,
+ * planes; for spheres the principal and world inertia) and the impulse cache, byte for byte,
+ * so that a run resumed with sg_checkpoint_load continues bit-identically.  It does not hold
+ * the learned warm start's network.  sg_checkpoint_size returns the bytes sg_checkpoint_save
+ * writes (negative for a batched or empty context); sg_checkpoint_load replaces the context's
+ * settings (keeping its device) and scene. */
+SG_API int64_t sg_checkpoint_size(sg_ctx* ctx);
+SG_API int sg_checkpoint_save(sg_ctx* ctx, void* buf, int64_t bytes);
+SG_API int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes);
+
+/* Performance knobs that leave the solve's contract unchanged (no counterpart in the reference):
+ * two_level (sg_set_two_level), the contact count from which a single-scene FP32 solve uses the
+ * two-level sweeps (default 20,000), and the base interval in sweeps of the FP64 checks of the
+ * FP32 form (default 16; the interval grows from it while the residual is far from tol). */
+typedef struct {
+  int32_t two_level;
+  int32_t check_interval;
+  int32_t two_level_min_contacts;
+  int32_t reserved;
+} sg_tuning;
+
+SG_API int sg_get_tuning(sg_ctx* ctx, sg_tuning* tuning);
+SG_API int sg_set_tuning(sg_ctx* ctx, const sg_tuning* tuning);
+
+/* Autotuner: from the current state of a single-scene context, times trial_steps steps under each
+ * candidate (two-level on, check interval 8 / 16 / 32; then two-level off, the same intervals),
+ * one untimed run first, each from a checkpoint of that state; restores the state and keeps the
+ * fastest candidate.  ms_per_step (6 entries, may be NULL) gets each candidate's time per step,
+ * NaN for candidates that do not apply (the FP64 form has none: its one timing goes to entry 0;
+ * sphere scenes have no two-level sweeps).  best (may be NULL) gets the chosen tuning.  The
+ * profile counters include the trial steps. */
+SG_API int sg_autotune(sg_ctx* ctx, int32_t trial_steps, uint32_t first_iteration, sg_tuning* best,
+                       double* ms_per_step);
+
 /* Layout of the last solve's two-level sweeps (diagnostics and tests).  counts[0] = patches P,
  * counts[1] = shifted tiles Pb (the patch tiling shifted by half a tile).  Per contact, in the
  * order of sg_last_contacts: its group (g < P: inside patch g; P <= g < P + Pb: between patches,

@@ -41,6 +41,14 @@ class SgStepStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class SgTuning(C.Structure):
+    _fields_ = [("two_level", C.c_int32), ("check_interval", C.c_int32), ("two_level_min_contacts", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class SgProfile(C.Structure):
     _fields_ = [("gs_ms", C.c_double), ("gs_launches", C.c_uint64), ("contact_sweeps", C.c_uint64),
                 ("contact_evals", C.c_uint64), ("kernel_launches", C.c_uint64), ("steps", C.c_uint64),
@@ -99,6 +107,12 @@ SIGNATURES = {
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "sg_set_two_level": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sg_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sg_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_void_p, _dp]),
+    "sg_checkpoint_size": (_i64, [C.c_void_p]),
+    "sg_checkpoint_save": (C.c_int, [C.c_void_p, C.c_void_p, _i64]),
+    "sg_checkpoint_load": (C.c_int, [C.c_void_p, C.c_void_p, _i64]),
     "sg_last_patch_layout": (C.c_int, [C.c_void_p, _i64, _i64, _ip, _ip, _ip, _ip, _ip, _ip]),
     "sg_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sg_set_spin_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
@@ -391,6 +405,43 @@ class Context:
 
     def set_two_level(self, on=True):
         check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
+
+    def tuning(self):
+        t = SgTuning()
+        check(lib().sg_get_tuning(self._h, C.byref(t)), "sg_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **changes):
+        t = SgTuning(**{**self.tuning(), **changes})
+        check(lib().sg_set_tuning(self._h, C.byref(t)), "sg_set_tuning")
+
+    def autotune(self, trial_steps=3, first_iteration=1):
+        """Times each candidate tuning from the current state, keeps the fastest (sg_autotune).
+        Returns (chosen tuning, ms per step of the 6 candidates, NaN where not applicable)."""
+        best = SgTuning()
+        ms = np.full(6, np.nan)
+        check(lib().sg_autotune(self._h, trial_steps, first_iteration, C.byref(best), dptr(ms)), "sg_autotune")
+        return best.as_dict(), ms
+
+    def checkpoint(self):
+        """The context's settings, scene and impulse cache as bytes (sg_checkpoint_save)."""
+        n = lib().sg_checkpoint_size(self._h)
+        if n < 0:
+            raise SgError(SG_BAD_INPUT, "sg_checkpoint_size")
+        buf = C.create_string_buffer(int(n))
+        check(lib().sg_checkpoint_save(self._h, buf, n), "sg_checkpoint_save")
+        return buf.raw
+
+    def restore(self, data):
+        """Replaces settings, scene and impulse cache with a checkpoint's (sg_checkpoint_load)."""
+        data = bytes(data)
+        check(lib().sg_checkpoint_load(self._h, data, len(data)), "sg_checkpoint_load")
+        # Header: magic[8], version, dim, nb, np (int32), prev_n (int64), sg_config.
+        _, dim, nb, _ = np.frombuffer(data, np.int32, 4, 8)
+        self.dim, self.nb = int(dim), int(nb)
+        cfg = SgConfig.from_buffer_copy(data, 32)
+        cfg.device = self.config.device
+        self.config = cfg
 
     def patch_layout(self, nc, nb):
         """Layout of the last two-level solve: patches P, shifted tiles Pb, each contact's group

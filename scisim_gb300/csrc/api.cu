@@ -4,6 +4,8 @@
 #include "ctx.hpp"
 
 #include <algorithm>
+#include <chrono>
+#include <limits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -972,6 +974,225 @@ int sg_last_patch_layout(sg_ctx* ctx, int64_t nc, int64_t nb, int32_t* counts, i
   counts[0] = ctx->last_patch_P;
   counts[1] = ctx->last_patch_Pb;
   return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoint / resume of a single-scene context (the reference serialises the whole simulation,
+// ball2dcli/ball2d_cli.cpp:199-316, Ball2DSim.cpp:810-822).  Layout: CkptHeader, then the
+// device arrays byte for byte (so that a resumed run is bit-identical: normalised plane normals,
+// inverse masses and world inertia are restored as stored, not recomputed), then the impulse
+// cache (sorted keys, (alpha, beta) per key).
+namespace {
+struct CkptHeader {
+  char magic[8];
+  int32_t version, dim, nb, np;
+  int64_t prev_n;
+  sg_config cfg;
+};
+constexpr char kCkptMagic[8] = {'S', 'G', 'C', 'K', 'P', 'T', '1', 0};
+
+struct CkptPart {
+  Buf* buf;
+  size_t bytes;
+};
+
+std::vector<CkptPart> ckpt_parts(sg_ctx* ctx, int dim, int nb, int np, int64_t prev_n) {
+  const size_t d = sizeof(double), b = (size_t)nb, p = (size_t)np;
+  std::vector<CkptPart> v;
+  if (dim == 2) {
+    v = {{&ctx->q, 2 * b * d},       {&ctx->v, 2 * b * d},       {&ctx->r, b * d},
+         {&ctx->m, b * d},           {&ctx->minv, b * d},        {&ctx->plane_x, 2 * p * d},
+         {&ctx->plane_n, 2 * p * d}, {&ctx->plane_t, 2 * p * d}};
+  } else {
+    v = {{&ctx->q, 12 * b * d},  {&ctx->v, 6 * b * d},         {&ctx->r, b * d},
+         {&ctx->m, b * d},       {&ctx->minv, b * d},          {&ctx->I0, 3 * b * d},
+         {&ctx->Iw, 9 * b * d},  {&ctx->Iinv, 9 * b * d},      {&ctx->plane_x, 3 * p * d},
+         {&ctx->plane_n, 3 * p * d}};
+  }
+  v.push_back({&ctx->prev_key, (size_t)prev_n * sizeof(unsigned long long)});
+  v.push_back({&ctx->prev_ab, (size_t)prev_n * 2 * d});
+  return v;
+}
+
+bool ckpt_supported(const sg_ctx* ctx) { return ctx->n_scenes == 0 && (ctx->dim == 2 || ctx->dim == 3); }
+}  // namespace
+
+int64_t sg_checkpoint_size(sg_ctx* ctx) {
+  if (!ctx || !ckpt_supported(ctx)) {
+    set_error("sg_checkpoint_size: needs a context holding one Ball2D or sphere scene");
+    return -1;
+  }
+  size_t total = sizeof(CkptHeader);
+  for (const CkptPart& part : ckpt_parts(ctx, ctx->dim, ctx->nb, ctx->np, ctx->prev_n)) total += part.bytes;
+  return (int64_t)total;
+}
+
+int sg_checkpoint_save(sg_ctx* ctx, void* buf, int64_t bytes) {
+  const int64_t need = sg_checkpoint_size(ctx);
+  if (need < 0 || !buf || bytes < need) {
+    if (need >= 0) set_error("sg_checkpoint_save: buffer smaller than sg_checkpoint_size");
+    return SG_BAD_INPUT;
+  }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  CkptHeader h{};
+  std::memcpy(h.magic, kCkptMagic, sizeof(h.magic));
+  h.version = 1;
+  h.dim = ctx->dim;
+  h.nb = ctx->nb;
+  h.np = ctx->np;
+  h.prev_n = ctx->prev_n;
+  h.cfg = ctx->cfg;
+  char* out = static_cast<char*>(buf);
+  std::memcpy(out, &h, sizeof(h));
+  size_t off = sizeof(h);
+  for (const CkptPart& part : ckpt_parts(ctx, h.dim, h.nb, h.np, h.prev_n)) {
+    if (part.bytes)
+      SG_CUDA_TRY(cudaMemcpyAsync(out + off, part.buf->p, part.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    off += part.bytes;
+  }
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes) {
+  if (!ctx || !buf || bytes < (int64_t)sizeof(CkptHeader)) {
+    set_error("sg_checkpoint_load: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  CkptHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, kCkptMagic, sizeof(h.magic)) != 0 || h.version != 1 || (h.dim != 2 && h.dim != 3) ||
+      h.nb < 0 || h.np < 0 || h.prev_n < 0) {
+    set_error("sg_checkpoint_load: not a checkpoint of this library");
+    return SG_BAD_INPUT;
+  }
+  size_t need = sizeof(h);
+  for (const CkptPart& part : ckpt_parts(ctx, h.dim, h.nb, h.np, h.prev_n)) need += part.bytes;
+  if ((size_t)bytes < need) {
+    set_error("sg_checkpoint_load: truncated checkpoint");
+    return SG_BAD_INPUT;
+  }
+  sg_config cfg = h.cfg;
+  cfg.device = ctx->device;
+  if (int r = sg_ctx_reconfigure(ctx, &cfg)) return r;
+  // Upload through the normal path (allocation, validation), then overwrite every array with
+  // the stored bytes.
+  const char* in = static_cast<const char*>(buf) + sizeof(h);
+  const size_t b = (size_t)h.nb, d = sizeof(double);
+  std::vector<double> tmp;
+  auto arr = [&](size_t at_doubles, size_t n) {
+    tmp.resize(n);
+    if (n) std::memcpy(tmp.data(), in + at_doubles * d, n * d);
+    return tmp;
+  };
+  int rc;
+  if (h.dim == 2) {
+    const std::vector<double> qv = arr(0, 2 * b), vv = arr(2 * b, 2 * b), rv = arr(4 * b, b), mv = arr(5 * b, b);
+    const size_t p0 = 7 * b;
+    const std::vector<double> px = arr(p0, 2 * (size_t)h.np), pn = arr(p0 + 2 * (size_t)h.np, 2 * (size_t)h.np);
+    rc = sg_ball2d_upload(ctx, h.nb, qv.data(), vv.data(), rv.data(), mv.data(), h.np, px.data(), pn.data());
+  } else {
+    const std::vector<double> qv = arr(0, 12 * b), vv = arr(12 * b, 6 * b), rv = arr(18 * b, b),
+                              mv = arr(19 * b, b), iv = arr(21 * b, 3 * b);
+    const size_t p0 = 42 * b;
+    const std::vector<double> px = arr(p0, 3 * (size_t)h.np), pn = arr(p0 + 3 * (size_t)h.np, 3 * (size_t)h.np);
+    rc = sphere3d_upload_impl(ctx, h.nb, qv.data(), vv.data(), rv.data(), mv.data(), iv.data(), h.np, px.data(),
+                              pn.data());
+  }
+  if (rc != SG_OK) return rc;
+  size_t off = 0;
+  for (const CkptPart& part : ckpt_parts(ctx, h.dim, h.nb, h.np, h.prev_n)) {
+    if (int r = grow(*part.buf, std::max<size_t>(part.bytes, 16))) return r;
+    if (part.bytes)
+      SG_CUDA_TRY(cudaMemcpyAsync(part.buf->p, in + off, part.bytes, cudaMemcpyHostToDevice, ctx->stream));
+    off += part.bytes;
+  }
+  ctx->prev_n = h.prev_n;
+  ctx->last_nc = 0;
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Tuning of the launch-independent performance knobs (no counterpart in the reference).
+int sg_get_tuning(sg_ctx* ctx, sg_tuning* t) {
+  if (!ctx || !t) return SG_BAD_INPUT;
+  t->two_level = ctx->patches ? 1 : 0;
+  t->check_interval = ctx->check_interval;
+  t->two_level_min_contacts = ctx->two_level_min_contacts;
+  t->reserved = 0;
+  return SG_OK;
+}
+
+int sg_set_tuning(sg_ctx* ctx, const sg_tuning* t) {
+  if (!ctx || !t || t->check_interval < 1 || t->check_interval > 4096 || t->two_level_min_contacts < 0) {
+    set_error("sg_set_tuning: check_interval in [1, 4096] and two_level_min_contacts >= 0");
+    return SG_BAD_INPUT;
+  }
+  ctx->patches = t->two_level != 0;
+  ctx->check_interval = t->check_interval;
+  ctx->two_level_min_contacts = t->two_level_min_contacts;
+  return SG_OK;
+}
+
+int sg_autotune(sg_ctx* ctx, int32_t trial_steps, uint32_t first_iteration, sg_tuning* best, double* ms_per_step) {
+  if (!ctx || trial_steps < 1 || !ckpt_supported(ctx)) {
+    set_error("sg_autotune: needs a context holding one Ball2D or sphere scene and trial_steps >= 1");
+    return SG_BAD_INPUT;
+  }
+  const int64_t n = sg_checkpoint_size(ctx);
+  if (n < 0) return SG_BAD_INPUT;
+  std::vector<char> ck((size_t)n);
+  if (int r = sg_checkpoint_save(ctx, ck.data(), n)) return r;
+  sg_tuning cur;
+  sg_get_tuning(ctx, &cur);
+  // Candidates: two-level on/off x check interval 8/16/32.  The check interval acts only in
+  // the FP32 form; the two-level sweeps only on single Ball2D scenes in the FP32 form.
+  const bool fp32 = ctx->cfg.precision == SG_PRECISION_FP32_REFINE;
+  const bool two_level_applies = fp32 && ctx->dim == 2;
+  const int intervals[3] = {8, 16, 32};
+  sg_tuning cand[6];
+  bool use[6];
+  for (int i = 0; i < 6; ++i) {
+    cand[i] = cur;
+    cand[i].two_level = i < 3 ? 1 : 0;
+    cand[i].check_interval = intervals[i % 3];
+    use[i] = fp32 && (two_level_applies || i < 3);
+    if (ms_per_step) ms_per_step[i] = std::numeric_limits<double>::quiet_NaN();
+  }
+  if (!fp32) {  // nothing to choose: one timing of the current settings
+    cand[0] = cur;
+    use[0] = true;
+  }
+  auto run = [&](const sg_tuning& t, double* ms) -> int {
+    if (int r = sg_checkpoint_load(ctx, ck.data(), n)) return r;
+    sg_set_tuning(ctx, &t);
+    const auto t0 = std::chrono::steady_clock::now();
+    const int r = sg_step(ctx, first_iteration, (uint32_t)trial_steps, nullptr, nullptr);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
+    if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count() / trial_steps;
+    return SG_OK;
+  };
+  int rc = run(cur, nullptr);  // warm-up: first-use allocations and attributes
+  int chosen = -1;
+  double best_ms = std::numeric_limits<double>::infinity();
+  for (int i = 0; i < 6 && rc == SG_OK; ++i) {
+    if (!use[i]) continue;
+    double ms = 0.0;
+    rc = run(cand[i], &ms);
+    if (rc != SG_OK) break;
+    if (ms_per_step) ms_per_step[i] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      chosen = i;
+    }
+  }
+  // The state the tuning started from, with the fastest settings (or the old ones on failure).
+  const int lr = sg_checkpoint_load(ctx, ck.data(), n);
+  sg_set_tuning(ctx, rc == SG_OK && chosen >= 0 ? &cand[chosen] : &cur);
+  if (best) sg_get_tuning(ctx, best);
+  return rc != SG_OK ? rc : lr;
 }
 
 int sg_set_two_level(sg_ctx* ctx, int32_t on) {

@@ -152,6 +152,10 @@ struct sg_ctx {
   // Two-level FP32 sweeps (spatial patches, one per SM): patch of each body, patch-local
   // index, bodies by patch, contact keys (patch, colour) and the packed order.
   bool patches = true;
+  // Tunables (sg_set_tuning / sg_autotune): base interval of the FP64 checks in the FP32 form,
+  // and the contact count from which a single-scene FP32 solve uses the two-level sweeps.
+  int check_interval = 16;
+  int two_level_min_contacts = 20000;
   uint64_t patched_solves = 0;
   bool last_patched = false;  // the last FP32 solve ran the two-level sweeps
   int last_patch_P = 0, last_patch_Pb = 0;

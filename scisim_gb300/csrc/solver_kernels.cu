@@ -2363,7 +2363,8 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       // Two-level sweeps for large scene steps (the broad phase's grid gives the patches).
       int pmax = 0;
       const int maxP = ctx->num_sms;
-      const bool try_patches = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 && nc >= 20000;
+      const bool try_patches = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 &&
+                               nc >= ctx->two_level_min_contacts;
       int pmaxq = 0, cmax_p = 0, cmax_q = 0, nrest = 0, nrest_bodies = 0;
       PatchSetup hps{};
       if (try_patches) {
@@ -2542,7 +2543,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.body_off = off;
       GB.body_adj = adj;
       GB.nb = nb;
-      GB.eval32 = 16;
+      GB.eval32 = (unsigned)ctx->check_interval;
       if (patched) {
         // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
         // contacts as fit (the patch's first), 32 B each.
@@ -2725,7 +2726,7 @@ int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams
     GB.body_off = off;
     GB.body_adj = adj;
     GB.nb = nb;
-    GB.eval32 = 16;
+    GB.eval32 = (unsigned)ctx->check_interval;
     GsMixedBatchArgs M;
     M.X = B;
     M.pscene = X.pscene;

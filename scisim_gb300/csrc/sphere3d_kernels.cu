@@ -1720,7 +1720,7 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
     B.body_off = off;
     B.body_adj = adj;
     B.nb = nb;
-    B.eval32 = 16;
+    B.eval32 = (unsigned)ctx->check_interval;
     B.work = nullptr;
     k_pack3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), C, A.r, B, B.r);
     k_body32<<<blocks_for(nb), kBlock, 0, s>>>(nb, V, ctx->minv.as<double>(), ctx->Iinv.as<double>(), B.V,
