@@ -419,6 +419,15 @@ def run_ours(args):
     log("preroll %d steps in %.1f s, last step %s" % (args.preroll, time.perf_counter() - t0, pre))
     pw = fast.step(args.warmup) if args.warmup else None
     log("warmup", pw)
+    # Autotuner: each candidate tuning timed over a few steps from this state, which it restores.
+    autotune = None
+    if args.autotune_steps > 0:
+        t0 = time.perf_counter()
+        chosen, tms = fast.autotune(trial_steps=args.autotune_steps, first_iteration=args.preroll + args.warmup + 1)
+        autotune = {"trial_steps": args.autotune_steps, "chosen": chosen,
+                    "ms_per_step": [None if np.isnan(x) else round(float(x), 3) for x in tms],
+                    "candidates": "two-level on: check interval 8, 16, 32; two-level off: 8, 16, 32"}
+        log("autotune in %.1f s: %s" % (time.perf_counter() - t0, autotune))
     q_snap, v_snap = fast.state()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     fast.profile_enable(True)
@@ -552,8 +561,8 @@ def run_ours(args):
                 "plain_fp64_gpu": plain,
                 "warm_over_plain": (value / ws) / plain["value"] if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "gpu_launches": prof["kernel_launches"], "batched": batched, "spheres": spheres,
-                "learned": learned}
+                "gpu_launches": prof["kernel_launches"], "autotune": autotune, "batched": batched,
+                "spheres": spheres, "learned": learned}
         print(json.dumps(line), flush=True)
     fast.close()
     if ws > 1:
@@ -566,6 +575,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--autotune-steps", type=int, default=2, help="steps per autotuner candidate (0 = off)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=262144)
     ap.add_argument("--preroll", type=int, default=600)
