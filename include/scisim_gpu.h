@@ -106,6 +106,19 @@ SG_API int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const do
                               const double* m, const double* I0, int32_t np, const double* plane_x,
                               const double* plane_n);
 
+/* Uploads S independent sphere scenes stepped together (no counterpart in the reference, whose
+ * driver steps one RigidBody3DSim).  Scene s owns bodies body_off[s] .. body_off[s+1]-1 and planes
+ * plane_off[s] .. plane_off[s+1]-1 and has its own mu[s] and CoR[s]; q: [x (3N) | R (9N)],
+ * v: [v (3N) | omega (3N)] over all N = body_off[S] bodies, r, m: N, I0: 3N, planes 3 each.
+ * sg_step then steps every scene as sg_sphere3d_upload + sg_step would step it alone: its own
+ * broad phase, its contacts in the reference's order, and its own Gauss-Seidel termination
+ * (residual, best iterate, iteration count), solved in FP64 for every scene in one launch;
+ * sg_batch2d_scene_stats reports each scene.  The integrator must be SG_SPLIT_HAM. */
+SG_API int sg_sphere3d_batch_upload(sg_ctx* ctx, int32_t n_scenes, const int32_t* body_off, const double* q,
+                                    const double* v, const double* r, const double* m, const double* I0,
+                                    const int32_t* plane_off, const double* plane_x, const double* plane_n,
+                                    const double* mu, const double* CoR);
+
 /* Uploads n_scenes independent Ball2D scenes stepped together (no counterpart in the
  * reference, whose driver steps one Ball2DSim; each scene evolves exactly as
  * Ball2DSim::flow would step it alone, ball2d/Ball2DSim.cpp:305-326).  Scene s owns bodies

@@ -77,6 +77,8 @@ SIGNATURES = {
     "sg_batch2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _ip, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
     "sg_batch2d_scene_stats": (C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_uint32), _dp, _ip]),
     "sg_batch2d_set_capacity": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_sphere3d_batch_upload": (C.c_int, [C.c_void_p, C.c_int32, _ip, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp,
+                                           _dp]),
     "sg_step": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SgStepStats), C.POINTER(_i64)]),
     "sg_flow": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp, C.POINTER(SgStepStats)]),
     "sg_download_state": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -258,6 +260,26 @@ class Context:
         self._keep = (bo, po, q, v, r, m, px, pn, mu, CoR)
         check(lib().sg_batch2d_upload(self._h, S, iptr(bo), dptr(q), dptr(v), dptr(r), dptr(m), iptr(po), dptr(px),
                                       dptr(pn), dptr(mu), dptr(CoR)), "sg_batch2d_upload")
+
+    def upload_sphere3d_batch(self, body_off, q, v, r, m, I0, plane_off, plane_x, plane_n, mu, CoR):
+        """Independent sphere scenes stepped together: q = [x (3N) | R (9N)], v = [v (3N) | w (3N)]
+        over all bodies, global body and plane indices."""
+        bo, po = i32(body_off).reshape(-1), i32(plane_off).reshape(-1)
+        q, v, r, m = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1)
+        I0, px, pn = f64(I0).reshape(-1), f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        mu, CoR = f64(mu).reshape(-1), f64(CoR).reshape(-1)
+        S = bo.shape[0] - 1
+        N = int(bo[-1])
+        if (po.shape[0] != S + 1 or mu.shape[0] != S or CoR.shape[0] != S or r.shape[0] != N or
+                q.shape[0] != 12 * N or v.shape[0] != 6 * N or I0.shape[0] != 3 * N):
+            raise ValueError("inconsistent batch sizes")
+        self.nb = N
+        self.dim = 3
+        self.n_scenes = S
+        self._keep = (bo, po, q, v, r, m, I0, px, pn, mu, CoR)
+        check(lib().sg_sphere3d_batch_upload(self._h, S, iptr(bo), dptr(q), dptr(v), dptr(r), dptr(m), dptr(I0),
+                                             iptr(po), dptr(px), dptr(pn), dptr(mu), dptr(CoR)),
+              "sg_sphere3d_batch_upload")
 
     def batch_set_capacity(self, contacts):
         check(lib().sg_batch2d_set_capacity(self._h, int(contacts)), "sg_batch2d_set_capacity")

@@ -580,12 +580,13 @@ int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_sta
   (void)first_iteration;  // gravity is time independent
   if (int e = check_integrator(ctx)) return e;
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
-  if (ctx->n_scenes > 0) return batch_step(ctx, n_steps, stats, total_contacts);
+  if (ctx->n_scenes > 0 && ctx->dim == 2) return batch_step(ctx, n_steps, stats, total_contacts);
   int64_t tot = 0;
   int worst = SG_OK;
   sg_step_stats st{};
   for (uint32_t k = 0; k < n_steps; ++k) {
-    const int r = ctx->dim == 3 ? sphere3d_step(ctx, &st) : step_once(ctx, &st);
+    const int r = ctx->dim == 3 ? (ctx->n_scenes > 0 ? sphere3d_batch_step(ctx, &st) : sphere3d_step(ctx, &st))
+                                : step_once(ctx, &st);
     if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
     if (r == SG_NOT_CONVERGED) worst = r;
     tot += st.n_contacts;
@@ -700,6 +701,47 @@ int sg_batch2d_scene_stats(sg_ctx* ctx, int32_t* n_contacts, uint32_t* iteration
 int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
                        const double* I0, int32_t np, const double* plane_x, const double* plane_n) {
   return sphere3d_upload_impl(ctx, nb, q, v, r, m, I0, np, plane_x, plane_n);
+}
+
+int sg_sphere3d_batch_upload(sg_ctx* ctx, int32_t S, const int32_t* body_off, const double* q, const double* v,
+                             const double* r, const double* m, const double* I0, const int32_t* plane_off,
+                             const double* plane_x, const double* plane_n, const double* mu, const double* CoR) {
+  if (!ctx || S < 1 || !body_off || !plane_off || !mu || !CoR || body_off[0] != 0 || plane_off[0] != 0) {
+    set_error("sg_sphere3d_batch_upload: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  std::vector<int> sf(S + 1, 0), scene_of;
+  long cells = 0;
+  for (int s = 0; s < S; ++s) {
+    const int ns = body_off[s + 1] - body_off[s], np = plane_off[s + 1] - plane_off[s];
+    if (ns < 0 || np < 0 || !(mu[s] >= 0.0) || !(CoR[s] >= 0.0 && CoR[s] <= 1.0)) {
+      set_error("sg_sphere3d_batch_upload: offsets must not decrease; mu >= 0, 0 <= CoR <= 1 per scene");
+      return SG_BAD_INPUT;
+    }
+    const long f = (long)sf[s] + (long)ns * np;
+    cells += 4L * ns + 64;
+    if (f > (1L << 30) || cells > (1L << 30)) {
+      set_error("sg_sphere3d_batch_upload: batch too large");
+      return SG_CAPACITY;
+    }
+    sf[s + 1] = (int)f;
+    scene_of.insert(scene_of.end(), (size_t)ns, s);
+  }
+  const int N = body_off[S], NP = plane_off[S];
+  if (int e = sphere3d_upload_impl(ctx, N, q, v, r, m, I0, NP, plane_x, plane_n)) return e;
+  ctx->n_scenes = S;
+  ctx->bcells = cells;
+  ctx->bflags = sf[S];
+  const size_t s1 = sizeof(int) * (size_t)(S + 1);
+  if (int e = upload(ctx, ctx->sb_off, body_off, s1)) return e;
+  if (int e = upload(ctx, ctx->sp_off, plane_off, s1)) return e;
+  if (int e = upload(ctx, ctx->sf_off, sf.data(), s1)) return e;
+  if (int e = upload(ctx, ctx->scene_of, scene_of.data(), sizeof(int) * (size_t)std::max(N, 1))) return e;
+  if (int e = upload(ctx, ctx->s_mu, mu, sizeof(double) * (size_t)S)) return e;
+  if (int e = upload(ctx, ctx->s_CoR, CoR, sizeof(double) * (size_t)S)) return e;
+  if (int e = sphere3d_batch_setup(ctx, sf[S], cells)) return e;
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
 }
 
 int64_t sg_sphere3d_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* bases, double* alpha,

@@ -285,6 +285,8 @@ int mlp_targets(sg_ctx* ctx, const ContactProblem& P);
 // RigidBody3D sphere scenes (sphere3d_kernels.cu).
 int sphere3d_update_inertia(sg_ctx* ctx, bool construction);
 int sphere3d_step(sg_ctx* ctx, sg_step_stats* out);
+int sphere3d_batch_setup(sg_ctx* ctx, long flags, long cells);
+int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out);
 
 int wait_timeout_selftest(sg_ctx* ctx);
 

@@ -313,11 +313,13 @@ __global__ void k_cell_scatter3(int n, const int* __restrict__ cell_of, const in
 
 struct Scan3 {
   const double* aabb;
-  const Grid3* g;
+  const Grid3* g;         // one grid, or one per scene (batches)
   const int* cell_start;
   const int* sorted;
   const double* x1;   // q1 positions (3 per body)
   const double* rad;
+  const int* scene_of;    // batches: scene of each body (null for one scene)
+  const int* cell_off;    // batches: first cell of each scene's grid
 };
 
 // AABB::overlaps (rigidbody3d/SpatialGridDetector.cpp:8-25) then SphereSphereConstraint::isActive
@@ -328,7 +330,9 @@ __device__ __forceinline__ void visit_pairs3(const Scan3& s, int i, F&& f) {
   double bi[6];
 #pragma unroll
   for (int a = 0; a < 6; ++a) bi[a] = s.aabb[6 * (size_t)i + a];
-  const Grid3& g = *s.g;
+  const int sc = s.scene_of ? s.scene_of[i] : 0;
+  const Grid3& g = s.g[sc];
+  const int coff = s.cell_off ? s.cell_off[sc] : 0;
   const int cx = cell_coord3(bi[0], g.origin[0], g.h, g.dims[0]);
   const int cy = cell_coord3(bi[1], g.origin[1], g.h, g.dims[1]);
   const int cz = cell_coord3(bi[2], g.origin[2], g.h, g.dims[2]);
@@ -337,7 +341,7 @@ __device__ __forceinline__ void visit_pairs3(const Scan3& s, int i, F&& f) {
   for (int z = max(cz - 1, 0); z <= min(cz + 1, g.dims[2] - 1); ++z)
     for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y)
       for (int x = max(cx - 1, 0); x <= min(cx + 1, g.dims[0] - 1); ++x) {
-        const int cell = x + g.dims[0] * (y + g.dims[1] * z);
+        const int cell = coff + x + g.dims[0] * (y + g.dims[1] * z);
         const int e = s.cell_start[cell + 1];
         for (int p = s.cell_start[cell]; p < e; ++p) {
           const int j = s.sorted[p];
@@ -404,6 +408,161 @@ __global__ void k_plane_write3(int nb, int np, int npairs, const int* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// Batched sphere scenes: scene s owns bodies [sb_off[s], sb_off[s+1]), planes
+// [sp_off[s], sp_off[s+1]) and plane flags [sf_off[s], sf_off[s+1]) (plane-major, n_s per
+// plane); its contacts are [sc_off[s], sc_off[s+1]): its pairs in the order above, then its
+// plane contacts plane-major, as the scene alone would order them.
+
+__global__ void k_fill_int(int n, int v, int* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = v;
+}
+
+// One grid per scene (one block per scene), as k_bounds3 + k_grid3_setup do for one scene.
+__global__ void k_scene_grid3(const int* __restrict__ sb_off, const double* __restrict__ aabb,
+                              Grid3* __restrict__ grids, int* __restrict__ s_cells) {
+  const int sc = blockIdx.x;
+  const int b0 = sb_off[sc], b1 = sb_off[sc + 1];
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY}, e = 0.0;
+  for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double lo = aabb[6 * (size_t)i + a], hi = aabb[6 * (size_t)i + 3 + a];
+      mn[a] = fmin(mn[a], lo);
+      mx[a] = fmax(mx[a], hi);
+      e = fmax(e, hi - lo);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[a] = fmin(mn[a], __shfl_down_sync(0xffffffffu, mn[a], o));
+      mx[a] = fmax(mx[a], __shfl_down_sync(0xffffffffu, mx[a], o));
+    }
+  for (int o = 16; o > 0; o >>= 1) e = fmax(e, __shfl_down_sync(0xffffffffu, e, o));
+  __shared__ double red[7][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    for (int a = 0; a < 3; ++a) {
+      red[a][wid] = mn[a];
+      red[3 + a][wid] = mx[a];
+    }
+    red[6][wid] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int nw = (blockDim.x + 31) >> 5;
+  for (int w = 1; w < nw; ++w) {
+    for (int a = 0; a < 3; ++a) {
+      mn[a] = fmin(mn[a], red[a][w]);
+      mx[a] = fmax(mx[a], red[3 + a][w]);
+    }
+    e = fmax(e, red[6][w]);
+  }
+  const long cap = 4L * (b1 - b0) + 64;
+  double h = e * (1.0 + 0x1p-20) + 1e-300;
+  if (!(h > 0.0) || !isfinite(h)) h = 1.0;
+  double span[3], d[3];
+  for (int a = 0; a < 3; ++a) {
+    span[a] = mx[a] - mn[a];
+    if (!isfinite(span[a]) || span[a] < 0.0) span[a] = 0.0;
+    d[a] = floor(span[a] / h) + 1.0;
+  }
+  while (d[0] * d[1] * d[2] > (double)cap) {
+    h = h * fmax(1.01, cbrt(d[0] * d[1] * d[2] / (double)cap));
+    for (int a = 0; a < 3; ++a) d[a] = floor(span[a] / h) + 1.0;
+  }
+  Grid3& g = grids[sc];
+  for (int a = 0; a < 3; ++a) {
+    g.origin[a] = isfinite(mn[a]) ? mn[a] : 0.0;
+    g.dims[a] = (int)d[a];
+  }
+  g.h = h;
+  g.ncells = (int)(d[0] * d[1] * d[2]);
+  s_cells[sc] = g.ncells;
+}
+
+__global__ void k_cell_count3_b(int n, const int* __restrict__ scene_of, const double* __restrict__ aabb,
+                                const Grid3* __restrict__ grids, const int* __restrict__ cell_off,
+                                int* __restrict__ cell_of, int* __restrict__ cell_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = scene_of[i];
+  const Grid3& g = grids[sc];
+  const int cx = cell_coord3(aabb[6 * (size_t)i], g.origin[0], g.h, g.dims[0]);
+  const int cy = cell_coord3(aabb[6 * (size_t)i + 1], g.origin[1], g.h, g.dims[1]);
+  const int cz = cell_coord3(aabb[6 * (size_t)i + 2], g.origin[2], g.h, g.dims[2]);
+  const int cell = cell_off[sc] + cx + g.dims[0] * (cy + g.dims[1] * cz);
+  cell_of[i] = cell;
+  atomicAdd(&cell_count[cell], 1);
+}
+
+// Pairs of body i into its scene's contact slots (sorted by partner, as k_pair_write3).
+__global__ void k_pair_write3_b(int n, Scan3 s, const int* __restrict__ sb_off, const int* __restrict__ off,
+                                const int* __restrict__ sc_off, int* __restrict__ out_a, int* __restrict__ out_b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = s.scene_of[i];
+  const int base = sc_off[sc] + (off[i] - off[sb_off[sc]]);
+  int c = 0;
+  visit_pairs3(s, i, [&](int j) {
+    int p = base + c;
+    while (p > base && out_b[p - 1] > j) {
+      out_b[p] = out_b[p - 1];
+      --p;
+    }
+    out_b[p] = j;
+    ++c;
+  });
+  for (int k = 0; k < c; ++k) out_a[base + k] = i;
+}
+
+// Plane tests of body i against its scene's planes (flag index sf_off[s] + p_local n_s + i_local).
+__global__ void k_plane_flags3_b(int n, const int* __restrict__ scene_of, const int* __restrict__ sb_off,
+                                 const int* __restrict__ sp_off, const int* __restrict__ sf_off,
+                                 const double* __restrict__ x1, const double* __restrict__ rad,
+                                 const double* __restrict__ px, const double* __restrict__ pn, int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = scene_of[i], b0 = sb_off[sc], ns = sb_off[sc + 1] - b0;
+  const double xi[3] = {x1[3 * (size_t)i], x1[3 * (size_t)i + 1], x1[3 * (size_t)i + 2]};
+  for (int p = sp_off[sc]; p < sp_off[sc + 1]; ++p) {
+    const double d[3] = {xi[0] - px[3 * p], xi[1] - px[3 * p + 1], xi[2] - px[3 * p + 2]};
+    const double nn[3] = {pn[3 * p], pn[3 * p + 1], pn[3 * p + 2]};
+    flag[sf_off[sc] + (long)(p - sp_off[sc]) * ns + (i - b0)] = (dot3(nn, d) <= rad[i]) ? 1 : 0;
+  }
+}
+
+__global__ void k_plane_write3_b(int n, const int* __restrict__ scene_of, const int* __restrict__ sb_off,
+                                 const int* __restrict__ sp_off, const int* __restrict__ sf_off,
+                                 const int* __restrict__ flag, const int* __restrict__ off,
+                                 const int* __restrict__ sc_off, const int* __restrict__ s_npairs,
+                                 int* __restrict__ ia, int* __restrict__ ib) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sc = scene_of[i], b0 = sb_off[sc], ns = sb_off[sc + 1] - b0;
+  const int base = sc_off[sc] + s_npairs[sc] - off[sf_off[sc]];
+  for (int p = sp_off[sc]; p < sp_off[sc + 1]; ++p) {
+    const long t = sf_off[sc] + (long)(p - sp_off[sc]) * ns + (i - b0);
+    if (!flag[t]) continue;
+    const int k = base + off[t];
+    ia[k] = i;
+    ib[k] = -1 - p;
+  }
+}
+
+// Contacts per scene: pairs of its bodies plus its plane contacts.
+__global__ void k_scene_counts3(int S, const int* __restrict__ sb_off, const int* __restrict__ sf_off,
+                                const int* __restrict__ pair_off, const int* __restrict__ plane_off,
+                                int* __restrict__ s_nc, int* __restrict__ s_npairs) {
+  const int sc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sc >= S) return;
+  const int np = pair_off[sb_off[sc + 1]] - pair_off[sb_off[sc]];
+  s_npairs[sc] = np;
+  s_nc[sc] = np + (plane_off[sf_off[sc + 1]] - plane_off[sf_off[sc]]);
+}
+
+// ---------------------------------------------------------------------------
 // Contact assembly.
 struct Assemble3 {
   int nb, nc;
@@ -416,6 +575,9 @@ struct Assemble3 {
   const double* Iinv;
   const double* plane_n;
   double mu, CoR;
+  const int* scene_of;   // batches: scene of each body, and each scene's mu and CoR (null: mu, CoR)
+  const double* s_mu;
+  const double* s_CoR;
   double* E;    // 9 per contact: n, s, t
   double* Aa;   // 6: r_a x s, r_a x t
   double* Ab;   // 6: r_b x s, r_b x t
@@ -532,7 +694,9 @@ __global__ void k_assemble3(Assemble3 A) {
   const double zero[3] = {0.0, 0.0, 0.0};
   const double nrel = -dot3(zero, n);
   const double drel0 = -dot3(zero, s), drel1 = -dot3(zero, t);
-  const double sc = A.CoR * ndotv + nrel;
+  const int scene = A.scene_of ? A.scene_of[a] : -1;
+  const double CoR = scene >= 0 ? A.s_CoR[scene] : A.CoR;
+  const double sc = CoR * ndotv + nrel;
   double w[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) w[j] = ((0.0 + n[j] * sc) + s[j] * drel0) + t[j] * drel1;
@@ -574,7 +738,7 @@ __global__ void k_assemble3(Assemble3 A) {
       }
       Wk[q++] = wij;
     }
-  A.mu_out[k] = A.mu;
+  A.mu_out[k] = scene >= 0 ? A.s_mu[scene] : A.mu;
   // Warm start from alpha = beta = 0 (the 3D geometric map has no impulse cache):
   // r = alpha n + beta0 s + beta1 t, then local r = E^T r.
   double rw[3];
@@ -1132,6 +1296,157 @@ __global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
 }
 
 // ---------------------------------------------------------------------------
+// Batched sphere scenes: one coloured sweep over the contacts of all scenes (scenes share no
+// body, so the global colouring colours every scene), with each scene's own residual, best
+// iterate, convergence test and iteration count, as if every scene were solved alone
+// (Sobogus::solve per RigidBody3DSim).  A converged scene's contacts stop updating; the kernel
+// ends when every scene has converged or at max_iters.  FP64.
+struct Gs3BatchArgs {
+  Gs3Args g;                     // g.r_a / g.r_b: the two snapshot buffers
+  const int* scene_of;           // body -> scene (a contact's scene is that of its first body)
+  const int* sc_off;             // scene contact offsets (S + 1)
+  int S;
+  unsigned long long* err_slot;  // 3 S ordered residual maxima (rotating)
+  double* best;                  // S
+  int* bestbuf;                  // S
+  int* done;                     // S
+  unsigned* iters;               // S
+  int* done_count;
+  unsigned long long* unconverged;
+  unsigned long long* work;      // [1] contact updates, [2] contact evaluations
+};
+
+__device__ __forceinline__ void run_max_atomic3(unsigned long long v, int key, unsigned long long* slots) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+    const int kw = __shfl_down_sync(0xffffffffu, key, o);
+    if (lane + o < 32 && kw == key && w > v) v = w;
+  }
+  const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+  if (key >= 0 && (lane == 0 || kprev != key)) atomicMax(&slots[key], v);
+}
+
+__global__ void __launch_bounds__(kGs3Block, 1) k_gs3_batch(Gs3BatchArgs B) {
+  const Gs3Args& A = B.g;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  const int nc = A.nc, S = B.S;
+  for (int sc = tid; sc < S; sc += nthr) {
+    B.best[sc] = INFINITY;
+    B.bestbuf[sc] = 0;
+    B.iters[sc] = 0;
+    const bool empty = B.sc_off[sc + 1] == B.sc_off[sc];
+    B.done[sc] = empty ? 1 : 0;
+    if (empty) atomicAdd(B.done_count, 1);
+  }
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval_every = A.eval_every ? A.eval_every : 1u;
+  double* bufs[2] = {A.r_a, A.r_b};
+  if (!grid_sync(A.gb, A.spin)) {
+    if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+    return;
+  }
+  unsigned n_eval = 0, it = 0;
+  unsigned long long nupd = 0, nevw = 0;
+  if (*((volatile int*)B.done_count) < S) {
+    for (it = 1; it <= A.max_iters; ++it) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + blockIdx.x + gridDim.x * threadIdx.x; s < e; s += nthr) {
+          const int k = A.perm[s];
+          if (__ldcg(&B.done[B.scene_of[A.C.ia[k]]])) continue;
+          gs_update3(A, k);
+          ++nupd;
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      if (it % eval_every != 0) continue;
+      const int slot = n_eval % 3;
+      unsigned long long* slots = B.err_slot + (size_t)slot * S;
+      const int lane = threadIdx.x & 31;
+      for (int k0 = tid - lane; k0 < nc; k0 += nthr) {
+        const int k = k0 + lane;
+        int key = -1;
+        unsigned long long v = 0ull;
+        if (k < nc) {
+          const int a = A.C.ia[k], b = A.C.ib[k];
+          const int sc = B.scene_of[a];
+          if (!__ldcg(&B.done[sc])) {
+            double E[9], Aa[6], Ab[6], u[3];
+            load_contact(A.C, k, E, Aa, Ab);
+            local_u3(A.C, k, A.V, u, a, b, E, Aa, Ab);
+            const double rk[3] = {__ldcg(&A.r[3 * (size_t)k]), __ldcg(&A.r[3 * (size_t)k + 1]),
+                                  __ldcg(&A.r[3 * (size_t)k + 2])};
+            double* cand = bufs[1 - __ldcg(&B.bestbuf[sc])];
+            cand[3 * (size_t)k] = rk[0];
+            cand[3 * (size_t)k + 1] = rk[1];
+            cand[3 * (size_t)k + 2] = rk[2];
+            v = f64_to_ordered(fb_error_3d(rk, u, A.C.mu[k]));
+            key = sc;
+            ++nevw;
+          }
+        }
+        run_max_atomic3(v, key, slots);
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      unsigned long long* next = B.err_slot + (size_t)((n_eval + 1) % 3) * S;
+      for (int sc = tid; sc < S; sc += nthr) {
+        next[sc] = 0ull;
+        if (B.done[sc]) continue;
+        const double err = ordered_to_f64(__ldcg(&slots[sc]));
+        if (err < B.best[sc]) {
+          B.best[sc] = err;
+          B.bestbuf[sc] ^= 1;
+        }
+        if (err < A.tol) {
+          B.done[sc] = 1;
+          B.iters[sc] = it;
+          atomicAdd(B.done_count, 1);
+        }
+      }
+      ++n_eval;
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      if (*((volatile int*)B.done_count) == S) break;
+    }
+  }
+  // Scenes that did not converge return their best iterate (GaussSeidel: x = x_best).
+  for (int k = tid; k < nc; k += nthr) {
+    const int sc = B.scene_of[A.C.ia[k]];
+    if (__ldcg(&B.done[sc]) || !(__ldcg(&B.best[sc]) < INFINITY)) continue;
+    const double* src = bufs[__ldcg(&B.bestbuf[sc])];
+    for (int j = 0; j < 3; ++j) A.r[3 * (size_t)k + j] = __ldcg(&src[3 * (size_t)k + j]);
+  }
+  for (int sc = tid; sc < S; sc += nthr)
+    if (!__ldcg(&B.done[sc])) B.iters[sc] = A.max_iters;
+  if (tid == 0) *B.unconverged += (unsigned long long)(S - *((volatile int*)B.done_count));
+  atomicAdd(&B.work[1], nupd);
+  atomicAdd(&B.work[2], nevw);
+  if (tid == 0) {
+    A.st->iterations = it > A.max_iters ? A.max_iters : it;
+    A.st->sweeps64 = it > A.max_iters ? A.max_iters : it;
+    A.st->evals = n_eval;
+    A.st->converged = *((volatile int*)B.done_count) == S ? 1 : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Mixed precision for spheres, as k_gs_mixed for discs: FP32 sweeps over colour-packed
 // FP32 copies (contact s of the packed arrays is contact perm[s]), the FP64 image lifted and
 // checked on a growing schedule, FP64 sweeps to finish once FP32 reached tol or its rounding
@@ -1654,6 +1969,8 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   A.plane_n = ctx->plane_n.as<double>();
   A.mu = ctx->cfg.mu;
   A.CoR = ctx->cfg.CoR;
+  A.scene_of = nullptr;
+  A.s_mu = A.s_CoR = nullptr;
   A.E = ctx->E3.as<double>();
   A.Aa = ctx->Aa3.as<double>();
   A.Ab = ctx->Ab3.as<double>();
@@ -1772,6 +2089,240 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   st.error = ctx->h_stats.error;
   st.n_colors = (uint32_t)ctx->h_stats.n_colors;
   // Final map with the post-impact velocity, then the world inertia of the new state.
+  if (int r = splitham(ctx, ctx->v2.as<double>(), false)) return r;
+  std::swap(ctx->q, ctx->q1);
+  std::swap(ctx->v, ctx->v1);
+  if (int r = sphere3d_update_inertia(ctx, false)) return r;
+  ctx->kernel_launches += 2;
+  if (out) *out = st;
+  return st.succeeded ? SG_OK : SG_NOT_CONVERGED;
+}
+
+// ---------------------------------------------------------------------------
+// Batched sphere scenes (sg_sphere3d_batch_upload): buffers, and one step of every scene.
+int sphere3d_batch_setup(sg_ctx* ctx, long flags, long cells) {
+  const int S = ctx->n_scenes, N = ctx->nb;
+  const size_t s1 = sizeof(int) * (size_t)(S + 1), nbs = (size_t)std::max(N, 1);
+  Buf* ints_s1[] = {&ctx->s_cells, &ctx->s_cell_off, &ctx->s_nc, &ctx->s_npairs, &ctx->sc_off, &ctx->prev_sc_off,
+                    &ctx->s_bestbuf, &ctx->s_done, &ctx->s_iters};
+  for (Buf* b : ints_s1)
+    if (int e = grow(*b, s1)) return e;
+  if (int e = grow(ctx->s_grid, sizeof(Grid3) * (size_t)S)) return e;
+  if (int e = grow(ctx->s_best, sizeof(double) * (size_t)S)) return e;
+  if (int e = grow(ctx->s_err, sizeof(unsigned long long) * 3 * (size_t)S)) return e;
+  if (int e = grow(ctx->b_ctl, 4 * sizeof(int))) return e;
+  if (int e = grow(ctx->b_sums, 4 * sizeof(unsigned long long))) return e;
+  if (int e = grow(ctx->b_work, 5 * sizeof(unsigned long long))) return e;
+  if (int e = grow(ctx->cell_count, sizeof(int) * (size_t)(cells + 1))) return e;
+  if (int e = grow(ctx->cell_start, sizeof(int) * (size_t)(cells + 1))) return e;
+  if (int e = grow(ctx->cell_fill, sizeof(int) * (size_t)(cells + 1))) return e;
+  if (int e = grow(ctx->cell_of, sizeof(int) * nbs)) return e;
+  if (int e = grow(ctx->sorted, sizeof(int) * nbs)) return e;
+  if (int e = grow(ctx->pair_cnt, sizeof(int) * (nbs + 1))) return e;
+  if (int e = grow(ctx->pair_off, sizeof(int) * (nbs + 1))) return e;
+  if (int e = grow(ctx->plane_flag, sizeof(int) * (size_t)(flags + 1))) return e;
+  if (int e = grow(ctx->plane_off, sizeof(int) * (size_t)(flags + 1))) return e;
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->sc_off.p, 0, s1, ctx->stream));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_sums.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+  return SG_OK;
+}
+
+int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out) {
+  const int N = ctx->nb, S = ctx->n_scenes;
+  cudaStream_t s = ctx->stream;
+  sg_step_stats st{};
+  if (int r = splitham(ctx, ctx->v.as<double>(), true)) return r;
+  const double* aabb = ctx->aabb.as<double>();
+  const int* sb_off = ctx->sb_off.as<int>();
+  const int* sp_off = ctx->sp_off.as<int>();
+  const int* sf_off = ctx->sf_off.as<int>();
+  const int* scene_of = ctx->scene_of.as<int>();
+  Grid3* grids = ctx->s_grid.as<Grid3>();
+  // Per-scene grids, cells, pairs and planes.
+  k_scene_grid3<<<S, kBlock, 0, s>>>(sb_off, aabb, grids, ctx->s_cells.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->s_cells.as<int>(), ctx->s_cell_off.as<int>(), S)) return r;
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_count.p, 0, sizeof(int) * (size_t)(ctx->bcells + 1), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_fill.p, 0, sizeof(int) * (size_t)(ctx->bcells + 1), s));
+  k_cell_count3_b<<<blocks_for(N), kBlock, 0, s>>>(N, scene_of, aabb, grids, ctx->s_cell_off.as<int>(),
+                                                  ctx->cell_of.as<int>(), ctx->cell_count.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->cell_count.as<int>(), ctx->cell_start.as<int>(), (int)ctx->bcells)) return r;
+  k_cell_scatter3<<<blocks_for(N), kBlock, 0, s>>>(N, ctx->cell_of.as<int>(), ctx->cell_start.as<int>(),
+                                                  ctx->cell_fill.as<int>(), ctx->sorted.as<int>());
+  Scan3 sc{aabb, grids, ctx->cell_start.as<int>(), ctx->sorted.as<int>(), ctx->q1.as<double>(), ctx->r.as<double>(),
+           scene_of, ctx->s_cell_off.as<int>()};
+  k_pair_count3<<<blocks_for(N), kBlock, 0, s>>>(N, sc, ctx->pair_cnt.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->pair_cnt.as<int>(), ctx->pair_off.as<int>(), N)) return r;
+  if (ctx->bflags > 0) {
+    k_plane_flags3_b<<<blocks_for(N), kBlock, 0, s>>>(N, scene_of, sb_off, sp_off, sf_off, ctx->q1.as<double>(),
+                                                     ctx->r.as<double>(), ctx->plane_x.as<double>(),
+                                                     ctx->plane_n.as<double>(), ctx->plane_flag.as<int>());
+    SG_CUDA_TRY(cudaGetLastError());
+    if (int r = scan_exclusive(ctx, ctx->plane_flag.as<int>(), ctx->plane_off.as<int>(), (int)ctx->bflags)) return r;
+  } else {
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->plane_off.p, 0, sizeof(int), s));
+  }
+  k_scene_counts3<<<blocks_for(S), kBlock, 0, s>>>(S, sb_off, sf_off, ctx->pair_off.as<int>(),
+                                                  ctx->plane_off.as<int>(), ctx->s_nc.as<int>(),
+                                                  ctx->s_npairs.as<int>());
+  SG_CUDA_TRY(cudaGetLastError());
+  if (int r = scan_exclusive(ctx, ctx->s_nc.as<int>(), ctx->sc_off.as<int>(), S)) return r;
+  int totals[2] = {0, 0};
+  SG_CUDA_TRY(cudaMemcpyAsync(&totals[0], ctx->sc_off.as<int>() + S, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(&totals[1], ctx->pair_off.as<int>() + N, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  const int nc = totals[0], npairs = totals[1];
+  // splitham 1, scene grid 1 + scan 3, cell count 1 + scan 3, scatter 1, pair count 1 + scan 3,
+  // planes 1 + scan 3, scene counts 1 + scan 3
+  ctx->kernel_launches += 19 + (ctx->bflags > 0 ? 4 : 0);
+  ctx->steps += 1;
+  ctx->contacts_total += (uint64_t)nc;
+  st.n_contacts = nc;
+  st.n_ball_ball = npairs;
+  st.n_ball_plane = nc - npairs;
+  ctx->last_nc = nc;
+  ctx->last_nbb = npairs;
+  if (nc == 0) {
+    k_fill_int<<<blocks_for(S), kBlock, 0, s>>>(S, 1, ctx->s_done.as<int>());
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_iters.p, 0, sizeof(unsigned) * (size_t)S, s));
+    std::swap(ctx->q, ctx->q1);
+    std::swap(ctx->v, ctx->v1);
+    if (int r = sphere3d_update_inertia(ctx, false)) return r;
+    ctx->kernel_launches += 2;
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    st.succeeded = 1;
+    if (out) *out = st;
+    return SG_OK;
+  }
+  if (int r = ensure_contacts3(ctx, nc)) return r;
+  int* ia = ctx->ia.as<int>();
+  int* ib = ctx->ib.as<int>();
+  const int* sc_off = ctx->sc_off.as<int>();
+  k_pair_write3_b<<<blocks_for(N), kBlock, 0, s>>>(N, sc, sb_off, ctx->pair_off.as<int>(), sc_off, ia, ib);
+  if (ctx->bflags > 0)
+    k_plane_write3_b<<<blocks_for(N), kBlock, 0, s>>>(N, scene_of, sb_off, sp_off, sf_off, ctx->plane_flag.as<int>(),
+                                                     ctx->plane_off.as<int>(), sc_off, ctx->s_npairs.as<int>(), ia, ib);
+  SG_CUDA_TRY(cudaGetLastError());
+  Assemble3 A;
+  A.nb = N;
+  A.nc = nc;
+  A.ia = ia;
+  A.ib = ib;
+  A.q0 = ctx->q.as<double>();
+  A.v0 = ctx->v.as<double>();
+  A.rad = ctx->r.as<double>();
+  A.minv = ctx->minv.as<double>();
+  A.Iinv = ctx->Iinv.as<double>();
+  A.plane_n = ctx->plane_n.as<double>();
+  A.mu = ctx->cfg.mu;
+  A.CoR = ctx->cfg.CoR;
+  A.scene_of = scene_of;
+  A.s_mu = ctx->s_mu.as<double>();
+  A.s_CoR = ctx->s_CoR.as<double>();
+  A.E = ctx->E3.as<double>();
+  A.Aa = ctx->Aa3.as<double>();
+  A.Ab = ctx->Ab3.as<double>();
+  A.c = ctx->c3.as<double>();
+  A.W = ctx->W3.as<double>();
+  A.mu_out = ctx->mu.as<double>();
+  A.r = ctx->r3.as<double>();
+  k_assemble3<<<blocks_for(nc), kBlock, 0, s>>>(A);
+  SG_CUDA_TRY(cudaGetLastError());
+  // Solve every scene to its own tolerance (FP64).
+  if (int r = ensure_solver_capacity(ctx, N, nc)) return r;
+  if (int r = grow(ctx->vrun3, sizeof(double4_32a) * 2 * (size_t)N)) return r;
+  if (int r = grow(ctx->v2, sizeof(double) * 6 * (size_t)N)) return r;
+  if (int r = prepare_contact_graph(ctx, N, nc, ia, ib)) return r;
+  const int* off = ctx->body_off.as<int>();
+  const int* adj = ctx->body_adj.as<int>();
+  Contacts3 C{ia, ib, A.E, A.Aa, A.Ab, A.c, A.W, A.mu_out};
+  double4_32a* V = ctx->vrun3.as<double4_32a>();
+  k_vel_init3<<<blocks_for(N), kBlock, 0, s>>>(N, off, adj, C, A.r, ctx->v.as<double>(), ctx->minv.as<double>(),
+                                               ctx->Iinv.as<double>(), V);
+  SG_CUDA_TRY(cudaGetLastError());
+  SolveStats* sst = ctx->stats.as<SolveStats>();
+  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->s_err.p, 0, sizeof(unsigned long long) * 3 * (size_t)S, s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_ctl.p, 0, 4 * sizeof(int), s));
+  SG_CUDA_TRY(cudaMemsetAsync(ctx->b_work.p, 0, 5 * sizeof(unsigned long long), s));
+  Gs3BatchArgs B;
+  B.g.nc = nc;
+  B.g.C = C;
+  B.g.minv = ctx->minv.as<double>();
+  B.g.Iinv = ctx->Iinv.as<double>();
+  B.g.perm = ctx->perm.as<int>();
+  B.g.r = A.r;
+  B.g.r_a = ctx->r3a.as<double>();
+  B.g.r_b = ctx->r3b.as<double>();
+  B.g.V = V;
+  B.g.st = sst;
+  B.g.gb = gb;
+  B.g.spin = ctx->spin_limit;
+  B.g.tol = ctx->cfg.tol;
+  B.g.max_iters = ctx->cfg.max_iters;
+  B.g.eval_every = ctx->cfg.eval_every;
+  B.scene_of = scene_of;
+  B.sc_off = sc_off;
+  B.S = S;
+  B.err_slot = ctx->s_err.as<unsigned long long>();
+  B.best = ctx->s_best.as<double>();
+  B.bestbuf = ctx->s_bestbuf.as<int>();
+  B.done = ctx->s_done.as<int>();
+  B.iters = ctx->s_iters.as<unsigned>();
+  B.done_count = ctx->b_ctl.as<int>();
+  B.unconverged = ctx->b_sums.as<unsigned long long>() + 1;
+  B.work = ctx->b_work.as<unsigned long long>();
+  {
+    void* args[] = {&B};
+    const int grid = coop_grid(ctx, k_gs3_batch, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_batch, grid, kGs3Block, args, s));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+  }
+  k_final_vel3<<<blocks_for(N), kBlock, 0, s>>>(N, off, adj, C, A.r, ctx->v.as<double>(), ctx->m.as<double>(),
+                                                ctx->minv.as<double>(), ctx->Iw.as<double>(), ctx->Iinv.as<double>(),
+                                                ctx->v2.as<double>());
+  k_extract3<<<blocks_for(nc), kBlock, 0, s>>>(nc, A.E, A.r, ctx->ab3.as<double>());
+  SG_CUDA_TRY(cudaGetLastError());
+  unsigned long long work[5];
+  std::vector<double> best(S);
+  std::vector<int> done(S);
+  SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, sst, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(work, ctx->b_work.p, sizeof(work), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(best.data(), ctx->s_best.p, sizeof(double) * S, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(done.data(), ctx->s_done.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  // pair write, plane write, assemble, vel init, gs, final velocity, extract
+  ctx->kernel_launches += 6 + (ctx->bflags > 0 ? 1 : 0);
+  if (ctx->h_stats.status == SG_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its spin limit");
+    return SG_DEVICE_TIMEOUT;
+  }
+  if (ctx->h_stats.status == SG_CAPACITY) {
+    set_error("contact colouring exceeded 64 colours or its round limit");
+    return SG_CAPACITY;
+  }
+  ctx->gs_launches += 1;
+  ctx->contact_sweeps += work[1];
+  ctx->contact_evals += work[2];
+  if (ctx->profile) {
+    float ms = 0.f;
+    SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
+    ctx->gs_ms += ms;
+  }
+  int all_done = 1;
+  double worst = 0.0;
+  for (int k = 0; k < S; ++k) {
+    all_done &= done[k] ? 1 : 0;
+    if (best[k] < INFINITY && best[k] > worst) worst = best[k];
+  }
+  st.iterations = ctx->h_stats.iterations;
+  st.succeeded = all_done;
+  st.error = worst;
+  st.n_colors = (uint32_t)ctx->h_stats.n_colors;
   if (int r = splitham(ctx, ctx->v2.as<double>(), false)) return r;
   std::swap(ctx->q, ctx->q1);
   std::swap(ctx->v, ctx->v1);

@@ -208,6 +208,53 @@ def sphere_pile(n: int = 65536, seed: int = 5, width: float = 6.0, depth: float 
                 gravity=(0.0, -9.81, 0.0), CoR=0.2, mu=0.6, tol=1e-6, max_iters=5000, name="sphere_pile_%d" % n)
 
 
+def sphere_batch(n_scenes: int = 256, seed: int = 4, nmin: int = 64, nmax: int = 1024):
+    """Independent sphere piles (C5's batched configuration): sphere counts log-uniform in
+    [nmin, nmax], each a sphere_pile of its own (footprint sized to about 8 layers), per-scene
+    mu ~ U[0.2, 0.8] and CoR ~ U[0, 0.4]; SplitHam dt 0.004, gravity (0, -9.81, 0).  Every scene
+    lives in its own coordinates.  q = [x (3N) | R (9N)], v = [v (3N) | omega (3N)] over all N."""
+    rng = np.random.default_rng(seed)
+    counts = np.rint(np.exp(rng.uniform(math.log(nmin), math.log(nmax), n_scenes))).astype(np.int64)
+    body_off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    plane_off = (5 * np.arange(n_scenes + 1)).astype(np.int32)
+    xs, Rs, vs, ws, rs, ms, i0s, px, pn = [], [], [], [], [], [], [], [], []
+    for s in range(n_scenes):
+        n = int(counts[s])
+        side = max(2, int(math.ceil(math.sqrt(n / 8.0))))
+        one = sphere_pile(n=n, seed=int(rng.integers(1 << 30)), width=0.2 * side, depth=0.2 * side)
+        xs.append(one["q"][:3 * n])
+        Rs.append(one["q"][3 * n:])
+        vs.append(one["v"][:3 * n])
+        ws.append(one["v"][3 * n:])
+        rs.append(one["r"])
+        ms.append(one["m"])
+        i0s.append(one["I0"])
+        px.append(one["plane_x"])
+        pn.append(one["plane_n"])
+    q = np.concatenate(xs + Rs)
+    v = np.concatenate(vs + ws)
+    mu = rng.uniform(0.2, 0.8, n_scenes)
+    CoR = rng.uniform(0.0, 0.4, n_scenes)
+    return dict(body_off=body_off, plane_off=plane_off, q=q, v=v, r=np.concatenate(rs), m=np.concatenate(ms),
+                I0=np.concatenate(i0s), plane_x=np.concatenate(px), plane_n=np.concatenate(pn), mu=mu, CoR=CoR,
+                dt=0.004, gravity=(0.0, -9.81, 0.0), tol=1e-6, max_iters=5000, name="sphere_batch_%d" % n_scenes)
+
+
+def batch_scene3(b, s, q=None, v=None):
+    """Scene s of a sphere batch as a standalone sphere scene (local layout and indices); q, v
+    default to the batch's initial state."""
+    q = b["q"] if q is None else q
+    v = b["v"] if v is None else v
+    N = int(b["body_off"][-1])
+    b0, b1 = int(b["body_off"][s]), int(b["body_off"][s + 1])
+    p0, p1 = int(b["plane_off"][s]), int(b["plane_off"][s + 1])
+    qs = np.concatenate([q[3 * b0:3 * b1], q[3 * N + 9 * b0:3 * N + 9 * b1]])
+    vs = np.concatenate([v[3 * b0:3 * b1], v[3 * N + 3 * b0:3 * N + 3 * b1]])
+    return dict(q=qs, v=vs, r=b["r"][b0:b1], m=b["m"][b0:b1], I0=b["I0"][3 * b0:3 * b1],
+                plane_x=b["plane_x"][p0:p1], plane_n=b["plane_n"][p0:p1], mu=float(b["mu"][s]),
+                CoR=float(b["CoR"][s]), dt=b["dt"], gravity=b["gravity"])
+
+
 def min_gap(q, r, plane_x=None, plane_n=None):
     """Smallest pairwise gap (brute force on a grid; for tests of the generators)."""
     q = np.asarray(q).reshape(-1, 2)

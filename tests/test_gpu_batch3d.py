@@ -1,0 +1,79 @@
+"""Batched sphere scenes (sg_sphere3d_batch_upload) against the oracle stepping each scene alone.
+
+Bars, per scene and per step, with the oracle replaying the scene's part of the GPU's colour order
+from the GPU's state: the same contact count, the same Gauss-Seidel sweep count and convergence,
+positions and linear velocities bit-exact, orientations and angular velocities within 1e-13 (as
+for single sphere scenes: CUDA's sin/cos and the host's may differ in the last bit).
+"""
+import numpy as np
+import pytest
+
+from scisim_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _split(b, q, v, s):
+    x = scenes.batch_scene3(b, s, q, v)
+    return x["q"], x["v"]
+
+
+def test_sphere_batch_matches_scenes_alone(gpulib, oracle):
+    b = scenes.sphere_batch(n_scenes=6, seed=11, nmin=40, nmax=300)
+    S = len(b["mu"])
+    kw = dict(dt=b["dt"], gravity=b["gravity"], tol=1e-9, max_iters=300)
+    ctx = gpulib.Context(integrator=gpulib.SPLIT_HAM, mu=0.5, CoR=0.0, **kw)
+    ctx.upload_sphere3d_batch(b["body_off"], b["q"], b["v"], b["r"], b["m"], b["I0"], b["plane_off"], b["plane_x"],
+                              b["plane_n"], b["mu"], b["CoR"])
+    sims = []
+    for s in range(S):
+        x = scenes.batch_scene3(b, s)
+        sims.append(oracle.Sphere3D(x["q"], x["v"], x["r"], x["m"], x["I0"], x["plane_x"], x["plane_n"],
+                                    mu=x["mu"], CoR=x["CoR"], **kw))
+    checked_contacts = 0
+    for step in range(40):
+        q0, v0 = ctx.state()
+        ctx.step(1, first_iteration=step + 1)
+        stats = ctx.batch_scene_stats()
+        order, _ = ctx.last_solve_order()
+        coff = np.concatenate([[0], np.cumsum(stats["n_contacts"])])
+        q1, v1 = ctx.state()
+        for s in range(S):
+            o = sims[s]
+            if step > 0:
+                o.set_state(*_split(b, q0, v0, s))
+            c0, c1 = int(coff[s]), int(coff[s + 1])
+            if c1 > c0:
+                o.set_next_order(order[(order >= c0) & (order < c1)] - c0)
+            ost = o.step()
+            assert ost["n_contacts"] == c1 - c0, (step, s)
+            checked_contacts += c1 - c0
+            if c1 > c0:
+                assert stats["iterations"][s] == ost["iterations"], (step, s)
+                assert bool(stats["succeeded"][s]) == bool(ost["succeeded"]), (step, s)
+            gq, gv = _split(b, q1, v1, s)
+            oq, ov = o.state()
+            n = int(b["body_off"][s + 1] - b["body_off"][s])
+            assert np.array_equal(gq[:3 * n], oq[:3 * n]), ("positions", step, s)
+            assert np.array_equal(gv[:3 * n], ov[:3 * n]), ("velocities", step, s)
+            assert np.abs(gq[3 * n:] - oq[3 * n:]).max() <= 1e-13, ("orientations", step, s)
+            assert np.abs(gv[3 * n:] - ov[3 * n:]).max() <= 1e-13, ("angular velocities", step, s)
+    assert checked_contacts > 1000
+    ctx.close()
+
+
+def test_sphere_batch_c5_shape(gpulib):
+    """256 scenes of 64-1,024 spheres: every scene that reports convergence meets the tolerance,
+    and the per-scene contact counts add up to the step's."""
+    b = scenes.sphere_batch(n_scenes=256, seed=4)
+    ctx = gpulib.Context(integrator=gpulib.SPLIT_HAM, dt=b["dt"], gravity=b["gravity"], tol=1e-6, max_iters=500)
+    ctx.upload_sphere3d_batch(b["body_off"], b["q"], b["v"], b["r"], b["m"], b["I0"], b["plane_off"], b["plane_x"],
+                              b["plane_n"], b["mu"], b["CoR"])
+    for step in range(30):
+        st = ctx.step(1, first_iteration=step + 1)
+    stats = ctx.batch_scene_stats()
+    assert int(np.sum(stats["n_contacts"])) == st["n_contacts"] > 0
+    conv = stats["succeeded"].astype(bool)
+    assert conv.sum() > 0
+    assert np.all(stats["error"][conv] < 1e-6)
+    ctx.close()
