@@ -290,6 +290,70 @@ def batch_leg(args, torch, local, flush):
     return out
 
 
+def sphere_batch_leg(args, torch, local, flush):
+    """Batched sphere scenes (C5's 256 scenes of 64-1,024 spheres, FP64, no impulse cache) stepped
+    together, against the plain solver on a sample of the same scenes (one context per scene,
+    FP64), over the same steps from the same state."""
+    from scisim_gb300 import _lib, scenes
+    b = scenes.sphere_batch(n_scenes=args.sphere_batch_scenes)
+    S, N = len(b["mu"]), int(b["body_off"][-1])
+    kw = dict(dt=b["dt"], gravity=b["gravity"], tol=1e-6, max_iters=args.preroll_iters, device=local,
+              integrator=_lib.SPLIT_HAM)
+    ctx = _lib.Context(**kw)
+    ctx.upload_sphere3d_batch(b["body_off"], b["q"], b["v"], b["r"], b["m"], b["I0"], b["plane_off"], b["plane_x"],
+                              b["plane_n"], b["mu"], b["CoR"])
+    t0 = time.perf_counter()
+    ctx.step(args.sphere_batch_preroll)
+    ctx.reconfigure(max_iters=5000)
+    ctx.step(1)  # warm-up at the full settings
+    log("sphere batch preroll %d + 1 steps in %.1f s" % (args.sphere_batch_preroll, time.perf_counter() - t0))
+    q0, v0 = ctx.state()
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=local)
+    ctx.profile_read(reset=True)
+    flush.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st = ctx.step(args.sphere_batch_steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    prof = ctx.profile_read(reset=True)
+    stats = ctx.batch_scene_stats()
+    value = st["total_contacts"] / (ms / 1e3)
+    log("sphere batch: %d scenes, %d spheres, %d contact-steps in %.1f ms" % (S, N, st["total_contacts"], ms))
+    rng = np.random.default_rng(0)
+    pick = rng.choice(S, min(args.batch_plain_scenes, S), replace=False)
+    pc, pms = 0, 0.0
+    for sc in pick:
+        x = scenes.batch_scene3(b, sc, q0, v0)
+        c = _lib.Context(mu=x["mu"], CoR=x["CoR"], **dict(kw, max_iters=5000))
+        c.upload_sphere3d(x["q"], x["v"], x["r"], x["m"], x["I0"], x["plane_x"], x["plane_n"])
+        cs = torch.cuda.ExternalStream(c.stream_ptr(), device=local)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(cs)
+        r = c.step(args.sphere_batch_steps)
+        a1.record(cs)
+        a1.synchronize()
+        pc += r["total_contacts"]
+        pms += a0.elapsed_time(a1)
+        c.close()
+    plain = pc / (pms / 1e3) if pms > 0 else None
+    out = {"workload": "sphere_batch_%d" % S, "scenes": S, "spheres": N, "value": value, "unit": UNIT,
+           "steps": args.sphere_batch_steps,
+           "timed_steps": [args.sphere_batch_preroll + 2, args.sphere_batch_preroll + 1 + args.sphere_batch_steps],
+           "ms_per_step": ms / args.sphere_batch_steps, "contacts_per_step": st["total_contacts"] / args.sphere_batch_steps,
+           "form": "batched, one launch per step for all scenes, FP64, each scene to its own tolerance",
+           "scenes_converged_last_step": int(stats["succeeded"].sum()),
+           "gs_iterations_mean_last_step": float(stats["iterations"].mean()),
+           "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
+                              "form": "one context per scene, FP64, same steps from the same state"},
+           "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"]}
+    ctx.close()
+    return out
+
+
 def sphere_leg(args, torch, local, flush):
     """RigidBody3D spheres (65,536 by default): FP64 3x3-block solve, no impulse cache (the
     reference's 3D geometric map keeps none), after a pre-roll with capped solves."""
@@ -537,6 +601,10 @@ def run_ours(args):
     if rank == 0 and args.spheres > 0:
         spheres = sphere_leg(args, torch, local, flush)
         log("spheres:", spheres)
+    sphere_batch = None
+    if rank == 0 and args.sphere_batch_scenes > 0:
+        sphere_batch = sphere_batch_leg(args, torch, local, flush)
+        log("sphere batch:", sphere_batch)
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
@@ -562,7 +630,7 @@ def run_ours(args):
                 "warm_over_plain": (value / ws) / plain["value"] if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": prof["kernel_launches"], "autotune": autotune, "batched": batched,
-                "spheres": spheres, "learned": learned}
+                "spheres": spheres, "sphere_batch": sphere_batch, "learned": learned}
         print(json.dumps(line), flush=True)
     fast.close()
     if ws > 1:
@@ -591,6 +659,9 @@ def main():
     ap.add_argument("--spheres", type=int, default=65536, help="sphere leg (0 = skip)")
     ap.add_argument("--sphere-preroll", type=int, default=100)
     ap.add_argument("--sphere-steps", type=int, default=3)
+    ap.add_argument("--sphere-batch-scenes", type=int, default=256, help="sphere-batch leg (0 = skip)")
+    ap.add_argument("--sphere-batch-preroll", type=int, default=100)
+    ap.add_argument("--sphere-batch-steps", type=int, default=3)
     ap.add_argument("--mlp-hopper", type=int, default=0, help="learned-warm-start study on a hopper (0 = skip)")
     ap.add_argument("--mlp-preroll", type=int, default=1500)
     ap.add_argument("--mlp-record-steps", type=int, default=100)
