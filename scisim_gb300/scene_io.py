@@ -1,0 +1,243 @@
+"""Reader of SCISim's XML scene files, for the scenes this library steps.
+
+Ball2D (`<ball2d_scene>`, ball2dutils/Ball2DSceneParser.cpp) and RigidBody3D sphere scenes
+(`<rigidbody3d_scene>`, rigidbody3dutils/RigidBody3DSceneParser.cpp) with the elements of the contact
+path: integrator, `sobogus_friction_solver` with geometric staggering, gravity, static planes, balls
+or spheres.  Values are read the way the reference reads them: scalars as C++ stream extraction of
+a decimal (Python's float of the same text rounds the same way), the time step as an exact rational
+(`Rational<intmax_t>` from a decimal or `a/b`, Rational.h:204-260) taken as numerator / denominator.
+Elements of features outside the contact path (drums, portals, penalty forces, other solvers and
+staggerings, fixed bodies, scripting) raise SceneError naming them, instead of being dropped.
+"""
+from __future__ import annotations
+
+import math
+import os
+import xml.etree.ElementTree as ET
+from fractions import Fraction
+
+import numpy as np
+
+from . import scenes
+
+CACHE_MODES = {"none": 0, "normal": 1, "normal_and_friction": 2}
+
+
+class SceneError(ValueError):
+    pass
+
+
+def _root(source):
+    if isinstance(source, (str, os.PathLike)) and os.path.exists(source):
+        return ET.parse(source).getroot()
+    return ET.fromstring(source)
+
+
+def _attr(node, name, tag):
+    v = node.get(name)
+    if v is None:
+        raise SceneError("%s: missing attribute %s" % (tag, name))
+    return v
+
+
+def _scalar(node, name, tag):
+    try:
+        return float(_attr(node, name, tag))
+    except ValueError as e:
+        raise SceneError("%s: %s is not a scalar" % (tag, name)) from e
+
+
+def _vector(node, name, n, tag):
+    parts = _attr(node, name, tag).split()
+    if len(parts) != n:
+        raise SceneError("%s: %s needs %d scalars" % (tag, name, n))
+    return [float(p) for p in parts]
+
+
+def _bool(node, name, tag):
+    v = _attr(node, name, tag).strip()
+    if v not in ("0", "1"):
+        raise SceneError("%s: %s must be 0 or 1" % (tag, name))
+    return v == "1"
+
+
+def rational(text: str) -> Fraction:
+    """Rational<intmax_t> extraction (scisim/Math/Rational.h:204-260): a decimal or a/b, exact."""
+    t = text.strip().replace(" ", "")
+    if t.count("/") == 1 and "." not in t:
+        a, b = t.split("/")
+        return Fraction(int(a), int(b))
+    if t.count("/") > 0:
+        raise SceneError("dt: malformed rational %r" % text)
+    return Fraction(t)
+
+
+def _check_tags(root, allowed):
+    bad = sorted({c.tag for c in root} - set(allowed))
+    if bad:
+        raise SceneError("unsupported scene elements for this library's contact path: " + ", ".join(bad))
+
+
+def _solver(root, tag_3d=False):
+    nodes = root.findall("sobogus_friction_solver")
+    if len(nodes) != 1:
+        raise SceneError("needs exactly one sobogus_friction_solver")
+    nd = nodes[0]
+    tag = "sobogus_friction_solver"
+    stag = _attr(nd, "staggering", tag)
+    if stag != "geometric":
+        raise SceneError("%s: staggering %r is not supported (geometric only)" % (tag, stag))
+    cache = _attr(nd, "cache_impulses", tag)
+    if cache not in CACHE_MODES:
+        raise SceneError("%s: cache_impulses must be none, normal or normal_and_friction" % tag)
+    out = dict(mu=_scalar(nd, "mu", tag), CoR=_scalar(nd, "CoR", tag), tol=_scalar(nd, "tol", tag),
+               max_iters=int(_attr(nd, "max_iters", tag)), eval_every=int(_attr(nd, "eval_every", tag)),
+               cache_mode=CACHE_MODES[cache])
+    if tag_3d:
+        out["cache_mode"] = 0  # the 3D geometric map keeps no cache (RigidBody3DSceneParser.cpp:1877-1880)
+    return out
+
+
+def _dt(root, types):
+    nodes = root.findall("integrator")
+    if len(nodes) != 1:
+        raise SceneError("needs exactly one integrator")
+    nd = nodes[0]
+    kind = _attr(nd, "type", "integrator")
+    if kind not in types:
+        raise SceneError("integrator type %r is not supported (%s)" % (kind, ", ".join(types)))
+    dt = rational(_attr(nd, "dt", "integrator"))
+    if dt <= 0:
+        raise SceneError("integrator: dt must be positive")
+    return kind, dt
+
+
+def _end_time(root):
+    nd = root.find("end_time")
+    return None if nd is None else _scalar(nd, "t", "end_time")
+
+
+def load_ball2d_scene(source) -> dict:
+    """A `<ball2d_scene>` file or text as arrays and settings (Ball2DSceneParser.cpp:1486-1651).
+    Returns q, v (2 per ball), r, m, plane_x, plane_n (2 per plane), dt (float) and dt_rational,
+    integrator ('verlet' / 'symplectic_euler'), gravity, mu, CoR, tol, max_iters, eval_every,
+    cache_mode, end_time (None if absent)."""
+    root = _root(source)
+    if root.tag != "ball2d_scene":
+        raise SceneError("not a ball2d_scene")
+    _check_tags(root, ("camera", "end_time", "integrator", "sobogus_friction_solver", "gravity", "static_plane",
+                       "ball"))
+    kind, dt = _dt(root, ("verlet", "symplectic_euler"))
+    grav = root.findall("gravity")
+    if len(grav) > 1:
+        raise SceneError("more than one gravity force (their sum would round differently)")
+    g = (0.0, 0.0) if not grav else (_scalar(grav[0], "fx", "gravity"), _scalar(grav[0], "fy", "gravity"))
+    px, pn = [], []
+    for nd in root.findall("static_plane"):
+        px.append(_vector(nd, "x", 2, "static_plane"))
+        pn.append(_vector(nd, "n", 2, "static_plane"))
+    q, v, r, m = [], [], [], []
+    for nd in root.findall("ball"):
+        if _bool(nd, "fixed", "ball"):
+            raise SceneError("ball: fixed balls are not supported")
+        q += [_scalar(nd, "x", "ball"), _scalar(nd, "y", "ball")]
+        v += [_scalar(nd, "vx", "ball"), _scalar(nd, "vy", "ball")]
+        m.append(_scalar(nd, "m", "ball"))
+        r.append(_scalar(nd, "r", "ball"))
+    out = dict(q=np.array(q, np.float64), v=np.array(v, np.float64), r=np.array(r, np.float64),
+               m=np.array(m, np.float64), plane_x=np.array(px, np.float64).reshape(-1, 2),
+               plane_n=np.array(pn, np.float64).reshape(-1, 2), dt=float(dt), dt_rational=dt, integrator=kind,
+               gravity=g, end_time=_end_time(root))
+    out.update(_solver(root))
+    return out
+
+
+def load_rigidbody3d_scene(source) -> dict:
+    """A `<rigidbody3d_scene>` of spheres as arrays and settings (RigidBody3DSceneParser.cpp), for
+    the split_ham integrator and geometric staggering.  Bodies: `rigid_body_with_density` with a
+    sphere geometry, mass and inertia from rho (RigidBodySphere::computeMassAndInertia), identity
+    orientation (an `R` attribute, an Eigen AngleAxis, is not supported).  Returns q = [x | R],
+    v = [v | omega], r, m, I0, plane_x, plane_n (3 per plane), dt, gravity and the solver settings."""
+    root = _root(source)
+    if root.tag != "rigidbody3d_scene":
+        raise SceneError("not a rigidbody3d_scene")
+    _check_tags(root, ("camera_perspective", "camera_orthographic", "end_time", "integrator",
+                       "sobogus_friction_solver", "near_earth_gravity", "static_plane", "geometry",
+                       "rigid_body_with_density", "static_plane_renderer"))
+    kind, dt = _dt(root, ("split_ham",))
+    grav = root.findall("near_earth_gravity")
+    if len(grav) > 1:
+        raise SceneError("more than one near_earth_gravity force")
+    g = (0.0, 0.0, 0.0) if not grav else tuple(_vector(grav[0], "f", 3, "near_earth_gravity"))
+    px, pn = [], []
+    for nd in root.findall("static_plane"):
+        px.append(_vector(nd, "x", 3, "static_plane"))
+        pn.append(_vector(nd, "n", 3, "static_plane"))
+    geos = []
+    for nd in root.findall("geometry"):
+        if _attr(nd, "type", "geometry") != "sphere":
+            raise SceneError("geometry: only spheres are supported")
+        geos.append(_scalar(nd, "r", "geometry"))
+    xs, vs, ws, rs, rhos = [], [], [], [], []
+    for nd in root.findall("rigid_body_with_density"):
+        tag = "rigid_body_with_density"
+        if _bool(nd, "fixed", tag):
+            raise SceneError("%s: fixed bodies are not supported" % tag)
+        if nd.get("R") is not None:
+            raise SceneError("%s: an initial orientation (R) is not supported" % tag)
+        gi = int(_attr(nd, "geo_idx", tag))
+        if gi < 0:
+            gi += len(geos)
+        if not 0 <= gi < len(geos):
+            raise SceneError("%s: invalid geo_idx" % tag)
+        xs.append(_vector(nd, "x", 3, tag))
+        vs.append(_vector(nd, "v", 3, tag))
+        ws.append(_vector(nd, "omega", 3, tag))
+        rs.append(geos[gi])
+        rhos.append(_scalar(nd, "rho", tag))
+    n = len(xs)
+    r = np.array(rs, np.float64)
+    m = np.empty(n)
+    i0 = np.empty(n)
+    for k in range(n):
+        mk, ik = scenes.sphere_mass_inertia(np.array([r[k]]), rhos[k])
+        m[k], i0[k] = mk[0], ik[0]
+    x = np.array(xs, np.float64).reshape(-1) + 0.0  # x + CM with CM = 0 for a sphere
+    q = np.concatenate([x, np.tile(np.eye(3).reshape(-1), n)])
+    v = np.concatenate([np.array(vs, np.float64).reshape(-1), np.array(ws, np.float64).reshape(-1)])
+    out = dict(q=q, v=v, r=r, m=m, I0=np.repeat(i0, 3), plane_x=np.array(px, np.float64).reshape(-1, 3),
+               plane_n=np.array(pn, np.float64).reshape(-1, 3), dt=float(dt), dt_rational=dt, integrator=kind,
+               gravity=g, end_time=_end_time(root))
+    out.update(_solver(root, tag_3d=True))
+    return out
+
+
+def steps_to(end_time: float, dt: Fraction) -> int:
+    """Steps a driver takes to reach end_time (ceil of end_time / dt in exact arithmetic)."""
+    return int(math.ceil(Fraction(end_time) / dt))
+
+
+def ball2d_objects(scene: dict):
+    """The reference's objects for a loaded Ball2D scene, as ball2d_cli builds them: the simulation,
+    its unconstrained map, the Sobogus solver and the geometric impact-friction map.  Step with
+    sim.flow(iteration, scene['dt'], umap, scene['CoR'], scene['mu'], solver, ifmap)."""
+    from .ball2d import (Ball2DSim, Ball2DState, GeometricImpactFrictionMap, ImpulsesToCache, Sobogus,
+                         SobogusSolverType, StaticPlane, SymplecticEulerMap, VerletMap)
+    planes = [StaticPlane(x, n) for x, n in zip(scene["plane_x"], scene["plane_n"])]
+    sim = Ball2DSim(Ball2DState(scene["q"], scene["v"], scene["r"], scene["m"], planes), gravity=scene["gravity"])
+    umap = VerletMap() if scene["integrator"] == "verlet" else SymplecticEulerMap()
+    solver = Sobogus(SobogusSolverType.Balls2D, eval_every=scene["eval_every"])
+    ifmap = GeometricImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache(scene["cache_mode"]))
+    return sim, umap, solver, ifmap
+
+
+def rigidbody3d_objects(scene: dict):
+    """As ball2d_objects for a loaded sphere scene (SplitHamMap, no impulse cache)."""
+    from .ball2d import GeometricImpactFrictionMap, ImpulsesToCache, Sobogus, SobogusSolverType
+    from .rigidbody3d import RigidBody3DSim, RigidBody3DState, SplitHamMap, StaticPlane
+    planes = [StaticPlane(x, n) for x, n in zip(scene["plane_x"], scene["plane_n"])]
+    state = RigidBody3DState(scene["q"], scene["v"], scene["r"], scene["m"], scene["I0"], planes)
+    sim = RigidBody3DSim(state, gravity=scene["gravity"])
+    solver = Sobogus(SobogusSolverType.RigidBodies3D, eval_every=scene["eval_every"])
+    ifmap = GeometricImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache.NONE)
+    return sim, SplitHamMap(), solver, ifmap

@@ -1,0 +1,122 @@
+"""XML scene reader (scisim_gb300/scene_io.py) for the reference's ball2d_scene and rigidbody3d_scene
+formats: values as the reference's parsers read them, unsupported features rejected by name, and the
+reference's own asset scenes (when the reference tree is present) either loaded or rejected cleanly.
+"""
+import glob
+import os
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from scisim_gb300 import scene_io, scenes
+
+BALL2D = """<ball2d_scene>
+  <camera cx="0" cy="0" scale_factor="1" fps="50" render_at_fps="1" locked="1"/>
+  <integrator type="verlet" dt="1/300"/>
+  <end_time t="0.5"/>
+  <sobogus_friction_solver mu="0.4" CoR="0.2" max_iters="800" tol="1.0e-9" eval_every="2"
+     staggering="geometric" cache_impulses="normal_and_friction"/>
+  <gravity fx="0.5" fy="-9.81"/>
+  <static_plane x="0.0 -1.0" n="0.1 1.0"/>
+  <static_plane x="3.0 0.0" n="-1 0"/>
+  <ball x="0.1" y="0.25" vx="1.5" vy="-0.5" m="2.0" r="0.25" fixed="0"/>
+  <ball x="0.7" y="0.1" vx="0" vy="0" m="1.0" r="0.2" fixed="0"/>
+</ball2d_scene>"""
+
+SPHERES = """<rigidbody3d_scene>
+  <camera_perspective theta="1" phi="0.4" rho="12" lookat="0 0 0" up="0 1 0" fps="100" render_at_fps="1" locked="0"/>
+  <integrator type="split_ham" dt="0.001"/>
+  <sobogus_friction_solver mu="0.3" CoR="0.1" max_iters="500" tol="1.0e-10" eval_every="1" staggering="geometric"
+     cache_impulses="normal_and_friction"/>
+  <near_earth_gravity f="0.0 -9.81 0.0"/>
+  <static_plane x="0 0 0" n="0 1 0"/>
+  <geometry type="sphere" r="0.5"/>
+  <geometry type="sphere" r="0.25"/>
+  <rigid_body_with_density x="0.0 0.5 0.0" v="0.1 0.0 0.0" omega="0.0 1.0 0.0" rho="2.0" fixed="0" geo_idx="0"/>
+  <rigid_body_with_density x="1.0 0.3 0.0" v="0 0 0" omega="0 0 0" rho="1.0" fixed="0" geo_idx="-1"/>
+</rigidbody3d_scene>"""
+
+
+def test_ball2d_scene_values():
+    s = scene_io.load_ball2d_scene(BALL2D)
+    assert s["integrator"] == "verlet" and s["dt_rational"] == Fraction(1, 300) and s["dt"] == 1.0 / 300.0
+    assert s["end_time"] == 0.5 and scene_io.steps_to(s["end_time"], s["dt_rational"]) == 150
+    assert (s["mu"], s["CoR"], s["tol"], s["max_iters"], s["eval_every"], s["cache_mode"]) == (0.4, 0.2, 1e-9, 800, 2, 2)
+    assert s["gravity"] == (0.5, -9.81)
+    assert np.array_equal(s["q"], [0.1, 0.25, 0.7, 0.1]) and np.array_equal(s["v"], [1.5, -0.5, 0.0, 0.0])
+    assert np.array_equal(s["m"], [2.0, 1.0]) and np.array_equal(s["r"], [0.25, 0.2])
+    assert np.array_equal(s["plane_x"], [[0.0, -1.0], [3.0, 0.0]]) and np.array_equal(s["plane_n"], [[0.1, 1.0], [-1, 0]])
+    sim, umap, solver, ifmap = scene_io.ball2d_objects(s)
+    assert umap.name() == "verlet" and sim.state.nballs() == 2
+
+
+def test_decimal_dt_is_exact():
+    s = scene_io.load_ball2d_scene(BALL2D.replace('dt="1/300"', 'dt="0.00001"'))
+    assert s["dt_rational"] == Fraction(1, 100000) and s["dt"] == 1.0 / 100000.0
+
+
+UNSUPPORTED = {
+    "static_drum": BALL2D.replace('<ball x="0.7"', '<static_drum x="0" y="0" r="5"/>\n  <ball x="0.7"'),
+    "fixed": BALL2D.replace('m="1.0" r="0.2" fixed="0"', 'm="1.0" r="0.2" fixed="1"'),
+    "staggering": BALL2D.replace('staggering="geometric"', 'staggering="symplectic_euler"'),
+    "integrator": BALL2D.replace('type="verlet"', 'type="explicit_euler"'),
+}
+
+
+@pytest.mark.parametrize("word", sorted(UNSUPPORTED))
+def test_ball2d_unsupported_features_are_rejected(word):
+    with pytest.raises(scene_io.SceneError, match=word):
+        scene_io.load_ball2d_scene(UNSUPPORTED[word])
+
+
+def test_sphere_scene_values():
+    s = scene_io.load_rigidbody3d_scene(SPHERES)
+    m, i0 = scenes.sphere_mass_inertia(np.array([0.5, 0.25]), 1.0)
+    assert s["m"][1] == m[1] and s["I0"][3] == i0[1]
+    m2, i2 = scenes.sphere_mass_inertia(np.array([0.5]), 2.0)
+    assert s["m"][0] == m2[0] and s["I0"][0] == i2[0]
+    assert np.array_equal(s["q"][:6], [0.0, 0.5, 0.0, 1.0, 0.3, 0.0])
+    assert np.array_equal(s["q"][6:15], np.eye(3).reshape(-1))
+    assert np.array_equal(s["v"], [0.1, 0, 0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0])
+    assert s["cache_mode"] == 0 and s["gravity"] == (0.0, -9.81, 0.0)
+    sim, umap, solver, ifmap = scene_io.rigidbody3d_objects(s)
+    assert umap.name() == "split_ham"
+    with pytest.raises(scene_io.SceneError, match="orientation"):
+        scene_io.load_rigidbody3d_scene(SPHERES.replace('geo_idx="0"/>', 'geo_idx="0" R="0 0 1"/>'))
+
+
+ASSETS = "/root/reference/assets"
+
+
+@pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
+def test_reference_assets_load_or_are_rejected_by_name():
+    ok = bad = 0
+    for path in sorted(glob.glob(ASSETS + "/ball2d/**/*.xml", recursive=True)):
+        try:
+            s = scene_io.load_ball2d_scene(path)
+        except scene_io.SceneError:
+            bad += 1
+            continue
+        ok += 1
+        assert s["dt"] > 0 and s["q"].shape[0] == 2 * s["r"].shape[0]
+    assert ok >= 10 and bad >= 1
+
+
+@pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
+def test_registered_slope_scenes_match_the_golden_extraction():
+    """The 18 slope scenes registered in ball2dcli/CMakeLists.txt, read by this reader, equal the
+    values tests/golden/make_golden.py extracted from the same files with its own code."""
+    import json
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "slope_scenes.json")))
+    for g in golden:
+        s = scene_io.load_ball2d_scene(os.path.join(os.path.dirname(ASSETS), g["xml"]))
+        assert s["integrator"] == g["integrator"] and s["dt"] == g["dt"]
+        assert (s["mu"], s["CoR"], s["tol"], s["max_iters"], s["eval_every"]) == (
+            g["mu"], g["CoR"], g["tol"], g["max_iters"], g["eval_every"])
+        assert s["cache_mode"] == scene_io.CACHE_MODES[g["cache_impulses"]]
+        assert list(s["gravity"]) == g["gravity"]
+        assert list(s["plane_x"][0]) == g["plane_x"] and list(s["plane_n"][0]) == g["plane_n"]
+        b = g["ball"]
+        assert list(s["q"]) == [b["x"], b["y"]] and list(s["v"]) == [b["vx"], b["vy"]]
+        assert s["m"][0] == b["m"] and s["r"][0] == b["r"]
