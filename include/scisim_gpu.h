@@ -43,6 +43,8 @@ typedef enum {
 enum { SG_SYMPLECTIC_EULER = 0, SG_VERLET = 1, SG_SPLIT_HAM = 2 };
 /* ImpulsesToCache (scisim/ConstrainedMaps/ImpulsesToCache.h) */
 enum { SG_CACHE_NONE = 0, SG_CACHE_NORMAL = 1, SG_CACHE_NORMAL_AND_FRICTION = 2 };
+/* Staggering of a Ball2D step: GeometricImpactFrictionMap or SymplecticEulerImpactFrictionMap. */
+enum { SG_STAGGER_GEOMETRIC = 0, SG_STAGGER_SYMPLECTIC_EULER = 1 };
 /* Arithmetic of the Gauss-Seidel sweeps. */
 enum { SG_PRECISION_FP64 = 0, SG_PRECISION_FP32_REFINE = 1 };
 
@@ -305,6 +307,16 @@ SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
  * the same kind as the colour order, with three grid barriers a sweep instead of one per
  * colour.  0 keeps the one-level colour sweeps. */
 SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
+
+/* Selects the map a single Ball2D scene steps with (default SG_STAGGER_GEOMETRIC).
+ * SG_STAGGER_SYMPLECTIC_EULER is SymplecticEulerImpactFrictionMap
+ * (scisim/ConstrainedMaps/SymplecticEulerImpactFrictionMap.cpp:201-407): the force acts first
+ * (vdelta = dt Minv F), collisions are detected on q0 + dt (v0 + vdelta), the solve gets the
+ * extra relative velocities N^T vdelta and D^T vdelta (plus min(0, gap(q0)) / dt where stabilize
+ * is set and the gap exceeds penetration_threshold in magnitude), and the step ends with
+ * v1 = v + vdelta, q1 = q0 + dt v1, whatever the context's integrator.  It needs CoR = 0, as the
+ * reference does; batched and sphere scenes step with the geometric map only. */
+SG_API int sg_set_staggering(sg_ctx* ctx, int32_t staggering, int32_t stabilize, double penetration_threshold);
 
 /* Checkpoint / resume of a context holding one Ball2D or sphere scene (replaces SCISim's binary
  * serialisation of the simulation, ball2dcli/ball2d_cli.cpp:199-316, Ball2DSim.cpp:810-822).

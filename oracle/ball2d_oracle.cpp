@@ -367,13 +367,29 @@ extern "C" int64_t or_ball2d_last_contacts(const or_ball2d* s, int64_t cap, int3
   return nc;
 }
 
-// GeometricImpactFrictionMap::flow with Sobogus(Balls2D).
+// GeometricImpactFrictionMap::flow with Sobogus(Balls2D), or SymplecticEulerImpactFrictionMap::flow
+// (SymplecticEulerImpactFrictionMap.cpp:201-400) when p.staggering says so.
 extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* stats) {
   (void)iteration;
   const int nb = s->nb;
-  std::vector<double> q1(2 * nb), v1(2 * nb);
-  // Unconstrained predictor (GeometricImpactFrictionMap.cpp:279).
-  umap_flow(s, s->q.data(), s->v.data(), q1.data(), v1.data());
+  const bool se = s->p.staggering == OR_STAGGER_SYMPLECTIC_EULER;
+  const double dt = s->p.dt;
+  std::vector<double> q1(2 * nb), v1(2 * nb), vdelta;
+  if (se) {
+    // F = 0 + m g (Ball2DSim::computeForce, Ball2DGravityForce.cpp:36-46); vdelta = dt (Minv F), the
+    // sparse product accumulating from zero; predictor q1 = q0 + dt (v0 + vdelta) (:219-229).
+    vdelta.resize(2 * nb);
+    for (int i = 0; i < nb; ++i)
+      for (int d = 0; d < 2; ++d) {
+        const double F = 0.0 + s->m[i] * s->p.gravity[d];
+        vdelta[2 * i + d] = dt * (0.0 + s->minv[i] * F);
+        v1[2 * i + d] = s->v[2 * i + d] + vdelta[2 * i + d];
+        q1[2 * i + d] = s->q[2 * i + d] + dt * v1[2 * i + d];
+      }
+  } else {
+    // Unconstrained predictor (GeometricImpactFrictionMap.cpp:279).
+    umap_flow(s, s->q.data(), s->v.data(), q1.data(), v1.data());
+  }
   std::vector<Contact> cs;
   active_set(s, s->q.data(), q1.data(), cs);
   const int nc = int(cs.size());
@@ -428,8 +444,53 @@ extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* s
   or_gs_params gp{s->p.tol, s->p.max_iters, s->p.eval_every,
                   int64_t(s->next_order.size()) == int64_t(nc) ? s->next_order.data() : nullptr};
   or_gs_result gr{};
-  or_sobogus_solve_2d(nb, s->m.data(), s->v.data(), nc, ia.data(), ib.data(), bases.data(), CoR.data(), mu.data(),
-                      &gp, alpha.data(), beta.data(), v2.data(), f.data(), &gr);
+  if (se) {
+    // nrel = N^T vdelta, drel = D^T vdelta (:294-305): per contact the column's entries in row
+    // order (body a's, then body b's, a < b), accumulated from zero as Eigen's sparse product does;
+    // N holds n, -n and D holds t, -t.  Stabilisation: nrel += min(0, gap(q0)) / dt unless the gap
+    // is smaller in magnitude than the penetration threshold (:307-321).
+    std::vector<double> nrel(nc), drel(nc);
+    for (int k = 0; k < nc; ++k) {
+      const auto& c = cs[k];
+      const double* da = &vdelta[2 * c.a];
+      double tn = 0.0, tt = 0.0;
+      tn = tn + c.nx * da[0];
+      tn = tn + c.ny * da[1];
+      tt = tt + c.tx * da[0];
+      tt = tt + c.ty * da[1];
+      if (c.b >= 0) {
+        const double* db = &vdelta[2 * c.b];
+        tn = tn + (-c.nx) * db[0];
+        tn = tn + (-c.ny) * db[1];
+        tt = tt + (-c.tx) * db[0];
+        tt = tt + (-c.ty) * db[1];
+      }
+      nrel[k] = 0.0 + 1.0 * tn;
+      drel[k] = 0.0 + 1.0 * tt;
+      if (s->p.stabilize) {
+        double gap;
+        if (c.b >= 0) {
+          // BallBallConstraint::evaluateGapFunction (:76-86)
+          const double dx = s->q[2 * c.a] - s->q[2 * c.b], dy = s->q[2 * c.a + 1] - s->q[2 * c.b + 1];
+          gap = std::sqrt(dx * dx + dy * dy) - (s->r[c.a] + s->r[c.b]);
+        } else {
+          // StaticPlaneConstraint::evaluateGapFunction (BallStaticPlaneConstraint.cpp:58-63)
+          const int pl = -1 - c.b;
+          const double dx = s->q[2 * c.a] - s->px[2 * pl], dy = s->q[2 * c.a + 1] - s->px[2 * pl + 1];
+          gap = (s->pn[2 * pl] * dx + s->pn[2 * pl + 1] * dy) - s->r[c.a];
+        }
+        double g0 = std::min(0.0, gap);
+        if (std::fabs(g0) < s->p.penetration_threshold) g0 = 0.0;
+        nrel[k] = nrel[k] + g0 / dt;
+      }
+    }
+    or_sobogus_solve_2d_ex(nb, s->m.data(), s->v.data(), nc, ia.data(), ib.data(), bases.data(), CoR.data(),
+                           mu.data(), nrel.data(), drel.data(), &gp, alpha.data(), beta.data(), v2.data(), f.data(),
+                           &gr);
+  } else {
+    or_sobogus_solve_2d(nb, s->m.data(), s->v.data(), nc, ia.data(), ib.data(), bases.data(), CoR.data(),
+                        mu.data(), &gp, alpha.data(), beta.data(), v2.data(), f.data(), &gr);
+  }
   s->next_order.clear();
   // cacheImpulses (:222-264)
   if (s->p.cache_mode != OR_CACHE_NONE) {
@@ -451,8 +512,16 @@ extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* s
     stats->succeeded = gr.succeeded;
     stats->error = gr.error;
   }
-  // Final map with the post-impact velocity (:441).
-  umap_flow(s, s->q.data(), v2.data(), q1.data(), v1.data());
+  if (se) {
+    // v1 = v2 + vdelta, q1 = q0 + dt v1 (:363, :406).
+    for (int i = 0; i < 2 * nb; ++i) {
+      v1[i] = v2[i] + vdelta[i];
+      q1[i] = s->q[i] + dt * v1[i];
+    }
+  } else {
+    // Final map with the post-impact velocity (:441).
+    umap_flow(s, s->q.data(), v2.data(), q1.data(), v1.data());
+  }
   s->q.swap(q1);
   s->v.swap(v1);
   return gr.succeeded ? 0 : 1;

@@ -355,13 +355,23 @@ extern "C" void or_local_solve(int dim, const double* W, const double* b, double
 // residual of that impulse without iterating.
 static double solve2d_impl(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
                            const double* bases, const double* CoR, const double* mu, const or_gs_params* p,
-                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only);
+                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only,
+                           const double* nrel_in = nullptr, const double* drel_in = nullptr);
 
 extern "C" void or_sobogus_solve_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
                                     const int32_t* ib, const double* bases, const double* CoR,
                                     const double* mu, const or_gs_params* p, double* alpha, double* beta,
                                     double* v2, double* f, or_gs_result* res) {
   solve2d_impl(nb, m, v0, nc, ia, ib, bases, CoR, mu, p, alpha, beta, v2, f, res, false);
+}
+
+// With the extra relative velocities of the map (FrictionSolver::solve's nrel_extra, drel_extra;
+// SymplecticEulerImpactFrictionMap.cpp:293-321).
+extern "C" void or_sobogus_solve_2d_ex(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
+                                       const int32_t* ib, const double* bases, const double* CoR, const double* mu,
+                                       const double* nrel, const double* drel, const or_gs_params* p, double* alpha,
+                                       double* beta, double* v2, double* f, or_gs_result* res) {
+  solve2d_impl(nb, m, v0, nc, ia, ib, bases, CoR, mu, p, alpha, beta, v2, f, res, false, nrel, drel);
 }
 
 extern "C" double or_residual_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
@@ -374,7 +384,8 @@ extern "C" double or_residual_2d(int nb, const double* m, const double* v0, int 
 
 static double solve2d_impl(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
                            const double* bases, const double* CoR, const double* mu, const or_gs_params* p,
-                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only) {
+                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only,
+                           const double* nrel_in, const double* drel_in) {
   // Minv as the reference builds it: 1.0 / m (ball2d/Ball2DState.cpp:55-67).
   std::vector<double> minv(nb);
   for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];
@@ -408,8 +419,8 @@ static double solve2d_impl(int nb, const double* m, const double* v0, int nc, co
     const double ndotv = nx * vrx + ny * vry;
     // Kinematic relative velocity is zero for balls and static planes:
     // nrel = -(0 . n), drel = -(0 . t)  (Constraint.cpp:110-123).
-    const double nrel = -(0.0 * nx + 0.0 * ny);
-    const double drel = -(0.0 * tx + 0.0 * ty);
+    const double nrel = nrel_in ? nrel_in[k] : -(0.0 * nx + 0.0 * ny);
+    const double drel = drel_in ? drel_in[k] : -(0.0 * tx + 0.0 * ty);
     // Forcing term w = n (CoR ndotv + nrel) + t drel (Constraint.cpp:27-33).
     const double s = CoR[k] * ndotv + nrel;
     const double wx = (0.0 + nx * s) + tx * drel;

@@ -70,6 +70,13 @@ void or_sobogus_solve_2d(int nb, const double* m, const double* v0, int nc, cons
                          const or_gs_params* p, double* alpha, double* beta, double* v2, double* f,
                          or_gs_result* res);
 
+// As or_sobogus_solve_2d with the map's extra relative velocities per contact (nrel, drel; the
+// geometric map's are zero).
+void or_sobogus_solve_2d_ex(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
+                            const int32_t* ib, const double* bases, const double* CoR, const double* mu,
+                            const double* nrel, const double* drel, const or_gs_params* p, double* alpha,
+                            double* beta, double* v2, double* f, or_gs_result* res);
+
 // Coulomb residual (the solver's error function) of given impulses (alpha, beta).
 double or_residual_2d(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
                       const double* bases, const double* CoR, const double* mu, const double* alpha,
@@ -80,6 +87,7 @@ typedef struct or_ball2d or_ball2d;
 
 enum { OR_SYMPLECTIC_EULER = 0, OR_VERLET = 1 };
 enum { OR_CACHE_NONE = 0, OR_CACHE_NORMAL = 1, OR_CACHE_NORMAL_AND_FRICTION = 2 };
+enum { OR_STAGGER_GEOMETRIC = 0, OR_STAGGER_SYMPLECTIC_EULER = 1 };
 
 typedef struct {
   int32_t integrator;     // OR_SYMPLECTIC_EULER / OR_VERLET
@@ -91,6 +99,9 @@ typedef struct {
   double tol;
   uint32_t max_iters;
   uint32_t eval_every;
+  int32_t staggering;             // OR_STAGGER_* (GeometricImpactFrictionMap / SymplecticEulerImpactFrictionMap)
+  int32_t stabilize;              // symplectic Euler: pose stabilisation g0 / dt
+  double penetration_threshold;   // symplectic Euler: gaps smaller in magnitude are ignored
 } or_ball2d_params;
 
 typedef struct {

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 SYMPLECTIC_EULER, VERLET = 0, 1
 CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
+STAGGER_GEOMETRIC, STAGGER_SYMPLECTIC_EULER = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -34,7 +35,8 @@ class GsResult(C.Structure):
 class Ball2DParams(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("cache_mode", C.c_int32), ("dt", C.c_double),
                 ("gravity", C.c_double * 2), ("mu", C.c_double), ("CoR", C.c_double),
-                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
+                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32),
+                ("staggering", C.c_int32), ("stabilize", C.c_int32), ("penetration_threshold", C.c_double)]
 
 
 class Sphere3DParams(C.Structure):
@@ -239,14 +241,14 @@ class Ball2D:
 
     def __init__(self, q, v, r, m, plane_x, plane_n, *, dt, gravity=(0.0, -9.81), mu=0.5, CoR=0.0,
                  tol=1e-9, max_iters=5000, eval_every=1, integrator=SYMPLECTIC_EULER,
-                 cache_mode=CACHE_NONE):
+                 cache_mode=CACHE_NONE, staggering=0, stabilize=False, penetration_threshold=0.0):
         self.q, self.v = f64(q), f64(v)
         self.r, self.m = f64(r), f64(m)
         self.nb = self.r.shape[0]
         px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
         self.np = px.shape[0] // 2
         p = Ball2DParams(integrator, cache_mode, dt, (C.c_double * 2)(*gravity), mu, CoR, tol,
-                         max_iters, eval_every)
+                         max_iters, eval_every, staggering, 1 if stabilize else 0, penetration_threshold)
         self._h = lib().or_ball2d_create(self.nb, _d(self.q), _d(self.v), _d(self.r), _d(self.m),
                                          self.np, _d(px), _d(pn), C.byref(p))
         self.iteration = 0

@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "SG_OK", 1: "SG_NOT_CONVERGED", 2: "SG_BAD_INPUT", 3: "SG_DEV
 SYMPLECTIC_EULER, VERLET, SPLIT_HAM = 0, 1, 2
 CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
 PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
+STAGGER_GEOMETRIC, STAGGER_SYMPLECTIC_EULER = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -109,6 +110,7 @@ SIGNATURES = {
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "sg_set_two_level": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_set_staggering": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "sg_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sg_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sg_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32, C.c_void_p, _dp]),
@@ -427,6 +429,11 @@ class Context:
 
     def set_two_level(self, on=True):
         check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
+
+    def set_staggering(self, staggering=STAGGER_GEOMETRIC, stabilize=False, penetration_threshold=0.0):
+        """GeometricImpactFrictionMap (default) or SymplecticEulerImpactFrictionMap for this Ball2D scene."""
+        check(lib().sg_set_staggering(self._h, int(staggering), 1 if stabilize else 0, float(penetration_threshold)),
+              "sg_set_staggering")
 
     def tuning(self):
         t = SgTuning()

@@ -165,6 +165,34 @@ class GeometricImpactFrictionMap:
         return self._ctx.sphere3d_last_contacts() if self._ctx.dim == 3 else self._ctx.last_contacts()
 
 
+class SymplecticEulerImpactFrictionMap(GeometricImpactFrictionMap):
+    """scisim/ConstrainedMaps/SymplecticEulerImpactFrictionMap.cpp:201-407 on the GPU: the force acts
+    first, the solve gets N^T vdelta and D^T vdelta (and the pose stabilisation if enabled), and the
+    step ends with a linear update; the unconstrained map passed to flow() is not used.  CoR must
+    be 0 (the reference asserts it)."""
+
+    def __init__(self, abs_tol: float, max_iters: int, impulses_to_cache=ImpulsesToCache.NONE,
+                 stabilize: bool = False, penetration_threshold: float = 0.0):
+        super().__init__(abs_tol, max_iters, impulses_to_cache)
+        if penetration_threshold < 0.0:
+            raise ValueError("penetration_threshold must be non-negative")
+        self.stabilize = bool(stabilize)
+        self.penetration_threshold = float(penetration_threshold)
+
+    def name(self):
+        return "symplectic_euler_impact_friction_map"
+
+    def _context(self, sim, umap, solver, dt, CoR, mu):
+        if CoR != 0.0:
+            raise ValueError("the symplectic Euler staggering needs CoR = 0")
+        fresh = self._ctx is None
+        ctx = super()._context(sim, umap, solver, dt, CoR, mu)
+        if fresh or ctx is not getattr(self, "_staggered", None):
+            ctx.set_staggering(_lib.STAGGER_SYMPLECTIC_EULER, self.stabilize, self.penetration_threshold)
+            self._staggered = ctx
+        return ctx
+
+
 class StaticPlane:
     """ball2d/StaticGeometry/StaticPlane.cpp:10-19 (normal normalised on upload)."""
 

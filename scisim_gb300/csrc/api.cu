@@ -73,6 +73,10 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   const int nb = ctx->nb;
   cudaStream_t s = ctx->stream;
   sg_step_stats st{};
+  if (ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER && ctx->cfg.CoR != 0.0) {
+    set_error("the symplectic Euler staggering needs CoR = 0");
+    return SG_BAD_INPUT;
+  }
   if (nb == 0) {
     if (out) *out = st;
     return SG_OK;
@@ -1030,6 +1034,8 @@ struct CkptHeader {
   int32_t version, dim, nb, np;
   int64_t prev_n;
   sg_config cfg;
+  int32_t staggering, stabilize;
+  double pen_thresh;
 };
 constexpr char kCkptMagic[8] = {'S', 'G', 'C', 'K', 'P', 'T', '1', 0};
 
@@ -1084,6 +1090,9 @@ int sg_checkpoint_save(sg_ctx* ctx, void* buf, int64_t bytes) {
   h.np = ctx->np;
   h.prev_n = ctx->prev_n;
   h.cfg = ctx->cfg;
+  h.staggering = ctx->staggering;
+  h.stabilize = ctx->stabilize;
+  h.pen_thresh = ctx->pen_thresh;
   char* out = static_cast<char*>(buf);
   std::memcpy(out, &h, sizeof(h));
   size_t off = sizeof(h);
@@ -1151,7 +1160,26 @@ int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes) {
   }
   ctx->prev_n = h.prev_n;
   ctx->last_nc = 0;
+  ctx->staggering = h.staggering;
+  ctx->stabilize = h.stabilize;
+  ctx->pen_thresh = h.pen_thresh;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_set_staggering(sg_ctx* ctx, int32_t staggering, int32_t stabilize, double penetration_threshold) {
+  if (!ctx || (staggering != SG_STAGGER_GEOMETRIC && staggering != SG_STAGGER_SYMPLECTIC_EULER) ||
+      !(penetration_threshold >= 0.0)) {
+    set_error("sg_set_staggering: staggering SG_STAGGER_GEOMETRIC or SG_STAGGER_SYMPLECTIC_EULER, threshold >= 0");
+    return SG_BAD_INPUT;
+  }
+  if (staggering == SG_STAGGER_SYMPLECTIC_EULER && ctx->cfg.CoR != 0.0) {
+    set_error("sg_set_staggering: the symplectic Euler staggering needs CoR = 0");
+    return SG_BAD_INPUT;
+  }
+  ctx->staggering = staggering;
+  ctx->stabilize = stabilize != 0;
+  ctx->pen_thresh = penetration_threshold;
   return SG_OK;
 }
 

@@ -73,6 +73,43 @@ __global__ void k_predict_aabb(int nb, int integrator, double dt, double gx, dou
   aabb[i] = b;
 }
 
+// SymplecticEulerImpactFrictionMap predictor (SymplecticEulerImpactFrictionMap.cpp:219-229): the
+// velocity change vdelta = dt (Minv F) with F = 0 + m g accumulated as the reference's force and
+// sparse product do, q1 = q0 + dt (v0 + vdelta); swept AABBs as k_predict_aabb.
+__global__ void k_predict_se(int nb, double dt, double gx, double gy, const double2* __restrict__ q,
+                             const double2* __restrict__ v, const double* __restrict__ m,
+                             const double* __restrict__ minv, const double* __restrict__ rad, double2* __restrict__ q1,
+                             double2* __restrict__ v1, double2* __restrict__ vdelta, double4_32a* __restrict__ aabb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double2 q0 = q[i], v0 = v[i];
+  const double mi = m[i], wi = minv[i];
+  const double2 vd = make_double2(dt * (0.0 + wi * (0.0 + mi * gx)), dt * (0.0 + wi * (0.0 + mi * gy)));
+  const double2 vn = make_double2(v0.x + vd.x, v0.y + vd.y);
+  const double2 qn = make_double2(q0.x + dt * vn.x, q0.y + dt * vn.y);
+  vdelta[i] = vd;
+  q1[i] = qn;
+  v1[i] = vn;
+  const double r = rad[i];
+  double4_32a b;
+  b.x = smin(qn.x, q0.x) - r;
+  b.y = smin(qn.y, q0.y) - r;
+  b.z = smax(qn.x, q0.x) + r;
+  b.w = smax(qn.y, q0.y) + r;
+  aabb[i] = b;
+}
+
+// Its final update: v1 = v2 + vdelta, q1 = q0 + dt v1 (:363, :406).
+__global__ void k_final_se(int nb, double dt, const double2* __restrict__ q0, const double2* __restrict__ v2,
+                           const double2* __restrict__ vdelta, double2* __restrict__ q1, double2* __restrict__ v1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double2 q = q0[i], w = v2[i], d = vdelta[i];
+  const double2 vn = make_double2(w.x + d.x, w.y + d.y);
+  v1[i] = vn;
+  q1[i] = make_double2(q.x + dt * vn.x, q.y + dt * vn.y);
+}
+
 // Bounds of all boxes and the largest extent per axis (exact: min/max are order free).
 __global__ void k_bounds(int n, const double4_32a* __restrict__ aabb, GridParams* gp) {
   double mn0 = INFINITY, mn1 = INFINITY, mx0 = -INFINITY, mx1 = -INFINITY, e0 = 0.0, e1 = 0.0;
@@ -337,6 +374,14 @@ struct AssembleArgs {
   double* mu_out;
   double2* r;
   unsigned long long* key;
+  // SymplecticEulerImpactFrictionMap: the velocity change of the step (null for the geometric
+  // map), and its pose stabilisation (positions, radii, plane points, dt, threshold).
+  const double2* vdelta = nullptr;
+  const double* rad = nullptr;
+  const double2* plane_x = nullptr;
+  double dt = 0.0;
+  int stabilize = 0;
+  double pen_thresh = 0.0;
 };
 
 // Contact basis, forcing term, diagonal Delassus block and warm start per contact:
@@ -378,8 +423,43 @@ __device__ __forceinline__ void assemble_one(const AssembleArgs& A, int k, doubl
     vry = va.y - 0.0;
   }
   const double ndotv = nx * vrx + ny * vry;
-  const double nrel = -(0.0 * nx + 0.0 * ny);
-  const double drel = -(0.0 * tx + 0.0 * ty);
+  double nrel = -(0.0 * nx + 0.0 * ny);
+  double drel = -(0.0 * tx + 0.0 * ty);
+  if (A.vdelta) {
+    // nrel = N^T vdelta, drel = D^T vdelta (SymplecticEulerImpactFrictionMap.cpp:294-305): the
+    // column's entries (n, -n / t, -t) in row order, accumulated from zero as the sparse product;
+    // then the stabilisation nrel += min(0, gap(q0)) / dt beyond the threshold (:307-321).
+    const double2 da = A.vdelta[a];
+    double tn = 0.0, tt = 0.0;
+    tn = tn + nx * da.x;
+    tn = tn + ny * da.y;
+    tt = tt + tx * da.x;
+    tt = tt + ty * da.y;
+    if (b >= 0) {
+      const double2 db = A.vdelta[b];
+      tn = tn + (-nx) * db.x;
+      tn = tn + (-ny) * db.y;
+      tt = tt + (-tx) * db.x;
+      tt = tt + (-ty) * db.y;
+    }
+    nrel = 0.0 + 1.0 * tn;
+    drel = 0.0 + 1.0 * tt;
+    if (A.stabilize) {
+      const double2 qa = A.q0[a];
+      double gap;
+      if (b >= 0) {
+        const double2 qb = A.q0[b];
+        const double gx = qa.x - qb.x, gy = qa.y - qb.y;
+        gap = sqrt(gx * gx + gy * gy) - (A.rad[a] + A.rad[b]);
+      } else {
+        const double2 px = A.plane_x[-1 - b];
+        gap = (nx * (qa.x - px.x) + ny * (qa.y - px.y)) - A.rad[a];
+      }
+      double g0 = (gap < 0.0) ? gap : 0.0;  // std::min(0.0, gap)
+      if (fabs(g0) < A.pen_thresh) g0 = 0.0;
+      nrel = nrel + g0 / A.dt;
+    }
+  }
   const double s = CoR * ndotv + nrel;
   const double wx = (0.0 + nx * s) + tx * drel;
   const double wy = (0.0 + ny * s) + ty * drel;
@@ -723,6 +803,15 @@ __global__ void k_ccd_batch(int n, const double2* q0a, const double2* q1a, const
 int ball2d_predict_and_bounds(sg_ctx* ctx) {
   const int nb = ctx->nb;
   if (nb <= 0) return SG_OK;
+  if (ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER && ctx->n_scenes == 0) {
+    if (int r = grow(ctx->vdelta, sizeof(double) * 2 * (size_t)nb)) return r;
+    k_predict_se<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(
+        nb, ctx->cfg.dt, ctx->cfg.gravity[0], ctx->cfg.gravity[1], ctx->q.as<double2>(), ctx->v.as<double2>(),
+        ctx->m.as<double>(), ctx->minv.as<double>(), ctx->r.as<double>(), ctx->q1.as<double2>(),
+        ctx->v1.as<double2>(), ctx->vdelta.as<double2>(), ctx->aabb.as<double4_32a>());
+    SG_CUDA_TRY(cudaGetLastError());
+    return SG_OK;
+  }
   k_predict_aabb<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(
       nb, ctx->cfg.integrator, ctx->cfg.dt, ctx->cfg.gravity[0], ctx->cfg.gravity[1], ctx->q.as<double2>(),
       ctx->v.as<double2>(), ctx->m.as<double>(), ctx->minv.as<double>(), ctx->r.as<double>(), ctx->q1.as<double2>(),
@@ -839,6 +928,14 @@ int assemble_contacts(sg_ctx* ctx, int nc) {
   A.mu_out = ctx->mu.as<double>();
   A.r = ctx->r_loc.as<double2>();
   A.key = ctx->key.as<unsigned long long>();
+  if (ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER) {
+    A.vdelta = ctx->vdelta.as<double2>();
+    A.rad = ctx->r.as<double>();
+    A.plane_x = ctx->plane_x.as<double2>();
+    A.dt = ctx->cfg.dt;
+    A.stabilize = ctx->stabilize;
+    A.pen_thresh = ctx->pen_thresh;
+  }
   k_assemble<<<blocks_for(nc), kBlock, 0, ctx->stream>>>(A);
   SG_CUDA_TRY(cudaGetLastError());
   return SG_OK;
@@ -855,6 +952,14 @@ int extract_and_cache(sg_ctx* ctx, int nc) {
 int ball2d_final_map(sg_ctx* ctx, const double* vin) {
   const int nb = ctx->nb;
   if (nb <= 0) return SG_OK;
+  if (ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER && ctx->n_scenes == 0) {
+    k_final_se<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(nb, ctx->cfg.dt, ctx->q.as<double2>(),
+                                                          reinterpret_cast<const double2*>(vin),
+                                                          ctx->vdelta.as<double2>(), ctx->q1.as<double2>(),
+                                                          ctx->v1.as<double2>());
+    SG_CUDA_TRY(cudaGetLastError());
+    return SG_OK;
+  }
   k_final_map<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(nb, ctx->cfg.integrator, ctx->cfg.dt, ctx->cfg.gravity[0],
                                                           ctx->cfg.gravity[1], ctx->q.as<double2>(),
                                                           reinterpret_cast<const double2*>(vin), ctx->m.as<double>(),

@@ -152,6 +152,12 @@ struct sg_ctx {
   // Two-level FP32 sweeps (spatial patches, one per SM): patch of each body, patch-local
   // index, bodies by patch, contact keys (patch, colour) and the packed order.
   bool patches = true;
+  // Staggering of the single-scene Ball2D step (sg_set_staggering): SG_STAGGER_*, and the
+  // symplectic Euler map's pose stabilisation and threshold; its velocity change per body.
+  int staggering = 0;
+  int stabilize = 0;
+  double pen_thresh = 0.0;
+  sg::Buf vdelta;
   // Tunables (sg_set_tuning / sg_autotune): base interval of the FP64 checks in the FP32 form,
   // and the contact count from which a single-scene FP32 solve uses the two-level sweeps.
   int check_interval = 16;

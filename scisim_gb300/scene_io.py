@@ -2,8 +2,8 @@
 
 Ball2D (`<ball2d_scene>`, ball2dutils/Ball2DSceneParser.cpp) and RigidBody3D sphere scenes
 (`<rigidbody3d_scene>`, rigidbody3dutils/RigidBody3DSceneParser.cpp) with the elements of the contact
-path: integrator, `sobogus_friction_solver` with geometric staggering, gravity, static planes, balls
-or spheres.  Values are read the way the reference reads them: scalars as C++ stream extraction of
+path: integrator, `sobogus_friction_solver` with geometric staggering (and, for Ball2D, the
+symplectic_euler staggering), gravity, static planes, balls or spheres.  Values are read the way the reference reads them: scalars as C++ stream extraction of
 a decimal (Python's float of the same text rounds the same way), the time step as an exact rational
 (`Rational<intmax_t>` from a decimal or `a/b`, Rational.h:204-260) taken as numerator / denominator.
 Elements of features outside the contact path (drums, portals, penalty forces, other solvers and
@@ -85,14 +85,24 @@ def _solver(root, tag_3d=False):
     nd = nodes[0]
     tag = "sobogus_friction_solver"
     stag = _attr(nd, "staggering", tag)
-    if stag != "geometric":
-        raise SceneError("%s: staggering %r is not supported (geometric only)" % (tag, stag))
+    allowed = ("geometric",) if tag_3d else ("geometric", "symplectic_euler")
+    if stag not in allowed:
+        raise SceneError("%s: staggering %r is not supported (%s)" % (tag, stag, ", ".join(allowed)))
     cache = _attr(nd, "cache_impulses", tag)
     if cache not in CACHE_MODES:
         raise SceneError("%s: cache_impulses must be none, normal or normal_and_friction" % tag)
     out = dict(mu=_scalar(nd, "mu", tag), CoR=_scalar(nd, "CoR", tag), tol=_scalar(nd, "tol", tag),
                max_iters=int(_attr(nd, "max_iters", tag)), eval_every=int(_attr(nd, "eval_every", tag)),
                cache_mode=CACHE_MODES[cache])
+    out["staggering"] = stag
+    if stag == "symplectic_euler":
+        # Ball2DSceneParser.cpp:1354-1398: CoR must be 0; stabilization and its threshold.
+        if out["CoR"] != 0.0:
+            raise SceneError("%s: CoR must be 0 for the symplectic_euler staggering" % tag)
+        out["stabilization"] = _bool(nd, "stabilization", tag)
+        out["penetration_threshold"] = _scalar(nd, "penetration_threshold", tag)
+        if out["penetration_threshold"] < 0.0:
+            raise SceneError("%s: penetration_threshold must be non-negative" % tag)
     if tag_3d:
         out["cache_mode"] = 0  # the 3D geometric map keeps no cache (RigidBody3DSceneParser.cpp:1877-1880)
     return out
@@ -222,12 +232,17 @@ def ball2d_objects(scene: dict):
     its unconstrained map, the Sobogus solver and the geometric impact-friction map.  Step with
     sim.flow(iteration, scene['dt'], umap, scene['CoR'], scene['mu'], solver, ifmap)."""
     from .ball2d import (Ball2DSim, Ball2DState, GeometricImpactFrictionMap, ImpulsesToCache, Sobogus,
-                         SobogusSolverType, StaticPlane, SymplecticEulerMap, VerletMap)
+                         SobogusSolverType, StaticPlane, SymplecticEulerImpactFrictionMap, SymplecticEulerMap,
+                         VerletMap)
     planes = [StaticPlane(x, n) for x, n in zip(scene["plane_x"], scene["plane_n"])]
     sim = Ball2DSim(Ball2DState(scene["q"], scene["v"], scene["r"], scene["m"], planes), gravity=scene["gravity"])
     umap = VerletMap() if scene["integrator"] == "verlet" else SymplecticEulerMap()
     solver = Sobogus(SobogusSolverType.Balls2D, eval_every=scene["eval_every"])
-    ifmap = GeometricImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache(scene["cache_mode"]))
+    if scene.get("staggering") == "symplectic_euler":
+        ifmap = SymplecticEulerImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache(scene["cache_mode"]),
+                                                 scene["stabilization"], scene["penetration_threshold"])
+    else:
+        ifmap = GeometricImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache(scene["cache_mode"]))
     return sim, umap, solver, ifmap
 
 

@@ -94,15 +94,15 @@ def extract_ccd_cases(ref):
 def extract_slope_scenes(ref):
     cm = open(os.path.join(ref, "ball2dcli", "CMakeLists.txt")).read()
     scenes = []
-    for m in re.finditer(r"add_test\( (ball2d_(static|sliding)_friction_\w+) assets/shell_scripts/\w+\.sh "
-                         r"assets/(tests_friction/\S+\.xml) ([0-9.]+) (\d+) (\S+) (\S+) (\S+) (\S+) \)", cm):
+    for m in re.finditer(r"add_test\( (ball2d_(?:st_)?(static|sliding)_friction_\w+) assets/shell_scripts/\w+\.sh "
+                         r"assets/(tests_(?:friction|st)/\S+\.xml) ([0-9.]+) (\d+) (\S+) (\S+) (\S+) (\S+) \)", cm):
         name, kind, rel, end_time, freq = m.group(1), m.group(2), m.group(3), m.group(4), m.group(5)
         tols = [float(m.group(i)) for i in (6, 7, 8, 9)]
         xml = open(os.path.join(ref, "assets", "ball2d", rel)).read()
 
-        def attr(tag, name):
+        def attr(tag, name, default=None):
             mm = re.search(r"<%s[^>]*\s%s=\"([^\"]*)\"" % (tag, name), xml)
-            return mm.group(1)
+            return mm.group(1) if mm else default
 
         px = [float(t) for t in attr("static_plane", "x").split()]
         pn = [float(t) for t in attr("static_plane", "n").split()]
@@ -116,6 +116,8 @@ def extract_slope_scenes(ref):
             eval_every=int(attr("sobogus_friction_solver", "eval_every")),
             staggering=attr("sobogus_friction_solver", "staggering"),
             cache_impulses=attr("sobogus_friction_solver", "cache_impulses"),
+            stabilization=int(attr("sobogus_friction_solver", "stabilization", "0")),
+            penetration_threshold=float(attr("sobogus_friction_solver", "penetration_threshold", "0")),
             gravity=[float(attr("gravity", "fx")), float(attr("gravity", "fy"))],
             plane_x=px, plane_n=pn,
             ball=dict(x=float(attr("ball", "x")), y=float(attr("ball", "y")), vx=float(attr("ball", "vx")),

@@ -4,7 +4,8 @@
   with the reference's criterion (grid pairs == all pairs, :34-40).
 * CCD narrow phase: the 11 cases of scisimtests/narrowphase_tests.cpp.
 * Analytic friction: the ball-on-slope scenes registered in
-  ball2dcli/CMakeLists.txt:78-98, checked against the closed forms of
+  ball2dcli/CMakeLists.txt:78-98 (geometric staggering) and :102-122 (symplectic Euler
+  staggering with the impulse cache), checked against the closed forms of
   assets/ball2d/shell_scripts/sliding_particle_test.py:44-54 and
   static_particle_test.py:32-47 with the registered tolerances.
 """
@@ -85,18 +86,22 @@ def analytic_error(scene, q, v, time):
     return [abs(q[0] - dx), abs(q[1] - dy), abs(vx - v[0]), abs(vy - v[1])]
 
 
+CACHE = {"none": 0, "normal": 1, "normal_and_friction": 2}
+STAGGER = {"geometric": 0, "symplectic_euler": 1}
+
+
 def make_slope_oracle(oracle, s):
     b = s["ball"]
     return oracle.Ball2D([b["x"], b["y"]], [b["vx"], b["vy"]], [b["r"]], [b["m"]], s["plane_x"], s["plane_n"],
                          dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=s["tol"],
                          max_iters=s["max_iters"], eval_every=s["eval_every"],
                          integrator=oracle.VERLET if s["integrator"] == "verlet" else oracle.SYMPLECTIC_EULER,
-                         cache_mode=oracle.CACHE_NONE)
+                         cache_mode=CACHE[s["cache_impulses"]], staggering=STAGGER[s["staggering"]],
+                         stabilize=bool(s["stabilization"]), penetration_threshold=s["penetration_threshold"])
 
 
 @pytest.mark.parametrize("scene", SLOPES, ids=[s["name"] for s in SLOPES])
 def test_slope_scene_closed_form(oracle, scene):
-    assert scene["staggering"] == "geometric" and scene["cache_impulses"] == "none"
     sim = make_slope_oracle(oracle, scene)
     per = int(round(scene["output_frequency"] / scene["dt"]))
     for k in range(1, int(round(scene["end_time"] / scene["output_frequency"])) + 1):

@@ -59,7 +59,7 @@ def test_decimal_dt_is_exact():
 UNSUPPORTED = {
     "static_drum": BALL2D.replace('<ball x="0.7"', '<static_drum x="0" y="0" r="5"/>\n  <ball x="0.7"'),
     "fixed": BALL2D.replace('m="1.0" r="0.2" fixed="0"', 'm="1.0" r="0.2" fixed="1"'),
-    "staggering": BALL2D.replace('staggering="geometric"', 'staggering="symplectic_euler"'),
+    "staggering": BALL2D.replace('staggering="geometric"', 'staggering="stabilized"'),
     "integrator": BALL2D.replace('type="verlet"', 'type="explicit_euler"'),
 }
 
@@ -120,3 +120,14 @@ def test_registered_slope_scenes_match_the_golden_extraction():
         b = g["ball"]
         assert list(s["q"]) == [b["x"], b["y"]] and list(s["v"]) == [b["vx"], b["vy"]]
         assert s["m"][0] == b["m"] and s["r"][0] == b["r"]
+
+
+def test_symplectic_euler_staggering():
+    text = BALL2D.replace('CoR="0.2"', 'CoR="0.0"').replace(
+        'staggering="geometric"', 'staggering="symplectic_euler" stabilization="1" penetration_threshold="1.0e-5"')
+    s = scene_io.load_ball2d_scene(text)
+    assert s["staggering"] == "symplectic_euler" and s["stabilization"] and s["penetration_threshold"] == 1e-5
+    _, _, _, ifmap = scene_io.ball2d_objects(s)
+    assert ifmap.name() == "symplectic_euler_impact_friction_map" and ifmap.stabilize
+    with pytest.raises(scene_io.SceneError, match="CoR"):
+        scene_io.load_ball2d_scene(text.replace('CoR="0.0"', 'CoR="0.5"'))
