@@ -43,8 +43,9 @@ typedef enum {
 enum { SG_SYMPLECTIC_EULER = 0, SG_VERLET = 1, SG_SPLIT_HAM = 2 };
 /* ImpulsesToCache (scisim/ConstrainedMaps/ImpulsesToCache.h) */
 enum { SG_CACHE_NONE = 0, SG_CACHE_NORMAL = 1, SG_CACHE_NORMAL_AND_FRICTION = 2 };
-/* Staggering of a Ball2D step: GeometricImpactFrictionMap or SymplecticEulerImpactFrictionMap. */
-enum { SG_STAGGER_GEOMETRIC = 0, SG_STAGGER_SYMPLECTIC_EULER = 1 };
+/* Staggering of a Ball2D step: GeometricImpactFrictionMap, SymplecticEulerImpactFrictionMap or
+ * StabilizedImpactFrictionMap. */
+enum { SG_STAGGER_GEOMETRIC = 0, SG_STAGGER_SYMPLECTIC_EULER = 1, SG_STAGGER_STABILIZED = 2 };
 /* Arithmetic of the Gauss-Seidel sweeps. */
 enum { SG_PRECISION_FP64 = 0, SG_PRECISION_FP32_REFINE = 1 };
 
@@ -315,7 +316,10 @@ SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
  * extra relative velocities N^T vdelta and D^T vdelta (plus min(0, gap(q0)) / dt where stabilize
  * is set and the gap exceeds penetration_threshold in magnitude), and the step ends with
  * v1 = v + vdelta, q1 = q0 + dt v1, whatever the context's integrator.  It needs CoR = 0, as the
- * reference does; batched and sphere scenes step with the geometric map only. */
+ * reference does.  SG_STAGGER_STABILIZED is StabilizedImpactFrictionMap
+ * (scisim/ConstrainedMaps/StabilizedImpactFrictionMap.cpp:48-167): the unconstrained step, then
+ * a cold solve from its velocity, then q1 = q0 + dt v; it keeps no impulse cache (cache_mode NONE).
+ * Batched and sphere scenes step with the geometric map only. */
 SG_API int sg_set_staggering(sg_ctx* ctx, int32_t staggering, int32_t stabilize, double penetration_threshold);
 
 /* Checkpoint / resume of a context holding one Ball2D or sphere scene (replaces SCISim's binary

@@ -373,6 +373,9 @@ extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* s
   (void)iteration;
   const int nb = s->nb;
   const bool se = s->p.staggering == OR_STAGGER_SYMPLECTIC_EULER;
+  // StabilizedImpactFrictionMap::flow (StabilizedImpactFrictionMap.cpp:48-167): the unconstrained
+  // step first, then a cold solve from its velocity v1, then q1 = q0 + dt v.
+  const bool stab = s->p.staggering == OR_STAGGER_STABILIZED;
   const double dt = s->p.dt;
   std::vector<double> q1(2 * nb), v1(2 * nb), vdelta;
   if (se) {
@@ -488,8 +491,8 @@ extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* s
                            mu.data(), nrel.data(), drel.data(), &gp, alpha.data(), beta.data(), v2.data(), f.data(),
                            &gr);
   } else {
-    or_sobogus_solve_2d(nb, s->m.data(), s->v.data(), nc, ia.data(), ib.data(), bases.data(), CoR.data(),
-                        mu.data(), &gp, alpha.data(), beta.data(), v2.data(), f.data(), &gr);
+    or_sobogus_solve_2d(nb, s->m.data(), stab ? v1.data() : s->v.data(), nc, ia.data(), ib.data(), bases.data(),
+                        CoR.data(), mu.data(), &gp, alpha.data(), beta.data(), v2.data(), f.data(), &gr);
   }
   s->next_order.clear();
   // cacheImpulses (:222-264)
@@ -516,6 +519,12 @@ extern "C" int or_ball2d_step(or_ball2d* s, uint32_t iteration, or_step_stats* s
     // v1 = v2 + vdelta, q1 = q0 + dt v1 (:363, :406).
     for (int i = 0; i < 2 * nb; ++i) {
       v1[i] = v2[i] + vdelta[i];
+      q1[i] = s->q[i] + dt * v1[i];
+    }
+  } else if (stab) {
+    // v1 = v2, q1 = q0 + dt v1 (StabilizedImpactFrictionMap.cpp:136, :167).
+    for (int i = 0; i < 2 * nb; ++i) {
+      v1[i] = v2[i];
       q1[i] = s->q[i] + dt * v1[i];
     }
   } else {

@@ -419,8 +419,11 @@ static double solve2d_impl(int nb, const double* m, const double* v0, int nc, co
     const double ndotv = nx * vrx + ny * vry;
     // Kinematic relative velocity is zero for balls and static planes:
     // nrel = -(0 . n), drel = -(0 . t)  (Constraint.cpp:110-123).
-    const double nrel = nrel_in ? nrel_in[k] : -(0.0 * nx + 0.0 * ny);
-    const double drel = drel_in ? drel_in[k] : -(0.0 * tx + 0.0 * ty);
+    // Kinematic relative velocities, plus the map's extra ones (Sobogus.cpp:890-904).
+    double nrel = -(0.0 * nx + 0.0 * ny);
+    double drel = -(0.0 * tx + 0.0 * ty);
+    if (nrel_in) nrel = nrel + nrel_in[k];
+    if (drel_in) drel = drel + drel_in[k];
     // Forcing term w = n (CoR ndotv + nrel) + t drel (Constraint.cpp:27-33).
     const double s = CoR[k] * ndotv + nrel;
     const double wx = (0.0 + nx * s) + tx * drel;

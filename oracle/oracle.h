@@ -87,7 +87,7 @@ typedef struct or_ball2d or_ball2d;
 
 enum { OR_SYMPLECTIC_EULER = 0, OR_VERLET = 1 };
 enum { OR_CACHE_NONE = 0, OR_CACHE_NORMAL = 1, OR_CACHE_NORMAL_AND_FRICTION = 2 };
-enum { OR_STAGGER_GEOMETRIC = 0, OR_STAGGER_SYMPLECTIC_EULER = 1 };
+enum { OR_STAGGER_GEOMETRIC = 0, OR_STAGGER_SYMPLECTIC_EULER = 1, OR_STAGGER_STABILIZED = 2 };
 
 typedef struct {
   int32_t integrator;     // OR_SYMPLECTIC_EULER / OR_VERLET
@@ -99,7 +99,7 @@ typedef struct {
   double tol;
   uint32_t max_iters;
   uint32_t eval_every;
-  int32_t staggering;             // OR_STAGGER_* (GeometricImpactFrictionMap / SymplecticEulerImpactFrictionMap)
+  int32_t staggering;             // OR_STAGGER_* (Geometric / SymplecticEuler / Stabilized ImpactFrictionMap)
   int32_t stabilize;              // symplectic Euler: pose stabilisation g0 / dt
   double penetration_threshold;   // symplectic Euler: gaps smaller in magnitude are ignored
 } or_ball2d_params;

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 SYMPLECTIC_EULER, VERLET = 0, 1
 CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
-STAGGER_GEOMETRIC, STAGGER_SYMPLECTIC_EULER = 0, 1
+STAGGER_GEOMETRIC, STAGGER_SYMPLECTIC_EULER, STAGGER_STABILIZED = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)

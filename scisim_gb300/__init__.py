@@ -6,11 +6,11 @@ UnconstrainedMap / FrictionSolver / ImpactFrictionMap interfaces.
 """
 from ._lib import Context, SgError  # noqa: F401
 from .ball2d import (Ball2DSim, Ball2DState, GeometricImpactFrictionMap, ImpulsesToCache, Sobogus,  # noqa: F401
-                     SobogusSolverType, StaticPlane, SymplecticEulerImpactFrictionMap, SymplecticEulerMap,
-                     VerletMap)
+                     SobogusSolverType, StabilizedImpactFrictionMap, StaticPlane, SymplecticEulerImpactFrictionMap,
+                     SymplecticEulerMap, VerletMap)
 from .rigidbody3d import RigidBody3DSim, RigidBody3DState, RigidBodySphere, SplitHamMap  # noqa: F401
 
 __all__ = ["Context", "SgError", "Ball2DSim", "Ball2DState", "GeometricImpactFrictionMap", "ImpulsesToCache",
-           "Sobogus", "SobogusSolverType", "StaticPlane", "SymplecticEulerImpactFrictionMap", "SymplecticEulerMap",
+           "Sobogus", "SobogusSolverType", "StabilizedImpactFrictionMap", "StaticPlane", "SymplecticEulerImpactFrictionMap", "SymplecticEulerMap",
            "VerletMap", "RigidBody3DSim",
            "RigidBody3DState", "RigidBodySphere", "SplitHamMap"]

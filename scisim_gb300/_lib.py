@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "SG_OK", 1: "SG_NOT_CONVERGED", 2: "SG_BAD_INPUT", 3: "SG_DEV
 SYMPLECTIC_EULER, VERLET, SPLIT_HAM = 0, 1, 2
 CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
 PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
-STAGGER_GEOMETRIC, STAGGER_SYMPLECTIC_EULER = 0, 1
+STAGGER_GEOMETRIC, STAGGER_SYMPLECTIC_EULER, STAGGER_STABILIZED = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -431,7 +431,8 @@ class Context:
         check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
 
     def set_staggering(self, staggering=STAGGER_GEOMETRIC, stabilize=False, penetration_threshold=0.0):
-        """GeometricImpactFrictionMap (default) or SymplecticEulerImpactFrictionMap for this Ball2D scene."""
+        """GeometricImpactFrictionMap (default), SymplecticEulerImpactFrictionMap or
+        StabilizedImpactFrictionMap for this Ball2D scene."""
         check(lib().sg_set_staggering(self._h, int(staggering), 1 if stabilize else 0, float(penetration_threshold)),
               "sg_set_staggering")
 

@@ -193,6 +193,25 @@ class SymplecticEulerImpactFrictionMap(GeometricImpactFrictionMap):
         return ctx
 
 
+class StabilizedImpactFrictionMap(GeometricImpactFrictionMap):
+    """scisim/ConstrainedMaps/StabilizedImpactFrictionMap.cpp:48-167 on the GPU: the unconstrained step,
+    a cold solve from its velocity (no impulse cache), then q1 = q0 + dt v1."""
+
+    def __init__(self, abs_tol: float, max_iters: int):
+        super().__init__(abs_tol, max_iters, ImpulsesToCache.NONE)
+
+    def name(self):
+        return "stabilized_impact_friction_map"
+
+    def _context(self, sim, umap, solver, dt, CoR, mu):
+        fresh = self._ctx is None
+        ctx = super()._context(sim, umap, solver, dt, CoR, mu)
+        if fresh or ctx is not getattr(self, "_staggered", None):
+            ctx.set_staggering(_lib.STAGGER_STABILIZED)
+            self._staggered = ctx
+        return ctx
+
+
 class StaticPlane:
     """ball2d/StaticGeometry/StaticPlane.cpp:10-19 (normal normalised on upload)."""
 

@@ -77,6 +77,10 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     set_error("the symplectic Euler staggering needs CoR = 0");
     return SG_BAD_INPUT;
   }
+  if (ctx->staggering == SG_STAGGER_STABILIZED && ctx->cfg.cache_mode != SG_CACHE_NONE) {
+    set_error("the stabilized staggering keeps no impulse cache");
+    return SG_BAD_INPUT;
+  }
   if (nb == 0) {
     if (out) *out = st;
     return SG_OK;
@@ -124,7 +128,8 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   P.nc = nc;
   P.minv = ctx->minv.as<double>();
   P.m = ctx->m.as<double>();
-  P.v0 = ctx->v.as<double>();
+  // The stabilized map solves from the unconstrained step's velocity (StabilizedImpactFrictionMap.cpp:127).
+  P.v0 = ctx->staggering == SG_STAGGER_STABILIZED ? ctx->v1.as<double>() : ctx->v.as<double>();
   P.ia = ctx->ia.as<int>();
   P.ib = ctx->ib.as<int>();
   P.n = ctx->n.as<double>();
@@ -1168,9 +1173,13 @@ int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes) {
 }
 
 int sg_set_staggering(sg_ctx* ctx, int32_t staggering, int32_t stabilize, double penetration_threshold) {
-  if (!ctx || (staggering != SG_STAGGER_GEOMETRIC && staggering != SG_STAGGER_SYMPLECTIC_EULER) ||
+  if (!ctx || staggering < SG_STAGGER_GEOMETRIC || staggering > SG_STAGGER_STABILIZED ||
       !(penetration_threshold >= 0.0)) {
-    set_error("sg_set_staggering: staggering SG_STAGGER_GEOMETRIC or SG_STAGGER_SYMPLECTIC_EULER, threshold >= 0");
+    set_error("sg_set_staggering: staggering SG_STAGGER_GEOMETRIC, _SYMPLECTIC_EULER or _STABILIZED, threshold >= 0");
+    return SG_BAD_INPUT;
+  }
+  if (staggering == SG_STAGGER_STABILIZED && ctx->cfg.cache_mode != SG_CACHE_NONE) {
+    set_error("sg_set_staggering: the stabilized staggering keeps no impulse cache (cache_mode NONE)");
     return SG_BAD_INPUT;
   }
   if (staggering == SG_STAGGER_SYMPLECTIC_EULER && ctx->cfg.CoR != 0.0) {

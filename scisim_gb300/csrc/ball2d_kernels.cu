@@ -99,13 +99,18 @@ __global__ void k_predict_se(int nb, double dt, double gx, double gy, const doub
   aabb[i] = b;
 }
 
-// Its final update: v1 = v2 + vdelta, q1 = q0 + dt v1 (:363, :406).
+// Its final update: v1 = v2 + vdelta, q1 = q0 + dt v1 (:363, :406); without vdelta the
+// StabilizedImpactFrictionMap's v1 = v2, q1 = q0 + dt v1 (StabilizedImpactFrictionMap.cpp:136, :167).
 __global__ void k_final_se(int nb, double dt, const double2* __restrict__ q0, const double2* __restrict__ v2,
                            const double2* __restrict__ vdelta, double2* __restrict__ q1, double2* __restrict__ v1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
-  const double2 q = q0[i], w = v2[i], d = vdelta[i];
-  const double2 vn = make_double2(w.x + d.x, w.y + d.y);
+  const double2 q = q0[i], w = v2[i];
+  double2 vn = w;
+  if (vdelta) {
+    const double2 d = vdelta[i];
+    vn = make_double2(w.x + d.x, w.y + d.y);
+  }
   v1[i] = vn;
   q1[i] = make_double2(q.x + dt * vn.x, q.y + dt * vn.y);
 }
@@ -442,8 +447,8 @@ __device__ __forceinline__ void assemble_one(const AssembleArgs& A, int k, doubl
       tt = tt + (-tx) * db.x;
       tt = tt + (-ty) * db.y;
     }
-    nrel = 0.0 + 1.0 * tn;
-    drel = 0.0 + 1.0 * tt;
+    double ext_n = 0.0 + 1.0 * tn;
+    const double ext_d = 0.0 + 1.0 * tt;
     if (A.stabilize) {
       const double2 qa = A.q0[a];
       double gap;
@@ -457,8 +462,11 @@ __device__ __forceinline__ void assemble_one(const AssembleArgs& A, int k, doubl
       }
       double g0 = (gap < 0.0) ? gap : 0.0;  // std::min(0.0, gap)
       if (fabs(g0) < A.pen_thresh) g0 = 0.0;
-      nrel = nrel + g0 / A.dt;
+      ext_n = ext_n + g0 / A.dt;
     }
+    // Sobogus::solve adds the map's extra relative velocities to the kinematic ones (Sobogus.cpp:890-904).
+    nrel = nrel + ext_n;
+    drel = drel + ext_d;
   }
   const double s = CoR * ndotv + nrel;
   const double wx = (0.0 + nx * s) + tx * drel;
@@ -928,6 +936,7 @@ int assemble_contacts(sg_ctx* ctx, int nc) {
   A.mu_out = ctx->mu.as<double>();
   A.r = ctx->r_loc.as<double2>();
   A.key = ctx->key.as<unsigned long long>();
+  if (ctx->staggering == SG_STAGGER_STABILIZED) A.v0 = ctx->v1.as<double2>();  // the unconstrained step's
   if (ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER) {
     A.vdelta = ctx->vdelta.as<double2>();
     A.rad = ctx->r.as<double>();
@@ -952,11 +961,12 @@ int extract_and_cache(sg_ctx* ctx, int nc) {
 int ball2d_final_map(sg_ctx* ctx, const double* vin) {
   const int nb = ctx->nb;
   if (nb <= 0) return SG_OK;
-  if (ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER && ctx->n_scenes == 0) {
+  if (ctx->staggering != SG_STAGGER_GEOMETRIC && ctx->n_scenes == 0) {
+    const bool se = ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER;
     k_final_se<<<blocks_for(nb), kBlock, 0, ctx->stream>>>(nb, ctx->cfg.dt, ctx->q.as<double2>(),
                                                           reinterpret_cast<const double2*>(vin),
-                                                          ctx->vdelta.as<double2>(), ctx->q1.as<double2>(),
-                                                          ctx->v1.as<double2>());
+                                                          se ? ctx->vdelta.as<double2>() : nullptr,
+                                                          ctx->q1.as<double2>(), ctx->v1.as<double2>());
     SG_CUDA_TRY(cudaGetLastError());
     return SG_OK;
   }

@@ -3,7 +3,7 @@
 Ball2D (`<ball2d_scene>`, ball2dutils/Ball2DSceneParser.cpp) and RigidBody3D sphere scenes
 (`<rigidbody3d_scene>`, rigidbody3dutils/RigidBody3DSceneParser.cpp) with the elements of the contact
 path: integrator, `sobogus_friction_solver` with geometric staggering (and, for Ball2D, the
-symplectic_euler staggering), gravity, static planes, balls or spheres.  Values are read the way the reference reads them: scalars as C++ stream extraction of
+symplectic_euler and stabilized staggerings), gravity, static planes, balls or spheres.  Values are read the way the reference reads them: scalars as C++ stream extraction of
 a decimal (Python's float of the same text rounds the same way), the time step as an exact rational
 (`Rational<intmax_t>` from a decimal or `a/b`, Rational.h:204-260) taken as numerator / denominator.
 Elements of features outside the contact path (drums, portals, penalty forces, other solvers and
@@ -85,7 +85,7 @@ def _solver(root, tag_3d=False):
     nd = nodes[0]
     tag = "sobogus_friction_solver"
     stag = _attr(nd, "staggering", tag)
-    allowed = ("geometric",) if tag_3d else ("geometric", "symplectic_euler")
+    allowed = ("geometric",) if tag_3d else ("geometric", "symplectic_euler", "stabilized")
     if stag not in allowed:
         raise SceneError("%s: staggering %r is not supported (%s)" % (tag, stag, ", ".join(allowed)))
     cache = _attr(nd, "cache_impulses", tag)
@@ -95,6 +95,9 @@ def _solver(root, tag_3d=False):
                max_iters=int(_attr(nd, "max_iters", tag)), eval_every=int(_attr(nd, "eval_every", tag)),
                cache_mode=CACHE_MODES[cache])
     out["staggering"] = stag
+    if stag == "stabilized" and out["cache_mode"] != 0:
+        # Ball2DSceneParser.cpp:1400-1408
+        raise SceneError("%s: the stabilized staggering keeps no impulse cache" % tag)
     if stag == "symplectic_euler":
         # Ball2DSceneParser.cpp:1354-1398: CoR must be 0; stabilization and its threshold.
         if out["CoR"] != 0.0:
@@ -232,13 +235,15 @@ def ball2d_objects(scene: dict):
     its unconstrained map, the Sobogus solver and the geometric impact-friction map.  Step with
     sim.flow(iteration, scene['dt'], umap, scene['CoR'], scene['mu'], solver, ifmap)."""
     from .ball2d import (Ball2DSim, Ball2DState, GeometricImpactFrictionMap, ImpulsesToCache, Sobogus,
-                         SobogusSolverType, StaticPlane, SymplecticEulerImpactFrictionMap, SymplecticEulerMap,
-                         VerletMap)
+                         SobogusSolverType, StabilizedImpactFrictionMap, StaticPlane, SymplecticEulerImpactFrictionMap,
+                         SymplecticEulerMap, VerletMap)
     planes = [StaticPlane(x, n) for x, n in zip(scene["plane_x"], scene["plane_n"])]
     sim = Ball2DSim(Ball2DState(scene["q"], scene["v"], scene["r"], scene["m"], planes), gravity=scene["gravity"])
     umap = VerletMap() if scene["integrator"] == "verlet" else SymplecticEulerMap()
     solver = Sobogus(SobogusSolverType.Balls2D, eval_every=scene["eval_every"])
-    if scene.get("staggering") == "symplectic_euler":
+    if scene.get("staggering") == "stabilized":
+        ifmap = StabilizedImpactFrictionMap(scene["tol"], scene["max_iters"])
+    elif scene.get("staggering") == "symplectic_euler":
         ifmap = SymplecticEulerImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache(scene["cache_mode"]),
                                                  scene["stabilization"], scene["penetration_threshold"])
     else:

@@ -1,9 +1,11 @@
-"""SymplecticEulerImpactFrictionMap on the GPU (sg_set_staggering) against the oracle's restatement,
-which the reference's 18 registered symplectic-Euler slope tests pin (tests/test_oracle_golden.py).
+"""SymplecticEulerImpactFrictionMap and StabilizedImpactFrictionMap on the GPU (sg_set_staggering)
+against the oracle's restatements, which the reference's 18 registered symplectic-Euler slope tests and
+its drift-safe scene pin (tests/test_oracle_golden.py).
 
 Bars: a registered slope scene bit-exact over 2,000 steps; a frictional box drop with the impulse
 cache and pose stabilisation bit-exact every step (positions, velocities, impulses, sweeps and
 residual) when the oracle replays the GPU's colour order; restitution rejected as in the reference.
+The stabilized map: the drift-safe scene bit-exact and at rest, a box drop bit-exact every step.
 """
 import json
 import os
@@ -73,4 +75,42 @@ def test_restitution_is_rejected(gpulib):
     ctx = gpulib.Context(CoR=0.3)
     with pytest.raises(gpulib.SgError):
         ctx.set_staggering(gpulib.STAGGER_SYMPLECTIC_EULER)
+    ctx.close()
+
+
+def test_stabilized_drift_safe_scene_bitexact(gpulib, oracle):
+    kw = dict(dt=0.01, gravity=(0.0, -10.0), mu=0.5, CoR=0.0, tol=1e-12, max_iters=5000, eval_every=1, cache_mode=0)
+    ctx = gpulib.Context(integrator=gpulib.VERLET, **kw)
+    ctx.upload_ball2d([0.0, 1.0], [0.0, 0.0], [0.5], [8.0], [[0.0, 0.0]], [[0.0, 1.0]])
+    ctx.set_staggering(gpulib.STAGGER_STABILIZED)
+    ctx.step(450)
+    ora = oracle.Ball2D([0.0, 1.0], [0.0, 0.0], [0.5], [8.0], [[0.0, 0.0]], [[0.0, 1.0]], integrator=oracle.VERLET,
+                        staggering=oracle.STAGGER_STABILIZED, **kw)
+    ora.run(450)
+    gq, gv = ctx.state()
+    oq, ov = ora.state()
+    assert np.array_equal(gq, oq) and np.array_equal(gv, ov) and np.all(gv == 0.0)
+    ctx.close()
+
+
+def test_stabilized_box_drop_replayed_order_bitexact(gpulib, oracle):
+    s = scenes.box_drop_1024(seed=4, n_side=14)
+    kw = dict(dt=s["dt"], gravity=s["gravity"], mu=0.5, CoR=0.3, tol=1e-9, max_iters=500, cache_mode=0)
+    ctx = gpulib.Context(**kw)
+    ctx.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    ctx.set_staggering(gpulib.STAGGER_STABILIZED)
+    ora = oracle.Ball2D(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"],
+                        staggering=oracle.STAGGER_STABILIZED, **kw)
+    for step in range(60):
+        st = ctx.step(1)
+        order, _ = ctx.last_solve_order()
+        if st["n_contacts"]:
+            ora.set_next_order(order)
+        ost = ora.step()
+        assert st["n_contacts"] == ost["n_contacts"], step
+        gq, gv = ctx.state()
+        oq, ov = ora.state()
+        assert np.array_equal(gq, oq) and np.array_equal(gv, ov), step
+    with pytest.raises(gpulib.SgError):
+        gpulib.Context(cache_mode=2).set_staggering(gpulib.STAGGER_STABILIZED)
     ctx.close()

@@ -109,3 +109,20 @@ def test_slope_scene_closed_form(oracle, scene):
         q, v = sim.state()
         err = analytic_error(scene, q, v, sim.iteration * scene["dt"])
         assert all(e <= t for e, t in zip(err, scene["tolerances"])), (k, err, scene["tolerances"])
+
+
+def test_stabilized_map_is_drift_safe(oracle):
+    """StabilizedImpactFrictionMap on the reference's drift-safe scene
+    (assets/ball2d/tests_serialization/drift_safe_ball_on_plane.xml, registered in
+    ball2dcli/CMakeLists.txt:23): a ball dropped on a plane comes to rest above it and then does not
+    move at all (each step's solve cancels the unconstrained step's normal velocity)."""
+    sim = oracle.Ball2D([0.0, 1.0], [0.0, 0.0], [0.5], [8.0], [[0.0, 0.0]], [[0.0, 1.0]], dt=0.01,
+                        gravity=(0.0, -10.0), mu=0.5, CoR=0.0, tol=1e-12, max_iters=5000, eval_every=1,
+                        integrator=oracle.VERLET, cache_mode=oracle.CACHE_NONE,
+                        staggering=oracle.STAGGER_STABILIZED)
+    sim.run(200)
+    q_rest, v_rest = sim.state()
+    assert 0.5 - 1e-12 <= q_rest[1] <= 0.5 + 0.2 and np.all(v_rest == 0.0)
+    sim.run(250)
+    q, v = sim.state()
+    assert np.array_equal(q, q_rest) and np.all(v == 0.0)

@@ -59,7 +59,7 @@ def test_decimal_dt_is_exact():
 UNSUPPORTED = {
     "static_drum": BALL2D.replace('<ball x="0.7"', '<static_drum x="0" y="0" r="5"/>\n  <ball x="0.7"'),
     "fixed": BALL2D.replace('m="1.0" r="0.2" fixed="0"', 'm="1.0" r="0.2" fixed="1"'),
-    "staggering": BALL2D.replace('staggering="geometric"', 'staggering="stabilized"'),
+    "staggering": BALL2D.replace('staggering="geometric"', 'staggering="staggered_projections"'),
     "integrator": BALL2D.replace('type="verlet"', 'type="explicit_euler"'),
 }
 
@@ -131,3 +131,12 @@ def test_symplectic_euler_staggering():
     assert ifmap.name() == "symplectic_euler_impact_friction_map" and ifmap.stabilize
     with pytest.raises(scene_io.SceneError, match="CoR"):
         scene_io.load_ball2d_scene(text.replace('CoR="0.0"', 'CoR="0.5"'))
+
+
+def test_stabilized_staggering():
+    text = BALL2D.replace('staggering="geometric"', 'staggering="stabilized"')
+    with pytest.raises(scene_io.SceneError, match="cache"):
+        scene_io.load_ball2d_scene(text)
+    s = scene_io.load_ball2d_scene(text.replace('cache_impulses="normal_and_friction"', 'cache_impulses="none"'))
+    assert s["staggering"] == "stabilized"
+    assert scene_io.ball2d_objects(s)[3].name() == "stabilized_impact_friction_map"
