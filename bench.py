@@ -220,13 +220,18 @@ def timed_steps(ctx, torch, stream, k, flush):
     return ms, contacts
 
 
-def batch_leg(args, torch, local, flush):
+def batch_leg(args, torch, local, flush, ws=1, rank=0):
     """Batched Ball2D scenes (independent scenes of 16-4,096 discs stepped together from a
     CUDA graph, warm start from each scene's impulse cache) against the plain solver on a
     sample of the same scenes (one context per scene, FP64, cold start), over the same steps
-    from the same state."""
-    from scisim_gb300 import _lib, scenes
+    from the same state.  With several ranks the scenes are sharded by work (scisim_gb300.dist),
+    each rank steps its shard, and the throughput is the sum of contact-steps over the slowest
+    rank's time; the plain comparison runs on rank 0."""
+    from scisim_gb300 import _lib, dist, scenes
     b = scenes.ball2d_batch(n_scenes=args.batch_scenes)
+    S_all = len(b["mu"])
+    if ws > 1:
+        b = dist.batch_slice(b, dist.shard_scenes(dist.batch_work(b), ws)[rank])
     S, N = len(b["mu"]), int(b["body_off"][-1])
     kw = dict(dt=b["dt"], gravity=b["gravity"], tol=1e-6, max_iters=args.preroll_iters, device=local,
               integrator=_lib.SYMPLECTIC_EULER)
@@ -251,8 +256,14 @@ def batch_leg(args, torch, local, flush):
     ms = e0.elapsed_time(e1)
     prof = ctx.profile_read(reset=True)
     stats = ctx.batch_scene_stats()
-    value = st["total_contacts"] / (ms / 1e3)
+    job_contacts = dist.sum_over_ranks(st["total_contacts"], device="cuda")
+    N_all = int(dist.sum_over_ranks(N, device="cuda"))
+    ms = dist.max_over_ranks(ms, device="cuda")
+    value = job_contacts / (ms / 1e3)
     log("batch: %d scenes, %d discs, %d contact-steps in %.1f ms" % (S, N, st["total_contacts"], ms))
+    if rank != 0:
+        ctx.close()
+        return None
     # Plain: the first scenes of a fixed random sample, each alone, cold FP64, same steps.
     rng = np.random.default_rng(0)
     pick = rng.choice(S, min(args.batch_plain_scenes, S), replace=False)
@@ -275,9 +286,10 @@ def batch_leg(args, torch, local, flush):
         pms += a0.elapsed_time(a1)
         c.close()
     plain = pc / (pms / 1e3) if pms > 0 else None
-    out = {"workload": "ball2d_batch_%d" % S, "scenes": S, "discs": N, "value": value, "unit": UNIT,
+    out = {"workload": "ball2d_batch_%d" % S_all, "scenes": S_all, "ranks": ws, "discs": N_all, "value": value,
+           "unit": UNIT,
            "steps": args.batch_steps, "timed_steps": [args.batch_preroll + 9, args.batch_preroll + 8 + args.batch_steps],
-           "ms_per_step": ms / args.batch_steps, "contacts_per_step": st["total_contacts"] / args.batch_steps,
+           "ms_per_step": ms / args.batch_steps, "contacts_per_step": job_contacts / args.batch_steps,
            "form": "batched (one CUDA graph per 8 steps), warm start (cache), %s" % (
                "FP32 sweeps + FP64 residual and refinement per scene" if args.precision == 1 else "FP64 sweeps"),
            "fp32_sweep_share": prof["contact_sweeps32"] / max(prof["contact_sweeps"] + prof["contact_sweeps32"], 1),
@@ -590,9 +602,10 @@ def run_ours(args):
         ectx.close()
 
     batched = None
-    if rank == 0 and args.batch_scenes > 0:
-        batched = batch_leg(args, torch, local, flush)
-        log("batched:", batched)
+    if args.batch_scenes > 0:
+        batched = batch_leg(args, torch, local, flush, ws, rank)
+        if rank == 0:
+            log("batched:", batched)
     learned = None
     if rank == 0 and args.mlp_hopper > 0:
         learned = mlp_leg(args, torch, local)
