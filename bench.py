@@ -352,6 +352,25 @@ def sphere_batch_leg(args, torch, local, flush):
         pms += a0.elapsed_time(a1)
         c.close()
     plain = pc / (pms / 1e3) if pms > 0 else None
+    # The same steps from the same state with FP32 sweeps and FP64 refinement, scene by scene.
+    c32 = _lib.Context(precision=_lib.PRECISION_FP32_REFINE, **dict(kw, max_iters=5000))
+    up = (b["body_off"], q0, v0, b["r"], b["m"], b["I0"], b["plane_off"], b["plane_x"], b["plane_n"], b["mu"], b["CoR"])
+    c32.upload_sphere3d_batch(*up)
+    c32.step(1)  # warm-up, then back to the timed state
+    c32.upload_sphere3d_batch(*up)
+    s32 = torch.cuda.ExternalStream(c32.stream_ptr(), device=local)
+    flush.zero_()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(s32)
+    r32 = c32.step(args.sphere_batch_steps)
+    f1.record(s32)
+    f1.synchronize()
+    ms32 = f0.elapsed_time(f1)
+    st32 = c32.batch_scene_stats()
+    v32 = r32["total_contacts"] / (ms32 / 1e3)
+    log("sphere batch FP32+FP64 refinement: %d contact-steps in %.1f ms" % (r32["total_contacts"], ms32))
+    c32.close()
     out = {"workload": "sphere_batch_%d" % S, "scenes": S, "spheres": N, "value": value, "unit": UNIT,
            "steps": args.sphere_batch_steps,
            "timed_steps": [args.sphere_batch_preroll + 2, args.sphere_batch_preroll + 1 + args.sphere_batch_steps],
@@ -361,7 +380,12 @@ def sphere_batch_leg(args, torch, local, flush):
            "gs_iterations_mean_last_step": float(stats["iterations"].mean()),
            "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
                               "form": "one context per scene, FP64, same steps from the same state"},
-           "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"]}
+           "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"],
+           "fp32_refine": {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.sphere_batch_steps,
+                           "scenes_converged_last_step": int(st32["succeeded"].sum()),
+                           "over_fp64_batched": v32 / value, "over_plain": v32 / plain if plain else None,
+                           "form": "batched, FP32 sweeps with FP64 checks and refinement, each scene to its "
+                                   "own tolerance"}}
     ctx.close()
     return out
 

@@ -1829,6 +1829,230 @@ __global__ void __launch_bounds__(kGs3mBlock, 1) k_gs3_mixed(Gs3Args A, Gs3m B) 
   }
 }
 
+// Batched sphere scenes in the FP32 form: k_gs3_batch's per-scene control with k_gs3_mixed's
+// per-scene modes (0: FP32 sweeps with FP64 checks on a growing schedule, 1: FP64 sweeps to finish,
+// entered when the scene reaches tol or its FP32 rounding floor), as k_gs_mixed_batch does for discs.
+struct Gs3MixedBatchArgs {
+  Gs3BatchArgs X;
+  int* mode;                        // S
+  unsigned* since;                  // S: checks since the scene's best residual
+  unsigned long long* exc_slot;     // 3 S ordered FP32-floor excess maxima (rotating)
+  unsigned long long* gmax;         // 3: largest FP32-mode residual of a check (interval control)
+  int* n64;                         // scenes in mode 1
+};
+
+__global__ void __launch_bounds__(kGs3mBlock, 1) k_gs3_mixed_batch(Gs3MixedBatchArgs M, Gs3m B) {
+  Gs3BatchArgs& X = M.X;
+  const Gs3Args& A = X.g;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  const int nc = A.nc, S = X.S;
+  for (int sc = tid; sc < S; sc += nthr) {
+    X.best[sc] = INFINITY;
+    X.bestbuf[sc] = 0;
+    X.iters[sc] = 0;
+    M.mode[sc] = 0;
+    M.since[sc] = 0;
+    const bool empty = X.sc_off[sc + 1] == X.sc_off[sc];
+    X.done[sc] = empty ? 1 : 0;
+    if (empty) atomicAdd(X.done_count, 1);
+  }
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  const unsigned eval32 = B.eval32 ? B.eval32 : 1u;
+  double* bufs[2] = {A.r_a, A.r_b};
+  if (!grid_sync(A.gb, A.spin)) {
+    if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+    return;
+  }
+  unsigned long long n32 = 0, n64 = 0, nev = 0, nlc = 0, nlb = 0;
+  unsigned it = 0, n_eval = 0, next_eval = 1, interval = eval32;
+  if (*((volatile int*)X.done_count) < S) {
+    for (it = 1; it <= A.max_iters; ++it) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int s = s_off[col] + blockIdx.x + gridDim.x * threadIdx.x; s < e; s += nthr) {
+          const int sc = X.scene_of[B.ab[s].x];
+          if (__ldcg(&X.done[sc])) continue;
+          if (__ldcg(&M.mode[sc]) == 0) {
+            gs_update3_f(B, s);
+            ++n32;
+          } else {
+            gs_update3(A, A.perm[s]);
+            ++n64;
+          }
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      const bool due32 = it == next_eval || it == A.max_iters;
+      const bool due64 = *((volatile int*)M.n64) > 0 && ((it % eval64 == 0) || it == A.max_iters);
+      if (!due32 && !due64) continue;
+      if (due32) {
+        // Lift the FP32 scenes' iterates to FP64 and resynchronise their FP32 body velocities.
+        for (int s = tid; s < nc; s += nthr) {
+          const int sc = X.scene_of[B.ab[s].x];
+          if (__ldcg(&X.done[sc]) || __ldcg(&M.mode[sc]) != 0) continue;
+          const int k = A.perm[s];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) A.r[3 * (size_t)k + j] = (double)__ldcg(&B.r[3 * (size_t)s + j]);
+          ++nlc;
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+        for (int i = tid; i < B.nb; i += nthr) {
+          const int sc = X.scene_of[i];
+          if (__ldcg(&X.done[sc]) || __ldcg(&M.mode[sc]) != 0) continue;
+          double hl[3], ha[3], Ii[9], wa[3];
+          gather_htr3(i, B.body_off, B.body_adj, A.C, A.r, hl, ha);
+#pragma unroll
+          for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)i + j];
+          matvec3(Ii, ha, wa);
+          const double mi = A.minv[i];
+          const double* vl = B.v0 + 3 * (size_t)i;
+          const double* va = B.v0 + 3 * (size_t)B.nb + 3 * (size_t)i;
+          const double4_32a lv = make_double4_32a(vl[0] + mi * hl[0], vl[1] + mi * hl[1], vl[2] + mi * hl[2], 0.0);
+          const double4_32a wv = make_double4_32a(va[0] + wa[0], va[1] + wa[1], va[2] + wa[2], 0.0);
+          A.V[2 * i] = lv;
+          A.V[2 * i + 1] = wv;
+          B.V[2 * i] = make_float4((float)lv.x, (float)lv.y, (float)lv.z, 0.0f);
+          B.V[2 * i + 1] = make_float4((float)wv.x, (float)wv.y, (float)wv.z, 0.0f);
+          ++nlb;
+        }
+        if (!grid_sync(A.gb, A.spin)) {
+          if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+          return;
+        }
+      }
+      // FP64 residual and FP32-floor excess of every due scene (contacts are scene-major).
+      const int slot = n_eval % 3;
+      unsigned long long* eslots = X.err_slot + (size_t)slot * S;
+      unsigned long long* xslots = M.exc_slot + (size_t)slot * S;
+      const int lane = threadIdx.x & 31;
+      for (int k0 = tid - lane; k0 < nc; k0 += nthr) {
+        const int k = k0 + lane;
+        int key = -1;
+        unsigned long long ve = 0ull, vx = 0ull;
+        if (k < nc) {
+          const int a = A.C.ia[k], b = A.C.ib[k];
+          const int sc = X.scene_of[a];
+          const int md = __ldcg(&M.mode[sc]);
+          if (!__ldcg(&X.done[sc]) && ((md == 0 && due32) || (md == 1 && due64))) {
+            double E[9], Aa[6], Ab[6], u[3];
+            load_contact(A.C, k, E, Aa, Ab);
+            local_u3(A.C, k, A.V, u, a, b, E, Aa, Ab);
+            const double rk[3] = {__ldcg(&A.r[3 * (size_t)k]), __ldcg(&A.r[3 * (size_t)k + 1]),
+                                  __ldcg(&A.r[3 * (size_t)k + 2])};
+            double* cand = bufs[1 - __ldcg(&X.bestbuf[sc])];
+            cand[3 * (size_t)k] = rk[0];
+            cand[3 * (size_t)k + 1] = rk[1];
+            cand[3 * (size_t)k + 2] = rk[2];
+            const double ek = fb_error_3d(rk, u, A.C.mu[k]);
+            const double4_32a la = ld4cg(&A.V[2 * a]), wa = ld4cg(&A.V[2 * a + 1]);
+            double scale = fabs(la.x) + fabs(la.y) + fabs(la.z) + fabs(wa.x) + fabs(wa.y) + fabs(wa.z);
+            if (b >= 0) {
+              const double4_32a lb = ld4cg(&A.V[2 * b]), wb = ld4cg(&A.V[2 * b + 1]);
+              scale += fabs(lb.x) + fabs(lb.y) + fabs(lb.z) + fabs(wb.x) + fabs(wb.y) + fabs(wb.z);
+            }
+            scale += fabs(A.C.c[3 * (size_t)k]) + fabs(A.C.c[3 * (size_t)k + 1]) + fabs(A.C.c[3 * (size_t)k + 2]) +
+                     fabs(rk[0]) + fabs(rk[1]) + fabs(rk[2]);
+            ve = f64_to_ordered(ek);
+            vx = f64_to_ordered(ek - 64.0 * 1.1920929e-7 * scale);
+            key = sc;
+            ++nev;
+          }
+        }
+        run_max_atomic3(ve, key, eslots);
+        run_max_atomic3(vx, key, xslots);
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      unsigned long long* enext = X.err_slot + (size_t)((n_eval + 1) % 3) * S;
+      unsigned long long* xnext = M.exc_slot + (size_t)((n_eval + 1) % 3) * S;
+      double gm = 0.0;
+      for (int sc = tid; sc < S; sc += nthr) {
+        enext[sc] = 0ull;
+        xnext[sc] = 0ull;
+        if (X.done[sc]) continue;
+        const int md = M.mode[sc];
+        if (!((md == 0 && due32) || (md == 1 && due64))) continue;
+        const double err = ordered_to_f64(__ldcg(&eslots[sc]));
+        const double exc = ordered_to_f64(__ldcg(&xslots[sc]));
+        if (err < X.best[sc]) {
+          X.best[sc] = err;
+          X.bestbuf[sc] ^= 1;
+          M.since[sc] = 0;
+        } else {
+          M.since[sc] += 1;
+        }
+        if (md == 1) {
+          if (err < A.tol) {
+            X.done[sc] = 1;
+            X.iters[sc] = it;
+            atomicAdd(X.done_count, 1);
+            atomicSub(M.n64, 1);
+          }
+        } else {
+          gm = nanmax(gm, err);
+          if (err < A.tol || exc <= A.tol || (M.since[sc] >= 16 && exc <= 16.0 * A.tol)) {
+            M.mode[sc] = 1;
+            atomicAdd(M.n64, 1);
+          }
+        }
+      }
+      gm = block_nanmax(gm);
+      if (threadIdx.x == 0 && due32) atomicMax(&M.gmax[slot], f64_to_ordered(gm));
+      if (tid == 0) M.gmax[(n_eval + 1) % 3] = 0ull;
+      ++n_eval;
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      if (due32) {
+        const double g = ordered_to_f64(*((volatile unsigned long long*)&M.gmax[slot]));
+        if (it < eval32) {
+          next_eval = 2 * it;
+        } else {
+          interval = (g > 1e3 * A.tol) ? min(2u * interval, 16u * eval32) : (g > 10.0 * A.tol ? interval : eval32);
+          next_eval = it + interval;
+        }
+      }
+      if (*((volatile int*)X.done_count) == S) break;
+    }
+  }
+  for (int k = tid; k < nc; k += nthr) {
+    const int sc = X.scene_of[A.C.ia[k]];
+    if (__ldcg(&X.done[sc]) || !(__ldcg(&X.best[sc]) < INFINITY)) continue;
+    const double* src = bufs[__ldcg(&X.bestbuf[sc])];
+    for (int j = 0; j < 3; ++j) A.r[3 * (size_t)k + j] = __ldcg(&src[3 * (size_t)k + j]);
+  }
+  for (int sc = tid; sc < S; sc += nthr)
+    if (!__ldcg(&X.done[sc])) X.iters[sc] = A.max_iters;
+  if (tid == 0) *X.unconverged += (unsigned long long)(S - *((volatile int*)X.done_count));
+  atomicAdd(&X.work[0], n32);
+  atomicAdd(&X.work[1], n64);
+  atomicAdd(&X.work[2], nev);
+  atomicAdd(&X.work[3], nlc);
+  atomicAdd(&X.work[4], nlb);
+  if (tid == 0) {
+    A.st->iterations = it > A.max_iters ? A.max_iters : it;
+    A.st->evals = n_eval;
+    A.st->converged = *((volatile int*)X.done_count) == S ? 1 : 0;
+  }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -2275,7 +2499,58 @@ int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out) {
   B.done_count = ctx->b_ctl.as<int>();
   B.unconverged = ctx->b_sums.as<unsigned long long>() + 1;
   B.work = ctx->b_work.as<unsigned long long>();
-  {
+  if (ctx->cfg.precision == SG_PRECISION_FP32_REFINE) {
+    // FP32 sweeps with FP64 refinement, scene by scene.
+    const size_t c = (size_t)std::max(nc, 1), b1 = (size_t)std::max(N, 1);
+    if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
+    if (int r = grow(ctx->pk3, sizeof(float) * 31 * c)) return r;   // E 9, Aa 6, Ab 6, c 3, W 6, mu 1
+    if (int r = grow(ctx->pk_r, sizeof(float) * 3 * c)) return r;
+    if (int r = grow(ctx->v32, sizeof(float4) * 2 * b1)) return r;
+    if (int r = grow(ctx->minv32, sizeof(float) * b1)) return r;
+    if (int r = grow(ctx->Iinv32, sizeof(float) * 9 * b1)) return r;
+    if (int r = grow(ctx->s_mode, sizeof(int) * (size_t)S)) return r;
+    if (int r = grow(ctx->s_since, sizeof(unsigned) * (size_t)S)) return r;
+    if (int r = grow(ctx->s_exc, sizeof(unsigned long long) * 3 * (size_t)S)) return r;
+    if (int r = grow(ctx->s_gmax, sizeof(unsigned long long) * 3)) return r;
+    float* f = ctx->pk3.as<float>();
+    Gs3m P;
+    P.ab = ctx->pk_ab.as<int2>();
+    P.E = f;
+    P.Aa = f + 9 * c;
+    P.Ab = f + 15 * c;
+    P.c = f + 21 * c;
+    P.W = f + 24 * c;
+    P.mu = f + 30 * c;
+    P.r = ctx->pk_r.as<float>();
+    P.V = ctx->v32.as<float4>();
+    P.minv = ctx->minv32.as<float>();
+    P.Iinv = ctx->Iinv32.as<float>();
+    P.v0 = ctx->v.as<double>();
+    P.body_off = off;
+    P.body_adj = adj;
+    P.nb = N;
+    P.eval32 = (unsigned)ctx->check_interval;
+    P.work = nullptr;
+    k_pack3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), C, A.r, P, P.r);
+    k_body32<<<blocks_for(N), kBlock, 0, s>>>(N, V, ctx->minv.as<double>(), ctx->Iinv.as<double>(), P.V,
+                                             const_cast<float*>(P.minv), const_cast<float*>(P.Iinv));
+    SG_CUDA_TRY(cudaGetLastError());
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_exc.p, 0, sizeof(unsigned long long) * 3 * (size_t)S, s));
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_gmax.p, 0, sizeof(unsigned long long) * 3, s));
+    Gs3MixedBatchArgs M;
+    M.X = B;
+    M.mode = ctx->s_mode.as<int>();
+    M.since = ctx->s_since.as<unsigned>();
+    M.exc_slot = ctx->s_exc.as<unsigned long long>();
+    M.gmax = ctx->s_gmax.as<unsigned long long>();
+    M.n64 = ctx->b_ctl.as<int>() + 1;
+    void* args[] = {&M, &P};
+    const int grid = coop_grid(ctx, k_gs3_mixed_batch, (long)ctx->num_sms * kGs3mBlock, kGs3mBlock, 1);
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_mixed_batch, grid, kGs3mBlock, args, s));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+    ctx->kernel_launches += 2;
+  } else {
     void* args[] = {&B};
     const int grid = coop_grid(ctx, k_gs3_batch, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
     if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
@@ -2306,8 +2581,11 @@ int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out) {
     return SG_CAPACITY;
   }
   ctx->gs_launches += 1;
+  ctx->contact_sweeps32 += work[0];
   ctx->contact_sweeps += work[1];
   ctx->contact_evals += work[2];
+  ctx->contact_lifts += work[3];
+  ctx->body_lifts += work[4];
   if (ctx->profile) {
     float ms = 0.f;
     SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));

@@ -77,3 +77,65 @@ def test_sphere_batch_c5_shape(gpulib):
     assert conv.sum() > 0
     assert np.all(stats["error"][conv] < 1e-6)
     ctx.close()
+
+
+def test_sphere_batch_fp32_refine(gpulib, oracle):
+    """FP32 sweeps + FP64 refinement, scene by scene: every scene that reports convergence meets the
+    tolerance under the oracle's FP64 residual of its own contacts (with the GPU's impulses), the
+    reported residual is that residual, and positions stay within 1e-3 of the FP64 batch."""
+    b = scenes.sphere_batch(n_scenes=8, seed=13, nmin=60, nmax=500)
+    S = len(b["mu"])
+    tol = 1e-7
+    kw = dict(integrator=gpulib.SPLIT_HAM, dt=b["dt"], gravity=b["gravity"], tol=tol, max_iters=3000)
+
+    def make(**extra):
+        ctx = gpulib.Context(**kw, **extra)
+        ctx.upload_sphere3d_batch(b["body_off"], b["q"], b["v"], b["r"], b["m"], b["I0"], b["plane_off"],
+                                  b["plane_x"], b["plane_n"], b["mu"], b["CoR"])
+        return ctx
+
+    f64, f32 = make(), make(precision=gpulib.PRECISION_FP32_REFINE)
+    for step in range(40):
+        f64.step(1, first_iteration=step + 1)
+    for step in range(39):
+        f32.step(1, first_iteration=step + 1)
+    q0, v0 = f32.state()
+    f32.step(1, first_iteration=40)
+    stats = f32.batch_scene_stats()
+    g = f32.sphere3d_last_contacts()
+    order, _ = f32.last_solve_order()
+    coff = np.concatenate([[0], np.cumsum(stats["n_contacts"])])
+    checked = 0
+    for s in range(S):
+        c0, c1 = int(coff[s]), int(coff[s + 1])
+        if c1 == c0:
+            continue
+        b0 = int(b["body_off"][s])
+        x = scenes.batch_scene3(b, s, q0, v0)
+        sim = oracle.Sphere3D(x["q"], x["v"], x["r"], x["m"], x["I0"], x["plane_x"], x["plane_n"], mu=x["mu"],
+                              CoR=x["CoR"], dt=b["dt"], gravity=b["gravity"], tol=tol, max_iters=3000)
+        sim.set_state(x["q"], x["v"])
+        Iw, Iinv = sim.world_inertia()
+        sim.set_next_order(order[(order >= c0) & (order < c1)] - c0)
+        sim.step()
+        c = sim.last_contacts()
+        ia = g["ia"][c0:c1] - b0
+        ib = np.where(g["ib"][c0:c1] >= 0, g["ib"][c0:c1] - b0, -1).astype(np.int32)
+        assert np.array_equal(ia, c["ia"]) and np.array_equal(ib, np.where(c["ib"] >= 0, c["ib"], -1)), s
+        res = oracle.residual_3d(x["m"], Iinv, Iw, x["v"], ia.astype(np.int32), ib, g["bases"][c0:c1].reshape(-1),
+                                 c["arm_a"].reshape(-1), c["arm_b"].reshape(-1), float(x["CoR"]), float(x["mu"]),
+                                 g["alpha"][c0:c1], g["beta"][c0:c1].reshape(-1))
+        err = float(stats["error"][s])
+        assert abs(res - err) <= 1e-12 + 1e-6 * err, s
+        if stats["succeeded"][s]:
+            assert res <= tol * 1.001, s
+            checked += 1
+    assert checked >= 4
+    nb = int(b["body_off"][-1])
+    qa, _ = f64.state()
+    qb, _ = f32.state()
+    assert np.abs(qa[:3 * nb] - qb[:3 * nb]).max() <= 1e-3
+    prof = f32.profile_read()
+    assert prof["contact_sweeps32"] > 0
+    f64.close()
+    f32.close()
