@@ -1509,39 +1509,6 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
-// gs_update32 on the patch's shared-memory velocities (ab holds patch-local indices).
-__device__ __forceinline__ void gs_update32_local(const Gs32Args& B, int s, float2* sv, const float* sm) {
-  const int2 ab = B.ab[s];
-  const float2 nk = B.n[s], ck = B.c[s];
-  const float4 w = B.w[s];
-  const float2 va = sv[ab.x];
-  const bool has_b = ab.y >= 0;
-  const float2 vb = has_b ? sv[ab.y] : make_float2(0.0f, 0.0f);
-  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
-  float hn = nx * va.x + ny * va.y;
-  float ht = tx * va.x + ty * va.y;
-  if (has_b) {
-    hn -= nx * vb.x + ny * vb.y;
-    ht -= tx * vb.x + ty * vb.y;
-  }
-  const float u0 = hn + ck.x, u1 = ht + ck.y;
-  // Read through L1: only this thread writes this impulse while the sweeps run.
-  const float2 rk = B.r[s];
-  const float bt0 = u0 - (w.x * rk.x + w.y * rk.y);
-  const float bt1 = u1 - (w.y * rk.x + w.z * rk.y);
-  float rn0, rn1;
-  local_solve_2d_f(w.x, w.y, w.z, bt0, bt1, w.w, rn0, rn1);
-  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
-  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
-  const float ma = sm[ab.x];
-  sv[ab.x] = make_float2(va.x + ma * px, va.y + ma * py);
-  if (has_b) {
-    const float mb = sm[ab.y];
-    sv[ab.y] = make_float2(vb.x - mb * px, vb.y - mb * py);
-  }
-  B.r[s] = make_float2(rn0, rn1);
-}
-
 // A contact staged in shared memory: both body slots in one word (16 bits each, 0xffff for a
 // static plane), normal, forcing and friction coefficient; the impulse kept there too (written
 // back to global memory before each FP64 check).  The Delassus block of a disc contact is
@@ -1599,6 +1566,46 @@ __device__ __forceinline__ void gs_update32_staged(const Staged& S, int i, float
   sv[a] = make_float2(va.x + ma * px, va.y + ma * py);
   if (has_b) sv[b] = make_float2(vb.x - mb * px, vb.y - mb * py);
   S.r[i] = make_float2(rn0, rn1);
+}
+
+// A patch or tile contact that did not fit in shared memory: gs_update32_staged's arithmetic
+// (the isotropic block from the slots' inverse masses, the closed-form local solve) on the
+// contact's global record, so that a contact's update does not depend on whether it was
+// staged.  Which contacts are staged depends on their order within a colour, and that order is
+// not fixed from run to run; with one arithmetic for both, the sweep's result does not depend
+// on it.
+__device__ __forceinline__ void gs_update32_iso(const Gs32Args& B, int s, float2* sv, const float* sm) {
+  const int2 ab = B.ab[s];
+  const int a = ab.x, b = ab.y;
+  const bool has_b = b >= 0;
+  const float2 nk = B.n[s], ck = B.c[s];
+  const float2 va = sv[a];
+  const float2 vb = has_b ? sv[b] : make_float2(0.0f, 0.0f);
+  const float ma = sm[a], mb = has_b ? sm[b] : 0.0f;
+  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  float hn = nx * va.x + ny * va.y;
+  float ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn -= nx * vb.x + ny * vb.y;
+    ht -= tx * vb.x + ty * vb.y;
+  }
+  const float u0 = hn + ck.x, u1 = ht + ck.y;
+  const float2 rk = B.r[s];
+  const float wd = ma + mb;
+  const float bt0 = u0 - wd * rk.x;
+  const float bt1 = u1 - wd * rk.y;
+  float rn0 = 0.0f, rn1 = 0.0f;
+  if (bt0 < 0.0f) {
+    const float inv = __frcp_rn(wd);
+    const float mu = B.w[s].w;
+    rn0 = -bt0 * inv;
+    rn1 = fminf(fmaxf(-bt1 * inv, -mu * rn0), mu * rn0);
+  }
+  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
+  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
+  sv[a] = make_float2(va.x + ma * px, va.y + ma * py);
+  if (has_b) sv[b] = make_float2(vb.x - mb * px, vb.y - mb * py);
+  B.r[s] = make_float2(rn0, rn1);
 }
 
 // Highest non-empty colour + 1 of a group's offsets.
@@ -1723,7 +1730,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
           if (s < sp_end)
             gs_update32_staged(S, s - sp0, sv, sm);
           else
-            gs_update32_local(B, s, sv, sm);
+            gs_update32_iso(B, s, sv, sm);
         }
         __syncthreads();
       }
@@ -1748,7 +1755,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
             if (s < sq_end)
               gs_update32_staged(S, Q.stage_p + s - sq0, svq, smq);
             else
-              gs_update32_local(B, s, svq, smq);
+              gs_update32_iso(B, s, svq, smq);
           }
           __syncthreads();
         }

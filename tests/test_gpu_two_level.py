@@ -103,3 +103,22 @@ def test_patch_layout_is_race_free(gpulib):
     assert np.unique(pairs, axis=0).shape[0] == pairs.shape[0]
     # Most contacts between patches are swept inside a shifted tile.
     assert tile.sum() > 0 and rest.sum() < 0.25 * between.sum()
+
+
+def test_two_level_is_deterministic(gpulib):
+    """The same bits from run to run on the 262,144-disc pile over the 600 capped steps that form
+    it.  There the largest patches hold more contacts than fit in shared memory, so which
+    contacts are staged depends on their order within a colour, which atomics set and which
+    varies between runs; staged and unstaged contacts share one arithmetic, so the result does not."""
+    s = scenes.dense_pile(n=262144, seed=2, width=40.0, height=60.0)
+    out = []
+    for _ in range(2):
+        ctx = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE, max_iters=50)
+        ctx.profile_enable(True)
+        ctx.profile_read(reset=True)
+        ctx.step(600)
+        prof = ctx.profile_read()
+        assert prof["two_level_solves"] > 100
+        out.append(ctx.state())
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
