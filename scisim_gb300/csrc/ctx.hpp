@@ -119,6 +119,9 @@ struct sg_ctx {
   int device = 0;
   int num_sms = 0;
   unsigned long long spin_limit = 0;
+  // Kernel attributes are per device: set once per context (each context has one device).
+  int patch_smem_budget = -1;   // k_gs_patch's dynamic shared memory limit, once opted in
+  bool mlp_smem_set = false;    // k_mlp_fwdbwd's dynamic shared memory limit set
 
   // Scene: dim 2 = Ball2D (q, v: 2 per body), dim 3 = RigidBody3D spheres
   // (q: [x (3nb) | R row-major (9nb)], v: [v (3nb) | omega (3nb)], SCISim's layouts).

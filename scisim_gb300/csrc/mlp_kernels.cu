@@ -566,10 +566,9 @@ int launch_fwdbwd(sg_ctx* ctx, const float* p, long n, long first, long count, u
                   unsigned long long offset, float inv_batch, float* grad, double* loss) {
   TrainArgs A{p, ctx->mlp_x.as<float>(), ctx->mlp_t.as<float>(), n, first, count, stride, offset, inv_batch, grad, loss};
   const size_t smem = train_smem_bytes();
-  static bool attr_set = false;
-  if (!attr_set) {
+  if (!ctx->mlp_smem_set) {
     SG_CUDA_TRY(cudaFuncSetAttribute(k_mlp_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
+    ctx->mlp_smem_set = true;
   }
   k_mlp_fwdbwd<<<blocks_for(count, kTrainBlock), kTrainBlock, smem, ctx->stream>>>(A);
   SG_CUDA_TRY(cudaGetLastError());

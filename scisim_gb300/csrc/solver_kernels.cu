@@ -2554,16 +2554,16 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       if (patched) {
         // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
         // contacts as fit (the patch's first), 32 B each.
-        static int dyn_budget = -1;
-        if (dyn_budget < 0) {
+        if (ctx->patch_smem_budget < 0) {
           int optin = 0;
           SG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
           cudaFuncAttributes fa{};
           SG_CUDA_TRY(cudaFuncGetAttributes(&fa, k_gs_patch));
           const int budget = optin - (int)fa.sharedSizeBytes;
           SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch, cudaFuncAttributeMaxDynamicSharedMemorySize, budget));
-          dyn_budget = budget;
+          ctx->patch_smem_budget = budget;
         }
+        const int dyn_budget = ctx->patch_smem_budget;
         const int body_bytes = 12 * (capp + capq);
         // The remainder first (block 0 sweeps it whole or not at all), then the patch, the tile.
         int capc = (nrest_bodies + 1) & ~1, stage_c = nrest;
