@@ -1,0 +1,41 @@
+"""bench.py's reference arm on the CPU: one JSON line with the keys and meanings the benchmark
+contract fixes (impl, metric, unit, value, cpu_baseline, e2e with no host-device bytes), and under a
+multi-rank launch only rank 0 works and prints.  Small sizes: the oracle's strip for a
+65,536-disc pile is 2,048 discs."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ARGS = ["--impl", "reference", "--steps", "1", "--warmup", "3", "--n", "65536", "--preroll", "60"]
+
+
+def run(env_extra):
+    env = dict(os.environ, **env_extra)
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + ARGS, cwd=ROOT, env=env,
+                          capture_output=True, text=True, timeout=300)
+
+
+@pytest.mark.timeout(300)
+def test_reference_arm_line():
+    p = run({"WORLD_SIZE": "1", "RANK": "0", "LOCAL_RANK": "0"})
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [x for x in p.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "contact-steps/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] == 1 and "strip" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"].startswith("ball2d_dense_pile_")
+
+
+@pytest.mark.timeout(120)
+def test_reference_arm_other_ranks_exit_quietly():
+    p = run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"})
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert not [x for x in p.stdout.splitlines() if x.startswith("{")]
