@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import math
 import os
+import re
 import xml.etree.ElementTree as ET
 from fractions import Fraction
 
@@ -40,18 +41,50 @@ def _attr(node, name, tag):
     return v
 
 
+_MANTISSA = re.compile(r"\s*[+-]?(?:[0-9]+(?:\.[0-9]*)?|\.[0-9]+)")
+_EXPONENT = re.compile(r"[eE][+-]?[0-9]+")
+
+
+def stream_double(text: str):
+    """`std::stringstream >> double` (StringUtilities.h:64-69): leading whitespace skipped, the
+    longest decimal prefix read and the rest ignored; an exponent marker without digits fails, as
+    the whole accumulated token must convert.  Returns None on failure."""
+    m = _MANTISSA.match(text)
+    if m is None:
+        return None
+    end = m.end()
+    if end < len(text) and text[end] in "eE":
+        e = _EXPONENT.match(text, end)
+        if e is None:
+            return None
+        end = e.end()
+    return float(text[:end])
+
+
 def _scalar(node, name, tag):
-    try:
-        return float(_attr(node, name, tag))
-    except ValueError as e:
-        raise SceneError("%s: %s is not a scalar" % (tag, name)) from e
+    v = stream_double(_attr(node, name, tag))
+    if v is None:
+        raise SceneError("%s: %s is not a scalar" % (tag, name))
+    return v
 
 
 def _vector(node, name, n, tag):
-    parts = _attr(node, name, tag).split()
-    if len(parts) != n:
+    """readScalarList with a space delimiter (StringUtilities.h:92-112): exactly n tokens between
+    single spaces (StringUtilities.cpp:123-142: a doubled or trailing space makes an empty token),
+    each read by extractScalarFromString, which also takes "inf" and "-inf"."""
+    text = _attr(node, name, tag)
+    tokens = text.split(" ")  # the reference's tokenizer gives the same tokens
+    if len(tokens) != n:
         raise SceneError("%s: %s needs %d scalars" % (tag, name, n))
-    return [float(p) for p in parts]
+    out = []
+    for t in tokens:
+        v = stream_double(t)
+        if v is None:
+            v = {"-inf": -math.inf, "inf": math.inf}.get(t)
+        if v is None:
+            raise SceneError("%s: %s needs %d scalars" % (tag, name, n))
+        out.append(v)
+    return out
 
 
 def _bool(node, name, tag):
@@ -61,15 +94,40 @@ def _bool(node, name, tag):
     return v == "1"
 
 
-def rational(text: str) -> Fraction:
-    """Rational<intmax_t> extraction (scisim/Math/Rational.h:204-260): a decimal or a/b, exact."""
-    t = text.strip().replace(" ", "")
-    if t.count("/") == 1 and "." not in t:
-        a, b = t.split("/")
-        return Fraction(int(a), int(b))
-    if t.count("/") > 0:
-        raise SceneError("dt: malformed rational %r" % text)
-    return Fraction(t)
+def _stream_int(text: str, what: str) -> int:
+    """`std::stringstream >> integer` on whitespace-free text: an optional sign and at least one
+    digit at the start; anything after the digits is ignored (StringUtilities.h:64-69)."""
+    m = re.match(r"[+-]?[0-9]+", text)
+    if m is None:
+        raise SceneError("%s: malformed rational %r" % (what, text))
+    return int(m.group(0))
+
+
+def rational(text: str, what: str = "dt") -> Fraction:
+    """Rational<intmax_t> extraction as scisim/Math/Rational.h:203-260 does it: at most one slash
+    or one period; whitespace removed; `a/b` as two integers; otherwise split at the last period,
+    trailing zeros of the fraction digits dropped, an empty or bare-sign integer part read as 0,
+    and the fraction digits added with the integer part's sign (so "-0.5" reads as +1/2 there,
+    as in the reference).  Exact; the caller converts with numerator / denominator."""
+    slashes, periods = text.count("/"), text.count(".")
+    if slashes > 2 or periods > 2 or (slashes == 1 and periods != 0) or (periods == 1 and slashes != 0):
+        raise SceneError("%s: malformed rational %r" % (what, text))
+    t = "".join(text.split())
+    if slashes != 1:
+        pos = t.rfind(".")
+        left, right = (t, "") if pos < 0 else (t[:pos], t[pos + 1:])
+        right = right.rstrip("0")
+        left = {"": "0", "+": "+0", "-": "-0"}.get(left, left)
+        li = _stream_int(left, what)
+        ri = _stream_int(right, what) if right else 0
+        den = 10 ** len(right)
+        num = li * den + (-1 if li < 0 else 1) * ri
+    else:
+        pos = t.rfind("/")
+        num, den = _stream_int(t[:pos], what), _stream_int(t[pos + 1:], what)
+    if den == 0:
+        raise SceneError("%s: zero denominator in %r" % (what, text))
+    return Fraction(num, den)
 
 
 def _check_tags(root, allowed):

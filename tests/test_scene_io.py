@@ -140,3 +140,64 @@ def test_stabilized_staggering():
     s = scene_io.load_ball2d_scene(text.replace('cache_impulses="normal_and_friction"', 'cache_impulses="none"'))
     assert s["staggering"] == "stabilized"
     assert scene_io.ball2d_objects(s)[3].name() == "stabilized_impact_friction_map"
+
+
+RATIONAL_TESTS = "/root/reference/scisimtests/rational_number_tests.cpp"
+
+
+def _registered_rational_cases():
+    """(input string, expected double) of every parsing case in the reference's rational-number
+    test program: `extractFromString( "<in>", ... )` followed by `fabs( <expected> - scalar(...) )`."""
+    import re
+    src = open(RATIONAL_TESTS).read()
+    cases = re.findall(r'extractFromString\(\s*"([^"]*)"\s*,\s*rational_number\s*\).*?fabs\(\s*([^)]*?)\s+-\s+scalar',
+                       src, flags=re.S)
+    out = []
+    for text, expr in cases:
+        assert re.fullmatch(r"[-+0-9. /]+", expr), expr
+        out.append((text, float(eval(expr))))  # a numeric literal or a quotient of two
+    return out
+
+
+@pytest.mark.skipif(not os.path.isfile(RATIONAL_TESTS), reason="reference tests not present")
+def test_rational_matches_reference_tests():
+    """scene_io.rational reads every string of the reference's registered rational-number parsing
+    tests (scisimtests/CMakeLists.txt:9-19) to exactly the double the test expects."""
+    cases = _registered_rational_cases()
+    assert len(cases) == 11
+    for text, want in cases:
+        got = scene_io.rational(text)
+        assert float(got.numerator) / float(got.denominator) == want, (text, got, want)
+
+
+def test_rational_reference_rules():
+    """The rules of the reference's extraction beyond its registered cases: stream extraction of
+    each part (trailing characters ignored), the fraction digits taking the integer part's sign,
+    and rejected forms."""
+    r = scene_io.rational
+    assert r("1/100") == Fraction(1, 100) and r(" 3 / 6 ") == Fraction(1, 2)
+    assert r("0.0010") == Fraction(1, 1000) and r("7") == 7
+    assert r("-0.5") == Fraction(1, 2)      # integer part -0 is not negative
+    assert r("-1.5") == Fraction(-3, 2)
+    assert r("1.5e-3") == Fraction(1, 1) + Fraction(5, 10000)  # "5e-3" extracts as 5 over 10^4
+    assert r("+") == 0 and r(" - . ") == 0   # a bare sign is read as 0
+    for bad in ("1/2/3/4", "1.2/3", "abc", "1/0", "./", "1..2.3"):
+        with pytest.raises(scene_io.SceneError):
+            r(bad)
+
+
+def test_scalar_stream_extraction_rules():
+    """Scalars as `std::stringstream >> double` reads them (the longest decimal prefix, the rest
+    ignored; no nan, no digit separators), and vectors as readScalarList with single spaces."""
+    d = scene_io.stream_double
+    assert d("0.25") == 0.25 and d("  -3.5e2") == -350.0 and d("1.5abc") == 1.5 and d(".5") == 0.5
+    assert d("7.") == 7.0 and d("2e3x") == 2000.0
+    for bad in ("", "abc", "- 1", "nan", "1e", "1e+", "inf"):
+        assert d(bad) is None, bad
+    import xml.etree.ElementTree as ET
+    nd = ET.fromstring('<b x="1 2 3" y="1  2 3" z="-inf 0 inf" w="1 2 3 "/>')
+    assert scene_io._vector(nd, "x", 3, "b") == [1.0, 2.0, 3.0]
+    assert scene_io._vector(nd, "z", 3, "b")[0] == float("-inf")
+    for name in ("y", "w"):
+        with pytest.raises(scene_io.SceneError):
+            scene_io._vector(nd, name, 3, "b")
