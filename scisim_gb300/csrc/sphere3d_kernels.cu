@@ -2131,7 +2131,8 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   if (int r = scan_exclusive(ctx, ctx->cell_count.as<int>(), ctx->cell_start.as<int>(), (int)cap)) return r;
   k_cell_scatter3<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ctx->cell_start.as<int>(),
                                                    ctx->cell_fill.as<int>(), ctx->sorted.as<int>());
-  Scan3 sc{aabb, g, ctx->cell_start.as<int>(), ctx->sorted.as<int>(), ctx->q1.as<double>(), ctx->r.as<double>()};
+  Scan3 sc{aabb, g, ctx->cell_start.as<int>(), ctx->sorted.as<int>(), ctx->q1.as<double>(), ctx->r.as<double>(),
+           nullptr, nullptr};
   k_pair_count3<<<blocks_for(nb), kBlock, 0, s>>>(nb, sc, ctx->pair_cnt.as<int>());
   SG_CUDA_TRY(cudaGetLastError());
   if (int r = scan_exclusive(ctx, ctx->pair_cnt.as<int>(), ctx->pair_off.as<int>(), nb)) return r;
