@@ -363,6 +363,7 @@ def sphere_batch_leg(args, torch, local, flush):
     c32.step(1)  # warm-up, then back to the timed state
     c32.upload_sphere3d_batch(*up)
     s32 = torch.cuda.ExternalStream(c32.stream_ptr(), device=local)
+    c32.profile_read(reset=True)
     flush.zero_()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -372,7 +373,9 @@ def sphere_batch_leg(args, torch, local, flush):
     f1.synchronize()
     ms32 = f0.elapsed_time(f1)
     st32 = c32.batch_scene_stats()
+    p32 = c32.profile_read(reset=True)
     v32 = r32["total_contacts"] / (ms32 / 1e3)
+    sw = p32["contact_sweeps32"] + p32["contact_sweeps"]
     log("sphere batch FP32+FP64 refinement: %d contact-steps in %.1f ms" % (r32["total_contacts"], ms32))
     c32.close()
     out = {"workload": "sphere_batch_%d" % S, "scenes": S, "spheres": N, "value": value, "unit": UNIT,
@@ -387,6 +390,7 @@ def sphere_batch_leg(args, torch, local, flush):
            "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"],
            "fp32_refine": {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.sphere_batch_steps,
                            "scenes_converged_last_step": int(st32["succeeded"].sum()),
+                           "fp32_sweep_share": p32["contact_sweeps32"] / sw if sw else None,
                            "over_fp64_batched": v32 / value, "over_plain": v32 / plain if plain else None,
                            "form": "batched, FP32 sweeps with FP64 checks and refinement, each scene to its "
                                    "own tolerance"}}
