@@ -190,6 +190,36 @@ def cpu_sample(args, steps):
     return tot / dt, desc, 1
 
 
+def batch_cpu_sample(b, q0, v0, pick, steps):
+    """The oracle on the scenes the plain GPU comparison samples, from the same state over the
+    same number of steps, each scene on its own host thread (the oracle's C loop runs without the
+    GIL and keeps no shared state), so all host cores up to one per scene work at once.  Scenes
+    start from an empty impulse cache, then warm-start from their own.  Returns (contact-steps/s,
+    threads, description)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O  # checker / CPU baseline only
+    O.build()
+    sims = []
+    for sc in pick:
+        b0, b1 = int(b["body_off"][sc]), int(b["body_off"][sc + 1])
+        p0, p1 = int(b["plane_off"][sc]), int(b["plane_off"][sc + 1])
+        sims.append(O.Ball2D(q0[2 * b0:2 * b1], v0[2 * b0:2 * b1], b["r"][b0:b1], b["m"][b0:b1], b["plane_x"][p0:p1],
+                             b["plane_n"][p0:p1], dt=b["dt"], gravity=b["gravity"], mu=float(b["mu"][sc]),
+                             CoR=float(b["CoR"][sc]), tol=1e-6, max_iters=5000, eval_every=1,
+                             integrator=O.SYMPLECTIC_EULER, cache_mode=O.CACHE_NORMAL_AND_FRICTION))
+    threads = max(1, min(len(sims), os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(lambda sim: sim.run(steps), sims))
+    wall = time.perf_counter() - t0
+    tot = sum(r[1] for r in res)
+    desc = ("oracle (C++ restatement of SCISim + So-bogus, sequential block GS per scene) on the %d sampled "
+            "scenes (%d discs), one host thread per scene, %d threads, %d steps from the GPU's state: %d "
+            "contact-steps in %.2f s" % (len(sims), sum(x.nb for x in sims), threads, steps, tot, wall))
+    return (tot / wall if wall > 0 else None), threads, desc
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -290,6 +320,8 @@ def batch_leg(args, torch, local, flush, ws=1, rank=0):
         pms += a0.elapsed_time(a1)
         c.close()
     plain = pc / (pms / 1e3) if pms > 0 else None
+    cpu_v, cpu_threads, cpu_desc = batch_cpu_sample(b, q0, v0, pick, args.batch_steps)
+    log("batch cpu: %s" % cpu_desc)
     out = {"workload": "ball2d_batch_%d" % S_all, "scenes": S_all, "ranks": ws, "discs": N_all, "value": value,
            "unit": UNIT,
            "steps": args.batch_steps, "timed_steps": [args.batch_preroll + 9, args.batch_preroll + 8 + args.batch_steps],
@@ -301,7 +333,9 @@ def batch_leg(args, torch, local, flush, ws=1, rank=0):
            "gs_iterations_mean_last_step": float(stats["iterations"].mean()),
            "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
                               "form": "one context per scene, cold start, FP64, same steps from the same state"},
-           "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"]}
+           "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"],
+           "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port", "sample": cpu_desc},
+           "batched_over_cpu": value / cpu_v if cpu_v else None}
     ctx.close()
     return out
 
