@@ -220,6 +220,33 @@ def batch_cpu_sample(b, q0, v0, pick, steps):
     return (tot / wall if wall > 0 else None), threads, desc
 
 
+def sphere_batch_cpu_sample(b, q0, v0, pick, steps, first_iteration):
+    """As batch_cpu_sample for the sphere batch: the oracle on the sampled scenes from the GPU's
+    state, steps numbered as the GPU's, one host thread per scene."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O  # checker / CPU baseline only
+    from scisim_gb300 import scenes
+    O.build()
+    sims = []
+    for sc in pick:
+        x = scenes.batch_scene3(b, sc, q0, v0)
+        sim = O.Sphere3D(x["q"], x["v"], x["r"], x["m"], x["I0"], x["plane_x"], x["plane_n"], dt=b["dt"],
+                         gravity=b["gravity"], mu=x["mu"], CoR=x["CoR"], tol=1e-6, max_iters=5000, eval_every=1)
+        sim.iteration = first_iteration - 1
+        sims.append(sim)
+    threads = max(1, min(len(sims), os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(lambda sim: sim.run(steps), sims))
+    wall = time.perf_counter() - t0
+    tot = sum(r[1] for r in res)
+    desc = ("oracle (C++ restatement of SCISim + So-bogus, sequential 3x3-block GS per scene) on the %d sampled "
+            "scenes (%d spheres), one host thread per scene, %d threads, %d steps from the GPU's state: %d "
+            "contact-steps in %.2f s" % (len(sims), sum(x.nb for x in sims), threads, steps, tot, wall))
+    return (tot / wall if wall > 0 else None), threads, desc
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -390,6 +417,9 @@ def sphere_batch_leg(args, torch, local, flush):
         pms += a0.elapsed_time(a1)
         c.close()
     plain = pc / (pms / 1e3) if pms > 0 else None
+    cpu_v, cpu_threads, cpu_desc = sphere_batch_cpu_sample(b, q0, v0, pick, args.sphere_batch_steps,
+                                                           args.sphere_batch_preroll + 2)
+    log("sphere batch cpu: %s" % cpu_desc)
     # The same steps from the same state with FP32 sweeps and FP64 refinement, scene by scene.
     c32 = _lib.Context(precision=_lib.PRECISION_FP32_REFINE, **dict(kw, max_iters=5000))
     up = (b["body_off"], q0, v0, b["r"], b["m"], b["I0"], b["plane_off"], b["plane_x"], b["plane_n"], b["mu"], b["CoR"])
@@ -427,7 +457,9 @@ def sphere_batch_leg(args, torch, local, flush):
                            "fp32_sweep_share": p32["contact_sweeps32"] / sw if sw else None,
                            "over_fp64_batched": v32 / value, "over_plain": v32 / plain if plain else None,
                            "form": "batched, FP32 sweeps with FP64 checks and refinement, each scene to its "
-                                   "own tolerance"}}
+                                   "own tolerance"},
+           "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port", "sample": cpu_desc},
+           "batched_over_cpu": value / cpu_v if cpu_v else None}
     ctx.close()
     return out
 
