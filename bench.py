@@ -31,6 +31,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -103,8 +104,8 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.out = os.path.join(HERE, "gpurun_out", "clocks.csv") if os.path.isdir(
-            os.path.join(HERE, "gpurun_out")) else "/tmp/sg_clocks.csv"
+        # The raw samples (the JSON line carries their summary); SG_CLOCKS_CSV keeps them.
+        self.out = os.environ.get("SG_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(), "sg_clocks.csv")
 
     def start(self):
         try:
@@ -165,7 +166,7 @@ def cpu_sample(args, steps):
     runs to the 5,000-sweep cap, residual ~1e-2); a narrower one settles against its walls
     and converges in tens of sweeps, which times a different problem.
     Returns (contact-steps/s, description)."""
-    from oracle import oracle as O  # checker / CPU baseline only
+    from oracle import oracle as O  # the oracle: CPU baseline only
     O.build()
     n = max(2048, args.n // 32)
     s = make_scene(n)
@@ -198,7 +199,7 @@ def batch_cpu_sample(b, q0, v0, pick, steps):
     threads, description)."""
     from concurrent.futures import ThreadPoolExecutor
 
-    from oracle import oracle as O  # checker / CPU baseline only
+    from oracle import oracle as O  # the oracle: CPU baseline only
     O.build()
     sims = []
     for sc in pick:
@@ -225,7 +226,7 @@ def sphere_batch_cpu_sample(b, q0, v0, pick, steps, first_iteration):
     state, steps numbered as the GPU's, one host thread per scene."""
     from concurrent.futures import ThreadPoolExecutor
 
-    from oracle import oracle as O  # checker / CPU baseline only
+    from oracle import oracle as O  # the oracle: CPU baseline only
     from scisim_gb300 import scenes
     O.build()
     sims = []

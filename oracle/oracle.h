@@ -1,8 +1,8 @@
 // oracle.h -- CPU oracle for the SCISim per-step contact path.
 //
 // TEST INFRASTRUCTURE ONLY.  This is a plain C++ restatement of the reference
-// algorithm (breannansmith/scisim) used as the correctness checker for the GPU
-// library and as the timed CPU baseline.  Product code never links, imports or
+// algorithm (breannansmith/scisim) that the tests compare the GPU library with,
+// and the timed CPU baseline.  Product code never links, imports or
 // executes anything under oracle/; only tests/, __graft_entry__.smoke() and the
 // cpu_baseline / reference legs of bench.py do.
 //

@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in this folder from the SCISim sources.
 
 Run in a checkout that has the reference sources (default location given by
---ref).  The GPU machine and the test suite only read the committed outputs:
+--ref).  The tests read only the committed outputs:
 
   aabb2d_fixture_{00,01,02}.txt.gz  2D AABB known-answer fixtures (5k/10k/20k boxes),
                                     copied number-for-number from
