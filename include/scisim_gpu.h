@@ -80,7 +80,12 @@ typedef struct sg_ctx sg_ctx;
 /* Human-readable description of the last failure on this thread. */
 SG_API const char* sg_last_error_string(void);
 
-/* Creates a context on cfg->device; all device memory is owned by the context. */
+/* Creates a context on cfg->device; all device memory is owned by the context.  Replaces
+ * constructing the step's objects: the impact-friction map (GeometricImpactFrictionMap ctor,
+ * scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:20-31: tol, max_iters, impulses to cache),
+ * the friction solver (Sobogus ctor, scisim/ConstrainedMaps/Sobogus.cpp:642-645: eval_every) and
+ * the unconstrained map (cfg->integrator); the scene is uploaded separately.  sg_ctx_destroy
+ * releases the context and all its device memory. */
 SG_API int sg_ctx_create(const sg_config* cfg, sg_ctx** out);
 SG_API void sg_ctx_destroy(sg_ctx* ctx);
 
@@ -115,8 +120,10 @@ SG_API int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const do
  * v: [v (3N) | omega (3N)] over all N = body_off[S] bodies, r, m: N, I0: 3N, planes 3 each.
  * sg_step then steps every scene as sg_sphere3d_upload + sg_step would step it alone: its own
  * broad phase, its contacts in the reference's order, and its own Gauss-Seidel termination
- * (residual, best iterate, iteration count), solved in FP64 for every scene in one launch;
- * sg_batch2d_scene_stats reports each scene.  The integrator must be SG_SPLIT_HAM. */
+ * (residual, best iterate, iteration count), every scene solved in one launch, in FP64 or (the
+ * context's precision SG_PRECISION_FP32_REFINE) in FP32 sweeps with FP64 checks and refinement
+ * decided scene by scene; sg_batch2d_scene_stats reports each scene.  The integrator must be
+ * SG_SPLIT_HAM. */
 SG_API int sg_sphere3d_batch_upload(sg_ctx* ctx, int32_t n_scenes, const int32_t* body_off, const double* q,
                                     const double* v, const double* r, const double* m, const double* I0,
                                     const int32_t* plane_off, const double* plane_x, const double* plane_n,
@@ -136,12 +143,14 @@ SG_API int sg_batch2d_upload(sg_ctx* ctx, int32_t n_scenes, const int32_t* body_
                              const double* v, const double* r, const double* m, const int32_t* plane_off,
                              const double* plane_x, const double* plane_n, const double* mu, const double* CoR);
 
-/* Contact capacity of a batched context (default 3 per body + 1024).  It grows by itself
+/* Contact capacity of a batched context (no counterpart; default 3 per body + 1024).  It grows by itself
  * when a step overflows it; a smaller value bounds device memory up front. */
 SG_API int sg_batch2d_set_capacity(sg_ctx* ctx, int32_t contacts);
 
-/* Per-scene results of the last batched step: contact count, Gauss-Seidel sweeps, best
- * residual and whether the scene's solve reached the tolerance (any output may be NULL). */
+/* Per-scene results of the last batched step (Ball2D or sphere batch): contact count,
+ * Gauss-Seidel sweeps, best residual and whether the scene's solve reached the tolerance, as
+ * the step statistics of each scene's own GeometricImpactFrictionMap::flow would report them
+ * (scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:344-350).  Any output may be NULL. */
 SG_API int sg_batch2d_scene_stats(sg_ctx* ctx, int32_t* n_contacts, uint32_t* iterations, double* error,
                                   int32_t* succeeded);
 
@@ -162,7 +171,8 @@ SG_API int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_s
 SG_API int sg_flow(sg_ctx* ctx, uint32_t iteration, const double* q0, const double* v0, double* q1, double* v1,
             sg_step_stats* stats);
 
-/* Downloads the device-resident state (Ball2DState / RigidBody3DState q, v). */
+/* Downloads the device-resident state (Ball2DState::q()/v(), ball2d/Ball2DState.h:34-39;
+ * RigidBody3DState::q()/v(), rigidbody3d/RigidBody3DState.h:40-44; the same layouts). */
 SG_API int sg_download_state(sg_ctx* ctx, double* q, double* v);
 
 /* Contacts of the last step in active-set order (Ball2DSim::computeActiveSet,
@@ -186,8 +196,11 @@ SG_API int64_t sg_sphere3d_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, 
 SG_API int sg_sphere3d_world_inertia(sg_ctx* ctx, double* Iw, double* Iinv);
 
 /* The Gauss-Seidel processing order of the last step's solve (contacts of colour 0,
- * then colour 1, ...) and the colour offsets (n_colors + 1 entries).  Returns the
- * contact count, or -(count+1) if cap is too small. */
+ * then colour 1, ...) and the colour offsets (n_colors + 1 entries).  No counterpart: the
+ * reference sweeps in active-set order without colouring
+ * (scisim/ConstrainedMaps/bogus/Ball2DSobogusInterface.cpp:124-133, max_threads 0); the oracle
+ * replays this order to compare whole steps bit for bit.  Returns the contact count, or
+ * -(count+1) if cap is too small. */
 SG_API int64_t sg_last_solve_order(sg_ctx* ctx, int64_t cap, int32_t* order, int32_t* color_offsets,
                             int32_t* n_colors);
 
@@ -368,11 +381,12 @@ SG_API int sg_autotune(sg_ctx* ctx, int32_t trial_steps, uint32_t first_iteratio
 SG_API int sg_last_patch_layout(sg_ctx* ctx, int64_t nc, int64_t nb, int32_t* counts, int32_t* group,
                                 int32_t* color, int32_t* body_patch, int32_t* body_tile, int32_t* body_band);
 
-/* The context's CUDA stream (cudaStream_t) for stream-ordered timing by the caller. */
+/* The context's CUDA stream (cudaStream_t) for stream-ordered timing by the caller (no counterpart). */
 SG_API int sg_ctx_stream(sg_ctx* ctx, void** stream);
 
 /* Sets the iteration limit of every device-side wait (grid barriers); 0 restores the
- * default (about a second).  Used to exercise the SG_DEVICE_TIMEOUT path. */
+ * default (about a second).  Used to exercise the SG_DEVICE_TIMEOUT path (no counterpart: the
+ * reference runs on the CPU and has no device waits). */
 SG_API int sg_set_spin_limit(sg_ctx* ctx, uint64_t spins);
 
 /* Runs a kernel that waits on a device flag nothing sets, with the context's spin
