@@ -191,6 +191,41 @@ int64_t or_sphere3d_active_set(const or_sphere3d* s, const double* q0, const dou
 int64_t or_sphere3d_last_contacts(const or_sphere3d* s, int64_t cap, int32_t* ia, int32_t* ib, double* bases,
                                   double* arm_a, double* arm_b, double* alpha, double* beta);
 
+// ---------------------------------------------------------------- RigidBody2D circles
+// q = [x y theta] per body, v = [vx vy omega] per body (RigidBody2DState's layout); r, m, I per
+// body (CircleGeometry::computeMassAndInertia gives m = rho pi r^2, I = m r^2 / 2); planes 2 each.
+typedef struct or_rb2d or_rb2d;
+
+typedef struct {
+  int32_t integrator;  // OR_SYMPLECTIC_EULER / OR_VERLET (rigidbody2d/SymplecticEulerMap.cpp, VerletMap.cpp)
+  int32_t cache_mode;  // OR_CACHE_*
+  double dt;
+  double gravity[2];
+  double mu;
+  double CoR;
+  double tol;
+  uint32_t max_iters;
+  uint32_t eval_every;
+} or_rb2d_params;
+
+or_rb2d* or_rb2d_create(int nb, const double* q, const double* v, const double* r, const double* m,
+                        const double* I, int np, const double* plane_x, const double* plane_n,
+                        const or_rb2d_params* p);
+void or_rb2d_destroy(or_rb2d* s);
+// One GeometricImpactFrictionMap::flow step of RigidBody2DSim with Sobogus(RigidBody2D).
+int or_rb2d_step(or_rb2d* s, uint32_t iteration, or_step_stats* stats);
+int or_rb2d_run(or_rb2d* s, uint32_t first_iteration, uint32_t n_steps, or_step_stats* stats,
+                int64_t* total_contacts);
+void or_rb2d_get_state(const or_rb2d* s, double* q, double* v);
+void or_rb2d_set_state(or_rb2d* s, const double* q, const double* v);
+void or_rb2d_set_solver(or_rb2d* s, double tol, uint32_t max_iters);
+void or_rb2d_set_next_order(or_rb2d* s, int64_t nc, const int32_t* order);
+// Contacts of the last step (ib = -1 - plane for planes), normals (2 per contact), angular
+// entries of the tangent rows (cross(arm, t) for body a and body b; 0 for a plane's b) and
+// impulses; any output pointer may be NULL.
+int64_t or_rb2d_last_contacts(const or_rb2d* s, int64_t cap, int32_t* ia, int32_t* ib, double* n, double* ta,
+                              double* tb, double* alpha, double* beta);
+
 // ---------------------------------------------------------------- warm-start network
 // 12 -> 64 -> 64 -> 3 MLP with GELU; parameters W1 (64x12), b1, W2 (64x64), b2, W3 (3x64), b3.
 int or_mlp_param_count(void);

@@ -44,6 +44,12 @@ class Sphere3DParams(C.Structure):
                 ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
 
 
+class RigidBody2DParams(C.Structure):
+    _fields_ = [("integrator", C.c_int32), ("cache_mode", C.c_int32), ("dt", C.c_double),
+                ("gravity", C.c_double * 2), ("mu", C.c_double), ("CoR", C.c_double),
+                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("n_contacts", C.c_int64), ("n_ball_ball", C.c_int64), ("n_ball_plane", C.c_int64),
                 ("iterations", C.c_uint32), ("succeeded", C.c_int32), ("error", C.c_double)]
@@ -128,6 +134,20 @@ def lib():
         L.or_sphere3d_active_set.argtypes = [C.c_void_p, _dp, _dp, i64, _ip, _ip]
         L.or_sphere3d_last_contacts.restype = i64
         L.or_sphere3d_last_contacts.argtypes = [C.c_void_p, i64, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.or_rb2d_create.restype = C.c_void_p
+        L.or_rb2d_create.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp,
+                                     C.POINTER(RigidBody2DParams)]
+        L.or_rb2d_destroy.argtypes = [C.c_void_p]
+        L.or_rb2d_step.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(StepStats)]
+        L.or_rb2d_step.restype = C.c_int
+        L.or_rb2d_run.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(StepStats), C.POINTER(C.c_int64)]
+        L.or_rb2d_run.restype = C.c_int
+        L.or_rb2d_get_state.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_rb2d_set_state.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_rb2d_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_uint32]
+        L.or_rb2d_set_next_order.argtypes = [C.c_void_p, C.c_int64, _ip]
+        L.or_rb2d_last_contacts.restype = i64
+        L.or_rb2d_last_contacts.argtypes = [C.c_void_p, i64, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -474,3 +494,75 @@ def mlp_loss_grad(params, x, t):
     g = np.zeros(params.shape[0])
     loss = lib().or_mlp_loss_grad(_fp(params), x.shape[0], _fp(x), _fp(t), _d(g))
     return loss, g
+
+
+def circle_mass_inertia(r, density):
+    """CircleGeometry::computeMassAndInertia (rigidbody2d/CircleGeometry.cpp:29-33): m = rho pi r^2,
+    I = 0.5 m r^2."""
+    r = f64(r)
+    m = density * np.pi * r * r
+    return m, 0.5 * m * r * r
+
+
+class RigidBody2D:
+    """RigidBody2D circles stepped by GeometricImpactFrictionMap + Sobogus(RigidBody2D) (CPU oracle).
+    q, v: 3 per body ([x y theta], [vx vy omega]); r, m, I per body; planes 2 each."""
+
+    def __init__(self, q, v, r, m, I, plane_x, plane_n, *, dt, gravity=(0.0, -9.81), mu=0.5, CoR=0.0,
+                 tol=1e-9, max_iters=5000, eval_every=1, integrator=SYMPLECTIC_EULER, cache_mode=CACHE_NONE):
+        self.q, self.v = f64(q), f64(v)
+        self.r, self.m, self.I = f64(r), f64(m), f64(I)
+        self.nb = self.r.shape[0]
+        px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        self.np = px.shape[0] // 2
+        p = RigidBody2DParams(integrator, cache_mode, dt, (C.c_double * 2)(*gravity), mu, CoR, tol, max_iters,
+                              eval_every)
+        self._h = lib().or_rb2d_create(self.nb, _d(self.q), _d(self.v), _d(self.r), _d(self.m), _d(self.I),
+                                       self.np, _d(px), _d(pn), C.byref(p))
+        self.iteration = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().or_rb2d_destroy(h)
+            self._h = None
+
+    def step(self):
+        self.iteration += 1
+        st = StepStats()
+        lib().or_rb2d_step(self._h, self.iteration, C.byref(st))
+        return dict(n_contacts=st.n_contacts, n_circle_circle=st.n_ball_ball, n_circle_plane=st.n_ball_plane,
+                    iterations=st.iterations, succeeded=bool(st.succeeded), error=st.error)
+
+    def run(self, n_steps):
+        st = StepStats()
+        tot = C.c_int64(0)
+        bad = lib().or_rb2d_run(self._h, self.iteration + 1, n_steps, C.byref(st), C.byref(tot))
+        self.iteration += n_steps
+        return (dict(n_contacts=st.n_contacts, iterations=st.iterations, succeeded=bool(st.succeeded),
+                     error=st.error), tot.value, bad)
+
+    def state(self):
+        q, v = np.zeros(3 * self.nb), np.zeros(3 * self.nb)
+        lib().or_rb2d_get_state(self._h, _d(q), _d(v))
+        return q, v
+
+    def set_state(self, q, v):
+        q, v = f64(q), f64(v)
+        lib().or_rb2d_set_state(self._h, _d(q), _d(v))
+
+    def set_solver(self, tol, max_iters):
+        lib().or_rb2d_set_solver(self._h, tol, max_iters)
+
+    def set_next_order(self, order):
+        order = i32(order)
+        lib().or_rb2d_set_next_order(self._h, order.shape[0], _i(order))
+
+    def last_contacts(self):
+        L = lib()
+        nc = L.or_rb2d_last_contacts(self._h, 0, None, None, None, None, None, None, None)
+        nc = -nc - 1 if nc < 0 else nc
+        ia, ib = np.zeros(nc, np.int32), np.zeros(nc, np.int32)
+        n, ta, tb, a, b = np.zeros(2 * nc), np.zeros(nc), np.zeros(nc), np.zeros(nc), np.zeros(nc)
+        L.or_rb2d_last_contacts(self._h, nc, _i(ia), _i(ib), _d(n), _d(ta), _d(tb), _d(a), _d(b))
+        return dict(ia=ia, ib=ib, n=n.reshape(-1, 2), ta=ta, tb=tb, alpha=a, beta=b)
