@@ -223,6 +223,63 @@ def load_ball2d_scene(source) -> dict:
     return out
 
 
+def load_rigidbody2d_scene(source) -> dict:
+    """A `<rigidbody2d_scene>` of circles as arrays and settings (RigidBody2DSceneParser.cpp), for
+    the geometric staggering: `rigid_body` elements with a circle geometry, mass and inertia from
+    rho (CircleGeometry::computeMassAndInertia, rigidbody2d/CircleGeometry.cpp:29-33: m = rho pi r^2,
+    I = m r^2 / 2).  Returns q, v (3 per body: x, y, theta / vx, vy, omega), r, m, I, plane_x,
+    plane_n (2 per plane), dt, dt_rational, integrator, gravity, the solver settings and end_time.
+    Boxes, fixed bodies, portals and scripting are rejected by name.  The library steps these
+    scenes only through the oracle so far (no GPU path for RigidBody2D)."""
+    root = _root(source)
+    if root.tag != "rigidbody2d_scene":
+        raise SceneError("not a rigidbody2d_scene")
+    _check_tags(root, ("camera", "end_time", "integrator", "sobogus_friction_solver", "near_earth_gravity",
+                       "static_plane", "geometry", "rigid_body"))
+    kind, dt = _dt(root, ("verlet", "symplectic_euler"))
+    grav = root.findall("near_earth_gravity")
+    if len(grav) > 1:
+        raise SceneError("more than one near_earth_gravity force")
+    g = (0.0, 0.0) if not grav else tuple(_vector(grav[0], "f", 2, "near_earth_gravity"))
+    px, pn = [], []
+    for nd in root.findall("static_plane"):
+        px.append(_vector(nd, "x", 2, "static_plane"))
+        pn.append(_vector(nd, "n", 2, "static_plane"))
+    radii = []
+    for nd in root.findall("geometry"):
+        if _attr(nd, "type", "geometry") != "circle":
+            raise SceneError("geometry: only circles are supported")
+        radii.append(_scalar(nd, "r", "geometry"))
+    q, v, r, m, inertia = [], [], [], [], []
+    for nd in root.findall("rigid_body"):
+        tag = "rigid_body"
+        if nd.get("fixed") is not None and _bool(nd, "fixed", tag):
+            raise SceneError("%s: fixed bodies are not supported" % tag)
+        k = int(_attr(nd, "geo_idx", tag))
+        if not 0 <= k < len(radii):
+            raise SceneError("%s: invalid geo_idx" % tag)
+        rho = _scalar(nd, "rho", tag)
+        if not rho > 0.0:
+            raise SceneError("%s: rho must be positive" % tag)
+        x, vel = _vector(nd, "x", 2, tag), _vector(nd, "v", 2, tag)
+        q += [x[0], x[1], _scalar(nd, "theta", tag)]
+        v += [vel[0], vel[1], _scalar(nd, "omega", tag)]
+        rk = radii[k]
+        mk = rho * math.pi * rk * rk
+        r.append(rk)
+        m.append(mk)
+        inertia.append(0.5 * mk * rk * rk)
+    solver = _solver(root)
+    if solver["staggering"] != "geometric":
+        raise SceneError("sobogus_friction_solver: only the geometric staggering is supported for rigidbody2d")
+    out = dict(q=np.array(q, np.float64), v=np.array(v, np.float64), r=np.array(r, np.float64),
+               m=np.array(m, np.float64), I=np.array(inertia, np.float64),
+               plane_x=np.array(px, np.float64).reshape(-1, 2), plane_n=np.array(pn, np.float64).reshape(-1, 2),
+               dt=float(dt), dt_rational=dt, integrator=kind, gravity=g, end_time=_end_time(root))
+    out.update(solver)
+    return out
+
+
 def load_rigidbody3d_scene(source) -> dict:
     """A `<rigidbody3d_scene>` of spheres as arrays and settings (RigidBody3DSceneParser.cpp), for
     the split_ham integrator and geometric staggering.  Bodies: `rigid_body_with_density` with a

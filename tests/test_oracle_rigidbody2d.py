@@ -11,6 +11,8 @@ leaves the spins alone; an oblique frictional collision conserves linear and ang
 by the impulse m g dt and drifts as the geometric map makes it; and a run restarted from its
 state continues identically.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -133,3 +135,50 @@ def test_split_run_equals_whole_run(oracle):
     qb, vb = second.state()
     assert np.array_equal(qa, qb) and np.array_equal(va, vb)
     assert np.all(qa.reshape(-1, 3)[:, 1] >= 0.0)           # nothing fell through the floor
+
+
+ASSETS = "/root/reference/assets/rigidbody2d"
+
+
+def _sim(O, sc):
+    integ = O.SYMPLECTIC_EULER if sc["integrator"] == "symplectic_euler" else O.VERLET
+    return O.RigidBody2D(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["plane_x"], sc["plane_n"], dt=sc["dt"],
+                         gravity=sc["gravity"], mu=sc["mu"], CoR=sc["CoR"], tol=sc["tol"], max_iters=sc["max_iters"],
+                         eval_every=sc["eval_every"], integrator=integ, cache_mode=sc["cache_mode"])
+
+
+@pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
+def test_reference_ball_rolling_down_hill(oracle):
+    """The reference's own scene (tests_serialization/ball_rolling_down_hill.xml): "a ball rolling
+    down a valley that should come to rest at the bottom of the valley" (the valley's planes meet at
+    x = 2)."""
+    from scisim_gb300 import scene_io
+    sc = scene_io.load_rigidbody2d_scene(os.path.join(ASSETS, "tests_serialization", "ball_rolling_down_hill.xml"))
+    sim = _sim(oracle, sc)
+    st, tot, bad = sim.run(4000)
+    q, v = sim.state()
+    assert bad == 0 and tot >= 4000
+    assert abs(q[0] - 2.0) <= 1e-3 and abs(v[0]) <= 1e-12 and abs(v[2]) <= 1e-12
+    assert abs(v[1] - sc["gravity"][1] * sc["dt"]) <= 1e-12      # at rest but for the final map's kick
+
+
+@pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
+def test_reference_circle_scenes_step(oracle):
+    """Every circle-only rigidbody2d scene of the reference's assets loads and steps 200 times with
+    finite states and solves that stay within their iteration caps."""
+    import glob
+
+    from scisim_gb300 import scene_io
+    ran = 0
+    for f in sorted(glob.glob(os.path.join(ASSETS, "**", "*.xml"), recursive=True)):
+        try:
+            sc = scene_io.load_rigidbody2d_scene(f)
+        except scene_io.SceneError:
+            continue
+        sim = _sim(oracle, sc)
+        st, tot, bad = sim.run(200)
+        q, v = sim.state()
+        assert np.all(np.isfinite(q)) and np.all(np.isfinite(v)), f
+        assert st["iterations"] <= sc["max_iters"], f
+        ran += 1
+    assert ran >= 18

@@ -104,6 +104,46 @@ def test_reference_assets_load_or_are_rejected_by_name():
 
 
 @pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
+def test_reference_rigidbody2d_assets_load_or_are_rejected_by_name():
+    """Circle scenes load with the reference's mass and inertia from rho; boxes, portals, fixed
+    bodies and scripting are rejected with a SceneError naming them."""
+    ok, reasons = 0, set()
+    for path in sorted(glob.glob(ASSETS + "/rigidbody2d/**/*.xml", recursive=True)):
+        try:
+            s = scene_io.load_rigidbody2d_scene(path)
+        except scene_io.SceneError as e:
+            reasons.add(str(e).split(":")[0])
+            continue
+        ok += 1
+        n = s["r"].shape[0]
+        assert s["q"].shape[0] == 3 * n and s["v"].shape[0] == 3 * n
+        assert np.all(s["I"] == 0.5 * s["m"] * s["r"] * s["r"])
+    assert ok >= 18 and "geometry" in reasons
+
+
+def test_rigidbody2d_scene_values():
+    text = """<rigidbody2d_scene>
+      <integrator type="verlet" dt="1/200"/>
+      <sobogus_friction_solver mu="0.3" CoR="0.1" max_iters="100" eval_every="5" tol="1e-8"
+                               staggering="geometric" cache_impulses="normal"/>
+      <near_earth_gravity f="0.0 -10.0"/>
+      <static_plane x="0 0" n="0 2"/>
+      <geometry type="circle" r="0.5"/>
+      <rigid_body x="1.0 2.0" theta="0.25" v="0.5 -1.0" omega="3.0" rho="2.0" geo_idx="0"/>
+    </rigidbody2d_scene>"""
+    s = scene_io.load_rigidbody2d_scene(text)
+    assert s["dt_rational"] == Fraction(1, 200) and s["integrator"] == "verlet" and s["gravity"] == (0.0, -10.0)
+    assert list(s["q"]) == [1.0, 2.0, 0.25] and list(s["v"]) == [0.5, -1.0, 3.0]
+    assert s["m"][0] == 2.0 * np.pi * 0.5 * 0.5 and s["I"][0] == 0.5 * s["m"][0] * 0.5 * 0.5
+    assert (s["mu"], s["CoR"], s["max_iters"], s["eval_every"], s["cache_mode"]) == (0.3, 0.1, 100, 5, 1)
+    for bad in (text.replace('type="circle" r="0.5"', 'type="box" r="0.5 0.5"'),
+                text.replace('geo_idx="0"', 'geo_idx="0" fixed="1"'),
+                text.replace('staggering="geometric"', 'staggering="stabilized"')):
+        with pytest.raises(scene_io.SceneError):
+            scene_io.load_rigidbody2d_scene(bad)
+
+
+@pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
 def test_registered_slope_scenes_match_the_golden_extraction():
     """The 18 slope scenes registered in ball2dcli/CMakeLists.txt, read by this reader, equal the
     values tests/golden/make_golden.py extracted from the same files with its own code."""
