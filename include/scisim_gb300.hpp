@@ -24,6 +24,7 @@
 #ifndef SCISIM_GB300_HPP
 #define SCISIM_GB300_HPP
 
+#include <atomic>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -187,13 +188,31 @@ class Sobogus final : public FrictionSolver {
 
 // ---------------------------------------------------------------------------------------------
 // Systems.  A system uploads its scene into a context; the impact-friction map owns the context.
+// Each system has an identity of its own, renewed when it is copied or assigned, by which a map
+// knows whether its context still holds this system's scene.  A map keeps the radii, masses,
+// inertia and planes of the system from its first flow; after changing those in place, call the
+// map's resetCachedData() (positions and velocities are passed to every flow).
 class ContactSystem {
  public:
+  ContactSystem() : m_uid(next_uid()) {}
+  ContactSystem(const ContactSystem&) : m_uid(next_uid()) {}
+  ContactSystem& operator=(const ContactSystem&) {
+    m_uid = next_uid();
+    return *this;
+  }
   virtual ~ContactSystem() = default;
+  uint64_t uid() const { return m_uid; }
   virtual unsigned nbodies() const = 0;
   virtual unsigned ambientDimension() const = 0;  // 2 (Ball2D) or 3 (spheres)
   virtual std::vector<double> gravity() const = 0;
   virtual void upload(sg_ctx* ctx) const = 0;
+
+ private:
+  static uint64_t next_uid() {
+    static std::atomic<uint64_t> counter{0};
+    return ++counter;
+  }
+  uint64_t m_uid;
 };
 
 struct StaticPlane2D {  // ball2d/StaticGeometry/StaticPlane.cpp:10-19 (x, n; n normalised)
@@ -328,7 +347,7 @@ class ImpactFrictionMap {
   virtual void resetCachedData() {
     if (m_ctx) sg_ctx_destroy(m_ctx);
     m_ctx = nullptr;
-    m_sys = nullptr;
+    m_sys = 0;
   }
 
   // The context of the last flow (nullptr before the first): for sg_last_contacts and the like.
@@ -348,7 +367,7 @@ class ImpactFrictionMap {
     const Sobogus* sob = dynamic_cast<const Sobogus*>(&solver);
     if (sob == nullptr) throw Error(SG_BAD_INPUT, "only the Sobogus friction solver is available");
     const std::vector<double> g = sys.gravity();
-    const bool same = m_ctx && m_sys == &sys && m_nb == sys.nbodies() && m_integrator == umap.integrator() &&
+    const bool same = m_ctx && m_sys == sys.uid() && m_nb == sys.nbodies() && m_integrator == umap.integrator() &&
                       m_eval_every == sob->evalEvery() && m_precision == sob->precision() &&
                       m_device == sob->device() && m_dt == dt && m_CoR == CoR && m_mu == mu && m_g == g;
     if (same) return m_ctx;
@@ -373,7 +392,7 @@ class ImpactFrictionMap {
       resetCachedData();
       throw;
     }
-    m_sys = &sys;
+    m_sys = sys.uid();
     m_nb = sys.nbodies();
     m_integrator = umap.integrator();
     m_eval_every = sob->evalEvery();
@@ -390,7 +409,7 @@ class ImpactFrictionMap {
   unsigned m_max_iters;
   ImpulsesToCache m_cache;
   sg_ctx* m_ctx = nullptr;
-  const ContactSystem* m_sys = nullptr;
+  uint64_t m_sys = 0;  // uid of the system whose scene the context holds
   unsigned m_nb = 0;
   int32_t m_integrator = -1;
   unsigned m_eval_every = 0;

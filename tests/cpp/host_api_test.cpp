@@ -4,6 +4,7 @@
 //
 //   names       the mirrored classes report the reference's names (e.g. ball2d/VerletMap.cpp:43-46)
 //   validation  invalid settings and state sizes throw Error(SG_BAD_INPUT) before any GPU work
+//   identity    a copied or assigned system gets an identity of its own (a map's context follows it)
 //   no_device   where no GPU can be used, a flow throws Error(SG_CUDA_ERROR) and nothing else
 //               (exits 0 at once where a context can be created)
 //   ball2d_run  <scene file> <out file>: steps the scene through Ball2DSim::flow with the
@@ -114,6 +115,16 @@ int test_validation() {
   return EXIT_SUCCESS;
 }
 
+int test_identity() {
+  Ball2DSim a(two_balls());
+  Ball2DSim b(a);
+  if (a.uid() == b.uid() || a.uid() == 0) return fail("a copy has its own identity");
+  const uint64_t before = b.uid();
+  b = a;
+  if (b.uid() == before || b.uid() == a.uid()) return fail("assignment renews the identity");
+  return EXIT_SUCCESS;
+}
+
 int test_no_device() {
   sg_config c{};
   c.integrator = SG_SYMPLECTIC_EULER;
@@ -200,6 +211,7 @@ int main(int argc, char** argv) {
   try {
     if (test == "names") return test_names();
     if (test == "validation") return test_validation();
+    if (test == "identity") return test_identity();
     if (test == "no_device") return test_no_device();
     if (test == "ball2d_run" && argc == 4) return test_ball2d_run(argv[2], argv[3]);
   } catch (const std::exception& e) {

@@ -39,7 +39,7 @@ def run(exe, *args, timeout=120):
     return subprocess.run([exe] + list(args), capture_output=True, text=True, timeout=timeout)
 
 
-@pytest.mark.parametrize("name", ["names", "validation", "no_device"])
+@pytest.mark.parametrize("name", ["names", "validation", "identity", "no_device"])
 def test_host_api_cpu(host_test, name):
     p = run(host_test, name)
     assert p.returncode == 0, p.stderr
