@@ -18,6 +18,7 @@ signature (scisim/ConstrainedMaps/ImpactFrictionMap.h:36).
 from __future__ import annotations
 
 import enum
+import itertools
 
 import numpy as np
 
@@ -138,7 +139,7 @@ class GeometricImpactFrictionMap:
         self._key = None
 
     def _context(self, sim, umap, solver, dt, CoR, mu):
-        key = (sim.nbodies, id(sim), umap.integrator, solver.eval_every, solver.precision, float(dt), float(CoR),
+        key = (sim.nbodies, sim.system_id, umap.integrator, solver.eval_every, solver.precision, float(dt), float(CoR),
                float(mu), tuple(sim.gravity))
         if self._ctx is None or key != self._key:
             self._ctx = _lib.Context(dt=dt, gravity=sim.gravity, mu=mu, CoR=CoR, tol=self.abs_tol,
@@ -242,12 +243,24 @@ class Ball2DState:
         return np.array([p.n for p in self.static_planes]).reshape(-1)
 
 
+# Identities of simulations: a map's context holds one simulation's scene (radii, masses, planes),
+# and id() of a collected object can be reused, so each simulation draws its own number.
+_SYSTEM_IDS = itertools.count(1)
+
+
+def next_system_id() -> int:
+    return next(_SYSTEM_IDS)
+
+
 class Ball2DSim:
-    """ball2d/Ball2DSim.h: owns the state; flow() advances one step (Ball2DSim.cpp:305-326)."""
+    """ball2d/Ball2DSim.h: owns the state; flow() advances one step (Ball2DSim.cpp:305-326).  A map
+    keeps the radii, masses and planes from its first flow with this simulation; after changing
+    them in place call the map's resetCachedData()."""
 
     def __init__(self, state: Ball2DState, gravity=(0.0, -9.81)):
         self.state = state
         self.gravity = tuple(float(g) for g in gravity)
+        self.system_id = next_system_id()
 
     @property
     def nballs(self):

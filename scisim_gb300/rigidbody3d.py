@@ -24,7 +24,8 @@ import math
 import numpy as np
 
 from . import _lib
-from .ball2d import GeometricImpactFrictionMap, ImpulsesToCache, Sobogus, SobogusSolverType, UnconstrainedMap  # noqa: F401
+from .ball2d import (GeometricImpactFrictionMap, ImpulsesToCache, Sobogus, SobogusSolverType,  # noqa: F401
+                     UnconstrainedMap, next_system_id)
 
 
 class SplitHamMap(UnconstrainedMap):
@@ -111,6 +112,7 @@ class RigidBody3DSim:
         self.gravity = tuple(float(g) for g in gravity)
         if len(self.gravity) != 3:
             raise ValueError("NearEarthGravityForce takes a 3-vector")
+        self.system_id = next_system_id()
 
     @property
     def nbodies(self):
