@@ -206,6 +206,7 @@ typedef struct {
   double tol;
   uint32_t max_iters;
   uint32_t eval_every;
+  int32_t staggering;  // OR_STAGGER_GEOMETRIC or OR_STAGGER_STABILIZED
 } or_rb2d_params;
 
 or_rb2d* or_rb2d_create(int nb, const double* q, const double* v, const double* r, const double* m,

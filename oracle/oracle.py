@@ -47,7 +47,8 @@ class Sphere3DParams(C.Structure):
 class RigidBody2DParams(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("cache_mode", C.c_int32), ("dt", C.c_double),
                 ("gravity", C.c_double * 2), ("mu", C.c_double), ("CoR", C.c_double),
-                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
+                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32),
+                ("staggering", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -509,14 +510,15 @@ class RigidBody2D:
     q, v: 3 per body ([x y theta], [vx vy omega]); r, m, I per body; planes 2 each."""
 
     def __init__(self, q, v, r, m, I, plane_x, plane_n, *, dt, gravity=(0.0, -9.81), mu=0.5, CoR=0.0,
-                 tol=1e-9, max_iters=5000, eval_every=1, integrator=SYMPLECTIC_EULER, cache_mode=CACHE_NONE):
+                 tol=1e-9, max_iters=5000, eval_every=1, integrator=SYMPLECTIC_EULER, cache_mode=CACHE_NONE,
+                 staggering=STAGGER_GEOMETRIC):
         self.q, self.v = f64(q), f64(v)
         self.r, self.m, self.I = f64(r), f64(m), f64(I)
         self.nb = self.r.shape[0]
         px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
         self.np = px.shape[0] // 2
         p = RigidBody2DParams(integrator, cache_mode, dt, (C.c_double * 2)(*gravity), mu, CoR, tol, max_iters,
-                              eval_every)
+                              eval_every, staggering)
         self._h = lib().or_rb2d_create(self.nb, _d(self.q), _d(self.v), _d(self.r), _d(self.m), _d(self.I),
                                        self.np, _d(px), _d(pn), C.byref(p))
         self.iteration = 0

@@ -18,6 +18,7 @@
 //   SobogusFrictionProblem::solveRigidBody2D     scisim/ConstrainedMaps/Sobogus.cpp:375-470
 //   RigidBody2DSobogusInterface::fromPrimal      scisim/ConstrainedMaps/bogus/RigidBody2DSobogusInterface.cpp:31-89
 //   GeometricImpactFrictionMap::flow             scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:267-442
+//   StabilizedImpactFrictionMap::flow            scisim/ConstrainedMaps/StabilizedImpactFrictionMap.cpp:48-167
 //   ConstraintCache                              rigidbody2d/ConstraintCache.cpp (keys (i, j) for circle
 //                                                pairs, (plane, body) for planes)
 // A body has three degrees of freedom (x, y, theta) and the mass block diag(m, m, I).  The normal
@@ -388,6 +389,9 @@ extern "C" void or_rb2d_destroy(or_rb2d* s) { delete s; }
 extern "C" int or_rb2d_step(or_rb2d* s, uint32_t iteration, or_step_stats* stats) {
   (void)iteration;
   const int nb = s->nb;
+  // StabilizedImpactFrictionMap::flow (StabilizedImpactFrictionMap.cpp:48-167): the unconstrained
+  // step first, a cold solve from its velocity v1, then q1 = q0 + dt v.
+  const bool stab = s->p.staggering == OR_STAGGER_STABILIZED;
   std::vector<double> q1(3 * static_cast<size_t>(nb)), v1(3 * static_cast<size_t>(nb));
   umap_flow(s, s->q.data(), s->v.data(), q1.data(), v1.data());
   std::vector<Contact> cs;
@@ -435,7 +439,7 @@ extern "C" int or_rb2d_step(or_rb2d* s, uint32_t iteration, or_step_stats* stats
   std::vector<double> v2(3 * static_cast<size_t>(nb));
   or_gs_result gr{};
   const int32_t* order = int64_t(s->next_order.size()) == int64_t(nc) ? s->next_order.data() : nullptr;
-  solve_rb2d(s, s->v.data(), cs, order, alpha.data(), beta.data(), v2.data(), &gr);
+  solve_rb2d(s, stab ? v1.data() : s->v.data(), cs, order, alpha.data(), beta.data(), v2.data(), &gr);
   s->next_order.clear();
   if (s->p.cache_mode != OR_CACHE_NONE) {
     for (int k = 0; k < nc; ++k) {
@@ -458,7 +462,15 @@ extern "C" int or_rb2d_step(or_rb2d* s, uint32_t iteration, or_step_stats* stats
     stats->succeeded = gr.succeeded;
     stats->error = gr.error;
   }
-  umap_flow(s, s->q.data(), v2.data(), q1.data(), v1.data());
+  if (stab) {
+    for (int i = 0; i < 3 * nb; ++i) {
+      v1[i] = v2[i];
+      q1[i] = s->q[i] + s->p.dt * v1[i];
+    }
+  } else {
+    // Final map with the post-impact velocity (GeometricImpactFrictionMap.cpp:441).
+    umap_flow(s, s->q.data(), v2.data(), q1.data(), v1.data());
+  }
   s->q.swap(q1);
   s->v.swap(v1);
   return gr.succeeded ? 0 : 1;

@@ -225,7 +225,7 @@ def load_ball2d_scene(source) -> dict:
 
 def load_rigidbody2d_scene(source) -> dict:
     """A `<rigidbody2d_scene>` of circles as arrays and settings (RigidBody2DSceneParser.cpp), for
-    the geometric staggering: `rigid_body` elements with a circle geometry, mass and inertia from
+    the geometric or stabilized staggering: `rigid_body` elements with a circle geometry, mass and inertia from
     rho (CircleGeometry::computeMassAndInertia, rigidbody2d/CircleGeometry.cpp:29-33: m = rho pi r^2,
     I = m r^2 / 2).  Returns q, v (3 per body: x, y, theta / vx, vy, omega), r, m, I, plane_x,
     plane_n (2 per plane), dt, dt_rational, integrator, gravity, the solver settings and end_time.
@@ -270,8 +270,9 @@ def load_rigidbody2d_scene(source) -> dict:
         m.append(mk)
         inertia.append(0.5 * mk * rk * rk)
     solver = _solver(root)
-    if solver["staggering"] != "geometric":
-        raise SceneError("sobogus_friction_solver: only the geometric staggering is supported for rigidbody2d")
+    if solver["staggering"] not in ("geometric", "stabilized"):
+        # RigidBody2DSceneParser.cpp:1054-1061 knows these two
+        raise SceneError("sobogus_friction_solver: rigidbody2d takes the geometric or stabilized staggering")
     out = dict(q=np.array(q, np.float64), v=np.array(v, np.float64), r=np.array(r, np.float64),
                m=np.array(m, np.float64), I=np.array(inertia, np.float64),
                plane_x=np.array(px, np.float64).reshape(-1, 2), plane_n=np.array(pn, np.float64).reshape(-1, 2),

@@ -142,9 +142,10 @@ ASSETS = "/root/reference/assets/rigidbody2d"
 
 def _sim(O, sc):
     integ = O.SYMPLECTIC_EULER if sc["integrator"] == "symplectic_euler" else O.VERLET
+    stag = O.STAGGER_STABILIZED if sc["staggering"] == "stabilized" else O.STAGGER_GEOMETRIC
     return O.RigidBody2D(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["plane_x"], sc["plane_n"], dt=sc["dt"],
                          gravity=sc["gravity"], mu=sc["mu"], CoR=sc["CoR"], tol=sc["tol"], max_iters=sc["max_iters"],
-                         eval_every=sc["eval_every"], integrator=integ, cache_mode=sc["cache_mode"])
+                         eval_every=sc["eval_every"], integrator=integ, cache_mode=sc["cache_mode"], staggering=stag)
 
 
 @pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
@@ -181,4 +182,21 @@ def test_reference_circle_scenes_step(oracle):
         assert np.all(np.isfinite(q)) and np.all(np.isfinite(v)), f
         assert st["iterations"] <= sc["max_iters"], f
         ran += 1
-    assert ran >= 18
+    assert ran >= 22
+
+
+@pytest.mark.skipif(not os.path.isdir(ASSETS), reason="reference assets not present")
+def test_reference_drift_safe_ball_on_plane(oracle):
+    """tests_serialization/drift_safe_ball_on_plane.xml with its StabilizedImpactFrictionMap: the
+    ball falls onto the plane and then stays exactly where it stopped, at rest, above the plane
+    (the geometric map would sink it by g dt^2 every step)."""
+    from scisim_gb300 import scene_io
+    sc = scene_io.load_rigidbody2d_scene(os.path.join(ASSETS, "tests_serialization", "drift_safe_ball_on_plane.xml"))
+    assert sc["staggering"] == "stabilized"
+    sim = _sim(oracle, sc)
+    sim.run(200)
+    q_rest, _ = sim.state()
+    st, tot, bad = sim.run(1800)
+    q, v = sim.state()
+    assert bad == 0 and np.array_equal(q, q_rest) and np.all(v == 0.0)
+    assert 0.0 <= q[1] - sc["r"][0] <= 0.01

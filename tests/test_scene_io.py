@@ -118,7 +118,7 @@ def test_reference_rigidbody2d_assets_load_or_are_rejected_by_name():
         n = s["r"].shape[0]
         assert s["q"].shape[0] == 3 * n and s["v"].shape[0] == 3 * n
         assert np.all(s["I"] == 0.5 * s["m"] * s["r"] * s["r"])
-    assert ok >= 18 and "geometry" in reasons
+    assert ok >= 22 and "geometry" in reasons
 
 
 def test_rigidbody2d_scene_values():
@@ -138,7 +138,8 @@ def test_rigidbody2d_scene_values():
     assert (s["mu"], s["CoR"], s["max_iters"], s["eval_every"], s["cache_mode"]) == (0.3, 0.1, 100, 5, 1)
     for bad in (text.replace('type="circle" r="0.5"', 'type="box" r="0.5 0.5"'),
                 text.replace('geo_idx="0"', 'geo_idx="0" fixed="1"'),
-                text.replace('staggering="geometric"', 'staggering="stabilized"')):
+                text.replace('staggering="geometric"', 'staggering="symplectic_euler"'),
+                text.replace('staggering="geometric"', 'staggering="stabilized"')):  # with a cache
         with pytest.raises(scene_io.SceneError):
             scene_io.load_rigidbody2d_scene(bad)
 
