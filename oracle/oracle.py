@@ -13,7 +13,7 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+LIB_PATH = os.environ.get("SG_ORACLE_LIB") or os.path.join(HERE, "_build", "liboracle.so")
 
 SYMPLECTIC_EULER, VERLET = 0, 1
 CACHE_NONE, CACHE_NORMAL, CACHE_NORMAL_AND_FRICTION = 0, 1, 2
