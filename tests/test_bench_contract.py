@@ -39,3 +39,20 @@ def test_reference_arm_other_ranks_exit_quietly():
     p = run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert not [x for x in p.stdout.splitlines() if x.startswith("{")]
+
+
+def test_cpu_samplers_of_the_batched_legs():
+    """The CPU baselines of bench.py's batched legs (which run inside its GPU legs) on tiny
+    batches: a positive rate, one thread per sampled scene at most, and a description."""
+    import sys
+
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    from scisim_gb300 import scenes
+    b = scenes.ball2d_batch(n_scenes=6, nmax=80, seed=1)
+    v, threads, desc = bench.batch_cpu_sample(b, b["q"], b["v"], np.array([0, 2, 5]), 3)
+    assert v is not None and v >= 0.0 and 1 <= threads <= 3 and "3 sampled scenes" in desc
+    sb = scenes.sphere_batch(n_scenes=4, seed=2, nmin=20, nmax=60)
+    v3, threads3, desc3 = bench.sphere_batch_cpu_sample(sb, sb["q"], sb["v"], np.array([1, 3]), 2, 5)
+    assert v3 is not None and v3 >= 0.0 and 1 <= threads3 <= 2 and "2 sampled scenes" in desc3
