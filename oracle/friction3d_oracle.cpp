@@ -48,7 +48,8 @@ extern "C" double or_fb_error(int dim, const double* r, const double* u, double 
 static double solve3d_impl(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0, int nc,
                            const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
                            const double* arm_b, const double* CoR, const double* mu, const or_gs_params* p,
-                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only) {
+                           double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only,
+                           const double* nrel_in = nullptr, const double* drel_in = nullptr) {
   std::vector<double> minv(nb);
   for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];
   std::vector<char> touched(nb, 0);
@@ -81,8 +82,14 @@ static double solve3d_impl(int nb, const double* m, const double* Iinv, const do
     const double ndotv = dot3(n, vr);
     // Kinematic relative velocity is zero (static planes have no motion).
     const double zero3[3] = {0.0, 0.0, 0.0};
-    const double nrel = -dot3(zero3, n);
-    const double drel0 = -dot3(zero3, s), drel1 = -dot3(zero3, t);
+    // Plus the map's extra relative velocities when it supplies them (Sobogus.cpp:890-904).
+    double nrel = -dot3(zero3, n);
+    double drel0 = -dot3(zero3, s), drel1 = -dot3(zero3, t);
+    if (nrel_in) nrel = nrel + nrel_in[k];
+    if (drel_in) {
+      drel0 = drel0 + drel_in[2 * k];
+      drel1 = drel1 + drel_in[2 * k + 1];
+    }
     const double sc = CoR[k] * ndotv + nrel;
     double w[3];
     for (int j = 0; j < 3; ++j) w[j] = ((0.0 + n[j] * sc) + s[j] * drel0) + t[j] * drel1;
@@ -305,6 +312,18 @@ extern "C" void or_sobogus_solve_3d(int nb, const double* m, const double* Iinv,
                                     const or_gs_params* p, double* alpha, double* beta, double* v2, double* f,
                                     or_gs_result* res) {
   solve3d_impl(nb, m, Iinv, Iw, v0, nc, ia, ib, bases, arm_a, arm_b, CoR, mu, p, alpha, beta, v2, f, res, false);
+}
+
+// With the extra relative velocities of the map (nrel: 1, drel: 2 per contact;
+// SymplecticEulerImpactFrictionMap.cpp:293-321).
+extern "C" void or_sobogus_solve_3d_ex(int nb, const double* m, const double* Iinv, const double* Iw,
+                                       const double* v0, int nc, const int32_t* ia, const int32_t* ib,
+                                       const double* bases, const double* arm_a, const double* arm_b,
+                                       const double* CoR, const double* mu, const double* nrel, const double* drel,
+                                       const or_gs_params* p, double* alpha, double* beta, double* v2, double* f,
+                                       or_gs_result* res) {
+  solve3d_impl(nb, m, Iinv, Iw, v0, nc, ia, ib, bases, arm_a, arm_b, CoR, mu, p, alpha, beta, v2, f, res, false,
+               nrel, drel);
 }
 
 extern "C" double or_residual_3d(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0,

@@ -149,6 +149,12 @@ void or_sobogus_solve_3d(int nb, const double* m, const double* Iinv, const doub
                          const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
                          const double* arm_b, const double* CoR, const double* mu, const or_gs_params* p,
                          double* alpha, double* beta, double* v2, double* f, or_gs_result* res);
+// As or_sobogus_solve_3d with the map's extra relative velocities (nrel: 1, drel: 2 per contact).
+void or_sobogus_solve_3d_ex(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0,
+                            int nc, const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
+                            const double* arm_b, const double* CoR, const double* mu, const double* nrel,
+                            const double* drel, const or_gs_params* p, double* alpha, double* beta, double* v2,
+                            double* f, or_gs_result* res);
 double or_residual_3d(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0, int nc,
                       const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
                       const double* arm_b, const double* CoR, const double* mu, const double* alpha,
@@ -167,10 +173,16 @@ typedef struct {
   double tol;
   uint32_t max_iters;
   uint32_t eval_every;
+  int32_t staggering;             // OR_STAGGER_GEOMETRIC (SplitHam map) or OR_STAGGER_SYMPLECTIC_EULER
+  int32_t cache_mode;             // symplectic Euler: OR_CACHE_* (the geometric 3D map keeps none)
+  int32_t stabilize;              // symplectic Euler: pose stabilisation g0 / dt
+  double penetration_threshold;   // symplectic Euler: gaps smaller in magnitude are ignored
 } or_sphere3d_params;
 
 // q: [x (3nb) | R row-major (9nb)], v: [v (3nb) | omega (3nb)], r, m per body, I0: 3 per body.
-// Planes: x and unit n, 3 each.  SplitHam integrator, geometric staggering, no impulse cache.
+// Planes: x and unit n, 3 each.  Geometric staggering with the SplitHam map and no impulse cache,
+// or SymplecticEulerImpactFrictionMap (exponential-Euler configuration updates, impulse cache with
+// the transport of cached forces to the new normal, optional pose stabilisation).
 or_sphere3d* or_sphere3d_create(int nb, const double* q, const double* v, const double* r, const double* m,
                                 const double* I0, int np, const double* plane_x, const double* plane_n,
                                 const or_sphere3d_params* p);

@@ -41,7 +41,9 @@ class Ball2DParams(C.Structure):
 
 class Sphere3DParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("gravity", C.c_double * 3), ("mu", C.c_double), ("CoR", C.c_double),
-                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32)]
+                ("tol", C.c_double), ("max_iters", C.c_uint32), ("eval_every", C.c_uint32),
+                ("staggering", C.c_int32), ("cache_mode", C.c_int32), ("stabilize", C.c_int32),
+                ("penetration_threshold", C.c_double)]
 
 
 class RigidBody2DParams(C.Structure):
@@ -393,13 +395,15 @@ class Sphere3D:
     """RigidBody3D spheres stepped by SplitHam + GeometricImpactFrictionMap + Sobogus (CPU oracle)."""
 
     def __init__(self, q, v, r, m, I0, plane_x, plane_n, *, dt, gravity=(0.0, 0.0, -9.81), mu=0.5,
-                 CoR=0.0, tol=1e-9, max_iters=5000, eval_every=1):
+                 CoR=0.0, tol=1e-9, max_iters=5000, eval_every=1, staggering=STAGGER_GEOMETRIC,
+                 cache_mode=CACHE_NONE, stabilize=False, penetration_threshold=0.0):
         self.q, self.v = f64(q), f64(v)
         self.r, self.m, self.I0 = f64(r), f64(m), f64(I0)
         self.nb = self.r.shape[0]
         px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
         self.np = px.shape[0] // 3
-        p = Sphere3DParams(dt, (C.c_double * 3)(*gravity), mu, CoR, tol, max_iters, eval_every)
+        p = Sphere3DParams(dt, (C.c_double * 3)(*gravity), mu, CoR, tol, max_iters, eval_every, staggering,
+                           cache_mode, 1 if stabilize else 0, penetration_threshold)
         self._h = lib().or_sphere3d_create(self.nb, _d(self.q), _d(self.v), _d(self.r), _d(self.m),
                                            _d(self.I0), self.np, _d(px), _d(pn), C.byref(p))
         self.iteration = 0

@@ -20,6 +20,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <array>
+#include <map>
 #include <vector>
 
 extern "C" void or_sobogus_solve_3d(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0,
@@ -101,6 +103,10 @@ struct or_sphere3d {
   // last step
   std::vector<Contact3> contacts;
   std::vector<double> bases, arm_a, arm_b, alpha, beta;
+  // SymplecticEulerImpactFrictionMap's impulse cache (rigidbody3d/ConstraintCache.cpp): keys (i, j)
+  // for sphere pairs, (plane, sphere) for planes; values [alpha, 0, ...] (normal) or
+  // [n (3) | alpha n + beta0 s + beta1 t (3)] (normal and friction).
+  std::map<std::pair<unsigned, unsigned>, std::array<double, 6>> cache_ss, cache_ps;
 };
 
 namespace {
@@ -363,8 +369,274 @@ extern "C" int64_t or_sphere3d_last_contacts(const or_sphere3d* s, int64_t cap, 
   return n;
 }
 
+// Per contact of s->contacts: body indices, arms from the centres to the contact point at q0
+// (-r n for a plane) and the velocity-dependent basis [n s t] from the relative velocity at v0
+// (SphereSphereConstraint.cpp:273-300, StaticPlaneSphereConstraint.cpp:255-283).
+// IntegrationTools::exponentialEuler (rigidbody3d/UnconstrainedMaps/IntegrationTools.cpp:3-47):
+// x1 = x0 + dt v; R1 = rot(omega / |omega|, |omega| dt) R0, the rotation by the Rodrigues formula
+// (Eigen's AngleAxis::toRotationMatrix).
+static void exponential_euler(const or_sphere3d* s, const double* q0, const double* v, double* q1) {
+  const int nb = s->nb;
+  const double dt = s->prm.dt;
+  for (int i = 0; i < nb; ++i)
+    for (int j = 0; j < 3; ++j) q1[3 * i + j] = q0[3 * i + j] + dt * v[3 * i + j];
+  for (int i = 0; i < nb; ++i) {
+    double ax[3] = {v[3 * nb + 3 * i], v[3 * nb + 3 * i + 1], v[3 * nb + 3 * i + 2]};
+    double theta = std::sqrt(dot3(ax, ax));
+    if (theta != 0.0)
+      for (int j = 0; j < 3; ++j) ax[j] = ax[j] / theta;
+    theta = theta * dt;
+    const double sn = std::sin(theta), c = std::cos(theta);
+    const double sa[3] = {sn * ax[0], sn * ax[1], sn * ax[2]};
+    const double c1[3] = {(1.0 - c) * ax[0], (1.0 - c) * ax[1], (1.0 - c) * ax[2]};
+    double R[9];
+    double t = c1[0] * ax[1];
+    R[1] = t - sa[2];
+    R[3] = t + sa[2];
+    t = c1[0] * ax[2];
+    R[2] = t + sa[1];
+    R[6] = t - sa[1];
+    t = c1[1] * ax[2];
+    R[5] = t - sa[0];
+    R[7] = t + sa[0];
+    R[0] = c1[0] * ax[0] + c;
+    R[4] = c1[1] * ax[1] + c;
+    R[8] = c1[2] * ax[2] + c;
+    matmul3(R, &q0[3 * nb + 9 * i], &q1[3 * nb + 9 * i]);
+  }
+}
+
+// Quaternion (w, x, y, z) rotating direction a onto direction b (Eigen's
+// Quaternion::setFromTwoVectors: half-angle form; nearly opposite directions turn by pi about an
+// axis orthogonal to a).
+static void quat_from_two_vectors(const double* a, const double* b, double* q) {
+  double v0[3] = {a[0], a[1], a[2]}, v1[3] = {b[0], b[1], b[2]};
+  normalize3(v0);
+  normalize3(v1);
+  const double c = dot3(v1, v0);
+  if (c < -1.0 + 1e-12) {
+    double axis[3];
+    orthogonal_vector(v0, axis);
+    normalize3(axis);
+    const double w2 = (1.0 + std::max(c, -1.0)) * 0.5;
+    const double sv = std::sqrt(1.0 - w2);
+    q[0] = std::sqrt(w2);
+    for (int j = 0; j < 3; ++j) q[1 + j] = axis[j] * sv;
+    return;
+  }
+  double axis[3];
+  cross3(v0, v1, axis);
+  const double s2 = std::sqrt((1.0 + c) * 2.0);
+  const double invs = 1.0 / s2;
+  for (int j = 0; j < 3; ++j) q[1 + j] = axis[j] * invs;
+  q[0] = s2 * 0.5;
+}
+
+// q v q* for a unit quaternion: uv = 2 (q_v x v); v + w uv + q_v x uv.
+static void quat_rotate(const double* q, const double* v, double* out) {
+  double uv[3], uuv[3];
+  cross3(&q[1], v, uv);
+  for (int j = 0; j < 3; ++j) uv[j] = uv[j] + uv[j];
+  cross3(&q[1], uv, uuv);
+  for (int j = 0; j < 3; ++j) out[j] = (v[j] + q[0] * uv[j]) + uuv[j];
+}
+
+static std::pair<unsigned, unsigned> cache_key3(const Contact3& c) {
+  if (c.b >= 0) return {unsigned(c.a), unsigned(c.b)};
+  return {unsigned(-1 - c.b), unsigned(c.a)};
+}
+
+static void contact_frames(or_sphere3d* s, const double* q0, const double* v0, std::vector<int32_t>& ia,
+                           std::vector<int32_t>& ib) {
+  const int nb = s->nb;
+  const int nc = static_cast<int>(s->contacts.size());
+  for (int k = 0; k < nc; ++k) {
+    const Contact3& ct = s->contacts[k];
+    const int a = ct.a;
+    ia[k] = a;
+    double* ra = &s->arm_a[3 * k];
+    double* rb = &s->arm_b[3 * k];
+    double sv[3];
+    if (ct.b >= 0) {
+      const int b = ct.b;
+      ib[k] = b;
+      for (int j = 0; j < 3; ++j) {
+        ra[j] = ct.p[j] - q0[3 * a + j];
+        rb[j] = ct.p[j] - q0[3 * b + j];
+      }
+      double ca[3], cb[3];
+      cross3(&v0[3 * nb + 3 * a], ra, ca);
+      cross3(&v0[3 * nb + 3 * b], rb, cb);
+      for (int j = 0; j < 3; ++j) sv[j] = ((v0[3 * a + j] + ca[j]) - v0[3 * b + j]) - cb[j];
+    } else {
+      ib[k] = -1;
+      for (int j = 0; j < 3; ++j) ra[j] = (-s->r[a]) * ct.n[j];
+      double ca[3];
+      cross3(&v0[3 * nb + 3 * a], ra, ca);
+      for (int j = 0; j < 3; ++j) sv[j] = (v0[3 * a + j] + ca[j]) - 0.0;
+    }
+    basis_from_relvel(ct.n, sv, &s->bases[9 * k]);
+  }
+}
+
+// SymplecticEulerImpactFrictionMap::flow for spheres (SymplecticEulerImpactFrictionMap.cpp:201-407):
+// vdelta = dt (Minv F); predictor by exponential Euler from v0 + vdelta; the active set; impulses
+// from the cache, cached forces turned from the cached normal to the new one (:48-131); the solve
+// from v0 with nrel = N^T vdelta (+ min(0, gap) / dt when stabilising) and drel = D^T vdelta;
+// v1 = v2 + vdelta, impulses into the cache (:133-199), configuration by exponential Euler from v1.
+static int se_step(or_sphere3d* s, or_step_stats* stats) {
+  const int nb = s->nb;
+  const double dt = s->prm.dt;
+  const double* q0 = s->q.data();
+  const double* v0 = s->v.data();
+  const size_t nv = 6 * static_cast<size_t>(nb);
+  std::vector<double> vdelta(nv), vp(nv), q1(12 * static_cast<size_t>(nb)), v1(nv);
+  for (int i = 0; i < nb; ++i) {
+    const double minv = 1.0 / s->m[i];
+    const double* Ii = &s->Iinv[9 * static_cast<size_t>(i)];
+    for (int j = 0; j < 3; ++j) {
+      const double F = 0.0 + s->m[i] * s->prm.gravity[j];  // NearEarthGravityForce: no torque
+      vdelta[3 * i + j] = dt * (0.0 + minv * F);
+      vdelta[3 * nb + 3 * i + j] = dt * (((0.0 + Ii[3 * j] * 0.0) + Ii[3 * j + 1] * 0.0) + Ii[3 * j + 2] * 0.0);
+    }
+  }
+  for (size_t k = 0; k < nv; ++k) vp[k] = v0[k] + vdelta[k];
+  exponential_euler(s, q0, vp.data(), q1.data());
+  int64_t nss = 0;
+  active_set(s, q0, q1.data(), s->contacts, &nss);
+  const int nc = static_cast<int>(s->contacts.size());
+  or_step_stats st{};
+  st.n_contacts = nc;
+  st.n_ball_ball = nss;
+  st.n_ball_plane = nc - nss;
+  st.succeeded = 1;
+  s->bases.assign(9 * static_cast<size_t>(nc), 0.0);
+  s->arm_a.assign(3 * static_cast<size_t>(nc), 0.0);
+  s->arm_b.assign(3 * static_cast<size_t>(nc), 0.0);
+  s->alpha.assign(nc, 0.0);
+  s->beta.assign(2 * static_cast<size_t>(nc), 0.0);
+  if (nc == 0) {
+    for (size_t k = 0; k < nv; ++k) v1[k] = v0[k] + vdelta[k];
+    exponential_euler(s, q0, v1.data(), q1.data());
+    s->cache_ss.clear();
+    s->cache_ps.clear();
+  } else {
+    std::vector<int32_t> ia(nc), ib(nc);
+    contact_frames(s, q0, v0, ia, ib);
+    // initializeImpulses (:48-131)
+    const int cm = s->prm.cache_mode;
+    for (int k = 0; k < nc && cm != OR_CACHE_NONE; ++k) {
+      const Contact3& ct = s->contacts[k];
+      const auto& cache = ct.b >= 0 ? s->cache_ss : s->cache_ps;
+      const auto it = cache.find(cache_key3(ct));
+      if (it == cache.end()) continue;  // a missing entry reads as zeros
+      const std::array<double, 6>& c = it->second;
+      if (cm == OR_CACHE_NORMAL) {
+        s->alpha[k] = c[0];
+        continue;
+      }
+      bool zero = true;
+      for (double x : c) zero = zero && x == 0.0;
+      if (zero) continue;
+      const double* E = &s->bases[9 * static_cast<size_t>(k)];
+      double qr[4], f[3];
+      quat_from_two_vectors(&c[0], E, qr);
+      quat_rotate(qr, &c[3], f);
+      s->alpha[k] = dot3(f, E);
+      s->beta[2 * k] = dot3(f, E + 3);
+      s->beta[2 * k + 1] = dot3(f, E + 6);
+    }
+    s->cache_ss.clear();
+    s->cache_ps.clear();
+    // nrel = N^T vdelta, drel = D^T vdelta: each column's entries in row order (linear rows of a,
+    // of b, then angular rows of a, of b), accumulated from zero; the normal has no angular rows,
+    // a tangent's angular rows are arm x tangent.
+    std::vector<double> nrel(nc), drel(2 * static_cast<size_t>(nc));
+    for (int k = 0; k < nc; ++k) {
+      const Contact3& ct = s->contacts[k];
+      const double* E = &s->bases[9 * static_cast<size_t>(k)];
+      const int a = ct.a, b = ct.b;
+      const double* la = &vdelta[3 * a];
+      const double* wa = &vdelta[3 * nb + 3 * a];
+      double tn = 0.0;
+      for (int j = 0; j < 3; ++j) tn = tn + E[j] * la[j];
+      if (b >= 0)
+        for (int j = 0; j < 3; ++j) tn = tn + (-E[j]) * vdelta[3 * b + j];
+      nrel[k] = 0.0 + 1.0 * tn;
+      for (int d = 0; d < 2; ++d) {
+        const double* T = E + 3 * (d + 1);
+        double xa[3];
+        cross3(&s->arm_a[3 * k], T, xa);
+        double tt = 0.0;
+        for (int j = 0; j < 3; ++j) tt = tt + T[j] * la[j];
+        if (b >= 0)
+          for (int j = 0; j < 3; ++j) tt = tt + (-T[j]) * vdelta[3 * b + j];
+        for (int j = 0; j < 3; ++j) tt = tt + xa[j] * wa[j];
+        if (b >= 0) {
+          double xb[3];
+          cross3(&s->arm_b[3 * k], T, xb);
+          for (int j = 0; j < 3; ++j) tt = tt + (-xb[j]) * vdelta[3 * nb + 3 * b + j];
+        }
+        drel[2 * k + d] = 0.0 + 1.0 * tt;
+      }
+      if (s->prm.stabilize) {
+        double gap;
+        if (b >= 0) {
+          // SphereSphereConstraint::evaluateGapFunction (SphereSphereConstraint.cpp:28-31)
+          const double d[3] = {q0[3 * a] - q0[3 * b], q0[3 * a + 1] - q0[3 * b + 1], q0[3 * a + 2] - q0[3 * b + 2]};
+          gap = (std::sqrt(dot3(d, d)) - s->r[a]) - s->r[b];
+        } else {
+          // StaticPlaneSphereConstraint::evaluateGapFunction (StaticPlaneSphereConstraint.cpp:31-35)
+          const int pl = -1 - b;
+          const double d[3] = {q0[3 * a] - s->px[3 * pl], q0[3 * a + 1] - s->px[3 * pl + 1],
+                               q0[3 * a + 2] - s->px[3 * pl + 2]};
+          gap = dot3(&s->pn[3 * pl], d) - s->r[a];
+        }
+        double g0 = std::min(0.0, gap);
+        if (std::fabs(g0) < s->prm.penetration_threshold) g0 = 0.0;
+        nrel[k] = nrel[k] + g0 / dt;
+      }
+    }
+    std::vector<double> CoR(nc, s->prm.CoR), mu(nc, s->prm.mu), v2(nv), f(nv);
+    or_gs_params gp{s->prm.tol, s->prm.max_iters, s->prm.eval_every, nullptr};
+    if (static_cast<int64_t>(s->next_order.size()) == nc) gp.order = s->next_order.data();
+    or_gs_result res{};
+    or_sobogus_solve_3d_ex(nb, s->m.data(), s->Iinv.data(), s->Iw.data(), v0, nc, ia.data(), ib.data(),
+                           s->bases.data(), s->arm_a.data(), s->arm_b.data(), CoR.data(), mu.data(), nrel.data(),
+                           drel.data(), &gp, s->alpha.data(), s->beta.data(), v2.data(), f.data(), &res);
+    st.iterations = res.iterations;
+    st.succeeded = res.succeeded;
+    st.error = res.error;
+    for (size_t k = 0; k < nv; ++k) v1[k] = v2[k] + vdelta[k];
+    // cacheImpulses (:133-199)
+    for (int k = 0; k < nc && cm != OR_CACHE_NONE; ++k) {
+      const Contact3& ct = s->contacts[k];
+      auto& cache = ct.b >= 0 ? s->cache_ss : s->cache_ps;
+      std::array<double, 6> c{};
+      if (cm == OR_CACHE_NORMAL) {
+        c[0] = s->alpha[k];
+      } else {
+        const double* E = &s->bases[9 * static_cast<size_t>(k)];
+        for (int j = 0; j < 3; ++j) {
+          c[j] = E[j];
+          c[3 + j] = (s->alpha[k] * E[j] + s->beta[2 * k] * E[3 + j]) + s->beta[2 * k + 1] * E[6 + j];
+        }
+      }
+      cache[cache_key3(ct)] = c;
+    }
+    exponential_euler(s, q0, v1.data(), q1.data());
+  }
+  s->next_order.clear();
+  s->q.swap(q1);
+  s->v.swap(v1);
+  update_world_inertia(s, false);
+  if (stats) *stats = st;
+  return st.succeeded ? 0 : 1;
+}
+
 extern "C" int or_sphere3d_step(or_sphere3d* s, uint32_t iteration, or_step_stats* stats) {
   (void)iteration;
+  if (s->prm.staggering == OR_STAGGER_SYMPLECTIC_EULER) return se_step(s, stats);
   const int nb = s->nb;
   std::vector<double> q1(12 * static_cast<size_t>(nb)), v1(6 * static_cast<size_t>(nb));
   splitham(s, s->q.data(), s->v.data(), q1.data(), v1.data());
@@ -385,33 +657,7 @@ extern "C" int or_sphere3d_step(or_sphere3d* s, uint32_t iteration, or_step_stat
     const double* q0 = s->q.data();
     const double* v0 = s->v.data();
     std::vector<int32_t> ia(nc), ib(nc);
-    for (int k = 0; k < nc; ++k) {
-      const Contact3& ct = s->contacts[k];
-      const int a = ct.a;
-      ia[k] = a;
-      double* ra = &s->arm_a[3 * k];
-      double* rb = &s->arm_b[3 * k];
-      double sv[3];
-      if (ct.b >= 0) {
-        const int b = ct.b;
-        ib[k] = b;
-        for (int j = 0; j < 3; ++j) {
-          ra[j] = ct.p[j] - q0[3 * a + j];
-          rb[j] = ct.p[j] - q0[3 * b + j];
-        }
-        double ca[3], cb[3];
-        cross3(&v0[3 * nb + 3 * a], ra, ca);
-        cross3(&v0[3 * nb + 3 * b], rb, cb);
-        for (int j = 0; j < 3; ++j) sv[j] = ((v0[3 * a + j] + ca[j]) - v0[3 * b + j]) - cb[j];
-      } else {
-        ib[k] = -1;
-        for (int j = 0; j < 3; ++j) ra[j] = (-s->r[a]) * ct.n[j];
-        double ca[3];
-        cross3(&v0[3 * nb + 3 * a], ra, ca);
-        for (int j = 0; j < 3; ++j) sv[j] = (v0[3 * a + j] + ca[j]) - 0.0;
-      }
-      basis_from_relvel(ct.n, sv, &s->bases[9 * k]);
-    }
+    contact_frames(s, q0, v0, ia, ib);
     std::vector<double> CoR(nc, s->prm.CoR), mu(nc, s->prm.mu);
     or_gs_params gp{s->prm.tol, s->prm.max_iters, s->prm.eval_every, nullptr};
     if (static_cast<int64_t>(s->next_order.size()) == nc) gp.order = s->next_order.data();

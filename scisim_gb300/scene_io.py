@@ -143,7 +143,7 @@ def _solver(root, tag_3d=False):
     nd = nodes[0]
     tag = "sobogus_friction_solver"
     stag = _attr(nd, "staggering", tag)
-    allowed = ("geometric",) if tag_3d else ("geometric", "symplectic_euler", "stabilized")
+    allowed = ("geometric", "symplectic_euler") if tag_3d else ("geometric", "symplectic_euler", "stabilized")
     if stag not in allowed:
         raise SceneError("%s: staggering %r is not supported (%s)" % (tag, stag, ", ".join(allowed)))
     cache = _attr(nd, "cache_impulses", tag)
@@ -164,7 +164,7 @@ def _solver(root, tag_3d=False):
         out["penetration_threshold"] = _scalar(nd, "penetration_threshold", tag)
         if out["penetration_threshold"] < 0.0:
             raise SceneError("%s: penetration_threshold must be non-negative" % tag)
-    if tag_3d:
+    if tag_3d and stag == "geometric":
         out["cache_mode"] = 0  # the 3D geometric map keeps no cache (RigidBody3DSceneParser.cpp:1877-1880)
     return out
 
@@ -283,7 +283,9 @@ def load_rigidbody2d_scene(source) -> dict:
 
 def load_rigidbody3d_scene(source) -> dict:
     """A `<rigidbody3d_scene>` of spheres as arrays and settings (RigidBody3DSceneParser.cpp), for
-    the split_ham integrator and geometric staggering.  Bodies: `rigid_body_with_density` with a
+    the geometric staggering with the split_ham integrator, or the symplectic_euler staggering
+    (whose map does not call the integrator, so `dmv` is accepted there; the GPU library steps
+    only the geometric form, the oracle both).  Bodies: `rigid_body_with_density` with a
     sphere geometry, mass and inertia from rho (RigidBodySphere::computeMassAndInertia), identity
     orientation (an `R` attribute, an Eigen AngleAxis, is not supported).  Returns q = [x | R],
     v = [v | omega], r, m, I0, plane_x, plane_n (3 per plane), dt, gravity and the solver settings."""
@@ -293,7 +295,7 @@ def load_rigidbody3d_scene(source) -> dict:
     _check_tags(root, ("camera_perspective", "camera_orthographic", "end_time", "integrator",
                        "sobogus_friction_solver", "near_earth_gravity", "static_plane", "geometry",
                        "rigid_body_with_density", "static_plane_renderer"))
-    kind, dt = _dt(root, ("split_ham",))
+    kind, dt = _dt(root, ("split_ham", "dmv"))
     grav = root.findall("near_earth_gravity")
     if len(grav) > 1:
         raise SceneError("more than one near_earth_gravity force")
@@ -338,6 +340,9 @@ def load_rigidbody3d_scene(source) -> dict:
                plane_n=np.array(pn, np.float64).reshape(-1, 3), dt=float(dt), dt_rational=dt, integrator=kind,
                gravity=g, end_time=_end_time(root))
     out.update(_solver(root, tag_3d=True))
+    if out["staggering"] == "geometric" and kind != "split_ham":
+        # the geometric map runs the integrator; only SplitHamMap is built for spheres
+        raise SceneError("integrator: the geometric staggering of spheres takes split_ham")
     return out
 
 
@@ -369,6 +374,8 @@ def ball2d_objects(scene: dict):
 
 def rigidbody3d_objects(scene: dict):
     """As ball2d_objects for a loaded sphere scene (SplitHamMap, no impulse cache)."""
+    if scene.get("staggering", "geometric") != "geometric":
+        raise SceneError("the GPU library steps spheres with the geometric staggering only")
     from .ball2d import GeometricImpactFrictionMap, ImpulsesToCache, Sobogus, SobogusSolverType
     from .rigidbody3d import RigidBody3DSim, RigidBody3DState, SplitHamMap, StaticPlane
     planes = [StaticPlane(x, n) for x, n in zip(scene["plane_x"], scene["plane_n"])]
