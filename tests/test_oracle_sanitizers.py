@@ -1,8 +1,8 @@
 """The oracle under AddressSanitizer and UndefinedBehaviorSanitizer, as the reference runs its own
 C++ (CMakeLists.txt:261, SANITIZER=address|undefined): the Makefile's `sanitize` build of the same
 sources is loaded in a child process with libasan preloaded, and a workout of every oracle entry
-point the tests use (broad phase, CCD, the Ball2D, symplectic-Euler, stabilized, sphere and
-RigidBody2D steppers with and without the impulse cache, the standalone solves, the residuals
+point the tests use (broad phase, CCD, the Ball2D, symplectic-Euler, stabilized, sphere (both
+staggerings) and RigidBody2D steppers with and without the impulse cache, the standalone solves, the residuals
 and the MLP) must finish without a sanitizer report.
 """
 import os
@@ -39,6 +39,11 @@ o = O.Sphere3D(sp["q"], sp["v"], sp["r"], sp["m"], sp["I0"], sp["plane_x"], sp["
 o.run(30)
 o.last_contacts()
 o.world_inertia()
+se = O.Sphere3D(sp["q"], sp["v"], sp["r"], sp["m"], sp["I0"], sp["plane_x"], sp["plane_n"], dt=sp["dt"],
+                gravity=sp["gravity"], mu=sp["mu"], CoR=0.0, tol=1e-9, max_iters=200,
+                staggering=O.STAGGER_SYMPLECTIC_EULER, cache_mode=O.CACHE_NORMAL_AND_FRICTION, stabilize=True,
+                penetration_threshold=1e-5)
+se.run(30)
 n = 24
 r = rng.uniform(0.1, 0.2, n)
 m, I = O.circle_mass_inertia(r, 1.0)
