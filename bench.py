@@ -1,28 +1,33 @@
 #!/usr/bin/env python
-"""Contact-steps/s of SCISim's Ball2D contact path on one GB300.
+"""Contact-steps/s of SCISim's Ball2D contact path on one GB300, every step solved to residual <= 1e-6.
 
 Workload (the headline configuration): the Ball2D dense pile, 262,144 discs with
 radii log-uniform in [0.02, 0.06] (density 1), seeded non-overlapping fill of a
 40 x 60 box with four walls, gravity -9.81, symplectic Euler dt 0.005, CoR 0,
 mu 0.4, Coulomb residual tolerance 1e-6 (FP64-evaluated), at most 5,000
-Gauss-Seidel iterations per step.  The job starts from the fill; the first
---preroll steps (the pile forming) are run but not timed, then --warmup steps,
-then --steps timed steps.
+Gauss-Seidel sweeps per step.  The job starts from the fill: the pile falls and
+forms during capped pre-roll phases (--schedule, untimed), then settles at the full
+settings until --settle-converged consecutive steps reach the tolerance (untimed),
+then --warmup steps, then --steps timed steps.  Every timed step's residual and
+convergence are reported.
 
 A step is one GeometricImpactFrictionMap::flow of the whole scene: predictor,
 broad + narrow phase, contact assembly, coloured block Gauss-Seidel to tolerance,
 impulse cache, final map.  value = sum of active contacts over the timed steps /
 their device time (inputs resident in HBM, L2 flushed between steps).  e2e = the
 same through the reference-facing C-ABI call sg_flow with pinned host buffers
-(q0, v0 up; q1, v1 down) inside the timed region.
+(q0, v0 up; q1, v1 down) inside the timed region, from the same state and cache.
 
-Solver forms: "warm" (impulse cache NORMAL_AND_FRICTION, the previous step's
-impulses as the start) is the headline; "plain" (cold start, FP64) is timed on the
-same state and reported beside it.
+Solver forms, all from the state (positions, velocities, impulse cache) the timed
+steps start from: "warm" (impulse cache NORMAL_AND_FRICTION, FP32 sweeps with FP64
+residual and refinement, two-level sweeps) is the headline; "plain" is FP64 Gauss-Seidel,
+with the impulse cache (plain_fp64_gpu) and cold (plain_fp64_cold_gpu, one step with a
+larger sweep cap, which it does not reach the tolerance within).
 
 --impl reference times the reference algorithm's CPU implementation (the oracle,
 a restatement of SCISim + So-bogus; the reference itself needs Eigen/So-bogus,
-absent here) on a bounded sample of the same workload.
+absent here) on the same configuration: the same pile, formed and settled by the same
+deterministic GPU pre-roll (untimed), stepped from the same state and impulse cache.
 """
 from __future__ import annotations
 
@@ -159,36 +164,59 @@ def solver_kw(s, **over):
 
 
 # --------------------------------------------------------------------------- CPU leg
-def cpu_sample(args, steps):
-    """The oracle on a strip of the same workload: same disc distribution, depth and
-    solver settings, width 40/32 (8,192 discs).  Pre-rolled to the same step on the
-    CPU, then `steps` timed steps.  A strip this wide is in the pile's regime (every step
-    runs to the 5,000-sweep cap, residual ~1e-2); a narrower one settles against its walls
-    and converges in tens of sweeps, which times a different problem.
-    Returns (contact-steps/s, description)."""
+def cpu_from_state(s, q, v, cache, steps, first_iteration):
+    """The oracle (C++ restatement of SCISim + So-bogus, sequential block Gauss-Seidel in active-set
+    order, one host thread) stepping the pile from the given state and impulse cache (the contacts and
+    impulses of the step before, as the GPU left them) for `steps` steps at the full settings, each
+    step timed on the host clock.  Returns (contact-steps/s, description, per-step records)."""
+    from oracle import oracle as O  # the oracle: CPU baseline only
+    O.build()
+    kw = solver_kw(s)
+    sim = O.Ball2D(q, v, s["r"], s["m"], s["plane_x"], s["plane_n"], cache_mode=O.CACHE_NORMAL_AND_FRICTION, **kw)
+    if cache is not None:
+        sim.set_cache(cache["ia"], cache["ib"], cache["alpha"], cache["beta"])
+    sim.iteration = first_iteration - 1
+    recs, tot, wall = [], 0, 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        st = sim.step()
+        dt = time.perf_counter() - t0
+        wall += dt
+        tot += st["n_contacts"]
+        recs.append({"n_contacts": st["n_contacts"], "converged": bool(st["succeeded"]), "residual": st["error"],
+                     "sweeps": st["iterations"], "s": dt})
+    conv = sum(r["converged"] for r in recs)
+    desc = ("oracle (C++ restatement of SCISim + So-bogus: grid broad phase, CCD, sequential block Gauss-Seidel "
+            "in active-set order, 1 host thread) on the full %d-disc pile from the GPU's state and impulse cache, "
+            "%d steps at the full settings: %d contact-steps in %.2f s, %d of %d steps converged, residuals %s, "
+            "sweeps %s" % (s["r"].shape[0], steps, tot, wall, conv, steps,
+                           [float("%.3g" % r["residual"]) for r in recs], [r["sweeps"] for r in recs]))
+    return (tot / wall if wall > 0 else None), desc, recs
+
+
+def cpu_strip_sample(args, steps):
+    """Without a GPU (CPU-only runs of the reference arm): the oracle on a strip of the same fill
+    (width 40/32 of the pile's at this depth), pre-rolled on the CPU with capped solves, then `steps`
+    steps at the full settings.  Returns (contact-steps/s, description)."""
     from oracle import oracle as O  # the oracle: CPU baseline only
     O.build()
     n = max(2048, args.n // 32)
     s = make_scene(n)
-    frac = 262144.0 / n
     kw = solver_kw(s)
     sim = O.Ball2D(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"],
                    cache_mode=O.CACHE_NORMAL_AND_FRICTION, **kw)
-    t0 = time.perf_counter()
-    sim.set_solver(kw["tol"], args.preroll_iters)
-    sim.run(args.preroll)
+    pre = sum(n_ for n_, _ in parse_schedule(args.schedule))
+    sim.set_solver(kw["tol"], 50)
+    sim.run(pre)
     sim.set_solver(kw["tol"], kw["max_iters"])
     sim.run(args.warmup)
-    pre = time.perf_counter() - t0
     t0 = time.perf_counter()
     st, tot, bad = sim.run(steps)
     dt = time.perf_counter() - t0
-    desc = ("oracle (C++ restatement of SCISim + So-bogus, sequential block GS, 1 thread) on a %d-disc strip "
-            "(width 40/%d, same depth, radii, density and solver settings), pre-rolled %d steps on the CPU in "
-            "%.1f s, then %d timed steps: %d contact-steps in %.2f s (%d of them at the %d-sweep cap, last "
-            "residual %.1e)" % (n, frac, args.preroll + args.warmup, pre, steps, tot, dt, bad, kw["max_iters"],
-                                st["error"]))
-    return tot / dt, desc, 1
+    desc = ("no GPU: oracle (1 thread) on a %d-disc strip of the same fill pre-rolled %d capped steps on the "
+            "CPU, then %d steps: %d contact-steps in %.2f s (%d not converged, last residual %.1e)" %
+            (n, pre + args.warmup, steps, tot, dt, bad, st["error"]))
+    return tot / dt, desc
 
 
 def batch_cpu_sample(b, q0, v0, pick, steps):
@@ -249,37 +277,109 @@ def sphere_batch_cpu_sample(b, q0, v0, pick, steps, first_iteration):
 
 
 def run_reference(args):
-    ws, rank, _ = dist_env()
+    """The reference arm: the oracle on the CPU, on the headline configuration (the same pile formed
+    and settled by the same deterministic GPU pre-roll, untimed, then stepped on the CPU from the
+    state and impulse cache the GPU arm's timed steps start from).  Rank 0 only."""
+    ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    value, desc, cores = cpu_sample(args, args.steps)
+    gpu = False
+    try:
+        import torch
+        gpu = torch.cuda.is_available()
+    except Exception:
+        gpu = False
+    if gpu:
+        torch.cuda.set_device(local)
+        ctx, s, it, info = form_pile(args, local)
+        q, v = ctx.state()
+        cache = ctx.last_contacts()
+        ctx.close()
+        value, desc, recs = cpu_from_state(s, q, v, cache, args.steps, it)
+        sample = "the full %d-disc pile from the GPU-formed state (%s)" % (s["r"].shape[0], pile_note(info))
+        conv = {"steps_converged": sum(r["converged"] for r in recs), "steps": len(recs),
+                "max_residual": max(r["residual"] for r in recs) if recs else None,
+                "sweeps_per_step": [r["sweeps"] for r in recs]}
+        same = True
+    else:
+        value, desc = cpu_strip_sample(args, args.steps)
+        sample, conv, same = "8,192-disc strip of the same fill (no GPU to form the pile)", None, False
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dense-pile fill)",
-            "config": {"workload": WORKLOAD, "sample": "8,192-disc strip of the same fill",
-                       "tol": 1e-6, "max_iters": 5000, "warm_start": "normal_and_friction"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "config": {"workload": WORKLOAD if args.n == 262144 else "ball2d_dense_pile_%d" % args.n,
+                       "sample": sample, "tol": 1e-6, "max_iters": 5000, "warm_start": "normal_and_friction",
+                       "same_state_as_gpu_arm": same},
+            "convergence": conv,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
 # --------------------------------------------------------------------------- GPU leg
-def timed_steps(ctx, torch, stream, k, flush):
-    """k steps, each bracketed by CUDA events on the library's stream; L2 flushed between."""
-    ms, contacts = [], []
-    for _ in range(k):
+def timed_steps(ctx, torch, stream, k, flush, first_iteration=1):
+    """k steps, each bracketed by CUDA events on the library's stream; L2 flushed between.
+    Returns (ms per step, contacts per step, per-step solve records)."""
+    ms, contacts, recs = [], [], []
+    for j in range(k):
         flush.zero_()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        st = ctx.step(1)
+        st = ctx.step(1, first_iteration=first_iteration + j)
         e1.record(stream)
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
         contacts.append(st["n_contacts"])
-    return ms, contacts
+        recs.append({"converged": bool(st["succeeded"]), "residual": st["error"], "sweeps": st["iterations"]})
+    return ms, contacts, recs
+
+
+STAGES = ["predictor_and_grid", "pair_counting_and_plane_flags", "contact_writes_and_assembly", "colouring",
+          "start_check_partition_and_packing", "gauss_seidel", "final_velocity", "extract_cache_final_map"]
+
+
+def headline_roofline(prof, total_ms, args):
+    """Roofline of the Gauss-Seidel kernel over the timed steps (algorithmic bytes per launch over its
+    CUDA-event time per launch) and the step's stage times from the library's stage events."""
+    hbm, peak_kind = peaks()
+    gl = max(prof["gs_launches"], 1)
+    bytes_per_launch = gs_bytes(prof) / gl
+    gs_ms_per_launch = prof["gs_ms"] / gl
+    achieved = bytes_per_launch / (gs_ms_per_launch / 1e3) / 1e9 if gs_ms_per_launch > 0 else 0.0
+    two_level = prof.get("two_level_solves", 0) >= prof["gs_launches"] > 0
+    if two_level:
+        kname = "k_gs_patch (two-level FP32 sweeps: patches on shared memory, boundary contacts over the grid)"
+    elif prof.get("fp64_start_solves", 0) >= prof["gs_launches"] > 0 or args.precision == 0:
+        kname = "k_gs (cooperative coloured block Gauss-Seidel, FP64)"
+    else:
+        kname = "k_gs_mixed (cooperative FP32 sweeps, FP64 checks and refinement)"
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "k_gs_patch_traffic.txt" if two_level else "k_gs_mixed_traffic.txt")
+    if os.path.exists(tp) and two_level:
+        for line in open(tp):
+            if line.startswith("dram_bytes_per_algorithmic_byte"):
+                traffic = float(line.split()[1]) * bytes_per_launch
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind, "kernel": kname,
+                "bytes_per_launch": bytes_per_launch, "ms_per_launch": gs_ms_per_launch,
+                "gs_share_of_step": prof["gs_ms"] / total_ms if total_ms else None}
+    steps = max(prof["steps"], 1)
+    stages = {name: round(ms / steps, 4) for name, ms in zip(STAGES, prof["stage_ms"])}
+    return roofline, stages
+
+
+def convergence_record(recs):
+    """Per-step convergence of timed steps: solve_succeeded (error < tol) as SCISim reports it
+    (GeometricImpactFrictionMap.cpp:344-350), residuals and sweeps."""
+    if not recs:
+        return None
+    return {"steps_converged": sum(r["converged"] for r in recs), "steps": len(recs),
+            "all_converged": all(r["converged"] for r in recs),
+            "max_residual": max(r["residual"] for r in recs), "tol": 1e-6,
+            "residuals": [float("%.4g" % r["residual"]) for r in recs], "sweeps": [r["sweeps"] for r in recs]}
 
 
 def batch_leg(args, torch, local, flush, ws=1, rank=0):
@@ -481,7 +581,7 @@ def sphere_leg(args, torch, local, flush):
     stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=local)
     ctx.profile_enable(True)
     ctx.profile_read(reset=True)
-    ms, contacts = timed_steps(ctx, torch, stream, args.sphere_steps, flush)
+    ms, contacts, _ = timed_steps(ctx, torch, stream, args.sphere_steps, flush, args.sphere_preroll + 1)
     prof = ctx.profile_read(reset=True)
     tot = float(sum(ms))
     value = sum(contacts) / (tot / 1e3)
@@ -569,6 +669,63 @@ def mlp_leg(args, torch, local):
     return out
 
 
+def parse_schedule(txt):
+    """'600:50,300:200' -> [(600, 50), (300, 200)]: pre-roll phases of (steps, sweep cap)."""
+    out = []
+    for part in txt.split(","):
+        if part.strip():
+            a, b = part.split(":")
+            out.append((int(a), int(b)))
+    return out
+
+
+def pile_note(info):
+    return ("pre-roll %s steps:sweep cap, then %d settling steps at the full settings (%d converged, %s), "
+            "then %d warm-up steps" % (",".join("%d:%d" % (p["steps"], p["sweep_cap"]) for p in info["phases"]),
+                                      info["settle_steps"], info["settle_converged_steps"],
+                                      "settled" if info["settled"] else "not settled within the limit",
+                                      info["warmup_steps"]))
+
+
+def form_pile(args, local):
+    """The dense pile formed and settled on the GPU, untimed: pre-roll phases with capped sweeps
+    (--schedule: the fill falls, impacts and compacts), then steps at the full settings (tol 1e-6,
+    5,000 sweeps) until --settle-converged consecutive steps reach the tolerance (at most
+    --settle-max steps), then --warmup steps.  Deterministic: the same arguments give the same state.
+    Returns (context, scene, next step index, record)."""
+    from scisim_gb300 import _lib
+    s = make_scene(args.n)
+    ctx = _lib.Context(device=local, cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision,
+                       **solver_kw(s))
+    ctx.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
+    it = 1
+    t0 = time.perf_counter()
+    phases = []
+    for n, cap in parse_schedule(args.schedule):
+        ctx.reconfigure(max_iters=cap)
+        st = ctx.step(n, first_iteration=it)
+        it += n
+        phases.append({"steps": n, "sweep_cap": cap, "last_residual": st["error"]})
+    ctx.reconfigure(max_iters=5000)
+    t1 = time.perf_counter()
+    run = settle = conv = 0
+    while settle < args.settle_max and run < args.settle_converged:
+        st = ctx.step(1, first_iteration=it)
+        it += 1
+        settle += 1
+        run = run + 1 if st["succeeded"] else 0
+        conv += int(st["succeeded"])
+    t2 = time.perf_counter()
+    for _ in range(args.warmup):
+        ctx.step(1, first_iteration=it)
+        it += 1
+    info = {"phases": phases, "settle_steps": settle, "settle_converged_steps": conv,
+            "settled": run >= args.settle_converged, "warmup_steps": args.warmup,
+            "preroll_s": round(t1 - t0, 2), "settle_s": round(t2 - t1, 2)}
+    log("pile formed: %s" % info)
+    return ctx, s, it, info
+
+
 def run_ours(args):
     import torch
 
@@ -579,31 +736,22 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    s = make_scene(args.n)
+    fast, s, it0, pile = form_pile(args, local)
     nb = s["r"].shape[0]
-    fast = _lib.Context(device=local, cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision,
-                        **solver_kw(s))
-    fast.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
     stream = torch.cuda.ExternalStream(fast.stream_ptr(), device=local)
-    t0 = time.perf_counter()
-    # The pile forms during the pre-roll; its solves are capped at --preroll-iters sweeps
-    # (warm started) so that forming the pile costs seconds, not the full-tolerance price.
-    fast.reconfigure(max_iters=args.preroll_iters)
-    pre = fast.step(args.preroll) if args.preroll else {"total_contacts": 0}
-    fast.reconfigure(max_iters=5000)
-    log("preroll %d steps in %.1f s, last step %s" % (args.preroll, time.perf_counter() - t0, pre))
-    pw = fast.step(args.warmup) if args.warmup else None
-    log("warmup", pw)
     # Autotuner: each candidate tuning timed over a few steps from this state, which it restores.
     autotune = None
     if args.autotune_steps > 0:
         t0 = time.perf_counter()
-        chosen, tms = fast.autotune(trial_steps=args.autotune_steps, first_iteration=args.preroll + args.warmup + 1)
+        chosen, tms = fast.autotune(trial_steps=args.autotune_steps, first_iteration=it0)
         autotune = {"trial_steps": args.autotune_steps, "chosen": chosen,
                     "ms_per_step": [None if np.isnan(x) else round(float(x), 3) for x in tms],
                     "candidates": "two-level on: check interval 8, 16, 32; two-level off: 8, 16, 32"}
         log("autotune in %.1f s: %s" % (time.perf_counter() - t0, autotune))
+    # The state every arm starts from: positions, velocities and the impulse cache.
+    ck = fast.checkpoint()
     q_snap, v_snap = fast.state()
+    cache = fast.last_contacts()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     fast.profile_enable(True)
     fast.profile_read(reset=True)
@@ -614,7 +762,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     # NVTX range "timed": lets a profiler select the timed launches (--nvtx-include "timed/").
     torch.cuda.nvtx.range_push("timed")
-    ms, contacts = timed_steps(fast, torch, stream, args.steps, flush)
+    ms, contacts, recs = timed_steps(fast, torch, stream, args.steps, flush, it0)
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     if ws > 1:
@@ -628,75 +776,66 @@ def run_ours(args):
         total_ms = float(t.item())
     csteps = int(sum(contacts))
     value = csteps * ws / (total_ms / 1e3)
-    log("fast: %d contact-steps in %.1f ms; per step ms %s; profile %s" % (csteps, total_ms, [round(x, 2) for x in ms],
-                                                                         prof))
-    # Roofline of the dominant kernel (the Gauss-Seidel solve): algorithmic bytes per
-    # launch over its CUDA-event duration.
-    hbm, peak_kind = peaks()
-    gl = max(prof["gs_launches"], 1)
-    bytes_per_launch = gs_bytes(prof) / gl
-    gs_ms_per_launch = prof["gs_ms"] / gl
-    achieved = bytes_per_launch / (gs_ms_per_launch / 1e3) / 1e9 if gs_ms_per_launch > 0 else 0.0
-    # DRAM traffic per launch: the ratio of DRAM bytes to algorithmic bytes from one ncu
-    # capture of the same kernel on a smaller case, scaled to this launch's algorithmic bytes.
-    two_level = prof.get("two_level_solves", 0) >= prof["gs_launches"] > 0
-    if two_level:
-        kname = "k_gs_patch (two-level FP32 sweeps: patches on shared memory, boundary contacts over the grid)"
-    elif args.precision == 1:
-        kname = "k_gs_mixed (cooperative FP32 sweeps, FP64 checks and refinement)"
-    else:
-        kname = "k_gs (cooperative coloured block Gauss-Seidel)"
-    traffic = None
-    tp = os.path.join(HERE, "profiles", "k_gs_patch_traffic.txt" if two_level else "k_gs_mixed_traffic.txt")
-    if os.path.exists(tp) and args.precision == 1:
-        for line in open(tp):
-            if line.startswith("dram_bytes_per_algorithmic_byte"):
-                traffic = float(line.split()[1]) * bytes_per_launch
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": kname,
-                "bytes_per_launch": bytes_per_launch, "ms_per_launch": gs_ms_per_launch,
-                "gs_share_of_step": prof["gs_ms"] / total_ms if total_ms else None}
+    convergence = convergence_record(recs)
+    log("fast: %d contact-steps in %.1f ms; per step ms %s; %s; profile %s" % (
+        csteps, total_ms, [round(x, 2) for x in ms], convergence, prof))
+    roofline, stages = headline_roofline(prof, total_ms, args)
 
-    # Plain FP64 GPU solver (cold start) on the same state.
-    plain = None
+    def arm(**over):
+        c = _lib.Context(device=local, **solver_kw(s))
+        c.restore(ck)
+        c.reconfigure(**over)
+        c.profile_enable(True)
+        c.profile_read(reset=True)
+        return c
+
+    # Plain FP64 Gauss-Seidel from the same state: with the impulse cache, then cold (one step,
+    # a larger sweep cap).
+    plain = plain_cold = None
     if args.plain_steps > 0:
-        pctx = _lib.Context(device=local, cache_mode=_lib.CACHE_NONE, precision=_lib.PRECISION_FP64, **solver_kw(s))
-        pctx.upload_ball2d(q_snap, v_snap, s["r"], s["m"], s["plane_x"], s["plane_n"])
-        pstream = torch.cuda.ExternalStream(pctx.stream_ptr(), device=local)
-        pms, pc = timed_steps(pctx, torch, pstream, args.plain_steps, flush)
+        pctx = arm(precision=_lib.PRECISION_FP64)
+        pms, pc, precs = timed_steps(pctx, torch, torch.cuda.ExternalStream(pctx.stream_ptr(), device=local),
+                                     args.plain_steps, flush, it0)
         pst = pctx.profile_read()
         plain = {"value": sum(pc) / (sum(pms) / 1e3), "unit": UNIT, "steps": args.plain_steps,
-                 "ms_per_step": sum(pms) / len(pms),
-                 "gs_iterations_per_step": (pst["contact_sweeps"] + pst["contact_sweeps32"]) / max(sum(pc), 1)}
-        log("plain:", plain)
+                 "ms_per_step": sum(pms) / len(pms), "convergence": convergence_record(precs),
+                 "form": "FP64 sweeps, warm start from the impulse cache, same state and steps"}
+        log("plain FP64 (cache):", plain)
         pctx.close()
+    if args.cold_steps > 0:
+        cctx = arm(precision=_lib.PRECISION_FP64, cache_mode=_lib.CACHE_NONE, max_iters=args.cold_iters)
+        cms, cc, crecs = timed_steps(cctx, torch, torch.cuda.ExternalStream(cctx.stream_ptr(), device=local),
+                                     args.cold_steps, flush, it0)
+        plain_cold = {"value": sum(cc) / (sum(cms) / 1e3), "unit": UNIT, "steps": args.cold_steps,
+                      "ms_per_step": sum(cms) / len(cms), "max_iters": args.cold_iters,
+                      "convergence": convergence_record(crecs),
+                      "form": "FP64 sweeps, cold start (no impulse cache), sweep cap %d, same state" %
+                              args.cold_iters}
+        log("plain FP64 (cold):", plain_cold)
+        cctx.close()
 
-    # e2e through sg_flow with pinned host buffers.
+    # e2e through sg_flow with pinned host buffers, from the same state and impulse cache.
     e2e = None
     if args.e2e_steps > 0:
-        ectx = _lib.Context(device=local, cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision,
-                            **solver_kw(s))
-        ectx.upload_ball2d(q_snap, v_snap, s["r"], s["m"], s["plane_x"], s["plane_n"])
+        ectx = arm()
         bufs = [torch.empty(2 * nb, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
         bufs[0][:] = q_snap
         bufs[1][:] = v_snap
-        it = 1
-        for _ in range(args.warmup):
-            ectx.flow(it, bufs[0], bufs[1], bufs[2], bufs[3])
-            bufs = [bufs[2], bufs[3], bufs[0], bufs[1]]
-            it += 1
+        it = it0
         torch.cuda.synchronize()
-        ec = 0
+        ec, econv, eerr = 0, 0, 0.0
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             _, _, st = ectx.flow(it, bufs[0], bufs[1], bufs[2], bufs[3])
             bufs = [bufs[2], bufs[3], bufs[0], bufs[1]]
             ec += st["n_contacts"]
+            econv += int(st["succeeded"])
+            eerr = max(eerr, st["error"])
             it += 1
         el = time.perf_counter() - t0
         e2e = {"value": ec / el, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * nb, "d2h_bytes_per_step": 2 * 16 * nb,
-               "steps": args.e2e_steps, "api": "sg_flow (ImpactFrictionMap::flow), pinned host q/v"}
+               "steps": args.e2e_steps, "steps_converged": econv, "max_residual": eerr,
+               "api": "sg_flow (ImpactFrictionMap::flow), pinned host q/v, from the timed steps' state and cache"}
         log("e2e:", e2e)
         ectx.close()
 
@@ -720,26 +859,31 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
-        v, desc, cores = cpu_sample(args, args.cpu_steps)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+        v, desc, crecs = cpu_from_state(s, q_snap, v_snap, cache, args.cpu_steps, it0)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
         log("cpu:", cpu)
 
     if rank == 0:
+        timed0 = it0
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == 0 else "f32+f64",
                 "data": "synthetic (seeded dense-pile fill, no dataset)",
-                "config": {"workload": "ball2d_dense_pile_%d" % nb, "discs": nb, "box": [40, 60], "dt": s["dt"], "mu": s["mu"],
-                           "CoR": s["CoR"], "tol": 1e-6, "max_iters": 5000, "form": "warm start (cache)",
-                           "preroll_steps": args.preroll, "timed_steps": [args.preroll + args.warmup + 1,
-                                                                           args.preroll + args.warmup + args.steps],
-                           "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1
-                           else "single GPU"},
+                "config": {"workload": "ball2d_dense_pile_%d" % nb, "discs": nb, "box": [40, 60], "dt": s["dt"],
+                           "mu": s["mu"], "CoR": s["CoR"], "tol": 1e-6, "max_iters": 5000,
+                           "form": "warm start (impulse cache), FP32 sweeps + FP64 residual and refinement",
+                           "pile": pile_note(pile), "timed_steps": [timed0, timed0 + args.steps - 1],
+                           "l2": "flushed between timed steps (256 MB write)",
+                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "convergence": convergence, "pile": pile,
                 "contacts_per_step": csteps / args.steps,
                 "gs_iterations_per_step": (prof["contact_sweeps"] + prof["contact_sweeps32"]) / max(csteps, 1),
                 "fp32_sweep_share": prof["contact_sweeps32"] / max(prof["contact_sweeps"] + prof["contact_sweeps32"], 1),
+                "fp64_start_solves": prof["fp64_start_solves"], "stage_ms_per_step": stages,
                 "plain_fp64_gpu": plain,
                 "warm_over_plain": (value / ws) / plain["value"] if plain else None,
+                "plain_fp64_cold_gpu": plain_cold,
+                "warm_over_plain_cold": (value / ws) / plain_cold["value"] if plain_cold else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": prof["kernel_launches"], "autotune": autotune, "batched": batched,
                 "spheres": spheres, "sphere_batch": sphere_batch, "learned": learned}
@@ -758,9 +902,15 @@ def main():
     ap.add_argument("--autotune-steps", type=int, default=2, help="steps per autotuner candidate (0 = off)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=262144)
-    ap.add_argument("--preroll", type=int, default=600)
-    ap.add_argument("--preroll-iters", type=int, default=50)
-    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--schedule", default="600:50,300:200,200:1000",
+                    help="pre-roll phases steps:sweep cap of the pile (untimed)")
+    ap.add_argument("--settle-converged", type=int, default=10,
+                    help="settling ends after this many consecutive converged steps at the full settings")
+    ap.add_argument("--settle-max", type=int, default=200, help="settling steps at most")
+    ap.add_argument("--preroll-iters", type=int, default=50, help="sweep cap of the other legs' pre-rolls")
+    ap.add_argument("--plain-steps", type=int, default=5)
+    ap.add_argument("--cold-steps", type=int, default=1)
+    ap.add_argument("--cold-iters", type=int, default=20000)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--precision", type=int, default=1, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")

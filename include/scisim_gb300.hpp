@@ -140,42 +140,102 @@ class Sobogus final : public FrictionSolver {
   unsigned evalEvery() const { return m_eval_every; }
   Precision precision() const { return m_precision; }
   int device() const { return m_device; }
+  // The context of the last solve (null before the first): sg_last_solve_order reads its order.
+  sg_ctx* context() const { return m_ctx; }
 
   // FrictionSolver::solve for Ball2D contacts on host buffers: masses m (nb), v0 (2nb), contact
   // bodies ia/ib (ib = -1 for a static plane), bases (4 per contact, column-major [n t]),
-  // per-contact CoR and mu; alpha, beta are the warm start and receive the impulses; v2 and f
-  // (2nb) the post-impact velocity and the generalised impulse.  Returns solve_succeeded.
+  // per-contact CoR and mu; the map's extra relative velocities nrel_extra and drel_extra (one
+  // each per contact, or empty for zero: Sobogus::solve adds them to the kinematic relative
+  // velocities, Sobogus.cpp:892-904); alpha, beta are the warm start and receive the impulses; v2
+  // and f (2nb) the post-impact velocity and the generalised friction impulse.  Returns
+  // solve_succeeded.
   bool solve(const std::vector<double>& m, const std::vector<double>& v0, const std::vector<int32_t>& ia,
              const std::vector<int32_t>& ib, const std::vector<double>& bases, const std::vector<double>& CoR,
-             const std::vector<double>& mu, unsigned max_iters, double tol, std::vector<double>& alpha,
+             const std::vector<double>& mu, const std::vector<double>& nrel_extra,
+             const std::vector<double>& drel_extra, unsigned max_iters, double tol, std::vector<double>& alpha,
              std::vector<double>& beta, std::vector<double>& v2, std::vector<double>& f, double& error,
              unsigned& iterations) {
     if (m_type != SobogusSolverType::Balls2D) throw Error(SG_BAD_INPUT, "Sobogus::solve takes Balls2D contacts");
     const size_t nb = m.size(), nc = ia.size();
     if (v0.size() != 2 * nb || ib.size() != nc || bases.size() != 4 * nc || CoR.size() != nc || mu.size() != nc ||
-        alpha.size() != nc || beta.size() != nc)
+        alpha.size() != nc || beta.size() != nc || (!nrel_extra.empty() && nrel_extra.size() != nc) ||
+        (!drel_extra.empty() && drel_extra.size() != nc))
       throw Error(SG_BAD_INPUT, "Sobogus::solve: inconsistent sizes");
-    if (!m_ctx) {
-      sg_config c{};
-      c.integrator = SG_SYMPLECTIC_EULER;
-      c.precision = static_cast<int32_t>(m_precision);
-      c.device = m_device;
-      c.dt = 1.0;
-      c.tol = tol;
-      c.max_iters = max_iters;
-      c.eval_every = m_eval_every;
-      check(sg_ctx_create(&c, &m_ctx), "sg_ctx_create");
-    }
+    ensure_ctx(SG_SYMPLECTIC_EULER, tol, max_iters);
     v2.assign(2 * nb, 0.0);
     f.assign(2 * nb, 0.0);
     uint32_t its = 0;
-    const bool ok = check(sg_sobogus_solve_2d(m_ctx, static_cast<int32_t>(nb), m.data(), v0.data(),
-                                              static_cast<int32_t>(nc), ia.data(), ib.data(), bases.data(),
-                                              CoR.data(), mu.data(), max_iters, tol, m_eval_every, alpha.data(),
-                                              beta.data(), v2.data(), f.data(), &error, &its),
-                          "sg_sobogus_solve_2d");
+    const bool ok = check(sg_sobogus_solve_2d_ex(m_ctx, static_cast<int32_t>(nb), m.data(), v0.data(),
+                                                 static_cast<int32_t>(nc), ia.data(), ib.data(), bases.data(),
+                                                 CoR.data(), mu.data(), nrel_extra.empty() ? nullptr : nrel_extra.data(),
+                                                 drel_extra.empty() ? nullptr : drel_extra.data(), max_iters, tol,
+                                                 m_eval_every, alpha.data(), beta.data(), v2.data(), f.data(), &error,
+                                                 &its),
+                          "sg_sobogus_solve_2d_ex");
     iterations = its;
     return ok;
+  }
+
+  // The geometric map's call: no extra relative velocities (GeometricImpactFrictionMap.cpp:344).
+  bool solve(const std::vector<double>& m, const std::vector<double>& v0, const std::vector<int32_t>& ia,
+             const std::vector<int32_t>& ib, const std::vector<double>& bases, const std::vector<double>& CoR,
+             const std::vector<double>& mu, unsigned max_iters, double tol, std::vector<double>& alpha,
+             std::vector<double>& beta, std::vector<double>& v2, std::vector<double>& f, double& error,
+             unsigned& iterations) {
+    return solve(m, v0, ia, ib, bases, CoR, mu, {}, {}, max_iters, tol, alpha, beta, v2, f, error, iterations);
+  }
+
+  // FrictionSolver::solve for RigidBody3D sphere contacts (SobogusSolverType::RigidBodies3D,
+  // Sobogus.cpp:184-251,486-567) on host buffers: masses m (nb), world inertia Iw and its inverse
+  // Iinv (9 per body, row-major: the angular blocks of M and Minv), v0 (6nb, [v | omega]);
+  // contacts ia/ib, bases (9 per contact, column-major [n s t]), arms arm_a / arm_b (3 per contact:
+  // Constraint::getWorldSpaceContactPoint minus the body's centre), CoR, mu, nrel_extra (nc) and
+  // drel_extra (2nc) or empty; alpha (nc) and beta (2nc) in = warm start, out = impulses; v2 and f
+  // (6nb).  Returns solve_succeeded.
+  bool solve3D(const std::vector<double>& m, const std::vector<double>& Iw, const std::vector<double>& Iinv,
+               const std::vector<double>& v0, const std::vector<int32_t>& ia, const std::vector<int32_t>& ib,
+               const std::vector<double>& bases, const std::vector<double>& arm_a, const std::vector<double>& arm_b,
+               const std::vector<double>& CoR, const std::vector<double>& mu, const std::vector<double>& nrel_extra,
+               const std::vector<double>& drel_extra, unsigned max_iters, double tol, std::vector<double>& alpha,
+               std::vector<double>& beta, std::vector<double>& v2, std::vector<double>& f, double& error,
+               unsigned& iterations) {
+    if (m_type != SobogusSolverType::RigidBodies3D)
+      throw Error(SG_BAD_INPUT, "Sobogus::solve3D takes RigidBodies3D contacts");
+    const size_t nb = m.size(), nc = ia.size();
+    if (Iw.size() != 9 * nb || Iinv.size() != 9 * nb || v0.size() != 6 * nb || ib.size() != nc ||
+        bases.size() != 9 * nc || arm_a.size() != 3 * nc || arm_b.size() != 3 * nc || CoR.size() != nc ||
+        mu.size() != nc || alpha.size() != nc || beta.size() != 2 * nc ||
+        (!nrel_extra.empty() && nrel_extra.size() != nc) || (!drel_extra.empty() && drel_extra.size() != 2 * nc))
+      throw Error(SG_BAD_INPUT, "Sobogus::solve3D: inconsistent sizes");
+    ensure_ctx(SG_SPLIT_HAM, tol, max_iters);
+    v2.assign(6 * nb, 0.0);
+    f.assign(6 * nb, 0.0);
+    uint32_t its = 0;
+    const bool ok = check(sg_sobogus_solve_3d(m_ctx, static_cast<int32_t>(nb), m.data(), Iw.data(), Iinv.data(),
+                                              v0.data(), static_cast<int32_t>(nc), ia.data(), ib.data(),
+                                              bases.data(), arm_a.data(), arm_b.data(), CoR.data(), mu.data(),
+                                              nrel_extra.empty() ? nullptr : nrel_extra.data(),
+                                              drel_extra.empty() ? nullptr : drel_extra.data(), max_iters, tol,
+                                              m_eval_every, alpha.data(), beta.data(), v2.data(), f.data(), &error,
+                                              &its),
+                          "sg_sobogus_solve_3d");
+    iterations = its;
+    return ok;
+  }
+
+ private:
+  void ensure_ctx(int32_t integrator, double tol, unsigned max_iters) {
+    if (m_ctx) return;
+    sg_config c{};
+    c.integrator = integrator;
+    c.precision = static_cast<int32_t>(m_precision);
+    c.device = m_device;
+    c.dt = 1.0;
+    c.tol = tol;
+    c.max_iters = max_iters;
+    c.eval_every = m_eval_every;
+    check(sg_ctx_create(&c, &m_ctx), "sg_ctx_create");
   }
 
  private:

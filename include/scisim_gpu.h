@@ -114,6 +114,34 @@ SG_API int sg_sphere3d_upload(sg_ctx* ctx, int32_t nb, const double* q, const do
                               const double* m, const double* I0, int32_t np, const double* plane_x,
                               const double* plane_n);
 
+/* Uploads a RigidBody2D scene of circles (replaces RigidBody2DState setup with CircleGeometry bodies:
+ * rigidbody2d/RigidBody2DState.cpp, rigidbody2d/CircleGeometry.cpp; StaticPlane as the rigidbody2d
+ * scene parser stores it, rigidbody2dutils/RigidBody2DSceneParser.cpp:271-277).  q, v: 3 per body
+ * ([x y theta], [vx vy omega], RigidBody2DState's layout); r, m, I: per body (mass and moment of
+ * inertia; Minv = diag(1/m, 1/m, 1/I)); plane_x, plane_n: 2 per plane (normals are normalised
+ * here).  sg_step and sg_flow then step it with GeometricImpactFrictionMap::flow
+ * (scisim/ConstrainedMaps/GeometricImpactFrictionMap.cpp:267-442) or, after
+ * sg_set_staggering(SG_STAGGER_STABILIZED), StabilizedImpactFrictionMap::flow
+ * (scisim/ConstrainedMaps/StabilizedImpactFrictionMap.cpp:48-167): the context's integrator
+ * (SG_SYMPLECTIC_EULER or SG_VERLET, rigidbody2d/SymplecticEulerMap.cpp, VerletMap.cpp), the
+ * active set of RigidBody2DSim (rigidbody2d/RigidBody2DSim.cpp:248-312,638-714: swept-AABB grid,
+ * CCD, planes on the predictor), and Sobogus with SobogusSolverType::RigidBody2D
+ * (scisim/ConstrainedMaps/Sobogus.cpp:110-182,375-484) in FP64 sweeps (the context's precision
+ * does not apply).  Clears the impulse cache.  Checkpoints and the autotuner do not take
+ * RigidBody2D scenes. */
+SG_API int sg_rigidbody2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r,
+                                 const double* m, const double* I, int32_t np, const double* plane_x,
+                                 const double* plane_n);
+
+/* Contacts of the last RigidBody2D step in active-set order (RigidBody2DSim::computeActiveSet,
+ * rigidbody2d/RigidBody2DSim.cpp:696-714): ia, ib (ib = -1 - plane), n (2 per contact), ta, tb
+ * (the tangent row's angular entries cross(arm_a, t), cross(arm_b, t) of CircleCircleConstraint /
+ * StaticPlaneCircleConstraint::evalH; tb = 0 for a plane), alpha, beta (Sobogus.cpp:421-437).  Any
+ * output may be NULL.  Returns the contact count, -(count+1) if cap is too small, INT64_MIN when
+ * the context holds no RigidBody2D scene. */
+SG_API int64_t sg_rigidbody2d_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* n,
+                                            double* ta, double* tb, double* alpha, double* beta);
+
 /* Uploads S independent sphere scenes stepped together (no counterpart in the reference, whose
  * driver steps one RigidBody3DSim).  Scene s owns bodies body_off[s] .. body_off[s+1]-1 and planes
  * plane_off[s] .. plane_off[s+1]-1 and has its own mu[s] and CoR[s]; q: [x (3N) | R (9N)],
@@ -216,6 +244,40 @@ SG_API int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const d
                         double* alpha, double* beta, double* v2, double* f, double* error,
                         uint32_t* iterations);
 
+/* FrictionSolver::solve for Ball2D with all of its inputs (scisim/ConstrainedMaps/FrictionSolver.h:28):
+ * sg_sobogus_solve_2d plus the impact-friction map's extra relative velocities nrel_extra and
+ * drel_extra (one each per contact; NULL = zero), which Sobogus::solve adds to the kinematic
+ * relative velocities before forming the forcing terms (scisim/ConstrainedMaps/Sobogus.cpp:892-904;
+ * SymplecticEulerImpactFrictionMap passes N^T vdelta and D^T vdelta there,
+ * scisim/ConstrainedMaps/SymplecticEulerImpactFrictionMap.cpp:293-329).  With both NULL it is
+ * sg_sobogus_solve_2d bit for bit. */
+SG_API int sg_sobogus_solve_2d_ex(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc,
+                                  const int32_t* ia, const int32_t* ib, const double* bases, const double* CoR,
+                                  const double* mu, const double* nrel_extra, const double* drel_extra,
+                                  uint32_t max_iters, double tol, uint32_t eval_every, double* alpha, double* beta,
+                                  double* v2, double* f, double* error, uint32_t* iterations);
+
+/* FrictionSolver::solve for RigidBody3D spheres (Sobogus::solve with SobogusSolverType::RigidBodies3D:
+ * scisim/ConstrainedMaps/Sobogus.cpp:184-251 (initialize3D), :486-567 (solve3D);
+ * scisim/ConstrainedMaps/bogus/RigidBody3DSobogusInterface.cpp:31-145) on host buffers.
+ * Bodies: m (nb masses), Iw and Iinv (9 per body, row-major world inertia and its inverse: the
+ * angular blocks of RigidBody3DState's M and Minv), v0 (6nb, [v (3nb) | omega (3nb)]).
+ * Contacts: ia, ib (ib = -1 for a static plane); bases (9 per contact, column-major [n s t],
+ * right-handed orthonormal); arm_a, arm_b (3 per contact: the world contact point minus the
+ * body's centre, Constraint::getWorldSpaceContactPoint; arm_b is ignored for planes); the
+ * normal row carries no torque (sphere contacts: SphereSphereConstraint::evalH,
+ * rigidbody3d/Constraints/SphereSphereConstraint.cpp:254-265, asserts |arm x n| <= 1e-6, as this
+ * entry does); CoR, mu (per contact); nrel_extra (nc) and drel_extra (2nc, [s t] per contact),
+ * NULL = zero; alpha (nc) and beta (2nc) in = warm start, out = result; v2, f (6nb) outputs
+ * (f: the friction impulse and its torque, Sobogus.cpp:533-567).  Returns SG_NOT_CONVERGED when the
+ * solve hit max_iters, SG_BAD_INPUT for invalid indices, bases or arms. */
+SG_API int sg_sobogus_solve_3d(sg_ctx* ctx, int32_t nb, const double* m, const double* Iw, const double* Iinv,
+                               const double* v0, int32_t nc, const int32_t* ia, const int32_t* ib,
+                               const double* bases, const double* arm_a, const double* arm_b, const double* CoR,
+                               const double* mu, const double* nrel_extra, const double* drel_extra,
+                               uint32_t max_iters, double tol, uint32_t eval_every, double* alpha, double* beta,
+                               double* v2, double* f, double* error, uint32_t* iterations);
+
 /* The FrictionSolver solve above for callers that cannot allocate GPU memory: code
  * that runs inside another runtime's memory pool, in a real-time loop, or under a
  * policy that forbids device allocation after start-up.  It has no counterpart in the
@@ -224,12 +286,18 @@ SG_API int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const d
  * is a cudaStream_t (NULL = default stream).  No context is needed and nothing is
  * allocated: all scratch lives in one fixed static device array of about 8.1 MB that
  * every GPU loading the library keeps until the process exits.  Limits: at most
- * 16,384 bodies and 65,536 contacts; larger problems return SG_CAPACITY.  The first
- * call on a device looks up that array's device address (cudaGetSymbolAddress), so
- * make the first call on each device before any stream capture.  All calls share the
- * array: calls that overlap on the GPU (other streams, other host threads) race and
- * must be serialised by the caller.  Returns as sg_sobogus_solve_2d; invalid contact
- * indices or tangents give SG_BAD_INPUT before any solve work. */
+ * 16,384 bodies and 65,536 contacts; larger problems return SG_CAPACITY.  The array's
+ * device address is looked up (cudaGetSymbolAddress) on the first call in each context
+ * of a device -- again after the device's context was re-created, e.g. by
+ * cudaDeviceReset -- so make the first call on each device before any stream capture.
+ * The device is the calling thread's current device, and stream must belong to it.  The
+ * call synchronises stream before it returns (it reads the device-side input check and
+ * the solve statistics), so it cannot be made while stream is being captured.  All
+ * calls share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  The solve takes no extra
+ * relative velocities (those of sg_sobogus_solve_2d_ex are zero here).  Returns as
+ * sg_sobogus_solve_2d; invalid contact indices or tangents give SG_BAD_INPUT before
+ * any solve work. */
 SG_API int sg_sobogus_solve_2d_noalloc(int32_t nb, const double* m, const double* v0, int32_t nc,
                                        const int32_t* ia, const int32_t* ib, const double* bases,
                                        const double* CoR, const double* mu, uint32_t max_iters, double tol,
@@ -309,6 +377,13 @@ typedef struct {
   double patch_interior_max_ms; /* the slowest block's patch-interior time, summed over solves */
   int64_t patch_slowest_block;  /* that block (= its patch) in the last two-level solve */
   uint64_t patch_contacts_staged; /* per-patch contact capacity staged in shared memory, summed */
+  uint64_t fp64_start_solves;  /* FP32-form solves whose start was already within 10 tol of the
+                                  tolerance and were swept in FP64 from the first sweep */
+  /* Single-scene Ball2D steps: CUDA-event time of each stage, summed: [0] predictor and grid,
+   * [1] pair counting (grid scan, CCD) and plane flags, [2] contact writes and assembly,
+   * [3] adjacency and colouring, [4] start check, two-level partition and FP32 packing, [5] the
+   * Gauss-Seidel kernel, [6] final velocity, [7] impulse extraction, cache and final map. */
+  double stage_ms[8];
 } sg_profile;
 
 SG_API int sg_profile_enable(sg_ctx* ctx, int32_t on);
@@ -355,7 +430,10 @@ typedef struct {
   int32_t two_level;
   int32_t check_interval;
   int32_t two_level_min_contacts;
-  int32_t reserved;
+  int32_t fp64_factor;  /* FP32 form: FP64 sweeps from the first sweep when the start's FP64 residual is
+                           below fp64_factor tol (a few one-level sweeps first, then FP64 sweeps on
+                           the two-level partition), and from the first FP64 check at or below it
+                           (default 100; 0 keeps FP32 sweeps until their rounding floor) */
 } sg_tuning;
 
 SG_API int sg_get_tuning(sg_ctx* ctx, sg_tuning* tuning);

@@ -555,6 +555,22 @@ extern "C" void or_ball2d_set_solver(or_ball2d* s, double tol, uint32_t max_iter
   s->p.max_iters = max_iters;
 }
 
+// Replaces the impulse cache (ConstraintCache, ball2d/ConstraintCache.cpp:20-120) with the given contacts'
+// impulses: ia, ib as the step's contacts (ib = -1 - plane for a static plane), alpha, beta.  Used to
+// start the oracle from another solver's state, impulse cache included.
+extern "C" void or_ball2d_set_cache(or_ball2d* s, int64_t nc, const int32_t* ia, const int32_t* ib, const double* alpha,
+                                    const double* beta) {
+  s->cache_bb.clear();
+  s->cache_pb.clear();
+  for (int64_t k = 0; k < nc; ++k) {
+    Contact c{};
+    c.a = ia[k];
+    c.b = ib[k];
+    auto& cache = c.b >= 0 ? s->cache_bb : s->cache_pb;
+    cache[cache_key(c)] = {alpha[k], beta[k]};
+  }
+}
+
 extern "C" void or_ball2d_set_next_order(or_ball2d* s, int64_t nc, const int32_t* order) {
   s->next_order.assign(order, order + nc);
 }

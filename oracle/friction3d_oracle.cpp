@@ -334,3 +334,14 @@ extern "C" double or_residual_3d(int nb, const double* m, const double* Iinv, co
   return solve3d_impl(nb, m, Iinv, Iw, v0, nc, ia, ib, bases, arm_a, arm_b, CoR, mu, nullptr, a.data(), b.data(),
                       nullptr, nullptr, nullptr, true);
 }
+
+// The residual with the map's extra relative velocities folded into the forcing terms.
+extern "C" double or_residual_3d_ex(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0,
+                                    int nc, const int32_t* ia, const int32_t* ib, const double* bases,
+                                    const double* arm_a, const double* arm_b, const double* CoR, const double* mu,
+                                    const double* nrel, const double* drel, const double* alpha,
+                                    const double* beta) {
+  std::vector<double> a(alpha, alpha + nc), b(beta, beta + 2 * nc);
+  return solve3d_impl(nb, m, Iinv, Iw, v0, nc, ia, ib, bases, arm_a, arm_b, CoR, mu, nullptr, a.data(), b.data(),
+                      nullptr, nullptr, nullptr, true, nrel, drel);
+}

@@ -382,6 +382,16 @@ extern "C" double or_residual_2d(int nb, const double* m, const double* v0, int 
                       true);
 }
 
+// The residual with the map's extra relative velocities folded into the forcing terms.
+extern "C" double or_residual_2d_ex(int nb, const double* m, const double* v0, int nc, const int32_t* ia,
+                                    const int32_t* ib, const double* bases, const double* CoR, const double* mu,
+                                    const double* nrel, const double* drel, const double* alpha,
+                                    const double* beta) {
+  std::vector<double> a(alpha, alpha + nc), b(beta, beta + nc);
+  return solve2d_impl(nb, m, v0, nc, ia, ib, bases, CoR, mu, nullptr, a.data(), b.data(), nullptr, nullptr, nullptr,
+                      true, nrel, drel);
+}
+
 static double solve2d_impl(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
                            const double* bases, const double* CoR, const double* mu, const or_gs_params* p,
                            double* alpha, double* beta, double* v2, double* f, or_gs_result* res, bool eval_only,

@@ -82,6 +82,11 @@ double or_residual_2d(int nb, const double* m, const double* v0, int nc, const i
                       const double* bases, const double* CoR, const double* mu, const double* alpha,
                       const double* beta);
 
+// The same with the map's extra relative velocities (nrel, drel per contact; null = zero).
+double or_residual_2d_ex(int nb, const double* m, const double* v0, int nc, const int32_t* ia, const int32_t* ib,
+                         const double* bases, const double* CoR, const double* mu, const double* nrel,
+                         const double* drel, const double* alpha, const double* beta);
+
 // ---------------------------------------------------------------- Ball2D scene
 typedef struct or_ball2d or_ball2d;
 
@@ -128,6 +133,9 @@ void or_ball2d_set_state(or_ball2d* s, const double* q, const double* v);
 // Sweep order for the next step's solve only (a permutation of its nc contacts, e.g.
 // the GPU's colour order); ignored if the contact count differs.
 void or_ball2d_set_next_order(or_ball2d* s, int64_t nc, const int32_t* order);
+// Replaces the impulse cache with the given contacts' impulses (ib = -1 - plane for a plane).
+void or_ball2d_set_cache(or_ball2d* s, int64_t nc, const int32_t* ia, const int32_t* ib, const double* alpha,
+                         const double* beta);
 // New solver tolerance and iteration cap (scene and impulse cache kept).
 void or_ball2d_set_solver(or_ball2d* s, double tol, uint32_t max_iters);
 // Contacts of the last step: ia, ib (ib=-1-plane_idx for planes), n (2 per contact), alpha, beta.
@@ -159,6 +167,11 @@ double or_residual_3d(int nb, const double* m, const double* Iinv, const double*
                       const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
                       const double* arm_b, const double* CoR, const double* mu, const double* alpha,
                       const double* beta);
+// The same with the map's extra relative velocities (nrel: 1, drel: 2 per contact; null = zero).
+double or_residual_3d_ex(int nb, const double* m, const double* Iinv, const double* Iw, const double* v0, int nc,
+                         const int32_t* ia, const int32_t* ib, const double* bases, const double* arm_a,
+                         const double* arm_b, const double* CoR, const double* mu, const double* nrel,
+                         const double* drel, const double* alpha, const double* beta);
 
 // RigidBodySphere::computeMassAndInertia (RigidBodySphere.cpp:10-18): mass and principal inertia.
 void or_sphere_mass_inertia(double r, double density, double* M, double* I);

@@ -87,6 +87,8 @@ def lib():
         L.or_local_solve.argtypes = [C.c_int, _dp, _dp, C.c_double, _dp]
         L.or_sobogus_solve_2d.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp,
                                           C.POINTER(GsParams), _dp, _dp, _dp, _dp, C.POINTER(GsResult)]
+        L.or_sobogus_solve_2d_ex.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp,
+                                             C.POINTER(GsParams), _dp, _dp, _dp, _dp, C.POINTER(GsResult)]
         L.or_ball2d_create.restype = C.c_void_p
         L.or_ball2d_create.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp,
                                        C.POINTER(Ball2DParams)]
@@ -104,9 +106,12 @@ def lib():
         L.or_ball2d_active_set.argtypes = [C.c_void_p, _dp, _dp, i64, _ip, _ip]
         L.or_ball2d_umap.argtypes = [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp]
         L.or_ball2d_set_next_order.argtypes = [C.c_void_p, C.c_int64, _ip]
+        L.or_ball2d_set_cache.argtypes = [C.c_void_p, C.c_int64, _ip, _ip, _dp, _dp]
         L.or_ball2d_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_uint32]
         L.or_residual_2d.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
         L.or_residual_2d.restype = C.c_double
+        L.or_residual_2d_ex.argtypes = [C.c_int, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.or_residual_2d_ex.restype = C.c_double
         L.or_mlp_param_count.restype = C.c_int
         L.or_mlp_forward.argtypes = [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), _dp]
         L.or_mlp_loss_grad.argtypes = [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), _dp]
@@ -114,9 +119,15 @@ def lib():
         L.or_sobogus_solve_3d.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp,
                                           _dp, _dp, C.POINTER(GsParams), _dp, _dp, _dp, _dp,
                                           C.POINTER(GsResult)]
+        L.or_sobogus_solve_3d_ex.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp,
+                                             _dp, _dp, _dp, _dp, C.POINTER(GsParams), _dp, _dp, _dp, _dp,
+                                             C.POINTER(GsResult)]
         L.or_residual_3d.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp,
                                      _dp, _dp, _dp]
         L.or_residual_3d.restype = C.c_double
+        L.or_residual_3d_ex.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp,
+                                        _dp, _dp, _dp, _dp, _dp]
+        L.or_residual_3d_ex.restype = C.c_double
         L.or_sphere_mass_inertia.argtypes = [C.c_double, C.c_double, _dp, _dp]
         L.or_sphere3d_create.restype = C.c_void_p
         L.or_sphere3d_create.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp,
@@ -226,8 +237,9 @@ def local_solve(dim, W, b, mu):
 
 
 def sobogus_solve_2d(m, v0, ia, ib, bases, CoR, mu, tol, max_iters, eval_every=1, alpha=None,
-                     beta=None, order=None):
-    """Ball2D FrictionSolver::solve.  Returns dict(alpha, beta, v2, f, error, iterations, succeeded)."""
+                     beta=None, order=None, nrel_extra=None, drel_extra=None):
+    """Ball2D FrictionSolver::solve (with the map's extra relative velocities nrel_extra, drel_extra,
+    one per contact, when given).  Returns dict(alpha, beta, v2, f, error, iterations, succeeded)."""
     m, v0, bases = f64(m), f64(v0), f64(bases)
     ia, ib = i32(ia), i32(ib)
     nc = ia.shape[0]
@@ -241,20 +253,34 @@ def sobogus_solve_2d(m, v0, ia, ib, bases, CoR, mu, tol, max_iters, eval_every=1
     order_arr = None if order is None else i32(order)
     gp = GsParams(tol, max_iters, eval_every, _i(order_arr) if order_arr is not None else None)
     gr = GsResult()
-    lib().or_sobogus_solve_2d(nb, _d(m), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(CoR), _d(mu),
-                              C.byref(gp), _d(alpha), _d(beta), _d(v2), _d(f), C.byref(gr))
+    if nrel_extra is None and drel_extra is None:
+        lib().or_sobogus_solve_2d(nb, _d(m), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(CoR), _d(mu),
+                                  C.byref(gp), _d(alpha), _d(beta), _d(v2), _d(f), C.byref(gr))
+    else:
+        nr = None if nrel_extra is None else f64(nrel_extra)
+        dr = None if drel_extra is None else f64(drel_extra)
+        lib().or_sobogus_solve_2d_ex(nb, _d(m), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(CoR), _d(mu),
+                                     _d(nr) if nr is not None else None, _d(dr) if dr is not None else None,
+                                     C.byref(gp), _d(alpha), _d(beta), _d(v2), _d(f), C.byref(gr))
     return dict(alpha=alpha, beta=beta, v2=v2, f=f, error=gr.error, iterations=gr.iterations,
                 succeeded=bool(gr.succeeded))
 
 
-def residual_2d(m, v0, ia, ib, bases, CoR, mu, alpha, beta):
-    """The solver's Coulomb residual of given impulses (alpha, beta)."""
+def residual_2d(m, v0, ia, ib, bases, CoR, mu, alpha, beta, nrel_extra=None, drel_extra=None):
+    """The solver's Coulomb residual of given impulses (alpha, beta), with the map's extra relative
+    velocities folded into the forcing terms when given."""
     m, v0, bases = f64(m), f64(v0), f64(bases)
     ia, ib = i32(ia), i32(ib)
     nc = ia.shape[0]
     CoR = f64(np.broadcast_to(CoR, (nc,)))
     mu = f64(np.broadcast_to(mu, (nc,)))
     a, b = f64(alpha), f64(beta)
+    if nrel_extra is not None or drel_extra is not None:
+        nr = None if nrel_extra is None else f64(nrel_extra)
+        dr = None if drel_extra is None else f64(drel_extra)
+        return lib().or_residual_2d_ex(m.shape[0], _d(m), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(CoR), _d(mu),
+                                       _d(nr) if nr is not None else None, _d(dr) if dr is not None else None,
+                                       _d(a), _d(b))
     return lib().or_residual_2d(m.shape[0], _d(m), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(CoR), _d(mu),
                                 _d(a), _d(b))
 
@@ -308,6 +334,11 @@ class Ball2D:
         q, v = f64(q), f64(v)
         lib().or_ball2d_set_state(self._h, _d(q), _d(v))
 
+    def set_cache(self, ia, ib, alpha, beta):
+        """Replaces the impulse cache with the given contacts' impulses (ib = -1 - plane)."""
+        ia, ib, a, b = i32(ia), i32(ib), f64(alpha), f64(beta)
+        lib().or_ball2d_set_cache(self._h, ia.shape[0], _i(ia), _i(ib), _d(a), _d(b))
+
     def set_solver(self, tol, max_iters):
         lib().or_ball2d_set_solver(self._h, tol, max_iters)
 
@@ -357,8 +388,10 @@ def sphere_mass_inertia(r, density):
 
 
 def sobogus_solve_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, tol, max_iters, eval_every=1,
-                     alpha=None, beta=None, order=None):
-    """RigidBodies3D FrictionSolver::solve.  Returns dict(alpha, beta, v2, f, error, iterations, succeeded)."""
+                     alpha=None, beta=None, order=None, nrel_extra=None, drel_extra=None):
+    """RigidBodies3D FrictionSolver::solve (with the map's extra relative velocities nrel_extra (1 per
+    contact) and drel_extra (2 per contact) when given).  Returns dict(alpha, beta, v2, f, error,
+    iterations, succeeded)."""
     m, Iinv, Iw, v0 = f64(m), f64(Iinv), f64(Iw), f64(v0)
     bases, arm_a, arm_b = f64(bases), f64(arm_a), f64(arm_b)
     ia, ib = i32(ia), i32(ib)
@@ -371,15 +404,25 @@ def sobogus_solve_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, tol,
     order_arr = None if order is None else i32(order)
     gp = GsParams(tol, max_iters, eval_every, _i(order_arr) if order_arr is not None else None)
     gr = GsResult()
-    lib().or_sobogus_solve_3d(nb, _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(arm_a),
-                              _d(arm_b), _d(CoR), _d(mu), C.byref(gp), _d(alpha), _d(beta), _d(v2), _d(f),
-                              C.byref(gr))
+    if nrel_extra is None and drel_extra is None:
+        lib().or_sobogus_solve_3d(nb, _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases), _d(arm_a),
+                                  _d(arm_b), _d(CoR), _d(mu), C.byref(gp), _d(alpha), _d(beta), _d(v2), _d(f),
+                                  C.byref(gr))
+    else:
+        nr = None if nrel_extra is None else f64(nrel_extra)
+        dr = None if drel_extra is None else f64(drel_extra)
+        lib().or_sobogus_solve_3d_ex(nb, _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases),
+                                     _d(arm_a), _d(arm_b), _d(CoR), _d(mu), _d(nr) if nr is not None else None,
+                                     _d(dr) if dr is not None else None, C.byref(gp), _d(alpha), _d(beta),
+                                     _d(v2), _d(f), C.byref(gr))
     return dict(alpha=alpha, beta=beta, v2=v2, f=f, error=gr.error, iterations=gr.iterations,
                 succeeded=bool(gr.succeeded))
 
 
-def residual_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, alpha, beta):
-    """The 3D solver's Coulomb residual of given impulses (alpha, beta)."""
+def residual_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, alpha, beta, nrel_extra=None,
+                drel_extra=None):
+    """The 3D solver's Coulomb residual of given impulses (alpha, beta), with the map's extra relative
+    velocities folded into the forcing terms when given."""
     m, Iinv, Iw, v0 = f64(m), f64(Iinv), f64(Iw), f64(v0)
     bases, arm_a, arm_b = f64(bases), f64(arm_a), f64(arm_b)
     ia, ib = i32(ia), i32(ib)
@@ -387,6 +430,12 @@ def residual_3d(m, Iinv, Iw, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, alpha, be
     CoR = f64(np.broadcast_to(CoR, (nc,)))
     mu = f64(np.broadcast_to(mu, (nc,)))
     a, b = f64(alpha), f64(beta)
+    if nrel_extra is not None or drel_extra is not None:
+        nr = None if nrel_extra is None else f64(nrel_extra)
+        dr = None if drel_extra is None else f64(drel_extra)
+        return lib().or_residual_3d_ex(m.shape[0], _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases),
+                                       _d(arm_a), _d(arm_b), _d(CoR), _d(mu), _d(nr) if nr is not None else None,
+                                       _d(dr) if dr is not None else None, _d(a), _d(b))
     return lib().or_residual_3d(m.shape[0], _d(m), _d(Iinv), _d(Iw), _d(v0), nc, _i(ia), _i(ib), _d(bases),
                                 _d(arm_a), _d(arm_b), _d(CoR), _d(mu), _d(a), _d(b))
 

@@ -44,7 +44,7 @@ class SgStepStats(C.Structure):
 
 class SgTuning(C.Structure):
     _fields_ = [("two_level", C.c_int32), ("check_interval", C.c_int32), ("two_level_min_contacts", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("fp64_factor", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -57,7 +57,8 @@ class SgProfile(C.Structure):
                 ("body_lifts", C.c_uint64), ("two_level_solves", C.c_uint64), ("patch_interior_ms", C.c_double),
                 ("patch_wait_ms", C.c_double), ("patch_boundary_ms", C.c_double), ("boundary_contacts", C.c_uint64),
                 ("boundary_colors", C.c_uint64), ("patch_interior_max_ms", C.c_double),
-                ("patch_slowest_block", C.c_int64), ("patch_contacts_staged", C.c_uint64)]
+                ("patch_slowest_block", C.c_int64), ("patch_contacts_staged", C.c_uint64),
+                ("fp64_start_solves", C.c_uint64), ("stage_ms", C.c_double * 8)]
 
 
 class SgError(RuntimeError):
@@ -78,6 +79,8 @@ SIGNATURES = {
     "sg_batch2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _ip, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
     "sg_batch2d_scene_stats": (C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_uint32), _dp, _ip]),
     "sg_batch2d_set_capacity": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_rigidbody2d_upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp]),
+    "sg_rigidbody2d_last_contacts": (_i64, [C.c_void_p, _i64, _ip, _ip, _dp, _dp, _dp, _dp, _dp]),
     "sg_sphere3d_batch_upload": (C.c_int, [C.c_void_p, C.c_int32, _ip, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp,
                                            _dp]),
     "sg_step": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(SgStepStats), C.POINTER(_i64)]),
@@ -89,6 +92,12 @@ SIGNATURES = {
     "sg_last_solve_order": (_i64, [C.c_void_p, _i64, _ip, _ip, _ip]),
     "sg_sobogus_solve_2d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, C.c_int32, _ip, _ip, _dp, _dp, _dp,
                                       C.c_uint32, C.c_double, C.c_uint32, _dp, _dp, _dp, _dp, _dp,
+                                      C.POINTER(C.c_uint32)]),
+    "sg_sobogus_solve_2d_ex": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, C.c_int32, _ip, _ip, _dp, _dp, _dp, _dp,
+                                         _dp, C.c_uint32, C.c_double, C.c_uint32, _dp, _dp, _dp, _dp, _dp,
+                                         C.POINTER(C.c_uint32)]),
+    "sg_sobogus_solve_3d": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp, C.c_int32, _ip, _ip, _dp, _dp, _dp,
+                                      _dp, _dp, _dp, _dp, C.c_uint32, C.c_double, C.c_uint32, _dp, _dp, _dp, _dp, _dp,
                                       C.POINTER(C.c_uint32)]),
     "sg_sobogus_solve_2d_noalloc": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_double,
@@ -209,6 +218,7 @@ class Context:
         self._h = h
         self.nb = 0
         self.dim = 2
+        self.rb2d = False
 
     @property
     def handle(self):
@@ -243,6 +253,7 @@ class Context:
         px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
         self.nb = r.shape[0]
         self.dim = 2
+        self.rb2d = False
         self._keep = (q, v, r, m, px, pn)
         check(lib().sg_ball2d_upload(self._h, self.nb, dptr(q), dptr(v), dptr(r), dptr(m), px.shape[0] // 2,
                                      dptr(px), dptr(pn)), "sg_ball2d_upload")
@@ -258,6 +269,7 @@ class Context:
             raise ValueError("inconsistent batch sizes")
         self.nb = r.shape[0]
         self.dim = 2
+        self.rb2d = False
         self.n_scenes = S
         self._keep = (bo, po, q, v, r, m, px, pn, mu, CoR)
         check(lib().sg_batch2d_upload(self._h, S, iptr(bo), dptr(q), dptr(v), dptr(r), dptr(m), iptr(po), dptr(px),
@@ -277,6 +289,7 @@ class Context:
             raise ValueError("inconsistent batch sizes")
         self.nb = N
         self.dim = 3
+        self.rb2d = False
         self.n_scenes = S
         self._keep = (bo, po, q, v, r, m, I0, px, pn, mu, CoR)
         check(lib().sg_sphere3d_batch_upload(self._h, S, iptr(bo), dptr(q), dptr(v), dptr(r), dptr(m), dptr(I0),
@@ -294,6 +307,33 @@ class Context:
                                            iptr(ok)), "sg_batch2d_scene_stats")
         return dict(n_contacts=nc, iterations=it, error=err, succeeded=ok.astype(bool))
 
+    def upload_rigidbody2d(self, q, v, r, m, I, plane_x, plane_n):
+        """RigidBody2D circles: q, v 3 per body ([x y theta], [vx vy omega]), r, m, I per body."""
+        q, v, r, m, I = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1), f64(I).reshape(-1)
+        px, pn = f64(plane_x).reshape(-1), f64(plane_n).reshape(-1)
+        nb = r.shape[0]
+        if q.shape[0] != 3 * nb or v.shape[0] != 3 * nb or m.shape[0] != nb or I.shape[0] != nb:
+            raise ValueError("inconsistent RigidBody2D state sizes")
+        self.nb = nb
+        self.dim = 2
+        self.rb2d = True
+        self._keep = (q, v, r, m, I, px, pn)
+        check(lib().sg_rigidbody2d_upload(self._h, nb, dptr(q), dptr(v), dptr(r), dptr(m), dptr(I),
+                                          px.shape[0] // 2, dptr(px), dptr(pn)), "sg_rigidbody2d_upload")
+
+    def rigidbody2d_last_contacts(self):
+        L = lib()
+        nc = L.sg_rigidbody2d_last_contacts(self._h, 0, None, None, None, None, None, None, None)
+        nc = -nc - 1 if nc < 0 else nc
+        ia, ib = np.empty(nc, np.int32), np.empty(nc, np.int32)
+        n, ta, tb = np.empty(2 * nc), np.empty(nc), np.empty(nc)
+        a, b = np.empty(nc), np.empty(nc)
+        got = L.sg_rigidbody2d_last_contacts(self._h, nc, iptr(ia), iptr(ib), dptr(n), dptr(ta), dptr(tb), dptr(a),
+                                              dptr(b))
+        if got != nc:
+            raise SgError(SG_BAD_INPUT, "sg_rigidbody2d_last_contacts")
+        return dict(ia=ia, ib=ib, n=n.reshape(-1, 2), ta=ta, tb=tb, alpha=a, beta=b)
+
     def upload_sphere3d(self, q, v, r, m, I0, plane_x, plane_n):
         """RigidBody3D spheres: q 12nb [x | R row-major], v 6nb [v | omega], r, m, I0 (3 per body)."""
         q, v, r, m = f64(q).reshape(-1), f64(v).reshape(-1), f64(r).reshape(-1), f64(m).reshape(-1)
@@ -304,6 +344,7 @@ class Context:
             raise ValueError("inconsistent RigidBody3D state sizes")
         self.nb = nb
         self.dim = 3
+        self.rb2d = False
         self._keep = (q, v, r, m, I0, px, pn)
         check(lib().sg_sphere3d_upload(self._h, nb, dptr(q), dptr(v), dptr(r), dptr(m), dptr(I0), px.shape[0] // 3,
                                        dptr(px), dptr(pn)), "sg_sphere3d_upload")
@@ -329,8 +370,8 @@ class Context:
         return q1, v1, d
 
     def state(self):
-        q = np.empty((12 if self.dim == 3 else 2) * self.nb)
-        v = np.empty((6 if self.dim == 3 else 2) * self.nb)
+        q = np.empty((12 if self.dim == 3 else 3 if self.rb2d else 2) * self.nb)
+        v = np.empty((6 if self.dim == 3 else 3 if self.rb2d else 2) * self.nb)
         check(lib().sg_download_state(self._h, dptr(q), dptr(v)), "sg_download_state")
         return q, v
 
@@ -425,7 +466,9 @@ class Context:
     def profile_read(self, reset=False):
         p = SgProfile()
         check(lib().sg_profile_read(self._h, C.byref(p), 1 if reset else 0), "sg_profile_read")
-        return {k: getattr(p, k) for k, _ in p._fields_}
+        d = {k: getattr(p, k) for k, _ in p._fields_}
+        d["stage_ms"] = list(p.stage_ms)
+        return d
 
     def set_two_level(self, on=True):
         check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
@@ -500,7 +543,9 @@ class Context:
 
     # -- standalone entry points ----------------------------------------------
     def sobogus_solve_2d(self, m, v0, ia, ib, bases, CoR, mu, tol, max_iters, eval_every=1, alpha=None,
-                         beta=None):
+                         beta=None, nrel_extra=None, drel_extra=None):
+        """FrictionSolver::solve for Ball2D (sg_sobogus_solve_2d; with nrel_extra / drel_extra, one per
+        contact, sg_sobogus_solve_2d_ex)."""
         m, v0, bases = f64(m), f64(v0), f64(bases)
         ia, ib = i32(ia), i32(ib)
         nc, nb = ia.shape[0], m.shape[0]
@@ -511,10 +556,51 @@ class Context:
         v2, f = np.zeros(2 * nb), np.zeros(2 * nb)
         err = C.c_double(0.0)
         its = C.c_uint32(0)
-        s = check(lib().sg_sobogus_solve_2d(self._h, nb, dptr(m), dptr(v0), nc, iptr(ia), iptr(ib), dptr(bases),
-                                            dptr(CoR), dptr(mu), max_iters, tol, eval_every, dptr(alpha),
-                                            dptr(beta), dptr(v2), dptr(f), C.byref(err), C.byref(its)),
-                  "sg_sobogus_solve_2d")
+        if nrel_extra is None and drel_extra is None:
+            s = check(lib().sg_sobogus_solve_2d(self._h, nb, dptr(m), dptr(v0), nc, iptr(ia), iptr(ib), dptr(bases),
+                                                dptr(CoR), dptr(mu), max_iters, tol, eval_every, dptr(alpha),
+                                                dptr(beta), dptr(v2), dptr(f), C.byref(err), C.byref(its)),
+                      "sg_sobogus_solve_2d")
+        else:
+            nr = None if nrel_extra is None else f64(nrel_extra).reshape(-1)
+            dr = None if drel_extra is None else f64(drel_extra).reshape(-1)
+            if (nr is not None and nr.shape[0] != nc) or (dr is not None and dr.shape[0] != nc):
+                raise ValueError("nrel_extra and drel_extra take one value per contact")
+            s = check(lib().sg_sobogus_solve_2d_ex(self._h, nb, dptr(m), dptr(v0), nc, iptr(ia), iptr(ib),
+                                                   dptr(bases), dptr(CoR), dptr(mu), dptr(nr) if nr is not None
+                                                   else None, dptr(dr) if dr is not None else None, max_iters, tol,
+                                                   eval_every, dptr(alpha), dptr(beta), dptr(v2), dptr(f),
+                                                   C.byref(err), C.byref(its)), "sg_sobogus_solve_2d_ex")
+        return dict(alpha=alpha, beta=beta, v2=v2, f=f, error=err.value, iterations=its.value,
+                    succeeded=(s == SG_OK))
+
+    def sobogus_solve_3d(self, m, Iw, Iinv, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, tol, max_iters, eval_every=1,
+                         alpha=None, beta=None, nrel_extra=None, drel_extra=None):
+        """FrictionSolver::solve for RigidBody3D spheres (sg_sobogus_solve_3d): m (nb), Iw, Iinv (9 per body),
+        v0 (6nb, [v | omega]); bases (9 per contact, column-major [n s t]), arms (3 per contact)."""
+        m, Iw, Iinv, v0 = f64(m), f64(Iw).reshape(-1), f64(Iinv).reshape(-1), f64(v0).reshape(-1)
+        bases, arm_a, arm_b = f64(bases).reshape(-1), f64(arm_a).reshape(-1), f64(arm_b).reshape(-1)
+        ia, ib = i32(ia), i32(ib)
+        nc, nb = ia.shape[0], m.shape[0]
+        CoR = f64(np.broadcast_to(CoR, (nc,)))
+        mu = f64(np.broadcast_to(mu, (nc,)))
+        alpha = np.zeros(nc) if alpha is None else f64(alpha).copy()
+        beta = np.zeros(2 * nc) if beta is None else f64(beta).reshape(-1).copy()
+        nr = None if nrel_extra is None else f64(nrel_extra).reshape(-1)
+        dr = None if drel_extra is None else f64(drel_extra).reshape(-1)
+        if (Iw.shape[0] != 9 * nb or Iinv.shape[0] != 9 * nb or v0.shape[0] != 6 * nb or bases.shape[0] != 9 * nc or
+                arm_a.shape[0] != 3 * nc or arm_b.shape[0] != 3 * nc or beta.shape[0] != 2 * nc or
+                (nr is not None and nr.shape[0] != nc) or (dr is not None and dr.shape[0] != 2 * nc)):
+            raise ValueError("inconsistent RigidBody3D solve sizes")
+        v2, f = np.zeros(6 * nb), np.zeros(6 * nb)
+        err = C.c_double(0.0)
+        its = C.c_uint32(0)
+        s = check(lib().sg_sobogus_solve_3d(self._h, nb, dptr(m), dptr(Iw), dptr(Iinv), dptr(v0), nc, iptr(ia),
+                                            iptr(ib), dptr(bases), dptr(arm_a), dptr(arm_b), dptr(CoR), dptr(mu),
+                                            dptr(nr) if nr is not None else None,
+                                            dptr(dr) if dr is not None else None, max_iters, tol, eval_every,
+                                            dptr(alpha), dptr(beta), dptr(v2), dptr(f), C.byref(err),
+                                            C.byref(its)), "sg_sobogus_solve_3d")
         return dict(alpha=alpha, beta=beta, v2=v2, f=f, error=err.value, iterations=its.value,
                     succeeded=(s == SG_OK))
 

@@ -35,7 +35,7 @@ void release(Buf& b) {
 
 static constexpr unsigned long long kDefaultSpin = 1ull << 22;  // ~1 s of L2 polls
 
-static int ensure_contact_capacity(sg_ctx* ctx, int64_t nc) {
+int ensure_contact_capacity(sg_ctx* ctx, int64_t nc) {
   if (nc <= ctx->ccap && ctx->ia.p) return SG_OK;
   const int64_t cap = std::max<int64_t>(nc + nc / 4 + 64, 1024);
   const size_t c = (size_t)cap;
@@ -69,6 +69,26 @@ static int validate_config(const sg_config* c) {
 }
 
 // One geometric impact-friction step on the device-resident scene.
+// Closes the stage timing of a profiled step: the end mark, then each recorded mark's interval to
+// the next recorded one into stage_ms.
+static int finish_stage_timing(sg_ctx* ctx) {
+  if (!ctx->stage_timing) return SG_OK;
+  stage_mark(ctx, sg_ctx::kStageMarks - 1);
+  ctx->stage_timing = false;
+  SG_CUDA_TRY(cudaEventSynchronize(ctx->ev_stage[sg_ctx::kStageMarks - 1]));
+  int prev = -1;
+  for (int k = 0; k < sg_ctx::kStageMarks; ++k) {
+    if (!(ctx->stage_mask & (1u << k))) continue;
+    if (prev >= 0) {
+      float ms = 0.f;
+      SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_stage[prev], ctx->ev_stage[k]));
+      ctx->stage_ms[prev] += ms;
+    }
+    prev = k;
+  }
+  return SG_OK;
+}
+
 static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   const int nb = ctx->nb;
   cudaStream_t s = ctx->stream;
@@ -85,12 +105,17 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     if (out) *out = st;
     return SG_OK;
   }
+  ctx->stage_timing = ctx->profile && ctx->ev_stage[0];
+  ctx->stage_mask = 0;
+  stage_mark(ctx, 0);
   // Predictor + swept AABBs (GeometricImpactFrictionMap.cpp:279, Ball2DSim.cpp:566-572).
   if (int r = ball2d_predict_and_bounds(ctx)) return r;
   const double* aabb = ctx->aabb.as<double>();
   if (int r = broadphase_build_grid(ctx, aabb, nb)) return r;
+  stage_mark(ctx, 1);
   if (int r = broadphase_count_pairs(ctx, aabb, nb, true)) return r;
   if (int r = plane_flags(ctx)) return r;
+  stage_mark(ctx, 2);
   int totals[2] = {0, 0};
   SG_CUDA_TRY(cudaMemcpyAsync(&totals[0], ctx->pair_off.as<int>() + nb, sizeof(int), cudaMemcpyDeviceToHost, s));
   SG_CUDA_TRY(cudaMemcpyAsync(&totals[1], ctx->plane_off.as<int>() + (long)nb * ctx->np, sizeof(int),
@@ -115,6 +140,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->v, ctx->v1);
     ctx->prev_n = 0;
     st.succeeded = 1;
+    if (int r = finish_stage_timing(ctx)) return r;
     if (out) *out = st;
     return SG_OK;
   }
@@ -122,6 +148,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   if (int r = broadphase_write_pairs(ctx, aabb, nb, true, ctx->ia.as<int>(), ctx->ib.as<int>())) return r;
   if (int r = plane_write(ctx, npairs)) return r;
   if (int r = assemble_contacts(ctx, nc)) return r;
+  stage_mark(ctx, 3);
   if (int r = grow(ctx->v2, sizeof(double) * 2 * (size_t)nb)) return r;
   ContactProblem P;
   P.nb = nb;
@@ -162,6 +189,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   ctx->kernel_launches += 2 + (ctx->np > 0 ? 1 : 0) + 1 + 1;  // write pairs, assemble, plane write, extract, final map
   std::swap(ctx->q, ctx->q1);
   std::swap(ctx->v, ctx->v1);
+  if (int r = finish_stage_timing(ctx)) return r;
   if (out) *out = st;
   return sr;
 }
@@ -212,7 +240,7 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32, &ctx->pk3, &ctx->Iinv32, &ctx->pt_setup,
                   &ctx->pt_patch, &ctx->pt_lidx, &ctx->pt_body, &ctx->pt_cnt, &ctx->pt_start, &ctx->pt_fill,
                   &ctx->pt_key, &ctx->pt_kcnt, &ctx->pt_kstart, &ctx->pt_kfill, &ctx->pt_order, &ctx->pt_max,
-                  &ctx->pt_bcolor, &ctx->pt_rem, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
+                  &ctx->pt_bcolor, &ctx->pt_rem, &ctx->start_slot, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
                   &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill,
                   &ctx->pt_cflag, &ctx->pt_cpos, &ctx->pt_cbody, &ctx->pt_hist, &ctx->pt_pref,
                   &ctx->pt_cuts, &ctx->pt_maps};
@@ -234,11 +262,14 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                  &ctx->plane_off, &ctx->scan_tmp, &ctx->ia, &ctx->ib, &ctx->n, &ctx->c, &ctx->W, &ctx->mu,
                  &ctx->r_loc, &ctx->r_cand, &ctx->r_best, &ctx->key, &ctx->ab, &ctx->prev_key, &ctx->prev_ab,
                  &ctx->color, &ctx->perm, &ctx->body_cnt, &ctx->body_off, &ctx->body_fill, &ctx->body_adj,
-                 &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2};
+                 &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2,
+                 &ctx->fs_I, &ctx->fs_in};
   for (Buf* b : bufs) release(*b);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->ev_gs0) cudaEventDestroy(ctx->ev_gs0);
   if (ctx->ev_gs1) cudaEventDestroy(ctx->ev_gs1);
+  for (cudaEvent_t e : ctx->ev_stage)
+    if (e) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -269,6 +300,7 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
     }
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
   ctx->dim = 2;
+  ctx->rb2d = false;
   ctx->n_scenes = 0;
   if (ctx->graph) {
     cudaGraphExecDestroy(ctx->graph);
@@ -318,6 +350,101 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
   return SG_OK;
 }
 
+int sg_rigidbody2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
+                          const double* I, int32_t np, const double* plane_x, const double* plane_n) {
+  if (!ctx || nb < 0 || np < 0 || (nb > 0 && (!q || !v || !r || !m || !I)) || (np > 0 && (!plane_x || !plane_n))) {
+    set_error("sg_rigidbody2d_upload: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  for (int i = 0; i < nb; ++i)
+    if (!(r[i] > 0.0) || !(m[i] > 0.0) || !(I[i] > 0.0)) {
+      set_error("sg_rigidbody2d_upload: radii, masses and moments of inertia must be positive");
+      return SG_BAD_INPUT;
+    }
+  if (ctx->cfg.integrator == SG_SPLIT_HAM) {
+    set_error("sg_rigidbody2d_upload: RigidBody2D scenes step with SG_SYMPLECTIC_EULER or SG_VERLET");
+    return SG_BAD_INPUT;
+  }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  ctx->dim = 2;
+  ctx->rb2d = true;
+  ctx->n_scenes = 0;
+  if (ctx->graph) {
+    cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  ctx->nb = nb;
+  ctx->np = np;
+  const size_t n1 = (size_t)std::max(nb, 1);
+  // RigidBody2DState's Minv: 1 / m (x, y), 1 / I (theta).
+  std::vector<double> minv(nb), Iinv(nb);
+  for (int i = 0; i < nb; ++i) {
+    minv[i] = 1.0 / m[i];
+    Iinv[i] = 1.0 / I[i];
+  }
+  std::vector<double> pn(2 * (size_t)np), pt(2 * (size_t)np);
+  for (int p = 0; p < np; ++p) {
+    // The scene parser stores n.normalized() (rigidbody2dutils/RigidBody2DSceneParser.cpp:271-277); t = (-n_y, n_x).
+    double nx = plane_n[2 * p], ny = plane_n[2 * p + 1];
+    const double z = nx * nx + ny * ny;
+    if (!(z > 0.0)) {
+      set_error("sg_rigidbody2d_upload: zero plane normal");
+      return SG_BAD_INPUT;
+    }
+    const double sq = std::sqrt(z);
+    nx = nx / sq;
+    ny = ny / sq;
+    pn[2 * p] = nx;
+    pn[2 * p + 1] = ny;
+    pt[2 * p] = -ny;
+    pt[2 * p + 1] = nx;
+  }
+  if (int e = upload(ctx, ctx->q, q, sizeof(double) * 3 * nb)) return e;
+  if (int e = upload(ctx, ctx->v, v, sizeof(double) * 3 * nb)) return e;
+  if (int e = upload(ctx, ctx->r, r, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->m, m, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->minv, minv.data(), sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->rb_I, I, sizeof(double) * nb)) return e;
+  if (int e = upload(ctx, ctx->rb_Iinv, Iinv.data(), sizeof(double) * nb)) return e;
+  if (int e = grow(ctx->q1, sizeof(double) * 3 * n1)) return e;
+  if (int e = grow(ctx->v1, sizeof(double) * 3 * n1)) return e;
+  if (int e = grow(ctx->v2, sizeof(double) * 3 * n1)) return e;
+  if (int e = grow(ctx->pos0, sizeof(double) * 2 * n1)) return e;
+  if (int e = grow(ctx->pos1, sizeof(double) * 2 * n1)) return e;
+  if (int e = grow(ctx->aabb, sizeof(double) * 4 * n1)) return e;
+  if (int e = upload(ctx, ctx->plane_x, plane_x, sizeof(double) * 2 * np)) return e;
+  if (int e = upload(ctx, ctx->plane_n, pn.data(), sizeof(double) * 2 * np)) return e;
+  if (int e = upload(ctx, ctx->plane_t, pt.data(), sizeof(double) * 2 * np)) return e;
+  if (int e = grow(ctx->plane_x, 16)) return e;
+  if (int e = grow(ctx->plane_n, 16)) return e;
+  if (int e = grow(ctx->plane_t, 16)) return e;
+  ctx->prev_n = 0;
+  ctx->last_nc = 0;
+  SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int64_t sg_rigidbody2d_last_contacts(sg_ctx* ctx, int64_t cap, int32_t* ia, int32_t* ib, double* n, double* ta,
+                                     double* tb, double* alpha, double* beta) {
+  if (!ctx) return SG_BAD_INPUT;
+  if (!ctx->rb2d) {
+    set_error("sg_rigidbody2d_last_contacts: the context holds no RigidBody2D scene");
+    return INT64_MIN;
+  }
+  const int64_t nc = sg_last_contacts(ctx, cap, ia, ib, n, alpha, beta);
+  if (nc <= 0 || (!ta && !tb)) return nc;
+  std::vector<double> ct(2 * (size_t)nc);
+  if (cudaMemcpyAsync(ct.data(), ctx->rb_ct.p, sizeof(double) * 2 * (size_t)nc, cudaMemcpyDeviceToHost, ctx->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return -1;
+  for (int64_t k = 0; k < nc; ++k) {
+    if (ta) ta[k] = ct[2 * k];
+    if (tb) tb[k] = ct[2 * k + 1];
+  }
+  return nc;
+}
+
 static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const double* v, const double* r, const double* m,
                          const double* I0, int32_t np, const double* plane_x, const double* plane_n) {
   if (!ctx || nb < 0 || np < 0 || (nb > 0 && (!q || !v || !r || !m || !I0)) || (np > 0 && (!plane_x || !plane_n))) {
@@ -343,6 +470,7 @@ static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const 
   }
   SG_CUDA_TRY(cudaSetDevice(ctx->device));
   ctx->dim = 3;
+  ctx->rb2d = false;
   ctx->n_scenes = 0;
   ctx->nb = nb;
   ctx->np = np;
@@ -581,8 +709,8 @@ static int check_integrator(const sg_ctx* ctx) {
   return SG_OK;
 }
 
-static size_t q_doubles(const sg_ctx* ctx) { return (size_t)ctx->nb * (ctx->dim == 3 ? 12 : 2); }
-static size_t v_doubles(const sg_ctx* ctx) { return (size_t)ctx->nb * (ctx->dim == 3 ? 6 : 2); }
+static size_t q_doubles(const sg_ctx* ctx) { return (size_t)ctx->nb * (ctx->dim == 3 ? 12 : ctx->rb2d ? 3 : 2); }
+static size_t v_doubles(const sg_ctx* ctx) { return (size_t)ctx->nb * (ctx->dim == 3 ? 6 : ctx->rb2d ? 3 : 2); }
 
 int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_stats* stats, int64_t* total_contacts) {
   if (!ctx) return SG_BAD_INPUT;
@@ -595,7 +723,7 @@ int sg_step(sg_ctx* ctx, uint32_t first_iteration, uint32_t n_steps, sg_step_sta
   sg_step_stats st{};
   for (uint32_t k = 0; k < n_steps; ++k) {
     const int r = ctx->dim == 3 ? (ctx->n_scenes > 0 ? sphere3d_batch_step(ctx, &st) : sphere3d_step(ctx, &st))
-                                : step_once(ctx, &st);
+                                : ctx->rb2d ? rb2d_step(ctx, &st) : step_once(ctx, &st);
     if (r != SG_OK && r != SG_NOT_CONVERGED) return r;
     if (r == SG_NOT_CONVERGED) worst = r;
     tot += st.n_contacts;
@@ -811,10 +939,15 @@ int64_t sg_last_solve_order(sg_ctx* ctx, int64_t cap, int32_t* order, int32_t* c
   return nc;
 }
 
-int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc, const int32_t* ia,
-                        const int32_t* ib, const double* bases, const double* CoR, const double* mu, uint32_t max_iters,
-                        double tol, uint32_t eval_every, double* alpha, double* beta, double* v2, double* f,
-                        double* error, uint32_t* iterations) {
+// FrictionSolver::solve for Ball2D on host buffers (sg_sobogus_solve_2d and its form with the map's extra
+// relative velocities).  nrel_extra / drel_extra (one per contact, null = zero) are added to the kinematic
+// relative velocities before the forcing terms are formed, as Sobogus::solve does
+// (scisim/ConstrainedMaps/Sobogus.cpp:892-904, then Constraint::computeForcingTerm, Constraint.cpp:27-33).
+static int sobogus_solve_2d_impl(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc,
+                                 const int32_t* ia, const int32_t* ib, const double* bases, const double* CoR,
+                                 const double* mu, const double* nrel_extra, const double* drel_extra,
+                                 uint32_t max_iters, double tol, uint32_t eval_every, double* alpha, double* beta,
+                                 double* v2, double* f, double* error, uint32_t* iterations) {
   if (!ctx || nb < 0 || nc < 0 || (nb > 0 && (!m || !v0 || !v2 || !f)) ||
       (nc > 0 && (!ia || !ib || !bases || !CoR || !mu || !alpha || !beta))) {
     set_error("sg_sobogus_solve_2d: invalid arguments");
@@ -846,8 +979,10 @@ int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const double* 
       vry = vry - 0.0;
     }
     const double ndotv = nx * vrx + ny * vry;
-    const double nrel = -(0.0 * nx + 0.0 * ny);
-    const double drel = -(0.0 * tx + 0.0 * ty);
+    double nrel = -(0.0 * nx + 0.0 * ny);
+    double drel = -(0.0 * tx + 0.0 * ty);
+    if (nrel_extra) nrel = nrel + nrel_extra[k];
+    if (drel_extra) drel = drel + drel_extra[k];
     const double sc = CoR[k] * ndotv + nrel;
     const double wx = (0.0 + nx * sc) + tx * drel;
     const double wy = (0.0 + ny * sc) + ty * drel;
@@ -928,6 +1063,33 @@ int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const double* 
   if (error) *error = (nc == 0) ? 0.0 : ctx->h_stats.error;
   if (iterations) *iterations = ctx->h_stats.iterations;
   return sr;
+}
+
+int sg_sobogus_solve_2d(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc, const int32_t* ia,
+                        const int32_t* ib, const double* bases, const double* CoR, const double* mu, uint32_t max_iters,
+                        double tol, uint32_t eval_every, double* alpha, double* beta, double* v2, double* f,
+                        double* error, uint32_t* iterations) {
+  return sobogus_solve_2d_impl(ctx, nb, m, v0, nc, ia, ib, bases, CoR, mu, nullptr, nullptr, max_iters, tol,
+                               eval_every, alpha, beta, v2, f, error, iterations);
+}
+
+int sg_sobogus_solve_2d_ex(sg_ctx* ctx, int32_t nb, const double* m, const double* v0, int32_t nc,
+                           const int32_t* ia, const int32_t* ib, const double* bases, const double* CoR,
+                           const double* mu, const double* nrel_extra, const double* drel_extra, uint32_t max_iters,
+                           double tol, uint32_t eval_every, double* alpha, double* beta, double* v2, double* f,
+                           double* error, uint32_t* iterations) {
+  return sobogus_solve_2d_impl(ctx, nb, m, v0, nc, ia, ib, bases, CoR, mu, nrel_extra, drel_extra, max_iters, tol,
+                               eval_every, alpha, beta, v2, f, error, iterations);
+}
+
+int sg_sobogus_solve_3d(sg_ctx* ctx, int32_t nb, const double* m, const double* Iw, const double* Iinv,
+                        const double* v0, int32_t nc, const int32_t* ia, const int32_t* ib, const double* bases,
+                        const double* arm_a, const double* arm_b, const double* CoR, const double* mu,
+                        const double* nrel_extra, const double* drel_extra, uint32_t max_iters, double tol,
+                        uint32_t eval_every, double* alpha, double* beta, double* v2, double* f, double* error,
+                        uint32_t* iterations) {
+  return sobogus_solve_3d(ctx, nb, m, Iw, Iinv, v0, nc, ia, ib, bases, arm_a, arm_b, CoR, mu, nrel_extra, drel_extra,
+                          max_iters, tol, eval_every, alpha, beta, v2, f, error, iterations);
 }
 
 int sg_broadphase_2d(sg_ctx* ctx, int32_t n, const double* aabb, int64_t cap, int32_t* pairs, int64_t* npairs) {
@@ -1067,7 +1229,7 @@ std::vector<CkptPart> ckpt_parts(sg_ctx* ctx, int dim, int nb, int np, int64_t p
   return v;
 }
 
-bool ckpt_supported(const sg_ctx* ctx) { return ctx->n_scenes == 0 && (ctx->dim == 2 || ctx->dim == 3); }
+bool ckpt_supported(const sg_ctx* ctx) { return ctx->n_scenes == 0 && !ctx->rb2d && (ctx->dim == 2 || ctx->dim == 3); }
 }  // namespace
 
 int64_t sg_checkpoint_size(sg_ctx* ctx) {
@@ -1199,18 +1361,20 @@ int sg_get_tuning(sg_ctx* ctx, sg_tuning* t) {
   t->two_level = ctx->patches ? 1 : 0;
   t->check_interval = ctx->check_interval;
   t->two_level_min_contacts = ctx->two_level_min_contacts;
-  t->reserved = 0;
+  t->fp64_factor = ctx->fp64_factor;
   return SG_OK;
 }
 
 int sg_set_tuning(sg_ctx* ctx, const sg_tuning* t) {
-  if (!ctx || !t || t->check_interval < 1 || t->check_interval > 4096 || t->two_level_min_contacts < 0) {
-    set_error("sg_set_tuning: check_interval in [1, 4096] and two_level_min_contacts >= 0");
+  if (!ctx || !t || t->check_interval < 1 || t->check_interval > 4096 || t->two_level_min_contacts < 0 ||
+      t->fp64_factor < 0) {
+    set_error("sg_set_tuning: check_interval in [1, 4096], two_level_min_contacts >= 0, fp64_factor >= 0");
     return SG_BAD_INPUT;
   }
   ctx->patches = t->two_level != 0;
   ctx->check_interval = t->check_interval;
   ctx->two_level_min_contacts = t->two_level_min_contacts;
+  ctx->fp64_factor = t->fp64_factor;
   return SG_OK;
 }
 
@@ -1292,6 +1456,7 @@ int sg_profile_enable(sg_ctx* ctx, int32_t on) {
   if (on && !ctx->ev_gs0) {
     SG_CUDA_TRY(cudaEventCreate(&ctx->ev_gs0));
     SG_CUDA_TRY(cudaEventCreate(&ctx->ev_gs1));
+    for (cudaEvent_t& e : ctx->ev_stage) SG_CUDA_TRY(cudaEventCreate(&e));
   }
   ctx->profile = on != 0;
   return SG_OK;
@@ -1318,8 +1483,12 @@ int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset) {
   out->patch_interior_max_ms = 1e-6 * (double)ctx->patch_interior_max_ns;
   out->patch_slowest_block = ctx->patch_slowest_block;
   out->patch_contacts_staged = ctx->patch_staged;
+  out->fp64_start_solves = ctx->fp64_start_solves;
+  for (int k = 0; k < 8; ++k) out->stage_ms[k] = ctx->stage_ms[k];
   if (reset) {
+    for (double& x : ctx->stage_ms) x = 0.0;
     ctx->patched_solves = 0;
+    ctx->fp64_start_solves = 0;
     ctx->patch_phase_ns[0] = ctx->patch_phase_ns[1] = ctx->patch_phase_ns[2] = 0;
     ctx->patch_boundary_contacts = ctx->patch_boundary_colors = 0;
     ctx->patch_interior_max_ns = 0;

@@ -861,8 +861,9 @@ static PairScan make_scan(sg_ctx* ctx, const double* aabb, bool ccd) {
   s.gp = ctx->grid.as<GridParams>();
   s.cell_start = ctx->cell_start.as<int>();
   s.sorted = ctx->sorted.as<int>();
-  s.q0 = ccd ? ctx->q.as<double2>() : nullptr;
-  s.q1 = ccd ? ctx->q1.as<double2>() : nullptr;
+  // RigidBody2D circles keep 3 entries per body: their CCD reads the centres the predictor copied out.
+  s.q0 = ccd ? (ctx->rb2d ? ctx->pos0.as<double2>() : ctx->q.as<double2>()) : nullptr;
+  s.q1 = ccd ? (ctx->rb2d ? ctx->pos1.as<double2>() : ctx->q1.as<double2>()) : nullptr;
   s.rad = ccd ? ctx->r.as<double>() : nullptr;
   return s;
 }
@@ -897,7 +898,8 @@ int plane_flags(sg_ctx* ctx) {
     SG_CUDA_TRY(cudaMemsetAsync(ctx->plane_off.p, 0, sizeof(int), ctx->stream));
     return SG_OK;
   }
-  k_plane_flags<<<blocks_for(t), kBlock, 0, ctx->stream>>>(ctx->nb, ctx->np, ctx->q1.as<double2>(), ctx->r.as<double>(),
+  const double2* q1 = ctx->rb2d ? ctx->pos1.as<double2>() : ctx->q1.as<double2>();
+  k_plane_flags<<<blocks_for(t), kBlock, 0, ctx->stream>>>(ctx->nb, ctx->np, q1, ctx->r.as<double>(),
                                                            ctx->plane_x.as<double2>(), ctx->plane_n.as<double2>(),
                                                            ctx->plane_flag.as<int>());
   SG_CUDA_TRY(cudaGetLastError());

@@ -130,6 +130,12 @@ struct sg_ctx {
   sg::Buf q, v, r, m, minv, q1, v1, v2;
   sg::Buf plane_x, plane_n, plane_t;
   sg::Buf I0, Iw, Iinv;  // 3D: principal inertia (3nb), world inertia and inverse (9nb, row-major)
+  // RigidBody2D circles (dim 2, rb2d): q, v hold 3 per body ([x y theta], [vx vy omega]); the moments
+  // of inertia and their inverses; the centres at the start and end of the predictor (the broad
+  // phase's CCD and the plane test read them as Ball2D positions); per contact the tangent row's
+  // angular entries cross(arm_a, t), cross(arm_b, t); running velocities (vx, vy, omega, 0).
+  bool rb2d = false;
+  sg::Buf rb_I, rb_Iinv, pos0, pos1, rb_ct, rb_vrun;
 
   // broad phase
   sg::Buf aabb, cell_of, cell_count, cell_start, cell_fill, sorted, pair_cnt, pair_off, grid;
@@ -165,7 +171,12 @@ struct sg_ctx {
   // and the contact count from which a single-scene FP32 solve uses the two-level sweeps.
   int check_interval = 16;
   int two_level_min_contacts = 20000;
+  // FP32 form: FP64 sweeps from the start when the start's residual is below fp64_factor tol, and
+  // from the first FP64 check at or below it.
+  int fp64_factor = 100;
   uint64_t patched_solves = 0;
+  uint64_t fp64_start_solves = 0;  // FP32-form solves swept in FP64 from the start (start near tol)
+  sg::Buf start_slot;              // the start's FP64 residual (ordered encoding)
   bool last_patched = false;  // the last FP32 solve ran the two-level sweeps
   int last_patch_P = 0, last_patch_Pb = 0;
   uint64_t patch_phase_ns[3] = {0, 0, 0};
@@ -205,6 +216,7 @@ struct sg_ctx {
   sg::Buf mlp_p, mlp_feat, mlp_tgt, mlp_x, mlp_t, mlp_slots, mlp_choice;
   // buffers of the standalone FrictionSolver entry (kept apart from the scene)
   sg::Buf fs_m, fs_minv, fs_v0, fs_v2;
+  sg::Buf fs_I, fs_in;  // sphere entry: world inertia and its inverse; packed per-contact inputs
 
   // host mirrors of the last step
   int64_t last_nc = 0, last_nbb = 0;
@@ -213,6 +225,15 @@ struct sg_ctx {
   // profiling counters (sg_profile_read)
   bool profile = false;
   cudaEvent_t ev_gs0 = nullptr, ev_gs1 = nullptr;
+  // Stage timers of the single-scene Ball2D step while profiling: marks 0..8 recorded on the stream
+  // (start, after predictor + grid, after pair counting + plane flags, after contact writes and
+  // assembly, after colouring, before and after the Gauss-Seidel kernel, after the final velocity,
+  // end of step); stage_ms[k] sums the time between mark k and the next recorded mark.
+  static constexpr int kStageMarks = 9;
+  cudaEvent_t ev_stage[kStageMarks] = {};
+  bool stage_timing = false;
+  unsigned stage_mask = 0;
+  double stage_ms[kStageMarks - 1] = {};
   double gs_ms = 0.0;
   uint64_t gs_launches = 0, contact_sweeps = 0, contact_evals = 0, kernel_launches = 0, steps = 0;
   uint64_t contact_sweeps32 = 0, contact_lifts = 0, body_lifts = 0;
@@ -248,6 +269,8 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp);
 // device, no host synchronisation (capturable).
 int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp, const BatchSolve& X);
 int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc);
+// Per-contact buffers of a single-scene 2D step for nc contacts (grown with slack).
+int ensure_contact_capacity(sg_ctx* ctx, int64_t nc);
 // Body -> contact adjacency (ctx->body_off / body_adj, ascending contact order), the
 // solve counters cleared, and the contact colouring with its processing permutation
 // (ctx->perm, colour offsets in ctx->stats).  Shared by the 2D and 3D solvers.
@@ -296,7 +319,20 @@ int sphere3d_update_inertia(sg_ctx* ctx, bool construction);
 int sphere3d_step(sg_ctx* ctx, sg_step_stats* out);
 int sphere3d_batch_setup(sg_ctx* ctx, long flags, long cells);
 int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out);
+// RigidBody2D circles (rigidbody2d_kernels.cu): one step of the geometric or stabilized map.
+int rb2d_step(sg_ctx* ctx, sg_step_stats* out);
+int sobogus_solve_3d(sg_ctx* ctx, int nb, const double* m, const double* Iw, const double* Iinv, const double* v0,
+                     int nc, const int* ia, const int* ib, const double* bases, const double* arm_a,
+                     const double* arm_b, const double* CoR, const double* mu, const double* nrel_extra,
+                     const double* drel_extra, unsigned max_iters, double tol, unsigned eval_every, double* alpha,
+                     double* beta, double* v2, double* f, double* error, unsigned* iterations);
 
 int wait_timeout_selftest(sg_ctx* ctx);
+
+// Records stage mark k of the step being profiled (no-op outside a profiled single-scene step).
+inline void stage_mark(sg_ctx* ctx, int k) {
+  if (ctx->stage_timing && ctx->ev_stage[k] && cudaEventRecord(ctx->ev_stage[k], ctx->stream) == cudaSuccess)
+    ctx->stage_mask |= 1u << k;
+}
 
 }  // namespace sg

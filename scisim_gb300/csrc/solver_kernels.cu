@@ -18,8 +18,13 @@
 //                                          best-iterate tracking, early exit at tol
 //   k_final_velocity                       v2 = Minv (H^T r - f), f = -M v0
 #include "ctx.hpp"
+#include "coulomb2d.cuh"
+#include "na_cache.hpp"
+
+#include <cuda.h>
 
 #include <algorithm>
+#include <cstring>
 
 namespace sg {
 namespace {
@@ -28,105 +33,18 @@ constexpr int kBlock = 256;
 constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (fewer barrier arrivals)
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
 constexpr int kPatchBlock = 384;  // two-level kernel
+// FP32 form: a start whose FP64 residual is below this many tolerances is swept in FP64.
+// FP64 sweeps a start near tol first runs one-level before the two-level partition is set up.
+constexpr unsigned kFp64Probe = 4;
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
-
-// ---------------------------------------------------------------------------
-// Fischer-Burmeister Coulomb error (mu-scaled self-dual cone, De Saxce change of
-// variable); normal component first.
-__device__ __forceinline__ double fb_error_2d(double r0, double r1, double u0, double u1, double mu) {
-  const double nut = sqrt(u1 * u1);
-  if (mu == 0.0) {
-    const double fn = r0 + u0 - sqrt(r0 * r0 + u0 * u0);
-    double e2 = fn * fn;
-    e2 += r1 * r1;
-    return sqrt(e2);
-  }
-  const double x0 = mu * r0, x1 = r1;
-  const double y0 = u0 + mu * nut, y1 = mu * u1;
-  double z0 = 0.0;
-  z0 += x0 * x0;
-  z0 += x1 * x1;
-  z0 += y0 * y0;
-  z0 += y1 * y1;
-  const double zb = 2.0 * (x0 * x1 + y0 * y1);
-  double nzb2 = 0.0;
-  nzb2 += zb * zb;
-  const double nzb = sqrt(nzb2);
-  double l1 = z0 - nzb;
-  if (l1 < 0.0) l1 = 0.0;
-  const double l2 = z0 + nzb;
-  const double s1 = sqrt(l1), s2 = sqrt(l2);
-  const double sq0 = 0.5 * (s1 + s2);
-  const double half_diff = 0.5 * (s2 - s1);
-  const double sq1 = (nzb > 0.0) ? half_diff * (zb / nzb) : half_diff;
-  double e2 = 0.0;
-  const double p0 = x0 + y0 - sq0;
-  e2 += p0 * p0;
-  const double p1 = x1 + y1 - sq1;
-  e2 += p1 * p1;
-  return sqrt(e2);
+// Host decoding of the ordered encoding of a non-negative double (f64_to_ordered).
+inline double host_ordered_to_f64(unsigned long long u) {
+  u = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+  double d;
+  std::memcpy(&d, &u, sizeof(d));
+  return d;
 }
 
-// Local 2x2 Coulomb problem u = W r + b: take-off, stick, slide (+/-), else the
-// admissible candidate with the smallest FB error.
-__device__ __forceinline__ void local_solve_2d(double w00, double w01, double w11, double b0, double b1, double mu,
-                                               double& r0, double& r1) {
-  if (b0 >= 0.0) {
-    r0 = 0.0;
-    r1 = 0.0;
-    return;
-  }
-  const double det = w00 * w11 - w01 * w01;
-  const double rs0 = (w01 * b1 - w11 * b0) / det;
-  const double rs1 = (w01 * b0 - w00 * b1) / det;
-  if (rs0 >= 0.0 && fabs(rs1) <= mu * rs0) {
-    r0 = rs0;
-    r1 = rs1;
-    return;
-  }
-  double c0[2], c1[2];
-  bool have[2] = {false, false};
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    const double s = (k == 0) ? 1.0 : -1.0;
-    const double den = w00 - s * mu * w01;
-    if (!(den > 0.0)) continue;
-    const double rn = -b0 / den;
-    const double rt = -s * mu * rn;
-    const double ut = w01 * rn + w11 * rt + b1;
-    c0[k] = rn;
-    c1[k] = rt;
-    have[k] = true;
-    if (s * ut >= 0.0) {
-      r0 = rn;
-      r1 = rt;
-      return;
-    }
-  }
-  double best = INFINITY, br0 = 0.0, br1 = 0.0;
-  {
-    const double e = fb_error_2d(0.0, 0.0, b0, b1, mu);
-    if (e < best) {
-      best = e;
-      br0 = 0.0;
-      br1 = 0.0;
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (!have[k]) continue;
-    const double u0 = w00 * c0[k] + w01 * c1[k] + b0;
-    const double u1 = w01 * c0[k] + w11 * c1[k] + b1;
-    const double e = fb_error_2d(c0[k], c1[k], u0, u1, mu);
-    if (e < best) {
-      best = e;
-      br0 = c0[k];
-      br1 = c1[k];
-    }
-  }
-  r0 = br0;
-  r1 = br1;
-}
 
 // u = H v + c for contact k (body b < 0: static).
 __device__ __forceinline__ void local_velocity(const double2 nk, const double2 ck, const double2 va, bool has_b,
@@ -748,6 +666,11 @@ struct Gs32Args {
   const int* body_adj;
   int nb;
   unsigned eval32;
+  // FP64 sweeps take over once the FP64 residual is at or below fp64_below (and from the first
+  // sweep with fp64_start: a start already that close to tol).
+  double fp64_below = 0.0;
+  int fp64_start = 0;
+  int fp64_local = 1;  // k_gs_patch: FP64 sweeps on the two-level partition (0: one-level colours)
 };
 
 // The velocity-independent data of one packed contact (prefetched before the
@@ -895,7 +818,7 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
   double2* best = A.r_a;
   double2* cand = A.r_b;
   double err_best = INFINITY;
-  bool converged = false, fp64 = false;
+  bool converged = false, fp64 = B.fp64_start != 0;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   unsigned next_eval = 1, interval = eval32;
   C32 pf;
@@ -1056,7 +979,8 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
         converged = true;
         break;
       }
-    } else if (err < A.tol || excess32 <= A.tol || (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
+    } else if (err < A.tol || err <= B.fp64_below || excess32 <= A.tol ||
+               (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
       // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
       // FP64 sweeps once every contact's remaining error is within FP32 rounding of
       // its floor (or FP32 stopped improving the best iterate close to it).
@@ -1608,6 +1532,36 @@ __device__ __forceinline__ void gs_update32_iso(const Gs32Args& B, int s, float2
   B.r[s] = make_float2(rn0, rn1);
 }
 
+// FP64 update of contact k (gs_update's arithmetic: the FP64 record, the general 2x2 local solve)
+// on shared-memory FP64 velocities: la, lb are the bodies' slots (lb < 0 for a static plane).
+__device__ __forceinline__ void gs_update64_local(const GsArgs& A, int k, int la, int lb, double2* sv,
+                                                  const double* sm) {
+  const double2 nk = A.n[k], ck = A.c[k];
+  const double2 va = sv[la];
+  const bool has_b = lb >= 0;
+  const double2 vb = has_b ? sv[lb] : make_double2(0.0, 0.0);
+  double u0, u1;
+  local_velocity(nk, ck, va, has_b, vb, u0, u1);
+  const double2 rk = A.r[k];
+  const double r0 = rk.x, r1 = rk.y;
+  const double w00 = A.W[3 * k], w01 = A.W[3 * k + 1], w11 = A.W[3 * k + 2];
+  const double bt0 = u0 - (w00 * r0 + w01 * r1);
+  const double bt1 = u1 - (w01 * r0 + w11 * r1);
+  double rn0, rn1;
+  local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
+  const double d0 = rn0 - r0, d1 = rn1 - r1;
+  const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  const double px = nx * d0 + tx * d1;
+  const double py = ny * d0 + ty * d1;
+  const double ma = sm[la];
+  sv[la] = make_double2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const double mb = sm[lb];
+    sv[lb] = make_double2(vb.x - mb * px, vb.y - mb * py);
+  }
+  A.r[k] = make_double2(rn0, rn1);
+}
+
 // Highest non-empty colour + 1 of a group's offsets.
 __device__ __forceinline__ int group_colors(const int* off) {
   int n = kMaxColors;
@@ -1631,7 +1585,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   // as in k_gs_mixed.  Slots: patch velocities, patch 1/m, tile velocities, tile 1/m (cap and
   // capq even, so every float2 stays 8-byte aligned), then the staged contacts (Staged), the
   // patch's first stage_p in slots [0, stage_p), the tile's first stage_q after them.
-  extern __shared__ float2 sv[];
+  extern __shared__ __align__(16) float2 sv[];
   float* sm = reinterpret_cast<float*>(sv + Q.cap);
   float2* svq = reinterpret_cast<float2*>(sm + Q.cap);
   float* smq = reinterpret_cast<float*>(svq + Q.capq);
@@ -1702,7 +1656,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   double2* best = A.r_a;
   double2* cand = A.r_b;
   double err_best = INFINITY;
-  bool converged = false, fp64 = false;
+  bool converged = false, fp64 = B.fp64_start != 0;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   unsigned next_eval = 1, interval = eval32;
   // Phase timers of block 0 (shared memory, so that they take no registers from the sweeps):
@@ -1715,6 +1669,8 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   // touched outside the patch, so only they are reloaded and written back, except after an
   // FP64 check, which resets every velocity from the impulses.
   bool reload_all = true;
+  // Entering the FP64 sweeps: every velocity and inverse mass is loaded afresh.
+  bool fresh64 = true;
   for (it = 1; it <= A.max_iters; ++it) {
     bool do_eval;
     if (!fp64) {
@@ -1862,10 +1818,10 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
           return;
         }
       }
-    } else {
+    } else if (!B.fp64_local) {
       for (int col = 0; col < ncol; ++col) {
         const int e = s_off[col + 1];
-        for (int s = s_off[col] + tid; s < e; s += nthr) gs_update(A, A.perm[s]);
+        for (int q = s_off[col] + tid; q < e; q += nthr) gs_update(A, A.perm[q]);
         if (!grid_sync(A.gb, A.spin)) {
           if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
           return;
@@ -1873,6 +1829,66 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
       }
       ++s64;
       do_eval = (it % eval64 == 0) || it == A.max_iters;
+    } else {
+      // FP64 sweeps on the same partition: the patch's FP64 velocities and inverse masses in
+      // shared memory (the FP32 layout is dead once the solve is in FP64, which it never leaves),
+      // the shifted tile's likewise, the remainder by block 0 on global velocities; three grid
+      // barriers a sweep.  Before a residual evaluation every patch body goes back to global memory.
+      do_eval = (it % eval64 == 0) || it == A.max_iters;
+      double2* sv64 = reinterpret_cast<double2*>(sv);
+      double* sm64 = reinterpret_cast<double*>(sv64 + Q.cap);
+      double2* svq64 = reinterpret_cast<double2*>(sm64 + Q.cap);
+      double* smq64 = reinterpret_cast<double*>(svq64 + Q.capq);
+      if (fresh64) {
+        for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) sm64[j - pb0] = A.minv[Q.pbody[j]];
+        for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) smq64[j - qb0] = A.minv[Q.qbody[j]];
+      }
+      const int lend = fresh64 ? pb1 : pbe;
+      fresh64 = false;
+      for (int j = pb0 + threadIdx.x; j < lend; j += blockDim.x) sv64[j - pb0] = __ldcg(&A.v[Q.pbody[j]]);
+      __syncthreads();
+      for (int col = 0; col < ncol_p; ++col) {
+        const int e = s_goff[col + 1];
+        for (int q = s_goff[col] + threadIdx.x; q < e; q += blockDim.x) {
+          const int2 ab = B.ab[q];
+          gs_update64_local(A, Q.order[q], ab.x, ab.y, sv64, sm64);
+        }
+        __syncthreads();
+      }
+      const int wend = do_eval ? pb1 : pbe;
+      for (int j = pb0 + threadIdx.x; j < wend; j += blockDim.x) A.v[Q.pbody[j]] = sv64[j - pb0];
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      if (qb1 > qb0) {
+        for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) svq64[j - qb0] = __ldcg(&A.v[Q.qbody[j]]);
+        __syncthreads();
+        for (int col = 0; col < ncol_q; ++col) {
+          const int e = s_hoff[col + 1];
+          for (int q = s_hoff[col] + threadIdx.x; q < e; q += blockDim.x) {
+            const int2 ab = B.ab[q];
+            gs_update64_local(A, Q.order[q], ab.x, ab.y, svq64, smq64);
+          }
+          __syncthreads();
+        }
+        for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) A.v[Q.qbody[j]] = svq64[j - qb0];
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      if (blockIdx.x == 0 && nrest > 0) {
+        for (int col = 0; col < ncol_r; ++col) {
+          for (int q = s_boff[col] + threadIdx.x; q < s_boff[col + 1]; q += blockDim.x) gs_update(A, Q.order[q]);
+          __syncthreads();
+        }
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+      ++s64;
     }
     if (!do_eval) continue;
     // emax: the residual.  excess: the largest amount by which a contact's error exceeds
@@ -1936,7 +1952,8 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
         converged = true;
         break;
       }
-    } else if (err < A.tol || excess32 <= A.tol || (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
+    } else if (err < A.tol || err <= B.fp64_below || excess32 <= A.tol ||
+               (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
       // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
       // FP64 sweeps once every contact's remaining error is within FP32 rounding of
       // its floor (or FP32 stopped improving the best iterate close to it).
@@ -2302,6 +2319,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
 
   // Adjacency and colouring first: the velocity initialisation reads the adjacency.
   if (int r = prepare_contact_graph(ctx, nb, nc, P.ia, P.ib)) return r;
+  stage_mark(ctx, 4);
   double2* vrun = ctx->v_run.as<double2>();
   if (sp.learned && nc > 0 && (ctx->mlp_on || ctx->mlp_record)) {
     if (int r = mlp_features(ctx, P)) return r;
@@ -2335,6 +2353,37 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
                                                P.minv, vrun);
   SG_CUDA_TRY(cudaGetLastError());
 
+  // FP32 form: the FP64 residual of the start decides the arithmetic.  A start already within
+  // fp64_factor tol of the tolerance (a warm start on a settled scene) is swept in FP64 from the
+  // first sweep: FP32 sweeps would only add their rounding, whose floor lies near tol where the
+  // impulses of deep stacks reach hundreds of times the velocity scale.  Such a solve first runs a
+  // few one-level FP64 sweeps (it usually converges within them, for less than the two-level
+  // partition's setup costs) and, if it has not converged, goes on with FP64 sweeps on the
+  // two-level partition.
+  const bool fp32_form = sp.precision == SG_PRECISION_FP32_REFINE;
+  bool fp64_start = false;
+  if (fp32_form && nc > 0) {
+    if (!ctx->start_slot.p) {
+      if (int r = grow(ctx->start_slot, sizeof(unsigned long long))) return r;
+    }
+    unsigned long long* slot = ctx->start_slot.as<unsigned long long>();
+    SG_CUDA_TRY(cudaMemsetAsync(slot, 0, sizeof(unsigned long long), s));
+    const int eb = std::max(1, std::min(blocks_for(nc), ctx->num_sms * 8));
+    k_start_err<<<eb, kBlock, 0, s>>>(nc, P.ia, P.ib, n2, reinterpret_cast<const double2*>(P.c), P.mu, r2, vrun, slot);
+    SG_CUDA_TRY(cudaGetLastError());
+    unsigned long long h = 0;
+    SG_CUDA_TRY(cudaMemcpyAsync(&h, slot, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    ctx->kernel_launches += 1;
+    const double err0 = host_ordered_to_f64(h);
+    if (err0 < (double)ctx->fp64_factor * sp.tol) {
+      fp64_start = true;
+      ctx->fp64_start_solves += 1;
+    }
+  }
+  bool fp32_sweeps = fp32_form;
+  unsigned probe_iters = 0, probe_evals = 0;
+
   if (nc > 0) {
     // Gauss-Seidel.
     SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
@@ -2358,7 +2407,48 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     GA.tol = sp.tol;
     GA.max_iters = sp.max_iters;
     GA.eval_every = sp.eval_every;
-    if (sp.precision == SG_PRECISION_FP32_REFINE) {
+    const bool two_level_applies = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 &&
+                                   nc >= ctx->two_level_min_contacts;
+    if (fp64_start) {
+      GsArgs GP = GA;
+      const bool probe = two_level_applies && sp.max_iters > kFp64Probe;
+      if (probe) GP.max_iters = kFp64Probe;
+      void* pargs[] = {&GP};
+      const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);
+      stage_mark(ctx, 5);
+      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+      SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kGsBlock), pargs, 0, s));
+      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+      stage_mark(ctx, 6);
+      ctx->kernel_launches += 1;
+      fp32_sweeps = false;
+      if (probe) {
+        SolveStats hp{};
+        SG_CUDA_TRY(cudaMemcpyAsync(&hp, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+        SG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!hp.converged && hp.status == 0) {
+          // Not converged in the probe: FP64 sweeps on the two-level partition from its best
+          // iterate, within the remaining sweeps; the residual slots start afresh.
+          if (ctx->profile) {
+            float ms = 0.f;
+            SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
+            ctx->gs_ms += ms;
+          }
+          probe_iters = hp.iterations;
+          probe_evals = hp.evals;
+          k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2,
+                                                       reinterpret_cast<const double2*>(P.v0), P.minv, vrun);
+          SG_CUDA_TRY(cudaGetLastError());
+          SG_CUDA_TRY(cudaMemsetAsync(st->err_slot, 0, sizeof(st->err_slot), s));
+          SG_CUDA_TRY(cudaMemsetAsync(st->mag_slot, 0, sizeof(st->mag_slot), s));
+          SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+          GA.max_iters = sp.max_iters - probe_iters;
+          fp32_sweeps = true;
+          ctx->kernel_launches += 1;
+        }
+      }
+    }
+    if (fp32_sweeps) {
       const size_t c = (size_t)nc, b = (size_t)std::max(nb, 1);
       if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
       if (int r = grow(ctx->pk_n, sizeof(float2) * c)) return r;
@@ -2551,6 +2641,8 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.body_adj = adj;
       GB.nb = nb;
       GB.eval32 = (unsigned)ctx->check_interval;
+      GB.fp64_below = (double)ctx->fp64_factor * sp.tol;
+      GB.fp64_start = probe_iters > 0 ? 1 : 0;
       if (patched) {
         // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
         // contacts as fit (the patch's first), 32 B each.
@@ -2578,11 +2670,17 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
                     ctx->pt_bcnt.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qbody.as<int>(),
                     ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), capp, capq, stage_p, stage_q,
                     ctx->pt_cbody.as<int>(), ctx->pt_cpos.as<int>(), capc, capc ? nrest_bodies : 0, stage_c};
-        const size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q) + (size_t)rest_bytes;
+        size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q) + (size_t)rest_bytes;
+        // The FP64 sweeps reuse the same shared memory for the patch's and the tile's FP64
+        // velocities and inverse masses (24 B per body) when they fit.
+        const size_t smem64 = (size_t)24 * (size_t)(capp + capq);
+        GB.fp64_local = smem64 <= (size_t)dyn_budget ? 1 : 0;
+        if (GB.fp64_local && smem64 > smem) smem = smem64;
         ctx->patch_staged += (uint64_t)stage_p;
         void* args[] = {&GA, &GB, &Q};
         // The boundary colouring used the barrier: start it afresh for this grid.
         SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+        stage_mark(ctx, 5);
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(maxP);
@@ -2596,23 +2694,28 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         lc.numAttrs = 1;
         SG_CUDA_TRY(cudaLaunchKernelExC(&lc, (const void*)k_gs_patch, args));
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+        stage_mark(ctx, 6);
         ctx->patched_solves += 1;
       } else {
         void* args[] = {&GA, &GB};
         const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
         // The patch setup's colouring kernels used the barrier with their own grid: reset it.
         SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+        stage_mark(ctx, 5);
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
         SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+        stage_mark(ctx, 6);
       }
       ctx->kernel_launches += 2;
-    } else {
+    } else if (!fp32_form) {
       void* args[] = {&GA};
       const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);
-      if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+      stage_mark(ctx, 5);
+        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
       SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs, dim3(g), dim3(kGsBlock), args, 0, s));
       if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+        stage_mark(ctx, 6);
     }
     ctx->kernel_launches += 1;  // gs
   }
@@ -2620,12 +2723,18 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
   k_final_velocity<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2, reinterpret_cast<const double2*>(P.v0),
                                                      P.m, P.minv, reinterpret_cast<double2*>(P.v2));
   SG_CUDA_TRY(cudaGetLastError());
+  stage_mark(ctx, 7);
   if (sp.learned && ctx->mlp_record) {
     if (int r = mlp_targets(ctx, P)) return r;
     ctx->mlp_last_n = nc;
   }
   SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
   SG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (probe_iters > 0) {  // the one-level FP64 sweeps before the two-level ones
+    ctx->h_stats.iterations += probe_iters;
+    ctx->h_stats.sweeps64 += probe_iters;
+    ctx->h_stats.evals += probe_evals;
+  }
   if (nc == 0) {
     ctx->h_stats.iterations = 0;
     ctx->h_stats.converged = 1;
@@ -2814,9 +2923,41 @@ static_assert(kNoAllocScratchBytes < 9u * 1024u * 1024u, "scratch must stay mode
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device ordinal, looked up once per device.
+// Device address of g_noalloc_scratch, looked up per device and per context: the cache keeps it
+// with the identity of the context it was looked up in (cuCtxGetId, reached through the runtime's
+// driver entry points so that the library needs no link to the driver library) and looks it up
+// again when another context is current, e.g. after cudaDeviceReset re-created the primary context.
 constexpr int kNaMaxDevices = 64;
-unsigned char* g_na_addr[kNaMaxDevices] = {};
+DeviceAddressCache<kNaMaxDevices> g_na_cache;
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+struct NaDriverFns {
+  PfnCtxGetCurrent get_current = nullptr;
+  PfnCtxGetId get_id = nullptr;
+  NaDriverFns() {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PfnCtxGetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PfnCtxGetId>(p);
+  }
+};
+
+// Identity of the context current on this thread; false when there is none or it is unknown.
+bool na_current_ctx_id(unsigned long long* id) {
+  static const NaDriverFns fns;  // resolved once (thread-safe initialisation)
+  *id = 0;
+  if (!fns.get_current || !fns.get_id) return false;
+  CUcontext c = nullptr;
+  if (fns.get_current(&c) != CUDA_SUCCESS || c == nullptr) return false;
+  return fns.get_id(c, id) == CUDA_SUCCESS && *id != 0;
+}
 
 int na_scratch_address(unsigned char** out) {
   int dev = -1;
@@ -2825,16 +2966,20 @@ int na_scratch_address(unsigned char** out) {
     set_error("sg_sobogus_solve_2d_noalloc: device ordinal beyond 63");
     return SG_BAD_INPUT;
   }
-  if (!g_na_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") + cudaGetErrorString(e));
-      return SG_CUDA_ERROR;
-    }
-    g_na_addr[dev] = static_cast<unsigned char*>(p);
-  }
-  *out = g_na_addr[dev];
+  void* p = nullptr;
+  const int r = g_na_cache.get(
+      dev, na_current_ctx_id,
+      [](void** addr) {
+        const cudaError_t e = cudaGetSymbolAddress(addr, g_noalloc_scratch);
+        if (e != cudaSuccess || !*addr) {
+          set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") + cudaGetErrorString(e));
+          return (int)SG_CUDA_ERROR;
+        }
+        return (int)SG_OK;
+      },
+      &p);
+  if (r != SG_OK) return r;
+  *out = static_cast<unsigned char*>(p);
   return SG_OK;
 }
 

@@ -2053,6 +2053,138 @@ __global__ void __launch_bounds__(kGs3mBlock, 1) k_gs3_mixed_batch(Gs3MixedBatch
   }
 }
 
+
+// Assembly of caller-given sphere contacts (the FrictionSolver entry, sg_sobogus_solve_3d): the basis
+// [n s t] (column-major, stored as the rows E), the angular rows r x s and r x t from the caller's arms,
+// the forcing term with the map's extra relative velocities, the Delassus block and the warm start,
+// in the arithmetic of k_assemble3 (SobogusFrictionProblem::initialize3D, Sobogus.cpp:184-251;
+// Constraint::computeForcingTerm, scisim/Constraints/Constraint.cpp:18-34).
+struct FsAssemble3 {
+  int nb, nc;
+  const int* ia;
+  const int* ib;
+  const double* bases;   // 9 per contact
+  const double* arm_a;   // 3 per contact
+  const double* arm_b;   // 3 per contact
+  const double* v0;      // 6nb
+  const double* minv;
+  const double* Iinv;
+  const double* CoR;
+  const double* mu;
+  const double* nrel;    // nc or null
+  const double* drel;    // 2nc or null
+  const double* alpha;   // nc
+  const double* beta;    // 2nc
+  double* E;
+  double* Aa;
+  double* Ab;
+  double* c;
+  double* W;
+  double* mu_out;
+  double* r;
+};
+
+__global__ void k_fs_assemble3(FsAssemble3 A) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.nc) return;
+  const int nb = A.nb;
+  const int a = A.ia[k], b = A.ib[k];
+  const bool has_b = b >= 0;
+  double n[3], s[3], t[3], ra[3], rb[3];
+  const double* Bk = A.bases + 9 * (size_t)k;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    n[j] = Bk[j];
+    s[j] = Bk[3 + j];
+    t[j] = Bk[6 + j];
+    ra[j] = A.arm_a[3 * (size_t)k + j];
+    rb[j] = has_b ? A.arm_b[3 * (size_t)k + j] : 0.0;
+  }
+  double* E = A.E + 9 * (size_t)k;
+#pragma unroll
+  for (int j = 0; j < 9; ++j) E[j] = Bk[j];
+  double as[3], at[3], bs[3] = {0.0, 0.0, 0.0}, bt[3] = {0.0, 0.0, 0.0};
+  cross3(ra, s, as);
+  cross3(ra, t, at);
+  if (has_b) {
+    cross3(rb, s, bs);
+    cross3(rb, t, bt);
+  }
+  double* Aa = A.Aa + 6 * (size_t)k;
+  double* Ab = A.Ab + 6 * (size_t)k;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Aa[j] = as[j];
+    Aa[3 + j] = at[j];
+    Ab[j] = bs[j];
+    Ab[3 + j] = bt[j];
+  }
+  // n . (v_a - v_b) on the linear velocities (the normal row has no angular part).
+  double vr[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) vr[j] = A.v0[3 * (size_t)a + j] - (has_b ? A.v0[3 * (size_t)b + j] : 0.0);
+  const double ndotv = dot3(n, vr);
+  const double zero[3] = {0.0, 0.0, 0.0};
+  double nrel = -dot3(zero, n);
+  double drel0 = -dot3(zero, s), drel1 = -dot3(zero, t);
+  if (A.nrel) nrel = nrel + A.nrel[k];
+  if (A.drel) {
+    drel0 = drel0 + A.drel[2 * (size_t)k];
+    drel1 = drel1 + A.drel[2 * (size_t)k + 1];
+  }
+  const double sc = A.CoR[k] * ndotv + nrel;
+  double w[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) w[j] = ((0.0 + n[j] * sc) + s[j] * drel0) + t[j] * drel1;
+  A.c[3 * (size_t)k] = dot3(n, w);
+  A.c[3 * (size_t)k + 1] = dot3(s, w);
+  A.c[3 * (size_t)k + 2] = dot3(t, w);
+  const double* B[3] = {n, s, t};
+  const double* AaR[3] = {nullptr, as, at};
+  const double* AbR[3] = {nullptr, bs, bt};
+  double Ia[9], Ib[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Ia[j] = A.Iinv[9 * (size_t)a + j];
+  if (has_b) {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) Ib[j] = A.Iinv[9 * (size_t)b + j];
+  }
+  const double ma = A.minv[a], mb = has_b ? A.minv[b] : 0.0;
+  double* Wk = A.W + 6 * (size_t)k;
+  int q = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      double wij = ma * dot3(B[i], B[j]);
+      if (i > 0) {
+        double x[3];
+        matvec3(Ia, AaR[j], x);
+        wij = wij + dot3(AaR[i], x);
+      }
+      if (has_b) {
+        double wb = mb * dot3(B[i], B[j]);
+        if (i > 0) {
+          double x[3];
+          matvec3(Ib, AbR[j], x);
+          wb = wb + dot3(AbR[i], x);
+        }
+        wij = wij + wb;
+      }
+      Wk[q++] = wij;
+    }
+  A.mu_out[k] = A.mu[k];
+  // Warm start r = alpha n + beta0 s + beta1 t, then local r = E^T r (Sobogus.cpp:514-518).
+  const double al = A.alpha[k], b0 = A.beta[2 * (size_t)k], b1 = A.beta[2 * (size_t)k + 1];
+  double rw[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) rw[j] = (al * n[j] + b0 * s[j]) + b1 * t[j];
+  A.r[3 * (size_t)k] = dot3(n, rw);
+  A.r[3 * (size_t)k + 1] = dot3(s, rw);
+  A.r[3 * (size_t)k + 2] = dot3(t, rw);
+  (void)nb;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -2095,6 +2227,284 @@ static int splitham(sg_ctx* ctx, const double* v0, bool with_aabb) {
       with_aabb ? ctx->aabb.as<double>() : nullptr);
   SG_CUDA_TRY(cudaGetLastError());
   return SG_OK;
+}
+
+// The block Gauss-Seidel solve of nc assembled sphere contacts (C, impulses rimp in local
+// coordinates, in = start, out = result) over nb bodies (v0 6nb [v | omega], masses, world inertia
+// and its inverse): running velocities, the FP64 or FP32+FP64 sweeps, v2 = M^-1 (H^T r - f) with
+// f = -M v0, and (alpha, beta0, beta1) per contact into ab.  Fills ctx->h_stats and the work counters.
+static int solve3_contacts(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const Contacts3& C, double* rimp,
+                           const double* v0, const double* m, const double* minv, const double* Iw,
+                           const double* Iinv, double* v2, double* ab, double tol, unsigned max_iters,
+                           unsigned eval_every) {
+  cudaStream_t s = ctx->stream;
+  if (int r = ensure_solver_capacity(ctx, nb, nc)) return r;
+  if (int r = grow(ctx->vrun3, sizeof(double4_32a) * 2 * (size_t)nb)) return r;
+  if (int r = prepare_contact_graph(ctx, nb, nc, ia, ib)) return r;
+  const int* off = ctx->body_off.as<int>();
+  const int* adj = ctx->body_adj.as<int>();
+  double4_32a* V = ctx->vrun3.as<double4_32a>();
+  k_vel_init3<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, C, rimp, v0, minv, Iinv, V);
+  SG_CUDA_TRY(cudaGetLastError());
+  SolveStats* sst = ctx->stats.as<SolveStats>();
+  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
+  SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+  Gs3Args G;
+  G.nc = nc;
+  G.C = C;
+  G.minv = minv;
+  G.Iinv = Iinv;
+  G.perm = ctx->perm.as<int>();
+  G.r = rimp;
+  G.r_a = ctx->r3a.as<double>();
+  G.r_b = ctx->r3b.as<double>();
+  G.V = V;
+  G.st = sst;
+  G.gb = gb;
+  G.spin = ctx->spin_limit;
+  G.tol = tol;
+  G.max_iters = max_iters;
+  G.eval_every = eval_every;
+  if (ctx->cfg.precision == SG_PRECISION_FP32_REFINE) {
+    const size_t c = (size_t)std::max(nc, 1), b1 = (size_t)std::max(nb, 1);
+    if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
+    if (int r = grow(ctx->pk3, sizeof(float) * 31 * c)) return r;   // E 9, Aa 6, Ab 6, c 3, W 6, mu 1
+    if (int r = grow(ctx->pk_r, sizeof(float) * 3 * c)) return r;
+    if (int r = grow(ctx->v32, sizeof(float4) * 2 * b1)) return r;
+    if (int r = grow(ctx->minv32, sizeof(float) * b1)) return r;
+    if (int r = grow(ctx->Iinv32, sizeof(float) * 9 * b1)) return r;
+    float* f = ctx->pk3.as<float>();
+    Gs3m B;
+    B.ab = ctx->pk_ab.as<int2>();
+    B.E = f;
+    B.Aa = f + 9 * c;
+    B.Ab = f + 15 * c;
+    B.c = f + 21 * c;
+    B.W = f + 24 * c;
+    B.mu = f + 30 * c;
+    B.r = ctx->pk_r.as<float>();
+    B.V = ctx->v32.as<float4>();
+    B.minv = ctx->minv32.as<float>();
+    B.Iinv = ctx->Iinv32.as<float>();
+    B.v0 = v0;
+    B.body_off = off;
+    B.body_adj = adj;
+    B.nb = nb;
+    B.eval32 = (unsigned)ctx->check_interval;
+    B.work = nullptr;
+    k_pack3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), C, rimp, B, B.r);
+    k_body32<<<blocks_for(nb), kBlock, 0, s>>>(nb, V, minv, Iinv, B.V,
+                                              const_cast<float*>(B.minv), const_cast<float*>(B.Iinv));
+    SG_CUDA_TRY(cudaGetLastError());
+    void* args[] = {&G, &B};
+    const int grid = coop_grid(ctx, k_gs3_mixed, (long)ctx->num_sms * kGs3mBlock, kGs3mBlock, 1);
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_mixed, grid, kGs3mBlock, args, s));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+    ctx->kernel_launches += 2;
+  } else {
+    void* args[] = {&G};
+    const int grid = coop_grid(ctx, k_gs3, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs3, dim3(grid), dim3(kGs3Block), args, 0, s));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+  }
+  k_final_vel3<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, C, rimp, v0, m, minv, Iw, Iinv, v2);
+  k_extract3<<<blocks_for(nc), kBlock, 0, s>>>(nc, C.E, rimp, ab);
+  SG_CUDA_TRY(cudaGetLastError());
+  SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, sst, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  // vel init, gs, final velocity, extract
+  ctx->kernel_launches += 4;
+  if (ctx->h_stats.status == SG_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its spin limit");
+    return SG_DEVICE_TIMEOUT;
+  }
+  if (ctx->h_stats.status == SG_CAPACITY) {
+    set_error("contact colouring exceeded 64 colours or its round limit");
+    return SG_CAPACITY;
+  }
+  ctx->gs_launches += 1;
+  ctx->contact_sweeps += (uint64_t)ctx->h_stats.sweeps64 * (uint64_t)nc;
+  ctx->contact_sweeps32 += (uint64_t)ctx->h_stats.sweeps32 * (uint64_t)nc;
+  ctx->contact_evals += (uint64_t)ctx->h_stats.evals * (uint64_t)nc;
+  ctx->contact_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nc;
+  ctx->body_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nb;
+  if (ctx->profile) {
+    float ms = 0.f;
+    SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
+    ctx->gs_ms += ms;
+  }
+  return SG_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// FrictionSolver::solve for spheres on host buffers (sg_sobogus_solve_3d).
+static inline void h_cross3(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+int sobogus_solve_3d(sg_ctx* ctx, int nb, const double* m, const double* Iw, const double* Iinv, const double* v0,
+                     int nc, const int* ia, const int* ib, const double* bases, const double* arm_a,
+                     const double* arm_b, const double* CoR, const double* mu, const double* nrel_extra,
+                     const double* drel_extra, unsigned max_iters, double tol, unsigned eval_every, double* alpha,
+                     double* beta, double* v2, double* f, double* error, unsigned* iterations) {
+  if (!ctx || nb < 0 || nc < 0 || (nb > 0 && (!m || !Iw || !Iinv || !v0 || !v2 || !f)) ||
+      (nc > 0 && (!ia || !ib || !bases || !arm_a || !arm_b || !CoR || !mu || !alpha || !beta))) {
+    set_error("sg_sobogus_solve_3d: invalid arguments");
+    return SG_BAD_INPUT;
+  }
+  // The reference's invariants (asserts in Sobogus.cpp:497-512 and SphereSphereConstraint::evalH):
+  // valid body indices, right-handed orthonormal bases, arms parallel to the normal.
+  for (int k = 0; k < nc; ++k) {
+    if (ia[k] < 0 || ia[k] >= nb || ib[k] >= nb || ib[k] == ia[k] || ib[k] < -1) {
+      set_error("sg_sobogus_solve_3d: contact body index out of range");
+      return SG_BAD_INPUT;
+    }
+    const double* E = bases + 9 * (size_t)k;
+    double dev = 0.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const double d = E[3 * i] * E[3 * j] + E[3 * i + 1] * E[3 * j + 1] + E[3 * i + 2] * E[3 * j + 2];
+        dev = std::max(dev, std::fabs(d - (i == j ? 1.0 : 0.0)));
+      }
+    double nxs[3];
+    h_cross3(E, E + 3, nxs);
+    const double det = nxs[0] * E[6] + nxs[1] * E[7] + nxs[2] * E[8];
+    double xa[3], xb[3] = {0.0, 0.0, 0.0};
+    h_cross3(arm_a + 3 * (size_t)k, E, xa);
+    if (ib[k] >= 0) h_cross3(arm_b + 3 * (size_t)k, E, xb);
+    double par = 0.0;
+    for (int j = 0; j < 3; ++j) par = std::max(par, std::max(std::fabs(xa[j]), std::fabs(xb[j])));
+    if (!(dev <= 1.0e-6) || !(std::fabs(det - 1.0) <= 1.0e-6) || !(par <= 1.0e-6)) {
+      set_error("sg_sobogus_solve_3d: basis not right-handed orthonormal or arm not parallel to the normal");
+      return SG_BAD_INPUT;
+    }
+  }
+  if (nc == 0) {
+    for (int i = 0; i < 6 * nb; ++i) {
+      v2[i] = v0[i];
+      f[i] = 0.0;
+    }
+    if (error) *error = 0.0;
+    if (iterations) *iterations = 0;
+    ctx->last_nc = 0;
+    return SG_OK;
+  }
+  SG_CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  std::vector<double> minv(nb);
+  for (int i = 0; i < nb; ++i) minv[i] = 1.0 / m[i];
+  const size_t nbs = (size_t)nb, ncs = (size_t)nc;
+  // Body data: m, minv, Iw, Iinv, v0, v2; contact inputs packed after each other.
+  if (int r = grow(ctx->fs_m, sizeof(double) * nbs)) return r;
+  if (int r = grow(ctx->fs_minv, sizeof(double) * nbs)) return r;
+  if (int r = grow(ctx->fs_v0, sizeof(double) * 6 * nbs)) return r;
+  if (int r = grow(ctx->fs_v2, sizeof(double) * 6 * nbs)) return r;
+  if (int r = grow(ctx->fs_I, sizeof(double) * 18 * nbs)) return r;
+  const size_t in_doubles = ncs * (9 + 3 + 3 + 1 + 1 + 1 + 2 + 1 + 2);
+  if (int r = grow(ctx->fs_in, sizeof(double) * in_doubles)) return r;
+  if (int r = ensure_contacts3(ctx, nc)) return r;
+  double* dI = ctx->fs_I.as<double>();
+  double* din = ctx->fs_in.as<double>();
+  double* d_bases = din;
+  double* d_arm_a = d_bases + 9 * ncs;
+  double* d_arm_b = d_arm_a + 3 * ncs;
+  double* d_CoR = d_arm_b + 3 * ncs;
+  double* d_mu = d_CoR + ncs;
+  double* d_nrel = d_mu + ncs;
+  double* d_drel = d_nrel + ncs;
+  double* d_alpha = d_drel + 2 * ncs;
+  double* d_beta = d_alpha + ncs;
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->fs_m.p, m, sizeof(double) * nbs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->fs_minv.p, minv.data(), sizeof(double) * nbs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->fs_v0.p, v0, sizeof(double) * 6 * nbs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(dI, Iw, sizeof(double) * 9 * nbs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(dI + 9 * nbs, Iinv, sizeof(double) * 9 * nbs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->ia.p, ia, sizeof(int) * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(ctx->ib.p, ib, sizeof(int) * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_bases, bases, sizeof(double) * 9 * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_arm_a, arm_a, sizeof(double) * 3 * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_arm_b, arm_b, sizeof(double) * 3 * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_CoR, CoR, sizeof(double) * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_mu, mu, sizeof(double) * ncs, cudaMemcpyHostToDevice, s));
+  if (nrel_extra) SG_CUDA_TRY(cudaMemcpyAsync(d_nrel, nrel_extra, sizeof(double) * ncs, cudaMemcpyHostToDevice, s));
+  if (drel_extra)
+    SG_CUDA_TRY(cudaMemcpyAsync(d_drel, drel_extra, sizeof(double) * 2 * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_alpha, alpha, sizeof(double) * ncs, cudaMemcpyHostToDevice, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(d_beta, beta, sizeof(double) * 2 * ncs, cudaMemcpyHostToDevice, s));
+  FsAssemble3 A;
+  A.nb = nb;
+  A.nc = nc;
+  A.ia = ctx->ia.as<int>();
+  A.ib = ctx->ib.as<int>();
+  A.bases = d_bases;
+  A.arm_a = d_arm_a;
+  A.arm_b = d_arm_b;
+  A.v0 = ctx->fs_v0.as<double>();
+  A.minv = ctx->fs_minv.as<double>();
+  A.Iinv = dI + 9 * nbs;
+  A.CoR = d_CoR;
+  A.mu = d_mu;
+  A.nrel = nrel_extra ? d_nrel : nullptr;
+  A.drel = drel_extra ? d_drel : nullptr;
+  A.alpha = d_alpha;
+  A.beta = d_beta;
+  A.E = ctx->E3.as<double>();
+  A.Aa = ctx->Aa3.as<double>();
+  A.Ab = ctx->Ab3.as<double>();
+  A.c = ctx->c3.as<double>();
+  A.W = ctx->W3.as<double>();
+  A.mu_out = ctx->mu.as<double>();
+  A.r = ctx->r3.as<double>();
+  k_fs_assemble3<<<blocks_for(nc), kBlock, 0, s>>>(A);
+  SG_CUDA_TRY(cudaGetLastError());
+  ctx->kernel_launches += 1;
+  const Contacts3 C{A.ia, A.ib, A.E, A.Aa, A.Ab, A.c, A.W, A.mu_out};
+  const int sr = solve3_contacts(ctx, nb, nc, A.ia, A.ib, C, A.r, A.v0, ctx->fs_m.as<double>(), A.minv, dI, A.Iinv,
+                                 ctx->fs_v2.as<double>(), ctx->ab3.as<double>(), tol, max_iters,
+                                 eval_every == 0 ? 1u : eval_every);
+  if (sr != SG_OK) return sr;
+  ctx->last_nc = nc;
+  std::vector<double> ab(3 * ncs), E(9 * ncs);
+  SG_CUDA_TRY(cudaMemcpyAsync(v2, ctx->fs_v2.p, sizeof(double) * 6 * nbs, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaMemcpyAsync(ab.data(), ctx->ab3.p, sizeof(double) * 3 * ncs, cudaMemcpyDeviceToHost, s));
+  SG_CUDA_TRY(cudaStreamSynchronize(s));
+  // alpha, beta and the friction impulse with its torque, in contact order (Sobogus.cpp:533-567).
+  for (size_t i = 0; i < 6 * nbs; ++i) f[i] = 0.0;
+  for (int k = 0; k < nc; ++k) {
+    const double* Bk = bases + 9 * (size_t)k;
+    const double* sv = Bk + 3;
+    const double* tv = Bk + 6;
+    alpha[k] = ab[3 * (size_t)k];
+    const double b0 = ab[3 * (size_t)k + 1], b1 = ab[3 * (size_t)k + 2];
+    beta[2 * (size_t)k] = b0;
+    beta[2 * (size_t)k + 1] = b1;
+    double as[3], at[3];
+    h_cross3(arm_a + 3 * (size_t)k, sv, as);
+    h_cross3(arm_a + 3 * (size_t)k, tv, at);
+    const int a = ia[k], b = ib[k];
+    for (int j = 0; j < 3; ++j) {
+      const double f0 = b0 * sv[j] + b1 * tv[j];
+      const double ta = b0 * as[j] + b1 * at[j];
+      f[3 * (size_t)a + j] += f0;
+      f[3 * nbs + 3 * (size_t)a + j] += ta;
+      if (b >= 0) {
+        double bs[3], bt[3];
+        h_cross3(arm_b + 3 * (size_t)k, sv, bs);
+        h_cross3(arm_b + 3 * (size_t)k, tv, bt);
+        const double tb = b0 * bs[j] + b1 * bt[j];
+        f[3 * (size_t)b + j] -= f0;
+        f[3 * nbs + 3 * (size_t)b + j] -= tb;
+      }
+    }
+  }
+  if (error) *error = ctx->h_stats.error;
+  if (iterations) *iterations = ctx->h_stats.iterations;
+  return ctx->h_stats.converged ? SG_OK : SG_NOT_CONVERGED;
 }
 
 // One GeometricImpactFrictionMap::flow step of a sphere scene (cache forced NONE in 3D:
@@ -2207,108 +2617,15 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   SG_CUDA_TRY(cudaGetLastError());
 
   // Solve.
-  if (int r = ensure_solver_capacity(ctx, nb, nc)) return r;
-  if (int r = grow(ctx->vrun3, sizeof(double4_32a) * 2 * (size_t)nb)) return r;
   if (int r = grow(ctx->v2, sizeof(double) * 6 * (size_t)nb)) return r;
-  if (int r = prepare_contact_graph(ctx, nb, nc, ia, ib)) return r;
-  const int* off = ctx->body_off.as<int>();
-  const int* adj = ctx->body_adj.as<int>();
-  Contacts3 C{ia, ib, A.E, A.Aa, A.Ab, A.c, A.W, A.mu_out};
-  double4_32a* V = ctx->vrun3.as<double4_32a>();
-  k_vel_init3<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, C, A.r, ctx->v.as<double>(), ctx->minv.as<double>(),
-                                                ctx->Iinv.as<double>(), V);
-  SG_CUDA_TRY(cudaGetLastError());
-  SolveStats* sst = ctx->stats.as<SolveStats>();
-  GridBarrier* gb = ctx->barrier.as<GridBarrier>();
-  SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-  Gs3Args G;
-  G.nc = nc;
-  G.C = C;
-  G.minv = ctx->minv.as<double>();
-  G.Iinv = ctx->Iinv.as<double>();
-  G.perm = ctx->perm.as<int>();
-  G.r = A.r;
-  G.r_a = ctx->r3a.as<double>();
-  G.r_b = ctx->r3b.as<double>();
-  G.V = V;
-  G.st = sst;
-  G.gb = gb;
-  G.spin = ctx->spin_limit;
-  G.tol = ctx->cfg.tol;
-  G.max_iters = ctx->cfg.max_iters;
-  G.eval_every = ctx->cfg.eval_every;
-  if (ctx->cfg.precision == SG_PRECISION_FP32_REFINE) {
-    const size_t c = (size_t)std::max(nc, 1), b1 = (size_t)std::max(nb, 1);
-    if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
-    if (int r = grow(ctx->pk3, sizeof(float) * 31 * c)) return r;   // E 9, Aa 6, Ab 6, c 3, W 6, mu 1
-    if (int r = grow(ctx->pk_r, sizeof(float) * 3 * c)) return r;
-    if (int r = grow(ctx->v32, sizeof(float4) * 2 * b1)) return r;
-    if (int r = grow(ctx->minv32, sizeof(float) * b1)) return r;
-    if (int r = grow(ctx->Iinv32, sizeof(float) * 9 * b1)) return r;
-    float* f = ctx->pk3.as<float>();
-    Gs3m B;
-    B.ab = ctx->pk_ab.as<int2>();
-    B.E = f;
-    B.Aa = f + 9 * c;
-    B.Ab = f + 15 * c;
-    B.c = f + 21 * c;
-    B.W = f + 24 * c;
-    B.mu = f + 30 * c;
-    B.r = ctx->pk_r.as<float>();
-    B.V = ctx->v32.as<float4>();
-    B.minv = ctx->minv32.as<float>();
-    B.Iinv = ctx->Iinv32.as<float>();
-    B.v0 = ctx->v.as<double>();
-    B.body_off = off;
-    B.body_adj = adj;
-    B.nb = nb;
-    B.eval32 = (unsigned)ctx->check_interval;
-    B.work = nullptr;
-    k_pack3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), C, A.r, B, B.r);
-    k_body32<<<blocks_for(nb), kBlock, 0, s>>>(nb, V, ctx->minv.as<double>(), ctx->Iinv.as<double>(), B.V,
-                                              const_cast<float*>(B.minv), const_cast<float*>(B.Iinv));
-    SG_CUDA_TRY(cudaGetLastError());
-    void* args[] = {&G, &B};
-    const int grid = coop_grid(ctx, k_gs3_mixed, (long)ctx->num_sms * kGs3mBlock, kGs3mBlock, 1);
-    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-    SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_mixed, grid, kGs3mBlock, args, s));
-    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
-    ctx->kernel_launches += 2;
-  } else {
-    void* args[] = {&G};
-    const int grid = coop_grid(ctx, k_gs3, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
-    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs3, dim3(grid), dim3(kGs3Block), args, 0, s));
-    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
-  }
-  k_final_vel3<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, C, A.r, ctx->v.as<double>(), ctx->m.as<double>(),
-                                                 ctx->minv.as<double>(), ctx->Iw.as<double>(), ctx->Iinv.as<double>(),
-                                                 ctx->v2.as<double>());
-  k_extract3<<<blocks_for(nc), kBlock, 0, s>>>(nc, A.E, A.r, ctx->ab3.as<double>());
-  SG_CUDA_TRY(cudaGetLastError());
-  SG_CUDA_TRY(cudaMemcpyAsync(&ctx->h_stats, sst, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
-  SG_CUDA_TRY(cudaStreamSynchronize(s));
-  // pair write, plane write, assemble, vel init, gs, final velocity, extract
-  ctx->kernel_launches += 6 + (t > 0 ? 1 : 0);
-  if (ctx->h_stats.status == SG_DEVICE_TIMEOUT) {
-    set_error("a device-side wait exceeded its spin limit");
-    return SG_DEVICE_TIMEOUT;
-  }
-  if (ctx->h_stats.status == SG_CAPACITY) {
-    set_error("contact colouring exceeded 64 colours or its round limit");
-    return SG_CAPACITY;
-  }
-  ctx->gs_launches += 1;
-  ctx->contact_sweeps += (uint64_t)ctx->h_stats.sweeps64 * (uint64_t)nc;
-  ctx->contact_sweeps32 += (uint64_t)ctx->h_stats.sweeps32 * (uint64_t)nc;
-  ctx->contact_evals += (uint64_t)ctx->h_stats.evals * (uint64_t)nc;
-  ctx->contact_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nc;
-  ctx->body_lifts += (uint64_t)ctx->h_stats.lifts * (uint64_t)nb;
-  if (ctx->profile) {
-    float ms = 0.f;
-    SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
-    ctx->gs_ms += ms;
-  }
+  const Contacts3 C{ia, ib, A.E, A.Aa, A.Ab, A.c, A.W, A.mu_out};
+  // pair write, plane write, assemble
+  ctx->kernel_launches += 2 + (t > 0 ? 1 : 0);
+  if (int r = solve3_contacts(ctx, nb, nc, ia, ib, C, A.r, ctx->v.as<double>(), ctx->m.as<double>(),
+                              ctx->minv.as<double>(), ctx->Iw.as<double>(), ctx->Iinv.as<double>(),
+                              ctx->v2.as<double>(), ctx->ab3.as<double>(), ctx->cfg.tol, ctx->cfg.max_iters,
+                              ctx->cfg.eval_every))
+    return r;
   st.iterations = ctx->h_stats.iterations;
   st.succeeded = ctx->h_stats.converged;
   st.error = ctx->h_stats.error;

@@ -10,6 +10,10 @@
 //   ball2d_run  <scene file> <out file>: steps the scene through Ball2DSim::flow with the
 //               geometric, symplectic-Euler and stabilized impact-friction maps and writes each
 //               final (q, v); the test compares them with the same steps through the C ABI.
+//   solve_run   <problem file> <out file>: Sobogus::solve on a Ball2D problem with the map's extra
+//               relative velocities and Sobogus::solve3D on a sphere problem with extras; writes the
+//               impulses, v2, f, residual, sweeps and the solve order of each, which the test
+//               replays on the oracle.
 //
 // Scene file: little-endian doubles n, np, dt, gx, gy, mu, tol, max_iters, steps, then q (2n),
 // v (2n), r (n), m (n), plane x (2np), plane n (2np).
@@ -147,6 +151,8 @@ int test_no_device() {
   return EXIT_SUCCESS;
 }
 
+constexpr int kMaxSolveColors = 64;  // colour limit of the solver (SG_CAPACITY beyond it)
+
 int test_ball2d_run(const char* scene_path, const char* out_path) {
   std::ifstream in(scene_path, std::ios::binary);
   if (!in) return fail("cannot open the scene file");
@@ -200,6 +206,78 @@ int test_ball2d_run(const char* scene_path, const char* out_path) {
   return EXIT_SUCCESS;
 }
 
+// Problem file (little-endian doubles): 2D block nb, nc, max_iters, tol, m, v0, ia, ib, bases, CoR,
+// mu, nrel, drel, alpha, beta; then the 3D block nb, nc, max_iters, tol, m, Iw, Iinv, v0, ia, ib,
+// bases, arm_a, arm_b, CoR, mu, nrel, drel, alpha, beta (sizes as the solve calls take them).
+int test_solve_run(const char* problem_path, const char* out_path) {
+  std::ifstream in(problem_path, std::ios::binary);
+  if (!in) return fail("cannot open the problem file");
+  auto rd = [&in](size_t n) {
+    std::vector<double> x(n);
+    in.read(reinterpret_cast<char*>(x.data()), static_cast<std::streamsize>(sizeof(double) * n));
+    return x;
+  };
+  auto rdi = [&rd](size_t n) {
+    const std::vector<double> x = rd(n);
+    return std::vector<int32_t>(x.begin(), x.end());
+  };
+  std::ofstream out(out_path, std::ios::binary);
+  auto wr = [&out](const std::vector<double>& x) {
+    out.write(reinterpret_cast<const char*>(x.data()), static_cast<std::streamsize>(sizeof(double) * x.size()));
+  };
+  auto order_of = [](sg_ctx* ctx, size_t nc) {
+    std::vector<int32_t> order(nc), off(kMaxSolveColors + 1);
+    int32_t ncol = 0;
+    if (sg_last_solve_order(ctx, static_cast<int64_t>(nc), order.data(), off.data(), &ncol) !=
+        static_cast<int64_t>(nc))
+      throw Error(SG_BAD_INPUT, "sg_last_solve_order");
+    return std::vector<double>(order.begin(), order.end());
+  };
+  {  // Ball2D with nrel_extra, drel_extra
+    const std::vector<double> h = rd(4);
+    const size_t nb = static_cast<size_t>(h[0]), nc = static_cast<size_t>(h[1]);
+    const std::vector<double> m = rd(nb), v0 = rd(2 * nb);
+    const std::vector<int32_t> ia = rdi(nc), ib = rdi(nc);
+    const std::vector<double> bases = rd(4 * nc), CoR = rd(nc), mu = rd(nc), nrel = rd(nc), drel = rd(nc);
+    std::vector<double> alpha = rd(nc), beta = rd(nc), v2, f;
+    if (!in) return fail("short 2D problem");
+    Sobogus sob(SobogusSolverType::Balls2D, 1);
+    double err = 0.0;
+    unsigned its = 0;
+    sob.solve(m, v0, ia, ib, bases, CoR, mu, nrel, drel, static_cast<unsigned>(h[2]), h[3], alpha, beta, v2, f, err,
+              its);
+    wr(alpha);
+    wr(beta);
+    wr(v2);
+    wr(f);
+    wr({err, static_cast<double>(its)});
+    wr(order_of(sob.context(), nc));
+  }
+  {  // spheres with nrel_extra, drel_extra
+    const std::vector<double> h = rd(4);
+    const size_t nb = static_cast<size_t>(h[0]), nc = static_cast<size_t>(h[1]);
+    const std::vector<double> m = rd(nb), Iw = rd(9 * nb), Iinv = rd(9 * nb), v0 = rd(6 * nb);
+    const std::vector<int32_t> ia = rdi(nc), ib = rdi(nc);
+    const std::vector<double> bases = rd(9 * nc), arm_a = rd(3 * nc), arm_b = rd(3 * nc), CoR = rd(nc), mu = rd(nc);
+    const std::vector<double> nrel = rd(nc), drel = rd(2 * nc);
+    std::vector<double> alpha = rd(nc), beta = rd(2 * nc), v2, f;
+    if (!in) return fail("short 3D problem");
+    Sobogus sob(SobogusSolverType::RigidBodies3D, 1);
+    double err = 0.0;
+    unsigned its = 0;
+    sob.solve3D(m, Iw, Iinv, v0, ia, ib, bases, arm_a, arm_b, CoR, mu, nrel, drel, static_cast<unsigned>(h[2]),
+                h[3], alpha, beta, v2, f, err, its);
+    wr(alpha);
+    wr(beta);
+    wr(v2);
+    wr(f);
+    wr({err, static_cast<double>(its)});
+    wr(order_of(sob.context(), nc));
+  }
+  if (!out) return fail("cannot write the output file");
+  return EXIT_SUCCESS;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -214,6 +292,7 @@ int main(int argc, char** argv) {
     if (test == "identity") return test_identity();
     if (test == "no_device") return test_no_device();
     if (test == "ball2d_run" && argc == 4) return test_ball2d_run(argv[2], argv[3]);
+    if (test == "solve_run" && argc == 4) return test_solve_run(argv[2], argv[3]);
   } catch (const std::exception& e) {
     return fail(std::string("unexpected exception: ") + e.what());
   }

@@ -18,6 +18,10 @@ Run in a checkout that has the reference sources (default location given by
                                     ball2dcli/CMakeLists.txt:78-98
   sphere_inertia.json               the sphere mass/inertia known answer of
                                     rigidbody3dtests/rigidbody3d_inertia_tests.cpp:17-47
+  rigidbody2d_scenes.json           the reference's circle-only rigidbody2d scenes
+                                    (assets/rigidbody2d/**/*.xml) as scisim_gb300.scene_io
+                                    reads them (state, planes, map and solver settings), for the
+                                    GPU tests, which cannot read the reference's assets
 """
 from __future__ import annotations
 
@@ -136,6 +140,25 @@ def extract_sphere_inertia(ref):
     return [dict(r=float(r), density=float(rho), M=float(M), I=float(I), tol_M=float(tolM), tol_I=float(tolI))]
 
 
+def extract_rigidbody2d_scenes(ref):
+    import glob
+
+    from scisim_gb300 import scene_io
+    base = os.path.join(ref, "assets", "rigidbody2d")
+    out = []
+    for f in sorted(glob.glob(os.path.join(base, "**", "*.xml"), recursive=True)):
+        try:
+            sc = scene_io.load_rigidbody2d_scene(f)
+        except scene_io.SceneError:
+            continue
+        d = {k: (v.tolist() if isinstance(v, np.ndarray) else v) for k, v in sc.items()
+             if k not in ("dt_rational", "end_time")}
+        d["gravity"] = list(sc["gravity"])
+        d["xml"] = "assets/rigidbody2d/" + os.path.relpath(f, base)
+        out.append(d)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -162,6 +185,8 @@ def main():
         json.dump(extract_slope_scenes(args.ref), fh, indent=1)
     with open(os.path.join(HERE, "sphere_inertia.json"), "w") as fh:
         json.dump(extract_sphere_inertia(args.ref), fh, indent=1)
+    with open(os.path.join(HERE, "rigidbody2d_scenes.json"), "w") as fh:
+        json.dump(extract_rigidbody2d_scenes(args.ref), fh)
 
 
 if __name__ == "__main__":

@@ -1,6 +1,7 @@
 """bench.py's reference arm on the CPU: one JSON line with the keys and meanings the benchmark
 contract fixes (impl, metric, unit, value, cpu_baseline, e2e with no host-device bytes), and under a
-multi-rank launch only rank 0 works and prints.  Small sizes: the oracle's strip for a
+multi-rank launch only rank 0 works and prints.  With a GPU the arm steps the pile the GPU formed;
+without one (here) it pre-rolls a strip of the fill on the CPU: small sizes, the strip for a
 65,536-disc pile is 2,048 discs."""
 import json
 import os
@@ -10,7 +11,7 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-ARGS = ["--impl", "reference", "--steps", "1", "--warmup", "3", "--n", "65536", "--preroll", "60"]
+ARGS = ["--impl", "reference", "--steps", "1", "--warmup", "3", "--n", "65536", "--schedule", "60:50"]
 
 
 def run(env_extra):

@@ -77,3 +77,56 @@ def test_host_api_ball2d_maps_match_c_abi(host_test, gpulib, tmp_path):
             q, v, _ = ctx.flow(it, q, v)
         ctx.close()
         assert np.array_equal(got[k, 0], q) and np.array_equal(got[k, 1], v), k
+
+
+@pytest.mark.gpu
+def test_host_api_solves_with_extras_match_oracle(host_test, gpulib, oracle, tmp_path):
+    """Sobogus::solve (Ball2D) and Sobogus::solve3D (spheres) of the C++ interface with non-zero
+    nrel_extra / drel_extra, bit-exact with the oracle replaying the solve order each reports."""
+    from test_gpu_friction_solver import ball2d_problem, sphere_problem
+
+    rng = np.random.default_rng(11)
+    s2, v0, ia, ib, bases = ball2d_problem(gpulib)
+    nb2, nc2 = s2["r"].shape[0], ia.shape[0]
+    p2 = dict(m=s2["m"], v0=v0, ia=ia.astype(np.float64), ib=ib.astype(np.float64), bases=bases,
+              CoR=rng.uniform(0.0, 0.5, nc2), mu=np.full(nc2, 0.5), nrel=rng.normal(0.0, 0.05, nc2),
+              drel=rng.normal(0.0, 0.05, nc2), alpha=np.abs(rng.normal(0.0, 1e-3, nc2)),
+              beta=rng.normal(0.0, 1e-4, nc2))
+    s3, w0, Iw, Iinv, ja, jb, E, arm_a, arm_b = sphere_problem(gpulib)
+    nb3, nc3 = s3["r"].shape[0], ja.shape[0]
+    p3 = dict(m=s3["m"], Iw=Iw, Iinv=Iinv, v0=w0, ia=ja.astype(np.float64), ib=jb.astype(np.float64), bases=E,
+              arm_a=arm_a, arm_b=arm_b, CoR=np.full(nc3, s3["CoR"]), mu=np.full(nc3, s3["mu"]),
+              nrel=rng.normal(0.0, 0.02, nc3), drel=rng.normal(0.0, 0.02, 2 * nc3),
+              alpha=np.abs(rng.normal(0.0, 1e-4, nc3)), beta=rng.normal(0.0, 1e-5, 2 * nc3))
+    blob = np.concatenate([np.array([nb2, nc2, 500, 1e-9])] + list(p2.values()) +
+                          [np.array([nb3, nc3, 300, 1e-10])] + list(p3.values()))
+    prob, out = tmp_path / "problem.bin", tmp_path / "out.bin"
+    blob.astype("<f8").tofile(prob)
+    p = run(host_test, "solve_run", str(prob), str(out), timeout=600)
+    assert p.returncode == 0, p.stderr
+    got = np.fromfile(out, dtype="<f8")
+    o = 0
+
+    def take(n):
+        nonlocal o
+        o += n
+        return got[o - n:o]
+
+    g2 = dict(alpha=take(nc2), beta=take(nc2), v2=take(2 * nb2), f=take(2 * nb2))
+    err2, its2 = take(2)
+    order2 = take(nc2).astype(np.int32)
+    r2 = oracle.sobogus_solve_2d(s2["m"], v0, ia, ib, bases, p2["CoR"], p2["mu"], 1e-9, 500, alpha=p2["alpha"],
+                                 beta=p2["beta"], order=order2, nrel_extra=p2["nrel"], drel_extra=p2["drel"])
+    for k in g2:
+        assert np.array_equal(g2[k], r2[k]), k
+    assert err2 == r2["error"] and int(its2) == r2["iterations"]
+    g3 = dict(alpha=take(nc3), beta=take(2 * nc3), v2=take(6 * nb3), f=take(6 * nb3))
+    err3, its3 = take(2)
+    order3 = take(nc3).astype(np.int32)
+    assert o == got.shape[0]
+    r3 = oracle.sobogus_solve_3d(s3["m"], Iinv, Iw, w0, ja, jb, E, arm_a, arm_b, p3["CoR"], p3["mu"], 1e-10, 300,
+                                 alpha=p3["alpha"], beta=p3["beta"], order=order3, nrel_extra=p3["nrel"],
+                                 drel_extra=p3["drel"])
+    for k in g3:
+        assert np.array_equal(g3[k], r3[k]), k
+    assert err3 == r3["error"] and int(its3) == r3["iterations"]

@@ -100,3 +100,54 @@ def test_noalloc_rejects_oversized_and_invalid_problems(gpulib):
     ib[0] = 10_000
     status, _ = noalloc_solve(gpulib, m, v0, ia, ib, bases, 0.0, 0.5, 1e-9, 10)
     assert status == gpulib.SG_BAD_INPUT
+
+
+def lattice(n_side, seed):
+    """n_side^2 discs on a square lattice whose spacing lets each disc touch its 8 neighbours,
+    resting on a floor: about 4 contacts per body, near the scratch's contact limit at 128^2."""
+    rng = np.random.default_rng(seed)
+    r = 0.1
+    d = 2.0 * r / np.sqrt(2.0) * 0.999
+    i, j = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
+    idx = (i * n_side + j).reshape(-1)
+    q = np.stack([j.reshape(-1) * d, i.reshape(-1) * d + r * 0.999], axis=1)
+    m = rng.uniform(0.5, 2.0, n_side * n_side)
+    v = rng.normal(0, 0.5, (n_side * n_side, 2))
+    ia, ib = [], []
+    for di, dj in ((0, 1), (1, 0), (1, 1), (1, -1)):
+        ok = (i + di < n_side) & (j + dj >= 0) & (j + dj < n_side)
+        a = (i * n_side + j)[ok]
+        b = ((i + di) * n_side + (j + dj))[ok]
+        ia.append(np.minimum(a, b))
+        ib.append(np.maximum(a, b))
+    ia, ib = np.concatenate(ia), np.concatenate(ib)
+    order = np.lexsort((ib, ia))
+    ia, ib = ia[order], ib[order]
+    nrm = q[ia] - q[ib]
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    floor = idx[q[:, 1] <= r]
+    ia = np.concatenate([ia, floor]).astype(np.int32)
+    ib = np.concatenate([ib, np.full(floor.shape[0], -1)]).astype(np.int32)
+    nrm = np.concatenate([nrm, np.tile([0.0, 1.0], (floor.shape[0], 1))])
+    bases = np.stack([nrm[:, 0], nrm[:, 1], -nrm[:, 1], nrm[:, 0]], axis=1).reshape(-1)
+    return m, v.reshape(-1), ia, ib, bases
+
+
+def test_noalloc_at_the_scratch_limits(gpulib):
+    """Exactly 16,384 bodies and close to 65,536 contacts, bit-identical with the regular entry, twice;
+    then bodies with no contacts (v2 = v0, no friction impulse)."""
+    ctx = gpulib.Context()
+    m, v0, ia, ib, bases = lattice(128, 21)
+    assert m.shape[0] == 16384 and 64000 < ia.shape[0] <= 65536
+    for _ in range(2):
+        ref = ctx.sobogus_solve_2d(m, v0, ia, ib, bases, 0.2, 0.5, 1e-9, 60)
+        status, got = noalloc_solve(gpulib, m, v0, ia, ib, bases, 0.2, 0.5, 1e-9, 60)
+        assert status in (gpulib.SG_OK, gpulib.SG_NOT_CONVERGED)
+        for key in ("alpha", "beta", "v2", "f"):
+            assert np.array_equal(got[key], ref[key]), key
+        assert got["error"] == ref["error"] and got["iterations"] == ref["iterations"]
+    empty = np.zeros(0, np.int32)
+    status, got = noalloc_solve(gpulib, m, v0, empty, empty, np.zeros(0), 0.2, 0.5, 1e-9, 60)
+    assert status == gpulib.SG_OK
+    assert np.array_equal(got["v2"], v0) and not got["f"].any() and got["iterations"] == 0
+    ctx.close()
