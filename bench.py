@@ -164,11 +164,12 @@ def solver_kw(s, **over):
 
 
 # --------------------------------------------------------------------------- CPU leg
-def cpu_from_state(s, q, v, cache, steps, first_iteration):
+def cpu_from_state(s, q, v, cache, steps, first_iteration, budget_s=None):
     """The oracle (C++ restatement of SCISim + So-bogus, sequential block Gauss-Seidel in active-set
     order, one host thread) stepping the pile from the given state and impulse cache (the contacts and
     impulses of the step before, as the GPU left them) for `steps` steps at the full settings, each
-    step timed on the host clock.  Returns (contact-steps/s, description, per-step records)."""
+    step timed on the host clock; with budget_s, no step starts once that many seconds have gone
+    (at least one step runs).  Returns (contact-steps/s, description, per-step records)."""
     from oracle import oracle as O  # the oracle: CPU baseline only
     O.build()
     kw = solver_kw(s)
@@ -178,6 +179,8 @@ def cpu_from_state(s, q, v, cache, steps, first_iteration):
     sim.iteration = first_iteration - 1
     recs, tot, wall = [], 0, 0.0
     for _ in range(steps):
+        if budget_s is not None and recs and wall >= budget_s:
+            break
         t0 = time.perf_counter()
         st = sim.step()
         dt = time.perf_counter() - t0
@@ -189,7 +192,7 @@ def cpu_from_state(s, q, v, cache, steps, first_iteration):
     desc = ("oracle (C++ restatement of SCISim + So-bogus: grid broad phase, CCD, sequential block Gauss-Seidel "
             "in active-set order, 1 host thread) on the full %d-disc pile from the GPU's state and impulse cache, "
             "%d steps at the full settings: %d contact-steps in %.2f s, %d of %d steps converged, residuals %s, "
-            "sweeps %s" % (s["r"].shape[0], steps, tot, wall, conv, steps,
+            "sweeps %s" % (s["r"].shape[0], len(recs), tot, wall, conv, len(recs),
                            [float("%.3g" % r["residual"]) for r in recs], [r["sweeps"] for r in recs]))
     return (tot / wall if wall > 0 else None), desc, recs
 
@@ -295,9 +298,10 @@ def run_reference(args):
         q, v = ctx.state()
         cache = ctx.last_contacts()
         ctx.close()
-        value, desc, recs = cpu_from_state(s, q, v, cache, args.steps, it)
+        value, desc, recs = cpu_from_state(s, q, v, cache, args.steps, it, args.cpu_budget)
         sample = "the full %d-disc pile from the GPU-formed state (%s)" % (s["r"].shape[0], pile_note(info))
         conv = {"steps_converged": sum(r["converged"] for r in recs), "steps": len(recs),
+                "budget_s": args.cpu_budget,
                 "max_residual": max(r["residual"] for r in recs) if recs else None,
                 "sweeps_per_step": [r["sweeps"] for r in recs]}
         same = True
@@ -739,6 +743,12 @@ def run_ours(args):
     fast, s, it0, pile = form_pile(args, local)
     nb = s["r"].shape[0]
     stream = torch.cuda.ExternalStream(fast.stream_ptr(), device=local)
+    # The state every arm starts from: positions, velocities and the impulse cache (the last step's
+    # contacts and impulses; a restored context has no last step, so this is read before the
+    # autotuner's trials, which end by restoring this state).
+    ck = fast.checkpoint()
+    q_snap, v_snap = fast.state()
+    cache = fast.last_contacts()
     # Autotuner: each candidate tuning timed over a few steps from this state, which it restores.
     autotune = None
     if args.autotune_steps > 0:
@@ -748,10 +758,6 @@ def run_ours(args):
                     "ms_per_step": [None if np.isnan(x) else round(float(x), 3) for x in tms],
                     "candidates": "two-level on: check interval 8, 16, 32; two-level off: 8, 16, 32"}
         log("autotune in %.1f s: %s" % (time.perf_counter() - t0, autotune))
-    # The state every arm starts from: positions, velocities and the impulse cache.
-    ck = fast.checkpoint()
-    q_snap, v_snap = fast.state()
-    cache = fast.last_contacts()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     fast.profile_enable(True)
     fast.profile_read(reset=True)
@@ -792,12 +798,13 @@ def run_ours(args):
     # Plain FP64 Gauss-Seidel from the same state: with the impulse cache, then cold (one step,
     # a larger sweep cap).
     plain = plain_cold = None
-    if args.plain_steps > 0:
+    plain_steps = args.steps if args.plain_steps is None else args.plain_steps
+    if plain_steps > 0:
         pctx = arm(precision=_lib.PRECISION_FP64)
         pms, pc, precs = timed_steps(pctx, torch, torch.cuda.ExternalStream(pctx.stream_ptr(), device=local),
-                                     args.plain_steps, flush, it0)
+                                     plain_steps, flush, it0)
         pst = pctx.profile_read()
-        plain = {"value": sum(pc) / (sum(pms) / 1e3), "unit": UNIT, "steps": args.plain_steps,
+        plain = {"value": sum(pc) / (sum(pms) / 1e3), "unit": UNIT, "steps": plain_steps,
                  "ms_per_step": sum(pms) / len(pms), "convergence": convergence_record(precs),
                  "form": "FP64 sweeps, warm start from the impulse cache, same state and steps"}
         log("plain FP64 (cache):", plain)
@@ -859,7 +866,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
-        v, desc, crecs = cpu_from_state(s, q_snap, v_snap, cache, args.cpu_steps, it0)
+        v, desc, crecs = cpu_from_state(s, q_snap, v_snap, cache, args.cpu_steps, it0, args.cpu_budget)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
         log("cpu:", cpu)
 
@@ -881,7 +888,7 @@ def run_ours(args):
                 "fp32_sweep_share": prof["contact_sweeps32"] / max(prof["contact_sweeps"] + prof["contact_sweeps32"], 1),
                 "fp64_start_solves": prof["fp64_start_solves"], "stage_ms_per_step": stages,
                 "plain_fp64_gpu": plain,
-                "warm_over_plain": (value / ws) / plain["value"] if plain else None,
+                "warm_over_plain": (value / ws) / plain["value"] if plain and plain["steps"] == args.steps else None,
                 "plain_fp64_cold_gpu": plain_cold,
                 "warm_over_plain_cold": (value / ws) / plain_cold["value"] if plain_cold else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
@@ -908,11 +915,14 @@ def main():
                     help="settling ends after this many consecutive converged steps at the full settings")
     ap.add_argument("--settle-max", type=int, default=200, help="settling steps at most")
     ap.add_argument("--preroll-iters", type=int, default=50, help="sweep cap of the other legs' pre-rolls")
-    ap.add_argument("--plain-steps", type=int, default=5)
+    ap.add_argument("--plain-steps", type=int, default=None,
+                    help="steps of the plain FP64 arm (default: --steps, the timed steps themselves)")
     ap.add_argument("--cold-steps", type=int, default=1)
     ap.add_argument("--cold-iters", type=int, default=20000)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=60.0,
+                    help="seconds of oracle stepping after which the CPU legs start no further step")
     ap.add_argument("--precision", type=int, default=1, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
     ap.add_argument("--batch-scenes", type=int, default=512, help="batched-scene leg (0 = skip)")
     ap.add_argument("--batch-preroll", type=int, default=40)

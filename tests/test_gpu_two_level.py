@@ -1,11 +1,12 @@
 """Two-level FP32 sweeps (spatial patches on shared-memory velocities, contacts between patches
 by shifted tile, the rest over the grid) on a dense pile large enough to use them.
 
-Bars: the two-level path runs; every step that reports convergence meets the tolerance under
+Bars, from a settled pile (a checkpoint taken after a converged step): the two-level path runs;
+at least one step converges, and every step that reports convergence meets the tolerance under
 the oracle's FP64 residual of the GPU's impulses; the reported residual equals the oracle's
-evaluation; positions stay within 5e-3 of the one-level FP32 solve and of FP64 after four
-steps from a common state (both are Gauss-Seidel orders of a solve that hits its iteration cap
-in this still-settling pile, so their iterates differ within the residual they reach).
+evaluation; positions stay within 5e-3 of the one-level FP32 solve and of FP64 after four steps
+from the common state (different Gauss-Seidel orders of a frictional solve, whose solution set is
+not a single point, so their iterates differ within the residual they reach).
 """
 import numpy as np
 import pytest
@@ -27,24 +28,45 @@ def pile(gpulib, s, **kw):
 def test_two_level_sweeps(gpulib, oracle):
     n = 32768
     s = scenes.dense_pile(n=n, seed=2, width=20.0, height=15.0)
-    # Form the pile once (capped solves), then start all three solvers from that state.
+    # Form the pile (capped solves), settle it at the full settings until a step converges, then
+    # start all three solvers from that state and impulse cache (a checkpoint).
     pre = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE, max_iters=50)
-    pre.step(420)
-    q, v = pre.state()
-    s = dict(s, q=q, v=v)
-    two = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE)
-    one = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE)
+    it = 1
+    for steps, cap in ((420, 50), (200, 200), (100, 1000)):
+        pre.reconfigure(max_iters=cap)
+        pre.step(steps, first_iteration=it)
+        it += steps
+    pre.reconfigure(max_iters=2000)
+    for _ in range(200):
+        st = pre.step(1, first_iteration=it)
+        it += 1
+        if st["succeeded"]:
+            break
+    assert st["succeeded"]
+    ck = pre.checkpoint()
+    pre.close()
+
+    def from_ck(**kw):
+        c = gpulib.Context(dt=s["dt"], gravity=s["gravity"])
+        c.restore(ck)
+        c.reconfigure(**kw)
+        return c
+
+    two = from_ck(precision=gpulib.PRECISION_FP32_REFINE)
+    one = from_ck(precision=gpulib.PRECISION_FP32_REFINE)
+    f64 = from_ck(precision=gpulib.PRECISION_FP64)
+    # FP32 sweeps from the start (no FP64 start near the tolerance), so the two-level path runs.
+    for c in (two, one):
+        c.set_tuning(fp64_factor=0)
     one.set_two_level(False)
-    f64 = pile(gpulib, s)
     two.profile_enable(True)
     two.profile_read(reset=True)
     checked = 0
-    for _ in range(4):
+    for j in range(4):
         q0, v0 = two.state()
-        st = two.step(1)
+        st = two.step(1, first_iteration=it + j)
         g = two.last_contacts()
         assert st["n_contacts"] >= 20000
-        nb = s["r"].shape[0]
         bases = np.concatenate([g["n"], np.stack([-g["n"][:, 1], g["n"][:, 0]], 1)], 1).reshape(-1)
         ib = np.where(g["ib"] >= 0, g["ib"], -1)
         res = oracle.residual_2d(s["m"], v0, g["ia"], ib, bases, s["CoR"], s["mu"], g["alpha"], g["beta"])
@@ -52,10 +74,11 @@ def test_two_level_sweeps(gpulib, oracle):
         if st["succeeded"]:
             assert res <= 1e-6 * 1.001
             checked += 1
-        one.step(1)
-        f64.step(1)
+        one.step(1, first_iteration=it + j)
+        f64.step(1, first_iteration=it + j)
     prof = two.profile_read()
-    assert prof["two_level_solves"] == 4
+    assert checked > 0
+    assert prof["two_level_solves"] >= 1
     qa, _ = two.state()
     qb, _ = one.state()
     qc, _ = f64.state()
