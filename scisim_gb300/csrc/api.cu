@@ -58,6 +58,23 @@ static int upload(sg_ctx* ctx, Buf& b, const void* host, size_t bytes) {
   return SG_OK;
 }
 
+// One block per scene when every scene's bodies fit in a block's shared memory (max_bodies): the
+// work list takes the scenes largest first (ties in scene order); s_smax = 0 selects the grid-wide
+// batched sweeps instead.
+static int scene_work_order(sg_ctx* ctx, int S, const int32_t* body_off, int max_bodies) {
+  std::vector<int> order(S);
+  int smax = 0;
+  for (int k = 0; k < S; ++k) {
+    order[k] = k;
+    smax = std::max(smax, body_off[k + 1] - body_off[k]);
+  }
+  std::stable_sort(order.begin(), order.end(), [body_off](int x, int y) {
+    return body_off[x + 1] - body_off[x] > body_off[y + 1] - body_off[y];
+  });
+  ctx->s_smax = smax <= max_bodies ? std::max(smax, 1) : 0;
+  return upload(ctx, ctx->s_order, order.data(), sizeof(int) * (size_t)S);
+}
+
 static int validate_config(const sg_config* c) {
   if (!c) return SG_BAD_INPUT;
   if (c->integrator != SG_SYMPLECTIC_EULER && c->integrator != SG_VERLET && c->integrator != SG_SPLIT_HAM)
@@ -253,7 +270,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->prev_sc_off, &ctx->cscene, &ctx->b_ctl,     &ctx->b_sums,   &ctx->s_err,   &ctx->s_best,
                   &ctx->s_bestbuf, &ctx->s_done, &ctx->s_iters,     &ctx->snap_q,   &ctx->snap_v,  &ctx->snap_key,
                   &ctx->snap_ab, &ctx->snap_off, &ctx->s_mode, &ctx->s_since, &ctx->s_exc, &ctx->s_gmax,
-                  &ctx->b_work, &ctx->pk_scene};
+                  &ctx->b_work, &ctx->pk_scene, &ctx->s_kcnt, &ctx->s_kstart, &ctx->s_kfill, &ctx->s_sperm,
+                  &ctx->s_order, &ctx->s_next};
   for (Buf* b : bufsb) release(*b);
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
   Buf* bufs[] = {&ctx->q, &ctx->v, &ctx->r, &ctx->m, &ctx->minv, &ctx->q1, &ctx->v1, &ctx->v2, &ctx->plane_x,
@@ -263,7 +281,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                  &ctx->r_loc, &ctx->r_cand, &ctx->r_best, &ctx->key, &ctx->ab, &ctx->prev_key, &ctx->prev_ab,
                  &ctx->color, &ctx->perm, &ctx->body_cnt, &ctx->body_off, &ctx->body_fill, &ctx->body_adj,
                  &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2,
-                 &ctx->fs_I, &ctx->fs_in};
+                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->vdelta, &ctx->rb_I, &ctx->rb_Iinv,
+                 &ctx->pos0, &ctx->pos1, &ctx->rb_ct, &ctx->rb_vrun};
   for (Buf* b : bufs) release(*b);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->ev_gs0) cudaEventDestroy(ctx->ev_gs0);
@@ -565,6 +584,7 @@ static int batch_upload(sg_ctx* ctx, int32_t S, const int32_t* body_off, const d
   SG_CUDA_TRY(cudaMemsetAsync(ctx->prev_sc_off.p, 0, s1, ctx->stream));
   SG_CUDA_TRY(cudaMemsetAsync(ctx->sc_off.p, 0, s1, ctx->stream));
   SG_CUDA_TRY(cudaMemsetAsync(ctx->b_ctl.p, 0, 4 * sizeof(int), ctx->stream));
+  if (int e = scene_work_order(ctx, S, body_off, kSceneBlockMaxBodies)) return e;
   if (int e = batch2d_reserve(ctx, std::max(3 * N + 1024, ctx->bcap))) return e;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -877,6 +897,7 @@ int sg_sphere3d_batch_upload(sg_ctx* ctx, int32_t S, const int32_t* body_off, co
   if (int e = upload(ctx, ctx->s_mu, mu, sizeof(double) * (size_t)S)) return e;
   if (int e = upload(ctx, ctx->s_CoR, CoR, sizeof(double) * (size_t)S)) return e;
   if (int e = sphere3d_batch_setup(ctx, sf[S], cells)) return e;
+  if (int e = scene_work_order(ctx, S, body_off, kScene3MaxBodies)) return e;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }
@@ -1224,8 +1245,13 @@ std::vector<CkptPart> ckpt_parts(sg_ctx* ctx, int dim, int nb, int np, int64_t p
          {&ctx->Iw, 9 * b * d},  {&ctx->Iinv, 9 * b * d},      {&ctx->plane_x, 3 * p * d},
          {&ctx->plane_n, 3 * p * d}};
   }
+  // The impulse cache: (alpha, beta) per Ball2D contact; the cached normal and force (6) per
+  // sphere contact (symplectic-Euler staggering; the geometric sphere map keeps none).
   v.push_back({&ctx->prev_key, (size_t)prev_n * sizeof(unsigned long long)});
-  v.push_back({&ctx->prev_ab, (size_t)prev_n * 2 * d});
+  if (dim == 2)
+    v.push_back({&ctx->prev_ab, (size_t)prev_n * 2 * d});
+  else
+    v.push_back({&ctx->prev_c6, (size_t)prev_n * 6 * d});
   return v;
 }
 

@@ -1031,9 +1031,19 @@ int batch2d_reserve(sg_ctx* ctx, int cap) {
   if (int r = grow(ctx->s_exc, sizeof(unsigned long long) * 3 * S)) return r;
   if (int r = grow(ctx->s_gmax, sizeof(unsigned long long) * 3)) return r;
   if (int r = grow(ctx->b_work, sizeof(unsigned long long) * 5)) return r;
+  // One block per scene: (scene, colour) keys and the contacts in their order.
+  const size_t keys = S * kMaxColors + 1;
+  if (ctx->s_smax > 0) {
+    if (int r = grow(ctx->s_kcnt, sizeof(int) * keys)) return r;
+    if (int r = grow(ctx->s_kstart, sizeof(int) * keys)) return r;
+    if (int r = grow(ctx->s_kfill, sizeof(int) * keys)) return r;
+    if (int r = grow(ctx->s_sperm, sizeof(int) * c)) return r;
+    if (int r = grow(ctx->s_next, sizeof(int))) return r;
+    if (int r = scene_blocks_prepare(ctx->s_smax)) return r;
+  }
   // Scan scratch for the largest scan of a step, so that nothing allocates while capturing.
   const long big = std::max<long>({(long)ctx->nb + 1, ctx->bcells + 1, ctx->bflags + 1, (long)ctx->n_scenes + 1,
-                                   (long)c});
+                                   (long)c, (long)keys});
   if (int r = grow(ctx->scan_tmp, sizeof(int) * (size_t)(scan_tile_count((int)big) + 2))) return r;
   ctx->bcap = (int)c;
   ctx->ccap = std::min<int64_t>(ctx->ccap, (int64_t)c);
@@ -1149,6 +1159,17 @@ int batch2d_step_enqueue(sg_ctx* ctx) {
   X.gmax = ctx->s_gmax.as<unsigned long long>();
   X.work = ctx->b_work.as<unsigned long long>();
   X.n64 = ctl + 3;
+  if (ctx->s_smax > 0) {
+    X.scene_blocks = true;
+    X.sb_off = ctx->sb_off.as<int>();
+    X.key_cnt = ctx->s_kcnt.as<int>();
+    X.key_start = ctx->s_kstart.as<int>();
+    X.key_fill = ctx->s_kfill.as<int>();
+    X.sperm = ctx->s_sperm.as<int>();
+    X.order = ctx->s_order.as<int>();
+    X.next = ctx->s_next.as<int>();
+    X.smax = ctx->s_smax;
+  }
   SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, ctx->cfg.precision};
   if (int r = solve_contacts_batch(ctx, P, sp, X)) return r;
   k_extract<<<blocks_for(cap), kBlock, 0, s>>>(cap, ctl, ctx->n.as<double2>(), ctx->r_loc.as<double2>(),

@@ -101,6 +101,16 @@ struct BatchSolve {
   unsigned long long* gmax = nullptr;      // 3
   unsigned long long* work = nullptr;      // 5 counters (FP32 / FP64 updates, evaluations, lifts)
   int* n64 = nullptr;                      // scenes in FP64 mode
+  // One block per scene (scene_blocks): every scene's bodies fit in a block's shared memory.
+  bool scene_blocks = false;
+  const int* sb_off = nullptr;      // S + 1 body offsets
+  int* key_cnt = nullptr;           // S * kMaxColors + 1 (scene, colour) counts
+  int* key_start = nullptr;         // their exclusive scan
+  int* key_fill = nullptr;
+  int* sperm = nullptr;             // contacts by (scene, colour)
+  const int* order = nullptr;       // scenes, largest first
+  int* next = nullptr;              // work-list counter
+  int smax = 0;                     // bodies of the largest scene
 };
 
 struct SolveParams {
@@ -146,6 +156,9 @@ struct sg_ctx {
   sg::Buf ia, ib, n, c, W, mu, r_loc, r_cand, r_best, key, ab;
   // impulse cache of the previous step (sorted keys and (alpha, beta))
   sg::Buf prev_key, prev_ab;
+  // Sphere scenes under the symplectic-Euler staggering: 6 doubles per contact (cached normal and
+  // force), this step's and the step before's.
+  sg::Buf c6, prev_c6;
   int64_t prev_n = 0;
 
   // solver
@@ -205,6 +218,11 @@ struct sg_ctx {
   sg::Buf sb_off, sp_off, sf_off, scene_of, s_mu, s_CoR, s_grid, s_cells, s_cell_off, s_nc, s_npairs;
   sg::Buf sc_off, prev_sc_off, cscene, b_ctl, b_sums;
   sg::Buf s_err, s_best, s_bestbuf, s_done, s_iters, s_mode, s_since, s_exc, s_gmax, b_work, pk_scene;
+  // One block per scene: (scene, colour) counts, their scan and fill, the contacts in that order,
+  // the scenes largest first and the work-list counter; s_smax = bodies of the largest scene
+  // (0: a scene exceeds a block's shared memory, grid-wide sweeps instead).
+  sg::Buf s_kcnt, s_kstart, s_kfill, s_sperm, s_order, s_next;
+  int s_smax = 0;
   sg::Buf snap_q, snap_v, snap_key, snap_ab, snap_off;
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_launches = 0;  // kernel launches per graph replay
@@ -307,6 +325,12 @@ int coop_grid(sg_ctx* ctx, K kernel, long work, int block, int max_per_sm = 64) 
 // capture) and one step enqueued without host synchronisation.
 int batch2d_reserve(sg_ctx* ctx, int cap);
 int batch2d_step_enqueue(sg_ctx* ctx);
+// One block per scene: scenes of at most this many discs (24 B of shared memory each) or spheres
+// (64 B each) are swept by one block; the per-scene kernels' shared-memory limits are set by
+// scene_blocks_prepare (once per context, outside any capture).
+constexpr int kSceneBlockMaxBodies = 8192;
+constexpr int kScene3MaxBodies = 3072;
+int scene_blocks_prepare(int smax);
 
 // Learned warm start (mlp_kernels.cu).
 int mlp_param_count();

@@ -2242,6 +2242,345 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed_batch(GsMixedBatchAr
   }
 }
 
+// ---------------------------------------------------------------------------
+// Batched scenes, one scene per block.  A scene's bodies fit in a block's shared memory, so the
+// block sweeps the scene's contacts colour by colour (the global colouring restricted to the scene:
+// contacts ordered by (scene, colour)) with block barriers only, keeps the running velocities in
+// shared memory, evaluates the scene's own residual, keeps its best iterate and stops at tol or
+// max_iters.  Blocks take scenes from a largest-first work list.
+//
+// kMixed = false: FP64 sweeps, each scene seeing k_gs_batch's update sequence (the same results).
+// kMixed = true (SG_PRECISION_FP32_REFINE): FP32 sweeps over colour-packed FP32 copies; on a
+// doubling-then-adaptive schedule the FP32 iterate is lifted to FP64 (impulses, then velocities
+// gathered from v0 and the impulses), its FP64 residual evaluated, and the scene turns to FP64
+// sweeps once the residual reaches tol or the FP32 rounding floor (as k_gs_mixed_batch per scene).
+constexpr int kSceneBlock = 256;
+
+struct SceneBlockArgs {
+  GsArgs g;                 // FP64 contacts, impulses (g.r), snapshot buffers g.r_a / g.r_b
+  Gs32Args f;               // FP32 copies in (scene, colour) order (kMixed), v0, minv64, body adjacency
+  const double2* v;         // running velocities at the start (warm start)
+  const int* sb_off;        // S + 1 body offsets
+  const int* sc_off;        // S + 1 contact offsets
+  const int* key_start;     // S * kMaxColors + 1: (scene, colour) runs of sperm
+  const int* sperm;         // contacts by (scene, colour)
+  const int* order;         // scenes, largest first
+  int* next;                // work-list counter
+  int S;
+  int smax;                 // shared-memory body slots (the largest scene)
+  double* best;
+  int* done;
+  unsigned* iters;
+  unsigned long long* unconverged;
+  unsigned long long* work;  // [0] FP32 updates, [1] FP64 updates, [2] evaluations, [3] contact lifts, [4] body lifts
+};
+
+// gs_update's arithmetic on shared-memory velocities (la, lb: the bodies' slots; lb < 0 for a plane).
+__device__ __forceinline__ void gs_update_sv(const GsArgs& A, int k, int a, int b, int la, int lb, double2* sv) {
+  const double2 nk = A.n[k], ck = A.c[k];
+  const double2 va = sv[la];
+  const bool has_b = lb >= 0;
+  const double2 vb = has_b ? sv[lb] : make_double2(0.0, 0.0);
+  double u0, u1;
+  local_velocity(nk, ck, va, has_b, vb, u0, u1);
+  const double2 rk = A.r[k];
+  const double r0 = rk.x, r1 = rk.y;
+  const double w00 = A.W[3 * k], w01 = A.W[3 * k + 1], w11 = A.W[3 * k + 2];
+  const double bt0 = u0 - (w00 * r0 + w01 * r1);
+  const double bt1 = u1 - (w01 * r0 + w11 * r1);
+  double rn0, rn1;
+  local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
+  const double d0 = rn0 - r0, d1 = rn1 - r1;
+  const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  const double px = nx * d0 + tx * d1;
+  const double py = ny * d0 + ty * d1;
+  const double ma = A.minv[a];
+  sv[la] = make_double2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const double mb = A.minv[b];
+    sv[lb] = make_double2(vb.x - mb * px, vb.y - mb * py);
+  }
+  A.r[k] = make_double2(rn0, rn1);
+}
+
+// gs_update32's arithmetic on shared-memory FP32 velocities; q indexes the (scene, colour) packing.
+__device__ __forceinline__ void gs_update32_sv(const Gs32Args& B, int q, int b0, float2* sv) {
+  const int2 ab = B.ab[q];
+  const float2 nk = B.n[q], ck = B.c[q];
+  const float4 w = B.w[q];
+  const int la = ab.x - b0;
+  const bool has_b = ab.y >= 0;
+  const int lb = has_b ? ab.y - b0 : -1;
+  const float2 va = sv[la];
+  const float2 vb = has_b ? sv[lb] : make_float2(0.0f, 0.0f);
+  const float nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
+  float hn = nx * va.x + ny * va.y;
+  float ht = tx * va.x + ty * va.y;
+  if (has_b) {
+    hn -= nx * vb.x + ny * vb.y;
+    ht -= tx * vb.x + ty * vb.y;
+  }
+  const float u0 = hn + ck.x, u1 = ht + ck.y;
+  const float2 rk = B.r[q];
+  const float bt0 = u0 - (w.x * rk.x + w.y * rk.y);
+  const float bt1 = u1 - (w.y * rk.x + w.z * rk.y);
+  float rn0, rn1;
+  local_solve_2d_f(w.x, w.y, w.z, bt0, bt1, w.w, rn0, rn1);
+  const float d0 = rn0 - rk.x, d1 = rn1 - rk.y;
+  const float px = nx * d0 + tx * d1, py = ny * d0 + ty * d1;
+  const float ma = B.minv[ab.x];
+  sv[la] = make_float2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const float mb = B.minv[ab.y];
+    sv[lb] = make_float2(vb.x - mb * px, vb.y - mb * py);
+  }
+  B.r[q] = make_float2(rn0, rn1);
+}
+
+// Block-wide nanmax of a (residual) and plain max of x (floor excess); every thread gets both.
+__device__ __forceinline__ void block_max2(double& a, double& x, double* s_red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a = nanmax(a, __shfl_down_sync(0xffffffffu, a, o));
+    x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    s_red[wid] = a;
+    s_red[32 + wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    a = lane < nw ? s_red[lane] : 0.0;
+    x = lane < nw ? s_red[32 + lane] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) {
+      a = nanmax(a, __shfl_down_sync(0xffffffffu, a, o));
+      x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+    }
+    if (lane == 0) {
+      s_red[64] = a;
+      s_red[65] = x;
+    }
+  }
+  __syncthreads();
+  a = s_red[64];
+  x = s_red[65];
+  __syncthreads();
+}
+
+template <bool kMixed>
+__global__ void __launch_bounds__(kSceneBlock) k_gs_scenes(SceneBlockArgs Z) {
+  const GsArgs& A = Z.g;
+  const Gs32Args& F = Z.f;
+  extern __shared__ __align__(16) double2 sv64[];
+  float2* sv32 = reinterpret_cast<float2*>(sv64 + Z.smax);
+  __shared__ int s_w;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ double s_red[66];
+  if (*((volatile int*)&A.st->status) != 0) return;  // the colouring failed
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  const unsigned eval32 = F.eval32 ? F.eval32 : 1u;
+  double2* bufs[2] = {A.r_a, A.r_b};
+  unsigned long long n32 = 0, n64 = 0, nev = 0, nlc = 0, nlb = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_w = atomicAdd(Z.next, 1);
+    __syncthreads();
+    const int w = s_w;
+    __syncthreads();
+    if (w >= Z.S) break;
+    const int sc = Z.order[w];
+    const int b0 = Z.sb_off[sc], nbs = Z.sb_off[sc + 1] - b0;
+    const int c0 = Z.sc_off[sc], c1 = Z.sc_off[sc + 1];
+    if (c1 == c0) {
+      if (threadIdx.x == 0) {
+        Z.done[sc] = 1;
+        Z.iters[sc] = 0;
+        Z.best[sc] = INFINITY;
+      }
+      continue;
+    }
+    for (int j = threadIdx.x; j < nbs; j += blockDim.x) {
+      const double2 vj = Z.v[b0 + j];
+      sv64[j] = vj;
+      if (kMixed) sv32[j] = make_float2((float)vj.x, (float)vj.y);
+    }
+    for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x)
+      s_off[c] = c < kMaxColors ? Z.key_start[sc * kMaxColors + c] : Z.key_start[(sc + 1) * kMaxColors];
+    __syncthreads();
+    int ncol = kMaxColors;
+    while (ncol > 0 && s_off[ncol] == s_off[ncol - 1]) --ncol;
+    // Per-scene state, the same in every thread.
+    double err_best = INFINITY;
+    int bestbuf = 0;
+    bool converged = false;
+    int mode = kMixed ? 0 : 1;
+    unsigned since = 0, next_eval = 1, interval = eval32;
+    unsigned it;
+    for (it = 1; it <= A.max_iters; ++it) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        if (mode == 0) {
+          for (int q = s_off[col] + threadIdx.x; q < e; q += blockDim.x) {
+            gs_update32_sv(F, q, b0, sv32);
+            ++n32;
+          }
+        } else {
+          for (int q = s_off[col] + threadIdx.x; q < e; q += blockDim.x) {
+            const int k = Z.sperm[q];
+            const int a = A.ia[k], b = A.ib[k];
+            gs_update_sv(A, k, a, b, a - b0, b >= 0 ? b - b0 : -1, sv64);
+            ++n64;
+          }
+        }
+        __syncthreads();
+      }
+      const bool due = mode == 0 ? (it == next_eval || it == A.max_iters)
+                                 : (it % eval64 == 0 || (kMixed && it == A.max_iters));
+      if (!due) continue;
+      if (mode == 0) {
+        // Lift: FP64 impulses from the FP32 ones, then each body's FP64 velocity from v0 and them.
+        for (int q = s_off[0] + threadIdx.x; q < s_off[ncol]; q += blockDim.x) {
+          const float2 r32 = F.r[q];
+          A.r[Z.sperm[q]] = make_double2((double)r32.x, (double)r32.y);
+          ++nlc;
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < nbs; j += blockDim.x) {
+          const int i = b0 + j;
+          double hx = 0.0, hy = 0.0;
+          const int e = F.body_off[i + 1];
+          for (int p = F.body_off[i]; p < e; ++p) {
+            const int k = F.body_adj[p];
+            const double sgn = (A.ia[k] == i) ? 1.0 : -1.0;
+            const double2 nk = A.n[k], rk = A.r[k];
+            const double px = nk.x * rk.x + (-nk.y) * rk.y;
+            const double py = nk.y * rk.x + nk.x * rk.y;
+            hx = hx + sgn * px;
+            hy = hy + sgn * py;
+          }
+          const double2 a0 = F.v0[i];
+          const double mi = F.minv64[i];
+          const double2 vi = make_double2(a0.x + mi * hx, a0.y + mi * hy);
+          sv64[j] = vi;
+          sv32[j] = make_float2((float)vi.x, (float)vi.y);
+          ++nlb;
+        }
+        __syncthreads();
+      }
+      // FP64 residual of the scene (and, in FP32 mode, its excess over the FP32 rounding floor).
+      double emax = 0.0, xmax = -INFINITY;
+      double2* cand = bufs[1 - bestbuf];
+      for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) {
+        const int a = A.ia[k], b = A.ib[k];
+        const bool has_b = b >= 0;
+        const double2 va = sv64[a - b0];
+        const double2 vb = has_b ? sv64[b - b0] : make_double2(0.0, 0.0);
+        const double2 ck = A.c[k];
+        double u0, u1;
+        local_velocity(A.n[k], ck, va, has_b, vb, u0, u1);
+        const double2 rk = A.r[k];
+        cand[k] = rk;
+        const double ek = fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]);
+        emax = nanmax(emax, ek);
+        if (kMixed && mode == 0) {
+          const double scale = fabs(va.x) + fabs(va.y) + fabs(vb.x) + fabs(vb.y) + fabs(ck.x) + fabs(ck.y) +
+                               fabs(rk.x) + fabs(rk.y);
+          xmax = fmax(xmax, ek - 64.0 * 1.1920929e-7 * scale);
+        }
+        ++nev;
+      }
+      block_max2(emax, xmax, s_red);
+      const double err = emax;
+      if (err < err_best) {
+        err_best = err;
+        bestbuf ^= 1;
+        since = 0;
+      } else {
+        ++since;
+      }
+      if (mode == 1) {
+        if (err < A.tol) {
+          converged = true;
+          break;
+        }
+      } else {
+        if (err < A.tol || xmax <= A.tol || (since >= 16 && xmax <= 16.0 * A.tol)) {
+          mode = 1;
+        } else if (it < eval32) {
+          next_eval = 2 * it;
+        } else {
+          interval = (err > 1e3 * A.tol) ? min(2u * interval, 16u * eval32) : (err > 10.0 * A.tol ? interval : eval32);
+          next_eval = it + interval;
+        }
+      }
+    }
+    if (!converged) {
+      if (err_best < INFINITY)
+        for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) A.r[k] = bufs[bestbuf][k];
+      it = A.max_iters;
+    }
+    if (threadIdx.x == 0) {
+      Z.done[sc] = converged ? 1 : 0;
+      Z.iters[sc] = it;
+      Z.best[sc] = err_best;
+      if (!converged) atomicAdd(Z.unconverged, 1ull);
+      atomicMax(&A.st->iterations, it);
+    }
+    __syncthreads();
+  }
+  n32 = warp_sum(n32);
+  n64 = warp_sum(n64);
+  nev = warp_sum(nev);
+  nlc = warp_sum(nlc);
+  nlb = warp_sum(nlb);
+  if ((threadIdx.x & 31) == 0) {
+    if (n32) atomicAdd(&Z.work[0], n32);
+    atomicAdd(&Z.work[1], n64);
+    atomicAdd(&Z.work[2], nev);
+    if (nlc) atomicAdd(&Z.work[3], nlc);
+    if (nlb) atomicAdd(&Z.work[4], nlb);
+  }
+}
+
+// (scene, colour) runs of a batch's contacts.
+__global__ void k_scene_color_count(const int* __restrict__ nc_dev, const int* __restrict__ cscene,
+                                    const int* __restrict__ color, int* __restrict__ cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *nc_dev) return;
+  const int c = color[k];
+  if (c < 0 || c >= kMaxColors) return;  // a failed colouring (its status ends the solve)
+  atomicAdd(&cnt[cscene[k] * kMaxColors + c], 1);
+}
+
+__global__ void k_scene_color_scatter(const int* __restrict__ nc_dev, const int* __restrict__ cscene,
+                                      const int* __restrict__ color, const int* __restrict__ start,
+                                      int* __restrict__ fill, int* __restrict__ sperm) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *nc_dev) return;
+  const int c = color[k];
+  if (c < 0 || c >= kMaxColors) return;
+  const int key = cscene[k] * kMaxColors + c;
+  sperm[start[key] + atomicAdd(&fill[key], 1)] = k;
+}
+
+// FP32 copies of the contacts in (scene, colour) order (position q holds contact sperm[q]).
+__global__ void k_pack32_scenes(const int* __restrict__ n_dev, const int* __restrict__ sperm,
+                                const int* __restrict__ ia, const int* __restrict__ ib,
+                                const double2* __restrict__ n, const double2* __restrict__ c,
+                                const double* __restrict__ W, const double* __restrict__ mu,
+                                const double2* __restrict__ r, int2* __restrict__ ab, float2* __restrict__ n32,
+                                float2* __restrict__ c32, float4* __restrict__ w32, float2* __restrict__ r32) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= *n_dev) return;
+  const int k = sperm[q];
+  const int b = ib[k];
+  ab[q] = make_int2(ia[k], b >= 0 ? b : -1);
+  const double2 nk = n[k], ck = c[k], rk = r[k];
+  n32[q] = make_float2((float)nk.x, (float)nk.y);
+  c32[q] = make_float2((float)ck.x, (float)ck.y);
+  w32[q] = make_float4((float)W[3 * k], (float)W[3 * k + 1], (float)W[3 * k + 2], (float)mu[k]);
+  r32[q] = make_float2((float)rk.x, (float)rk.y);
+}
+
 __global__ void k_wait_flag(const int* flag, int* status, unsigned long long spin) {
   volatile const int* f = flag;
   unsigned long long n = 0;
@@ -2820,7 +3159,67 @@ int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams
   B.done_count = X.done_count;
   B.unconverged = X.unconverged;
   B.work = X.work;
-  if (sp.precision == SG_PRECISION_FP32_REFINE) {
+  if (X.scene_blocks) {
+    // One block per scene: contacts ordered by (scene, colour), then the persistent per-scene sweeps.
+    const bool mixed = sp.precision == SG_PRECISION_FP32_REFINE;
+    const size_t keys = (size_t)X.S * kMaxColors;
+    SG_CUDA_TRY(cudaMemsetAsync(X.key_cnt, 0, sizeof(int) * (keys + 1), s));
+    SG_CUDA_TRY(cudaMemsetAsync(X.key_fill, 0, sizeof(int) * (keys + 1), s));
+    SG_CUDA_TRY(cudaMemsetAsync(X.next, 0, sizeof(int), s));
+    k_scene_color_count<<<blocks_for(cap), kBlock, 0, s>>>(X.nc_dev, X.cscene, ctx->color.as<int>(), X.key_cnt);
+    SG_CUDA_TRY(cudaGetLastError());
+    if (int r = scan_exclusive(ctx, X.key_cnt, X.key_start, (int)keys)) return r;
+    k_scene_color_scatter<<<blocks_for(cap), kBlock, 0, s>>>(X.nc_dev, X.cscene, ctx->color.as<int>(), X.key_start,
+                                                            X.key_fill, X.sperm);
+    SG_CUDA_TRY(cudaGetLastError());
+    SceneBlockArgs Z;
+    Z.g = GA;
+    if (mixed) {
+      k_pack32_scenes<<<blocks_for(cap), kBlock, 0, s>>>(X.key_start + keys, X.sperm, P.ia, P.ib, n2,
+                                                         reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2,
+                                                         ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(),
+                                                         ctx->pk_c.as<float2>(), ctx->pk_w.as<float4>(),
+                                                         ctx->pk_r.as<float2>());
+      k_vel32<<<blocks_for(nb), kBlock, 0, s>>>(nb, vrun, P.minv, ctx->v32.as<float2>(), ctx->minv32.as<float>());
+      SG_CUDA_TRY(cudaGetLastError());
+      ctx->kernel_launches += 2;
+    }
+    Z.f.ab = ctx->pk_ab.as<int2>();
+    Z.f.n = ctx->pk_n.as<float2>();
+    Z.f.c = ctx->pk_c.as<float2>();
+    Z.f.w = ctx->pk_w.as<float4>();
+    Z.f.r = ctx->pk_r.as<float2>();
+    Z.f.v = ctx->v32.as<float2>();
+    Z.f.minv = ctx->minv32.as<float>();
+    Z.f.minv64 = P.minv;
+    Z.f.v0 = reinterpret_cast<const double2*>(P.v0);
+    Z.f.body_off = off;
+    Z.f.body_adj = adj;
+    Z.f.nb = nb;
+    Z.f.eval32 = (unsigned)ctx->check_interval;
+    Z.v = vrun;
+    Z.sb_off = X.sb_off;
+    Z.sc_off = X.sc_off;
+    Z.key_start = X.key_start;
+    Z.sperm = X.sperm;
+    Z.order = X.order;
+    Z.next = X.next;
+    Z.S = X.S;
+    Z.smax = X.smax;
+    Z.best = X.best;
+    Z.done = X.done;
+    Z.iters = X.iters;
+    Z.unconverged = X.unconverged;
+    Z.work = X.work;
+    const size_t smem = (size_t)(mixed ? 24 : 16) * (size_t)X.smax;
+    const void* kern = mixed ? (const void*)k_gs_scenes<true> : (const void*)k_gs_scenes<false>;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kSceneBlock, smem) != cudaSuccess || bps < 1) bps = 1;
+    const int g = std::max(1, std::min(ctx->num_sms * bps, X.S));
+    void* args[] = {&Z};
+    SG_CUDA_TRY(cudaLaunchKernel(kern, dim3(g), dim3(kSceneBlock), args, smem, s));
+    ctx->kernel_launches += 5;  // count, 3 scan, scatter
+  } else if (sp.precision == SG_PRECISION_FP32_REFINE) {
     k_pack32_b<<<blocks_for(cap), kBlock, 0, s>>>(X.nc_dev, ctx->perm.as<int>(), P.ia, P.ib, n2,
                                                  reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2, X.cscene,
                                                  ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
@@ -2867,6 +3266,14 @@ int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams
                                                      P.m, P.minv, reinterpret_cast<double2*>(P.v2));
   SG_CUDA_TRY(cudaGetLastError());
   ctx->kernel_launches += 3;  // vel_init, gs, final velocity
+  return SG_OK;
+}
+
+int scene_blocks_prepare(int smax) {
+  SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_scenes<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   std::max(16 * smax, 48 * 1024)));
+  SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_scenes<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   std::max(24 * smax, 48 * 1024)));
   return SG_OK;
 }
 

@@ -195,6 +195,93 @@ __global__ void k_splitham(int nb, double dt, double gx, double gy, double gz, c
   }
 }
 
+// IntegrationTools::exponentialEuler (rigidbody3d/UnconstrainedMaps/IntegrationTools.cpp:3-47) for
+// body i: x1 = x0 + dt v; R1 = rot(omega / |omega|, |omega| dt) R0, the rotation by the Rodrigues
+// formula (Eigen's AngleAxis::toRotationMatrix).  sin and cos are CUDA's.
+__device__ __forceinline__ void exp_euler_body(int nb, int i, double dt, const double* __restrict__ q0,
+                                               const double* v, const double* w, double* __restrict__ q1) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j) q1[3 * i + j] = q0[3 * i + j] + dt * v[j];
+  double ax[3] = {w[0], w[1], w[2]};
+  double theta = sqrt(dot3(ax, ax));
+  if (theta != 0.0)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ax[j] = ax[j] / theta;
+  theta = theta * dt;
+  const double sn = sin(theta), c = cos(theta);
+  const double sa[3] = {sn * ax[0], sn * ax[1], sn * ax[2]};
+  const double c1[3] = {(1.0 - c) * ax[0], (1.0 - c) * ax[1], (1.0 - c) * ax[2]};
+  double R[9];
+  double t = c1[0] * ax[1];
+  R[1] = t - sa[2];
+  R[3] = t + sa[2];
+  t = c1[0] * ax[2];
+  R[2] = t + sa[1];
+  R[6] = t - sa[1];
+  t = c1[1] * ax[2];
+  R[5] = t - sa[0];
+  R[7] = t + sa[0];
+  R[0] = c1[0] * ax[0] + c;
+  R[4] = c1[1] * ax[1] + c;
+  R[8] = c1[2] * ax[2] + c;
+  double R0[9], R1[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) R0[j] = q0[3 * (size_t)nb + 9 * (size_t)i + j];
+  matmul3(R, R0, R1);
+#pragma unroll
+  for (int j = 0; j < 9; ++j) q1[3 * (size_t)nb + 9 * (size_t)i + j] = R1[j];
+}
+
+// SymplecticEulerImpactFrictionMap::flow, first half (SymplecticEulerImpactFrictionMap.cpp:201-260):
+// vdelta = dt M^-1 F (gravity, no torque), the predictor by exponential Euler from v0 + vdelta and
+// its AABBs (centre +- r).
+__global__ void k_se3_predict(int nb, double dt, double gx, double gy, double gz, const double* __restrict__ q0,
+                              const double* __restrict__ v0, const double* __restrict__ m,
+                              const double* __restrict__ Iinv, const double* __restrict__ rad,
+                              double* __restrict__ vdelta, double* __restrict__ q1, double* __restrict__ aabb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double g[3] = {gx, gy, gz};
+  const double mi = m[i];
+  const double minv = 1.0 / mi;
+  double vp[3], wp[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double F = 0.0 + mi * g[j];
+    const double* Ii = Iinv + 9 * (size_t)i + 3 * j;
+    const double dl = dt * (0.0 + minv * F);
+    const double da = dt * (((0.0 + Ii[0] * 0.0) + Ii[1] * 0.0) + Ii[2] * 0.0);
+    vdelta[3 * (size_t)i + j] = dl;
+    vdelta[3 * (size_t)nb + 3 * (size_t)i + j] = da;
+    vp[j] = v0[3 * (size_t)i + j] + dl;
+    wp[j] = v0[3 * (size_t)nb + 3 * (size_t)i + j] + da;
+  }
+  exp_euler_body(nb, i, dt, q0, vp, wp, q1);
+  const double r = rad[i];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    aabb[6 * (size_t)i + j] = q1[3 * i + j] - r;
+    aabb[6 * (size_t)i + 3 + j] = q1[3 * i + j] + r;
+  }
+}
+
+// The map's end (:330-407): v1 = v2 + vdelta, the configuration by exponential Euler from v1 (with
+// v2 = v0 where no constraint is active).
+__global__ void k_se3_final(int nb, double dt, const double* __restrict__ q0, const double* __restrict__ v2,
+                            const double* __restrict__ vdelta, double* __restrict__ q1, double* __restrict__ v1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  double vl[3], wl[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    vl[j] = v2[3 * (size_t)i + j] + vdelta[3 * (size_t)i + j];
+    wl[j] = v2[3 * (size_t)nb + 3 * (size_t)i + j] + vdelta[3 * (size_t)nb + 3 * (size_t)i + j];
+    v1[3 * (size_t)i + j] = vl[j];
+    v1[3 * (size_t)nb + 3 * (size_t)i + j] = wl[j];
+  }
+  exp_euler_body(nb, i, dt, q0, vl, wl, q1);
+}
+
 // World inertia and its inverse from R (updateMandMinv).  At construction the
 // reference inserts I(row, col) at sparse entry (col, row) (RigidBody3DState.cpp:175-182).
 __global__ void k_inertia(int nb, const double* __restrict__ q, const double* __restrict__ I0,
@@ -585,7 +672,40 @@ struct Assemble3 {
   double* W;    // 6: w00 w01 w02 w11 w12 w22
   double* mu_out;
   double* r;    // 3
+  // SymplecticEulerImpactFrictionMap (vdelta non-null): the force's velocity change, the pose
+  // stabilisation, and the impulse cache of the step before (keys ascending, 6 doubles each: the
+  // cached normal and force); this step's keys go to key.
+  const double* vdelta = nullptr;   // 6 nb [linear | angular]
+  const double* plane_x = nullptr;
+  double dt = 0.0;
+  int stabilize = 0;
+  double pen_thresh = 0.0;
+  int cache_mode = 0;
+  const unsigned long long* prev_key = nullptr;
+  const double* prev_c6 = nullptr;
+  int prev_n = 0;
+  unsigned long long* key = nullptr;
 };
+
+// Impulse-cache key of a sphere contact: (a, b) for a pair, (plane, a) flagged by the top bit for a
+// plane; contacts are written pairs first (a, then b ascending), then plane-major, so a step's keys
+// ascend.
+__device__ __forceinline__ unsigned long long contact_key3(int a, int b) {
+  if (b >= 0) return ((unsigned long long)(unsigned)a << 32) | (unsigned)b;
+  return (1ull << 63) | ((unsigned long long)(unsigned)(-1 - b) << 32) | (unsigned)a;
+}
+
+__device__ __forceinline__ int find_key3(const unsigned long long* keys, int n, unsigned long long k) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (keys[mid] < k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return (lo < n && keys[lo] == k) ? lo : -1;
+}
 
 __device__ void orthogonal_vector(const double* n, double* o) {
   const double ax = fabs(n[0]), ay = fabs(n[1]), az = fabs(n[2]);
@@ -600,6 +720,45 @@ __device__ void orthogonal_vector(const double* n, double* o) {
 #pragma unroll
   for (int j = 0; j < 3; ++j) o[j] = o[j] - d * n[j];
   normalize3(o);
+}
+
+// Quaternion (w, x, y, z) turning direction a onto direction b (Eigen's
+// Quaternion::setFromTwoVectors, half-angle form; directions within 1e-12 of opposite turn by pi
+// about an axis orthogonal to a).
+__device__ void quat_from_two_vectors(const double* a, const double* b, double* q) {
+  double v0[3] = {a[0], a[1], a[2]}, v1[3] = {b[0], b[1], b[2]};
+  normalize3(v0);
+  normalize3(v1);
+  const double c = dot3(v1, v0);
+  if (c < -1.0 + 1e-12) {
+    double axis[3];
+    orthogonal_vector(v0, axis);
+    normalize3(axis);
+    const double w2 = (1.0 + fmax(c, -1.0)) * 0.5;
+    const double sv = sqrt(1.0 - w2);
+    q[0] = sqrt(w2);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) q[1 + j] = axis[j] * sv;
+    return;
+  }
+  double axis[3];
+  cross3(v0, v1, axis);
+  const double s2 = sqrt((1.0 + c) * 2.0);
+  const double invs = 1.0 / s2;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) q[1 + j] = axis[j] * invs;
+  q[0] = s2 * 0.5;
+}
+
+// q v q* for a unit quaternion: uv = 2 (q_v x v), v + w uv + q_v x uv.
+__device__ __forceinline__ void quat_rotate(const double* q, const double* v, double* out) {
+  double uv[3], uuv[3];
+  cross3(q + 1, v, uv);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) uv[j] = uv[j] + uv[j];
+  cross3(q + 1, uv, uuv);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) out[j] = (v[j] + q[0] * uv[j]) + uuv[j];
 }
 
 __global__ void k_assemble3(Assemble3 A) {
@@ -692,8 +851,66 @@ __global__ void k_assemble3(Assemble3 A) {
   // Forcing term w = n (CoR n.v + nrel) + s drel0 + t drel1 (kinematic velocities are zero).
   const double ndotv = dot3(n, vr);
   const double zero[3] = {0.0, 0.0, 0.0};
-  const double nrel = -dot3(zero, n);
-  const double drel0 = -dot3(zero, s), drel1 = -dot3(zero, t);
+  double nrel = -dot3(zero, n);
+  double drel0 = -dot3(zero, s), drel1 = -dot3(zero, t);
+  if (A.vdelta) {
+    // SymplecticEulerImpactFrictionMap.cpp:291-329: nrel += N^T vdelta (+ min(0, gap) / dt when
+    // stabilising), drel += D^T vdelta, each column's entries in row order (linear rows of a, of b,
+    // then angular rows of a, of b) accumulated from zero.
+    const double* la = A.vdelta + 3 * (size_t)a;
+    const double* wda = A.vdelta + 3 * (size_t)nb + 3 * (size_t)a;
+    const double* lb = has_b ? A.vdelta + 3 * (size_t)b : nullptr;
+    const double* wdb = has_b ? A.vdelta + 3 * (size_t)nb + 3 * (size_t)b : nullptr;
+    double tn = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) tn = tn + n[j] * la[j];
+    if (has_b)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) tn = tn + (-n[j]) * lb[j];
+    double xn = 0.0 + 1.0 * tn;
+    double xd[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const double* T = d == 0 ? s : t;
+      double xt[3];
+      cross3(ra, T, xt);
+      double tt = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) tt = tt + T[j] * la[j];
+      if (has_b)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tt = tt + (-T[j]) * lb[j];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) tt = tt + xt[j] * wda[j];
+      if (has_b) {
+        double xb[3];
+        cross3(rb, T, xb);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tt = tt + (-xb[j]) * wdb[j];
+      }
+      xd[d] = 0.0 + 1.0 * tt;
+    }
+    if (A.stabilize) {
+      double gap;
+      if (has_b) {
+        // SphereSphereConstraint::evaluateGapFunction (SphereSphereConstraint.cpp:28-31)
+        const double* xb = A.q0 + 3 * (size_t)b;
+        const double dd[3] = {xa[0] - xb[0], xa[1] - xb[1], xa[2] - xb[2]};
+        gap = (sqrt(dot3(dd, dd)) - A.rad[a]) - A.rad[b];
+      } else {
+        // StaticPlaneSphereConstraint::evaluateGapFunction (StaticPlaneSphereConstraint.cpp:31-35)
+        const int pl = -1 - b;
+        const double dd[3] = {xa[0] - A.plane_x[3 * pl], xa[1] - A.plane_x[3 * pl + 1], xa[2] - A.plane_x[3 * pl + 2]};
+        gap = dot3(A.plane_n + 3 * pl, dd) - A.rad[a];
+      }
+      double g0 = fmin(0.0, gap);
+      if (fabs(g0) < A.pen_thresh) g0 = 0.0;
+      xn = xn + g0 / A.dt;
+    }
+    nrel = nrel + xn;
+    drel0 = drel0 + xd[0];
+    drel1 = drel1 + xd[1];
+  }
   const int scene = A.scene_of ? A.scene_of[a] : -1;
   const double CoR = scene >= 0 ? A.s_CoR[scene] : A.CoR;
   const double sc = CoR * ndotv + nrel;
@@ -739,11 +956,34 @@ __global__ void k_assemble3(Assemble3 A) {
       Wk[q++] = wij;
     }
   A.mu_out[k] = scene >= 0 ? A.s_mu[scene] : A.mu;
-  // Warm start from alpha = beta = 0 (the 3D geometric map has no impulse cache):
-  // r = alpha n + beta0 s + beta1 t, then local r = E^T r.
+  // Warm start: r = alpha n + beta0 s + beta1 t, then local r = E^T r.  The geometric map starts
+  // from zero (no 3D impulse cache); the symplectic-Euler map from its cache, the cached force
+  // turned from the cached normal onto the new one (SymplecticEulerImpactFrictionMap.cpp:48-131;
+  // a missing entry reads as zeros).
+  double al = 0.0, b0 = 0.0, b1 = 0.0;
+  if (A.vdelta) {
+    const unsigned long long key = contact_key3(a, b);
+    A.key[k] = key;
+    const int p = (A.cache_mode != SG_CACHE_NONE && A.prev_n > 0) ? find_key3(A.prev_key, A.prev_n, key) : -1;
+    if (p >= 0) {
+      double c6[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) c6[j] = A.prev_c6[6 * (size_t)p + j];
+      if (A.cache_mode == SG_CACHE_NORMAL) {
+        al = c6[0];
+      } else if (c6[0] != 0.0 || c6[1] != 0.0 || c6[2] != 0.0 || c6[3] != 0.0 || c6[4] != 0.0 || c6[5] != 0.0) {
+        double qr[4], f[3];
+        quat_from_two_vectors(c6, n, qr);
+        quat_rotate(qr, c6 + 3, f);
+        al = dot3(f, n);
+        b0 = dot3(f, s);
+        b1 = dot3(f, t);
+      }
+    }
+  }
   double rw[3];
 #pragma unroll
-  for (int j = 0; j < 3; ++j) rw[j] = (0.0 * n[j] + 0.0 * s[j]) + 0.0 * t[j];
+  for (int j = 0; j < 3; ++j) rw[j] = (al * n[j] + b0 * s[j]) + b1 * t[j];
   A.r[3 * (size_t)k] = dot3(n, rw);
   A.r[3 * (size_t)k + 1] = dot3(s, rw);
   A.r[3 * (size_t)k + 2] = dot3(t, rw);
@@ -1149,6 +1389,29 @@ __global__ void k_extract3(int nc, const double* __restrict__ E3, const double* 
   ab[3 * (size_t)k + 2] = dot3(rw, E + 6);
 }
 
+// SymplecticEulerImpactFrictionMap::cacheImpulses (SymplecticEulerImpactFrictionMap.cpp:133-199):
+// per contact the normal and the force f = alpha n + beta0 s + beta1 t (or alpha alone when only
+// normals are cached), from the step's (alpha, beta0, beta1).
+__global__ void k_cache3(int nc, int cache_mode, const double* __restrict__ E3, const double* __restrict__ ab,
+                         double* __restrict__ c6) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  double* c = c6 + 6 * (size_t)k;
+  const double al = ab[3 * (size_t)k], b0 = ab[3 * (size_t)k + 1], b1 = ab[3 * (size_t)k + 2];
+  if (cache_mode == SG_CACHE_NORMAL) {
+    c[0] = al;
+#pragma unroll
+    for (int j = 1; j < 6; ++j) c[j] = 0.0;
+    return;
+  }
+  const double* E = E3 + 9 * (size_t)k;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    c[j] = E[j];
+    c[3 + j] = (al * E[j] + b0 * E[3 + j]) + b1 * E[6 + j];
+  }
+}
+
 struct Gs3Args {
   int nc;
   Contacts3 C;
@@ -1293,6 +1556,248 @@ __global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
     A.st->sweeps64 = it;
     A.st->evals = n_eval;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Batched sphere scenes, one scene per block: the block takes the next scene of a largest-first
+// work list, keeps the scene's (v, omega) in shared memory, sweeps its contacts colour by colour
+// (the global colouring restricted to the scene, by (scene, colour)) with block barriers, evaluates
+// the scene's own residual every eval_every sweeps, keeps its best iterate and stops at tol or
+// max_iters.  Each scene sees k_gs3_batch's update sequence, so the results are the same.
+constexpr int kScene3Block = 256;
+
+struct Scene3Args {
+  Gs3Args g;                  // contacts, inverse masses and inertias, impulses, snapshot buffers
+  const double4_32a* V;       // running velocities at the start
+  const int* sb_off;          // S + 1 body offsets
+  const int* sc_off;          // S + 1 contact offsets
+  const int* key_start;       // S * kMaxColors + 1
+  const int* sperm;           // contacts by (scene, colour)
+  const int* order;           // scenes, largest first
+  int* next;                  // work-list counter
+  int S;
+  int smax;                   // shared-memory body slots (largest scene)
+  double* best;
+  int* done;
+  unsigned* iters;
+  unsigned long long* unconverged;
+  unsigned long long* work;   // [1] contact updates, [2] contact evaluations
+};
+
+// local_u3 on shared-memory velocities (la, lb: the bodies' slots, lb < 0 for a plane).
+__device__ __forceinline__ void local_u3_sv(const Contacts3& C, int k, const double4_32a* sV, double* u, int la, int lb,
+                                            const double* E, const double* Aa, const double* Ab) {
+  const double4_32a l_a = sV[2 * la], w_a = sV[2 * la + 1];
+  const double va[3] = {l_a.x, l_a.y, l_a.z}, oa[3] = {w_a.x, w_a.y, w_a.z};
+  double vb[3] = {0.0, 0.0, 0.0}, ob[3] = {0.0, 0.0, 0.0};
+  const bool has_b = lb >= 0;
+  if (has_b) {
+    const double4_32a l_b = sV[2 * lb], w_b = sV[2 * lb + 1];
+    vb[0] = l_b.x;
+    vb[1] = l_b.y;
+    vb[2] = l_b.z;
+    ob[0] = w_b.x;
+    ob[1] = w_b.y;
+    ob[2] = w_b.z;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double h = dot3(E + 3 * i, va);
+    if (i > 0) h = h + dot3(Aa + 3 * (i - 1), oa);
+    if (has_b) {
+      double hb = dot3(E + 3 * i, vb);
+      if (i > 0) hb = hb + dot3(Ab + 3 * (i - 1), ob);
+      h = h - hb;
+    }
+    u[i] = h + C.c[3 * (size_t)k + i];
+  }
+}
+
+// gs_update3's arithmetic on shared-memory velocities (la, lb: the bodies' slots, lb < 0 for a
+// plane; a, b: their global indices for the inverse masses and inertias).
+__device__ __forceinline__ void gs_update3_sv(const Gs3Args& A, int k, int a, int b, int la, int lb, double4_32a* sV) {
+  const Contacts3& C = A.C;
+  const bool has_b = lb >= 0;
+  double E[9], Aa[6], Ab[6];
+  load_contact(C, k, E, Aa, Ab);
+  double u[3];
+  local_u3_sv(C, k, sV, u, la, lb, E, Aa, Ab);
+  const double r0 = A.r[3 * (size_t)k], r1 = A.r[3 * (size_t)k + 1], r2 = A.r[3 * (size_t)k + 2];
+  double W[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) W[j] = C.W[6 * (size_t)k + j];
+  const double bt[3] = {u[0] - ((W[0] * r0 + W[1] * r1) + W[2] * r2), u[1] - ((W[1] * r0 + W[3] * r1) + W[4] * r2),
+                        u[2] - ((W[2] * r0 + W[4] * r1) + W[5] * r2)};
+  double rn[3];
+  local_solve_3d(W, bt, C.mu[k], rn);
+  const double d0 = rn[0] - r0, d1 = rn[1] - r1, d2 = rn[2] - r2;
+  double pl[3], pa[3], pb[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    pl[j] = (E[j] * d0 + E[3 + j] * d1) + E[6 + j] * d2;
+    pa[j] = Aa[j] * d1 + Aa[3 + j] * d2;
+    pb[j] = Ab[j] * d1 + Ab[3 + j] * d2;
+  }
+  double Ii[9], wa[3];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)a + j];
+  matvec3(Ii, pa, wa);
+  const double ma = A.minv[a];
+  {
+    const double4_32a l_a = sV[2 * la], o_a = sV[2 * la + 1];
+    sV[2 * la] = make_double4_32a(l_a.x + ma * pl[0], l_a.y + ma * pl[1], l_a.z + ma * pl[2], 0.0);
+    sV[2 * la + 1] = make_double4_32a(o_a.x + wa[0], o_a.y + wa[1], o_a.z + wa[2], 0.0);
+  }
+  if (has_b) {
+    double wb[3];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)b + j];
+    matvec3(Ii, pb, wb);
+    const double mb = A.minv[b];
+    const double4_32a l_b = sV[2 * lb], o_b = sV[2 * lb + 1];
+    sV[2 * lb] = make_double4_32a(l_b.x - mb * pl[0], l_b.y - mb * pl[1], l_b.z - mb * pl[2], 0.0);
+    sV[2 * lb + 1] = make_double4_32a(o_b.x - wb[0], o_b.y - wb[1], o_b.z - wb[2], 0.0);
+  }
+  A.r[3 * (size_t)k] = rn[0];
+  A.r[3 * (size_t)k + 1] = rn[1];
+  A.r[3 * (size_t)k + 2] = rn[2];
+}
+
+__global__ void __launch_bounds__(kScene3Block) k_gs3_scenes(Scene3Args Z) {
+  const Gs3Args& A = Z.g;
+  extern __shared__ __align__(32) double4_32a sV3[];
+  __shared__ int s_w;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ double s_red[33];
+  if (*((volatile int*)&A.st->status) != 0) return;  // the colouring failed
+  const unsigned eval_every = A.eval_every ? A.eval_every : 1u;
+  double* bufs[2] = {A.r_a, A.r_b};
+  unsigned long long nupd = 0, nevl = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_w = atomicAdd(Z.next, 1);
+    __syncthreads();
+    const int w = s_w;
+    __syncthreads();
+    if (w >= Z.S) break;
+    const int sc = Z.order[w];
+    const int b0 = Z.sb_off[sc], nbs = Z.sb_off[sc + 1] - b0;
+    const int c0 = Z.sc_off[sc], c1 = Z.sc_off[sc + 1];
+    if (c1 == c0) {
+      if (threadIdx.x == 0) {
+        Z.done[sc] = 1;
+        Z.iters[sc] = 0;
+        Z.best[sc] = INFINITY;
+      }
+      continue;
+    }
+    for (int j = threadIdx.x; j < 2 * nbs; j += blockDim.x) sV3[j] = Z.V[2 * (size_t)b0 + j];
+    for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x)
+      s_off[c] = c < kMaxColors ? Z.key_start[sc * kMaxColors + c] : Z.key_start[(sc + 1) * kMaxColors];
+    __syncthreads();
+    int ncol = kMaxColors;
+    while (ncol > 0 && s_off[ncol] == s_off[ncol - 1]) --ncol;
+    double err_best = INFINITY;
+    int bestbuf = 0;
+    bool converged = false;
+    unsigned it;
+    for (it = 1; it <= A.max_iters; ++it) {
+      for (int col = 0; col < ncol; ++col) {
+        const int e = s_off[col + 1];
+        for (int q = s_off[col] + threadIdx.x; q < e; q += blockDim.x) {
+          const int k = Z.sperm[q];
+          const int a = A.C.ia[k], b = A.C.ib[k];
+          gs_update3_sv(A, k, a, b, a - b0, b >= 0 ? b - b0 : -1, sV3);
+          ++nupd;
+        }
+        __syncthreads();
+      }
+      if (it % eval_every != 0) continue;
+      double emax = 0.0;
+      double* cand = bufs[1 - bestbuf];
+      for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) {
+        const int a = A.C.ia[k], b = A.C.ib[k];
+        double E[9], Aa[6], Ab[6], u[3];
+        load_contact(A.C, k, E, Aa, Ab);
+        local_u3_sv(A.C, k, sV3, u, a - b0, b >= 0 ? b - b0 : -1, E, Aa, Ab);
+        const double rk[3] = {A.r[3 * (size_t)k], A.r[3 * (size_t)k + 1], A.r[3 * (size_t)k + 2]};
+        cand[3 * (size_t)k] = rk[0];
+        cand[3 * (size_t)k + 1] = rk[1];
+        cand[3 * (size_t)k + 2] = rk[2];
+        emax = nanmax(emax, fb_error_3d(rk, u, A.C.mu[k]));
+        ++nevl;
+      }
+      emax = warp_nanmax(emax);
+      if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = emax;
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        double x = threadIdx.x < (blockDim.x + 31) / 32 ? s_red[threadIdx.x] : 0.0;
+        x = warp_nanmax(x);
+        if (threadIdx.x == 0) s_red[32] = x;
+      }
+      __syncthreads();
+      const double err = s_red[32];
+      __syncthreads();
+      if (err < err_best) {
+        err_best = err;
+        bestbuf ^= 1;
+      }
+      if (err < A.tol) {
+        converged = true;
+        break;
+      }
+    }
+    if (!converged) {
+      if (err_best < INFINITY)
+        for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) {
+          A.r[3 * (size_t)k] = bufs[bestbuf][3 * (size_t)k];
+          A.r[3 * (size_t)k + 1] = bufs[bestbuf][3 * (size_t)k + 1];
+          A.r[3 * (size_t)k + 2] = bufs[bestbuf][3 * (size_t)k + 2];
+        }
+      it = A.max_iters;
+    }
+    if (threadIdx.x == 0) {
+      Z.done[sc] = converged ? 1 : 0;
+      Z.iters[sc] = it;
+      Z.best[sc] = err_best;
+      if (!converged) atomicAdd(Z.unconverged, 1ull);
+      atomicMax(&A.st->iterations, it);
+    }
+    __syncthreads();
+  }
+  nupd = warp_sum(nupd);
+  nevl = warp_sum(nevl);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&Z.work[1], nupd);
+    atomicAdd(&Z.work[2], nevl);
+  }
+}
+
+// (scene, colour) runs of a batch's contacts (scene of a contact = scene of its first body).
+__global__ void k_scene_color_count3(int nc, const int* __restrict__ ia, const int* __restrict__ scene_of,
+                                     const int* __restrict__ color, int* __restrict__ cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int c = color[k];
+  if (c < 0 || c >= kMaxColors) return;  // a failed colouring (its status ends the solve)
+  atomicAdd(&cnt[scene_of[ia[k]] * kMaxColors + c], 1);
+}
+
+__global__ void k_scene_color_scatter3(int nc, const int* __restrict__ ia, const int* __restrict__ scene_of,
+                                       const int* __restrict__ color, const int* __restrict__ start,
+                                       int* __restrict__ fill, int* __restrict__ sperm) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int c = color[k];
+  if (c < 0 || c >= kMaxColors) return;
+  const int key = scene_of[ia[k]] * kMaxColors + c;
+  sperm[start[key] + atomicAdd(&fill[key], 1)] = k;
+}
+
+// The per-scene sphere kernel's dynamic shared memory limit for scenes of up to smax bodies.
+static int scene3_blocks_prepare(int smax) {
+  SG_CUDA_TRY(cudaFuncSetAttribute(k_gs3_scenes, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   std::max(64 * smax, 48 * 1024)));
+  return SG_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -2513,12 +3018,32 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   const int nb = ctx->nb, np = ctx->np;
   cudaStream_t s = ctx->stream;
   sg_step_stats st{};
+  const bool se = ctx->staggering == SG_STAGGER_SYMPLECTIC_EULER;
+  if (ctx->staggering == SG_STAGGER_STABILIZED) {
+    set_error("sphere scenes step with the geometric or the symplectic Euler staggering");
+    return SG_BAD_INPUT;
+  }
+  if (se && ctx->cfg.CoR != 0.0) {
+    set_error("the symplectic Euler staggering needs CoR = 0");
+    return SG_BAD_INPUT;
+  }
   if (nb == 0) {
     if (out) *out = st;
     return SG_OK;
   }
-  // Predictor and q1 AABBs.
-  if (int r = splitham(ctx, ctx->v.as<double>(), true)) return r;
+  // Predictor and q1 AABBs: the unconstrained map (geometric staggering), or vdelta and the
+  // exponential-Euler predictor (symplectic Euler).
+  if (se) {
+    if (int r = grow(ctx->vdelta, sizeof(double) * 6 * (size_t)nb)) return r;
+    const double* g = ctx->cfg.gravity;
+    k_se3_predict<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cfg.dt, g[0], g[1], g[2], ctx->q.as<double>(),
+                                                    ctx->v.as<double>(), ctx->m.as<double>(), ctx->Iinv.as<double>(),
+                                                    ctx->r.as<double>(), ctx->vdelta.as<double>(), ctx->q1.as<double>(),
+                                                    ctx->aabb.as<double>());
+    SG_CUDA_TRY(cudaGetLastError());
+  } else if (int r = splitham(ctx, ctx->v.as<double>(), true)) {
+    return r;
+  }
   // Grid.
   const long cap = 4L * nb + 64;
   if (int r = grow(ctx->grid, sizeof(Grid3))) return r;
@@ -2575,6 +3100,15 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   ctx->last_nc = nc;
   ctx->last_nbb = npairs;
   if (nc == 0) {
+    if (se) {
+      // No active constraint: v1 = v0 + vdelta, the configuration from v1; the cache empties.
+      k_se3_final<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cfg.dt, ctx->q.as<double>(), ctx->v.as<double>(),
+                                                    ctx->vdelta.as<double>(), ctx->q1.as<double>(),
+                                                    ctx->v1.as<double>());
+      SG_CUDA_TRY(cudaGetLastError());
+      ctx->prev_n = 0;
+      ctx->kernel_launches += 1;
+    }
     std::swap(ctx->q, ctx->q1);
     std::swap(ctx->v, ctx->v1);
     if (int r = sphere3d_update_inertia(ctx, false)) return r;
@@ -2613,6 +3147,21 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   A.W = ctx->W3.as<double>();
   A.mu_out = ctx->mu.as<double>();
   A.r = ctx->r3.as<double>();
+  if (se) {
+    const size_t c = (size_t)nc;
+    if (int r = grow(ctx->key, sizeof(unsigned long long) * c)) return r;
+    if (int r = grow(ctx->c6, sizeof(double) * 6 * c)) return r;
+    A.vdelta = ctx->vdelta.as<double>();
+    A.plane_x = ctx->plane_x.as<double>();
+    A.dt = ctx->cfg.dt;
+    A.stabilize = ctx->stabilize;
+    A.pen_thresh = ctx->pen_thresh;
+    A.cache_mode = ctx->cfg.cache_mode;
+    A.prev_key = ctx->prev_key.as<unsigned long long>();
+    A.prev_c6 = ctx->prev_c6.as<double>();
+    A.prev_n = (int)ctx->prev_n;
+    A.key = ctx->key.as<unsigned long long>();
+  }
   k_assemble3<<<blocks_for(nc), kBlock, 0, s>>>(A);
   SG_CUDA_TRY(cudaGetLastError());
 
@@ -2630,8 +3179,25 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
   st.succeeded = ctx->h_stats.converged;
   st.error = ctx->h_stats.error;
   st.n_colors = (uint32_t)ctx->h_stats.n_colors;
-  // Final map with the post-impact velocity, then the world inertia of the new state.
-  if (int r = splitham(ctx, ctx->v2.as<double>(), false)) return r;
+  if (se) {
+    // Impulses into the cache, v1 = v2 + vdelta and the configuration from v1.
+    if (ctx->cfg.cache_mode != SG_CACHE_NONE) {
+      k_cache3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->cfg.cache_mode, A.E, ctx->ab3.as<double>(),
+                                                 ctx->c6.as<double>());
+      SG_CUDA_TRY(cudaGetLastError());
+      std::swap(ctx->key, ctx->prev_key);
+      std::swap(ctx->c6, ctx->prev_c6);
+      ctx->prev_n = nc;
+      ctx->kernel_launches += 1;
+    } else {
+      ctx->prev_n = 0;
+    }
+    k_se3_final<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cfg.dt, ctx->q.as<double>(), ctx->v2.as<double>(),
+                                                  ctx->vdelta.as<double>(), ctx->q1.as<double>(), ctx->v1.as<double>());
+    SG_CUDA_TRY(cudaGetLastError());
+  } else if (int r = splitham(ctx, ctx->v2.as<double>(), false)) {
+    return r;
+  }
   std::swap(ctx->q, ctx->q1);
   std::swap(ctx->v, ctx->v1);
   if (int r = sphere3d_update_inertia(ctx, false)) return r;
@@ -2868,6 +3434,53 @@ int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out) {
     SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_mixed_batch, grid, kGs3mBlock, args, s));
     if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
     ctx->kernel_launches += 2;
+  } else if (ctx->s_smax > 0) {
+    // One block per scene: contacts ordered by (scene, colour), then the persistent per-scene sweeps.
+    const size_t keys = (size_t)S * kMaxColors;
+    if (int r = grow(ctx->s_kcnt, sizeof(int) * (keys + 1))) return r;
+    if (int r = grow(ctx->s_kstart, sizeof(int) * (keys + 1))) return r;
+    if (int r = grow(ctx->s_kfill, sizeof(int) * (keys + 1))) return r;
+    if (int r = grow(ctx->s_sperm, sizeof(int) * (size_t)std::max(nc, 1))) return r;
+    if (int r = grow(ctx->s_next, sizeof(int))) return r;
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_kcnt.p, 0, sizeof(int) * (keys + 1), s));
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_kfill.p, 0, sizeof(int) * (keys + 1), s));
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_next.p, 0, sizeof(int), s));
+    k_scene_color_count3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, scene_of, ctx->color.as<int>(),
+                                                           ctx->s_kcnt.as<int>());
+    SG_CUDA_TRY(cudaGetLastError());
+    if (int r = scan_exclusive(ctx, ctx->s_kcnt.as<int>(), ctx->s_kstart.as<int>(), (int)keys)) return r;
+    k_scene_color_scatter3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, scene_of, ctx->color.as<int>(),
+                                                             ctx->s_kstart.as<int>(), ctx->s_kfill.as<int>(),
+                                                             ctx->s_sperm.as<int>());
+    SG_CUDA_TRY(cudaGetLastError());
+    Scene3Args Z;
+    Z.g = B.g;
+    Z.V = V;
+    Z.sb_off = ctx->sb_off.as<int>();
+    Z.sc_off = sc_off;
+    Z.key_start = ctx->s_kstart.as<int>();
+    Z.sperm = ctx->s_sperm.as<int>();
+    Z.order = ctx->s_order.as<int>();
+    Z.next = ctx->s_next.as<int>();
+    Z.S = S;
+    Z.smax = ctx->s_smax;
+    Z.best = B.best;
+    Z.done = B.done;
+    Z.iters = B.iters;
+    Z.unconverged = B.unconverged;
+    Z.work = B.work;
+    const size_t smem = (size_t)64 * (size_t)ctx->s_smax;
+    if (int r = scene3_blocks_prepare(ctx->s_smax)) return r;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_gs3_scenes, kScene3Block, smem) != cudaSuccess ||
+        bps < 1)
+      bps = 1;
+    const int grid = std::max(1, std::min(ctx->num_sms * bps, S));
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+    k_gs3_scenes<<<grid, kScene3Block, smem, s>>>(Z);
+    SG_CUDA_TRY(cudaGetLastError());
+    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+    ctx->kernel_launches += 5;  // count, 3 scan, scatter
   } else {
     void* args[] = {&B};
     const int grid = coop_grid(ctx, k_gs3_batch, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
