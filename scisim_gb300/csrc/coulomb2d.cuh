@@ -44,6 +44,23 @@ __device__ __forceinline__ double fb_error_2d(double r0, double r1, double u0, d
 
 // Local 2x2 Coulomb problem u = W r + b: take-off, stick, slide (+/-), else the
 // admissible candidate with the smallest FB error.
+// The local solve for an isotropic block W = w I (a disc contact: no rotation, so the normal and
+// tangent rows have the same inverse-mass weight and no coupling): take-off when b0 >= 0, else the
+// stick impulse -b / w clamped onto the friction cone's edge on the side of its tangential part.
+// It agrees with local_solve_2d on such blocks to rounding; the FP32 form's FP64 sweeps use it.
+__device__ __forceinline__ void local_solve_2d_iso(double w, double b0, double b1, double mu, double& r0,
+                                                   double& r1) {
+  if (b0 >= 0.0) {
+    r0 = 0.0;
+    r1 = 0.0;
+    return;
+  }
+  const double inv = 1.0 / w;
+  const double rn = -b0 * inv, rt = -b1 * inv, lim = mu * rn;
+  r0 = rn;
+  r1 = fabs(rt) <= lim ? rt : copysign(lim, rt);
+}
+
 __device__ __forceinline__ void local_solve_2d(double w00, double w01, double w11, double b0, double b1, double mu,
                                                double& r0, double& r1) {
   if (b0 >= 0.0) {

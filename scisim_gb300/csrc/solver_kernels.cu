@@ -351,6 +351,7 @@ struct GsArgs {
   double tol;
   unsigned max_iters;
   unsigned eval_every;
+  int iso = 0;  // isotropic blocks take local_solve_2d_iso (the FP32 form's FP64 sweeps)
 };
 
 __device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
@@ -369,7 +370,10 @@ __device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
   const double bt0 = u0 - (w00 * r0 + w01 * r1);
   const double bt1 = u1 - (w01 * r0 + w11 * r1);
   double rn0, rn1;
-  local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
+  if (A.iso && w01 == 0.0 && w00 == w11)
+    local_solve_2d_iso(w00, bt0, bt1, A.mu[k], rn0, rn1);
+  else
+    local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
   const double d0 = rn0 - r0, d1 = rn1 - r1;
   const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
   const double px = nx * d0 + tx * d1;
@@ -1548,7 +1552,10 @@ __device__ __forceinline__ void gs_update64_local(const GsArgs& A, int k, int la
   const double bt0 = u0 - (w00 * r0 + w01 * r1);
   const double bt1 = u1 - (w01 * r0 + w11 * r1);
   double rn0, rn1;
-  local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
+  if (w01 == 0.0 && w00 == w11)
+    local_solve_2d_iso(w00, bt0, bt1, A.mu[k], rn0, rn1);
+  else
+    local_solve_2d(w00, w01, w11, bt0, bt1, A.mu[k], rn0, rn1);
   const double d0 = rn0 - r0, d1 = rn1 - r1;
   const double nx = nk.x, ny = nk.y, tx = -ny, ty = nx;
   const double px = nx * d0 + tx * d1;
@@ -2746,6 +2753,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     GA.tol = sp.tol;
     GA.max_iters = sp.max_iters;
     GA.eval_every = sp.eval_every;
+    GA.iso = fp32_form ? 1 : 0;
     const bool two_level_applies = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 &&
                                    nc >= ctx->two_level_min_contacts;
     if (fp64_start) {
