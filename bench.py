@@ -73,6 +73,20 @@ BYTES_PER_CONTACT_LIFT_3D = 344
 BYTES_PER_BODY_LIFT_3D = 224
 
 
+def step_roofline(kernel, bytes_total, ms_total, basis):
+    """Algorithmic bytes of the sweeps over a measured time, against the measured HBM copy rate."""
+    hbm, peak_kind = peaks()
+    ach = bytes_total / (ms_total / 1e3) / 1e9 if ms_total > 0 else 0.0
+    return {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "peak_kind": peak_kind, "bytes": bytes_total, "ms": ms_total, "time_basis": basis, "traffic": None}
+
+
+def gs3_bytes(prof):
+    return (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP_3D + prof["contact_sweeps32"] * BYTES_PER_CONTACT_SWEEP32_3D +
+            prof["contact_evals"] * BYTES_PER_CONTACT_EVAL_3D + prof["contact_lifts"] * BYTES_PER_CONTACT_LIFT_3D +
+            prof["body_lifts"] * BYTES_PER_BODY_LIFT_3D)
+
+
 def gs_bytes(prof):
     """Algorithmic bytes moved by the Gauss-Seidel kernel(s) counted in a profile."""
     return (prof["contact_sweeps"] * BYTES_PER_CONTACT_SWEEP + prof["contact_sweeps32"] * BYTES_PER_CONTACT_SWEEP32 +
@@ -375,6 +389,38 @@ def headline_roofline(prof, total_ms, args):
     return roofline, stages
 
 
+def fp32_form_error(ck, s, it0, local, **tuning):
+    """One step from the checkpointed state in the FP32 form and in plain FP64, to the same
+    tolerance: the FP32 form's deviation from FP64 in impulses (alpha, beta), velocities and
+    positions.  Both solves stop anywhere in the tolerance's neighbourhood of a frictional solution
+    set, so the figures bound the form's effect at this tolerance rather than its rounding alone."""
+    from scisim_gb300 import _lib
+    out = {}
+    for prec in (1, 0):
+        c = _lib.Context(device=local, **solver_kw(s))
+        c.restore(ck)
+        c.reconfigure(precision=prec)
+        if prec == 1 and tuning:
+            c.set_tuning(**tuning)
+        st = c.step(1, first_iteration=it0)
+        q, v = c.state()
+        out[prec] = (st, c.last_contacts(), q, v)
+        c.close()
+    (s32, c32, q32, v32), (s64, c64, q64, v64) = out[1], out[0]
+    same = np.array_equal(c32["ia"], c64["ia"]) and np.array_equal(c32["ib"], c64["ib"])
+    rec = {"same_contacts": bool(same), "residual_fp32_form": s32["error"], "residual_fp64": s64["error"],
+           "sweeps_fp32_form": s32["iterations"], "sweeps_fp64": s64["iterations"],
+           "velocity_abs": float(np.abs(v32 - v64).max()), "velocity_scale": float(np.abs(v64).max()),
+           "position_abs": float(np.abs(q32 - q64).max())}
+    if same and c64["alpha"].size:
+        scale = float(np.abs(c64["alpha"]).max())
+        da = float(np.abs(c32["alpha"] - c64["alpha"]).max())
+        db = float(np.abs(c32["beta"] - c64["beta"]).max())
+        rec.update({"alpha_abs": da, "beta_abs": db, "impulse_scale": scale,
+                    "impulse_rel": max(da, db) / scale if scale > 0 else None})
+    return rec
+
+
 def convergence_record(recs):
     """Per-step convergence of timed steps: solve_succeeded (error < tol) as SCISim reports it
     (GeometricImpactFrictionMap.cpp:344-350), residuals and sweeps."""
@@ -466,6 +512,10 @@ def batch_leg(args, torch, local, flush, ws=1, rank=0):
            "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
                               "form": "one context per scene, cold start, FP64, same steps from the same state"},
            "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"],
+           "roofline": step_roofline("k_gs_scenes (one block per scene)" if int(np.diff(b["body_off"]).max()) <= 8192
+                                     else "k_gs_mixed_batch", gs_bytes(prof), ms,
+                                     "the whole timed graph replay (detection, assembly and sweeps), so a lower "
+                                     "bound on the sweep kernel's rate"),
            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port", "sample": cpu_desc},
            "batched_over_cpu": value / cpu_v if cpu_v else None}
     ctx.close()
@@ -557,6 +607,8 @@ def sphere_batch_leg(args, torch, local, flush):
            "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
                               "form": "one context per scene, FP64, same steps from the same state"},
            "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"],
+           "roofline": step_roofline("k_gs3_scenes (one block per scene)", gs3_bytes(prof), prof["gs_ms"] or ms,
+                                     "the sweep kernel's CUDA events" if prof["gs_ms"] else "the whole timed steps"),
            "fp32_refine": {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.sphere_batch_steps,
                            "scenes_converged_last_step": int(st32["succeeded"].sum()),
                            "fp32_sweep_share": p32["contact_sweeps32"] / sw if sw else None,
@@ -821,6 +873,14 @@ def run_ours(args):
         log("plain FP64 (cold):", plain_cold)
         cctx.close()
 
+    # The FP32 form against FP64 from the timed state: as run (the start's residual picks FP64
+    # sweeps near tol), and with FP32 sweeps from the first sweep.
+    form_err = None
+    if args.form_error:
+        form_err = {"as_run": fp32_form_error(ck, s, it0, local),
+                    "fp32_sweeps_from_start": fp32_form_error(ck, s, it0, local, fp64_factor=0)}
+        log("fp32 form error:", form_err)
+
     # e2e through sg_flow with pinned host buffers, from the same state and impulse cache.
     e2e = None
     if args.e2e_steps > 0:
@@ -889,7 +949,7 @@ def run_ours(args):
                 "fp64_start_solves": prof["fp64_start_solves"], "stage_ms_per_step": stages,
                 "plain_fp64_gpu": plain,
                 "warm_over_plain": (value / ws) / plain["value"] if plain and plain["steps"] == args.steps else None,
-                "plain_fp64_cold_gpu": plain_cold,
+                "plain_fp64_cold_gpu": plain_cold, "fp32_form_error": form_err,
                 "warm_over_plain_cold": (value / ws) / plain_cold["value"] if plain_cold else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": prof["kernel_launches"], "autotune": autotune, "batched": batched,
@@ -920,6 +980,7 @@ def main():
     ap.add_argument("--cold-steps", type=int, default=1)
     ap.add_argument("--cold-iters", type=int, default=20000)
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--form-error", type=int, default=1, help="FP32-form vs FP64 error from the timed state (0 = skip)")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=60.0,
                     help="seconds of oracle stepping after which the CPU legs start no further step")

@@ -156,6 +156,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->q, ctx->q1);
     std::swap(ctx->v, ctx->v1);
     ctx->prev_n = 0;
+    ctx->prev_rows = false;
     st.succeeded = 1;
     if (int r = finish_stage_timing(ctx)) return r;
     if (out) *out = st;
@@ -195,11 +196,18 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->key, ctx->prev_key);
     std::swap(ctx->ab, ctx->prev_ab);
     ctx->prev_n = nc;
+    // This step's rows (pair offsets, plane flags and their scan) locate next step's cache entries.
+    std::swap(ctx->pair_off, ctx->prev_pair_off);
+    std::swap(ctx->plane_off, ctx->prev_plane_off);
+    std::swap(ctx->plane_flag, ctx->prev_plane_flag);
+    ctx->prev_npairs = npairs;
+    ctx->prev_rows = true;
     // keep ccap consistent with the smaller of the swapped buffers
     const int64_t kcap = (int64_t)std::min(ctx->key.bytes / sizeof(unsigned long long), ctx->ab.bytes / (2 * sizeof(double)));
     ctx->ccap = std::min<int64_t>(ctx->ccap, kcap);
   } else {
     ctx->prev_n = 0;
+    ctx->prev_rows = false;
   }
   // Final map with the post-impact velocity (:441).
   if (int r = ball2d_final_map(ctx, ctx->v2.as<double>())) return r;
@@ -281,7 +289,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                  &ctx->r_loc, &ctx->r_cand, &ctx->r_best, &ctx->key, &ctx->ab, &ctx->prev_key, &ctx->prev_ab,
                  &ctx->color, &ctx->perm, &ctx->body_cnt, &ctx->body_off, &ctx->body_fill, &ctx->body_adj,
                  &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2,
-                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->vdelta, &ctx->rb_I, &ctx->rb_Iinv,
+                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->prev_pair_off, &ctx->prev_plane_off,
+                 &ctx->prev_plane_flag, &ctx->vdelta, &ctx->rb_I, &ctx->rb_Iinv,
                  &ctx->pos0, &ctx->pos1, &ctx->rb_ct, &ctx->rb_vrun};
   for (Buf* b : bufs) release(*b);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
@@ -364,6 +373,7 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
   if (int e = grow(ctx->plane_n, 16)) return e;
   if (int e = grow(ctx->plane_t, 16)) return e;
   ctx->prev_n = 0;
+  ctx->prev_rows = false;
   ctx->last_nc = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -438,6 +448,7 @@ int sg_rigidbody2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double
   if (int e = grow(ctx->plane_n, 16)) return e;
   if (int e = grow(ctx->plane_t, 16)) return e;
   ctx->prev_n = 0;
+  ctx->prev_rows = false;
   ctx->last_nc = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -515,6 +526,7 @@ static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const 
   // World inertia at construction (RigidBody3DState.cpp:140-230).
   if (int e = sphere3d_update_inertia(ctx, true)) return e;
   ctx->prev_n = 0;
+  ctx->prev_rows = false;
   ctx->last_nc = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -1352,6 +1364,7 @@ int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes) {
     off += part.bytes;
   }
   ctx->prev_n = h.prev_n;
+  ctx->prev_rows = false;
   ctx->last_nc = 0;
   ctx->staggering = h.staggering;
   ctx->stabilize = h.stabilize;
@@ -1452,7 +1465,10 @@ int sg_autotune(sg_ctx* ctx, int32_t trial_steps, uint32_t first_iteration, sg_t
     rc = run(cand[i], &ms);
     if (rc != SG_OK) break;
     if (ms_per_step) ms_per_step[i] = ms;
-    if (ms < best_ms) {
+    // A later candidate replaces an earlier one only when 3 % faster: on steps that every candidate
+    // solves alike (a settled scene converging in the first FP64 sweeps) the differences are timing
+    // noise, and the earlier candidates (two-level on) are the ones that pay on the hard steps.
+    if (chosen < 0 || ms < 0.97 * best_ms) {
       best_ms = ms;
       chosen = i;
     }

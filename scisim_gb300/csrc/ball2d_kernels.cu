@@ -387,7 +387,39 @@ struct AssembleArgs {
   double dt = 0.0;
   int stabilize = 0;
   double pen_thresh = 0.0;
+  // The step before's rows (single-scene steps): its pair offsets per body, plane flags and their
+  // scan, so that a contact's cache entry is found in O(1): a pair (a, b) among a's pairs of the
+  // step before, a plane contact by its flag (null: binary search over all keys).
+  const int* prev_pair_off = nullptr;
+  const int* prev_plane_off = nullptr;
+  const int* prev_plane_flag = nullptr;
+  int prev_npairs = 0;
+  int nb = 0;
 };
+
+// Index of key among the cached contacts of the step before, through its rows: a pair (a, b) among
+// a's pairs (sorted by b), a plane contact (plane p, body a) at prev_npairs + its flag's scan.
+__device__ __forceinline__ long find_key_rows(const AssembleArgs& A, int a, int b, unsigned long long key) {
+  long idx = -1;
+  if (b >= 0) {
+    long lo = A.prev_pair_off[a], hi = A.prev_pair_off[a + 1];
+    while (lo < hi) {
+      const long mid = (lo + hi) >> 1;
+      if (A.prev_key[mid] < key)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (lo < A.prev_pair_off[a + 1] && A.prev_key[lo] == key) idx = lo;
+  } else {
+    const long t = (long)(-1 - b) * A.nb + a;
+    if (A.prev_plane_flag[t]) {
+      const long j = (long)A.prev_npairs + A.prev_plane_off[t];
+      if (j < A.prev_n && A.prev_key[j] == key) idx = j;
+    }
+  }
+  return idx;
+}
 
 // Contact basis, forcing term, diagonal Delassus block and warm start per contact:
 // BallBallConstraint ctor (:26-37) and computeContactBasis (:244-252),
@@ -492,7 +524,7 @@ __device__ __forceinline__ void assemble_one(const AssembleArgs& A, int k, doubl
   A.key[k] = key;
   double alpha = 0.0, beta = 0.0;
   if (A.cache_mode != SG_CACHE_NONE && prev_n > 0) {
-    const long idx = find_key(prev_key, prev_n, key);
+    const long idx = A.prev_pair_off ? find_key_rows(A, a, b, key) : find_key(prev_key, prev_n, key);
     if (idx >= 0) {
       const double2 ab = prev_ab[idx];
       alpha = ab.x;
@@ -932,6 +964,13 @@ int assemble_contacts(sg_ctx* ctx, int nc) {
   A.prev_key = ctx->prev_key.as<unsigned long long>();
   A.prev_ab = ctx->prev_ab.as<double2>();
   A.prev_n = ctx->prev_n;
+  if (ctx->prev_rows && ctx->n_scenes == 0 && !ctx->rb2d) {
+    A.prev_pair_off = ctx->prev_pair_off.as<int>();
+    A.prev_plane_off = ctx->prev_plane_off.as<int>();
+    A.prev_plane_flag = ctx->prev_plane_flag.as<int>();
+    A.prev_npairs = ctx->prev_npairs;
+    A.nb = ctx->nb;
+  }
   A.n = ctx->n.as<double2>();
   A.c = ctx->c.as<double2>();
   A.W = ctx->W.as<double>();

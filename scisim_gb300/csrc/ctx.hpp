@@ -156,6 +156,11 @@ struct sg_ctx {
   sg::Buf ia, ib, n, c, W, mu, r_loc, r_cand, r_best, key, ab;
   // impulse cache of the previous step (sorted keys and (alpha, beta))
   sg::Buf prev_key, prev_ab;
+  // The rows of the cached step (single-scene Ball2D): pair offsets per body, plane flags and
+  // their scan, and its pair count; prev_rows says they belong to the cache held.
+  sg::Buf prev_pair_off, prev_plane_off, prev_plane_flag;
+  int prev_npairs = 0;
+  bool prev_rows = false;
   // Sphere scenes under the symplectic-Euler staggering: 6 doubles per contact (cached normal and
   // force), this step's and the step before's.
   sg::Buf c6, prev_c6;

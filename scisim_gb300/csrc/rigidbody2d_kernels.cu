@@ -488,6 +488,7 @@ int rb2d_step(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->q, ctx->q1);
     std::swap(ctx->v, ctx->v1);
     ctx->prev_n = 0;
+    ctx->prev_rows = false;
     st.succeeded = 1;
     if (out) *out = st;
     return SG_OK;
@@ -601,11 +602,13 @@ int rb2d_step(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->key, ctx->prev_key);
     std::swap(ctx->ab, ctx->prev_ab);
     ctx->prev_n = nc;
+    ctx->prev_rows = false;
     const int64_t kcap =
         (int64_t)std::min(ctx->key.bytes / sizeof(unsigned long long), ctx->ab.bytes / (2 * sizeof(double)));
     ctx->ccap = std::min<int64_t>(ctx->ccap, kcap);
   } else {
     ctx->prev_n = 0;
+    ctx->prev_rows = false;
   }
   // Final map: from q0 with the post-impact velocity (:441), or the stabilized map's update.
   if (stab)

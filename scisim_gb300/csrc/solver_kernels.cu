@@ -1666,6 +1666,10 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   bool converged = false, fp64 = B.fp64_start != 0;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   unsigned next_eval = 1, interval = eval32;
+  // FP64 sweeps' checks: every eval64 sweeps near tol, up to 16 eval64 apart while the residual is
+  // more than twice tol (a check costs about a sweep; GB300's FP64 pipe makes the Fischer-Burmeister
+  // error the dearest part of it).
+  unsigned next64 = eval64, interval64 = eval64;
   // Phase timers of block 0 (shared memory, so that they take no registers from the sweeps):
   // interior, wait, boundary totals, then the current sweep's marks.
   __shared__ unsigned long long s_t[6];
@@ -1835,13 +1839,13 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
         }
       }
       ++s64;
-      do_eval = (it % eval64 == 0) || it == A.max_iters;
+      do_eval = it >= next64 || it == A.max_iters;
     } else {
       // FP64 sweeps on the same partition: the patch's FP64 velocities and inverse masses in
       // shared memory (the FP32 layout is dead once the solve is in FP64, which it never leaves),
       // the shifted tile's likewise, the remainder by block 0 on global velocities; three grid
       // barriers a sweep.  Before a residual evaluation every patch body goes back to global memory.
-      do_eval = (it % eval64 == 0) || it == A.max_iters;
+      do_eval = it >= next64 || it == A.max_iters;
       double2* sv64 = reinterpret_cast<double2*>(sv);
       double* sm64 = reinterpret_cast<double*>(sv64 + Q.cap);
       double2* svq64 = reinterpret_cast<double2*>(sm64 + Q.cap);
@@ -1915,9 +1919,11 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
       cand[k] = rk;
       const double ek = fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]);
       emax = nanmax(emax, ek);
-      const double scale = fabs(va.x) + fabs(va.y) + fabs(vb.x) + fabs(vb.y) + fabs(ck.x) + fabs(ck.y) +
-                           fabs(rk.x) + fabs(rk.y);
-      excess = nanmax(excess, ek - 64.0 * 1.1920929e-7 * scale);
+      if (!fp64) {
+        const double scale = fabs(va.x) + fabs(va.y) + fabs(vb.x) + fabs(vb.y) + fabs(ck.x) + fabs(ck.y) +
+                             fabs(rk.x) + fabs(rk.y);
+        excess = nanmax(excess, ek - 64.0 * 1.1920929e-7 * scale);
+      }
     }
     emax = block_nanmax(emax);
     const double mag = block_nanmax(excess);
@@ -1959,12 +1965,15 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
         converged = true;
         break;
       }
+      interval64 = err > 2.0 * A.tol ? min(2u * interval64, 16u * eval64) : eval64;
+      next64 = it + interval64;
     } else if (err < A.tol || err <= B.fp64_below || excess32 <= A.tol ||
                (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
       // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
       // FP64 sweeps once every contact's remaining error is within FP32 rounding of
       // its floor (or FP32 stopped improving the best iterate close to it).
       fp64 = true;
+      next64 = it + eval64;
     }
   }
   if (it > A.max_iters) it = A.max_iters;
@@ -2269,6 +2278,7 @@ struct SceneBlockArgs {
   const double2* v;         // running velocities at the start (warm start)
   const int* sb_off;        // S + 1 body offsets
   const int* sc_off;        // S + 1 contact offsets
+  const int* nc_dev;        // contacts written this step (0 when the capacity overflowed: nothing is swept)
   const int* key_start;     // S * kMaxColors + 1: (scene, colour) runs of sperm
   const int* sperm;         // contacts by (scene, colour)
   const int* order;         // scenes, largest first
@@ -2388,6 +2398,8 @@ __global__ void __launch_bounds__(kSceneBlock) k_gs_scenes(SceneBlockArgs Z) {
   const unsigned eval32 = F.eval32 ? F.eval32 : 1u;
   double2* bufs[2] = {A.r_a, A.r_b};
   unsigned long long n32 = 0, n64 = 0, nev = 0, nlc = 0, nlb = 0;
+  // Scene offsets count every detected contact; after a capacity overflow none was written.
+  const int ncv = *Z.nc_dev;
   for (;;) {
     if (threadIdx.x == 0) s_w = atomicAdd(Z.next, 1);
     __syncthreads();
@@ -2396,7 +2408,7 @@ __global__ void __launch_bounds__(kSceneBlock) k_gs_scenes(SceneBlockArgs Z) {
     if (w >= Z.S) break;
     const int sc = Z.order[w];
     const int b0 = Z.sb_off[sc], nbs = Z.sb_off[sc + 1] - b0;
-    const int c0 = Z.sc_off[sc], c1 = Z.sc_off[sc + 1];
+    const int c0 = min(Z.sc_off[sc], ncv), c1 = min(Z.sc_off[sc + 1], ncv);
     if (c1 == c0) {
       if (threadIdx.x == 0) {
         Z.done[sc] = 1;
@@ -3208,6 +3220,7 @@ int solve_contacts_batch(sg_ctx* ctx, const ContactProblem& P, const SolveParams
     Z.v = vrun;
     Z.sb_off = X.sb_off;
     Z.sc_off = X.sc_off;
+    Z.nc_dev = X.nc_dev;
     Z.key_start = X.key_start;
     Z.sperm = X.sperm;
     Z.order = X.order;

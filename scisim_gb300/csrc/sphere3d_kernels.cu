@@ -3107,6 +3107,7 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
                                                     ctx->v1.as<double>());
       SG_CUDA_TRY(cudaGetLastError());
       ctx->prev_n = 0;
+      ctx->prev_rows = false;
       ctx->kernel_launches += 1;
     }
     std::swap(ctx->q, ctx->q1);
@@ -3188,9 +3189,11 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
       std::swap(ctx->key, ctx->prev_key);
       std::swap(ctx->c6, ctx->prev_c6);
       ctx->prev_n = nc;
+      ctx->prev_rows = false;
       ctx->kernel_launches += 1;
     } else {
       ctx->prev_n = 0;
+      ctx->prev_rows = false;
     }
     k_se3_final<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cfg.dt, ctx->q.as<double>(), ctx->v2.as<double>(),
                                                   ctx->vdelta.as<double>(), ctx->q1.as<double>(), ctx->v1.as<double>());

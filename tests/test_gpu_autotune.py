@@ -1,7 +1,8 @@
 """Autotuner (sg_autotune) and tuning knobs (sg_get_tuning / sg_set_tuning).
 
 Bars: the autotuner leaves the scene exactly as it found it (same checkpoint bytes) and keeps
-the fastest of the candidates it timed; the step after tuning is the step a fresh context gives
+the fastest of the candidates it timed (a later candidate replaces an earlier one only when 3 %
+faster); the step after tuning is the step a fresh context gives
 from the same checkpoint with the chosen tuning (bit-identical); candidates that do not apply
 (two-level sweeps for spheres, everything in the FP64 form) are reported as NaN.
 """
@@ -24,7 +25,11 @@ def test_autotune_dense_pile(gpulib):
     best, ms = ctx.autotune(trial_steps=2, first_iteration=421)
     assert ctx.checkpoint() == before, "the autotuner must restore the state it started from"
     assert np.all(np.isfinite(ms)) and np.all(ms > 0.0)
-    i = int(np.argmin(ms))
+    # The rule: candidates in order, a later one replaces the kept one only when 3 % faster.
+    i = 0
+    for j in range(1, len(ms)):
+        if ms[j] < 0.97 * ms[i]:
+            i = j
     assert best["two_level"] == (1 if i < 3 else 0) and best["check_interval"] == (8, 16, 32)[i % 3]
     assert ctx.tuning() == best
     ctx.step(1, first_iteration=421)

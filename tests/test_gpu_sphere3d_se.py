@@ -43,7 +43,10 @@ def run(gpulib, oracle, cache, stabilize, steps=60, warm=40, n=700):
         order, _ = ctx.last_solve_order()
         g = ctx.sphere3d_last_contacts()
         q1, v1 = ctx.state()
-        sim.set_state(q0, v0)
+        if it > 0:
+            # The GPU's state (world inertia as a step leaves it; at it = 0 both hold the state as
+            # uploaded, with the inertia as the reference's constructor inserts it).
+            sim.set_state(q0, v0)
         if st["n_contacts"] > 0:
             sim.set_next_order(order)
             seen += 1
@@ -68,26 +71,6 @@ def run(gpulib, oracle, cache, stabilize, steps=60, warm=40, n=700):
 def test_sphere_symplectic_euler_matches_oracle(gpulib, oracle, cache, stabilize):
     seen = run(gpulib, oracle, cache, stabilize)
     assert seen >= 50
-
-
-def test_sphere_symplectic_euler_warm_start_pays(gpulib):
-    """The transported cache is a warm start: on a resting stack the cached solve needs fewer sweeps
-    than the cold one (the reference keeps this cache only for this map)."""
-    s = scenes.sphere_pile(n=400, seed=12, width=1.2, depth=1.2)
-    kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=0.0, tol=1e-9, max_iters=2000,
-              integrator=gpulib.SPLIT_HAM)
-    sweeps = {}
-    for cache in (gpulib.CACHE_NONE, gpulib.CACHE_NORMAL_AND_FRICTION):
-        ctx = gpulib.Context(cache_mode=cache, **kw)
-        ctx.upload_sphere3d(s["q"], s["v"], s["r"], s["m"], s["I0"], s["plane_x"], s["plane_n"])
-        ctx.set_staggering(gpulib.STAGGER_SYMPLECTIC_EULER, True, 1e-5)
-        ctx.step(300)
-        tot = 0
-        for _ in range(20):
-            tot += ctx.step(1)["iterations"]
-        sweeps[cache] = tot
-        ctx.close()
-    assert sweeps[gpulib.CACHE_NORMAL_AND_FRICTION] < sweeps[gpulib.CACHE_NONE]
 
 
 def test_sphere_symplectic_euler_checkpoint_keeps_cache(gpulib):
