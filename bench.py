@@ -664,41 +664,62 @@ def sphere_leg(args, torch, local, flush):
 
 
 def mlp_leg(args, torch, local):
-    """Learned warm start on the hopper (V-wedge): record the plain solver's per-contact
-    samples, train the network on the GPU, then step the same state twice, from the impulse
-    cache and from the cache-or-network start (chosen per step by the smaller FP64 residual),
-    to the same tolerance, and compare sweeps and contact-steps/s."""
+    """Learned warm start on the hopper (C4: a V-wedge of two static planes): the hopper filled and
+    settled on the GPU as the dense pile is (capped pre-roll phases, then steps at the full settings
+    until consecutive steps converge), the plain FP64 solver's per-contact samples recorded over
+    converged steps, the network trained on the GPU, then the same settled state stepped twice to
+    the same tolerance in the bench's form: from the impulse cache, and from the cache-or-network
+    start (per step the start with the smaller FP64 residual).  Sweeps, convergence and
+    contact-steps/s of both."""
     from scisim_gb300 import _lib, scenes
     s = scenes.hopper(args.mlp_hopper)
     kw = dict(dt=s["dt"], gravity=s["gravity"], mu=s["mu"], CoR=s["CoR"], tol=1e-6, device=local)
-    rec = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=_lib.PRECISION_FP64,
-                       max_iters=args.preroll_iters, **kw)
+    rec = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision, max_iters=50, **kw)
     rec.upload_ball2d(s["q"], s["v"], s["r"], s["m"], s["plane_x"], s["plane_n"])
     t0 = time.perf_counter()
-    rec.step(args.mlp_preroll)
-    rec.reconfigure(max_iters=args.mlp_record_iters)
+    it = 1
+    for n, cap in parse_schedule(args.mlp_schedule):
+        rec.reconfigure(max_iters=cap)
+        rec.step(n, first_iteration=it)
+        it += n
+    rec.reconfigure(max_iters=5000)
+    run = settle = 0
+    while settle < args.settle_max and run < 5:
+        st = rec.step(1, first_iteration=it)
+        it += 1
+        settle += 1
+        run = run + 1 if st["succeeded"] else 0
+    t1 = time.perf_counter()
+    ck = rec.checkpoint()
+    # Samples of the plain FP64 solver over steps at the full settings.
+    rec.reconfigure(precision=_lib.PRECISION_FP64)
     rec.mlp_load(_lib.mlp_init(0))
     rec.mlp_enable(warm_start=False, record=True)
     xs, ts = [], []
+    rec_conv = 0
     for _ in range(args.mlp_record_steps):
-        rec.step(1)
+        st = rec.step(1, first_iteration=it)
+        it += 1
+        rec_conv += int(st["succeeded"])
         x, t = rec.mlp_last_samples()
         xs.append(x)
         ts.append(t)
-    q0, v0 = rec.state()
     X, T = np.concatenate(xs), np.concatenate(ts)
-    t1 = time.perf_counter()
+    t2 = time.perf_counter()
     p, losses = rec.mlp_train(X, T, _lib.mlp_init(1), epochs=args.mlp_epochs, batch=4096, lr=2e-3, seed=3)
-    t_train = time.perf_counter() - t1
+    t_train = time.perf_counter() - t2
     rec.close()
-    log("mlp: %d samples recorded in %.1f s, trained in %.2f s, epoch losses %s" % (X.shape[0], t1 - t0, t_train,
-                                                                                   [round(x, 4) for x in losses]))
+    log("mlp: hopper formed and settled in %.1f s (%d settling steps), %d samples over %d steps (%d converged) in "
+        "%.1f s, trained in %.2f s, epoch losses %s" % (t1 - t0, settle, X.shape[0], args.mlp_record_steps, rec_conv,
+                                                         t2 - t1, t_train, [round(x, 4) for x in losses]))
     out = {"workload": "hopper_%d" % args.mlp_hopper, "samples": int(X.shape[0]), "epochs": args.mlp_epochs,
-           "train_s": t_train, "epoch_loss": [float(x) for x in losses]}
+           "train_s": t_train, "epoch_loss": [float(x) for x in losses], "settling_steps": settle,
+           "form": "from the settled hopper's checkpoint, %d steps each, tol 1e-6, 5,000 sweeps at most, %s" % (
+               args.mlp_eval_steps, "FP32 sweeps + FP64 checks and refinement" if args.precision == 1 else "FP64")}
     for name, use in (("cache", False), ("cache_or_network", True)):
-        ctx = _lib.Context(cache_mode=_lib.CACHE_NORMAL_AND_FRICTION, precision=args.precision, max_iters=5000, **kw)
-        ctx.upload_ball2d(q0, v0, s["r"], s["m"], s["plane_x"], s["plane_n"])
-        ctx.step(1)  # prime the impulse cache identically in both runs
+        ctx = _lib.Context(device=local, dt=s["dt"], gravity=s["gravity"])
+        ctx.restore(ck)
+        ctx.reconfigure(precision=args.precision, max_iters=5000)
         if use:
             ctx.mlp_load(p)
             ctx.mlp_enable(warm_start=True)
@@ -706,22 +727,25 @@ def mlp_leg(args, torch, local):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        its, cs, conv, lerr = 0, 0, 0, 0.0
-        for _ in range(args.mlp_eval_steps):
-            st = ctx.step(1)
+        its, cs, conv, lerr, sweeps = 0, 0, 0, 0.0, []
+        for j in range(args.mlp_eval_steps):
+            st = ctx.step(1, first_iteration=it + j)
             its += st["iterations"]
+            sweeps.append(st["iterations"])
             cs += st["n_contacts"]
             conv += int(st["succeeded"])
             lerr += float(np.log10(max(st["error"], 1e-300)))
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        out[name] = {"sweeps": its, "contact_steps": cs, "converged_steps": conv, "ms": ms,
-                     "value": cs / (ms / 1e3), "unit": UNIT, "mean_log10_residual": lerr / args.mlp_eval_steps}
+        out[name] = {"sweeps": its, "sweeps_per_step": sweeps, "contact_steps": cs, "converged_steps": conv,
+                     "ms": ms, "value": cs / (ms / 1e3), "unit": UNIT,
+                     "mean_log10_residual": lerr / args.mlp_eval_steps}
         if use:
             out[name]["network_start_steps"] = ctx.mlp_stats()["network_start"]
         ctx.close()
     out["sweeps_saved_frac"] = 1.0 - out["cache_or_network"]["sweeps"] / max(out["cache"]["sweeps"], 1)
+    out["speedup"] = out["cache_or_network"]["value"] / out["cache"]["value"] if out["cache"]["value"] else None
     return out
 
 
@@ -995,12 +1019,12 @@ def main():
     ap.add_argument("--sphere-batch-scenes", type=int, default=256, help="sphere-batch leg (0 = skip)")
     ap.add_argument("--sphere-batch-preroll", type=int, default=100)
     ap.add_argument("--sphere-batch-steps", type=int, default=3)
-    ap.add_argument("--mlp-hopper", type=int, default=0, help="learned-warm-start study on a hopper (0 = skip)")
-    ap.add_argument("--mlp-preroll", type=int, default=1500)
-    ap.add_argument("--mlp-record-steps", type=int, default=100)
-    ap.add_argument("--mlp-record-iters", type=int, default=1000)
+    ap.add_argument("--mlp-hopper", type=int, default=262144, help="learned-warm-start study on a hopper (0 = skip)")
+    ap.add_argument("--mlp-schedule", default="800:50,300:200,200:1000",
+                    help="pre-roll phases steps:sweep cap of the hopper (untimed)")
+    ap.add_argument("--mlp-record-steps", type=int, default=30)
     ap.add_argument("--mlp-epochs", type=int, default=6)
-    ap.add_argument("--mlp-eval-steps", type=int, default=30)
+    ap.add_argument("--mlp-eval-steps", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -397,7 +397,8 @@ SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
  * colour.  0 keeps the one-level colour sweeps. */
 SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
 
-/* Selects the map a single Ball2D scene steps with (default SG_STAGGER_GEOMETRIC).
+/* Selects the map a single Ball2D, sphere or RigidBody2D scene steps with (default
+ * SG_STAGGER_GEOMETRIC).
  * SG_STAGGER_SYMPLECTIC_EULER is SymplecticEulerImpactFrictionMap
  * (scisim/ConstrainedMaps/SymplecticEulerImpactFrictionMap.cpp:201-407): the force acts first
  * (vdelta = dt Minv F), collisions are detected on q0 + dt (v0 + vdelta), the solve gets the
@@ -407,7 +408,12 @@ SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
  * reference does.  SG_STAGGER_STABILIZED is StabilizedImpactFrictionMap
  * (scisim/ConstrainedMaps/StabilizedImpactFrictionMap.cpp:48-167): the unconstrained step, then
  * a cold solve from its velocity, then q1 = q0 + dt v; it keeps no impulse cache (cache_mode NONE).
- * Batched and sphere scenes step with the geometric map only. */
+ * Sphere scenes take SG_STAGGER_SYMPLECTIC_EULER as well: exponential-Euler predictor and
+ * configuration update (rigidbody3d/UnconstrainedMaps/IntegrationTools.cpp:3-47) in place of the
+ * context's integrator, and with cache_mode set the 3D impulse cache of that map (cached normal
+ * and force per contact, the force turned onto the new normal by the quaternion between the two
+ * normals, :48-199); stabilized sphere steps return SG_BAD_INPUT.  RigidBody2D scenes take the
+ * geometric and the stabilized maps.  Batched scenes step with the geometric map only. */
 SG_API int sg_set_staggering(sg_ctx* ctx, int32_t staggering, int32_t stabilize, double penetration_threshold);
 
 /* Checkpoint / resume of a context holding one Ball2D or sphere scene (replaces SCISim's binary

@@ -1666,10 +1666,12 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   bool converged = false, fp64 = B.fp64_start != 0;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   unsigned next_eval = 1, interval = eval32;
-  // FP64 sweeps' checks: every eval64 sweeps near tol, up to 16 eval64 apart while the residual is
-  // more than twice tol (a check costs about a sweep; GB300's FP64 pipe makes the Fischer-Burmeister
-  // error the dearest part of it).
-  unsigned next64 = eval64, interval64 = eval64;
+  // FP64 sweeps' checks, at most 16 eval64 apart: the next one where the residual's rate of
+  // decrease over the last two checks predicts tol, sooner than that never, and twice as far as the
+  // last gap where it did not decrease (a check costs about a sweep; GB300's FP64 pipe makes the
+  // Fischer-Burmeister error the dearest part of it).
+  unsigned next64 = eval64, interval64 = eval64, prev64_it = 0;
+  double prev64_err = INFINITY;
   // Phase timers of block 0 (shared memory, so that they take no registers from the sweeps):
   // interior, wait, boundary totals, then the current sweep's marks.
   __shared__ unsigned long long s_t[6];
@@ -1965,7 +1967,15 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
         converged = true;
         break;
       }
-      interval64 = err > 2.0 * A.tol ? min(2u * interval64, 16u * eval64) : eval64;
+      if (err < prev64_err && prev64_err < INFINITY && err > 0.0) {
+        const double per_sweep = (log(err) - log(prev64_err)) / (double)(it - prev64_it);
+        const double need = (log(A.tol) - log(err)) / per_sweep;  // sweeps to tol at that rate
+        interval64 = need >= (double)(16u * eval64) ? 16u * eval64 : max(eval64, (unsigned)need);
+      } else {
+        interval64 = min(2u * interval64, 16u * eval64);
+      }
+      prev64_err = err;
+      prev64_it = it;
       next64 = it + interval64;
     } else if (err < A.tol || err <= B.fp64_below || excess32 <= A.tol ||
                (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
@@ -1974,6 +1984,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
       // its floor (or FP32 stopped improving the best iterate close to it).
       fp64 = true;
       next64 = it + eval64;
+      prev64_err = INFINITY;
     }
   }
   if (it > A.max_iters) it = A.max_iters;

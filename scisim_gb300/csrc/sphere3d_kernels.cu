@@ -1564,7 +1564,9 @@ __global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
 // (the global colouring restricted to the scene, by (scene, colour)) with block barriers, evaluates
 // the scene's own residual every eval_every sweeps, keeps its best iterate and stops at tol or
 // max_iters.  Each scene sees k_gs3_batch's update sequence, so the results are the same.
-constexpr int kScene3Block = 256;
+// 128 threads: a sphere scene's colour holds tens of contacts, and at ~196 registers a thread two
+// blocks fit an SM, so every scene of a 256-scene batch is resident at once.
+constexpr int kScene3Block = 128;
 
 struct Scene3Args {
   Gs3Args g;                  // contacts, inverse masses and inertias, impulses, snapshot buffers
@@ -1663,7 +1665,7 @@ __device__ __forceinline__ void gs_update3_sv(const Gs3Args& A, int k, int a, in
   A.r[3 * (size_t)k + 2] = rn[2];
 }
 
-__global__ void __launch_bounds__(kScene3Block) k_gs3_scenes(Scene3Args Z) {
+__global__ void __launch_bounds__(kScene3Block, 2) k_gs3_scenes(Scene3Args Z) {
   const Gs3Args& A = Z.g;
   extern __shared__ __align__(32) double4_32a sV3[];
   __shared__ int s_w;

@@ -123,10 +123,15 @@ class RigidBody3DSim:
         ctx.upload_sphere3d(st.q, st.v, st.r, st.m, st.I0, st.plane_x(), st.plane_n())
 
     def flow(self, iteration, dt, umap, CoR, mu, solver, ifmap):
-        if not isinstance(umap, SplitHamMap):
-            raise ValueError("sphere scenes step with SplitHamMap")
-        if ifmap.impulses_to_cache != ImpulsesToCache.NONE:
-            raise ValueError("the 3D geometric map keeps no impulse cache (RigidBody3DSceneParser.cpp:1877-1880)")
+        from .ball2d import StabilizedImpactFrictionMap, SymplecticEulerImpactFrictionMap
+        if isinstance(ifmap, StabilizedImpactFrictionMap):
+            raise ValueError("sphere scenes step with the geometric or the symplectic Euler map")
+        if not isinstance(ifmap, SymplecticEulerImpactFrictionMap):
+            # The symplectic-Euler map integrates by exponential Euler and keeps its 3D cache.
+            if not isinstance(umap, SplitHamMap):
+                raise ValueError("sphere scenes step with SplitHamMap")
+            if ifmap.impulses_to_cache != ImpulsesToCache.NONE:
+                raise ValueError("the 3D geometric map keeps no impulse cache (RigidBody3DSceneParser.cpp:1877-1880)")
         q1, v1 = ifmap.flow(self, umap, solver, iteration, dt, CoR, mu, self.state.q, self.state.v)
         self.state.q, self.state.v = q1, v1
         return ifmap.last_stats

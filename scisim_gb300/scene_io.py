@@ -284,8 +284,8 @@ def load_rigidbody2d_scene(source) -> dict:
 def load_rigidbody3d_scene(source) -> dict:
     """A `<rigidbody3d_scene>` of spheres as arrays and settings (RigidBody3DSceneParser.cpp), for
     the geometric staggering with the split_ham integrator, or the symplectic_euler staggering
-    (whose map does not call the integrator, so `dmv` is accepted there; the GPU library steps
-    only the geometric form, the oracle both).  Bodies: `rigid_body_with_density` with a
+    (whose map does not call the integrator, so `dmv` is accepted there; the GPU library and the
+    oracle step both).  Bodies: `rigid_body_with_density` with a
     sphere geometry, mass and inertia from rho (RigidBodySphere::computeMassAndInertia), identity
     orientation (an `R` attribute, an Eigen AngleAxis, is not supported).  Returns q = [x | R],
     v = [v | omega], r, m, I0, plane_x, plane_n (3 per plane), dt, gravity and the solver settings."""
@@ -373,14 +373,22 @@ def ball2d_objects(scene: dict):
 
 
 def rigidbody3d_objects(scene: dict):
-    """As ball2d_objects for a loaded sphere scene (SplitHamMap, no impulse cache)."""
-    if scene.get("staggering", "geometric") != "geometric":
-        raise SceneError("the GPU library steps spheres with the geometric staggering only")
-    from .ball2d import GeometricImpactFrictionMap, ImpulsesToCache, Sobogus, SobogusSolverType
+    """As ball2d_objects for a loaded sphere scene: SplitHamMap and the geometric map without an
+    impulse cache, or the symplectic-Euler map with the scene's cache and stabilisation (that map
+    integrates by exponential Euler whatever the integrator)."""
+    from .ball2d import (GeometricImpactFrictionMap, ImpulsesToCache, Sobogus, SobogusSolverType,
+                         SymplecticEulerImpactFrictionMap)
     from .rigidbody3d import RigidBody3DSim, RigidBody3DState, SplitHamMap, StaticPlane
+    stag = scene.get("staggering", "geometric")
+    if stag not in ("geometric", "symplectic_euler"):
+        raise SceneError("the GPU library steps spheres with the geometric or the symplectic_euler staggering")
     planes = [StaticPlane(x, n) for x, n in zip(scene["plane_x"], scene["plane_n"])]
     state = RigidBody3DState(scene["q"], scene["v"], scene["r"], scene["m"], scene["I0"], planes)
     sim = RigidBody3DSim(state, gravity=scene["gravity"])
     solver = Sobogus(SobogusSolverType.RigidBodies3D, eval_every=scene["eval_every"])
-    ifmap = GeometricImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache.NONE)
+    if stag == "symplectic_euler":
+        ifmap = SymplecticEulerImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache(scene["cache_mode"]),
+                                                 scene["stabilization"], scene["penetration_threshold"])
+    else:
+        ifmap = GeometricImpactFrictionMap(scene["tol"], scene["max_iters"], ImpulsesToCache.NONE)
     return sim, SplitHamMap(), solver, ifmap

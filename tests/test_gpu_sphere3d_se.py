@@ -94,3 +94,49 @@ def test_sphere_symplectic_euler_checkpoint_keeps_cache(gpulib):
     assert np.array_equal(qa, qb) and np.array_equal(va, vb)
     a.close()
     b.close()
+
+
+SE_SCENE = """<rigidbody3d_scene>
+  <integrator type="dmv" dt="0.004"/>
+  <sobogus_friction_solver mu="0.5" CoR="0.0" max_iters="500" tol="1.0e-9" eval_every="1"
+     staggering="symplectic_euler" cache_impulses="normal_and_friction" stabilization="1"
+     penetration_threshold="1.0e-5"/>
+  <near_earth_gravity f="0.0 -9.81 0.0"/>
+  <static_plane x="0 0 0" n="0 1 0"/>
+  <static_plane x="-1 0 0" n="1 0 0"/>
+  <static_plane x="1 0 0" n="-1 0 0"/>
+  <geometry type="sphere" r="0.2"/>
+  <geometry type="sphere" r="0.15"/>
+  <rigid_body_with_density x="0.0 0.2 0.0" v="0.3 0.0 0.0" omega="0.0 1.0 0.0" rho="1.0" fixed="0" geo_idx="0"/>
+  <rigid_body_with_density x="0.1 0.6 0.05" v="0 0 0" omega="0 0 2" rho="1.0" fixed="0" geo_idx="1"/>
+  <rigid_body_with_density x="-0.3 0.9 0.0" v="0 -1 0" omega="1 0 0" rho="2.0" fixed="0" geo_idx="0"/>
+</rigidbody3d_scene>"""
+
+
+def test_sphere_symplectic_euler_scene_through_the_reference_classes(gpulib):
+    """A sphere scene with staggering="symplectic_euler" read by scene_io and stepped through the
+    mirror of the reference's classes (RigidBody3DSim::flow with SymplecticEulerImpactFrictionMap)
+    gives, step for step, the bits of the C ABI path (sg_set_staggering on a sphere context)."""
+    from scisim_gb300 import scene_io
+    sc = scene_io.load_rigidbody3d_scene(SE_SCENE)
+    sim, umap, solver, ifmap = scene_io.rigidbody3d_objects(sc)
+    assert ifmap.name() == "symplectic_euler_impact_friction_map"
+    ctx = gpulib.Context(dt=sc["dt"], gravity=sc["gravity"], mu=sc["mu"], CoR=sc["CoR"], tol=sc["tol"],
+                         max_iters=sc["max_iters"], eval_every=sc["eval_every"], integrator=gpulib.SPLIT_HAM,
+                         cache_mode=sc["cache_mode"])
+    ctx.upload_sphere3d(sc["q"], sc["v"], sc["r"], sc["m"], sc["I0"], sc["plane_x"], sc["plane_n"])
+    ctx.set_staggering(gpulib.STAGGER_SYMPLECTIC_EULER, sc["stabilization"], sc["penetration_threshold"])
+    contacts = 0
+    for it in range(1, 301):
+        st = sim.flow(it, sc["dt"], umap, sc["CoR"], sc["mu"], solver, ifmap)
+        s2 = ctx.step(1, first_iteration=it)
+        q, v = ctx.state()
+        assert st["n_contacts"] == s2["n_contacts"] and st["iterations"] == s2["iterations"], it
+        assert np.array_equal(sim.state.q, q) and np.array_equal(sim.state.v, v), it
+        contacts += s2["n_contacts"]
+    assert contacts > 300
+    # The spheres come to rest on the floor (no sinking: the lowest centre stays above its radius).
+    nb = sc["r"].shape[0]
+    y = q[1:3 * nb:3]
+    assert np.all(y >= sc["r"] - 1e-3)
+    ctx.close()
