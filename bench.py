@@ -607,7 +607,7 @@ def sphere_batch_leg(args, torch, local, flush):
            "plain_fp64_gpu": {"value": plain, "unit": UNIT, "sample_scenes": len(pick),
                               "form": "one context per scene, FP64, same steps from the same state"},
            "batched_over_plain": value / plain if plain else None, "gpu_launches": prof["kernel_launches"],
-           "roofline": step_roofline("k_gs3_scenes (one block per scene)", gs3_bytes(prof), prof["gs_ms"] or ms,
+           "roofline": step_roofline("k_gs3_batch", gs3_bytes(prof), prof["gs_ms"] or ms,
                                      "the sweep kernel's CUDA events" if prof["gs_ms"] else "the whole timed steps"),
            "fp32_refine": {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.sphere_batch_steps,
                            "scenes_converged_last_step": int(st32["succeeded"].sum()),
@@ -1009,7 +1009,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=60.0,
                     help="seconds of oracle stepping after which the CPU legs start no further step")
     ap.add_argument("--precision", type=int, default=1, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
-    ap.add_argument("--batch-scenes", type=int, default=512, help="batched-scene leg (0 = skip)")
+    ap.add_argument("--batch-scenes", type=int, default=4096, help="batched-scene leg (0 = skip)")
     ap.add_argument("--batch-preroll", type=int, default=40)
     ap.add_argument("--batch-steps", type=int, default=8)
     ap.add_argument("--batch-plain-scenes", type=int, default=16)

@@ -289,7 +289,7 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                  &ctx->r_loc, &ctx->r_cand, &ctx->r_best, &ctx->key, &ctx->ab, &ctx->prev_key, &ctx->prev_ab,
                  &ctx->color, &ctx->perm, &ctx->body_cnt, &ctx->body_off, &ctx->body_fill, &ctx->body_adj,
                  &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2,
-                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->prev_pair_off, &ctx->prev_plane_off,
+                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->pair_slots, &ctx->aabb32, &ctx->prev_pair_off, &ctx->prev_plane_off,
                  &ctx->prev_plane_flag, &ctx->vdelta, &ctx->rb_I, &ctx->rb_Iinv,
                  &ctx->pos0, &ctx->pos1, &ctx->rb_ct, &ctx->rb_vrun};
   for (Buf* b : bufs) release(*b);
@@ -909,7 +909,7 @@ int sg_sphere3d_batch_upload(sg_ctx* ctx, int32_t S, const int32_t* body_off, co
   if (int e = upload(ctx, ctx->s_mu, mu, sizeof(double) * (size_t)S)) return e;
   if (int e = upload(ctx, ctx->s_CoR, CoR, sizeof(double) * (size_t)S)) return e;
   if (int e = sphere3d_batch_setup(ctx, sf[S], cells)) return e;
-  if (int e = scene_work_order(ctx, S, body_off, kScene3MaxBodies)) return e;
+  ctx->s_smax = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }

@@ -116,10 +116,15 @@ __global__ void k_final_se(int nb, double dt, const double2* __restrict__ q0, co
 }
 
 // Bounds of all boxes and the largest extent per axis (exact: min/max are order free).
-__global__ void k_bounds(int n, const double4_32a* __restrict__ aabb, GridParams* gp) {
+// With aabb32 non-null it also writes each box rounded outward to FP32 (min corners down, max
+// corners up), the pair scans' prefilter: FP32 boxes apart imply FP64 boxes apart.
+__global__ void k_bounds(int n, const double4_32a* __restrict__ aabb, GridParams* gp, float4* __restrict__ aabb32) {
   double mn0 = INFINITY, mn1 = INFINITY, mx0 = -INFINITY, mx1 = -INFINITY, e0 = 0.0, e1 = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double4_32a b = aabb[i];
+    if (aabb32)
+      aabb32[i] = make_float4(__double2float_rd(b.x), __double2float_rd(b.y), __double2float_ru(b.z),
+                              __double2float_ru(b.w));
     mn0 = fmin(mn0, b.x);
     mn1 = fmin(mn1, b.y);
     mx0 = fmax(mx0, b.z);
@@ -223,6 +228,10 @@ __device__ __forceinline__ void ccd_coeffs(double2 q0a, double2 q1a, double ra, 
 }
 
 __device__ __forceinline__ bool ccd_happens(double c0, double c1, double c2, double* t) {
+  // Touching or overlapping at t = 0: the roots below give root1 >= 0 >= root0 for any c1, c2 (a
+  // quadratic with c2 >= 0 and c0 <= 0), so the answer is yes without the square root and the
+  // divisions; only the time of impact needs them.
+  if (!t && c0 <= 0.0) return true;
   if (c2 != 0.0) {
     const double c1c1 = c1 * c1;
     const double fc2c0 = 4.0 * c2 * c0;
@@ -244,6 +253,7 @@ __device__ __forceinline__ bool ccd_happens(double c0, double c1, double c2, dou
 
 struct PairScan {
   const double4_32a* aabb;
+  const float4* aabb32;  // the boxes rounded outward to FP32 (prefilter)
   const GridParams* gp;
   const int* cell_start;
   const int* sorted;
@@ -258,6 +268,7 @@ struct PairScan {
 template <bool kCcd, typename F>
 __device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
   const double4_32a bi = s.aabb[i];
+  const float4 fi = s.aabb32[i];
   const GridParams& g = *s.gp;
   const int cx = cell_coord(bi.x, g.origin[0], g.h, g.dims[0]);
   const int cy = cell_coord(bi.y, g.origin[1], g.h, g.dims[1]);
@@ -275,6 +286,8 @@ __device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
       for (int p = s.cell_start[cell]; p < e; ++p) {
         const int j = s.sorted[p];
         if (j <= i) continue;
+        const float4 fj = s.aabb32[j];
+        if (fi.z < fj.x || fi.w < fj.y || fj.z < fi.x || fj.w < fi.y) continue;
         if (!aabb_overlap(bi, s.aabb[j])) continue;
         if (kCcd) {
           double c0, c1, c2;
@@ -287,21 +300,44 @@ __device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
   }
 }
 
+// The counting pass keeps each box's first kPairSlots partners (in visiting order) so that the
+// writing pass of a box with at most that many only sorts them; a box with more visits again.
+constexpr int kPairSlots = 8;
+
 template <bool kCcd>
-__global__ void k_pair_count(int n, PairScan s, int* __restrict__ cnt) {
+__global__ void k_pair_count(int n, PairScan s, int* __restrict__ cnt, int* __restrict__ slots) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c = 0;
-  visit_pairs<kCcd>(s, i, [&](int) { ++c; });
+  int* mine = slots + (size_t)i * kPairSlots;
+  visit_pairs<kCcd>(s, i, [&](int j) {
+    if (c < kPairSlots) mine[c] = j;
+    ++c;
+  });
   cnt[i] = c;
 }
 
 template <bool kCcd>
-__global__ void k_pair_write(int n, PairScan s, const int* __restrict__ off, int* __restrict__ out_a,
-                             int* __restrict__ out_b) {
+__global__ void k_pair_write(int n, PairScan s, const int* __restrict__ off, const int* __restrict__ slots,
+                             int* __restrict__ out_a, int* __restrict__ out_b) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int base = off[i];
+  const int total = off[i + 1] - base;
+  if (total <= kPairSlots) {
+    const int* mine = slots + (size_t)i * kPairSlots;
+    for (int c = 0; c < total; ++c) {
+      const int j = mine[c];
+      int p = base + c;
+      while (p > base && out_b[p - 1] > j) {
+        out_b[p] = out_b[p - 1];
+        --p;
+      }
+      out_b[p] = j;
+    }
+    for (int k = 0; k < total; ++k) out_a[base + k] = i;
+    return;
+  }
   int c = 0;
   visit_pairs<kCcd>(s, i, [&](int j) {
     // insertion into the sorted segment [base, base + c)
@@ -874,7 +910,8 @@ int broadphase_build_grid(sg_ctx* ctx, const double* aabb, int n) {
   const double4_32a* bx = reinterpret_cast<const double4_32a*>(aabb);
   k_bounds_init<<<1, 1, 0, ctx->stream>>>(gp);
   const int nblk = std::min(blocks_for(n), ctx->num_sms * 8);
-  k_bounds<<<std::max(nblk, 1), kBlock, 0, ctx->stream>>>(n, bx, gp);
+  if (int r = grow(ctx->aabb32, sizeof(float4) * (size_t)std::max(n, 1))) return r;
+  k_bounds<<<std::max(nblk, 1), kBlock, 0, ctx->stream>>>(n, bx, gp, ctx->aabb32.as<float4>());
   k_grid_setup<<<1, 1, 0, ctx->stream>>>(gp, cap);
   SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_count.p, 0, sizeof(int) * (size_t)(cap + 1), ctx->stream));
   SG_CUDA_TRY(cudaMemsetAsync(ctx->cell_fill.p, 0, sizeof(int) * (size_t)(cap + 1), ctx->stream));
@@ -890,6 +927,7 @@ int broadphase_build_grid(sg_ctx* ctx, const double* aabb, int n) {
 static PairScan make_scan(sg_ctx* ctx, const double* aabb, bool ccd) {
   PairScan s;
   s.aabb = reinterpret_cast<const double4_32a*>(aabb);
+  s.aabb32 = ctx->aabb32.as<float4>();
   s.gp = ctx->grid.as<GridParams>();
   s.cell_start = ctx->cell_start.as<int>();
   s.sorted = ctx->sorted.as<int>();
@@ -903,11 +941,14 @@ static PairScan make_scan(sg_ctx* ctx, const double* aabb, bool ccd) {
 int broadphase_count_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd) {
   if (int r = grow(ctx->pair_cnt, sizeof(int) * (size_t)(n + 1))) return r;
   if (int r = grow(ctx->pair_off, sizeof(int) * (size_t)(n + 1))) return r;
+  if (int r = grow(ctx->pair_slots, sizeof(int) * kPairSlots * (size_t)std::max(n, 1))) return r;
   const PairScan s = make_scan(ctx, aabb, ccd);
   if (ccd)
-    k_pair_count<true><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_cnt.as<int>());
+    k_pair_count<true><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_cnt.as<int>(),
+                                                                 ctx->pair_slots.as<int>());
   else
-    k_pair_count<false><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_cnt.as<int>());
+    k_pair_count<false><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_cnt.as<int>(),
+                                                                  ctx->pair_slots.as<int>());
   SG_CUDA_TRY(cudaGetLastError());
   return scan_exclusive(ctx, ctx->pair_cnt.as<int>(), ctx->pair_off.as<int>(), n);
 }
@@ -915,9 +956,11 @@ int broadphase_count_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd) {
 int broadphase_write_pairs(sg_ctx* ctx, const double* aabb, int n, bool ccd, int* out_a, int* out_b) {
   const PairScan s = make_scan(ctx, aabb, ccd);
   if (ccd)
-    k_pair_write<true><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_off.as<int>(), out_a, out_b);
+    k_pair_write<true><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_off.as<int>(),
+                                                                 ctx->pair_slots.as<int>(), out_a, out_b);
   else
-    k_pair_write<false><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_off.as<int>(), out_a, out_b);
+    k_pair_write<false><<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, s, ctx->pair_off.as<int>(),
+                                                                  ctx->pair_slots.as<int>(), out_a, out_b);
   SG_CUDA_TRY(cudaGetLastError());
   return SG_OK;
 }

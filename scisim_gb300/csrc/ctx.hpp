@@ -156,6 +156,8 @@ struct sg_ctx {
   sg::Buf ia, ib, n, c, W, mu, r_loc, r_cand, r_best, key, ab;
   // impulse cache of the previous step (sorted keys and (alpha, beta))
   sg::Buf prev_key, prev_ab;
+  sg::Buf pair_slots;  // the pair count's first partners per box (8 each), read by the pair write
+  sg::Buf aabb32;      // the boxes rounded outward to FP32, the pair scans' prefilter
   // The rows of the cached step (single-scene Ball2D): pair offsets per body, plane flags and
   // their scan, and its pair count; prev_rows says they belong to the cache held.
   sg::Buf prev_pair_off, prev_plane_off, prev_plane_flag;
@@ -330,11 +332,10 @@ int coop_grid(sg_ctx* ctx, K kernel, long work, int block, int max_per_sm = 64) 
 // capture) and one step enqueued without host synchronisation.
 int batch2d_reserve(sg_ctx* ctx, int cap);
 int batch2d_step_enqueue(sg_ctx* ctx);
-// One block per scene: scenes of at most this many discs (24 B of shared memory each) or spheres
-// (64 B each) are swept by one block; the per-scene kernels' shared-memory limits are set by
-// scene_blocks_prepare (once per context, outside any capture).
+// One block per scene: Ball2D scenes of at most this many discs (24 B of shared memory each) are
+// swept by one block; the per-scene kernels' shared-memory limits are set by scene_blocks_prepare
+// (once per context, outside any capture).
 constexpr int kSceneBlockMaxBodies = 8192;
-constexpr int kScene3MaxBodies = 3072;
 int scene_blocks_prepare(int smax);
 
 // Learned warm start (mlp_kernels.cu).

@@ -33,6 +33,7 @@ constexpr int kBlock = 256;
 constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (fewer barrier arrivals)
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
 constexpr int kPatchBlock = 384;  // two-level kernel
+constexpr int kColorBlock = 1024;  // colouring kernel
 // FP32 form: a start whose FP64 residual is below this many tolerances is swept in FP64.
 // FP64 sweeps a start near tol first runs one-level before the two-level partition is set up.
 constexpr unsigned kFp64Probe = 4;
@@ -177,7 +178,7 @@ struct ColorArgs {
   int max_rounds;
 };
 
-__global__ void k_color_jp(ColorArgs A) {
+__global__ void __launch_bounds__(kColorBlock, 1) k_color_jp(ColorArgs A) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   if (A.nc_dev) A.nc = *A.nc_dev;
@@ -2668,8 +2669,11 @@ int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int*
   ColorArgs CA{nc, nc_dev, ia, ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit,
                4096};
   void* args[] = {&CA};
-  const int g = coop_grid(ctx, k_color_jp, nc, kBlock);
-  SG_CUDA_TRY(launch_cooperative((const void*)k_color_jp, g, kBlock, args, s));
+  // One 1,024-thread block per SM: the colouring is a chain of grid barriers (a Jones-Plassmann
+  // round each, a colour class each in the recolouring passes), and a barrier's cost grows with the
+  // blocks arriving at it.
+  const int g = coop_grid(ctx, k_color_jp, nc, kColorBlock, 1);
+  SG_CUDA_TRY(launch_cooperative((const void*)k_color_jp, g, kColorBlock, args, s));
   ctx->kernel_launches += 4;  // body_count, body_fill, body_sort, colouring
   return SG_OK;
 }

@@ -1559,250 +1559,6 @@ __global__ void __launch_bounds__(kGs3Block, 1) k_gs3(Gs3Args A) {
 }
 
 // ---------------------------------------------------------------------------
-// Batched sphere scenes, one scene per block: the block takes the next scene of a largest-first
-// work list, keeps the scene's (v, omega) in shared memory, sweeps its contacts colour by colour
-// (the global colouring restricted to the scene, by (scene, colour)) with block barriers, evaluates
-// the scene's own residual every eval_every sweeps, keeps its best iterate and stops at tol or
-// max_iters.  Each scene sees k_gs3_batch's update sequence, so the results are the same.
-// 128 threads: a sphere scene's colour holds tens of contacts, and at ~196 registers a thread two
-// blocks fit an SM, so every scene of a 256-scene batch is resident at once.
-constexpr int kScene3Block = 128;
-
-struct Scene3Args {
-  Gs3Args g;                  // contacts, inverse masses and inertias, impulses, snapshot buffers
-  const double4_32a* V;       // running velocities at the start
-  const int* sb_off;          // S + 1 body offsets
-  const int* sc_off;          // S + 1 contact offsets
-  const int* key_start;       // S * kMaxColors + 1
-  const int* sperm;           // contacts by (scene, colour)
-  const int* order;           // scenes, largest first
-  int* next;                  // work-list counter
-  int S;
-  int smax;                   // shared-memory body slots (largest scene)
-  double* best;
-  int* done;
-  unsigned* iters;
-  unsigned long long* unconverged;
-  unsigned long long* work;   // [1] contact updates, [2] contact evaluations
-};
-
-// local_u3 on shared-memory velocities (la, lb: the bodies' slots, lb < 0 for a plane).
-__device__ __forceinline__ void local_u3_sv(const Contacts3& C, int k, const double4_32a* sV, double* u, int la, int lb,
-                                            const double* E, const double* Aa, const double* Ab) {
-  const double4_32a l_a = sV[2 * la], w_a = sV[2 * la + 1];
-  const double va[3] = {l_a.x, l_a.y, l_a.z}, oa[3] = {w_a.x, w_a.y, w_a.z};
-  double vb[3] = {0.0, 0.0, 0.0}, ob[3] = {0.0, 0.0, 0.0};
-  const bool has_b = lb >= 0;
-  if (has_b) {
-    const double4_32a l_b = sV[2 * lb], w_b = sV[2 * lb + 1];
-    vb[0] = l_b.x;
-    vb[1] = l_b.y;
-    vb[2] = l_b.z;
-    ob[0] = w_b.x;
-    ob[1] = w_b.y;
-    ob[2] = w_b.z;
-  }
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    double h = dot3(E + 3 * i, va);
-    if (i > 0) h = h + dot3(Aa + 3 * (i - 1), oa);
-    if (has_b) {
-      double hb = dot3(E + 3 * i, vb);
-      if (i > 0) hb = hb + dot3(Ab + 3 * (i - 1), ob);
-      h = h - hb;
-    }
-    u[i] = h + C.c[3 * (size_t)k + i];
-  }
-}
-
-// gs_update3's arithmetic on shared-memory velocities (la, lb: the bodies' slots, lb < 0 for a
-// plane; a, b: their global indices for the inverse masses and inertias).
-__device__ __forceinline__ void gs_update3_sv(const Gs3Args& A, int k, int a, int b, int la, int lb, double4_32a* sV) {
-  const Contacts3& C = A.C;
-  const bool has_b = lb >= 0;
-  double E[9], Aa[6], Ab[6];
-  load_contact(C, k, E, Aa, Ab);
-  double u[3];
-  local_u3_sv(C, k, sV, u, la, lb, E, Aa, Ab);
-  const double r0 = A.r[3 * (size_t)k], r1 = A.r[3 * (size_t)k + 1], r2 = A.r[3 * (size_t)k + 2];
-  double W[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) W[j] = C.W[6 * (size_t)k + j];
-  const double bt[3] = {u[0] - ((W[0] * r0 + W[1] * r1) + W[2] * r2), u[1] - ((W[1] * r0 + W[3] * r1) + W[4] * r2),
-                        u[2] - ((W[2] * r0 + W[4] * r1) + W[5] * r2)};
-  double rn[3];
-  local_solve_3d(W, bt, C.mu[k], rn);
-  const double d0 = rn[0] - r0, d1 = rn[1] - r1, d2 = rn[2] - r2;
-  double pl[3], pa[3], pb[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    pl[j] = (E[j] * d0 + E[3 + j] * d1) + E[6 + j] * d2;
-    pa[j] = Aa[j] * d1 + Aa[3 + j] * d2;
-    pb[j] = Ab[j] * d1 + Ab[3 + j] * d2;
-  }
-  double Ii[9], wa[3];
-#pragma unroll
-  for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)a + j];
-  matvec3(Ii, pa, wa);
-  const double ma = A.minv[a];
-  {
-    const double4_32a l_a = sV[2 * la], o_a = sV[2 * la + 1];
-    sV[2 * la] = make_double4_32a(l_a.x + ma * pl[0], l_a.y + ma * pl[1], l_a.z + ma * pl[2], 0.0);
-    sV[2 * la + 1] = make_double4_32a(o_a.x + wa[0], o_a.y + wa[1], o_a.z + wa[2], 0.0);
-  }
-  if (has_b) {
-    double wb[3];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) Ii[j] = A.Iinv[9 * (size_t)b + j];
-    matvec3(Ii, pb, wb);
-    const double mb = A.minv[b];
-    const double4_32a l_b = sV[2 * lb], o_b = sV[2 * lb + 1];
-    sV[2 * lb] = make_double4_32a(l_b.x - mb * pl[0], l_b.y - mb * pl[1], l_b.z - mb * pl[2], 0.0);
-    sV[2 * lb + 1] = make_double4_32a(o_b.x - wb[0], o_b.y - wb[1], o_b.z - wb[2], 0.0);
-  }
-  A.r[3 * (size_t)k] = rn[0];
-  A.r[3 * (size_t)k + 1] = rn[1];
-  A.r[3 * (size_t)k + 2] = rn[2];
-}
-
-__global__ void __launch_bounds__(kScene3Block, 2) k_gs3_scenes(Scene3Args Z) {
-  const Gs3Args& A = Z.g;
-  extern __shared__ __align__(32) double4_32a sV3[];
-  __shared__ int s_w;
-  __shared__ int s_off[kMaxColors + 1];
-  __shared__ double s_red[33];
-  if (*((volatile int*)&A.st->status) != 0) return;  // the colouring failed
-  const unsigned eval_every = A.eval_every ? A.eval_every : 1u;
-  double* bufs[2] = {A.r_a, A.r_b};
-  unsigned long long nupd = 0, nevl = 0;
-  for (;;) {
-    if (threadIdx.x == 0) s_w = atomicAdd(Z.next, 1);
-    __syncthreads();
-    const int w = s_w;
-    __syncthreads();
-    if (w >= Z.S) break;
-    const int sc = Z.order[w];
-    const int b0 = Z.sb_off[sc], nbs = Z.sb_off[sc + 1] - b0;
-    const int c0 = Z.sc_off[sc], c1 = Z.sc_off[sc + 1];
-    if (c1 == c0) {
-      if (threadIdx.x == 0) {
-        Z.done[sc] = 1;
-        Z.iters[sc] = 0;
-        Z.best[sc] = INFINITY;
-      }
-      continue;
-    }
-    for (int j = threadIdx.x; j < 2 * nbs; j += blockDim.x) sV3[j] = Z.V[2 * (size_t)b0 + j];
-    for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x)
-      s_off[c] = c < kMaxColors ? Z.key_start[sc * kMaxColors + c] : Z.key_start[(sc + 1) * kMaxColors];
-    __syncthreads();
-    int ncol = kMaxColors;
-    while (ncol > 0 && s_off[ncol] == s_off[ncol - 1]) --ncol;
-    double err_best = INFINITY;
-    int bestbuf = 0;
-    bool converged = false;
-    unsigned it;
-    for (it = 1; it <= A.max_iters; ++it) {
-      for (int col = 0; col < ncol; ++col) {
-        const int e = s_off[col + 1];
-        for (int q = s_off[col] + threadIdx.x; q < e; q += blockDim.x) {
-          const int k = Z.sperm[q];
-          const int a = A.C.ia[k], b = A.C.ib[k];
-          gs_update3_sv(A, k, a, b, a - b0, b >= 0 ? b - b0 : -1, sV3);
-          ++nupd;
-        }
-        __syncthreads();
-      }
-      if (it % eval_every != 0) continue;
-      double emax = 0.0;
-      double* cand = bufs[1 - bestbuf];
-      for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) {
-        const int a = A.C.ia[k], b = A.C.ib[k];
-        double E[9], Aa[6], Ab[6], u[3];
-        load_contact(A.C, k, E, Aa, Ab);
-        local_u3_sv(A.C, k, sV3, u, a - b0, b >= 0 ? b - b0 : -1, E, Aa, Ab);
-        const double rk[3] = {A.r[3 * (size_t)k], A.r[3 * (size_t)k + 1], A.r[3 * (size_t)k + 2]};
-        cand[3 * (size_t)k] = rk[0];
-        cand[3 * (size_t)k + 1] = rk[1];
-        cand[3 * (size_t)k + 2] = rk[2];
-        emax = nanmax(emax, fb_error_3d(rk, u, A.C.mu[k]));
-        ++nevl;
-      }
-      emax = warp_nanmax(emax);
-      if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = emax;
-      __syncthreads();
-      if (threadIdx.x < 32) {
-        double x = threadIdx.x < (blockDim.x + 31) / 32 ? s_red[threadIdx.x] : 0.0;
-        x = warp_nanmax(x);
-        if (threadIdx.x == 0) s_red[32] = x;
-      }
-      __syncthreads();
-      const double err = s_red[32];
-      __syncthreads();
-      if (err < err_best) {
-        err_best = err;
-        bestbuf ^= 1;
-      }
-      if (err < A.tol) {
-        converged = true;
-        break;
-      }
-    }
-    if (!converged) {
-      if (err_best < INFINITY)
-        for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) {
-          A.r[3 * (size_t)k] = bufs[bestbuf][3 * (size_t)k];
-          A.r[3 * (size_t)k + 1] = bufs[bestbuf][3 * (size_t)k + 1];
-          A.r[3 * (size_t)k + 2] = bufs[bestbuf][3 * (size_t)k + 2];
-        }
-      it = A.max_iters;
-    }
-    if (threadIdx.x == 0) {
-      Z.done[sc] = converged ? 1 : 0;
-      Z.iters[sc] = it;
-      Z.best[sc] = err_best;
-      if (!converged) atomicAdd(Z.unconverged, 1ull);
-      atomicMax(&A.st->iterations, it);
-    }
-    __syncthreads();
-  }
-  nupd = warp_sum(nupd);
-  nevl = warp_sum(nevl);
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&Z.work[1], nupd);
-    atomicAdd(&Z.work[2], nevl);
-  }
-}
-
-// (scene, colour) runs of a batch's contacts (scene of a contact = scene of its first body).
-__global__ void k_scene_color_count3(int nc, const int* __restrict__ ia, const int* __restrict__ scene_of,
-                                     const int* __restrict__ color, int* __restrict__ cnt) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nc) return;
-  const int c = color[k];
-  if (c < 0 || c >= kMaxColors) return;  // a failed colouring (its status ends the solve)
-  atomicAdd(&cnt[scene_of[ia[k]] * kMaxColors + c], 1);
-}
-
-__global__ void k_scene_color_scatter3(int nc, const int* __restrict__ ia, const int* __restrict__ scene_of,
-                                       const int* __restrict__ color, const int* __restrict__ start,
-                                       int* __restrict__ fill, int* __restrict__ sperm) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nc) return;
-  const int c = color[k];
-  if (c < 0 || c >= kMaxColors) return;
-  const int key = scene_of[ia[k]] * kMaxColors + c;
-  sperm[start[key] + atomicAdd(&fill[key], 1)] = k;
-}
-
-// The per-scene sphere kernel's dynamic shared memory limit for scenes of up to smax bodies.
-static int scene3_blocks_prepare(int smax) {
-  SG_CUDA_TRY(cudaFuncSetAttribute(k_gs3_scenes, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   std::max(64 * smax, 48 * 1024)));
-  return SG_OK;
-}
-
-// ---------------------------------------------------------------------------
 // Batched sphere scenes: one coloured sweep over the contacts of all scenes (scenes share no
 // body, so the global colouring colours every scene), with each scene's own residual, best
 // iterate, convergence test and iteration count, as if every scene were solved alone
@@ -3439,53 +3195,6 @@ int sphere3d_batch_step(sg_ctx* ctx, sg_step_stats* out) {
     SG_CUDA_TRY(launch_cooperative((const void*)k_gs3_mixed_batch, grid, kGs3mBlock, args, s));
     if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
     ctx->kernel_launches += 2;
-  } else if (ctx->s_smax > 0) {
-    // One block per scene: contacts ordered by (scene, colour), then the persistent per-scene sweeps.
-    const size_t keys = (size_t)S * kMaxColors;
-    if (int r = grow(ctx->s_kcnt, sizeof(int) * (keys + 1))) return r;
-    if (int r = grow(ctx->s_kstart, sizeof(int) * (keys + 1))) return r;
-    if (int r = grow(ctx->s_kfill, sizeof(int) * (keys + 1))) return r;
-    if (int r = grow(ctx->s_sperm, sizeof(int) * (size_t)std::max(nc, 1))) return r;
-    if (int r = grow(ctx->s_next, sizeof(int))) return r;
-    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_kcnt.p, 0, sizeof(int) * (keys + 1), s));
-    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_kfill.p, 0, sizeof(int) * (keys + 1), s));
-    SG_CUDA_TRY(cudaMemsetAsync(ctx->s_next.p, 0, sizeof(int), s));
-    k_scene_color_count3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, scene_of, ctx->color.as<int>(),
-                                                           ctx->s_kcnt.as<int>());
-    SG_CUDA_TRY(cudaGetLastError());
-    if (int r = scan_exclusive(ctx, ctx->s_kcnt.as<int>(), ctx->s_kstart.as<int>(), (int)keys)) return r;
-    k_scene_color_scatter3<<<blocks_for(nc), kBlock, 0, s>>>(nc, ia, scene_of, ctx->color.as<int>(),
-                                                             ctx->s_kstart.as<int>(), ctx->s_kfill.as<int>(),
-                                                             ctx->s_sperm.as<int>());
-    SG_CUDA_TRY(cudaGetLastError());
-    Scene3Args Z;
-    Z.g = B.g;
-    Z.V = V;
-    Z.sb_off = ctx->sb_off.as<int>();
-    Z.sc_off = sc_off;
-    Z.key_start = ctx->s_kstart.as<int>();
-    Z.sperm = ctx->s_sperm.as<int>();
-    Z.order = ctx->s_order.as<int>();
-    Z.next = ctx->s_next.as<int>();
-    Z.S = S;
-    Z.smax = ctx->s_smax;
-    Z.best = B.best;
-    Z.done = B.done;
-    Z.iters = B.iters;
-    Z.unconverged = B.unconverged;
-    Z.work = B.work;
-    const size_t smem = (size_t)64 * (size_t)ctx->s_smax;
-    if (int r = scene3_blocks_prepare(ctx->s_smax)) return r;
-    int bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_gs3_scenes, kScene3Block, smem) != cudaSuccess ||
-        bps < 1)
-      bps = 1;
-    const int grid = std::max(1, std::min(ctx->num_sms * bps, S));
-    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-    k_gs3_scenes<<<grid, kScene3Block, smem, s>>>(Z);
-    SG_CUDA_TRY(cudaGetLastError());
-    if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
-    ctx->kernel_launches += 5;  // count, 3 scan, scatter
   } else {
     void* args[] = {&B};
     const int grid = coop_grid(ctx, k_gs3_batch, (long)ctx->num_sms * kGs3Block, kGs3Block, 1);
