@@ -1014,7 +1014,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=8)
     ap.add_argument("--batch-plain-scenes", type=int, default=16)
     ap.add_argument("--spheres", type=int, default=65536, help="sphere leg (0 = skip)")
-    ap.add_argument("--sphere-preroll", type=int, default=100)
+    ap.add_argument("--sphere-preroll", type=int, default=800,
+                    help="capped pre-roll steps of the sphere leg (the 65,536-sphere pile forms in ~600)")
     ap.add_argument("--sphere-steps", type=int, default=3)
     ap.add_argument("--sphere-batch-scenes", type=int, default=256, help="sphere-batch leg (0 = skip)")
     ap.add_argument("--sphere-batch-preroll", type=int, default=100)

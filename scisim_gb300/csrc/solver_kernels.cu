@@ -353,6 +353,7 @@ struct GsArgs {
   unsigned max_iters;
   unsigned eval_every;
   int iso = 0;  // isotropic blocks take local_solve_2d_iso (the FP32 form's FP64 sweeps)
+  unsigned first_eval = 1;  // k_gs: no residual check before this sweep (the FP32 form's probe: 2)
 };
 
 __device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs(GsArgs A) {
         return;
       }
     }
-    if (it % eval_every == 0) {
+    if (it % eval_every == 0 && it >= A.first_eval) {
       double emax = 0.0;
       for (int k = tid; k < A.nc; k += nthr) {
         const int a = A.ia[k], b = A.ib[k];
@@ -2787,6 +2788,9 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GsArgs GP = GA;
       const bool probe = two_level_applies && sp.max_iters > kFp64Probe;
       if (probe) GP.max_iters = kFp64Probe;
+      // A warm start within fp64_factor tol rarely converges in one sweep, and a residual check
+      // costs about three FP64 sweeps on GB300: the first check follows the second sweep.
+      GP.first_eval = GP.max_iters >= 2 ? 2u : 1u;
       void* pargs[] = {&GP};
       const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);
       stage_mark(ctx, 5);
