@@ -157,6 +157,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->v, ctx->v1);
     ctx->prev_n = 0;
     ctx->prev_rows = false;
+    ctx->prev_color_valid = false;
     st.succeeded = 1;
     if (int r = finish_stage_timing(ctx)) return r;
     if (out) *out = st;
@@ -165,6 +166,9 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   if (int r = ensure_contact_capacity(ctx, nc)) return r;
   if (int r = broadphase_write_pairs(ctx, aabb, nb, true, ctx->ia.as<int>(), ctx->ib.as<int>())) return r;
   if (int r = plane_write(ctx, npairs)) return r;
+  // Colours carried over from the cached step (assemble_contacts writes them beside the warm start).
+  const bool warm_colors = ctx->prev_color_valid && ctx->prev_n > 0 && ctx->n_scenes == 0 && !ctx->rb2d &&
+                           ctx->cfg.cache_mode != SG_CACHE_NONE;
   if (int r = assemble_contacts(ctx, nc)) return r;
   stage_mark(ctx, 3);
   if (int r = grow(ctx->v2, sizeof(double) * 2 * (size_t)nb)) return r;
@@ -183,6 +187,7 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
   P.mu = ctx->mu.as<double>();
   P.r = ctx->r_loc.as<double>();
   P.v2 = ctx->v2.as<double>();
+  P.warm_color = warm_colors ? ctx->init_color.as<int>() : nullptr;
   SolveParams sp{ctx->cfg.tol, ctx->cfg.max_iters, ctx->cfg.eval_every, ctx->cfg.precision, true};
   const int sr = solve_contacts(ctx, P, sp);
   if (sr != SG_OK && sr != SG_NOT_CONVERGED) return sr;
@@ -202,12 +207,17 @@ static int step_once(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->plane_flag, ctx->prev_plane_flag);
     ctx->prev_npairs = npairs;
     ctx->prev_rows = true;
+    // This step's colouring seeds the next one's.
+    if (int r = grow(ctx->prev_color, sizeof(int) * (size_t)nc)) return r;
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->prev_color.p, ctx->color.p, sizeof(int) * (size_t)nc, cudaMemcpyDeviceToDevice, s));
+    ctx->prev_color_valid = true;
     // keep ccap consistent with the smaller of the swapped buffers
     const int64_t kcap = (int64_t)std::min(ctx->key.bytes / sizeof(unsigned long long), ctx->ab.bytes / (2 * sizeof(double)));
     ctx->ccap = std::min<int64_t>(ctx->ccap, kcap);
   } else {
     ctx->prev_n = 0;
     ctx->prev_rows = false;
+    ctx->prev_color_valid = false;
   }
   // Final map with the post-impact velocity (:441).
   if (int r = ball2d_final_map(ctx, ctx->v2.as<double>())) return r;
@@ -289,8 +299,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                  &ctx->r_loc, &ctx->r_cand, &ctx->r_best, &ctx->key, &ctx->ab, &ctx->prev_key, &ctx->prev_ab,
                  &ctx->color, &ctx->perm, &ctx->body_cnt, &ctx->body_off, &ctx->body_fill, &ctx->body_adj,
                  &ctx->v_run, &ctx->stats, &ctx->barrier, &ctx->fs_m, &ctx->fs_minv, &ctx->fs_v0, &ctx->fs_v2,
-                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->pair_slots, &ctx->aabb32, &ctx->prev_pair_off, &ctx->prev_plane_off,
-                 &ctx->prev_plane_flag, &ctx->vdelta, &ctx->rb_I, &ctx->rb_Iinv,
+                 &ctx->fs_I, &ctx->fs_in, &ctx->c6, &ctx->prev_c6, &ctx->pair_slots, &ctx->aabb32, &ctx->aabb32s, &ctx->prev_pair_off, &ctx->prev_plane_off,
+                 &ctx->prev_plane_flag, &ctx->prev_color, &ctx->init_color, &ctx->vdelta, &ctx->rb_I, &ctx->rb_Iinv,
                  &ctx->pos0, &ctx->pos1, &ctx->rb_ct, &ctx->rb_vrun};
   for (Buf* b : bufs) release(*b);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
@@ -374,6 +384,7 @@ int sg_ball2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double* v, 
   if (int e = grow(ctx->plane_t, 16)) return e;
   ctx->prev_n = 0;
   ctx->prev_rows = false;
+  ctx->prev_color_valid = false;
   ctx->last_nc = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -449,6 +460,7 @@ int sg_rigidbody2d_upload(sg_ctx* ctx, int32_t nb, const double* q, const double
   if (int e = grow(ctx->plane_t, 16)) return e;
   ctx->prev_n = 0;
   ctx->prev_rows = false;
+  ctx->prev_color_valid = false;
   ctx->last_nc = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -527,6 +539,7 @@ static int sphere3d_upload_impl(sg_ctx* ctx, int32_t nb, const double* q, const 
   if (int e = sphere3d_update_inertia(ctx, true)) return e;
   ctx->prev_n = 0;
   ctx->prev_rows = false;
+  ctx->prev_color_valid = false;
   ctx->last_nc = 0;
   SG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -1260,10 +1273,14 @@ std::vector<CkptPart> ckpt_parts(sg_ctx* ctx, int dim, int nb, int np, int64_t p
   // The impulse cache: (alpha, beta) per Ball2D contact; the cached normal and force (6) per
   // sphere contact (symplectic-Euler staggering; the geometric sphere map keeps none).
   v.push_back({&ctx->prev_key, (size_t)prev_n * sizeof(unsigned long long)});
-  if (dim == 2)
+  if (dim == 2) {
     v.push_back({&ctx->prev_ab, (size_t)prev_n * 2 * d});
-  else
+    // The cached step's colours: the next step's colouring starts from them, so a resumed run
+    // colours, and therefore sweeps, as the uninterrupted one.
+    v.push_back({&ctx->prev_color, (size_t)prev_n * sizeof(int)});
+  } else {
     v.push_back({&ctx->prev_c6, (size_t)prev_n * 6 * d});
+  }
   return v;
 }
 
@@ -1365,6 +1382,7 @@ int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes) {
   }
   ctx->prev_n = h.prev_n;
   ctx->prev_rows = false;
+  ctx->prev_color_valid = h.dim == 2 && h.prev_n > 0;
   ctx->last_nc = 0;
   ctx->staggering = h.staggering;
   ctx->stabilize = h.stabilize;

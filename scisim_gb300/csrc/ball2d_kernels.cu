@@ -200,12 +200,17 @@ __global__ void k_cell_count(int n, const double4_32a* __restrict__ aabb, const 
   atomicAdd(&cell_count[cell], 1);
 }
 
+// With box32 non-null the FP32 boxes go along into cell order (box32_sorted), so that the pair
+// scans read each cell's boxes as one contiguous run.
 __global__ void k_cell_scatter(int n, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
-                               int* __restrict__ cell_fill, int* __restrict__ sorted) {
+                               int* __restrict__ cell_fill, int* __restrict__ sorted,
+                               const float4* __restrict__ box32 = nullptr, float4* __restrict__ box32_sorted = nullptr) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cell = cell_of[i];
-  sorted[cell_start[cell] + atomicAdd(&cell_fill[cell], 1)] = i;
+  const int pos = cell_start[cell] + atomicAdd(&cell_fill[cell], 1);
+  sorted[pos] = i;
+  if (box32) box32_sorted[pos] = box32[i];
 }
 
 // AABB::overlaps (ball2d/SpatialGridDetector.cpp:15-26): touching boxes overlap.
@@ -253,7 +258,8 @@ __device__ __forceinline__ bool ccd_happens(double c0, double c1, double c2, dou
 
 struct PairScan {
   const double4_32a* aabb;
-  const float4* aabb32;  // the boxes rounded outward to FP32 (prefilter)
+  const float4* aabb32;   // the boxes rounded outward to FP32 (prefilter), by body
+  const float4* aabb32s;  // the same in cell order (position p holds body sorted[p])
   const GridParams* gp;
   const int* cell_start;
   const int* sorted;
@@ -284,10 +290,10 @@ __device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
       const int cell = x + g.dims[0] * y;
       const int e = s.cell_start[cell + 1];
       for (int p = s.cell_start[cell]; p < e; ++p) {
+        const float4 fj = s.aabb32s[p];
+        if (fi.z < fj.x || fi.w < fj.y || fj.z < fi.x || fj.w < fi.y) continue;
         const int j = s.sorted[p];
         if (j <= i) continue;
-        const float4 fj = s.aabb32[j];
-        if (fi.z < fj.x || fi.w < fj.y || fj.z < fi.x || fj.w < fi.y) continue;
         if (!aabb_overlap(bi, s.aabb[j])) continue;
         if (kCcd) {
           double c0, c1, c2;
@@ -306,8 +312,9 @@ constexpr int kPairSlots = 8;
 
 template <bool kCcd>
 __global__ void k_pair_count(int n, PairScan s, int* __restrict__ cnt, int* __restrict__ slots) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = s.sorted[t];  // bodies in cell order: neighbouring threads scan the same cells
   int c = 0;
   int* mine = slots + (size_t)i * kPairSlots;
   visit_pairs<kCcd>(s, i, [&](int j) {
@@ -320,8 +327,9 @@ __global__ void k_pair_count(int n, PairScan s, int* __restrict__ cnt, int* __re
 template <bool kCcd>
 __global__ void k_pair_write(int n, PairScan s, const int* __restrict__ off, const int* __restrict__ slots,
                              int* __restrict__ out_a, int* __restrict__ out_b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = s.sorted[t];
   const int base = off[i];
   const int total = off[i + 1] - base;
   if (total <= kPairSlots) {
@@ -431,6 +439,10 @@ struct AssembleArgs {
   const int* prev_plane_flag = nullptr;
   int prev_npairs = 0;
   int nb = 0;
+  // Colours carried over: init_color[k] = the step before's colour of contact k (prev_color, by
+  // cache index) or -1 for a new contact (null: none).
+  const int* prev_color = nullptr;
+  int* init_color = nullptr;
 };
 
 // Index of key among the cached contacts of the step before, through its rows: a pair (a, b) among
@@ -559,14 +571,16 @@ __device__ __forceinline__ void assemble_one(const AssembleArgs& A, int k, doubl
   const unsigned long long key = contact_key(a, b);
   A.key[k] = key;
   double alpha = 0.0, beta = 0.0;
+  long idx = -1;
   if (A.cache_mode != SG_CACHE_NONE && prev_n > 0) {
-    const long idx = A.prev_pair_off ? find_key_rows(A, a, b, key) : find_key(prev_key, prev_n, key);
+    idx = A.prev_pair_off ? find_key_rows(A, a, b, key) : find_key(prev_key, prev_n, key);
     if (idx >= 0) {
       const double2 ab = prev_ab[idx];
       alpha = ab.x;
       beta = (A.cache_mode == SG_CACHE_NORMAL_AND_FRICTION) ? ab.y : 0.0;
     }
   }
+  if (A.init_color) A.init_color[k] = idx >= 0 ? A.prev_color[idx] : -1;
   const double rwx = alpha * nx + beta * tx;
   const double rwy = alpha * ny + beta * ty;
   A.r[k] = make_double2(nx * rwx + ny * rwy, tx * rwx + ty * rwy);
@@ -918,8 +932,10 @@ int broadphase_build_grid(sg_ctx* ctx, const double* aabb, int n) {
   k_cell_count<<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, bx, gp, ctx->cell_of.as<int>(), ctx->cell_count.as<int>());
   SG_CUDA_TRY(cudaGetLastError());
   if (int r = scan_exclusive(ctx, ctx->cell_count.as<int>(), ctx->cell_start.as<int>(), (int)cap)) return r;
+  if (int r = grow(ctx->aabb32s, sizeof(float4) * (size_t)std::max(n, 1))) return r;
   k_cell_scatter<<<blocks_for(n), kBlock, 0, ctx->stream>>>(n, ctx->cell_of.as<int>(), ctx->cell_start.as<int>(),
-                                                            ctx->cell_fill.as<int>(), ctx->sorted.as<int>());
+                                                            ctx->cell_fill.as<int>(), ctx->sorted.as<int>(),
+                                                            ctx->aabb32.as<float4>(), ctx->aabb32s.as<float4>());
   SG_CUDA_TRY(cudaGetLastError());
   return SG_OK;
 }
@@ -928,6 +944,7 @@ static PairScan make_scan(sg_ctx* ctx, const double* aabb, bool ccd) {
   PairScan s;
   s.aabb = reinterpret_cast<const double4_32a*>(aabb);
   s.aabb32 = ctx->aabb32.as<float4>();
+  s.aabb32s = ctx->aabb32s.as<float4>();
   s.gp = ctx->grid.as<GridParams>();
   s.cell_start = ctx->cell_start.as<int>();
   s.sorted = ctx->sorted.as<int>();
@@ -1007,6 +1024,12 @@ int assemble_contacts(sg_ctx* ctx, int nc) {
   A.prev_key = ctx->prev_key.as<unsigned long long>();
   A.prev_ab = ctx->prev_ab.as<double2>();
   A.prev_n = ctx->prev_n;
+  if (ctx->prev_color_valid && ctx->prev_n > 0 && ctx->n_scenes == 0 && !ctx->rb2d &&
+      ctx->cfg.cache_mode != SG_CACHE_NONE) {
+    if (int r = grow(ctx->init_color, sizeof(int) * (size_t)nc)) return r;
+    A.prev_color = ctx->prev_color.as<int>();
+    A.init_color = ctx->init_color.as<int>();
+  }
   if (ctx->prev_rows && ctx->n_scenes == 0 && !ctx->rb2d) {
     A.prev_pair_off = ctx->prev_pair_off.as<int>();
     A.prev_plane_off = ctx->prev_plane_off.as<int>();

@@ -77,6 +77,9 @@ struct ContactProblem {
   const double* mu = nullptr;    // nc
   double* r = nullptr;           // 2nc in: warm start (local), out: solution
   double* v2 = nullptr;          // 2nb out
+  // Colours carried over from the step before (nc: the contact's colour then, -1 for a new
+  // contact); null: the colouring starts from nothing.
+  const int* warm_color = nullptr;
 };
 
 // Per-scene solver state of a batched solve (device arrays of S entries).
@@ -157,12 +160,17 @@ struct sg_ctx {
   // impulse cache of the previous step (sorted keys and (alpha, beta))
   sg::Buf prev_key, prev_ab;
   sg::Buf pair_slots;  // the pair count's first partners per box (8 each), read by the pair write
-  sg::Buf aabb32;      // the boxes rounded outward to FP32, the pair scans' prefilter
+  sg::Buf aabb32, aabb32s;  // the boxes rounded outward to FP32 (the pair scans' prefilter), by body
+                            // and in cell order
   // The rows of the cached step (single-scene Ball2D): pair offsets per body, plane flags and
   // their scan, and its pair count; prev_rows says they belong to the cache held.
   sg::Buf prev_pair_off, prev_plane_off, prev_plane_flag;
   int prev_npairs = 0;
   bool prev_rows = false;
+  // The cached step's contact colours (prev_n of them) and each contact's colour carried over
+  // (single-scene Ball2D steps with a cache): the colouring starts from them.
+  sg::Buf prev_color, init_color;
+  bool prev_color_valid = false;
   // Sphere scenes under the symplectic-Euler staggering: 6 doubles per contact (cached normal and
   // force), this step's and the step before's.
   sg::Buf c6, prev_c6;
@@ -300,7 +308,10 @@ int ensure_contact_capacity(sg_ctx* ctx, int64_t nc);
 // solve counters cleared, and the contact colouring with its processing permutation
 // (ctx->perm, colour offsets in ctx->stats).  Shared by the 2D and 3D solvers.
 // nc is the host-side count (or, with nc_dev, the capacity the launches are sized to).
-int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const int* nc_dev = nullptr);
+// With warm_color, the colouring starts from those colours (a valid colouring of the contacts that
+// carry one) and colours the rest.
+int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const int* nc_dev = nullptr,
+                          const int* warm_color = nullptr);
 
 // Cooperative launch through cudaLaunchKernelEx (capturable in a CUDA graph).
 inline cudaError_t launch_cooperative(const void* kernel, int grid, int block, void** args, cudaStream_t s) {

@@ -489,6 +489,7 @@ int rb2d_step(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->v, ctx->v1);
     ctx->prev_n = 0;
     ctx->prev_rows = false;
+    ctx->prev_color_valid = false;
     st.succeeded = 1;
     if (out) *out = st;
     return SG_OK;
@@ -603,12 +604,14 @@ int rb2d_step(sg_ctx* ctx, sg_step_stats* out) {
     std::swap(ctx->ab, ctx->prev_ab);
     ctx->prev_n = nc;
     ctx->prev_rows = false;
+    ctx->prev_color_valid = false;
     const int64_t kcap =
         (int64_t)std::min(ctx->key.bytes / sizeof(unsigned long long), ctx->ab.bytes / (2 * sizeof(double)));
     ctx->ccap = std::min<int64_t>(ctx->ccap, kcap);
   } else {
     ctx->prev_n = 0;
     ctx->prev_rows = false;
+    ctx->prev_color_valid = false;
   }
   // Final map: from q0 with the post-impact velocity (:441), or the stabilized map's update.
   if (stab)

@@ -176,6 +176,11 @@ struct ColorArgs {
   GridBarrier* gb;
   unsigned long long spin;
   int max_rounds;
+  // Warm start: contacts with a colour >= 0 on entry keep it (colours of an earlier step, valid
+  // among themselves) and the Jones-Plassmann rounds begin at 1, so those count as coloured before
+  // them; then ig_passes recolouring passes.
+  int first_round = 0;
+  int ig_passes = 3;
 };
 
 __global__ void __launch_bounds__(kColorBlock, 1) k_color_jp(ColorArgs A) {
@@ -183,7 +188,7 @@ __global__ void __launch_bounds__(kColorBlock, 1) k_color_jp(ColorArgs A) {
   const int nthr = gridDim.x * blockDim.x;
   if (A.nc_dev) A.nc = *A.nc_dev;
   volatile int* vcolor = A.color;
-  for (int round = 0;; ++round) {
+  for (int round = A.first_round;; ++round) {
     if (round >= A.max_rounds) {
       if (tid == 0) atomicExch(&A.st->status, (int)SG_CAPACITY);
       return;
@@ -253,7 +258,7 @@ __global__ void __launch_bounds__(kColorBlock, 1) k_color_jp(ColorArgs A) {
     }
     int cmax = *((volatile int*)&A.st->n_colors);
     volatile int* vnew = A.perm;
-    for (int pass = 0; pass < 3; ++pass) {
+    for (int pass = 0; pass < A.ig_passes; ++pass) {
       for (int k = tid; k < A.nc; k += nthr) vnew[k] = -1;
       if (!grid_sync(A.gb, A.spin)) {
         if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
@@ -2644,7 +2649,8 @@ int ensure_solver_capacity(sg_ctx* ctx, int nb, int nc) {
   return SG_OK;
 }
 
-int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const int* nc_dev) {
+int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int* ib, const int* nc_dev,
+                          const int* warm_color) {
   cudaStream_t s = ctx->stream;
   int* cnt = ctx->body_cnt.as<int>();
   int* off = ctx->body_off.as<int>();
@@ -2665,10 +2671,19 @@ int prepare_contact_graph(sg_ctx* ctx, int nb, int nc, const int* ia, const int*
   k_body_fill<<<blocks_for(nc), kBlock, 0, s>>>(nc, nc_dev, ia, ib, off, fill, adj);
   k_body_sort<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj);
   SG_CUDA_TRY(cudaGetLastError());
-  SG_CUDA_TRY(cudaMemsetAsync(ctx->color.p, 0xff, sizeof(int) * (size_t)nc, s));
+  if (warm_color)
+    SG_CUDA_TRY(cudaMemcpyAsync(ctx->color.p, warm_color, sizeof(int) * (size_t)nc, cudaMemcpyDeviceToDevice, s));
+  else
+    SG_CUDA_TRY(cudaMemsetAsync(ctx->color.p, 0xff, sizeof(int) * (size_t)nc, s));
   SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
   ColorArgs CA{nc, nc_dev, ia, ib, off, adj, ctx->color.as<int>(), ctx->perm.as<int>(), st, gb, ctx->spin_limit,
                4096};
+  if (warm_color) {
+    // The carried colours need no Jones-Plassmann round; one recolouring pass keeps the count
+    // from creeping up as new contacts take the first free colour.
+    CA.first_round = 1;
+    CA.ig_passes = 1;
+  }
   void* args[] = {&CA};
   // One 1,024-thread block per SM: the colouring is a chain of grid barriers (a Jones-Plassmann
   // round each, a colour class each in the recolouring passes), and a barrier's cost grows with the
@@ -2692,7 +2707,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
   double2* r2 = reinterpret_cast<double2*>(P.r);
 
   // Adjacency and colouring first: the velocity initialisation reads the adjacency.
-  if (int r = prepare_contact_graph(ctx, nb, nc, P.ia, P.ib)) return r;
+  if (int r = prepare_contact_graph(ctx, nb, nc, P.ia, P.ib, nullptr, P.warm_color)) return r;
   stage_mark(ctx, 4);
   double2* vrun = ctx->v_run.as<double2>();
   if (sp.learned && nc > 0 && (ctx->mlp_on || ctx->mlp_record)) {

@@ -2866,6 +2866,7 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
       SG_CUDA_TRY(cudaGetLastError());
       ctx->prev_n = 0;
       ctx->prev_rows = false;
+      ctx->prev_color_valid = false;
       ctx->kernel_launches += 1;
     }
     std::swap(ctx->q, ctx->q1);
@@ -2948,10 +2949,12 @@ int sphere3d_step(sg_ctx* ctx, sg_step_stats* out) {
       std::swap(ctx->c6, ctx->prev_c6);
       ctx->prev_n = nc;
       ctx->prev_rows = false;
+      ctx->prev_color_valid = false;
       ctx->kernel_launches += 1;
     } else {
       ctx->prev_n = 0;
       ctx->prev_rows = false;
+      ctx->prev_color_valid = false;
     }
     k_se3_final<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cfg.dt, ctx->q.as<double>(), ctx->v2.as<double>(),
                                                   ctx->vdelta.as<double>(), ctx->q1.as<double>(), ctx->v1.as<double>());
