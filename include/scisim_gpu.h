@@ -377,11 +377,11 @@ typedef struct {
   double patch_interior_max_ms; /* the slowest block's patch-interior time, summed over solves */
   int64_t patch_slowest_block;  /* that block (= its patch) in the last two-level solve */
   uint64_t patch_contacts_staged; /* per-patch contact capacity staged in shared memory, summed */
-  uint64_t fp64_start_solves;  /* FP32-form solves whose start was already within 10 tol of the
-                                  tolerance and were swept in FP64 from the first sweep */
+  uint64_t fp64_start_solves;  /* FP32-form solves swept in FP64 throughout: converged in the FP64
+                                  probe, or within fp64_factor tol after it */
   /* Single-scene Ball2D steps: CUDA-event time of each stage, summed: [0] predictor and grid,
    * [1] pair counting (grid scan, CCD) and plane flags, [2] contact writes and assembly,
-   * [3] adjacency and colouring, [4] start check, two-level partition and FP32 packing, [5] the
+   * [3] adjacency and colouring, [4] FP64 probe, two-level partition and FP32 packing, [5] the
    * Gauss-Seidel kernel, [6] final velocity, [7] impulse extraction, cache and final map. */
   double stage_ms[8];
 } sg_profile;
@@ -436,10 +436,11 @@ typedef struct {
   int32_t two_level;
   int32_t check_interval;
   int32_t two_level_min_contacts;
-  int32_t fp64_factor;  /* FP32 form: FP64 sweeps from the first sweep when the start's FP64 residual is
-                           below fp64_factor tol (a few one-level sweeps first, then FP64 sweeps on
-                           the two-level partition), and from the first FP64 check at or below it
-                           (default 100; 0 keeps FP32 sweeps until their rounding floor) */
+  int32_t fp64_factor;  /* FP32 form: a probe of four one-level FP64 sweeps first; a solve it leaves
+                           within fp64_factor tol goes on in FP64 (on the two-level partition for
+                           large scenes), any other in FP32 sweeps until the first FP64 check at or
+                           below fp64_factor tol (default 100; 0: no probe, FP32 sweeps until their
+                           rounding floor) */
 } sg_tuning;
 
 SG_API int sg_get_tuning(sg_ctx* ctx, sg_tuning* tuning);

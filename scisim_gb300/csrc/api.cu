@@ -275,7 +275,7 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->pk_w, &ctx->pk_r, &ctx->v32, &ctx->minv32, &ctx->pk3, &ctx->Iinv32, &ctx->pt_setup,
                   &ctx->pt_patch, &ctx->pt_lidx, &ctx->pt_body, &ctx->pt_cnt, &ctx->pt_start, &ctx->pt_fill,
                   &ctx->pt_key, &ctx->pt_kcnt, &ctx->pt_kstart, &ctx->pt_kfill, &ctx->pt_order, &ctx->pt_max,
-                  &ctx->pt_bcolor, &ctx->pt_rem, &ctx->start_slot, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
+                  &ctx->pt_bcolor, &ctx->pt_rem, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
                   &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill,
                   &ctx->pt_cflag, &ctx->pt_cpos, &ctx->pt_cbody, &ctx->pt_hist, &ctx->pt_pref,
                   &ctx->pt_cuts, &ctx->pt_maps};

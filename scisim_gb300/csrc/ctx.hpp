@@ -203,8 +203,7 @@ struct sg_ctx {
   // from the first FP64 check at or below it.
   int fp64_factor = 100;
   uint64_t patched_solves = 0;
-  uint64_t fp64_start_solves = 0;  // FP32-form solves swept in FP64 from the start (start near tol)
-  sg::Buf start_slot;              // the start's FP64 residual (ordered encoding)
+  uint64_t fp64_start_solves = 0;  // FP32-form solves swept in FP64 throughout (probe near tol)
   bool last_patched = false;  // the last FP32 solve ran the two-level sweeps
   int last_patch_P = 0, last_patch_Pb = 0;
   uint64_t patch_phase_ns[3] = {0, 0, 0};

@@ -34,18 +34,9 @@ constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (few
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
 constexpr int kPatchBlock = 384;  // two-level kernel
 constexpr int kColorBlock = 1024;  // colouring kernel
-// FP32 form: a start whose FP64 residual is below this many tolerances is swept in FP64.
-// FP64 sweeps a start near tol first runs one-level before the two-level partition is set up.
+// FP32 form: the one-level FP64 sweeps of the probe that starts every solve.
 constexpr unsigned kFp64Probe = 4;
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
-// Host decoding of the ordered encoding of a non-negative double (f64_to_ordered).
-inline double host_ordered_to_f64(unsigned long long u) {
-  u = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
-  double d;
-  std::memcpy(&d, &u, sizeof(d));
-  return d;
-}
-
 
 // u = H v + c for contact k (body b < 0: static).
 __device__ __forceinline__ void local_velocity(const double2 nk, const double2 ck, const double2 va, bool has_b,
@@ -2742,34 +2733,15 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
                                                P.minv, vrun);
   SG_CUDA_TRY(cudaGetLastError());
 
-  // FP32 form: the FP64 residual of the start decides the arithmetic.  A start already within
-  // fp64_factor tol of the tolerance (a warm start on a settled scene) is swept in FP64 from the
-  // first sweep: FP32 sweeps would only add their rounding, whose floor lies near tol where the
-  // impulses of deep stacks reach hundreds of times the velocity scale.  Such a solve first runs a
-  // few one-level FP64 sweeps (it usually converges within them, for less than the two-level
-  // partition's setup costs) and, if it has not converged, goes on with FP64 sweeps on the
-  // two-level partition.
+  // FP32 form: a probe of up to kFp64Probe one-level FP64 sweeps first (isotropic closed form; a
+  // warm start on a settled scene converges within them, for less than the two-level partition's
+  // setup costs).  If it has not converged, its residual decides the arithmetic: within
+  // fp64_factor tol of the tolerance the solve goes on in FP64 (on the two-level partition for a
+  // large scene), because FP32 sweeps would only add their rounding, whose floor lies near tol
+  // where the impulses of deep stacks reach hundreds of times the velocity scale; further away,
+  // FP32 sweeps with FP64 checks and refinement.
   const bool fp32_form = sp.precision == SG_PRECISION_FP32_REFINE;
   bool fp64_start = false;
-  if (fp32_form && nc > 0) {
-    if (!ctx->start_slot.p) {
-      if (int r = grow(ctx->start_slot, sizeof(unsigned long long))) return r;
-    }
-    unsigned long long* slot = ctx->start_slot.as<unsigned long long>();
-    SG_CUDA_TRY(cudaMemsetAsync(slot, 0, sizeof(unsigned long long), s));
-    const int eb = std::max(1, std::min(blocks_for(nc), ctx->num_sms * 8));
-    k_start_err<<<eb, kBlock, 0, s>>>(nc, P.ia, P.ib, n2, reinterpret_cast<const double2*>(P.c), P.mu, r2, vrun, slot);
-    SG_CUDA_TRY(cudaGetLastError());
-    unsigned long long h = 0;
-    SG_CUDA_TRY(cudaMemcpyAsync(&h, slot, sizeof(h), cudaMemcpyDeviceToHost, s));
-    SG_CUDA_TRY(cudaStreamSynchronize(s));
-    ctx->kernel_launches += 1;
-    const double err0 = host_ordered_to_f64(h);
-    if (err0 < (double)ctx->fp64_factor * sp.tol) {
-      fp64_start = true;
-      ctx->fp64_start_solves += 1;
-    }
-  }
   bool fp32_sweeps = fp32_form;
   unsigned probe_iters = 0, probe_evals = 0;
 
@@ -2797,14 +2769,12 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
     GA.max_iters = sp.max_iters;
     GA.eval_every = sp.eval_every;
     GA.iso = fp32_form ? 1 : 0;
-    const bool two_level_applies = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 &&
-                                   nc >= ctx->two_level_min_contacts;
-    if (fp64_start) {
+    if (fp32_form && ctx->fp64_factor > 0) {  // fp64_factor 0: FP32 sweeps from the start
       GsArgs GP = GA;
-      const bool probe = two_level_applies && sp.max_iters > kFp64Probe;
+      const bool probe = sp.max_iters > kFp64Probe;
       if (probe) GP.max_iters = kFp64Probe;
-      // A warm start within fp64_factor tol rarely converges in one sweep, and a residual check
-      // costs about three FP64 sweeps on GB300: the first check follows the second sweep.
+      // A warm start rarely converges in one sweep, and a residual check costs about three FP64
+      // sweeps on GB300: the first check follows the second sweep.
       GP.first_eval = GP.max_iters >= 2 ? 2u : 1u;
       void* pargs[] = {&GP};
       const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);
@@ -2819,9 +2789,12 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         SolveStats hp{};
         SG_CUDA_TRY(cudaMemcpyAsync(&hp, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
         SG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (hp.converged) ctx->fp64_start_solves += 1;
         if (!hp.converged && hp.status == 0) {
-          // Not converged in the probe: FP64 sweeps on the two-level partition from its best
-          // iterate, within the remaining sweeps; the residual slots start afresh.
+          // Not converged in the probe: on from its best iterate, within the remaining sweeps, in
+          // FP64 or in the FP32 form as its residual says; the residual slots start afresh.
+          fp64_start = hp.error < (double)ctx->fp64_factor * sp.tol;
+          if (fp64_start) ctx->fp64_start_solves += 1;
           if (ctx->profile) {
             float ms = 0.f;
             SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
@@ -3035,7 +3008,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       GB.nb = nb;
       GB.eval32 = (unsigned)ctx->check_interval;
       GB.fp64_below = (double)ctx->fp64_factor * sp.tol;
-      GB.fp64_start = probe_iters > 0 ? 1 : 0;
+      GB.fp64_start = fp64_start ? 1 : 0;
       if (patched) {
         // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
         // contacts as fit (the patch's first), 32 B each.
