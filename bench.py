@@ -367,15 +367,22 @@ def headline_roofline(prof, total_ms, args):
     bytes_per_launch = gs_bytes(prof) / gl
     gs_ms_per_launch = prof["gs_ms"] / gl
     achieved = bytes_per_launch / (gs_ms_per_launch / 1e3) / 1e9 if gs_ms_per_launch > 0 else 0.0
-    two_level = prof.get("two_level_solves", 0) >= prof["gs_launches"] > 0
-    if two_level:
-        kname = "k_gs_patch (two-level FP32 sweeps: patches on shared memory, boundary contacts over the grid)"
-    elif prof.get("fp64_start_solves", 0) >= prof["gs_launches"] > 0 or args.precision == 0:
+    n_two = prof.get("two_level_solves", 0)
+    n_f64 = prof.get("fp64_start_solves", 0)
+    two_level = n_two >= prof["gs_launches"] > 0 and n_f64 == 0
+    if args.precision == 0:
         kname = "k_gs (cooperative coloured block Gauss-Seidel, FP64)"
+    elif two_level:
+        kname = "k_gs_patch (two-level FP32 sweeps: patches on shared memory, boundary contacts over the grid)"
+    elif n_f64 > 0 and n_two > 0:
+        kname = ("k_gs (the FP64 probe, one-level) and k_gs_patch (FP64 sweeps on the two-level partition for "
+                 "the %d of %d solves the probe left unconverged), together" % (n_two, prof["gs_launches"]))
+    elif n_f64 >= prof["gs_launches"] > 0:
+        kname = "k_gs (the FP64 probe, one-level: every solve converged in it)"
     else:
         kname = "k_gs_mixed (cooperative FP32 sweeps, FP64 checks and refinement)"
     traffic = None
-    tp = os.path.join(HERE, "profiles", "k_gs_patch_traffic.txt" if two_level else "k_gs_mixed_traffic.txt")
+    tp = os.path.join(HERE, "profiles", "k_gs_patch_traffic.txt")
     if os.path.exists(tp) and two_level:
         for line in open(tp):
             if line.startswith("dram_bytes_per_algorithmic_byte"):

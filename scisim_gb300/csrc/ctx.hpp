@@ -134,6 +134,7 @@ struct sg_ctx {
   unsigned long long spin_limit = 0;
   // Kernel attributes are per device: set once per context (each context has one device).
   int patch_smem_budget = -1;   // k_gs_patch's dynamic shared memory limit, once opted in
+  bool patch64_ready = false;   // k_gs_patch64's shared-memory limit set
   bool mlp_smem_set = false;    // k_mlp_fwdbwd's dynamic shared memory limit set
 
   // Scene: dim 2 = Ball2D (q, v: 2 per body), dim 3 = RigidBody3D spheres

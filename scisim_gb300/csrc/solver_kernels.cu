@@ -2009,6 +2009,235 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 sweeps on the two-level partition, for solves that stay in FP64 (the FP32 form's FP64
+// probe left them within fp64_factor tol): k_gs_patch's FP64 phase in a kernel of its own, so
+// that each thread can hold its next contact's data in registers.  A patch or tile colour-round
+// costs one L2 round trip for the contact's normal, forcing, Delassus block, mu and impulse when
+// they are loaded after the barrier; here each thread loads its first contact of the next colour
+// before the barrier that ends the current one (contact data do not change during a solve, and a
+// contact's impulse is written only by the thread that sweeps it), so that after the barrier only
+// the shared-memory velocities remain to be read.  Same arithmetic and order as the FP64 phase of
+// k_gs_patch (gs_update64_local), so the same bits.
+struct C64 {
+  int k, la, lb;
+  double2 n, c, r;
+  double w00, w01, w11, mu;
+};
+
+__device__ __forceinline__ void load64(const GsArgs& A, const Gs32Args& B, const PatchArgs& Q, int q, C64& x) {
+  const int2 ab = B.ab[q];
+  x.k = Q.order[q];
+  x.la = ab.x;
+  x.lb = ab.y;
+  x.n = A.n[x.k];
+  x.c = A.c[x.k];
+  x.w00 = A.W[3 * x.k];
+  x.w01 = A.W[3 * x.k + 1];
+  x.w11 = A.W[3 * x.k + 2];
+  x.mu = A.mu[x.k];
+  x.r = __ldcg(&A.r[x.k]);
+}
+
+__device__ __forceinline__ void update64(const GsArgs& A, const C64& x, double2* sv, const double* sm) {
+  const double2 va = sv[x.la];
+  const bool has_b = x.lb >= 0;
+  const double2 vb = has_b ? sv[x.lb] : make_double2(0.0, 0.0);
+  double u0, u1;
+  local_velocity(x.n, x.c, va, has_b, vb, u0, u1);
+  const double r0 = x.r.x, r1 = x.r.y;
+  const double bt0 = u0 - (x.w00 * r0 + x.w01 * r1);
+  const double bt1 = u1 - (x.w01 * r0 + x.w11 * r1);
+  double rn0, rn1;
+  if (x.w01 == 0.0 && x.w00 == x.w11)
+    local_solve_2d_iso(x.w00, bt0, bt1, x.mu, rn0, rn1);
+  else
+    local_solve_2d(x.w00, x.w01, x.w11, bt0, bt1, x.mu, rn0, rn1);
+  const double d0 = rn0 - r0, d1 = rn1 - r1;
+  const double nx = x.n.x, ny = x.n.y, tx = -ny, ty = nx;
+  const double px = nx * d0 + tx * d1;
+  const double py = ny * d0 + ty * d1;
+  const double ma = sm[x.la];
+  sv[x.la] = make_double2(va.x + ma * px, va.y + ma * py);
+  if (has_b) {
+    const double mb = sm[x.lb];
+    sv[x.lb] = make_double2(vb.x - mb * px, vb.y - mb * py);
+  }
+  A.r[x.k] = make_double2(rn0, rn1);
+}
+
+// One group's colours on shared-memory velocities: off[0..ncol] are its (group, colour) runs.
+__device__ __forceinline__ void sweep_group64(const GsArgs& A, const Gs32Args& B, const PatchArgs& Q,
+                                              const int* off, int ncol, double2* sv, const double* sm) {
+  C64 nxt;
+  bool have = false;
+  if (ncol > 0 && off[0] + (int)threadIdx.x < off[1]) {
+    load64(A, B, Q, off[0] + threadIdx.x, nxt);
+    have = true;
+  }
+  for (int col = 0; col < ncol; ++col) {
+    const int e = off[col + 1];
+    int q = off[col] + threadIdx.x;
+    if (have) {
+      const C64 cur = nxt;
+      // The next colour's first contact of this thread, loaded before this colour's barrier.
+      const int qn = (col + 1 < ncol) ? off[col + 1] + threadIdx.x : e;
+      have = col + 1 < ncol && qn < off[col + 2];
+      update64(A, cur, sv, sm);
+      q += blockDim.x;
+      for (; q < e; q += blockDim.x) {
+        C64 x;
+        load64(A, B, Q, q, x);
+        update64(A, x, sv, sm);
+      }
+      if (have) load64(A, B, Q, qn, nxt);
+    } else {
+      const int qn = (col + 1 < ncol) ? off[col + 1] + threadIdx.x : e;
+      have = col + 1 < ncol && qn < off[col + 2];
+      if (have) load64(A, B, Q, qn, nxt);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Args B, PatchArgs Q) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  extern __shared__ __align__(16) double2 sv64[];
+  double* sm64 = reinterpret_cast<double*>(sv64 + Q.cap);
+  double2* svq64 = reinterpret_cast<double2*>(sm64 + Q.cap);
+  double* smq64 = reinterpret_cast<double*>(svq64 + Q.capq);
+  __shared__ int s_goff[kMaxColors + 1];
+  __shared__ int s_hoff[kMaxColors + 1];
+  __shared__ int s_boff[kMaxColors + 1];
+  const int P = Q.ps->P, Pb = Q.ps->Pb;
+  const bool has_p = blockIdx.x < P, has_q = blockIdx.x < Pb;
+  const int pb0 = has_p ? Q.pstart[blockIdx.x] : 0;
+  const int pb1 = has_p ? Q.pstart[blockIdx.x + 1] : 0;
+  const int pbe = pb0 + (has_p ? Q.pband[blockIdx.x] : 0);  // band bodies: [pb0, pbe)
+  const int qb0 = has_q ? Q.qstart[blockIdx.x] : 0;
+  const int qb1 = has_q ? Q.qstart[blockIdx.x + 1] : 0;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) {
+    s_goff[c] = has_p ? Q.goff[blockIdx.x * kMaxColors + c] : 0;
+    s_hoff[c] = has_q ? Q.goff[(P + blockIdx.x) * kMaxColors + c] : 0;
+    s_boff[c] = Q.goff[(P + Pb) * kMaxColors + c];
+  }
+  for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) {
+    sm64[j - pb0] = A.minv[Q.pbody[j]];
+    sv64[j - pb0] = __ldcg(&A.v[Q.pbody[j]]);
+  }
+  for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) smq64[j - qb0] = A.minv[Q.qbody[j]];
+  __syncthreads();
+  const int ncol_p = group_colors(s_goff), ncol_q = group_colors(s_hoff), ncol_r = group_colors(s_boff);
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  double2* best = A.r_a;
+  double2* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false;
+  unsigned it = 0, n_eval = 0, s64 = 0;
+  // Checks as in k_gs_patch's FP64 phase: where the residual's rate predicts tol, at most
+  // 16 eval64 apart, the gap doubling where the residual did not decrease.
+  unsigned next64 = eval64, interval64 = eval64, prev64_it = 0;
+  double prev64_err = INFINITY;
+  for (it = 1; it <= A.max_iters; ++it) {
+    const bool do_eval = it >= next64 || it == A.max_iters;
+    // The patch's interior (band bodies reloaded: tiles and the remainder touched them).
+    if (it > 1)
+      for (int j = pb0 + threadIdx.x; j < pbe; j += blockDim.x) sv64[j - pb0] = __ldcg(&A.v[Q.pbody[j]]);
+    __syncthreads();
+    sweep_group64(A, B, Q, s_goff, ncol_p, sv64, sm64);
+    const int wend = do_eval ? pb1 : pbe;
+    for (int j = pb0 + threadIdx.x; j < wend; j += blockDim.x) A.v[Q.pbody[j]] = sv64[j - pb0];
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    // The shifted tile's contacts between patches.
+    if (qb1 > qb0) {
+      for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) svq64[j - qb0] = __ldcg(&A.v[Q.qbody[j]]);
+      __syncthreads();
+      sweep_group64(A, B, Q, s_hoff, ncol_q, svq64, smq64);
+      for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) A.v[Q.qbody[j]] = svq64[j - qb0];
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    // The remainder, by block 0 on global velocities.
+    if (blockIdx.x == 0 && s_boff[ncol_r] > s_boff[0]) {
+      for (int col = 0; col < ncol_r; ++col) {
+        for (int q = s_boff[col] + threadIdx.x; q < s_boff[col + 1]; q += blockDim.x) gs_update(A, Q.order[q]);
+        __syncthreads();
+      }
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    ++s64;
+    if (!do_eval) continue;
+    double emax = 0.0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int a = A.ia[k], b = A.ib[k];
+      const bool has_b = b >= 0;
+      const double2 va = __ldcg(&A.v[a]);
+      const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+      double u0, u1;
+      local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+      const double2 rk = __ldcg(&A.r[k]);
+      cand[k] = rk;
+      emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+    }
+    emax = block_nanmax(emax);
+    const int slot = n_eval % 3;
+    if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+    if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    ++n_eval;
+    if (err < err_best) {
+      err_best = err;
+      double2* t = best;
+      best = cand;
+      cand = t;
+    }
+    if (err < A.tol) {
+      converged = true;
+      break;
+    }
+    if (err < prev64_err && prev64_err < INFINITY && err > 0.0) {
+      const double per_sweep = (log(err) - log(prev64_err)) / (double)(it - prev64_it);
+      const double need = (log(A.tol) - log(err)) / per_sweep;
+      interval64 = need >= (double)(16u * eval64) ? 16u * eval64 : max(eval64, (unsigned)need);
+    } else {
+      interval64 = min(2u * interval64, 16u * eval64);
+    }
+    prev64_err = err;
+    prev64_it = it;
+    next64 = it + interval64;
+  }
+  if (it > A.max_iters) it = A.max_iters;
+  if (!converged && err_best < INFINITY)
+    for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps32 = 0;
+    A.st->sweeps64 = s64;
+    A.st->evals = n_eval;
+    A.st->lifts = 0;
+    A.st->boundary_contacts = Q.goff[(P + Pb + 1) * kMaxColors] - Q.goff[P * kMaxColors];
+    int nbc = 0;
+    for (int c = 0; c < ncol_r; ++c) nbc += s_boff[c + 1] > s_boff[c];
+    A.st->boundary_colors = nbc;
+  }
+}
+
 // FP64 Coulomb residual of a start impulse r at running velocities v (one residual
 // evaluation of k_gs), maximum into *slot (ordered encoding).
 __global__ void k_start_err(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
@@ -3048,17 +3277,23 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
         stage_mark(ctx, 5);
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+        // A solve that stays in FP64 takes the FP64 kernel (its velocities fit shared memory).
+        const bool only64 = fp64_start && GB.fp64_local;
+        if (only64 && !ctx->patch64_ready) {
+          SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch64, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_budget));
+          ctx->patch64_ready = true;
+        }
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(maxP);
         lc.blockDim = dim3(kPatchBlock);
-        lc.dynamicSmemBytes = smem;
+        lc.dynamicSmemBytes = only64 ? smem64 : smem;
         lc.stream = s;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeCooperative;
         at[0].val.cooperative = 1;
         lc.attrs = at;
         lc.numAttrs = 1;
-        SG_CUDA_TRY(cudaLaunchKernelExC(&lc, (const void*)k_gs_patch, args));
+        SG_CUDA_TRY(cudaLaunchKernelExC(&lc, only64 ? (const void*)k_gs_patch64 : (const void*)k_gs_patch, args));
         if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
         stage_mark(ctx, 6);
         ctx->patched_solves += 1;
