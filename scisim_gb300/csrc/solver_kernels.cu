@@ -2017,8 +2017,9 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch(GsArgs A, Gs32Args 
 // they are loaded after the barrier; here each thread loads its first contact of the next colour
 // before the barrier that ends the current one (contact data do not change during a solve, and a
 // contact's impulse is written only by the thread that sweeps it), so that after the barrier only
-// the shared-memory velocities remain to be read.  Same arithmetic and order as the FP64 phase of
-// k_gs_patch (gs_update64_local), so the same bits.
+// the shared-memory velocities remain to be read.  The update of an isotropic disc block spends
+// about half the FP64 operations of gs_update64_local (fused multiply-adds, the increment in
+// FP32); checks and results stay FP64.
 struct C64 {
   int k, la, lb;
   double2 n, c, r;
@@ -2043,25 +2044,38 @@ __device__ __forceinline__ void update64(const GsArgs& A, const C64& x, double2*
   const double2 va = sv[x.la];
   const bool has_b = x.lb >= 0;
   const double2 vb = has_b ? sv[x.lb] : make_double2(0.0, 0.0);
-  double u0, u1;
-  local_velocity(x.n, x.c, va, has_b, vb, u0, u1);
-  const double r0 = x.r.x, r1 = x.r.y;
-  const double bt0 = u0 - (x.w00 * r0 + x.w01 * r1);
-  const double bt1 = u1 - (x.w01 * r0 + x.w11 * r1);
   double rn0, rn1;
-  if (x.w01 == 0.0 && x.w00 == x.w11)
-    local_solve_2d_iso(x.w00, bt0, bt1, x.mu, rn0, rn1);
-  else
+  const double r0 = x.r.x, r1 = x.r.y;
+  const double nx = x.n.x, ny = x.n.y;
+  if (x.w01 == 0.0 && x.w00 == x.w11) {
+    // Isotropic block: r_new = proj_cone(r - u / w).  GB300's FP64 pipe bounds these sweeps, so
+    // u is formed with fused multiply-adds and the increment u / w in FP32 (near the solution u is
+    // residual-sized, and its relative rounding, 6e-8, is far below what the FP64 check resolves);
+    // the impulse and the velocities stay FP64.
+    const double dvx = va.x - vb.x, dvy = va.y - vb.y;
+    const double u0 = fma(nx, dvx, fma(ny, dvy, x.c.x));
+    const double u1 = fma(-ny, dvx, fma(nx, dvy, x.c.y));
+    const float iw = 1.0f / (float)x.w00;
+    const double rn = r0 - (double)((float)u0 * iw);
+    rn0 = rn > 0.0 ? rn : 0.0;
+    const double rt = r1 - (double)((float)u1 * iw);
+    const double lim = x.mu * rn0;
+    rn1 = fabs(rt) <= lim ? rt : copysign(lim, rt);
+  } else {
+    double u0, u1;
+    local_velocity(x.n, x.c, va, has_b, vb, u0, u1);
+    const double bt0 = u0 - (x.w00 * r0 + x.w01 * r1);
+    const double bt1 = u1 - (x.w01 * r0 + x.w11 * r1);
     local_solve_2d(x.w00, x.w01, x.w11, bt0, bt1, x.mu, rn0, rn1);
+  }
   const double d0 = rn0 - r0, d1 = rn1 - r1;
-  const double nx = x.n.x, ny = x.n.y, tx = -ny, ty = nx;
-  const double px = nx * d0 + tx * d1;
-  const double py = ny * d0 + ty * d1;
+  const double px = fma(nx, d0, -ny * d1);
+  const double py = fma(ny, d0, nx * d1);
   const double ma = sm[x.la];
-  sv[x.la] = make_double2(va.x + ma * px, va.y + ma * py);
+  sv[x.la] = make_double2(fma(ma, px, va.x), fma(ma, py, va.y));
   if (has_b) {
     const double mb = sm[x.lb];
-    sv[x.lb] = make_double2(vb.x - mb * px, vb.y - mb * py);
+    sv[x.lb] = make_double2(fma(-mb, px, vb.x), fma(-mb, py, vb.y));
   }
   A.r[x.k] = make_double2(rn0, rn1);
 }
@@ -2100,7 +2114,11 @@ __device__ __forceinline__ void sweep_group64(const GsArgs& A, const Gs32Args& B
   }
 }
 
-__global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Args B, PatchArgs Q) {
+// 256 threads: the FP64 pipe, not the thread count, bounds a colour-round, and 256 threads leave
+// room for the prefetched contact in registers.
+constexpr int kPatch64Block = 256;
+
+__global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32Args B, PatchArgs Q) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   if (*((volatile int*)&A.st->status) != 0) return;
@@ -2140,13 +2158,23 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Arg
   // 16 eval64 apart, the gap doubling where the residual did not decrease.
   unsigned next64 = eval64, interval64 = eval64, prev64_it = 0;
   double prev64_err = INFINITY;
+  // Block 0's phase times (globaltimer): [0] patch interior, [1] the barrier after it and the
+  // shifted tile, [2] the barrier after that and the remainder, [3] checks.
+  unsigned long long t_ph[4] = {0ull, 0ull, 0ull, 0ull}, t_mark = 0ull;
+  const bool timer = tid == 0;
   for (it = 1; it <= A.max_iters; ++it) {
     const bool do_eval = it >= next64 || it == A.max_iters;
+    if (timer) t_mark = globaltimer_ns();
     // The patch's interior (band bodies reloaded: tiles and the remainder touched them).
     if (it > 1)
       for (int j = pb0 + threadIdx.x; j < pbe; j += blockDim.x) sv64[j - pb0] = __ldcg(&A.v[Q.pbody[j]]);
     __syncthreads();
     sweep_group64(A, B, Q, s_goff, ncol_p, sv64, sm64);
+    if (timer) {
+      const unsigned long long t = globaltimer_ns();
+      t_ph[0] += t - t_mark;
+      t_mark = t;
+    }
     const int wend = do_eval ? pb1 : pbe;
     for (int j = pb0 + threadIdx.x; j < wend; j += blockDim.x) A.v[Q.pbody[j]] = sv64[j - pb0];
     if (!grid_sync(A.gb, A.spin)) {
@@ -2159,6 +2187,11 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Arg
       __syncthreads();
       sweep_group64(A, B, Q, s_hoff, ncol_q, svq64, smq64);
       for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) A.v[Q.qbody[j]] = svq64[j - qb0];
+    }
+    if (timer) {
+      const unsigned long long t = globaltimer_ns();
+      t_ph[1] += t - t_mark;
+      t_mark = t;
     }
     if (!grid_sync(A.gb, A.spin)) {
       if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
@@ -2176,6 +2209,11 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Arg
       return;
     }
     ++s64;
+    if (timer) {
+      const unsigned long long t = globaltimer_ns();
+      t_ph[2] += t - t_mark;
+      t_mark = t;
+    }
     if (!do_eval) continue;
     double emax = 0.0;
     for (int k = tid; k < A.nc; k += nthr) {
@@ -2199,6 +2237,7 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Arg
     }
     const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
     ++n_eval;
+    if (timer) t_ph[3] += globaltimer_ns() - t_mark;
     if (err < err_best) {
       err_best = err;
       double2* t = best;
@@ -2235,6 +2274,11 @@ __global__ void __launch_bounds__(kPatchBlock, 1) k_gs_patch64(GsArgs A, Gs32Arg
     int nbc = 0;
     for (int c = 0; c < ncol_r; ++c) nbc += s_boff[c + 1] > s_boff[c];
     A.st->boundary_colors = nbc;
+    // Profile fields: interior; the barrier after it and the tile; the barrier after that, the
+    // remainder and the checks.
+    A.st->phase_ns[0] = t_ph[0];
+    A.st->phase_ns[1] = t_ph[1];
+    A.st->phase_ns[2] = t_ph[2] + t_ph[3];
   }
 }
 
@@ -3285,7 +3329,7 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
         }
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(maxP);
-        lc.blockDim = dim3(kPatchBlock);
+        lc.blockDim = dim3(only64 ? kPatch64Block : kPatchBlock);
         lc.dynamicSmemBytes = only64 ? smem64 : smem;
         lc.stream = s;
         cudaLaunchAttribute at[1];
