@@ -989,7 +989,9 @@ def run_ours(args):
                 "data": "synthetic (seeded dense-pile fill, no dataset)",
                 "config": {"workload": "ball2d_dense_pile_%d" % nb, "discs": nb, "box": [40, 60], "dt": s["dt"],
                            "mu": s["mu"], "CoR": s["CoR"], "tol": 1e-6, "max_iters": 5000,
-                           "form": "warm start (impulse cache), FP32 sweeps + FP64 residual and refinement",
+                           "form": ("warm start (impulse cache), FP32 form: an FP64 probe of four sweeps, then FP64 sweeps "
+                                    "on the two-level partition near tol or FP32 sweeps with FP64 checks further "
+                                    "away" if args.precision == 1 else "warm start (impulse cache), FP64 sweeps"),
                            "pile": pile_note(pile), "timed_steps": [timed0, timed0 + args.steps - 1],
                            "l2": "flushed between timed steps (256 MB write)",
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
