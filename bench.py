@@ -846,6 +846,12 @@ def run_ours(args):
     fast, s, it0, pile = form_pile(args, local)
     nb = s["r"].shape[0]
     stream = torch.cuda.ExternalStream(fast.stream_ptr(), device=local)
+    # Profiling cases only (the headline keeps tol 1e-6 and the library's tuning): another tolerance
+    # and fp64_factor for the steps after the formed pile.
+    if args.tol is not None:
+        fast.reconfigure(tol=args.tol)
+    if args.fp64_factor is not None:
+        fast.set_tuning(fp64_factor=args.fp64_factor)
     # The state every arm starts from: positions, velocities and the impulse cache (the last step's
     # contacts and impulses; a restored context has no last step, so this is read before the
     # autotuner's trials, which end by restoring this state).
@@ -988,7 +994,8 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == 0 else "f32+f64",
                 "data": "synthetic (seeded dense-pile fill, no dataset)",
                 "config": {"workload": "ball2d_dense_pile_%d" % nb, "discs": nb, "box": [40, 60], "dt": s["dt"],
-                           "mu": s["mu"], "CoR": s["CoR"], "tol": 1e-6, "max_iters": 5000,
+                           "mu": s["mu"], "CoR": s["CoR"], "tol": args.tol if args.tol is not None else 1e-6,
+                           "max_iters": 5000,
                            "form": ("warm start (impulse cache), FP32 form: an FP64 probe of four sweeps, then FP64 sweeps "
                                     "on the two-level partition near tol or FP32 sweeps with FP64 checks further "
                                     "away" if args.precision == 1 else "warm start (impulse cache), FP64 sweeps"),
@@ -1038,6 +1045,10 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=60.0,
                     help="seconds of oracle stepping after which the CPU legs start no further step")
     ap.add_argument("--precision", type=int, default=1, help="0 = FP64 sweeps, 1 = FP32 sweeps + FP64 refinement")
+    ap.add_argument("--tol", type=float, default=None,
+                    help="profiling cases: tolerance of the steps after the formed pile (default: 1e-6 throughout)")
+    ap.add_argument("--fp64-factor", type=int, default=None,
+                    help="profiling cases: the FP32 form's fp64_factor for those steps (default: the library's)")
     ap.add_argument("--batch-scenes", type=int, default=4096, help="batched-scene leg (0 = skip)")
     ap.add_argument("--batch-preroll", type=int, default=40)
     ap.add_argument("--batch-steps", type=int, default=8)

@@ -436,7 +436,7 @@ typedef struct {
   int32_t two_level;
   int32_t check_interval;
   int32_t two_level_min_contacts;
-  int32_t fp64_factor;  /* FP32 form: a probe of four one-level FP64 sweeps first; a solve it leaves
+  int32_t fp64_factor;  /* FP32 form: a probe of eight one-level FP64 sweeps first; a solve it leaves
                            within fp64_factor tol goes on in FP64 (on the two-level partition for
                            large scenes), any other in FP32 sweeps until the first FP64 check at or
                            below fp64_factor tol (default 100; 0: no probe, FP32 sweeps until their
@@ -449,7 +449,7 @@ SG_API int sg_set_tuning(sg_ctx* ctx, const sg_tuning* tuning);
 /* Autotuner: from the current state of a single-scene context, times trial_steps steps under each
  * candidate (two-level on, check interval 8 / 16 / 32; then two-level off, the same intervals),
  * one untimed run first, each from a checkpoint of that state; restores the state and keeps the
- * fastest candidate.  ms_per_step (6 entries, may be NULL) gets each candidate's time per step,
+ * fastest candidate, a later candidate replacing an earlier one only when 3 % faster.  ms_per_step (6 entries, may be NULL) gets each candidate's time per step,
  * NaN for candidates that do not apply (the FP64 form has none: its one timing goes to entry 0;
  * sphere scenes have no two-level sweeps).  best (may be NULL) gets the chosen tuning.  The
  * profile counters include the trial steps. */

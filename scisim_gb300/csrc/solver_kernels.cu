@@ -34,8 +34,10 @@ constexpr int kGsBlock = 512;    // FP64 sweep kernel: one fat block per SM (few
 constexpr int kGs32Block = 768;  // FP32 sweep kernel: enough threads for the largest colours
 constexpr int kPatchBlock = 384;  // two-level kernel
 constexpr int kColorBlock = 1024;  // colouring kernel
-// FP32 form: the one-level FP64 sweeps of the probe that starts every solve.
-constexpr unsigned kFp64Probe = 4;
+// FP32 form: the one-level FP64 sweeps of the probe that starts every solve.  A solve that needs
+// more goes on on the two-level partition, whose setup (~1 ms at 500k contacts) pays back after
+// about six of its sweeps; steps of a settled pile mostly need 2-8.
+constexpr unsigned kFp64Probe = 8;
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // u = H v + c for contact k (body b < 0: static).
@@ -350,6 +352,7 @@ struct GsArgs {
   unsigned eval_every;
   int iso = 0;  // isotropic blocks take local_solve_2d_iso (the FP32 form's FP64 sweeps)
   unsigned first_eval = 1;  // k_gs: no residual check before this sweep (the FP32 form's probe: 2)
+  unsigned eval_stride = 1; // k_gs: after sweep 4, checks every eval_stride sweeps (the probe: 2)
 };
 
 __device__ __forceinline__ void gs_update(const GsArgs& A, int k) {
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(kGsBlock, 1) k_gs(GsArgs A) {
         return;
       }
     }
-    if (it % eval_every == 0 && it >= A.first_eval) {
+    if (it % eval_every == 0 && it >= A.first_eval && (it <= 4 || it % A.eval_stride == 0 || it == A.max_iters)) {
       double emax = 0.0;
       for (int k = tid; k < A.nc; k += nthr) {
         const int a = A.ia[k], b = A.ib[k];
@@ -3047,8 +3050,10 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       const bool probe = sp.max_iters > kFp64Probe;
       if (probe) GP.max_iters = kFp64Probe;
       // A warm start rarely converges in one sweep, and a residual check costs about three FP64
-      // sweeps on GB300: the first check follows the second sweep.
+      // sweeps on GB300: the first check follows the second sweep, and after the fourth every
+      // second sweep is checked.
       GP.first_eval = GP.max_iters >= 2 ? 2u : 1u;
+      GP.eval_stride = 2;
       void* pargs[] = {&GP};
       const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);
       stage_mark(ctx, 5);

@@ -149,8 +149,8 @@ def test_two_level_is_deterministic(gpulib):
 
 def test_fp64_continuation_on_the_partition(gpulib, oracle):
     """The FP32 form's FP64 continuation (k_gs_patch64): from a settled pile, with a tolerance the
-    FP64 probe does not reach and fp64_factor so large that every solve stays in FP64, the solves
-    run on the two-level partition in FP64; the reported residual is the oracle's residual of the
+    eight-sweep FP64 probe does not reach and fp64_factor so large that every solve stays in FP64,
+    the solves the probe leaves run on the two-level partition in FP64; the reported residual is the oracle's residual of the
     GPU's impulses, and every step that reports convergence meets the tolerance under it."""
     n = 32768
     s = scenes.dense_pile(n=n, seed=2, width=20.0, height=15.0)
@@ -170,12 +170,12 @@ def test_fp64_continuation_on_the_partition(gpulib, oracle):
     pre.close()
     c = gpulib.Context(dt=s["dt"], gravity=s["gravity"])
     c.restore(ck)
-    tol = 1e-7
-    c.reconfigure(precision=gpulib.PRECISION_FP32_REFINE, tol=tol, max_iters=3000)
+    tol = 5e-8
+    c.reconfigure(precision=gpulib.PRECISION_FP32_REFINE, tol=tol, max_iters=5000)
     c.set_tuning(fp64_factor=1000000)
     c.profile_enable(True)
     c.profile_read(reset=True)
-    checked = 0
+    checked = continued = 0
     for j in range(3):
         q0, v0 = c.state()
         st = c.step(1, first_iteration=it + j)
@@ -184,12 +184,12 @@ def test_fp64_continuation_on_the_partition(gpulib, oracle):
         ib = np.where(g["ib"] >= 0, g["ib"], -1)
         res = oracle.residual_2d(s["m"], v0, g["ia"], ib, bases, s["CoR"], s["mu"], g["alpha"], g["beta"])
         assert abs(res - st["error"]) <= 1e-15 + 1e-6 * st["error"]
-        assert st["iterations"] > 4
+        continued += int(st["iterations"] > 8)  # beyond the eight-sweep FP64 probe
         if st["succeeded"]:
             assert res <= tol * 1.001
             checked += 1
     prof = c.profile_read()
-    assert prof["two_level_solves"] == 3 and prof["fp64_start_solves"] == 3
+    assert continued >= 1 and prof["two_level_solves"] == continued and prof["fp64_start_solves"] == 3
     assert prof["contact_sweeps32"] == 0
     assert checked > 0
     c.close()
