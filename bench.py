@@ -356,7 +356,7 @@ def timed_steps(ctx, torch, stream, k, flush, first_iteration=1):
 
 
 STAGES = ["predictor_and_grid", "pair_counting_and_plane_flags", "contact_writes_and_assembly", "colouring",
-          "start_check_partition_and_packing", "gauss_seidel", "final_velocity", "extract_cache_final_map"]
+          "fp64_probe_partition_and_packing", "gauss_seidel", "final_velocity", "extract_cache_final_map"]
 
 
 def headline_roofline(prof, total_ms, args):
@@ -996,7 +996,7 @@ def run_ours(args):
                 "config": {"workload": "ball2d_dense_pile_%d" % nb, "discs": nb, "box": [40, 60], "dt": s["dt"],
                            "mu": s["mu"], "CoR": s["CoR"], "tol": args.tol if args.tol is not None else 1e-6,
                            "max_iters": 5000,
-                           "form": ("warm start (impulse cache), FP32 form: an FP64 probe of four sweeps, then FP64 sweeps "
+                           "form": ("warm start (impulse cache), FP32 form: an FP64 probe of up to eight sweeps, then FP64 sweeps "
                                     "on the two-level partition near tol or FP32 sweeps with FP64 checks further "
                                     "away" if args.precision == 1 else "warm start (impulse cache), FP64 sweeps"),
                            "pile": pile_note(pile), "timed_steps": [timed0, timed0 + args.steps - 1],

@@ -9,6 +9,7 @@
 // Layout in HBM: q, v interleaved [x0 y0 x1 y1 ...] (double2 per body, as SCISim's
 // VectorXs), r, m, minv one double per body; contacts as SoA arrays (ia, ib int32,
 // n double2, forcing c double2, W 3 doubles, mu, local impulse r double2, key u64).
+#include "ccd2d.hpp"
 #include "ctx.hpp"
 
 #include <algorithm>
@@ -220,8 +221,8 @@ __device__ __forceinline__ bool aabb_overlap(const double4_32a& a, const double4
   return true;
 }
 
-// CollisionDetectionUtilities::computeCCDQuadraticCoeffs + ballBallCCDCollisionHappens
-// (CollisionDetectionUtilities.cpp:3-126).
+// CollisionDetectionUtilities::computeCCDQuadraticCoeffs (CollisionDetectionUtilities.cpp:3-126);
+// the answers on these coefficients are in ccd2d.hpp.
 __device__ __forceinline__ void ccd_coeffs(double2 q0a, double2 q1a, double ra, double2 q0b, double2 q1b,
                                            double rb, double& c0, double& c1, double& c2) {
   const double d0x = q0a.x - q0b.x, d0y = q0a.y - q0b.y;
@@ -232,30 +233,6 @@ __device__ __forceinline__ void ccd_coeffs(double2 q0a, double2 q1a, double ra, 
   c2 = ex * ex + ey * ey;
 }
 
-__device__ __forceinline__ bool ccd_happens(double c0, double c1, double c2, double* t) {
-  // Touching or overlapping at t = 0: the roots below give root1 >= 0 >= root0 for any c1, c2 (a
-  // quadratic with c2 >= 0 and c0 <= 0), so the answer is yes without the square root and the
-  // divisions; only the time of impact needs them.
-  if (!t && c0 <= 0.0) return true;
-  if (c2 != 0.0) {
-    const double c1c1 = c1 * c1;
-    const double fc2c0 = 4.0 * c2 * c0;
-    if (c1c1 < fc2c0) return false;
-    const double ds = sqrt(c1c1 - fc2c0);
-    const double root1 = (c1 > 0.0) ? (2.0 * c0) / (-c1 - ds) : (-c1 + ds) / (2.0 * c2);
-    if (root1 < 0.0) return false;
-    const double root0 = (c1 >= 0.0) ? (-c1 - ds) / (2.0 * c2) : (2.0 * c0) / (-c1 + ds);
-    if (root0 > 1.0) return false;
-    if (t) *t = fmax(0.0, root0);
-    return true;
-  }
-  if (c0 <= 0.0) {
-    if (t) *t = 0.0;
-    return true;
-  }
-  return false;
-}
-
 struct PairScan {
   const double4_32a* aabb;
   const float4* aabb32;   // the boxes rounded outward to FP32 (prefilter), by body
@@ -263,6 +240,7 @@ struct PairScan {
   const GridParams* gp;
   const int* cell_start;
   const int* sorted;
+  const int* cell_of;     // each box's cell (of its min corner), as k_cell_count placed it
   // narrow phase inputs (ccd mode)
   const double2* q0;
   const double2* q1;
@@ -298,7 +276,7 @@ __device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
         if (kCcd) {
           double c0, c1, c2;
           ccd_coeffs(q0a, q1a, ra, s.q0[j], s.q1[j], s.rad[j], c0, c1, c2);
-          if (!ccd_happens(c0, c1, c2, nullptr)) continue;
+          if (!ccd_hits(c0, c1, c2)) continue;
         }
         f(j);
       }
@@ -309,18 +287,85 @@ __device__ __forceinline__ void visit_pairs(const PairScan& s, int i, F&& f) {
 // The counting pass keeps each box's first kPairSlots partners (in visiting order) so that the
 // writing pass of a box with at most that many only sorts them; a box with more visits again.
 constexpr int kPairSlots = 8;
+// Partners a thread queues for its warp's FP64 tests.
+constexpr int kPairQueue = 16;
 
+// Pair counting in two phases per warp.  Each thread runs the FP32 box prefilter over its 3x3 cells
+// and queues the partners j > i that pass; the warp then runs the FP64 box test and the CCD test
+// over all its queued partners 32 at a time, so that the FP64 pipe (narrow on this GPU) issues them
+// for full warps rather than for the few lanes of a warp whose cell loops hit at the same step.  The
+// tests and their arithmetic are those of visit_pairs, so the pairs (and the slots, in visiting
+// order) are the same; a thread whose queue overflows counts with visit_pairs after the warp phase.
 template <bool kCcd>
-__global__ void k_pair_count(int n, PairScan s, int* __restrict__ cnt, int* __restrict__ slots) {
+__global__ void __launch_bounds__(kBlock) k_pair_count(int n, PairScan s, int* __restrict__ cnt,
+                                                       int* __restrict__ slots) {
+  __shared__ int queue[kBlock * kPairQueue];             // per thread: partner j, -1 once rejected
+  __shared__ unsigned short order[kBlock * kPairQueue];  // per warp: its queue entries in lane order
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int* mine_q = queue + threadIdx.x * kPairQueue;
+  int i = -1, m = 0;
+  if (t < n) {
+    i = s.sorted[t];  // bodies in cell order: neighbouring threads scan the same cells
+    const float4 fi = s.aabb32[i];
+    const GridParams& g = *s.gp;
+    const int cell = s.cell_of[i];
+    const int cy = cell / g.dims[0], cx = cell - cy * g.dims[0];
+    for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y) {
+      for (int x = max(cx - 1, 0); x <= min(cx + 1, g.dims[0] - 1); ++x) {
+        const int c = x + g.dims[0] * y;
+        const int e = s.cell_start[c + 1];
+        for (int p = s.cell_start[c]; p < e; ++p) {
+          const float4 fj = s.aabb32s[p];
+          if (fi.z < fj.x || fi.w < fj.y || fj.z < fi.x || fj.w < fi.y) continue;
+          const int j = s.sorted[p];
+          if (j <= i) continue;
+          if (m < kPairQueue) mine_q[m] = j;
+          ++m;
+        }
+      }
+    }
+  }
+  const int q = m <= kPairQueue ? m : 0;
+  int incl = q;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += u;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned short* w_order = order + (threadIdx.x - lane) * kPairQueue;
+  for (int k = 0; k < q; ++k) w_order[incl - q + k] = (unsigned short)(threadIdx.x * kPairQueue + k);
+  __syncwarp();
+  const int block0 = blockIdx.x * blockDim.x;
+  for (int k = lane; k < total; k += 32) {
+    const int e = w_order[k];
+    const int io = s.sorted[block0 + e / kPairQueue];
+    const int j = queue[e];
+    bool hit = aabb_overlap(s.aabb[io], s.aabb[j]);
+    if (kCcd && hit) {
+      double c0, c1, c2;
+      ccd_coeffs(s.q0[io], s.q1[io], s.rad[io], s.q0[j], s.q1[j], s.rad[j], c0, c1, c2);
+      hit = ccd_hits(c0, c1, c2);
+    }
+    if (!hit) queue[e] = -1;
+  }
+  __syncwarp();
   if (t >= n) return;
-  const int i = s.sorted[t];  // bodies in cell order: neighbouring threads scan the same cells
   int c = 0;
   int* mine = slots + (size_t)i * kPairSlots;
-  visit_pairs<kCcd>(s, i, [&](int j) {
-    if (c < kPairSlots) mine[c] = j;
-    ++c;
-  });
+  if (m <= kPairQueue) {
+    for (int k = 0; k < m; ++k) {
+      const int j = mine_q[k];
+      if (j < 0) continue;
+      if (c < kPairSlots) mine[c] = j;
+      ++c;
+    }
+  } else {
+    visit_pairs<kCcd>(s, i, [&](int j) {
+      if (c < kPairSlots) mine[c] = j;
+      ++c;
+    });
+  }
   cnt[i] = c;
 }
 
@@ -752,7 +797,7 @@ __device__ __forceinline__ void visit_pairs_b(const BatchScan& s, int i, F&& f) 
         if (!aabb_overlap(bi, s.aabb[j])) continue;
         double c0, c1, c2;
         ccd_coeffs(q0a, q1a, ra, s.q0[j], s.q1[j], s.rad[j], c0, c1, c2);
-        if (!ccd_happens(c0, c1, c2, nullptr)) continue;
+        if (!ccd_hits(c0, c1, c2)) continue;
         f(j);
       }
     }
@@ -948,6 +993,7 @@ static PairScan make_scan(sg_ctx* ctx, const double* aabb, bool ccd) {
   s.gp = ctx->grid.as<GridParams>();
   s.cell_start = ctx->cell_start.as<int>();
   s.sorted = ctx->sorted.as<int>();
+  s.cell_of = ctx->cell_of.as<int>();
   // RigidBody2D circles keep 3 entries per body: their CCD reads the centres the predictor copied out.
   s.q0 = ccd ? (ctx->rb2d ? ctx->pos0.as<double2>() : ctx->q.as<double2>()) : nullptr;
   s.q1 = ccd ? (ctx->rb2d ? ctx->pos1.as<double2>() : ctx->q1.as<double2>()) : nullptr;
