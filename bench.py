@@ -359,9 +359,10 @@ STAGES = ["predictor_and_grid", "pair_counting_and_plane_flags", "contact_writes
           "fp64_probe_partition_and_packing", "gauss_seidel", "final_velocity", "extract_cache_final_map"]
 
 
-def headline_roofline(prof, total_ms, args):
+def headline_roofline(prof, total_ms, args, sweeps=()):
     """Roofline of the Gauss-Seidel kernel over the timed steps (algorithmic bytes per launch over its
-    CUDA-event time per launch) and the step's stage times from the library's stage events."""
+    CUDA-event time per launch) and the step's stage times from the library's stage events.  sweeps:
+    the timed steps' sweep counts (a solve of more than eight went on after the FP64 probe)."""
     hbm, peak_kind = peaks()
     gl = max(prof["gs_launches"], 1)
     bytes_per_launch = gs_bytes(prof) / gl
@@ -374,11 +375,14 @@ def headline_roofline(prof, total_ms, args):
         kname = "k_gs (cooperative coloured block Gauss-Seidel, FP64)"
     elif two_level:
         kname = "k_gs_patch (two-level FP32 sweeps: patches on shared memory, boundary contacts over the grid)"
-    elif n_f64 > 0 and n_two > 0:
-        kname = ("k_gs (the FP64 probe, one-level) and k_gs_patch (FP64 sweeps on the two-level partition for "
-                 "the %d of %d solves the probe left unconverged), together" % (n_two, prof["gs_launches"]))
     elif n_f64 >= prof["gs_launches"] > 0:
-        kname = "k_gs (the FP64 probe, one-level: every solve converged in it)"
+        n_cont = sum(1 for x in sweeps if x > 8)
+        if n_cont == 0:
+            kname = "k_gs (the FP64 probe, one-level: every solve converged in it)"
+        else:
+            kname = ("k_gs (the FP64 probe, one-level), then for the %d of %d solves it left unconverged "
+                     "k_gs_mixed's one-level FP64 sweeps (up to 160) and, for %d of them, k_gs_patch64 "
+                     "(FP64 sweeps on the two-level partition), together" % (n_cont, prof["gs_launches"], n_two))
     else:
         kname = "k_gs_mixed (cooperative FP32 sweeps, FP64 checks and refinement)"
     traffic = None
@@ -894,7 +898,7 @@ def run_ours(args):
     convergence = convergence_record(recs)
     log("fast: %d contact-steps in %.1f ms; per step ms %s; %s; profile %s" % (
         csteps, total_ms, [round(x, 2) for x in ms], convergence, prof))
-    roofline, stages = headline_roofline(prof, total_ms, args)
+    roofline, stages = headline_roofline(prof, total_ms, args, [r["sweeps"] for r in recs])
 
     def arm(**over):
         c = _lib.Context(device=local, **solver_kw(s))

@@ -389,12 +389,18 @@ typedef struct {
 SG_API int sg_profile_enable(sg_ctx* ctx, int32_t on);
 SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
 
-/* Two-level FP32 sweeps for large single-scene steps (default on): contacts inside a spatial
+/* Two-level sweeps for large single-scene steps of the FP32 form: contacts inside a spatial
  * patch (one per SM) are swept on shared-memory velocities with block barriers, then the
  * contacts between patches that lie inside one tile of the patch tiling shifted by half a
  * tile, the same way; the few left over are swept over the grid.  A Gauss-Seidel order of
  * the same kind as the colour order, with three grid barriers a sweep instead of one per
- * colour.  0 keeps the one-level colour sweeps. */
+ * colour.  on: 0 keeps the one-level colour sweeps; 1 (default) takes the two-level sweeps for
+ * FP32 sweeps, while a solve that the FP64 probe leaves near tol goes on in up to 160 one-level
+ * FP64 sweeps before the two-level ones (near tol the two-level order, which sweeps the contacts
+ * between patches after the patches, can hold the residual on a plateau just above tol for
+ * hundreds of sweeps that the colour order crosses in tens, while a solve that needs thousands
+ * of sweeps either way is cheaper on the partition); 2 takes the two-level sweeps for those FP64
+ * sweeps from the start.  SG_BAD_INPUT for other values. */
 SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
 
 /* Selects the map a single Ball2D, sphere or RigidBody2D scene steps with (default
@@ -429,7 +435,7 @@ SG_API int sg_checkpoint_save(sg_ctx* ctx, void* buf, int64_t bytes);
 SG_API int sg_checkpoint_load(sg_ctx* ctx, const void* buf, int64_t bytes);
 
 /* Performance knobs that leave the solve's contract unchanged (no counterpart in the reference):
- * two_level (sg_set_two_level), the contact count from which a single-scene FP32 solve uses the
+ * two_level (sg_set_two_level: 0, 1 or 2), the contact count from which a single-scene FP32 solve uses the
  * two-level sweeps (default 20,000), and the base interval in sweeps of the FP64 checks of the
  * FP32 form (default 16; the interval grows from it while the residual is far from tol). */
 typedef struct {
@@ -437,8 +443,8 @@ typedef struct {
   int32_t check_interval;
   int32_t two_level_min_contacts;
   int32_t fp64_factor;  /* FP32 form: a probe of eight one-level FP64 sweeps first; a solve it leaves
-                           within fp64_factor tol goes on in FP64 (on the two-level partition for
-                           large scenes), any other in FP32 sweeps until the first FP64 check at or
+                           within fp64_factor tol goes on in FP64 (see sg_set_two_level for the
+                           order), any other in FP32 sweeps until the first FP64 check at or
                            below fp64_factor tol (default 100; 0: no probe, FP32 sweeps until their
                            rounding floor) */
 } sg_tuning;

@@ -471,7 +471,10 @@ class Context:
         return d
 
     def set_two_level(self, on=True):
-        check(lib().sg_set_two_level(self._h, 1 if on else 0), "sg_set_two_level")
+        """0 / False: one-level sweeps; 1 / True (default): two-level FP32 sweeps, and for a solve the
+        FP64 probe leaves near tol up to 160 one-level FP64 sweeps before two-level ones; 2: two-level
+        FP64 sweeps for such a solve from the start."""
+        check(lib().sg_set_two_level(self._h, int(on)), "sg_set_two_level")
 
     def set_staggering(self, staggering=STAGGER_GEOMETRIC, stabilize=False, penetration_threshold=0.0):
         """GeometricImpactFrictionMap (default), SymplecticEulerImpactFrictionMap or

@@ -1415,7 +1415,7 @@ int sg_set_staggering(sg_ctx* ctx, int32_t staggering, int32_t stabilize, double
 // Tuning of the launch-independent performance knobs (no counterpart in the reference).
 int sg_get_tuning(sg_ctx* ctx, sg_tuning* t) {
   if (!ctx || !t) return SG_BAD_INPUT;
-  t->two_level = ctx->patches ? 1 : 0;
+  t->two_level = ctx->patches;
   t->check_interval = ctx->check_interval;
   t->two_level_min_contacts = ctx->two_level_min_contacts;
   t->fp64_factor = ctx->fp64_factor;
@@ -1423,12 +1423,13 @@ int sg_get_tuning(sg_ctx* ctx, sg_tuning* t) {
 }
 
 int sg_set_tuning(sg_ctx* ctx, const sg_tuning* t) {
-  if (!ctx || !t || t->check_interval < 1 || t->check_interval > 4096 || t->two_level_min_contacts < 0 ||
-      t->fp64_factor < 0) {
-    set_error("sg_set_tuning: check_interval in [1, 4096], two_level_min_contacts >= 0, fp64_factor >= 0");
+  if (!ctx || !t || t->two_level < 0 || t->two_level > 2 || t->check_interval < 1 || t->check_interval > 4096 ||
+      t->two_level_min_contacts < 0 || t->fp64_factor < 0) {
+    set_error("sg_set_tuning: two_level in [0, 2], check_interval in [1, 4096], two_level_min_contacts >= 0, "
+              "fp64_factor >= 0");
     return SG_BAD_INPUT;
   }
-  ctx->patches = t->two_level != 0;
+  ctx->patches = t->two_level;
   ctx->check_interval = t->check_interval;
   ctx->two_level_min_contacts = t->two_level_min_contacts;
   ctx->fp64_factor = t->fp64_factor;
@@ -1499,8 +1500,11 @@ int sg_autotune(sg_ctx* ctx, int32_t trial_steps, uint32_t first_iteration, sg_t
 }
 
 int sg_set_two_level(sg_ctx* ctx, int32_t on) {
-  if (!ctx) return SG_BAD_INPUT;
-  ctx->patches = on != 0;
+  if (!ctx || on < 0 || on > 2) {
+    set_error("sg_set_two_level: 0 (off), 1 (FP32 sweeps) or 2 (also the FP64 continuation)");
+    return SG_BAD_INPUT;
+  }
+  ctx->patches = on;
   return SG_OK;
 }
 

@@ -187,9 +187,9 @@ struct sg_ctx {
   int64_t ccap3 = 0;
   sg::Buf E3, Aa3, Ab3, c3, W3, r3, r3a, r3b, ab3, vrun3;
   sg::Buf pk3, Iinv32;  // 3D FP32 sweep data (colour-packed contacts, body inverse inertia)
-  // Two-level FP32 sweeps (spatial patches, one per SM): patch of each body, patch-local
-  // index, bodies by patch, contact keys (patch, colour) and the packed order.
-  bool patches = true;
+  // Two-level sweeps (spatial patches, one per SM): 0 off, 1 for FP32 sweeps, 2 also for the
+  // FP64 sweeps of a solve the probe leaves near tol (sg_set_two_level).
+  int patches = 1;
   // Staggering of the single-scene Ball2D step (sg_set_staggering): SG_STAGGER_*, and the
   // symplectic Euler map's pose stabilisation and threshold; its velocity change per body.
   int staggering = 0;

@@ -38,6 +38,8 @@ constexpr int kColorBlock = 1024;  // colouring kernel
 // more goes on on the two-level partition, whose setup (~1 ms at 500k contacts) pays back after
 // about six of its sweeps; steps of a settled pile mostly need 2-8.
 constexpr unsigned kFp64Probe = 8;
+// FP32 form, two_level 1: one-level FP64 sweeps after the probe before the two-level partition.
+constexpr unsigned kOneLevel64 = 160;
 inline int blocks_for(long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // u = H v + c for contact k (body b < 0: static).
@@ -826,6 +828,10 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
   bool converged = false, fp64 = B.fp64_start != 0;
   unsigned it = 0, n_eval = 0, s32 = 0, s64 = 0, lifts = 0, since_best = 0;
   unsigned next_eval = 1, interval = eval32;
+  // FP64 sweeps' checks as in k_gs_patch64: where the residual's rate over the last two checks
+  // predicts tol, at most 16 eval64 apart, the gap doubling where the residual did not decrease.
+  unsigned next64 = 0, interval64 = eval64, prev64_it = 0;
+  double prev64_err = INFINITY;
   C32 pf;
   bool have_pf = false, have_pf_valid = false;
   for (it = 1; it <= A.max_iters; ++it) {
@@ -920,7 +926,8 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
         }
       }
       ++s64;
-      do_eval = (it % eval64 == 0) || it == A.max_iters;
+      if (next64 == 0) next64 = it + eval64 - 1;  // the first FP64 sweep: a check eval64 sweeps on
+      do_eval = it >= next64 || it == A.max_iters;
     }
     if (!do_eval) continue;
     // emax: the residual.  excess: the largest amount by which a contact's error exceeds
@@ -984,12 +991,24 @@ __global__ void __launch_bounds__(kGs32Block, 1) k_gs_mixed(GsArgs A, Gs32Args B
         converged = true;
         break;
       }
+      if (err < prev64_err && prev64_err < INFINITY && err > 0.0) {
+        const double per_sweep = (log(err) - log(prev64_err)) / (double)(it - prev64_it);
+        const double need = (log(A.tol) - log(err)) / per_sweep;
+        interval64 = need >= (double)(16u * eval64) ? 16u * eval64 : max(eval64, (unsigned)need);
+      } else {
+        interval64 = prev64_err < INFINITY ? min(2u * interval64, 16u * eval64) : eval64;
+      }
+      prev64_err = err;
+      prev64_it = it;
+      next64 = it + interval64;
     } else if (err < A.tol || err <= B.fp64_below || excess32 <= A.tol ||
                (since_best >= 16 && excess32 <= 16.0 * A.tol)) {
       // FP64 refinement from the FP64 image: a closing sweep once FP32 reached tol, or
       // FP64 sweeps once every contact's remaining error is within FP32 rounding of
       // its floor (or FP32 stopped improving the best iterate close to it).
       fp64 = true;
+      prev64_err = err;
+      prev64_it = it;
     }
   }
   if (it > A.max_iters) it = A.max_iters;
@@ -1046,6 +1065,8 @@ struct PatchArgs {
   int capc;           // their shared-memory slots (even), 0 if the remainder is not staged
   int ncbody;         // their number
   int stage_c;        // remaining contacts staged in block 0 (all of them, or 0)
+  int rest64;         // k_gs_patch64: the remainder's bodies held in block 0's shared memory
+                      //   (all of them, or 0: the remainder then sweeps on global velocities)
 };
 
 // Bodies of the remaining contacts (group P + Pb): flagged here, compacted by a scan.
@@ -2029,11 +2050,20 @@ struct C64 {
   double w00, w01, w11, mu;
 };
 
-__device__ __forceinline__ void load64(const GsArgs& A, const Gs32Args& B, const PatchArgs& Q, int q, C64& x) {
-  const int2 ab = B.ab[q];
+// sab non-null: the group is the remainder, whose body slots come packed from shared memory
+// (sab[q - sab0] = slot of a | slot of b << 16); otherwise from the packed pairs B.ab.
+__device__ __forceinline__ void load64(const GsArgs& A, const Gs32Args& B, const PatchArgs& Q, int q, C64& x,
+                                       const unsigned* sab, int sab0) {
+  if (sab) {
+    const unsigned ab = sab[q - sab0];
+    x.la = (int)(ab & 0xffffu);
+    x.lb = (int)(ab >> 16);
+  } else {
+    const int2 ab = B.ab[q];
+    x.la = ab.x;
+    x.lb = ab.y;
+  }
   x.k = Q.order[q];
-  x.la = ab.x;
-  x.lb = ab.y;
   x.n = A.n[x.k];
   x.c = A.c[x.k];
   x.w00 = A.W[3 * x.k];
@@ -2041,6 +2071,19 @@ __device__ __forceinline__ void load64(const GsArgs& A, const Gs32Args& B, const
   x.w11 = A.W[3 * x.k + 2];
   x.mu = A.mu[x.k];
   x.r = __ldcg(&A.r[x.k]);
+}
+
+// The local solve of a block that is not isotropic (none in a disc scene: the Delassus block of
+// two discs or of a disc and a plane is a multiple of the identity), kept out of line so that its
+// registers do not count against the sweeps'.
+__device__ __noinline__ double2 general_local64(double2 n, double2 c, double2 r, double w00, double w01,
+                                                double w11, double mu, double2 va, bool has_b, double2 vb) {
+  double u0, u1, rn0, rn1;
+  local_velocity(n, c, va, has_b, vb, u0, u1);
+  const double bt0 = u0 - (w00 * r.x + w01 * r.y);
+  const double bt1 = u1 - (w01 * r.x + w11 * r.y);
+  local_solve_2d(w00, w01, w11, bt0, bt1, mu, rn0, rn1);
+  return make_double2(rn0, rn1);
 }
 
 __device__ __forceinline__ void update64(const GsArgs& A, const C64& x, double2* sv, const double* sm) {
@@ -2065,11 +2108,9 @@ __device__ __forceinline__ void update64(const GsArgs& A, const C64& x, double2*
     const double lim = x.mu * rn0;
     rn1 = fabs(rt) <= lim ? rt : copysign(lim, rt);
   } else {
-    double u0, u1;
-    local_velocity(x.n, x.c, va, has_b, vb, u0, u1);
-    const double bt0 = u0 - (x.w00 * r0 + x.w01 * r1);
-    const double bt1 = u1 - (x.w01 * r0 + x.w11 * r1);
-    local_solve_2d(x.w00, x.w01, x.w11, bt0, bt1, x.mu, rn0, rn1);
+    const double2 rn = general_local64(x.n, x.c, x.r, x.w00, x.w01, x.w11, x.mu, va, has_b, vb);
+    rn0 = rn.x;
+    rn1 = rn.y;
   }
   const double d0 = rn0 - r0, d1 = rn1 - r1;
   const double px = fma(nx, d0, -ny * d1);
@@ -2083,36 +2124,35 @@ __device__ __forceinline__ void update64(const GsArgs& A, const C64& x, double2*
   A.r[x.k] = make_double2(rn0, rn1);
 }
 
-// One group's colours on shared-memory velocities: off[0..ncol] are its (group, colour) runs.
+// One group's colours on shared-memory velocities: off[0..ncol] are its (group, colour) runs.  A
+// thread's contacts are loaded one ahead: the next colour's first before this colour's barrier,
+// and within a colour each next one before the update of the one before it (contact data do not
+// depend on the velocities).
 __device__ __forceinline__ void sweep_group64(const GsArgs& A, const Gs32Args& B, const PatchArgs& Q,
-                                              const int* off, int ncol, double2* sv, const double* sm) {
+                                              const int* off, int ncol, double2* sv, const double* sm,
+                                              const unsigned* sab = nullptr, int sab0 = 0) {
   C64 nxt;
   bool have = false;
   if (ncol > 0 && off[0] + (int)threadIdx.x < off[1]) {
-    load64(A, B, Q, off[0] + threadIdx.x, nxt);
+    load64(A, B, Q, off[0] + threadIdx.x, nxt, sab, sab0);
     have = true;
   }
   for (int col = 0; col < ncol; ++col) {
     const int e = off[col + 1];
-    int q = off[col] + threadIdx.x;
+    const int qn = (col + 1 < ncol) ? off[col + 1] + threadIdx.x : e;
+    const bool have_n = col + 1 < ncol && qn < off[col + 2];
     if (have) {
-      const C64 cur = nxt;
-      // The next colour's first contact of this thread, loaded before this colour's barrier.
-      const int qn = (col + 1 < ncol) ? off[col + 1] + threadIdx.x : e;
-      have = col + 1 < ncol && qn < off[col + 2];
-      update64(A, cur, sv, sm);
-      q += blockDim.x;
-      for (; q < e; q += blockDim.x) {
+      C64 cur = nxt;
+      for (int q = off[col] + threadIdx.x + blockDim.x; q < e; q += blockDim.x) {
         C64 x;
-        load64(A, B, Q, q, x);
-        update64(A, x, sv, sm);
+        load64(A, B, Q, q, x, sab, sab0);
+        update64(A, cur, sv, sm);
+        cur = x;
       }
-      if (have) load64(A, B, Q, qn, nxt);
-    } else {
-      const int qn = (col + 1 < ncol) ? off[col + 1] + threadIdx.x : e;
-      have = col + 1 < ncol && qn < off[col + 2];
-      if (have) load64(A, B, Q, qn, nxt);
+      update64(A, cur, sv, sm);
     }
+    have = have_n;
+    if (have) load64(A, B, Q, qn, nxt, sab, sab0);
     __syncthreads();
   }
 }
@@ -2129,6 +2169,12 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
   double* sm64 = reinterpret_cast<double*>(sv64 + Q.cap);
   double2* svq64 = reinterpret_cast<double2*>(sm64 + Q.cap);
   double* smq64 = reinterpret_cast<double*>(svq64 + Q.capq);
+  // Block 0's copy of the remainder: its bodies' velocities and inverse masses (slots as cslot
+  // numbers them), then each remaining contact's two slots packed in 32 bits.
+  const int capc64 = (Q.rest64 + 1) & ~1;
+  double2* svc64 = reinterpret_cast<double2*>(smq64 + Q.capq);
+  double* smc64 = reinterpret_cast<double*>(svc64 + capc64);
+  unsigned* sab64 = reinterpret_cast<unsigned*>(smc64 + capc64);
   __shared__ int s_goff[kMaxColors + 1];
   __shared__ int s_hoff[kMaxColors + 1];
   __shared__ int s_boff[kMaxColors + 1];
@@ -2151,6 +2197,20 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
   for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) smq64[j - qb0] = A.minv[Q.qbody[j]];
   __syncthreads();
   const int ncol_p = group_colors(s_goff), ncol_q = group_colors(s_hoff), ncol_r = group_colors(s_boff);
+  // The remainder's colours: the large leading ones over the grid (one grid barrier each), the
+  // small trailing ones by block 0 (staged in its shared memory when the host found room).
+  int btail = ncol_r;
+  while (btail > 0 && s_boff[btail] - s_boff[btail - 1] <= 2 * (int)blockDim.x) --btail;
+  const int sc0 = s_boff[btail], nrest_tail = s_boff[ncol_r] - sc0;
+  const bool rest_staged = Q.rest64 > 0 && nrest_tail > 0;
+  if (rest_staged && blockIdx.x == 0) {
+    for (int j = threadIdx.x; j < Q.rest64; j += blockDim.x) smc64[j] = A.minv[Q.cbody[j]];
+    for (int q = sc0 + threadIdx.x; q < sc0 + nrest_tail; q += blockDim.x) {
+      const int2 ab = B.ab[q];
+      sab64[q - sc0] = (unsigned)Q.cslot[ab.x] | ((unsigned)Q.cslot[ab.y] << 16);
+    }
+  }
+  __syncthreads();
   const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
   double2* best = A.r_a;
   double2* cand = A.r_b;
@@ -2163,11 +2223,13 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
   double prev64_err = INFINITY;
   // Block 0's phase times (globaltimer): [0] patch interior, [1] the barrier after it and the
   // shifted tile, [2] the barrier after that and the remainder, [3] checks.
-  unsigned long long t_ph[4] = {0ull, 0ull, 0ull, 0ull}, t_mark = 0ull;
+  // In shared memory, so that they take no registers from the sweeps; [4] is the running mark.
+  __shared__ unsigned long long t_ph[5];
   const bool timer = tid == 0;
+  if (timer) t_ph[0] = t_ph[1] = t_ph[2] = t_ph[3] = t_ph[4] = 0ull;
   for (it = 1; it <= A.max_iters; ++it) {
     const bool do_eval = it >= next64 || it == A.max_iters;
-    if (timer) t_mark = globaltimer_ns();
+    if (timer) t_ph[4] = globaltimer_ns();
     // The patch's interior (band bodies reloaded: tiles and the remainder touched them).
     if (it > 1)
       for (int j = pb0 + threadIdx.x; j < pbe; j += blockDim.x) sv64[j - pb0] = __ldcg(&A.v[Q.pbody[j]]);
@@ -2175,8 +2237,8 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
     sweep_group64(A, B, Q, s_goff, ncol_p, sv64, sm64);
     if (timer) {
       const unsigned long long t = globaltimer_ns();
-      t_ph[0] += t - t_mark;
-      t_mark = t;
+      t_ph[0] += t - t_ph[4];
+      t_ph[4] = t;
     }
     const int wend = do_eval ? pb1 : pbe;
     for (int j = pb0 + threadIdx.x; j < wend; j += blockDim.x) A.v[Q.pbody[j]] = sv64[j - pb0];
@@ -2193,29 +2255,48 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
     }
     if (timer) {
       const unsigned long long t = globaltimer_ns();
-      t_ph[1] += t - t_mark;
-      t_mark = t;
+      t_ph[1] += t - t_ph[4];
+      t_ph[4] = t;
     }
     if (!grid_sync(A.gb, A.spin)) {
       if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
       return;
     }
-    // The remainder, by block 0 on global velocities.
-    if (blockIdx.x == 0 && s_boff[ncol_r] > s_boff[0]) {
-      for (int col = 0; col < ncol_r; ++col) {
-        for (int q = s_boff[col] + threadIdx.x; q < s_boff[col + 1]; q += blockDim.x) gs_update(A, Q.order[q]);
-        __syncthreads();
+    // The remainder: large colours over the grid on global velocities, then the small trailing
+    // ones by block 0, on shared-memory velocities when staged.
+    for (int col = 0; col < btail; ++col) {
+      const int b0 = s_boff[col], e = s_boff[col + 1];
+      if (b0 == e) continue;
+      for (int q = b0 + tid; q < e; q += nthr) gs_update(A, Q.order[q]);
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
       }
     }
-    if (!grid_sync(A.gb, A.spin)) {
-      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
-      return;
+    if (nrest_tail > 0) {
+      if (blockIdx.x == 0) {
+        if (rest_staged) {
+          for (int j = threadIdx.x; j < Q.rest64; j += blockDim.x) svc64[j] = __ldcg(&A.v[Q.cbody[j]]);
+          __syncthreads();
+          sweep_group64(A, B, Q, s_boff + btail, ncol_r - btail, svc64, smc64, sab64, sc0);
+          for (int j = threadIdx.x; j < Q.rest64; j += blockDim.x) A.v[Q.cbody[j]] = svc64[j];
+        } else {
+          for (int col = btail; col < ncol_r; ++col) {
+            for (int q = s_boff[col] + threadIdx.x; q < s_boff[col + 1]; q += blockDim.x) gs_update(A, Q.order[q]);
+            __syncthreads();
+          }
+        }
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
     }
     ++s64;
     if (timer) {
       const unsigned long long t = globaltimer_ns();
-      t_ph[2] += t - t_mark;
-      t_mark = t;
+      t_ph[2] += t - t_ph[4];
+      t_ph[4] = t;
     }
     if (!do_eval) continue;
     double emax = 0.0;
@@ -2240,7 +2321,7 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
     }
     const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
     ++n_eval;
-    if (timer) t_ph[3] += globaltimer_ns() - t_mark;
+    if (timer) t_ph[3] += globaltimer_ns() - t_ph[4];
     if (err < err_best) {
       err_best = err;
       double2* t = best;
@@ -3093,271 +3174,316 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
       }
     }
     if (fp32_sweeps) {
-      const size_t c = (size_t)nc, b = (size_t)std::max(nb, 1);
-      if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
-      if (int r = grow(ctx->pk_n, sizeof(float2) * c)) return r;
-      if (int r = grow(ctx->pk_c, sizeof(float2) * c)) return r;
-      if (int r = grow(ctx->pk_w, sizeof(float4) * c)) return r;
-      if (int r = grow(ctx->pk_r, sizeof(float2) * c)) return r;
-      if (int r = grow(ctx->v32, sizeof(float2) * b)) return r;
-      if (int r = grow(ctx->minv32, sizeof(float) * b)) return r;
-      // Two-level sweeps for large scene steps (the broad phase's grid gives the patches).
-      int pmax = 0;
-      const int maxP = ctx->num_sms;
-      const bool try_patches = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 &&
-                               nc >= ctx->two_level_min_contacts;
-      int pmaxq = 0, cmax_p = 0, cmax_q = 0, nrest = 0, nrest_bodies = 0;
-      PatchSetup hps{};
-      if (try_patches) {
-        // Groups: at most maxP patches, maxP shifted tiles and the remainder (a degenerate
-        // setup is rejected below before any launch uses it).
-        const int groups = 2 * maxP + 8;
-        const size_t keys = (size_t)groups * kMaxColors + 1;
-        const size_t gsz = sizeof(int) * (size_t)(groups + 1);
-        if (int r = grow(ctx->pt_setup, sizeof(PatchSetup))) return r;
-        if (int r = grow(ctx->pt_patch, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_qpatch, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_band, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_lidx, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_lidxq, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_body, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_qbody, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_cnt, gsz)) return r;
-        if (int r = grow(ctx->pt_start, gsz)) return r;
-        if (int r = grow(ctx->pt_fill, gsz)) return r;
-        if (int r = grow(ctx->pt_bcnt, gsz)) return r;
-        if (int r = grow(ctx->pt_nfill, gsz)) return r;
-        if (int r = grow(ctx->pt_qcnt, gsz)) return r;
-        if (int r = grow(ctx->pt_qstart, gsz)) return r;
-        if (int r = grow(ctx->pt_qfill, gsz)) return r;
-        if (int r = grow(ctx->pt_key, sizeof(int) * c)) return r;
-        if (int r = grow(ctx->pt_kcnt, sizeof(int) * keys)) return r;
-        if (int r = grow(ctx->pt_kstart, sizeof(int) * keys)) return r;
-        if (int r = grow(ctx->pt_kfill, sizeof(int) * keys)) return r;
-        if (int r = grow(ctx->pt_order, sizeof(int) * c)) return r;
-        if (int r = grow(ctx->pt_max, 7 * sizeof(int))) return r;
-        // Cell columns and rows number at most the broad phase's cell capacity (4 nb + 64).
-        const size_t gcap = 4 * (size_t)nb + 64;
-        if (int r = grow(ctx->pt_hist, 2 * sizeof(int) * gcap)) return r;
-        if (int r = grow(ctx->pt_pref, 2 * sizeof(int) * (gcap + 1))) return r;
-        if (int r = grow(ctx->pt_cuts, 2 * sizeof(int) * (size_t)(maxP + 2))) return r;
-        if (int r = grow(ctx->pt_maps, 4 * sizeof(int) * gcap)) return r;
-        if (int r = grow(ctx->pt_cflag, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_cpos, sizeof(int) * (b + 1))) return r;
-        if (int r = grow(ctx->pt_cbody, sizeof(int) * b)) return r;
-        if (int r = grow(ctx->pt_bcolor, sizeof(int) * c)) return r;
-        if (int r = grow(ctx->pt_rem, 4 * sizeof(int))) return r;
-        PatchSetup* ps = ctx->pt_setup.as<PatchSetup>();
-        k_patch_setup<<<1, 1, 0, s>>>(ctx->grid.as<GridParams>(), maxP, ps);
-        for (Buf* z : {&ctx->pt_cnt, &ctx->pt_fill, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qfill})
-          SG_CUDA_TRY(cudaMemsetAsync(z->p, 0, gsz, s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kcnt.p, 0, sizeof(int) * keys, s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kfill.p, 0, sizeof(int) * keys, s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, 7 * sizeof(int), s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_cflag.p, 0, sizeof(int) * b, s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_band.p, 0, sizeof(int) * b, s));
-        {
-          int* hx = ctx->pt_hist.as<int>();
-          int* hy = hx + gcap;
-          int* px = ctx->pt_pref.as<int>();
-          int* py = px + gcap + 1;
-          int* cx = ctx->pt_cuts.as<int>();
-          int* cy = cx + maxP + 2;
-          int* maps = ctx->pt_maps.as<int>();
-          SG_CUDA_TRY(cudaMemsetAsync(hx, 0, 2 * sizeof(int) * gcap, s));
-          k_patch_hist<<<blocks_for((long)nc + nb), kBlock, 0, s>>>(nc, nb, P.ia, ctx->cell_of.as<int>(), ps, hx, hy);
+      // A solve the probe leaves near tol under two_level 1: up to kOneLevel64 one-level FP64
+      // sweeps first, then, unconverged, the two-level partition for the rest.  Near tol the
+      // two-level order, which sweeps the contacts between patches after the patches, can hold
+      // the residual on a plateau just above tol for hundreds of sweeps that the colour order
+      // crosses in tens; a solve that needs thousands of sweeps either way gets the two-level
+      // sweeps' lower cost for all but the first kOneLevel64.
+      const bool eligible = sp.learned && ctx->patches && ctx->dim == 2 && ctx->n_scenes == 0 &&
+                            nc >= ctx->two_level_min_contacts;
+      bool second_pass = false;
+      for (int pass = 0;; ++pass) {
+        const bool one_level = pass == 0 && fp64_start && ctx->patches == 1;
+        const bool one_level_first = one_level && eligible && GA.max_iters > kOneLevel64;
+        const unsigned remaining = GA.max_iters;
+        if (one_level_first) GA.max_iters = kOneLevel64;
+        const size_t c = (size_t)nc, b = (size_t)std::max(nb, 1);
+        if (int r = grow(ctx->pk_ab, sizeof(int2) * c)) return r;
+        if (int r = grow(ctx->pk_n, sizeof(float2) * c)) return r;
+        if (int r = grow(ctx->pk_c, sizeof(float2) * c)) return r;
+        if (int r = grow(ctx->pk_w, sizeof(float4) * c)) return r;
+        if (int r = grow(ctx->pk_r, sizeof(float2) * c)) return r;
+        if (int r = grow(ctx->v32, sizeof(float2) * b)) return r;
+        if (int r = grow(ctx->minv32, sizeof(float) * b)) return r;
+        // Two-level sweeps for large scene steps (the broad phase's grid gives the patches).
+        int pmax = 0;
+        const int maxP = ctx->num_sms;
+        const bool try_patches = eligible && !one_level;
+        int pmaxq = 0, cmax_p = 0, cmax_q = 0, nrest = 0, nrest_bodies = 0;
+        PatchSetup hps{};
+        if (try_patches) {
+          // Groups: at most maxP patches, maxP shifted tiles and the remainder (a degenerate
+          // setup is rejected below before any launch uses it).
+          const int groups = 2 * maxP + 8;
+          const size_t keys = (size_t)groups * kMaxColors + 1;
+          const size_t gsz = sizeof(int) * (size_t)(groups + 1);
+          if (int r = grow(ctx->pt_setup, sizeof(PatchSetup))) return r;
+          if (int r = grow(ctx->pt_patch, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_qpatch, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_band, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_lidx, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_lidxq, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_body, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_qbody, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_cnt, gsz)) return r;
+          if (int r = grow(ctx->pt_start, gsz)) return r;
+          if (int r = grow(ctx->pt_fill, gsz)) return r;
+          if (int r = grow(ctx->pt_bcnt, gsz)) return r;
+          if (int r = grow(ctx->pt_nfill, gsz)) return r;
+          if (int r = grow(ctx->pt_qcnt, gsz)) return r;
+          if (int r = grow(ctx->pt_qstart, gsz)) return r;
+          if (int r = grow(ctx->pt_qfill, gsz)) return r;
+          if (int r = grow(ctx->pt_key, sizeof(int) * c)) return r;
+          if (int r = grow(ctx->pt_kcnt, sizeof(int) * keys)) return r;
+          if (int r = grow(ctx->pt_kstart, sizeof(int) * keys)) return r;
+          if (int r = grow(ctx->pt_kfill, sizeof(int) * keys)) return r;
+          if (int r = grow(ctx->pt_order, sizeof(int) * c)) return r;
+          if (int r = grow(ctx->pt_max, 7 * sizeof(int))) return r;
+          // Cell columns and rows number at most the broad phase's cell capacity (4 nb + 64).
+          const size_t gcap = 4 * (size_t)nb + 64;
+          if (int r = grow(ctx->pt_hist, 2 * sizeof(int) * gcap)) return r;
+          if (int r = grow(ctx->pt_pref, 2 * sizeof(int) * (gcap + 1))) return r;
+          if (int r = grow(ctx->pt_cuts, 2 * sizeof(int) * (size_t)(maxP + 2))) return r;
+          if (int r = grow(ctx->pt_maps, 4 * sizeof(int) * gcap)) return r;
+          if (int r = grow(ctx->pt_cflag, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_cpos, sizeof(int) * (b + 1))) return r;
+          if (int r = grow(ctx->pt_cbody, sizeof(int) * b)) return r;
+          if (int r = grow(ctx->pt_bcolor, sizeof(int) * c)) return r;
+          if (int r = grow(ctx->pt_rem, 4 * sizeof(int))) return r;
+          PatchSetup* ps = ctx->pt_setup.as<PatchSetup>();
+          k_patch_setup<<<1, 1, 0, s>>>(ctx->grid.as<GridParams>(), maxP, ps);
+          for (Buf* z : {&ctx->pt_cnt, &ctx->pt_fill, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qfill})
+            SG_CUDA_TRY(cudaMemsetAsync(z->p, 0, gsz, s));
+          SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kcnt.p, 0, sizeof(int) * keys, s));
+          SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_kfill.p, 0, sizeof(int) * keys, s));
+          SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_max.p, 0, 7 * sizeof(int), s));
+          SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_cflag.p, 0, sizeof(int) * b, s));
+          SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_band.p, 0, sizeof(int) * b, s));
+          {
+            int* hx = ctx->pt_hist.as<int>();
+            int* hy = hx + gcap;
+            int* px = ctx->pt_pref.as<int>();
+            int* py = px + gcap + 1;
+            int* cx = ctx->pt_cuts.as<int>();
+            int* cy = cx + maxP + 2;
+            int* maps = ctx->pt_maps.as<int>();
+            SG_CUDA_TRY(cudaMemsetAsync(hx, 0, 2 * sizeof(int) * gcap, s));
+            k_patch_hist<<<blocks_for((long)nc + nb), kBlock, 0, s>>>(nc, nb, P.ia, ctx->cell_of.as<int>(), ps, hx, hy);
+            SG_CUDA_TRY(cudaGetLastError());
+            if (int r = scan_exclusive(ctx, hx, px, (int)gcap)) return r;
+            if (int r = scan_exclusive(ctx, hy, py, (int)gcap)) return r;
+            k_patch_cuts<<<1, kBlock, 0, s>>>(ps, px, py, cx, cy);
+            k_patch_maps<<<blocks_for((long)gcap), kBlock, 0, s>>>(ps, cx, cy, maps, maps + gcap, maps + 2 * gcap,
+                                                                 maps + 3 * gcap);
+            k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, maps, maps + gcap,
+                                                             maps + 2 * gcap, maps + 3 * gcap, ctx->pt_patch.as<int>(),
+                                                             ctx->pt_qpatch.as<int>(), ctx->pt_cnt.as<int>());
+          }
           SG_CUDA_TRY(cudaGetLastError());
-          if (int r = scan_exclusive(ctx, hx, px, (int)gcap)) return r;
-          if (int r = scan_exclusive(ctx, hy, py, (int)gcap)) return r;
-          k_patch_cuts<<<1, kBlock, 0, s>>>(ps, px, py, cx, cy);
-          k_patch_maps<<<blocks_for((long)gcap), kBlock, 0, s>>>(ps, cx, cy, maps, maps + gcap, maps + 2 * gcap,
-                                                               maps + 3 * gcap);
-          k_patch_of_body<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->cell_of.as<int>(), ps, maps, maps + gcap,
-                                                           maps + 2 * gcap, maps + 3 * gcap, ctx->pt_patch.as<int>(),
-                                                           ctx->pt_qpatch.as<int>(), ctx->pt_cnt.as<int>());
+          int* cpatch = ctx->pt_order.as<int>();  // scratch until the order is built
+          int* bcolor = ctx->pt_bcolor.as<int>();
+          k_contact_side<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, ctx->pt_patch.as<int>(),
+                                                           ctx->pt_qpatch.as<int>(), ps, cpatch, bcolor,
+                                                           ctx->pt_band.as<int>());
+          k_rest_mark<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, cpatch, ps, ctx->pt_cflag.as<int>());
+          SG_CUDA_TRY(cudaGetLastError());
+          if (int r = scan_exclusive(ctx, ctx->pt_cflag.as<int>(), ctx->pt_cpos.as<int>(), nb)) return r;
+          k_rest_scatter<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_cflag.as<int>(), ctx->pt_cpos.as<int>(),
+                                                          ctx->pt_cbody.as<int>());
+          SG_CUDA_TRY(cudaMemcpyAsync(ctx->pt_max.as<int>() + 6, ctx->pt_cpos.as<int>() + nb, sizeof(int),
+                                      cudaMemcpyDeviceToDevice, s));
+          k_band_count<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_band.as<int>(), ctx->pt_patch.as<int>(),
+                                                         ctx->pt_qpatch.as<int>(), ctx->pt_bcnt.as<int>(),
+                                                         ctx->pt_qcnt.as<int>());
+          SG_CUDA_TRY(cudaGetLastError());
+          if (int r = scan_exclusive(ctx, ctx->pt_cnt.as<int>(), ctx->pt_start.as<int>(), groups)) return r;
+          if (int r = scan_exclusive(ctx, ctx->pt_qcnt.as<int>(), ctx->pt_qstart.as<int>(), groups)) return r;
+          k_patch_scatter<<<blocks_for(nb), kBlock, 0, s>>>(
+              nb, ctx->pt_patch.as<int>(), ctx->pt_qpatch.as<int>(), ctx->pt_band.as<int>(), ctx->pt_start.as<int>(),
+              ctx->pt_bcnt.as<int>(), ctx->pt_fill.as<int>(), ctx->pt_nfill.as<int>(), ctx->pt_body.as<int>(),
+              ctx->pt_lidx.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qfill.as<int>(), ctx->pt_qbody.as<int>(),
+              ctx->pt_lidxq.as<int>());
+          k_patch_max<<<1, kBlock, 0, s>>>(groups, ctx->pt_cnt.as<int>(), ctx->pt_max.as<int>());
+          k_patch_max<<<1, kBlock, 0, s>>>(groups, ctx->pt_qcnt.as<int>(), ctx->pt_max.as<int>() + 1);
+          SG_CUDA_TRY(cudaGetLastError());
+          SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+          SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_rem.p, 0, 4 * sizeof(int), s));
+          {
+            BColorArgs BA{nc, P.ia, P.ib, off, adj, cpatch, ps, bcolor, ctx->pt_rem.as<int>(), &st->status, gb,
+                          ctx->spin_limit, 4096};
+            void* bargs[] = {&BA};
+            const int g = coop_grid(ctx, k_color_boundary, nc, kBlock);
+            SG_CUDA_TRY(launch_cooperative((const void*)k_color_boundary, g, kBlock, bargs, s));
+          }
+          k_group_color_init<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->color.as<int>(), cpatch, ps, bcolor,
+                                                              ctx->pt_max.as<int>() + 2);
+          SG_CUDA_TRY(cudaGetLastError());
+          SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+          {
+            RecolorArgs RA{nc, P.ia, P.ib, off, adj, cpatch, bcolor, ctx->pt_max.as<int>() + 2, &st->status, gb,
+                           ctx->spin_limit};
+            void* rargs[] = {&RA};
+            const int g = coop_grid(ctx, k_recolor_groups, nc, kBlock);
+            SG_CUDA_TRY(launch_cooperative((const void*)k_recolor_groups, g, kBlock, rargs, s));
+          }
+          k_contact_key<<<blocks_for(nc), kBlock, 0, s>>>(nc, bcolor, cpatch, ctx->pt_key.as<int>(),
+                                                         ctx->pt_kcnt.as<int>());
+          SG_CUDA_TRY(cudaGetLastError());
+          if (int r = scan_exclusive(ctx, ctx->pt_kcnt.as<int>(), ctx->pt_kstart.as<int>(), (int)(keys - 1))) return r;
+          k_contact_scatter<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_key.as<int>(), ctx->pt_kstart.as<int>(),
+                                                             ctx->pt_kfill.as<int>(), ctx->pt_order.as<int>());
+          k_group_max<<<1, kBlock, 0, s>>>(ps, ctx->pt_kstart.as<int>(), ctx->pt_max.as<int>() + 3);
+          SG_CUDA_TRY(cudaGetLastError());
+          int hmax[7] = {0, 0, 0, 0, 0, 0, 0};
+          SG_CUDA_TRY(cudaMemcpyAsync(hmax, ctx->pt_max.p, 7 * sizeof(int), cudaMemcpyDeviceToHost, s));
+          SG_CUDA_TRY(cudaMemcpyAsync(&hps, ps, sizeof(PatchSetup), cudaMemcpyDeviceToHost, s));
+          SG_CUDA_TRY(cudaStreamSynchronize(s));
+          pmax = hmax[0];
+          pmaxq = hmax[1];
+          cmax_p = hmax[3];
+          cmax_q = hmax[4];
+          nrest = hmax[5];
+          nrest_bodies = hmax[6];
+          // setup, hist, 2 x 3 scan, cuts, maps, of_body, side, rest mark, 3 scan, rest scatter,
+          // band_count, 2 x 3 scan, scatter, 2 max, colour, colour init, recolour, key, 3 scan,
+          // scatter, group max
+          ctx->kernel_launches += 36;
         }
-        SG_CUDA_TRY(cudaGetLastError());
-        int* cpatch = ctx->pt_order.as<int>();  // scratch until the order is built
-        int* bcolor = ctx->pt_bcolor.as<int>();
-        k_contact_side<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, ctx->pt_patch.as<int>(),
-                                                         ctx->pt_qpatch.as<int>(), ps, cpatch, bcolor,
-                                                         ctx->pt_band.as<int>());
-        k_rest_mark<<<blocks_for(nc), kBlock, 0, s>>>(nc, P.ia, P.ib, cpatch, ps, ctx->pt_cflag.as<int>());
-        SG_CUDA_TRY(cudaGetLastError());
-        if (int r = scan_exclusive(ctx, ctx->pt_cflag.as<int>(), ctx->pt_cpos.as<int>(), nb)) return r;
-        k_rest_scatter<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_cflag.as<int>(), ctx->pt_cpos.as<int>(),
-                                                        ctx->pt_cbody.as<int>());
-        SG_CUDA_TRY(cudaMemcpyAsync(ctx->pt_max.as<int>() + 6, ctx->pt_cpos.as<int>() + nb, sizeof(int),
-                                    cudaMemcpyDeviceToDevice, s));
-        k_band_count<<<blocks_for(nb), kBlock, 0, s>>>(nb, ctx->pt_band.as<int>(), ctx->pt_patch.as<int>(),
-                                                       ctx->pt_qpatch.as<int>(), ctx->pt_bcnt.as<int>(),
-                                                       ctx->pt_qcnt.as<int>());
-        SG_CUDA_TRY(cudaGetLastError());
-        if (int r = scan_exclusive(ctx, ctx->pt_cnt.as<int>(), ctx->pt_start.as<int>(), groups)) return r;
-        if (int r = scan_exclusive(ctx, ctx->pt_qcnt.as<int>(), ctx->pt_qstart.as<int>(), groups)) return r;
-        k_patch_scatter<<<blocks_for(nb), kBlock, 0, s>>>(
-            nb, ctx->pt_patch.as<int>(), ctx->pt_qpatch.as<int>(), ctx->pt_band.as<int>(), ctx->pt_start.as<int>(),
-            ctx->pt_bcnt.as<int>(), ctx->pt_fill.as<int>(), ctx->pt_nfill.as<int>(), ctx->pt_body.as<int>(),
-            ctx->pt_lidx.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qfill.as<int>(), ctx->pt_qbody.as<int>(),
-            ctx->pt_lidxq.as<int>());
-        k_patch_max<<<1, kBlock, 0, s>>>(groups, ctx->pt_cnt.as<int>(), ctx->pt_max.as<int>());
-        k_patch_max<<<1, kBlock, 0, s>>>(groups, ctx->pt_qcnt.as<int>(), ctx->pt_max.as<int>() + 1);
-        SG_CUDA_TRY(cudaGetLastError());
-        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-        SG_CUDA_TRY(cudaMemsetAsync(ctx->pt_rem.p, 0, 4 * sizeof(int), s));
-        {
-          BColorArgs BA{nc, P.ia, P.ib, off, adj, cpatch, ps, bcolor, ctx->pt_rem.as<int>(), &st->status, gb,
-                        ctx->spin_limit, 4096};
-          void* bargs[] = {&BA};
-          const int g = coop_grid(ctx, k_color_boundary, nc, kBlock);
-          SG_CUDA_TRY(launch_cooperative((const void*)k_color_boundary, g, kBlock, bargs, s));
+        // Shared-memory slots rounded up to even counts (8-byte alignment of the second block).
+        const int capp = (pmax + 1) & ~1, capq = (pmaxq + 1) & ~1;
+        // Body slots must fit in shared memory beside the kernel's static arrays (12 B each).
+        const bool patched = try_patches && hps.P >= 2 && hps.Pb <= maxP && pmax > 0 &&
+                             capp + capq <= kPatchBodyCap;
+        patched_run = patched;
+        ctx->last_patched = patched;
+        if (patched) {
+          ctx->last_patch_P = hps.P;
+          ctx->last_patch_Pb = hps.Pb;
         }
-        k_group_color_init<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->color.as<int>(), cpatch, ps, bcolor,
-                                                            ctx->pt_max.as<int>() + 2);
+        if (patched)
+          k_pack32_patch<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_order.as<int>(), ctx->pt_key.as<int>(),
+                                                           ctx->pt_setup.as<PatchSetup>(), P.ia, P.ib,
+                                                           ctx->pt_lidx.as<int>(), ctx->pt_lidxq.as<int>(), n2, reinterpret_cast<const double2*>(P.c),
+                                                           P.W, P.mu, r2, ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(),
+                                                           ctx->pk_c.as<float2>(), ctx->pk_w.as<float4>(),
+                                                           ctx->pk_r.as<float2>());
+        else
+          k_pack32<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), P.ia, P.ib, n2,
+                                                     reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2,
+                                                     ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
+                                                     ctx->pk_w.as<float4>(), ctx->pk_r.as<float2>());
+        k_vel32<<<blocks_for(nb), kBlock, 0, s>>>(nb, vrun, P.minv, ctx->v32.as<float2>(), ctx->minv32.as<float>());
         SG_CUDA_TRY(cudaGetLastError());
-        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-        {
-          RecolorArgs RA{nc, P.ia, P.ib, off, adj, cpatch, bcolor, ctx->pt_max.as<int>() + 2, &st->status, gb,
-                         ctx->spin_limit};
-          void* rargs[] = {&RA};
-          const int g = coop_grid(ctx, k_recolor_groups, nc, kBlock);
-          SG_CUDA_TRY(launch_cooperative((const void*)k_recolor_groups, g, kBlock, rargs, s));
+        Gs32Args GB;
+        GB.ab = ctx->pk_ab.as<int2>();
+        GB.n = ctx->pk_n.as<float2>();
+        GB.c = ctx->pk_c.as<float2>();
+        GB.w = ctx->pk_w.as<float4>();
+        GB.r = ctx->pk_r.as<float2>();
+        GB.v = ctx->v32.as<float2>();
+        GB.minv = ctx->minv32.as<float>();
+        GB.minv64 = P.minv;
+        GB.v0 = reinterpret_cast<const double2*>(P.v0);
+        GB.body_off = off;
+        GB.body_adj = adj;
+        GB.nb = nb;
+        GB.eval32 = (unsigned)ctx->check_interval;
+        GB.fp64_below = (double)ctx->fp64_factor * sp.tol;
+        GB.fp64_start = fp64_start ? 1 : 0;
+        if (patched) {
+          // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
+          // contacts as fit (the patch's first), 32 B each.
+          if (ctx->patch_smem_budget < 0) {
+            int optin = 0;
+            SG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+            cudaFuncAttributes fa{};
+            SG_CUDA_TRY(cudaFuncGetAttributes(&fa, k_gs_patch));
+            const int budget = optin - (int)fa.sharedSizeBytes;
+            SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch, cudaFuncAttributeMaxDynamicSharedMemorySize, budget));
+            ctx->patch_smem_budget = budget;
+          }
+          const int dyn_budget = ctx->patch_smem_budget;
+          const int body_bytes = 12 * (capp + capq);
+          // The remainder first (block 0 sweeps it whole or not at all), then the patch, the tile.
+          int capc = (nrest_bodies + 1) & ~1, stage_c = nrest;
+          int rest_bytes = 12 * capc + 32 * stage_c;
+          if (nrest == 0 || nrest_bodies > kPatchBodyCap || rest_bytes > dyn_budget - body_bytes) {
+            capc = stage_c = rest_bytes = 0;
+          }
+          const int avail = std::max(0, dyn_budget - body_bytes - rest_bytes) / 32;
+          const int stage_p = std::min(cmax_p, avail);
+          const int stage_q = std::min(cmax_q, avail - stage_p);
+          PatchArgs Q{ctx->pt_setup.as<PatchSetup>(), ctx->pt_start.as<int>(), ctx->pt_body.as<int>(),
+                      ctx->pt_bcnt.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qbody.as<int>(),
+                      ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), capp, capq, stage_p, stage_q,
+                      ctx->pt_cbody.as<int>(), ctx->pt_cpos.as<int>(), capc, capc ? nrest_bodies : 0, stage_c, 0};
+          size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q) + (size_t)rest_bytes;
+          // The FP64 sweeps reuse the same shared memory for the patch's and the tile's FP64
+          // velocities and inverse masses (24 B per body) when they fit.
+          size_t smem64 = (size_t)24 * (size_t)(capp + capq);
+          GB.fp64_local = smem64 <= (size_t)dyn_budget ? 1 : 0;
+          if (GB.fp64_local && smem64 > smem) smem = smem64;
+          // k_gs_patch64 also holds the remainder in block 0 (24 B per body, 4 B per contact) when
+          // that fits beside the patch and the tile.
+          const size_t rest64_bytes = (size_t)24 * (size_t)((nrest_bodies + 1) & ~1) + (size_t)4 * (size_t)nrest;
+          if (GB.fp64_local && nrest > 0 && nrest_bodies <= kPatchBodyCap &&
+              smem64 + rest64_bytes <= (size_t)dyn_budget) {
+            Q.rest64 = nrest_bodies;
+            smem64 += rest64_bytes;
+          }
+          ctx->patch_staged += (uint64_t)stage_p;
+          void* args[] = {&GA, &GB, &Q};
+          // The boundary colouring used the barrier: start it afresh for this grid.
+          SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+          if (!second_pass) stage_mark(ctx, 5);
+          if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+          // A solve that stays in FP64 takes the FP64 kernel (its velocities fit shared memory).
+          const bool only64 = fp64_start && GB.fp64_local;
+          if (only64 && !ctx->patch64_ready) {
+            SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch64, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_budget));
+            ctx->patch64_ready = true;
+          }
+          cudaLaunchConfig_t lc = {};
+          lc.gridDim = dim3(maxP);
+          lc.blockDim = dim3(only64 ? kPatch64Block : kPatchBlock);
+          lc.dynamicSmemBytes = only64 ? smem64 : smem;
+          lc.stream = s;
+          cudaLaunchAttribute at[1];
+          at[0].id = cudaLaunchAttributeCooperative;
+          at[0].val.cooperative = 1;
+          lc.attrs = at;
+          lc.numAttrs = 1;
+          SG_CUDA_TRY(cudaLaunchKernelExC(&lc, only64 ? (const void*)k_gs_patch64 : (const void*)k_gs_patch, args));
+          if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+          stage_mark(ctx, 6);
+          ctx->patched_solves += 1;
+        } else {
+          void* args[] = {&GA, &GB};
+          const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
+          // The patch setup's colouring kernels used the barrier with their own grid: reset it.
+          SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+          if (!second_pass) stage_mark(ctx, 5);
+          if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+          SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
+          if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+          stage_mark(ctx, 6);
         }
-        k_contact_key<<<blocks_for(nc), kBlock, 0, s>>>(nc, bcolor, cpatch, ctx->pt_key.as<int>(),
-                                                       ctx->pt_kcnt.as<int>());
-        SG_CUDA_TRY(cudaGetLastError());
-        if (int r = scan_exclusive(ctx, ctx->pt_kcnt.as<int>(), ctx->pt_kstart.as<int>(), (int)(keys - 1))) return r;
-        k_contact_scatter<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_key.as<int>(), ctx->pt_kstart.as<int>(),
-                                                           ctx->pt_kfill.as<int>(), ctx->pt_order.as<int>());
-        k_group_max<<<1, kBlock, 0, s>>>(ps, ctx->pt_kstart.as<int>(), ctx->pt_max.as<int>() + 3);
-        SG_CUDA_TRY(cudaGetLastError());
-        int hmax[7] = {0, 0, 0, 0, 0, 0, 0};
-        SG_CUDA_TRY(cudaMemcpyAsync(hmax, ctx->pt_max.p, 7 * sizeof(int), cudaMemcpyDeviceToHost, s));
-        SG_CUDA_TRY(cudaMemcpyAsync(&hps, ps, sizeof(PatchSetup), cudaMemcpyDeviceToHost, s));
+        ctx->kernel_launches += 2;
+        if (!one_level_first) break;
+        SolveStats h1{};
+        SG_CUDA_TRY(cudaMemcpyAsync(&h1, st, sizeof(SolveStats), cudaMemcpyDeviceToHost, s));
         SG_CUDA_TRY(cudaStreamSynchronize(s));
-        pmax = hmax[0];
-        pmaxq = hmax[1];
-        cmax_p = hmax[3];
-        cmax_q = hmax[4];
-        nrest = hmax[5];
-        nrest_bodies = hmax[6];
-        // setup, hist, 2 x 3 scan, cuts, maps, of_body, side, rest mark, 3 scan, rest scatter,
-        // band_count, 2 x 3 scan, scatter, 2 max, colour, colour init, recolour, key, 3 scan,
-        // scatter, group max
-        ctx->kernel_launches += 36;
-      }
-      // Shared-memory slots rounded up to even counts (8-byte alignment of the second block).
-      const int capp = (pmax + 1) & ~1, capq = (pmaxq + 1) & ~1;
-      // Body slots must fit in shared memory beside the kernel's static arrays (12 B each).
-      const bool patched = try_patches && hps.P >= 2 && hps.Pb <= maxP && pmax > 0 &&
-                           capp + capq <= kPatchBodyCap;
-      patched_run = patched;
-      ctx->last_patched = patched;
-      if (patched) {
-        ctx->last_patch_P = hps.P;
-        ctx->last_patch_Pb = hps.Pb;
-      }
-      if (patched)
-        k_pack32_patch<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->pt_order.as<int>(), ctx->pt_key.as<int>(),
-                                                         ctx->pt_setup.as<PatchSetup>(), P.ia, P.ib,
-                                                         ctx->pt_lidx.as<int>(), ctx->pt_lidxq.as<int>(), n2, reinterpret_cast<const double2*>(P.c),
-                                                         P.W, P.mu, r2, ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(),
-                                                         ctx->pk_c.as<float2>(), ctx->pk_w.as<float4>(),
-                                                         ctx->pk_r.as<float2>());
-      else
-        k_pack32<<<blocks_for(nc), kBlock, 0, s>>>(nc, ctx->perm.as<int>(), P.ia, P.ib, n2,
-                                                   reinterpret_cast<const double2*>(P.c), P.W, P.mu, r2,
-                                                   ctx->pk_ab.as<int2>(), ctx->pk_n.as<float2>(), ctx->pk_c.as<float2>(),
-                                                   ctx->pk_w.as<float4>(), ctx->pk_r.as<float2>());
-      k_vel32<<<blocks_for(nb), kBlock, 0, s>>>(nb, vrun, P.minv, ctx->v32.as<float2>(), ctx->minv32.as<float>());
-      SG_CUDA_TRY(cudaGetLastError());
-      Gs32Args GB;
-      GB.ab = ctx->pk_ab.as<int2>();
-      GB.n = ctx->pk_n.as<float2>();
-      GB.c = ctx->pk_c.as<float2>();
-      GB.w = ctx->pk_w.as<float4>();
-      GB.r = ctx->pk_r.as<float2>();
-      GB.v = ctx->v32.as<float2>();
-      GB.minv = ctx->minv32.as<float>();
-      GB.minv64 = P.minv;
-      GB.v0 = reinterpret_cast<const double2*>(P.v0);
-      GB.body_off = off;
-      GB.body_adj = adj;
-      GB.nb = nb;
-      GB.eval32 = (unsigned)ctx->check_interval;
-      GB.fp64_below = (double)ctx->fp64_factor * sp.tol;
-      GB.fp64_start = fp64_start ? 1 : 0;
-      if (patched) {
-        // Dynamic shared memory: the body slots, then as many of the patch's and the tile's
-        // contacts as fit (the patch's first), 32 B each.
-        if (ctx->patch_smem_budget < 0) {
-          int optin = 0;
-          SG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-          cudaFuncAttributes fa{};
-          SG_CUDA_TRY(cudaFuncGetAttributes(&fa, k_gs_patch));
-          const int budget = optin - (int)fa.sharedSizeBytes;
-          SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch, cudaFuncAttributeMaxDynamicSharedMemorySize, budget));
-          ctx->patch_smem_budget = budget;
+        if (h1.converged || h1.status != 0) break;
+        // On from the one-level sweeps' best iterate (velocities recomputed from it) on the
+        // two-level partition, within the remaining sweeps; the residual slots start afresh.
+        if (ctx->profile) {
+          float ms = 0.f;
+          SG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev_gs0, ctx->ev_gs1));
+          ctx->gs_ms += ms;
         }
-        const int dyn_budget = ctx->patch_smem_budget;
-        const int body_bytes = 12 * (capp + capq);
-        // The remainder first (block 0 sweeps it whole or not at all), then the patch, the tile.
-        int capc = (nrest_bodies + 1) & ~1, stage_c = nrest;
-        int rest_bytes = 12 * capc + 32 * stage_c;
-        if (nrest == 0 || nrest_bodies > kPatchBodyCap || rest_bytes > dyn_budget - body_bytes) {
-          capc = stage_c = rest_bytes = 0;
-        }
-        const int avail = std::max(0, dyn_budget - body_bytes - rest_bytes) / 32;
-        const int stage_p = std::min(cmax_p, avail);
-        const int stage_q = std::min(cmax_q, avail - stage_p);
-        PatchArgs Q{ctx->pt_setup.as<PatchSetup>(), ctx->pt_start.as<int>(), ctx->pt_body.as<int>(),
-                    ctx->pt_bcnt.as<int>(), ctx->pt_qstart.as<int>(), ctx->pt_qbody.as<int>(),
-                    ctx->pt_kstart.as<int>(), ctx->pt_order.as<int>(), capp, capq, stage_p, stage_q,
-                    ctx->pt_cbody.as<int>(), ctx->pt_cpos.as<int>(), capc, capc ? nrest_bodies : 0, stage_c};
-        size_t smem = (size_t)body_bytes + (size_t)32 * (size_t)(stage_p + stage_q) + (size_t)rest_bytes;
-        // The FP64 sweeps reuse the same shared memory for the patch's and the tile's FP64
-        // velocities and inverse masses (24 B per body) when they fit.
-        const size_t smem64 = (size_t)24 * (size_t)(capp + capq);
-        GB.fp64_local = smem64 <= (size_t)dyn_budget ? 1 : 0;
-        if (GB.fp64_local && smem64 > smem) smem = smem64;
-        ctx->patch_staged += (uint64_t)stage_p;
-        void* args[] = {&GA, &GB, &Q};
-        // The boundary colouring used the barrier: start it afresh for this grid.
+        probe_iters += h1.iterations;
+        probe_evals += h1.evals;
+        GA.max_iters = remaining - h1.iterations;
+        k_vel_init<<<blocks_for(nb), kBlock, 0, s>>>(nb, off, adj, P.ia, n2, r2,
+                                                     reinterpret_cast<const double2*>(P.v0), P.minv, vrun);
+        SG_CUDA_TRY(cudaGetLastError());
+        SG_CUDA_TRY(cudaMemsetAsync(st->err_slot, 0, sizeof(st->err_slot), s));
+        SG_CUDA_TRY(cudaMemsetAsync(st->mag_slot, 0, sizeof(st->mag_slot), s));
         SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-        stage_mark(ctx, 5);
-        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-        // A solve that stays in FP64 takes the FP64 kernel (its velocities fit shared memory).
-        const bool only64 = fp64_start && GB.fp64_local;
-        if (only64 && !ctx->patch64_ready) {
-          SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch64, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_budget));
-          ctx->patch64_ready = true;
-        }
-        cudaLaunchConfig_t lc = {};
-        lc.gridDim = dim3(maxP);
-        lc.blockDim = dim3(only64 ? kPatch64Block : kPatchBlock);
-        lc.dynamicSmemBytes = only64 ? smem64 : smem;
-        lc.stream = s;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeCooperative;
-        at[0].val.cooperative = 1;
-        lc.attrs = at;
-        lc.numAttrs = 1;
-        SG_CUDA_TRY(cudaLaunchKernelExC(&lc, only64 ? (const void*)k_gs_patch64 : (const void*)k_gs_patch, args));
-        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
-        stage_mark(ctx, 6);
-        ctx->patched_solves += 1;
-      } else {
-        void* args[] = {&GA, &GB};
-        const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);
-        // The patch setup's colouring kernels used the barrier with their own grid: reset it.
-        SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
-        stage_mark(ctx, 5);
-        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-        SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_mixed, dim3(g), dim3(kGs32Block), args, 0, s));
-        if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
-        stage_mark(ctx, 6);
+        ctx->kernel_launches += 1;
+        second_pass = true;
       }
-      ctx->kernel_launches += 2;
     } else if (!fp32_form) {
       void* args[] = {&GA};
       const int g = coop_grid(ctx, k_gs, nc, kGsBlock, 1);

@@ -147,11 +147,16 @@ def test_two_level_is_deterministic(gpulib):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
 
-def test_fp64_continuation_on_the_partition(gpulib, oracle):
-    """The FP32 form's FP64 continuation (k_gs_patch64): from a settled pile, with a tolerance the
-    eight-sweep FP64 probe does not reach and fp64_factor so large that every solve stays in FP64,
-    the solves the probe leaves run on the two-level partition in FP64; the reported residual is the oracle's residual of the
-    GPU's impulses, and every step that reports convergence meets the tolerance under it."""
+@pytest.mark.parametrize("two_level", [1, 2])
+def test_fp64_continuation(gpulib, oracle, two_level):
+    """The FP32 form's FP64 continuation: from a settled pile, with a tolerance the eight-sweep
+    FP64 probe does not reach and fp64_factor so large that every solve stays in FP64, the solves
+    the probe leaves go on in FP64 sweeps: under the default two_level 1 one-level (k_gs_mixed's
+    FP64 sweeps with their rate-predicted checks) for up to 160 sweeps, then on the two-level
+    partition (k_gs_patch64); under two_level 2 on the partition from the start.  The reported
+    residual is the oracle's residual of the GPU's impulses, every continued solve ends below the
+    residual the probe alone reaches from the same state, and every step that reports convergence
+    meets the tolerance under it."""
     n = 32768
     s = scenes.dense_pile(n=n, seed=2, width=20.0, height=15.0)
     pre = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE, max_iters=50)
@@ -173,10 +178,20 @@ def test_fp64_continuation_on_the_partition(gpulib, oracle):
     tol = 5e-8
     c.reconfigure(precision=gpulib.PRECISION_FP32_REFINE, tol=tol, max_iters=5000)
     c.set_tuning(fp64_factor=1000000)
+    for bad in (-1, 3):
+        with pytest.raises(gpulib.SgError):
+            c.set_two_level(bad)
+    c.set_two_level(two_level)
     c.profile_enable(True)
     c.profile_read(reset=True)
-    checked = continued = 0
+    continued = partitioned = 0
     for j in range(3):
+        # The probe alone (eight FP64 sweeps) from the same state.
+        p8 = gpulib.Context(dt=s["dt"], gravity=s["gravity"])
+        p8.restore(c.checkpoint())
+        p8.reconfigure(max_iters=8)
+        e8 = p8.step(1, first_iteration=it + j)["error"]
+        p8.close()
         q0, v0 = c.state()
         st = c.step(1, first_iteration=it + j)
         g = c.last_contacts()
@@ -184,12 +199,14 @@ def test_fp64_continuation_on_the_partition(gpulib, oracle):
         ib = np.where(g["ib"] >= 0, g["ib"], -1)
         res = oracle.residual_2d(s["m"], v0, g["ia"], ib, bases, s["CoR"], s["mu"], g["alpha"], g["beta"])
         assert abs(res - st["error"]) <= 1e-15 + 1e-6 * st["error"]
-        continued += int(st["iterations"] > 8)  # beyond the eight-sweep FP64 probe
+        if st["iterations"] > 8:  # beyond the eight-sweep FP64 probe
+            continued += 1
+            partitioned += int(two_level == 2 or st["iterations"] > 8 + 160)
+            assert st["error"] < e8, (st["error"], e8)
         if st["succeeded"]:
             assert res <= tol * 1.001
-            checked += 1
     prof = c.profile_read()
-    assert continued >= 1 and prof["two_level_solves"] == continued and prof["fp64_start_solves"] == 3
+    assert continued >= 1 and prof["fp64_start_solves"] == 3
+    assert prof["two_level_solves"] == partitioned
     assert prof["contact_sweeps32"] == 0
-    assert checked > 0
     c.close()
