@@ -381,8 +381,9 @@ def headline_roofline(prof, total_ms, args, sweeps=()):
             kname = "k_gs (the FP64 probe, one-level: every solve converged in it)"
         else:
             kname = ("k_gs (the FP64 probe, one-level), then for the %d of %d solves it left unconverged "
-                     "k_gs_mixed's one-level FP64 sweeps (up to 160) and, for %d of them, k_gs_patch64 "
-                     "(FP64 sweeps on the two-level partition), together" % (n_cont, prof["gs_launches"], n_two))
+                     "k_gs_mixed's one-level FP64 sweeps (up to 160) and, for %d of them, k_gs_patch_ff "
+                     "(FP64-precision sweeps on the two-level partition in float-float pairs), together"
+                     % (n_cont, prof["gs_launches"], n_two))
     else:
         kname = "k_gs_mixed (cooperative FP32 sweeps, FP64 checks and refinement)"
     traffic = None
@@ -944,7 +945,8 @@ def run_ours(args):
 
     # e2e through sg_flow with pinned host buffers, from the same state and impulse cache.
     e2e = None
-    if args.e2e_steps > 0:
+    e2e_steps = args.steps if args.e2e_steps is None else args.e2e_steps
+    if e2e_steps > 0:
         ectx = arm()
         bufs = [torch.empty(2 * nb, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
         bufs[0][:] = q_snap
@@ -953,7 +955,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         ec, econv, eerr = 0, 0, 0.0
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
+        for _ in range(e2e_steps):
             _, _, st = ectx.flow(it, bufs[0], bufs[1], bufs[2], bufs[3])
             bufs = [bufs[2], bufs[3], bufs[0], bufs[1]]
             ec += st["n_contacts"]
@@ -962,7 +964,7 @@ def run_ours(args):
             it += 1
         el = time.perf_counter() - t0
         e2e = {"value": ec / el, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * nb, "d2h_bytes_per_step": 2 * 16 * nb,
-               "steps": args.e2e_steps, "steps_converged": econv, "max_residual": eerr,
+               "steps": e2e_steps, "steps_converged": econv, "max_residual": eerr,
                "api": "sg_flow (ImpactFrictionMap::flow), pinned host q/v, from the timed steps' state and cache"}
         log("e2e:", e2e)
         ectx.close()
@@ -1043,7 +1045,8 @@ def main():
                     help="steps of the plain FP64 arm (default: --steps, the timed steps themselves)")
     ap.add_argument("--cold-steps", type=int, default=1)
     ap.add_argument("--cold-iters", type=int, default=20000)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="steps of the e2e leg (default: --steps, the timed steps themselves)")
     ap.add_argument("--form-error", type=int, default=1, help="FP32-form vs FP64 error from the timed state (0 = skip)")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=60.0,

@@ -119,6 +119,7 @@ SIGNATURES = {
     "sg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "sg_set_two_level": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sg_set_fp64_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "sg_set_staggering": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "sg_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sg_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -475,6 +476,10 @@ class Context:
         FP64 probe leaves near tol up to 160 one-level FP64 sweeps before two-level ones; 2: two-level
         FP64 sweeps for such a solve from the start."""
         check(lib().sg_set_two_level(self._h, int(on)), "sg_set_two_level")
+
+    def set_fp64_pairs(self, on=True):
+        """The two-level FP64 sweeps for discs in float-float pairs (True, default) or FP64 (False)."""
+        check(lib().sg_set_fp64_pairs(self._h, int(on)), "sg_set_fp64_pairs")
 
     def set_staggering(self, staggering=STAGGER_GEOMETRIC, stabilize=False, penetration_threshold=0.0):
         """GeometricImpactFrictionMap (default), SymplecticEulerImpactFrictionMap or

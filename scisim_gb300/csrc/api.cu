@@ -278,7 +278,8 @@ void sg_ctx_destroy(sg_ctx* ctx) {
                   &ctx->pt_bcolor, &ctx->pt_rem, &ctx->pt_qpatch, &ctx->pt_band, &ctx->pt_lidxq,
                   &ctx->pt_qbody, &ctx->pt_bcnt, &ctx->pt_nfill, &ctx->pt_qcnt, &ctx->pt_qstart, &ctx->pt_qfill,
                   &ctx->pt_cflag, &ctx->pt_cpos, &ctx->pt_cbody, &ctx->pt_hist, &ctx->pt_pref,
-                  &ctx->pt_cuts, &ctx->pt_maps};
+                  &ctx->pt_cuts, &ctx->pt_maps, &ctx->ff_n, &ctx->ff_c, &ctx->ff_m, &ctx->ff_r, &ctx->ff_v,
+                  &ctx->ff_minv};
   for (Buf* b : bufs3) release(*b);
   Buf* bufsm[] = {&ctx->mlp_p, &ctx->mlp_feat, &ctx->mlp_tgt, &ctx->mlp_x, &ctx->mlp_t, &ctx->mlp_slots,
                   &ctx->mlp_choice};
@@ -1505,6 +1506,15 @@ int sg_set_two_level(sg_ctx* ctx, int32_t on) {
     return SG_BAD_INPUT;
   }
   ctx->patches = on;
+  return SG_OK;
+}
+
+int sg_set_fp64_pairs(sg_ctx* ctx, int32_t on) {
+  if (!ctx || on < 0 || on > 1) {
+    set_error("sg_set_fp64_pairs: 0 (FP64 arithmetic) or 1 (float-float pairs)");
+    return SG_BAD_INPUT;
+  }
+  ctx->fp64_pairs = on != 0;
   return SG_OK;
 }
 

@@ -181,6 +181,9 @@ struct sg_ctx {
   sg::Buf color, perm, body_cnt, body_off, body_fill, body_adj, v_run, stats, barrier;
   // FP32 sweep data, packed in colour order (mixed-precision solve)
   sg::Buf pk_ab, pk_n, pk_c, pk_w, pk_r, v32, minv32;
+  // Float-float copies of the FP64 sweep data and state for k_gs_patch_ff (by packed contact: normal,
+  // forcing, mu and 1 / w, impulse; by body: velocity, 1 / m).
+  sg::Buf ff_n, ff_c, ff_m, ff_r, ff_v, ff_minv;
   // 3D contacts: basis rows n s t (9), angular rows (r_a x s, r_a x t) and (r_b x s, r_b x t)
   // (6 each), forcing (3), Delassus block (6), impulse (3: current, candidate, best),
   // (alpha, beta0, beta1) out (3); running velocities (2 double4 per body: v, omega).
@@ -190,6 +193,8 @@ struct sg_ctx {
   // Two-level sweeps (spatial patches, one per SM): 0 off, 1 for FP32 sweeps, 2 also for the
   // FP64 sweeps of a solve the probe leaves near tol (sg_set_two_level).
   int patches = 1;
+  // FP64 sweeps on the two-level partition in float-float pairs for discs (sg_set_fp64_pairs).
+  bool fp64_pairs = true;
   // Staggering of the single-scene Ball2D step (sg_set_staggering): SG_STAGGER_*, and the
   // symplectic Euler map's pose stabilisation and threshold; its velocity change per body.
   int staggering = 0;

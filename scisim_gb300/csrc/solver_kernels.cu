@@ -2366,6 +2366,445 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 continuation on the two-level partition in float-float arithmetic (k_gs_patch_ff).
+//
+// GB300 issues FP64 at a small fraction of its FP32 rate, and k_gs_patch64's patch sweeps are
+// bound by that pipe.  Here the sweep state (body velocities and contact impulses) is held as
+// float-float pairs (hi + lo, 48 significant bits) and updated on the FP32 pipe: error-free sums
+// and products (Knuth's two-sum, FMA two-product) as in the double-double arithmetic of Dekker
+// (1971) and of Hida, Li and Bailey's QD library, restated for pairs of floats.  The contact data
+// (normal, forcing, mu, 1/m) are split into pairs too, so that the iteration solves the FP64
+// problem to about 2^-46 of its magnitudes; only the increment u / w of the isotropic local solve
+// is an FP32 product, as in k_gs_patch64.  Velocities follow the impulses through float-float
+// updates.  Each check converts the impulses to FP64, recomputes the velocities from them in FP64
+// (v = v0 + M^-1 H^T r), evaluates the residual in FP64 as every other kernel, and restarts the
+// pairs from those velocities: the residual reported is that of the returned impulses, and the
+// pairs' rounding (amplified by 1/m where small discs carry large impulses) never accumulates past
+// a check.  Ball2D contacts only: their Delassus blocks are isotropic by construction (w01 = 0,
+// w00 = w11).
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_make(float hi, float lo) {
+  FF r;
+  r.hi = hi;
+  r.lo = lo;
+  return r;
+}
+
+// x to 48 bits: the nearest float, then the nearest float to the (exact) remainder.
+__device__ __forceinline__ FF ff_split(double x) {
+  const float h = __double2float_rn(x);
+  return ff_make(h, __double2float_rn(x - (double)h));
+}
+
+// hi + lo exactly (the two floats' significands span at most 49 bits).
+__device__ __forceinline__ double ff_value(FF a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return ff_make(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+
+__device__ __forceinline__ FF ff_quick_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return ff_make(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ FF ff_neg(FF a) { return ff_make(-a.hi, -a.lo); }
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
+
+__device__ __forceinline__ FF ff_add_f(FF a, float b) {
+  const FF s = ff_two_sum(a.hi, b);
+  return ff_quick_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return ff_quick_two_sum(p, e);
+}
+
+struct FfArgs {
+  float4* n;     // per packed contact: nx, ny as pairs (hi, lo, hi, lo)
+  float4* c;     // forcing c as pairs
+  float4* m;     // mu as a pair, 1 / w00 in FP32, unused
+  float4* r;     // impulse as pairs (the sweep state)
+  float4* v;     // per body: velocity as pairs (the state between phases)
+  float2* minv;  // per body: 1 / m as a pair
+};
+
+// Sweep data of one packed contact (a C64 in pairs).
+struct CFF {
+  int q, la, lb;
+  float4 n, c, m, r;
+};
+
+__device__ __forceinline__ void load_ff(const Gs32Args& B, const FfArgs& F, int q, CFF& x, const unsigned* sab,
+                                        int sab0) {
+  if (sab) {
+    const unsigned ab = sab[q - sab0];
+    x.la = (int)(ab & 0xffffu);
+    x.lb = (int)(ab >> 16);
+  } else {
+    const int2 ab = B.ab[q];
+    x.la = ab.x;
+    x.lb = ab.y;
+  }
+  x.q = q;
+  x.n = F.n[q];
+  x.c = F.c[q];
+  x.m = F.m[q];
+  x.r = __ldcg(&F.r[q]);
+}
+
+// The isotropic update of update64 in pairs: u = H v + c, r_new = proj_cone(r - u / w) with the
+// increment u / w in FP32, then v += M^-1 H^T (r_new - r).  kGlobal: the velocities are the
+// global pairs of F.v (read at L2: other SMs wrote them before the last grid barrier).
+template <bool kGlobal>
+__device__ __forceinline__ void update_ff(const FfArgs& F, const CFF& x, float4* sv, const float2* sm) {
+  const float4 a4 = kGlobal ? __ldcg(&sv[x.la]) : sv[x.la];
+  const bool has_b = x.lb >= 0;
+  const float4 b4 = has_b ? (kGlobal ? __ldcg(&sv[x.lb]) : sv[x.lb]) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const FF nx = ff_make(x.n.x, x.n.y), ny = ff_make(x.n.z, x.n.w);
+  const FF dvx = ff_sub(ff_make(a4.x, a4.y), ff_make(b4.x, b4.y));
+  const FF dvy = ff_sub(ff_make(a4.z, a4.w), ff_make(b4.z, b4.w));
+  const FF u0 = ff_add(ff_add(ff_mul(nx, dvx), ff_mul(ny, dvy)), ff_make(x.c.x, x.c.y));
+  const FF u1 = ff_add(ff_sub(ff_mul(nx, dvy), ff_mul(ny, dvx)), ff_make(x.c.z, x.c.w));
+  const float iw = x.m.z;
+  const FF r0 = ff_make(x.r.x, x.r.y), r1 = ff_make(x.r.z, x.r.w);
+  const FF rn = ff_add_f(r0, -__fmul_rn(u0.hi, iw));
+  const FF rn0 = rn.hi > 0.f ? rn : ff_make(0.f, 0.f);
+  const FF rt = ff_add_f(r1, -__fmul_rn(u1.hi, iw));
+  const FF lim = ff_mul(ff_make(x.m.x, x.m.y), rn0);
+  const bool neg = signbit(rt.hi);
+  const FF art = neg ? ff_neg(rt) : rt;
+  const bool inside = art.hi < lim.hi || (art.hi == lim.hi && art.lo <= lim.lo);
+  const FF rn1 = inside ? rt : (neg ? ff_neg(lim) : lim);
+  const FF d0 = ff_sub(rn0, r0), d1 = ff_sub(rn1, r1);
+  const FF px = ff_sub(ff_mul(nx, d0), ff_mul(ny, d1));
+  const FF py = ff_add(ff_mul(ny, d0), ff_mul(nx, d1));
+  const float2 ma2 = sm[x.la];
+  const FF ma = ff_make(ma2.x, ma2.y);
+  const FF vax = ff_add(ff_make(a4.x, a4.y), ff_mul(ma, px));
+  const FF vay = ff_add(ff_make(a4.z, a4.w), ff_mul(ma, py));
+  sv[x.la] = make_float4(vax.hi, vax.lo, vay.hi, vay.lo);
+  if (has_b) {
+    const float2 mb2 = sm[x.lb];
+    const FF mb = ff_make(mb2.x, mb2.y);
+    const FF vbx = ff_sub(ff_make(b4.x, b4.y), ff_mul(mb, px));
+    const FF vby = ff_sub(ff_make(b4.z, b4.w), ff_mul(mb, py));
+    sv[x.lb] = make_float4(vbx.hi, vbx.lo, vby.hi, vby.lo);
+  }
+  F.r[x.q] = make_float4(rn0.hi, rn0.lo, rn1.hi, rn1.lo);
+}
+
+// sweep_group64 in pairs.
+__device__ __forceinline__ void sweep_group_ff(const Gs32Args& B, const FfArgs& F, const int* off, int ncol,
+                                               float4* sv, const float2* sm, const unsigned* sab = nullptr,
+                                               int sab0 = 0) {
+  CFF nxt;
+  bool have = false;
+  if (ncol > 0 && off[0] + (int)threadIdx.x < off[1]) {
+    load_ff(B, F, off[0] + threadIdx.x, nxt, sab, sab0);
+    have = true;
+  }
+  for (int col = 0; col < ncol; ++col) {
+    const int e = off[col + 1];
+    const int qn = (col + 1 < ncol) ? off[col + 1] + threadIdx.x : e;
+    const bool have_n = col + 1 < ncol && qn < off[col + 2];
+    if (have) {
+      CFF cur = nxt;
+      for (int q = off[col] + threadIdx.x + blockDim.x; q < e; q += blockDim.x) {
+        CFF x;
+        load_ff(B, F, q, x, sab, sab0);
+        update_ff<false>(F, cur, sv, sm);
+        cur = x;
+      }
+      update_ff<false>(F, cur, sv, sm);
+    }
+    have = have_n;
+    if (have) load_ff(B, F, qn, nxt, sab, sab0);
+    __syncthreads();
+  }
+}
+
+// The FP64 state split into pairs, by packed position (contacts) and by body.
+__global__ void k_pack_ff(int nc, int nb, const int* __restrict__ order, const double2* __restrict__ n,
+                          const double2* __restrict__ c, const double* __restrict__ W, const double* __restrict__ mu,
+                          const double2* __restrict__ r, const double2* __restrict__ v,
+                          const double* __restrict__ minv, FfArgs F) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nc) {
+    const int k = order[t];
+    const double2 nk = n[k], ck = c[k], rk = r[k];
+    const FF nx = ff_split(nk.x), ny = ff_split(nk.y), cx = ff_split(ck.x), cy = ff_split(ck.y);
+    const FF m = ff_split(mu[k]), r0 = ff_split(rk.x), r1 = ff_split(rk.y);
+    F.n[t] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
+    F.c[t] = make_float4(cx.hi, cx.lo, cy.hi, cy.lo);
+    F.m[t] = make_float4(m.hi, m.lo, __double2float_rn(1.0 / W[3 * k]), 0.f);
+    F.r[t] = make_float4(r0.hi, r0.lo, r1.hi, r1.lo);
+  }
+  if (t < nb) {
+    const double2 vi = v[t];
+    const FF vx = ff_split(vi.x), vy = ff_split(vi.y), mi = ff_split(minv[t]);
+    F.v[t] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
+    F.minv[t] = make_float2(mi.hi, mi.lo);
+  }
+}
+
+__global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch_ff(GsArgs A, Gs32Args B, PatchArgs Q, FfArgs F) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  extern __shared__ __align__(16) float4 svf[];
+  float2* smf = reinterpret_cast<float2*>(svf + Q.cap);
+  float4* svqf = reinterpret_cast<float4*>(smf + Q.cap);
+  float2* smqf = reinterpret_cast<float2*>(svqf + Q.capq);
+  const int capc = (Q.rest64 + 1) & ~1;
+  float4* svcf = reinterpret_cast<float4*>(smqf + Q.capq);
+  float2* smcf = reinterpret_cast<float2*>(svcf + capc);
+  unsigned* sabf = reinterpret_cast<unsigned*>(smcf + capc);
+  __shared__ int s_goff[kMaxColors + 1];
+  __shared__ int s_hoff[kMaxColors + 1];
+  __shared__ int s_boff[kMaxColors + 1];
+  const int P = Q.ps->P, Pb = Q.ps->Pb;
+  const bool has_p = blockIdx.x < P, has_q = blockIdx.x < Pb;
+  const int pb0 = has_p ? Q.pstart[blockIdx.x] : 0;
+  const int pb1 = has_p ? Q.pstart[blockIdx.x + 1] : 0;
+  const int pbe = pb0 + (has_p ? Q.pband[blockIdx.x] : 0);  // band bodies: [pb0, pbe)
+  const int qb0 = has_q ? Q.qstart[blockIdx.x] : 0;
+  const int qb1 = has_q ? Q.qstart[blockIdx.x + 1] : 0;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) {
+    s_goff[c] = has_p ? Q.goff[blockIdx.x * kMaxColors + c] : 0;
+    s_hoff[c] = has_q ? Q.goff[(P + blockIdx.x) * kMaxColors + c] : 0;
+    s_boff[c] = Q.goff[(P + Pb) * kMaxColors + c];
+  }
+  for (int j = pb0 + threadIdx.x; j < pb1; j += blockDim.x) {
+    smf[j - pb0] = F.minv[Q.pbody[j]];
+    svf[j - pb0] = __ldcg(&F.v[Q.pbody[j]]);
+  }
+  for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) smqf[j - qb0] = F.minv[Q.qbody[j]];
+  __syncthreads();
+  const int ncol_p = group_colors(s_goff), ncol_q = group_colors(s_hoff), ncol_r = group_colors(s_boff);
+  int btail = ncol_r;
+  while (btail > 0 && s_boff[btail] - s_boff[btail - 1] <= 2 * (int)blockDim.x) --btail;
+  const int sc0 = s_boff[btail], nrest_tail = s_boff[ncol_r] - sc0;
+  const bool rest_staged = Q.rest64 > 0 && nrest_tail > 0;
+  if (rest_staged && blockIdx.x == 0) {
+    for (int j = threadIdx.x; j < Q.rest64; j += blockDim.x) smcf[j] = F.minv[Q.cbody[j]];
+    for (int q = sc0 + threadIdx.x; q < sc0 + nrest_tail; q += blockDim.x) {
+      const int2 ab = B.ab[q];
+      sabf[q - sc0] = (unsigned)Q.cslot[ab.x] | ((unsigned)Q.cslot[ab.y] << 16);
+    }
+  }
+  __syncthreads();
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  double2* best = A.r_a;
+  double2* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false;
+  unsigned it = 0, n_eval = 0, s64 = 0;
+  unsigned next64 = eval64, interval64 = eval64, prev64_it = 0;
+  double prev64_err = INFINITY;
+  __shared__ unsigned long long t_ph[5];
+  const bool timer = tid == 0;
+  if (timer) t_ph[0] = t_ph[1] = t_ph[2] = t_ph[3] = t_ph[4] = 0ull;
+  // After a check every velocity was recomputed from the impulses: the next sweep reloads them all.
+  bool reload_all = false;
+  for (it = 1; it <= A.max_iters; ++it) {
+    const bool do_eval = it >= next64 || it == A.max_iters;
+    if (timer) t_ph[4] = globaltimer_ns();
+    if (it > 1) {
+      const int lend = reload_all ? pb1 : pbe;
+      for (int j = pb0 + threadIdx.x; j < lend; j += blockDim.x) svf[j - pb0] = __ldcg(&F.v[Q.pbody[j]]);
+      reload_all = false;
+    }
+    __syncthreads();
+    sweep_group_ff(B, F, s_goff, ncol_p, svf, smf);
+    if (timer) {
+      const unsigned long long t = globaltimer_ns();
+      t_ph[0] += t - t_ph[4];
+      t_ph[4] = t;
+    }
+    const int wend = do_eval ? pb1 : pbe;
+    for (int j = pb0 + threadIdx.x; j < wend; j += blockDim.x) F.v[Q.pbody[j]] = svf[j - pb0];
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    if (qb1 > qb0) {
+      for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) svqf[j - qb0] = __ldcg(&F.v[Q.qbody[j]]);
+      __syncthreads();
+      sweep_group_ff(B, F, s_hoff, ncol_q, svqf, smqf);
+      for (int j = qb0 + threadIdx.x; j < qb1; j += blockDim.x) F.v[Q.qbody[j]] = svqf[j - qb0];
+    }
+    if (timer) {
+      const unsigned long long t = globaltimer_ns();
+      t_ph[1] += t - t_ph[4];
+      t_ph[4] = t;
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    for (int col = 0; col < btail; ++col) {
+      const int b0 = s_boff[col], e = s_boff[col + 1];
+      if (b0 == e) continue;
+      for (int q = b0 + tid; q < e; q += nthr) {
+        CFF x;
+        load_ff(B, F, q, x, nullptr, 0);
+        update_ff<true>(F, x, F.v, F.minv);
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+    }
+    if (nrest_tail > 0) {
+      if (blockIdx.x == 0) {
+        if (rest_staged) {
+          for (int j = threadIdx.x; j < Q.rest64; j += blockDim.x) svcf[j] = __ldcg(&F.v[Q.cbody[j]]);
+          __syncthreads();
+          sweep_group_ff(B, F, s_boff + btail, ncol_r - btail, svcf, smcf, sabf, sc0);
+          for (int j = threadIdx.x; j < Q.rest64; j += blockDim.x) F.v[Q.cbody[j]] = svcf[j];
+        } else {
+          for (int col = btail; col < ncol_r; ++col) {
+            for (int q = s_boff[col] + threadIdx.x; q < s_boff[col + 1]; q += blockDim.x) {
+              CFF x;
+              load_ff(B, F, q, x, nullptr, 0);
+              update_ff<true>(F, x, F.v, F.minv);
+            }
+            __syncthreads();
+          }
+        }
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+    }
+    ++s64;
+    if (timer) {
+      const unsigned long long t = globaltimer_ns();
+      t_ph[2] += t - t_ph[4];
+      t_ph[4] = t;
+    }
+    if (!do_eval) continue;
+    // The impulses in FP64, then the velocities recomputed from them in FP64 (v = v0 + M^-1 H^T r,
+    // as k_gs_mixed's lift), so that the check evaluates exactly the returned impulses, and the
+    // pairs restarted from those velocities; then the FP64 check.
+    for (int q = tid; q < A.nc; q += nthr) {
+      const float4 w = __ldcg(&F.r[q]);
+      A.r[Q.order[q]] = make_double2(ff_value(ff_make(w.x, w.y)), ff_value(ff_make(w.z, w.w)));
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    for (int i = tid; i < B.nb; i += nthr) {
+      double hx = 0.0, hy = 0.0;
+      const int e = B.body_off[i + 1];
+      for (int p = B.body_off[i]; p < e; ++p) {
+        const int k = B.body_adj[p];
+        const double sgn = (A.ia[k] == i) ? 1.0 : -1.0;
+        const double2 nk = A.n[k], rk = __ldcg(&A.r[k]);
+        const double px = nk.x * rk.x + (-nk.y) * rk.y;
+        const double py = nk.y * rk.x + nk.x * rk.y;
+        hx = hx + sgn * px;
+        hy = hy + sgn * py;
+      }
+      const double2 a = B.v0[i];
+      const double mi = B.minv64[i];
+      const double2 vi = make_double2(a.x + mi * hx, a.y + mi * hy);
+      A.v[i] = vi;
+      const FF vx = ff_split(vi.x), vy = ff_split(vi.y);
+      F.v[i] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
+    }
+    reload_all = true;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    double emax = 0.0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int a = A.ia[k], b = A.ib[k];
+      const bool has_b = b >= 0;
+      const double2 va = __ldcg(&A.v[a]);
+      const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+      double u0, u1;
+      local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+      const double2 rk = __ldcg(&A.r[k]);
+      cand[k] = rk;
+      emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+    }
+    emax = block_nanmax(emax);
+    const int slot = n_eval % 3;
+    if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+    if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    ++n_eval;
+    if (timer) t_ph[3] += globaltimer_ns() - t_ph[4];
+    if (err < err_best) {
+      err_best = err;
+      double2* t = best;
+      best = cand;
+      cand = t;
+    }
+    if (err < A.tol) {
+      converged = true;
+      break;
+    }
+    // A check (impulses to FP64, velocities recomputed, the residual) costs several of these
+    // sweeps: the gap may grow to 64 eval64 in a long solve, at most a quarter of the sweeps done.
+    const unsigned cap64 = min(64u * eval64, max(16u * eval64, it / 4u));
+    if (err < prev64_err && prev64_err < INFINITY && err > 0.0) {
+      const double per_sweep = (log(err) - log(prev64_err)) / (double)(it - prev64_it);
+      const double need = (log(A.tol) - log(err)) / per_sweep;
+      interval64 = need >= (double)cap64 ? cap64 : max(eval64, (unsigned)need);
+    } else {
+      interval64 = min(2u * interval64, cap64);
+    }
+    prev64_err = err;
+    prev64_it = it;
+    next64 = it + interval64;
+  }
+  if (it > A.max_iters) it = A.max_iters;
+  if (!converged && err_best < INFINITY)
+    for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps32 = 0;
+    A.st->sweeps64 = s64;
+    A.st->evals = n_eval;
+    A.st->lifts = 0;
+    A.st->boundary_contacts = Q.goff[(P + Pb + 1) * kMaxColors] - Q.goff[P * kMaxColors];
+    int nbc = 0;
+    for (int c = 0; c < ncol_r; ++c) nbc += s_boff[c + 1] > s_boff[c];
+    A.st->boundary_colors = nbc;
+    A.st->phase_ns[0] = t_ph[0];
+    A.st->phase_ns[1] = t_ph[1];
+    A.st->phase_ns[2] = t_ph[2] + t_ph[3];
+  }
+}
+
 // FP64 Coulomb residual of a start impulse r at running velocities v (one residual
 // evaluation of k_gs), maximum into *slot (ordered encoding).
 __global__ void k_start_err(int nc, const int* __restrict__ ia, const int* __restrict__ ib,
@@ -3423,15 +3862,34 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
             smem64 += rest64_bytes;
           }
           ctx->patch_staged += (uint64_t)stage_p;
-          void* args[] = {&GA, &GB, &Q};
+          // A solve that stays in FP64 takes the FP64 kernel (its velocities fit shared memory): for
+          // Ball2D discs the float-float one (k_gs_patch_ff), unless sg_set_fp64_pairs turned it off.
+          const bool only64 = fp64_start && GB.fp64_local;
+          const bool pairs = only64 && !ctx->rb2d && ctx->fp64_pairs;
+          FfArgs FA{};
+          if (pairs) {
+            const size_t c4 = sizeof(float4) * (size_t)nc, b = (size_t)std::max(nb, 1);
+            if (int r = grow(ctx->ff_n, c4)) return r;
+            if (int r = grow(ctx->ff_c, c4)) return r;
+            if (int r = grow(ctx->ff_m, c4)) return r;
+            if (int r = grow(ctx->ff_r, c4)) return r;
+            if (int r = grow(ctx->ff_v, sizeof(float4) * b)) return r;
+            if (int r = grow(ctx->ff_minv, sizeof(float2) * b)) return r;
+            FA = FfArgs{ctx->ff_n.as<float4>(), ctx->ff_c.as<float4>(), ctx->ff_m.as<float4>(),
+                        ctx->ff_r.as<float4>(), ctx->ff_v.as<float4>(), ctx->ff_minv.as<float2>()};
+            k_pack_ff<<<blocks_for(std::max(nc, nb)), kBlock, 0, s>>>(nc, nb, Q.order, n2, GA.c, GA.W, GA.mu, r2, vrun,
+                                                                     P.minv, FA);
+            SG_CUDA_TRY(cudaGetLastError());
+            ctx->kernel_launches += 1;
+          }
+          void* args[] = {&GA, &GB, &Q, &FA};
           // The boundary colouring used the barrier: start it afresh for this grid.
           SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
           if (!second_pass) stage_mark(ctx, 5);
           if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
-          // A solve that stays in FP64 takes the FP64 kernel (its velocities fit shared memory).
-          const bool only64 = fp64_start && GB.fp64_local;
           if (only64 && !ctx->patch64_ready) {
             SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch64, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_budget));
+            SG_CUDA_TRY(cudaFuncSetAttribute(k_gs_patch_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_budget));
             ctx->patch64_ready = true;
           }
           cudaLaunchConfig_t lc = {};
@@ -3444,7 +3902,8 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
           at[0].val.cooperative = 1;
           lc.attrs = at;
           lc.numAttrs = 1;
-          SG_CUDA_TRY(cudaLaunchKernelExC(&lc, only64 ? (const void*)k_gs_patch64 : (const void*)k_gs_patch, args));
+          const void* kfn = pairs ? (const void*)k_gs_patch_ff : only64 ? (const void*)k_gs_patch64 : (const void*)k_gs_patch;
+          SG_CUDA_TRY(cudaLaunchKernelExC(&lc, kfn, args));
           if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
           stage_mark(ctx, 6);
           ctx->patched_solves += 1;
