@@ -2540,14 +2540,15 @@ __device__ __forceinline__ void sweep_group_ff(const Gs32Args& B, const FfArgs& 
   }
 }
 
-// The FP64 state split into pairs, by packed position (contacts) and by body.
+// The FP64 state split into pairs, by packed position (contacts; by contact index when order is
+// null) and by body.
 __global__ void k_pack_ff(int nc, int nb, const int* __restrict__ order, const double2* __restrict__ n,
                           const double2* __restrict__ c, const double* __restrict__ W, const double* __restrict__ mu,
                           const double2* __restrict__ r, const double2* __restrict__ v,
                           const double* __restrict__ minv, FfArgs F) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < nc) {
-    const int k = order[t];
+    const int k = order ? order[t] : t;
     const double2 nk = n[k], ck = c[k], rk = r[k];
     const FF nx = ff_split(nk.x), ny = ff_split(nk.y), cx = ff_split(ck.x), cy = ff_split(ck.y);
     const FF m = ff_split(mu[k]), r0 = ff_split(rk.x), r1 = ff_split(rk.y);
@@ -2563,6 +2564,140 @@ __global__ void k_pack_ff(int nc, int nb, const int* __restrict__ order, const d
     F.minv[t] = make_float2(mi.hi, mi.lo);
   }
 }
+
+// One-level FP64-precision sweeps in float-float pairs (k_gs_mixed's FP64 sweeps in the pairs of
+// k_gs_patch_ff): the global colour order over all contacts, velocities as pairs in global memory,
+// contact data and impulses as pairs by contact index; checks as in k_gs_patch_ff.  The FP32
+// form's one-level FP64 continuation for discs.
+constexpr int kGsFf1Block = 256;
+
+__global__ void __launch_bounds__(kGsFf1Block, 1) k_gs_ff1(GsArgs A, Gs32Args B, FfArgs F) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  if (*((volatile int*)&A.st->status) != 0) return;
+  __shared__ int s_off[kMaxColors + 1];
+  __shared__ int s_ncol;
+  if (threadIdx.x == 0) s_ncol = A.st->n_colors;
+  for (int c = threadIdx.x; c <= kMaxColors; c += blockDim.x) s_off[c] = A.st->color_off[c];
+  __syncthreads();
+  const int ncol = s_ncol;
+  const unsigned eval64 = A.eval_every ? A.eval_every : 1u;
+  double2* best = A.r_a;
+  double2* cand = A.r_b;
+  double err_best = INFINITY;
+  bool converged = false;
+  unsigned it = 0, n_eval = 0;
+  unsigned next64 = eval64, interval64 = eval64, prev64_it = 0;
+  double prev64_err = INFINITY;
+  for (it = 1; it <= A.max_iters; ++it) {
+    for (int col = 0; col < ncol; ++col) {
+      const int e = s_off[col + 1];
+      for (int s = s_off[col] + tid; s < e; s += nthr) {
+        const int k = A.perm[s];
+        CFF x;
+        x.q = k;
+        x.la = A.ia[k];
+        x.lb = A.ib[k];
+        x.n = F.n[k];
+        x.c = F.c[k];
+        x.m = F.m[k];
+        x.r = __ldcg(&F.r[k]);
+        update_ff<true>(F, x, F.v, F.minv);
+      }
+      if (!grid_sync(A.gb, A.spin)) {
+        if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+        return;
+      }
+    }
+    if (!(it >= next64 || it == A.max_iters)) continue;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const float4 w = __ldcg(&F.r[k]);
+      A.r[k] = make_double2(ff_value(ff_make(w.x, w.y)), ff_value(ff_make(w.z, w.w)));
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    for (int i = tid; i < B.nb; i += nthr) {
+      double hx = 0.0, hy = 0.0;
+      const int e = B.body_off[i + 1];
+      for (int p = B.body_off[i]; p < e; ++p) {
+        const int k = B.body_adj[p];
+        const double sgn = (A.ia[k] == i) ? 1.0 : -1.0;
+        const double2 nk = A.n[k], rk = __ldcg(&A.r[k]);
+        const double px = nk.x * rk.x + (-nk.y) * rk.y;
+        const double py = nk.y * rk.x + nk.x * rk.y;
+        hx = hx + sgn * px;
+        hy = hy + sgn * py;
+      }
+      const double2 a = B.v0[i];
+      const double mi = B.minv64[i];
+      const double2 vi = make_double2(a.x + mi * hx, a.y + mi * hy);
+      A.v[i] = vi;
+      const FF vx = ff_split(vi.x), vy = ff_split(vi.y);
+      F.v[i] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
+    }
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    double emax = 0.0;
+    for (int k = tid; k < A.nc; k += nthr) {
+      const int a = A.ia[k], b = A.ib[k];
+      const bool has_b = b >= 0;
+      const double2 va = __ldcg(&A.v[a]);
+      const double2 vb = has_b ? __ldcg(&A.v[b]) : make_double2(0.0, 0.0);
+      double u0, u1;
+      local_velocity(A.n[k], A.c[k], va, has_b, vb, u0, u1);
+      const double2 rk = __ldcg(&A.r[k]);
+      cand[k] = rk;
+      emax = nanmax(emax, fb_error_2d(rk.x, rk.y, u0, u1, A.mu[k]));
+    }
+    emax = block_nanmax(emax);
+    const int slot = n_eval % 3;
+    if (threadIdx.x == 0) atomicMax(&A.st->err_slot[slot], f64_to_ordered(emax));
+    if (tid == 0) A.st->err_slot[(n_eval + 1) % 3] = 0ull;
+    if (!grid_sync(A.gb, A.spin)) {
+      if (tid == 0) atomicExch(&A.st->status, (int)SG_DEVICE_TIMEOUT);
+      return;
+    }
+    const double err = ordered_to_f64(*((volatile unsigned long long*)&A.st->err_slot[slot]));
+    ++n_eval;
+    if (err < err_best) {
+      err_best = err;
+      double2* t = best;
+      best = cand;
+      cand = t;
+    }
+    if (err < A.tol) {
+      converged = true;
+      break;
+    }
+    if (err < prev64_err && prev64_err < INFINITY && err > 0.0) {
+      const double per_sweep = (log(err) - log(prev64_err)) / (double)(it - prev64_it);
+      const double need = (log(A.tol) - log(err)) / per_sweep;
+      interval64 = need >= (double)(16u * eval64) ? 16u * eval64 : max(eval64, (unsigned)need);
+    } else {
+      interval64 = min(2u * interval64, 16u * eval64);
+    }
+    prev64_err = err;
+    prev64_it = it;
+    next64 = it + interval64;
+  }
+  if (it > A.max_iters) it = A.max_iters;
+  if (!converged && err_best < INFINITY)
+    for (int k = tid; k < A.nc; k += nthr) A.r[k] = __ldcg(&best[k]);
+  if (tid == 0) {
+    A.st->iterations = it;
+    A.st->converged = converged ? 1 : 0;
+    A.st->error = err_best;
+    A.st->sweeps32 = 0;
+    A.st->sweeps64 = it;
+    A.st->evals = n_eval;
+    A.st->lifts = 0;
+  }
+}
+
 
 __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch_ff(GsArgs A, Gs32Args B, PatchArgs Q, FfArgs F) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -3907,6 +4042,29 @@ int solve_contacts(sg_ctx* ctx, const ContactProblem& P, const SolveParams& sp) 
           if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
           stage_mark(ctx, 6);
           ctx->patched_solves += 1;
+        } else if (fp64_start && !ctx->rb2d && ctx->fp64_pairs) {
+          // A disc solve going on in one-level FP64 sweeps: in float-float pairs (k_gs_ff1).
+          const size_t c4 = sizeof(float4) * (size_t)nc, b = (size_t)std::max(nb, 1);
+          if (int r = grow(ctx->ff_n, c4)) return r;
+          if (int r = grow(ctx->ff_c, c4)) return r;
+          if (int r = grow(ctx->ff_m, c4)) return r;
+          if (int r = grow(ctx->ff_r, c4)) return r;
+          if (int r = grow(ctx->ff_v, sizeof(float4) * b)) return r;
+          if (int r = grow(ctx->ff_minv, sizeof(float2) * b)) return r;
+          FfArgs FA{ctx->ff_n.as<float4>(), ctx->ff_c.as<float4>(), ctx->ff_m.as<float4>(), ctx->ff_r.as<float4>(),
+                    ctx->ff_v.as<float4>(), ctx->ff_minv.as<float2>()};
+          k_pack_ff<<<blocks_for(std::max(nc, nb)), kBlock, 0, s>>>(nc, nb, nullptr, n2, GA.c, GA.W, GA.mu, r2, vrun,
+                                                                   P.minv, FA);
+          SG_CUDA_TRY(cudaGetLastError());
+          ctx->kernel_launches += 1;
+          void* args[] = {&GA, &GB, &FA};
+          const int g = coop_grid(ctx, k_gs_ff1, nc, kGsFf1Block, 1);
+          SG_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s));
+          if (!second_pass) stage_mark(ctx, 5);
+          if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs0, s));
+          SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_gs_ff1, dim3(g), dim3(kGsFf1Block), args, 0, s));
+          if (ctx->profile) SG_CUDA_TRY(cudaEventRecord(ctx->ev_gs1, s));
+          stage_mark(ctx, 6);
         } else {
           void* args[] = {&GA, &GB};
           const int g = coop_grid(ctx, k_gs_mixed, std::max(nc, nb), kGs32Block, 1);

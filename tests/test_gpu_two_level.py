@@ -147,17 +147,17 @@ def test_two_level_is_deterministic(gpulib):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
 
-@pytest.mark.parametrize("two_level,pairs", [(1, True), (2, True), (2, False)])
+@pytest.mark.parametrize("two_level,pairs", [(1, True), (1, False), (2, True), (2, False)])
 def test_fp64_continuation(gpulib, oracle, two_level, pairs):
     """The FP32 form's FP64 continuation: from a settled pile, with a tolerance the eight-sweep
     FP64 probe does not reach and fp64_factor so large that every solve stays in FP64, the solves
-    the probe leaves go on in FP64 sweeps: under the default two_level 1 one-level (k_gs_mixed's
-    FP64 sweeps with their rate-predicted checks) for up to 160 sweeps, then on the two-level
-    partition; under two_level 2 on the partition from the start.  On the partition the sweeps run
-    in float-float pairs on the FP32 pipe (k_gs_patch_ff, the default) or in FP64 (k_gs_patch64,
-    sg_set_fp64_pairs 0).  The reported residual is the oracle's residual of the GPU's impulses,
-    every continued solve ends below the residual the probe alone reaches from the same state, and
-    every step that reports convergence meets the tolerance under it."""
+    the probe leaves go on in FP64-precision sweeps: under the default two_level 1 one-level (with
+    rate-predicted checks) for up to 160 sweeps, then on the two-level partition; under two_level 2
+    on the partition from the start.  The sweeps run in float-float pairs on the FP32 pipe
+    (k_gs_ff1 one-level, k_gs_patch_ff on the partition; the default) or in FP64 (k_gs_mixed,
+    k_gs_patch64; sg_set_fp64_pairs 0).  The reported residual is the oracle's residual of the
+    GPU's impulses, every continued solve ends below the residual the probe alone reaches from the
+    same state, and every step that reports convergence meets the tolerance under it."""
     n = 32768
     s = scenes.dense_pile(n=n, seed=2, width=20.0, height=15.0)
     pre = pile(gpulib, s, precision=gpulib.PRECISION_FP32_REFINE, max_iters=50)
