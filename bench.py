@@ -381,8 +381,8 @@ def headline_roofline(prof, total_ms, args, sweeps=()):
             kname = "k_gs (the FP64 probe, one-level: every solve converged in it)"
         else:
             kname = ("k_gs (the FP64 probe, one-level), then for the %d of %d solves it left unconverged "
-                     "k_gs_mixed's one-level FP64 sweeps (up to 160) and, for %d of them, k_gs_patch_ff "
-                     "(FP64-precision sweeps on the two-level partition in float-float pairs), together"
+                     "k_gs_ff1 (one-level FP64-precision sweeps in float-float pairs, up to 160) and, for %d "
+                     "of them, k_gs_patch_ff (the same on the two-level partition), together"
                      % (n_cont, prof["gs_launches"], n_two))
     else:
         kname = "k_gs_mixed (cooperative FP32 sweeps, FP64 checks and refinement)"

@@ -403,11 +403,12 @@ SG_API int sg_profile_read(sg_ctx* ctx, sg_profile* out, int32_t reset);
  * sweeps from the start.  SG_BAD_INPUT for other values. */
 SG_API int sg_set_two_level(sg_ctx* ctx, int32_t on);
 
-/* The FP64 sweeps on the two-level partition (sg_set_two_level) for Ball2D discs: 1 (default) in
- * float-float arithmetic on the FP32 pipe (velocities and impulses as pairs of floats, 48
- * significant bits; the data split the same way; each check in FP64), which GB300 issues many
- * times faster than FP64; 0 in FP64 arithmetic.  Both iterate to the same FP64 residual checks
- * and tolerance.  SG_BAD_INPUT for other values. */
+/* The FP32 form's FP64 sweeps after the probe for Ball2D discs, one-level and on the two-level
+ * partition (sg_set_two_level): 1 (default) in float-float arithmetic on the FP32 pipe
+ * (velocities and impulses as pairs of floats, 48 significant bits; the data split the same way;
+ * each check recomputes the velocities from the impulses and evaluates the residual in FP64),
+ * which GB300 issues many times faster than FP64; 0 in FP64 arithmetic.  Both iterate to the same
+ * FP64 residual checks and tolerance.  SG_BAD_INPUT for other values. */
 SG_API int sg_set_fp64_pairs(sg_ctx* ctx, int32_t on);
 
 /* Selects the map a single Ball2D, sphere or RigidBody2D scene steps with (default

@@ -478,7 +478,8 @@ class Context:
         check(lib().sg_set_two_level(self._h, int(on)), "sg_set_two_level")
 
     def set_fp64_pairs(self, on=True):
-        """The two-level FP64 sweeps for discs in float-float pairs (True, default) or FP64 (False)."""
+        """The FP32 form's FP64 sweeps after the probe for discs (one-level and two-level) in
+        float-float pairs (True, default) or in FP64 (False)."""
         check(lib().sg_set_fp64_pairs(self._h, int(on)), "sg_set_fp64_pairs")
 
     def set_staggering(self, staggering=STAGGER_GEOMETRIC, stabilize=False, penetration_threshold=0.0):
