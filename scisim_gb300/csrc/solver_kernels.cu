@@ -19,6 +19,7 @@
 //   k_final_velocity                       v2 = Minv (H^T r - f), f = -M v0
 #include "ctx.hpp"
 #include "coulomb2d.cuh"
+#include "ffloat.hpp"
 #include "na_cache.hpp"
 
 #include <cuda.h>
@@ -2383,59 +2384,6 @@ __global__ void __launch_bounds__(kPatch64Block, 1) k_gs_patch64(GsArgs A, Gs32A
 // pairs' rounding (amplified by 1/m where small discs carry large impulses) never accumulates past
 // a check.  Ball2D contacts only: their Delassus blocks are isotropic by construction (w01 = 0,
 // w00 = w11).
-struct FF {
-  float hi, lo;
-};
-
-__device__ __forceinline__ FF ff_make(float hi, float lo) {
-  FF r;
-  r.hi = hi;
-  r.lo = lo;
-  return r;
-}
-
-// x to 48 bits: the nearest float, then the nearest float to the (exact) remainder.
-__device__ __forceinline__ FF ff_split(double x) {
-  const float h = __double2float_rn(x);
-  return ff_make(h, __double2float_rn(x - (double)h));
-}
-
-// hi + lo exactly (the two floats' significands span at most 49 bits).
-__device__ __forceinline__ double ff_value(FF a) { return (double)a.hi + (double)a.lo; }
-
-__device__ __forceinline__ FF ff_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  return ff_make(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
-}
-
-__device__ __forceinline__ FF ff_quick_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return ff_make(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-
-__device__ __forceinline__ FF ff_neg(FF a) { return ff_make(-a.hi, -a.lo); }
-
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  const FF s = ff_two_sum(a.hi, b.hi);
-  return ff_quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
-}
-
-__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
-
-__device__ __forceinline__ FF ff_add_f(FF a, float b) {
-  const FF s = ff_two_sum(a.hi, b);
-  return ff_quick_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
-}
-
-__device__ __forceinline__ FF ff_mul(FF a, FF b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = __fmaf_rn(a.hi, b.hi, -p);
-  e = __fmaf_rn(a.hi, b.lo, e);
-  e = __fmaf_rn(a.lo, b.hi, e);
-  return ff_quick_two_sum(p, e);
-}
-
 struct FfArgs {
   float4* n;     // per packed contact: nx, ny as pairs (hi, lo, hi, lo)
   float4* c;     // forcing c as pairs
